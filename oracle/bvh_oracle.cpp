@@ -1,0 +1,1023 @@
+// CPU oracle for the ray-BVH hot path of lambdaxymox/bvhtracer.
+//
+// TEST INFRASTRUCTURE ONLY: a restatement of the reference's Rust code used to
+// check the CUDA library and as the timed CPU baseline.  Nothing in the
+// product library links, loads or calls this file.
+//
+// Every function cites the reference file:line it restates (paths relative to
+// the reference repository root; "BT" = bvhtracer/).  Floating-point operation
+// order follows the reference exactly; the file must be compiled with
+// -ffp-contract=off so that no multiply-add is fused (Rust never fuses).
+//
+// Third-party arithmetic: Vector3 dot/cross/normalize, component min/max and
+// Matrix4x4 * Vector4 live in the `cglinalg` crate, which is not vendored in the
+// reference (BT/Cargo.toml:20-22 asks for 0.16.10, no lockfile).  They are
+// restated here as their published definitions: dot = (x*x' + y*y') + z*z',
+// cross = (y*z'-z*y', z*x'-x*z', x*y'-y*x'), normalize = v / |v| per component,
+// |v| = sqrt(dot(v,v)), M*v = ((m0*v0 + m1*v1) + m2*v2) + m3*v3 per row
+// (column-major m[col][row]).  The exact-t known answers of the reference's
+// tests pin dot/cross/normalize (see tests/test_oracle_known_answers.py).
+
+#include "bvh_oracle.h"
+
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <thread>
+#include <vector>
+#include <algorithm>
+
+namespace {
+
+struct V3 {
+    float x, y, z;
+};
+
+inline V3 mk(float x, float y, float z) { return V3{x, y, z}; }
+inline V3 add(V3 a, V3 b) { return mk(a.x + b.x, a.y + b.y, a.z + b.z); }
+inline V3 sub(V3 a, V3 b) { return mk(a.x - b.x, a.y - b.y, a.z - b.z); }
+inline V3 muls(V3 a, float s) { return mk(a.x * s, a.y * s, a.z * s); }
+inline V3 neg(V3 a) { return mk(-a.x, -a.y, -a.z); }
+inline float dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline V3 cross(V3 a, V3 b) {
+    return mk(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+inline float magnitude(V3 a) { return std::sqrt(dot(a, a)); }
+inline V3 normalize(V3 a) {
+    float m = magnitude(a);
+    return mk(a.x / m, a.y / m, a.z / m);
+}
+inline float comp(V3 a, int axis) { return axis == 0 ? a.x : (axis == 1 ? a.y : a.z); }
+
+// Rust f32::min / f32::max: NaN-ignoring.  The sign of a zero result is
+// unspecified in Rust; this restatement (and the CUDA refit / TLAS kernels) keep
+// the first argument on equality.
+inline float rmin(float a, float b) {
+    if (a != a) return b;
+    if (b != b) return a;
+    return (b < a) ? b : a;
+}
+inline float rmax(float a, float b) {
+    if (a != a) return b;
+    if (b != b) return a;
+    return (b > a) ? b : a;
+}
+inline V3 vmin(V3 a, V3 b) { return mk(rmin(a.x, b.x), rmin(a.y, b.y), rmin(a.z, b.z)); }
+inline V3 vmax(V3 a, V3 b) { return mk(rmax(a.x, b.x), rmax(a.y, b.y), rmax(a.z, b.z)); }
+
+// BT/src/geometry/aabb.rs:11-19; Default = zero box (derive(Default)).
+struct Aabb {
+    V3 bmin{0.f, 0.f, 0.f};
+    V3 bmax{0.f, 0.f, 0.f};
+};
+
+// aabb.rs:29-34
+inline Aabb aabb_new_empty() {
+    Aabb a;
+    a.bmin = mk(FLT_MAX, FLT_MAX, FLT_MAX);
+    a.bmax = mk(-FLT_MAX, -FLT_MAX, -FLT_MAX);
+    return a;
+}
+// aabb.rs:36-39
+inline void aabb_grow(Aabb& a, V3 p) {
+    a.bmin = vmin(a.bmin, p);
+    a.bmax = vmax(a.bmax, p);
+}
+// aabb.rs:41-46
+inline void aabb_grow_aabb(Aabb& a, const Aabb& b) {
+    if (b.bmin.x != FLT_MAX) {
+        aabb_grow(a, b.bmin);
+        aabb_grow(a, b.bmax);
+    }
+}
+// aabb.rs:48-57
+inline float aabb_area(const Aabb& a) {
+    V3 e = sub(a.bmax, a.bmin);
+    return e.x * e.y + e.y * e.z + e.z * e.x;
+}
+
+// BT/src/query/ray.rs:9-35
+struct Ray {
+    V3 o, d, rd;
+    float t;
+};
+inline Ray ray_new(V3 o, V3 d, float t) {
+    Ray r;
+    r.o = o;
+    r.d = d;
+    r.rd = mk(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
+    r.t = t;
+    return r;
+}
+
+// aabb.rs:65-84
+inline bool aabb_intersect(const Aabb& b, const Ray& r, float* out) {
+    float tx1 = (b.bmin.x - r.o.x) * r.rd.x;
+    float tx2 = (b.bmax.x - r.o.x) * r.rd.x;
+    float tmin = rmin(tx1, tx2);
+    float tmax = rmax(tx1, tx2);
+    float ty1 = (b.bmin.y - r.o.y) * r.rd.y;
+    float ty2 = (b.bmax.y - r.o.y) * r.rd.y;
+    tmin = rmax(tmin, rmin(ty1, ty2));
+    tmax = rmin(tmax, rmax(ty1, ty2));
+    float tz1 = (b.bmin.z - r.o.z) * r.rd.z;
+    float tz2 = (b.bmax.z - r.o.z) * r.rd.z;
+    tmin = rmax(tmin, rmin(tz1, tz2));
+    tmax = rmin(tmax, rmax(tz1, tz2));
+    if ((tmax >= tmin) && (tmin < r.t) && (tmax > 0.0f)) {
+        *out = tmin;
+        return true;
+    }
+    return false;
+}
+
+// BT/src/geometry/triangle.rs:11-17
+struct Tri {
+    V3 v[3];
+};
+inline Tri load_tri(const orc_tri& t) {
+    Tri r;
+    r.v[0] = mk(t.v[0], t.v[1], t.v[2]);
+    r.v[1] = mk(t.v[3], t.v[4], t.v[5]);
+    r.v[2] = mk(t.v[6], t.v[7], t.v[8]);
+    return r;
+}
+
+// triangle.rs:33-39: (v0 + v1 + v2) * (1/3), one/three computed in f32.
+inline V3 tri_centroid(const Tri& t) {
+    const float one = 1.0f;
+    const float three = one + one + one;
+    const float one_third = one / three;
+    return muls(add(add(t.v[0], t.v[1]), t.v[2]), one_third);
+}
+
+// triangle.rs:42-72 (Moeller-Trumbore); returns (min(ray.t, t), u, v).
+inline bool tri_intersect(const Tri& tri, const Ray& ray, float* ot, float* ou, float* ov) {
+    V3 e1 = sub(tri.v[1], tri.v[0]);
+    V3 e2 = sub(tri.v[2], tri.v[0]);
+    V3 n = cross(ray.d, e2);
+    float area = dot(e1, n);
+    const float threshold = 0.0001f;
+    if (std::fabs(area) < threshold) return false;
+    float f = 1.0f / area;
+    V3 s = sub(ray.o, tri.v[0]);
+    float u = f * dot(s, n);
+    if (u < 0.0f || u > 1.0f) return false;
+    V3 q = cross(s, e1);
+    float v = f * dot(ray.d, q);
+    if (v < 0.0f || u + v > 1.0f) return false;
+    float t = f * dot(e2, q);
+    if (t > threshold) {
+        *ot = rmin(ray.t, t);
+        *ou = u;
+        *ov = v;
+        return true;
+    }
+    return false;
+}
+
+// BT/src/model/bvh.rs:129-134 (32-byte node; leaf iff primitive_count > 0).
+struct Node {
+    Aabb aabb;
+    uint32_t count = 0;
+    uint32_t left_first = 0;
+};
+
+struct Bvh {
+    std::vector<Node> nodes;
+    std::vector<uint32_t> node_indices;
+    uint32_t root = 0;
+    uint32_t nodes_used = 0;
+};
+
+struct BuildError {};
+
+// bvh.rs:317-330
+void update_node_bounds(Bvh& b, const std::vector<Tri>& mesh, uint32_t ni) {
+    Aabb a;
+    a.bmin = mk(FLT_MAX, FLT_MAX, FLT_MAX);
+    a.bmax = mk(-FLT_MAX, -FLT_MAX, -FLT_MAX);
+    const Node& node = b.nodes[ni];
+    uint32_t base = b.node_indices[node.left_first];
+    for (uint32_t k = 0; k < node.count; ++k) {
+        const Tri& p = mesh[base + k];
+        a.bmin = vmin(a.bmin, p.v[0]);
+        a.bmin = vmin(a.bmin, p.v[1]);
+        a.bmin = vmin(a.bmin, p.v[2]);
+        a.bmax = vmax(a.bmax, p.v[0]);
+        a.bmax = vmax(a.bmax, p.v[1]);
+        a.bmax = vmax(a.bmax, p.v[2]);
+    }
+    b.nodes[ni].aabb = a;
+}
+
+// Rust `f as usize` (saturating; NaN -> 0).
+inline uint64_t as_usize(float f) {
+    if (!(f > 0.0f)) return 0;
+    if (f >= 18446744073709551616.0f) return UINT64_MAX;
+    return (uint64_t)f;
+}
+
+struct Split {
+    int axis;
+    float position;
+    float cost;
+};
+
+// bvh.rs:333-394
+Split find_best_split_plane(const Bvh& b, const std::vector<Tri>& mesh, const Node& node) {
+    const int BIN_COUNT = 8;
+    Split best{-1, 0.0f, FLT_MAX};
+    uint32_t base = b.node_indices[node.left_first];
+    for (int axis = 0; axis < 3; ++axis) {
+        float bounds_min = 1e30f;
+        float bounds_max = 1e-30f;
+        for (uint32_t k = 0; k < node.count; ++k) {
+            float c = comp(tri_centroid(mesh[base + k]), axis);
+            bounds_min = rmin(bounds_min, c);
+            bounds_max = rmax(bounds_max, c);
+        }
+        if (bounds_min == bounds_max) continue;
+
+        Aabb bin_box[BIN_COUNT];
+        uint32_t bin_count[BIN_COUNT] = {0, 0, 0, 0, 0, 0, 0, 0};
+        float bin_scale = ((float)BIN_COUNT) / (bounds_max - bounds_min);
+        for (uint32_t k = 0; k < node.count; ++k) {
+            const Tri& p = mesh[base + k];
+            uint64_t possible = as_usize((comp(tri_centroid(p), axis) - bounds_min) * bin_scale);
+            uint64_t idx = std::min<uint64_t>(BIN_COUNT - 1, possible);
+            bin_count[idx] += 1;
+            aabb_grow(bin_box[idx], p.v[0]);
+            aabb_grow(bin_box[idx], p.v[1]);
+            aabb_grow(bin_box[idx], p.v[2]);
+        }
+
+        float left_area[BIN_COUNT - 1], right_area[BIN_COUNT - 1];
+        uint32_t left_count[BIN_COUNT - 1], right_count[BIN_COUNT - 1];
+        Aabb left_box, right_box;  // zero boxes (Aabb::default)
+        uint32_t left_sum = 0, right_sum = 0;
+        for (int i = 0; i < BIN_COUNT - 1; ++i) {
+            left_sum += bin_count[i];
+            left_count[i] = left_sum;
+            aabb_grow_aabb(left_box, bin_box[i]);
+            left_area[i] = aabb_area(left_box);
+
+            right_sum += bin_count[BIN_COUNT - 1 - i];
+            right_count[BIN_COUNT - 2 - i] = right_sum;
+            aabb_grow_aabb(right_box, bin_box[BIN_COUNT - 1 - i]);
+            right_area[BIN_COUNT - 2 - i] = aabb_area(right_box);
+        }
+
+        float scale = (bounds_max - bounds_min) / ((float)BIN_COUNT);
+        for (int i = 0; i < BIN_COUNT - 1; ++i) {
+            float plane_cost = ((float)left_count[i]) * left_area[i] + ((float)right_count[i]) * right_area[i];
+            if (plane_cost < best.cost) {
+                best.axis = axis;
+                best.position = bounds_min + scale * ((float)(i + 1));
+                best.cost = plane_cost;
+            }
+        }
+    }
+    return best;
+}
+
+// bvh.rs:396-467 (recursive, depth-first: left subtree allocated before right).
+void subdivide(Bvh& b, std::vector<Tri>& mesh, uint32_t ni) {
+    Split s = find_best_split_plane(b, mesh, b.nodes[ni]);
+    const Node node = b.nodes[ni];
+    float no_split_cost = ((float)node.count) * aabb_area(node.aabb);
+    if (s.cost >= no_split_cost) return;
+    if (s.axis < 0) throw BuildError();  // `best_axis as usize` would index out of range
+
+    uint32_t i = node.left_first;
+    uint32_t j = i + node.count - 1;
+    while (i <= j) {
+        if (comp(tri_centroid(mesh[i]), s.axis) < s.position) {
+            i += 1;
+        } else {
+            std::swap(mesh[i], mesh[j]);
+            if (j == 0) throw BuildError();  // u32 underflow: the reference panics
+            j -= 1;
+        }
+    }
+    uint32_t left_count = i - node.left_first;
+    if (left_count == 0 || left_count == node.count) return;
+
+    uint32_t left = b.nodes_used++;
+    uint32_t right = b.nodes_used++;
+    b.nodes[left].left_first = b.nodes[ni].left_first;
+    b.nodes[left].count = left_count;
+    b.nodes[right].left_first = i;
+    b.nodes[right].count = b.nodes[ni].count - left_count;
+    b.nodes[ni].left_first = left;
+    b.nodes[ni].count = 0;
+
+    update_node_bounds(b, mesh, left);
+    update_node_bounds(b, mesh, right);
+    subdivide(b, mesh, left);
+    subdivide(b, mesh, right);
+}
+
+// bvh.rs:510-541
+bool bvh_build(std::vector<Tri>& mesh, Bvh& b) {
+    size_t n = mesh.size();
+    if (n == 0) return false;  // nodes[0] of an empty array: the reference panics
+    b.node_indices.resize(n);
+    for (size_t i = 0; i < n; ++i) b.node_indices[i] = (uint32_t)i;
+    b.nodes.assign(2 * n, Node());
+    b.root = 0;
+    b.nodes_used = 2;
+    b.nodes[0].left_first = 0;
+    b.nodes[0].count = (uint32_t)n;
+    update_node_bounds(b, mesh, 0);
+    try {
+        subdivide(b, mesh, 0);
+    } catch (const BuildError&) {
+        return false;
+    }
+    return true;
+}
+
+struct Hit {
+    float t, u, v;
+    uint32_t prim;
+};
+
+// bvh.rs:242-305 (Bvh::intersect_subtree).  Leaf triangles are tested against the
+// ray as passed in (bvh.rs:251); boxes against the shrinking closest ray (:269-270);
+// ties in entry distance visit the right child first (:271-275).
+template <class NodeAt, class TriAt>
+bool bvh_intersect_impl(NodeAt node_at, TriAt tri_at, uint32_t root, const Ray& ray, Hit* out,
+                        orc_counters* c) {
+    Node cur = node_at(root);
+    std::vector<Node> stack;
+    stack.reserve(64);
+    Ray closest = ray;
+    bool have = false;
+    Hit best{0, 0, 0, 0};
+    for (;;) {
+        if (cur.count > 0) {
+            if (c) c->leaves++;
+            uint32_t base = cur.left_first;  // node_indices is the identity (bvh.rs:526-528)
+            for (uint32_t k = 0; k < cur.count; ++k) {
+                uint32_t prim = base + k;
+                float t, u, v;
+                if (c) c->tris++;
+                if (tri_intersect(tri_at(prim), ray, &t, &u, &v)) {
+                    if (t < closest.t) {
+                        closest.t = t;
+                        best = Hit{t, u, v, prim};
+                        have = true;
+                    }
+                }
+            }
+            if (stack.empty()) break;
+            cur = stack.back();
+            stack.pop_back();
+        } else {
+            if (c) c->interior++;
+            Node l = node_at(cur.left_first);
+            Node r = node_at(cur.left_first + 1);
+            float dl = 0, dr = 0;
+            bool hl = aabb_intersect(l.aabb, closest, &dl);
+            bool hr = aabb_intersect(r.aabb, closest, &dr);
+            float kl = hl ? dl : FLT_MAX;
+            float kr = hr ? dr : FLT_MAX;
+            Node near_n, far_n;
+            bool near_h, far_h;
+            if (kl < kr) {
+                near_n = l; near_h = hl; far_n = r; far_h = hr;
+            } else {
+                near_n = r; near_h = hr; far_n = l; far_h = hl;
+            }
+            if (near_h) {
+                cur = near_n;
+                if (far_h) stack.push_back(far_n);
+                continue;
+            }
+            if (stack.empty()) break;
+            cur = stack.back();
+            stack.pop_back();
+        }
+    }
+    if (closest.t < FLT_MAX && have) {
+        *out = best;
+        return true;
+    }
+    return false;
+}
+
+inline Node load_node(const orc_node& n) {
+    Node r;
+    r.aabb.bmin = mk(n.bounds_min[0], n.bounds_min[1], n.bounds_min[2]);
+    r.aabb.bmax = mk(n.bounds_max[0], n.bounds_max[1], n.bounds_max[2]);
+    r.count = n.primitive_count;
+    r.left_first = n.left_first;
+    return r;
+}
+inline void store_node(const Node& n, orc_node* o) {
+    o->bounds_min[0] = n.aabb.bmin.x; o->bounds_min[1] = n.aabb.bmin.y; o->bounds_min[2] = n.aabb.bmin.z;
+    o->bounds_max[0] = n.aabb.bmax.x; o->bounds_max[1] = n.aabb.bmax.y; o->bounds_max[2] = n.aabb.bmax.z;
+    o->primitive_count = n.count;
+    o->left_first = n.left_first;
+}
+
+inline Ray load_ray(const orc_ray& r) {
+    return ray_new(mk(r.origin[0], r.origin[1], r.origin[2]),
+                   mk(r.direction[0], r.direction[1], r.direction[2]), r.t);
+}
+
+const orc_hit MISS = {FLT_MAX, 0.0f, 0.0f, 0xFFFFFFFFu, 0xFFFFFFFFu};
+
+void blas_trace_range(const orc_node* nodes, const orc_tri* mesh, const orc_ray* rays, orc_hit* hits,
+                      orc_counters* counters, uint32_t begin, uint32_t end) {
+    auto node_at = [nodes](uint32_t i) { return load_node(nodes[i]); };
+    auto tri_at = [mesh](uint32_t i) { return load_tri(mesh[i]); };
+    for (uint32_t i = begin; i < end; ++i) {
+        Ray r = load_ray(rays[i]);
+        Hit h{0, 0, 0, 0};
+        orc_counters* c = counters ? &counters[i] : nullptr;
+        if (c) std::memset(c, 0, sizeof(*c));
+        if (bvh_intersect_impl(node_at, tri_at, 0, r, &h, c)) {
+            hits[i] = orc_hit{h.t, h.u, h.v, h.prim, 0u};
+        } else {
+            hits[i] = MISS;
+        }
+    }
+}
+
+// --- TLAS (BT/src/scene/tlas.rs) -------------------------------------------------
+
+struct TlasNode {
+    Aabb aabb;          // Default: Aabb::new_empty (tlas.rs:48-56)
+    uint32_t left_right = 0;
+    uint32_t blas = 0;
+};
+// tlas.rs:17-32: new(l, r) = l + (r << 16); left() reads the HIGH half, right() the low.
+inline uint32_t lr_new(uint32_t l, uint32_t r) { return l + (r << 16); }
+inline uint32_t lr_left(uint32_t d) { return (d & 0xFFFF0000u) >> 16; }
+inline uint32_t lr_right(uint32_t d) { return d & 0x0000FFFFu; }
+
+// tlas.rs:179-202
+int find_best_match(const std::vector<TlasNode>& nodes, const std::vector<int32_t>& list, int n, int a) {
+    float smallest = FLT_MAX;
+    int best_b = -1;
+    for (int b = 0; b < n; ++b) {
+        if (b != a) {
+            V3 bmax = vmax(nodes[list[a]].aabb.bmax, nodes[list[b]].aabb.bmax);
+            V3 bmin = vmin(nodes[list[a]].aabb.bmin, nodes[list[b]].aabb.bmin);
+            V3 e = sub(bmax, bmin);
+            float sa = e.x * e.y + e.y * e.z + e.z * e.x;
+            if (sa < smallest) {
+                smallest = sa;
+                best_b = b;
+            }
+        }
+    }
+    return best_b;
+}
+
+// tlas.rs:204-250 (Tlas::rebuild) after TlasBuilder::build_for (tlas.rs:273-279).
+bool tlas_build(const std::vector<Aabb>& bounds, std::vector<TlasNode>& nodes, uint32_t* nodes_used_out) {
+    size_t count = bounds.size();
+    if (count == 0) return false;  // nodes[0] of an empty array
+    if (2 * count > 65536) return false;  // 16-bit child indices would wrap
+    TlasNode def;
+    def.aabb = aabb_new_empty();
+    nodes.assign(2 * count, def);
+    size_t node_index_count = count;
+    std::vector<int32_t> node_indices(count, 0);
+    int32_t nodes_used = 1;
+    for (size_t i = 0; i < count; ++i) {
+        node_indices[i] = nodes_used;
+        nodes[nodes_used].aabb = bounds[i];
+        nodes[nodes_used].blas = (uint32_t)i;
+        nodes[nodes_used].left_right = 0;
+        nodes_used += 1;
+    }
+    int a = 0;
+    int b = find_best_match(nodes, node_indices, (int)node_index_count, a);
+    while (node_index_count > 1) {
+        if (b < 0) return false;  // node_indices[-1]: the reference panics
+        int c = find_best_match(nodes, node_indices, (int)node_index_count, b);
+        if (a == c) {
+            int32_t ia = node_indices[a];
+            int32_t ib = node_indices[b];
+            TlasNode na = nodes[ia];
+            TlasNode nb = nodes[ib];
+            TlasNode& nn = nodes[nodes_used];
+            nn.left_right = lr_new((uint32_t)ia, (uint32_t)ib);
+            nn.aabb.bmin = vmin(na.aabb.bmin, nb.aabb.bmin);
+            nn.aabb.bmax = vmax(na.aabb.bmax, nb.aabb.bmax);
+            node_indices[a] = nodes_used;
+            nodes_used += 1;
+            node_indices[b] = node_indices[node_index_count - 1];
+            node_index_count -= 1;
+            b = find_best_match(nodes, node_indices, (int)node_index_count, a);
+        } else {
+            if (c < 0) return false;
+            a = b;
+            b = c;
+        }
+    }
+    nodes[0] = nodes[node_indices[a]];
+    *nodes_used_out = (uint32_t)nodes_used;
+    return true;
+}
+
+// BT/src/transform.rs:219-234 through cglinalg Matrix4x4 * Vector4 (column-major m[col*4+row]).
+inline V3 xf_point(const float* m, V3 p) {
+    return mk(((m[0] * p.x + m[4] * p.y) + m[8] * p.z) + m[12] * 1.0f,
+              ((m[1] * p.x + m[5] * p.y) + m[9] * p.z) + m[13] * 1.0f,
+              ((m[2] * p.x + m[6] * p.y) + m[10] * p.z) + m[14] * 1.0f);
+}
+inline V3 xf_vector(const float* m, V3 p) {
+    return mk(((m[0] * p.x + m[4] * p.y) + m[8] * p.z) + m[12] * 0.0f,
+              ((m[1] * p.x + m[5] * p.y) + m[9] * p.z) + m[13] * 0.0f,
+              ((m[2] * p.x + m[6] * p.y) + m[10] * p.z) + m[14] * 0.0f);
+}
+
+struct SceneView {
+    const orc_tlas_node* tlas;
+    const uint32_t* blas_of;
+    const float* inv;
+    uint32_t nobj;
+    const orc_node* nodes;
+    const uint32_t* node_off;
+    const orc_tri* tris;
+    const uint32_t* tri_off;
+};
+
+// tlas.rs:123-177 + scene_object.rs:78-89
+bool scene_intersect_one(const SceneView& s, const Ray& ray, orc_hit* out, orc_counters* c, int inst_zero) {
+    auto tnode = [&s](uint32_t i) {
+        TlasNode n;
+        const orc_tlas_node& o = s.tlas[i];
+        n.aabb.bmin = mk(o.bounds_min[0], o.bounds_min[1], o.bounds_min[2]);
+        n.aabb.bmax = mk(o.bounds_max[0], o.bounds_max[1], o.bounds_max[2]);
+        n.left_right = o.left_right;
+        n.blas = o.blas;
+        return n;
+    };
+    TlasNode cur = tnode(0);
+    std::vector<TlasNode> stack;
+    Ray closest = ray;
+    bool have = false;
+    orc_hit best = MISS;
+    for (;;) {
+        if (cur.left_right == 0) {
+            uint32_t obj = cur.blas;
+            if (c) c->blas_entries++;
+            const float* inv = s.inv + 16 * obj;
+            V3 o = xf_point(inv, closest.o);
+            V3 d = xf_vector(inv, closest.d);
+            Ray mray = ray_new(o, d, closest.t);
+            uint32_t bl = s.blas_of[obj];
+            const orc_node* nb = s.nodes + s.node_off[bl];
+            const orc_tri* tb = s.tris + s.tri_off[bl];
+            auto node_at = [nb](uint32_t i) { return load_node(nb[i]); };
+            auto tri_at = [tb](uint32_t i) { return load_tri(tb[i]); };
+            Hit h{0, 0, 0, 0};
+            if (bvh_intersect_impl(node_at, tri_at, 0, mray, &h, c)) {
+                // Intersection.ray.t is the BLAS's closest t, i.e. h.t (bvh.rs:253, :297-300).
+                if (h.t < closest.t) {
+                    closest.t = h.t;
+                    best = orc_hit{h.t, h.u, h.v, h.prim, inst_zero ? 0u : obj};
+                    have = true;
+                }
+            }
+            if (stack.empty()) break;
+            cur = stack.back();
+            stack.pop_back();
+        } else {
+            if (c) c->tlas_interior++;
+            TlasNode l = tnode(lr_left(cur.left_right));
+            TlasNode r = tnode(lr_right(cur.left_right));
+            float dl = 0, dr = 0;
+            bool hl = aabb_intersect(l.aabb, closest, &dl);
+            bool hr = aabb_intersect(r.aabb, closest, &dr);
+            float kl = hl ? dl : FLT_MAX;
+            float kr = hr ? dr : FLT_MAX;
+            TlasNode near_n, far_n;
+            bool near_h, far_h;
+            if (kl < kr) {
+                near_n = l; near_h = hl; far_n = r; far_h = hr;
+            } else {
+                near_n = r; near_h = hr; far_n = l; far_h = hl;
+            }
+            if (near_h) {
+                cur = near_n;
+                if (far_h) stack.push_back(far_n);
+                continue;
+            }
+            if (stack.empty()) break;
+            cur = stack.back();
+            stack.pop_back();
+        }
+    }
+    if (closest.t < FLT_MAX && have) {
+        *out = best;
+        return true;
+    }
+    *out = MISS;
+    return false;
+}
+
+// Cosine-weighted diffuse bounce (not in the reference; defined identically in the CUDA
+// library).  Only correctly rounded IEEE operations (+ - * / sqrt) are used, so the CPU
+// and GPU produce the same bits.  Marsaglia (1972) uniform sphere point q, direction
+// normalize(n + q) with n the face-forward geometric normal.
+inline uint32_t hash32(uint32_t x) {
+    x ^= x >> 16;
+    x *= 0x7feb352du;
+    x ^= x >> 15;
+    x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return x;
+}
+inline float rng_uniform(uint32_t key, uint32_t k) {
+    uint32_t h = hash32(key + k * 0x9E3779B9u);
+    return (float)(h >> 8) * (1.0f / 16777216.0f);
+}
+
+bool bounce_one(const Ray& prim, float t, const Tri& tri, uint32_t seed, uint32_t pixel, orc_ray* out) {
+    V3 p = add(prim.o, muls(prim.d, t));  // Ray::interpolate (ray.rs:37-39)
+    V3 e1 = sub(tri.v[1], tri.v[0]);
+    V3 e2 = sub(tri.v[2], tri.v[0]);
+    V3 n = cross(e1, e2);
+    float nl = std::sqrt(dot(n, n));
+    if (!(nl > 0.0f) || !(nl <= FLT_MAX)) return false;
+    n = mk(n.x / nl, n.y / nl, n.z / nl);
+    if (dot(n, prim.d) > 0.0f) n = neg(n);
+    uint32_t key = hash32(seed ^ hash32(pixel));
+    V3 q = n;
+    bool found = false;
+    for (uint32_t k = 0; k < 32u && !found; ++k) {
+        float x1 = 2.0f * rng_uniform(key, 2u * k) - 1.0f;
+        float x2 = 2.0f * rng_uniform(key, 2u * k + 1u) - 1.0f;
+        float s = x1 * x1 + x2 * x2;
+        if (s < 1.0f && s > 0.0f) {
+            float r = std::sqrt(1.0f - s);
+            q = mk((2.0f * x1) * r, (2.0f * x2) * r, 1.0f - 2.0f * s);
+            found = true;
+        }
+    }
+    V3 d = add(n, q);
+    float dl = std::sqrt(dot(d, d));
+    if (dl < 1e-6f) {
+        d = n;
+    } else {
+        d = mk(d.x / dl, d.y / dl, d.z / dl);
+    }
+    out->origin[0] = p.x; out->origin[1] = p.y; out->origin[2] = p.z;
+    out->direction[0] = d.x; out->direction[1] = d.y; out->direction[2] = d.z;
+    out->t = FLT_MAX;
+    out->pad = 0;
+    return true;
+}
+
+template <class F>
+void parallel_for(uint32_t n, int nthreads, F f) {
+    if (nthreads <= 1 || n < 1024) {
+        f(0u, n);
+        return;
+    }
+    std::vector<std::thread> th;
+    // Interleaved chunks keep threads balanced on uneven per-ray costs.
+    const uint32_t chunk = 256;
+    uint32_t nchunks = (n + chunk - 1) / chunk;
+    for (int t = 0; t < nthreads; ++t) {
+        th.emplace_back([=]() {
+            for (uint32_t c = (uint32_t)t; c < nchunks; c += (uint32_t)nthreads) {
+                uint32_t b = c * chunk;
+                uint32_t e = std::min(n, b + chunk);
+                f(b, e);
+            }
+        });
+    }
+    for (auto& x : th) x.join();
+}
+
+}  // namespace
+
+extern "C" {
+
+int orc_triangle_intersect(const orc_tri* tri, const orc_ray* ray, float* t, float* u, float* v) {
+    Tri tr = load_tri(*tri);
+    Ray r = load_ray(*ray);
+    return tri_intersect(tr, r, t, u, v) ? 1 : 0;
+}
+
+int orc_aabb_intersect(const float bmin[3], const float bmax[3], const orc_ray* ray, float* tmin) {
+    Aabb b;
+    b.bmin = mk(bmin[0], bmin[1], bmin[2]);
+    b.bmax = mk(bmax[0], bmax[1], bmax[2]);
+    Ray r = load_ray(*ray);
+    return aabb_intersect(b, r, tmin) ? 1 : 0;
+}
+
+void orc_normalize(const float in[3], float out[3]) {
+    V3 n = normalize(mk(in[0], in[1], in[2]));
+    out[0] = n.x; out[1] = n.y; out[2] = n.z;
+}
+
+void orc_triangle_centroid(const orc_tri* tri, float out[3]) {
+    V3 c = tri_centroid(load_tri(*tri));
+    out[0] = c.x; out[1] = c.y; out[2] = c.z;
+}
+
+int orc_bvh_build(orc_tri* mesh, uint32_t n, orc_node* nodes_out, uint32_t* nodes_used) {
+    if (!mesh || !nodes_out || !nodes_used) return ORC_ERR_ARG;
+    std::vector<Tri> m(n);
+    for (uint32_t i = 0; i < n; ++i) m[i] = load_tri(mesh[i]);
+    Bvh b;
+    if (!bvh_build(m, b)) return ORC_ERR_PANIC;
+    for (uint32_t i = 0; i < n; ++i) {
+        for (int k = 0; k < 3; ++k) {
+            mesh[i].v[3 * k + 0] = m[i].v[k].x;
+            mesh[i].v[3 * k + 1] = m[i].v[k].y;
+            mesh[i].v[3 * k + 2] = m[i].v[k].z;
+        }
+    }
+    for (size_t i = 0; i < b.nodes.size(); ++i) store_node(b.nodes[i], &nodes_out[i]);
+    *nodes_used = b.nodes_used;
+    return ORC_OK;
+}
+
+int orc_bvh_intersect(const orc_node* nodes, uint32_t nodes_used, const orc_tri* mesh, uint32_t n,
+                      const orc_ray* rays, uint32_t nrays, orc_hit* hits, orc_counters* counters) {
+    (void)nodes_used;
+    (void)n;
+    if (!nodes || !mesh || (!rays && nrays) || (!hits && nrays)) return ORC_ERR_ARG;
+    blas_trace_range(nodes, mesh, rays, hits, counters, 0, nrays);
+    return ORC_OK;
+}
+
+int orc_bvh_intersect_mt(const orc_node* nodes, uint32_t nodes_used, const orc_tri* mesh, uint32_t n,
+                         const orc_ray* rays, uint32_t nrays, orc_hit* hits, int nthreads) {
+    (void)nodes_used;
+    (void)n;
+    if (!nodes || !mesh || (!rays && nrays) || (!hits && nrays)) return ORC_ERR_ARG;
+    parallel_for(nrays, nthreads, [&](uint32_t b, uint32_t e) {
+        blas_trace_range(nodes, mesh, rays, hits, nullptr, b, e);
+    });
+    return ORC_OK;
+}
+
+// bvh.rs:469-493
+int orc_bvh_refit(orc_node* nodes, uint32_t nodes_used, const orc_tri* mesh, uint32_t n) {
+    if (!nodes || !mesh) return ORC_ERR_ARG;
+    (void)n;
+    for (uint32_t idx = nodes_used; idx-- > 0;) {
+        if (idx == 1) continue;
+        Node node = load_node(nodes[idx]);
+        if (node.count > 0) {
+            Aabb a;
+            a.bmin = mk(FLT_MAX, FLT_MAX, FLT_MAX);
+            a.bmax = mk(-FLT_MAX, -FLT_MAX, -FLT_MAX);
+            for (uint32_t k = 0; k < node.count; ++k) {
+                Tri p = load_tri(mesh[node.left_first + k]);
+                a.bmin = vmin(a.bmin, p.v[0]);
+                a.bmin = vmin(a.bmin, p.v[1]);
+                a.bmin = vmin(a.bmin, p.v[2]);
+                a.bmax = vmax(a.bmax, p.v[0]);
+                a.bmax = vmax(a.bmax, p.v[1]);
+                a.bmax = vmax(a.bmax, p.v[2]);
+            }
+            node.aabb = a;
+        } else {
+            Node l = load_node(nodes[node.left_first]);
+            Node r = load_node(nodes[node.left_first + 1]);
+            node.aabb.bmin = vmin(l.aabb.bmin, r.aabb.bmin);
+            node.aabb.bmax = vmax(l.aabb.bmax, r.aabb.bmax);
+        }
+        store_node(node, &nodes[idx]);
+    }
+    return ORC_OK;
+}
+
+uint32_t orc_bvh_depth(const orc_node* nodes, uint32_t nodes_used) {
+    if (!nodes || nodes_used == 0) return 0;
+    std::vector<std::pair<uint32_t, uint32_t>> st;
+    st.push_back({0u, 1u});
+    uint32_t best = 0;
+    while (!st.empty()) {
+        auto [i, d] = st.back();
+        st.pop_back();
+        best = std::max(best, d);
+        if (nodes[i].primitive_count == 0) {
+            st.push_back({nodes[i].left_first, d + 1});
+            st.push_back({nodes[i].left_first + 1, d + 1});
+        }
+    }
+    return best;
+}
+
+// scene_object.rs:60-75
+void orc_object_bounds(const float model_min[3], const float model_max[3], const float xf[16],
+                       float out_min[3], float out_max[3]) {
+    Aabb nb = aabb_new_empty();
+    for (int i = 0; i < 8; ++i) {
+        float x = (i & 1) ? model_max[0] : model_min[0];
+        float y = (i & 2) ? model_max[1] : model_min[1];
+        float z = (i & 4) ? model_max[2] : model_min[2];
+        aabb_grow(nb, xf_point(xf, mk(x, y, z)));
+    }
+    out_min[0] = nb.bmin.x; out_min[1] = nb.bmin.y; out_min[2] = nb.bmin.z;
+    out_max[0] = nb.bmax.x; out_max[1] = nb.bmax.y; out_max[2] = nb.bmax.z;
+}
+
+int orc_tlas_build(const float* obj_min, const float* obj_max, uint32_t count, orc_tlas_node* nodes_out,
+                   uint32_t* nodes_used) {
+    if (!obj_min || !obj_max || !nodes_out || !nodes_used) return ORC_ERR_ARG;
+    std::vector<Aabb> bounds(count);
+    for (uint32_t i = 0; i < count; ++i) {
+        bounds[i].bmin = mk(obj_min[3 * i], obj_min[3 * i + 1], obj_min[3 * i + 2]);
+        bounds[i].bmax = mk(obj_max[3 * i], obj_max[3 * i + 1], obj_max[3 * i + 2]);
+    }
+    std::vector<TlasNode> nodes;
+    uint32_t used = 0;
+    if (!tlas_build(bounds, nodes, &used)) return ORC_ERR_PANIC;
+    for (size_t i = 0; i < nodes.size(); ++i) {
+        orc_tlas_node& o = nodes_out[i];
+        o.bounds_min[0] = nodes[i].aabb.bmin.x; o.bounds_min[1] = nodes[i].aabb.bmin.y; o.bounds_min[2] = nodes[i].aabb.bmin.z;
+        o.bounds_max[0] = nodes[i].aabb.bmax.x; o.bounds_max[1] = nodes[i].aabb.bmax.y; o.bounds_max[2] = nodes[i].aabb.bmax.z;
+        o.left_right = nodes[i].left_right;
+        o.blas = nodes[i].blas;
+    }
+    *nodes_used = used;
+    return ORC_OK;
+}
+
+int orc_scene_intersect(const orc_tlas_node* tlas, uint32_t tlas_nodes_used, const uint32_t* blas_of,
+                        const float* inv, uint32_t nobj, const orc_node* nodes, const uint32_t* node_off,
+                        const orc_tri* tris, const uint32_t* tri_off, const orc_ray* rays, uint32_t nrays,
+                        orc_hit* hits, orc_counters* counters, int reference_instance_zero) {
+    (void)tlas_nodes_used;
+    if (!tlas || !blas_of || !inv || !nodes || !node_off || !tris || !tri_off) return ORC_ERR_ARG;
+    SceneView s{tlas, blas_of, inv, nobj, nodes, node_off, tris, tri_off};
+    for (uint32_t i = 0; i < nrays; ++i) {
+        orc_counters* c = counters ? &counters[i] : nullptr;
+        if (c) std::memset(c, 0, sizeof(*c));
+        scene_intersect_one(s, load_ray(rays[i]), &hits[i], c, reference_instance_zero);
+    }
+    return ORC_OK;
+}
+
+int orc_scene_intersect_mt(const orc_tlas_node* tlas, uint32_t tlas_nodes_used, const uint32_t* blas_of,
+                           const float* inv, uint32_t nobj, const orc_node* nodes, const uint32_t* node_off,
+                           const orc_tri* tris, const uint32_t* tri_off, const orc_ray* rays, uint32_t nrays,
+                           orc_hit* hits, int nthreads) {
+    (void)tlas_nodes_used;
+    if (!tlas || !blas_of || !inv || !nodes || !node_off || !tris || !tri_off) return ORC_ERR_ARG;
+    SceneView s{tlas, blas_of, inv, nobj, nodes, node_off, tris, tri_off};
+    parallel_for(nrays, nthreads, [&](uint32_t b, uint32_t e) {
+        for (uint32_t i = b; i < e; ++i) scene_intersect_one(s, load_ray(rays[i]), &hits[i], nullptr, 0);
+    });
+    return ORC_OK;
+}
+
+// BT/src/camera/camera.rs:994-1010 (get_ray_eye / get_ray_world).
+void orc_camera_ray(const float corners[9], const float view_inv[16], float u, float v, orc_ray* out) {
+    V3 tl = mk(corners[0], corners[1], corners[2]);
+    V3 tr = mk(corners[3], corners[4], corners[5]);
+    V3 bl = mk(corners[6], corners[7], corners[8]);
+    V3 origin = mk(0.0f, 0.0f, 0.0f);
+    V3 pixel = add(add(add(origin, tl), muls(sub(tr, tl), u)), muls(sub(bl, tl), v));
+    V3 dir = normalize(sub(pixel, origin));
+    V3 ow = xf_point(view_inv, origin);
+    V3 dw = xf_vector(view_inv, dir);
+    out->origin[0] = ow.x; out->origin[1] = ow.y; out->origin[2] = ow.z;
+    out->direction[0] = dw.x; out->direction[1] = dw.y; out->direction[2] = dw.z;
+    out->t = FLT_MAX;
+    out->pad = 0;
+}
+
+// Accumulator / shader kinds (same values as include/bvhgpu.h).
+enum { ACC_INTERSECTION = 0, ACC_DEPTH = 1, ACC_UV = 2, ACC_NORMAL = 3 };
+enum { SH_RADIANCE = 0, SH_INTERSECTION = 1, SH_DEPTH = 2 };
+
+static inline uint8_t rust_f32_as_u8(float x) {
+    if (!(x > 0.0f)) return 0;  // NaN and negatives saturate to 0
+    if (x >= 255.0f) return 255;
+    return (uint8_t)x;
+}
+static inline int32_t rust_f32_as_i32(float x) {
+    if (x != x) return 0;
+    if (x >= 2147483648.0f) return INT32_MAX;
+    if (x <= -2147483648.0f) return INT32_MIN;
+    return (int32_t)x;
+}
+
+// renderer.rs:345-384 (PathTracer::evaluate) with the accumulators of renderer.rs:134-286
+// and the shaders of renderer.rs:116-222.  The frame is w x h with 8x8 tiles; the
+// reference's fixed 80x80 tile grid is the w = h = 640 case.
+int orc_render(const float corners[9], const float view_inv[16], int width, int height, int accumulator,
+               const float* acc_params, int shader, const float* shader_params, const orc_node* nodes,
+               uint32_t nodes_used, const orc_tri* tris, uint32_t ntris, const float* normals, uint8_t* rgba,
+               float* radiance) {
+    (void)nodes_used;
+    (void)ntris;
+    if (width <= 0 || height <= 0 || !nodes || !tris || !rgba) return ORC_ERR_ARG;
+    if (accumulator == ACC_NORMAL && !normals) return ORC_ERR_ARG;
+    auto node_at = [nodes](uint32_t i) { return load_node(nodes[i]); };
+    auto tri_at = [tris](uint32_t i) { return load_tri(tris[i]); };
+    const float* P = acc_params;
+    const float* S = shader_params;
+    if ((accumulator == ACC_INTERSECTION || accumulator == ACC_NORMAL) && !P) return ORC_ERR_ARG;
+    if ((shader == SH_INTERSECTION || shader == SH_DEPTH) && !S) return ORC_ERR_ARG;
+    for (int y = 0; y < height; ++y) {
+        for (int x = 0; x < width; ++x) {
+            orc_ray rr;
+            orc_camera_ray(corners, view_inv, (float)x / (float)width, (float)y / (float)height, &rr);
+            Ray r = load_ray(rr);
+            Hit h{0, 0, 0, 0};
+            bool hit = bvh_intersect_impl(node_at, tri_at, 0, r, &h, nullptr);
+            V3 rad = mk(0, 0, 0);
+            switch (accumulator) {
+                case ACC_INTERSECTION:
+                    rad = hit ? mk(P[0], P[1], P[2]) : mk(P[3], P[4], P[5]);
+                    break;
+                case ACC_DEPTH: {
+                    float t = hit ? h.t : FLT_MAX;
+                    rad = mk(t, t, t);
+                    break;
+                }
+                case ACC_UV:
+                    rad = hit ? mk(h.u, h.v, 1.0f - (h.u + h.v)) : mk(0, 0, 0);
+                    break;
+                case ACC_NORMAL: {
+                    if (hit) {
+                        const float* nn = normals + 9 * (size_t)h.prim;
+                        V3 n0 = mk(nn[0], nn[1], nn[2]), n1 = mk(nn[3], nn[4], nn[5]), n2 = mk(nn[6], nn[7], nn[8]);
+                        float w0 = 1.0f - h.u - h.v;
+                        V3 nm = add(add(muls(n0, w0), muls(n1, h.u)), muls(n2, h.v));
+                        // object transform (accumulator params, 16 floats) applied as a vector
+                        V3 nw = xf_vector(P, nm);
+                        V3 nz = normalize(nw);
+                        rad = muls(add(nz, mk(1.0f, 1.0f, 1.0f)), 0.5f);
+                    }
+                    break;
+                }
+                default:
+                    return ORC_ERR_ARG;
+            }
+            size_t pix = (size_t)y * width + x;
+            if (radiance) {
+                radiance[3 * pix] = rad.x; radiance[3 * pix + 1] = rad.y; radiance[3 * pix + 2] = rad.z;
+            }
+            uint8_t* o = rgba + 4 * pix;
+            switch (shader) {
+                case SH_RADIANCE:
+                    o[0] = rust_f32_as_u8(255.0f * rad.x);
+                    o[1] = rust_f32_as_u8(255.0f * rad.y);
+                    o[2] = rust_f32_as_u8(255.0f * rad.z);
+                    o[3] = 255;
+                    break;
+                case SH_INTERSECTION: {
+                    // shader params: hit rgba, miss rgba (0..255)
+                    bool nz = !(rad.x == 0.0f && rad.y == 0.0f && rad.z == 0.0f);
+                    const float* c = nz ? S : S + 4;
+                    o[0] = (uint8_t)c[0]; o[1] = (uint8_t)c[1]; o[2] = (uint8_t)c[2]; o[3] = (uint8_t)c[3];
+                    break;
+                }
+                case SH_DEPTH: {
+                    float scale = S[0], offset = S[1];
+                    float t = rad.x;
+                    if (t < FLT_MAX) {
+                        uint32_t col = 255u - (uint32_t)rust_f32_as_i32((t - offset) * scale);
+                        uint32_t c = col * 0x010101u;
+                        o[0] = (uint8_t)((c & 0x00FF0000u) >> 16);
+                        o[1] = (uint8_t)((c & 0x0000FF00u) >> 8);
+                        o[2] = (uint8_t)(c & 0x000000FFu);
+                    } else {
+                        o[0] = 0; o[1] = 0; o[2] = 0;
+                    }
+                    o[3] = 255;
+                    break;
+                }
+                default:
+                    return ORC_ERR_ARG;
+            }
+        }
+    }
+    return ORC_OK;
+}
+
+int orc_bounce_ray(const orc_ray* primary, const orc_hit* hit, const orc_tri* tri, uint32_t seed, uint32_t pixel,
+                   orc_ray* out) {
+    if (hit->prim == 0xFFFFFFFFu) return 0;
+    return bounce_one(load_ray(*primary), hit->t, load_tri(*tri), seed, pixel, out) ? 1 : 0;
+}
+
+int orc_bounce_rays(const orc_ray* primaries, const orc_hit* hits, uint32_t nrays, const orc_tri* tris,
+                    uint32_t seed, orc_ray* out, uint8_t* valid) {
+    for (uint32_t i = 0; i < nrays; ++i) {
+        valid[i] = 0;
+        if (hits[i].prim == 0xFFFFFFFFu) continue;
+        valid[i] = bounce_one(load_ray(primaries[i]), hits[i].t, load_tri(tris[hits[i].prim]), seed, i, &out[i]) ? 1 : 0;
+    }
+    return ORC_OK;
+}
+
+}  // extern "C"
