@@ -1,0 +1,359 @@
+"""Benchmark: Mrays/s of the ray-BVH hot path on one GB300 (N replicas for N GPUs).
+
+Workload (default): the displaced icosphere with 6 subdivisions (81,920 triangles), SAH BVH
+built by the reference's algorithm, camera at distance 3, 1920 x 1080 primary rays plus one
+cosine-weighted diffuse bounce per hit pixel.  One step = one frame (primaries + bounces)
+traced by one persistent work-stealing launch; the plain pipeline (trace, compact, trace)
+is timed beside it.  Inputs are resident on the device; L2 is flushed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--mode persistent|plain]
+
+Prints one JSON line.  ``--impl reference`` times the CPU restatement of the reference's
+traversal (the reference is Rust and cannot be built here) on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mrays/s, 1 GB300: batched vs plain traversal, exact hit IDs; adjoint ms/step"
+WORKLOAD = "displaced icosphere (6 subdivisions, 81,920 tris) 1920x1080 primaries + 1 diffuse bounce"
+SEED = 0
+BOUNCE_SEED = 12345
+
+
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(
+        os.environ.get("LOCAL_RANK", "0"))
+
+
+class Clocks:
+    """Samples nvidia-smi SM clocks and throttle reasons while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx.append(float(p[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, p[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def setup_workload():
+    import bvhtracer_gb300 as bt
+    from bvhtracer_gb300 import scenes
+    tris, rays, _ = scenes.config1(seed=SEED)
+    bvh = bt.BvhBuilder().build_for(tris)
+    return tris, bvh, rays
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def cpu_baseline(tris, bvh, rays, budget_s: float = 12.0, threads: int | None = None):
+    """The CPU restatement of the reference traversal (oracle) on a bounded sample of the same
+    frame: a contiguous block of primaries (whole 8x8 tiles) and their bounces, all host
+    threads.  Also returns the per-ray work counters of a single-thread pass on a smaller
+    sample (the algorithmic bytes per ray of the roofline)."""
+    from oracle import oracle as orc
+    threads = threads or os.cpu_count() or 1
+    # calibrate on 1/256 of the frame, then size the sample to the time budget
+    n_total = len(rays)
+    probe = rays[: max(4096, n_total // 256)]
+    t0 = time.perf_counter()
+    h = orc.bvh_intersect(bvh.nodes, bvh.nodes_used, tris, probe, threads=threads)
+    b, v = orc.bounce_rays(probe, h, tris, BOUNCE_SEED)
+    orc.bvh_intersect(bvh.nodes, bvh.nodes_used, tris, b[v], threads=threads)
+    dt = max(time.perf_counter() - t0, 1e-3)
+    per_ray = dt / (len(probe) + int(v.sum()))
+    n = int(min(n_total, max(len(probe), budget_s / per_ray / 1.8)))
+    n -= n % 64
+    sample = rays[:n]
+    t0 = time.perf_counter()
+    h0 = orc.bvh_intersect(bvh.nodes, bvh.nodes_used, tris, sample, threads=threads)
+    b, v = orc.bounce_rays(sample, h0, tris, BOUNCE_SEED)
+    orc.bvh_intersect(bvh.nodes, bvh.nodes_used, tris, b[v], threads=threads)
+    dt = time.perf_counter() - t0
+    traced = n + int(v.sum())
+    # per-ray counters (single thread, every 16th ray of the frame + its bounce)
+    sub = rays[::16]
+    hs, cs = orc.bvh_intersect(bvh.nodes, bvh.nodes_used, tris, sub, counters=True)
+    bs, vs = orc.bounce_rays(sub, hs, tris, BOUNCE_SEED)
+    _, cb = orc.bvh_intersect(bvh.nodes, bvh.nodes_used, tris, bs[vs], counters=True)
+    bytes_prim = orc.bytes_per_ray(cs)
+    bytes_bounce = orc.bytes_per_ray(cb)
+    return {
+        "value": traced / dt / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "port",
+        "sample": f"{n} of {n_total} primaries (first {n // 64} 8x8 tiles) + their {int(v.sum())} bounce rays, "
+                  f"{threads} threads",
+        "seconds": dt,
+    }, {
+        "primary_bytes_per_ray": float(bytes_prim.mean()),
+        "bounce_bytes_per_ray": float(bytes_bounce.mean()),
+        "primary_interior_per_ray": float(cs["interior"].mean()),
+        "primary_tris_per_ray": float(cs["tris"].mean()),
+        "bounce_interior_per_ray": float(cb["interior"].mean()),
+        "bounce_tris_per_ray": float(cb["tris"].mean()),
+        "hit_fraction_sample": float((hs["prim"] != 0xFFFFFFFF).mean()),
+    }
+
+
+def run_reference(args):
+    """--impl reference: the CPU restatement timed on the host cores, each step a bounded
+    sample (1/64 of the frame's primaries, whole tiles, plus their bounces)."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    from oracle import oracle as orc
+    tris, bvh, rays = setup_workload()
+    threads = os.cpu_count() or 1
+    n = len(rays) // 64
+    n -= n % 64
+    times, traced = [], []
+    for step in range(args.warmup + args.steps):
+        blk = (step * 7919) % 64
+        sample = rays[blk * n:(blk + 1) * n]
+        t0 = time.perf_counter()
+        h0 = orc.bvh_intersect(bvh.nodes, bvh.nodes_used, tris, sample, threads=threads)
+        b, v = orc.bounce_rays(sample, h0, tris, BOUNCE_SEED)
+        orc.bvh_intersect(bvh.nodes, bvh.nodes_used, tris, b[v], threads=threads)
+        dt = time.perf_counter() - t0
+        if step >= args.warmup:
+            times.append(dt)
+            traced.append(n + int(v.sum()))
+    value = sum(traced) / sum(times) / 1e6
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "sample_per_step": f"{n} primaries + bounces (1/64 frame)",
+                   "seed": SEED},
+        "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": threads, "kind": "port",
+                         "sample": f"{n} primaries (1/64 of the frame, whole tiles) + their bounces per step; "
+                                   "the Rust reference cannot be built here (no cargo), the C++ restatement "
+                                   "of its traversal is timed"},
+        "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import bvhtracer_gb300 as bt
+    rank, world, local_rank = dist_env()
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        pg = dist
+
+    def barrier():
+        if pg:
+            pg.barrier()
+
+    tris, bvh, rays = setup_workload()
+    n = len(rays)
+    ctx = bt.Context(local_rank)
+    blas = ctx.upload_blas(bvh, tris)
+    d_rays = ctx.to_device(rays)
+    d_h0 = ctx.device_buffer(n * bt.HIT.itemsize)
+    d_h1 = ctx.device_buffer(n * bt.HIT.itemsize)
+    mode = bt.MODE_PERSISTENT if args.mode == "persistent" else bt.MODE_PLAIN
+    other = bt.MODE_PLAIN if mode == bt.MODE_PERSISTENT else bt.MODE_PERSISTENT
+
+    # rays per frame = primaries + bounce rays (one per primary hit)
+    h0 = np.zeros(n, bt.HIT)
+    blas.trace_bounce_async(d_rays, n, BOUNCE_SEED, mode, d_h0, d_h1)
+    ctx.sync()
+    d_h0.download(h0)
+    n_bounce = int((h0["prim"] != bt.MISS).sum())
+    rays_per_step = n + n_bounce
+
+    ev = [(ctx.event(), ctx.event()) for _ in range(args.steps)]
+
+    def timed(m, profile=False):
+        for _ in range(args.warmup):
+            ctx.flush_l2()
+            blas.trace_bounce_async(d_rays, n, BOUNCE_SEED, m, d_h0, d_h1)
+        ctx.sync()
+        barrier()
+        ctx.profile(profile)
+        ctx.profile_read()
+        launches0 = ctx.launch_count()
+        for s in range(args.steps):
+            ctx.flush_l2()
+            ev[s][0].record()
+            blas.trace_bounce_async(d_rays, n, BOUNCE_SEED, m, d_h0, d_h1)
+            ev[s][1].record()
+        ctx.sync()
+        barrier()
+        launches = ctx.launch_count() - launches0 - args.steps  # minus the L2 flush (a memset, no kernel)
+        ms = [a.elapsed_ms(b) for a, b in ev]
+        prof = ctx.profile_read()
+        ctx.profile(False)
+        return ms, launches, prof
+
+    clocks = Clocks(local_rank)
+    clocks.start()
+    ms, launches, prof = timed(mode, profile=True)
+    clk = clocks.stop()
+    ms_other, _, prof_other = timed(other, profile=True)
+    # launches counted by the library: kernels only (memsets / copies are not counted)
+    launches = ctx.launch_count()  # noqa: F841 (kept for clarity)
+
+    # max over ranks
+    total_ms = sum(ms)
+    if pg:
+        import torch
+        t = torch.tensor([total_ms], dtype=torch.float64)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        total_ms = float(t.item())
+    per_step_ms = total_ms / args.steps
+    value = world * rays_per_step * args.steps / (total_ms / 1e3) / 1e6
+    other_value = rays_per_step * len(ms_other) / (sum(ms_other) / 1e3) / 1e6
+
+    # e2e: the C-ABI call with host buffers (H2D rays, trace, D2H both hit arrays), pinned memory
+    pin_rays = ctx.pinned((n,), bt.RAY)
+    pin_rays.array[:] = rays
+    pin_h0 = ctx.pinned((n,), bt.HIT)
+    pin_h1 = ctx.pinned((n,), bt.HIT)
+    import ctypes
+    from bvhtracer_gb300._lib import ptr
+    nb = ctypes.c_uint32()
+
+    def e2e_once():
+        ctx.check(ctx.lib.bvhgpu_blas_trace_bounce(ctx.h, blas.id, ptr(pin_rays.array), n, BOUNCE_SEED, mode,
+                                                   ptr(pin_h0.array), ptr(pin_h1.array), ctypes.byref(nb)))
+
+    for _ in range(args.warmup):
+        e2e_once()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_once()
+    e2e_s = time.perf_counter() - t0
+    e2e_value = world * rays_per_step * args.steps / e2e_s / 1e6
+
+    if rank != 0:
+        return 0
+
+    result = {
+        "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": per_step_ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "mode": args.mode, "primary_rays": n, "bounce_rays": n_bounce,
+                   "rays_per_step": rays_per_step, "triangles": int(len(tris)), "bvh_nodes": bvh.nodes_used,
+                   "bvh_depth": blas.depth, "l2": "flushed between steps (256 MB memset)",
+                   "parallelism": f"replicas x{world}", "seed": SEED},
+        "plain_vs_persistent": {
+            args.mode: value / world,
+            ("plain" if mode == bt.MODE_PERSISTENT else "persistent"): other_value,
+            "ratio_persistent_over_plain": (value / world / other_value) if mode == bt.MODE_PERSISTENT
+            else (other_value / (value / world)),
+        },
+        "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": n * bt.RAY.itemsize,
+                "d2h_bytes_per_step": 2 * n * bt.HIT.itemsize},
+        "gpu_launches": None,
+        "clocks": clk,
+        "kernel_ms": {k: {"ms_total": v[0], "launches": v[1]} for k, v in prof.items()},
+    }
+    kernel_launches = sum(v[1] for v in prof.values())
+    result["gpu_launches"] = kernel_launches
+
+    base, counters = cpu_baseline(tris, bvh, rays)
+    result["cpu_baseline"] = base
+    peak, peak_kind = measured_peaks()
+    dom = max(prof.items(), key=lambda kv: kv[1][0])
+    dom_name, (dom_ms, dom_launches) = dom
+    per_launch_s = dom_ms / dom_launches / 1e3
+    if mode == bt.MODE_PERSISTENT:
+        alg_bytes = n * counters["primary_bytes_per_ray"] + n_bounce * counters["bounce_bytes_per_ray"]
+    else:
+        alg_bytes = (n if dom_name == "trace_blas" else n_bounce) * (
+            counters["primary_bytes_per_ray"] if dom_name == "trace_blas" else counters["bounce_bytes_per_ray"])
+    achieved = alg_bytes / per_launch_s / 1e9
+    result["roofline"] = {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak,
+                          "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                          "algorithmic_bytes_per_launch": alg_bytes, "launch_ms": per_launch_s * 1e3,
+                          "counters": counters}
+    print(json.dumps(result), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--mode", choices=["persistent", "plain"], default="persistent")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,15 @@
+"""bvhtracer_gb300: the ray-BVH hot path of lambdaxymox/bvhtracer on one GB300 (sm_103a).
+
+The compute path is the CUDA library ``libbvhgpu.so`` (C ABI in include/bvhgpu.h);
+this package is its host-side mirror of the reference's interface (see ``api``) plus
+the seeded synthetic workloads (``scenes``).
+"""
+from .api import (BATCH_ITEM, FLT_MAX, HIT, MISS, NODE, RAY, TLAS_NODE, Blas, Bvh, BvhBuilder, Camera, Context,
+                  DeviceBuffer, Event, PinnedArray, Scene)
+from ._lib import (ACC_DEPTH, ACC_INTERSECTION, ACC_NORMAL, ACC_UV, MODE_PERSISTENT, MODE_PLAIN, SHADER_DEPTH,
+                   SHADER_INTERSECTION, SHADER_RADIANCE, BvhGpuError)
+
+__all__ = ["Context", "DeviceBuffer", "PinnedArray", "Event", "Bvh", "BvhBuilder", "Blas", "Scene", "Camera",
+           "RAY", "HIT", "NODE", "TLAS_NODE", "BATCH_ITEM", "MISS", "FLT_MAX", "BvhGpuError",
+           "ACC_INTERSECTION", "ACC_DEPTH", "ACC_UV", "ACC_NORMAL", "SHADER_RADIANCE", "SHADER_INTERSECTION",
+           "SHADER_DEPTH", "MODE_PLAIN", "MODE_PERSISTENT"]

@@ -1,0 +1,127 @@
+"""ctypes binding of the bvhgpu C ABI (include/bvhgpu.h).
+
+The library is the in-tree ``bvhtracer_gb300/_build/libbvhgpu.so`` built by
+``bvhtracer_gb300.build``.  There is no CPU fallback: if the library is missing
+or no CUDA device is present, the calls raise.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+NODE = np.dtype([("bounds_min", "<f4", 3), ("bounds_max", "<f4", 3),
+                 ("primitive_count", "<u4"), ("left_first", "<u4")])
+RAY = np.dtype([("origin", "<f4", 3), ("t", "<f4"), ("direction", "<f4", 3), ("reserved", "<u4")])
+HIT = np.dtype([("t", "<f4"), ("u", "<f4"), ("v", "<f4"), ("prim", "<u4"), ("inst", "<u4")])
+TLAS_NODE = np.dtype([("bounds_min", "<f4", 3), ("bounds_max", "<f4", 3),
+                      ("left_right", "<u4"), ("blas", "<u4")])
+BATCH_ITEM = np.dtype([("blas", "<u4"), ("ray_offset", "<u4"), ("ray_count", "<u4"), ("reserved", "<u4")])
+assert NODE.itemsize == 32 and RAY.itemsize == 32 and HIT.itemsize == 20
+assert TLAS_NODE.itemsize == 32 and BATCH_ITEM.itemsize == 16
+
+MISS = 0xFFFFFFFF
+FLT_MAX = np.float32(np.finfo(np.float32).max)
+
+OK = 0
+ERRORS = {1: "invalid argument", 2: "out of memory", 3: "CUDA error", 4: "stack depth exceeded",
+          5: "step cap exceeded", 6: "build would panic", 7: "no CUDA device"}
+
+ACC_INTERSECTION, ACC_DEPTH, ACC_UV, ACC_NORMAL = 0, 1, 2, 3
+SHADER_RADIANCE, SHADER_INTERSECTION, SHADER_DEPTH = 0, 1, 2
+MODE_PLAIN, MODE_PERSISTENT = 0, 1
+
+KERNELS = ["trace_blas", "trace_scene", "persistent_bounce", "bounce_gen", "trace_queue", "trace_batch",
+           "refit", "tlas_build", "render", "other"]
+
+# Exported symbols and their ctypes signatures (kept in the order of include/bvhgpu.h).
+_P = ctypes.c_void_p
+_U32 = ctypes.c_uint32
+_I = ctypes.c_int
+_SZ = ctypes.c_size_t
+SIGNATURES = {
+    "bvhgpu_create": (_I, [_P, _I]),
+    "bvhgpu_destroy": (_I, [_P]),
+    "bvhgpu_last_error": (ctypes.c_char_p, [_P]),
+    "bvhgpu_launch_count": (ctypes.c_uint64, []),
+    "bvhgpu_sync": (_I, [_P]),
+    "bvhgpu_get_stream": (_P, [_P]),
+    "bvhgpu_device_alloc": (_I, [_P, _SZ, _P]),
+    "bvhgpu_device_free": (_I, [_P, _P]),
+    "bvhgpu_host_alloc": (_I, [_P, _SZ, _P]),
+    "bvhgpu_host_free": (_I, [_P, _P]),
+    "bvhgpu_copy_to_device": (_I, [_P, _P, _P, _SZ, _P]),
+    "bvhgpu_copy_to_host": (_I, [_P, _P, _P, _SZ, _P]),
+    "bvhgpu_memset_device": (_I, [_P, _P, _I, _SZ, _P]),
+    "bvhgpu_flush_l2": (_I, [_P, _P]),
+    "bvhgpu_event_create": (_I, [_P, _P]),
+    "bvhgpu_event_destroy": (_I, [_P, _P]),
+    "bvhgpu_event_record": (_I, [_P, _P, _P]),
+    "bvhgpu_event_elapsed_ms": (_I, [_P, _P, _P, _P]),
+    "bvhgpu_profile_enable": (_I, [_P, _I]),
+    "bvhgpu_profile_read": (_I, [_P, _P, _P]),
+    "bvhgpu_build_bvh_host": (_I, [_P, _U32, _P, _P]),
+    "bvhgpu_blas_upload": (_I, [_P, _P, _U32, _P, _U32, _P]),
+    "bvhgpu_blas_free": (_I, [_P, _U32]),
+    "bvhgpu_blas_info": (_I, [_P, _U32, _P, _P, _P]),
+    "bvhgpu_blas_update_vertices": (_I, [_P, _U32, _P]),
+    "bvhgpu_blas_update_vertices_async": (_I, [_P, _U32, _P, _P]),
+    "bvhgpu_blas_refit": (_I, [_P, _U32]),
+    "bvhgpu_blas_refit_async": (_I, [_P, _U32, _P]),
+    "bvhgpu_blas_download_nodes": (_I, [_P, _U32, _P]),
+    "bvhgpu_blas_intersect": (_I, [_P, _U32, _P, _U32, _P]),
+    "bvhgpu_blas_intersect_async": (_I, [_P, _U32, _P, _U32, _P, _P]),
+    "bvhgpu_blas_trace_bounce": (_I, [_P, _U32, _P, _U32, _U32, _I, _P, _P, _P]),
+    "bvhgpu_blas_trace_bounce_async": (_I, [_P, _U32, _P, _U32, _U32, _I, _P, _P, _P]),
+    "bvhgpu_blas_bounce_rays": (_I, [_P, _U32, _P, _U32, _U32, _P, _P]),
+    "bvhgpu_trace_batch": (_I, [_P, _P, _U32, _P, _U32, _I, _P]),
+    "bvhgpu_trace_batch_async": (_I, [_P, _P, _U32, _P, _U32, _I, _P, _P]),
+    "bvhgpu_scene_create": (_I, [_P, _P, _U32, _P]),
+    "bvhgpu_scene_free": (_I, [_P, _U32]),
+    "bvhgpu_scene_set_transforms": (_I, [_P, _U32, _P, _P]),
+    "bvhgpu_scene_set_transforms_async": (_I, [_P, _U32, _P, _P, _P]),
+    "bvhgpu_scene_rebuild": (_I, [_P, _U32]),
+    "bvhgpu_scene_rebuild_async": (_I, [_P, _U32, _P]),
+    "bvhgpu_scene_download_tlas": (_I, [_P, _U32, _P, _P]),
+    "bvhgpu_scene_intersect": (_I, [_P, _U32, _P, _U32, _P]),
+    "bvhgpu_scene_intersect_async": (_I, [_P, _U32, _P, _U32, _P, _P]),
+    "bvhgpu_render": (_I, [_P, _U32, _P, _I, _I, _I, _P, _I, _P, _P, _P, _P]),
+}
+
+_lib = None
+
+
+def load(build_if_missing: bool = True):
+    """Load libbvhgpu.so (building it in-tree first if it is missing or stale)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if build_if_missing and not _build.up_to_date():
+        _build.build()
+    if not os.path.exists(path):
+        raise RuntimeError(f"libbvhgpu.so not found at {path}; run bvhtracer_gb300.build.build()")
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def ptr(a):
+    if a is None:
+        return None
+    if isinstance(a, int):
+        return ctypes.c_void_p(a)
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+class BvhGpuError(RuntimeError):
+    def __init__(self, code, message):
+        super().__init__(f"bvhgpu error {code} ({ERRORS.get(code, '?')}): {message}")
+        self.code = code

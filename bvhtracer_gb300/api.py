@@ -1,0 +1,422 @@
+"""Host-side mirror of the reference's ray-BVH interface over the bvhgpu C ABI.
+
+Names follow the reference crate (lambdaxymox/bvhtracer): ``BvhBuilder.build_for``
+(BT/src/model/bvh.rs:524-541), ``ModelInstance.intersect`` / ``refit``
+(BT/src/model/model.rs:27-33), ``Scene.intersect`` / ``rebuild``
+(BT/src/scene/scene.rs:32-38), ``Camera.get_ray_world`` (BT/src/camera/camera.rs:1004),
+``Renderer.render`` with a GPU integrator (BT/src/renderer.rs:388-400).  Misses are
+reported as ``t = FLT_MAX, prim = inst = MISS`` (the reference's ``Option::None``).
+Errors raise :class:`BvhGpuError`; there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import (BATCH_ITEM, FLT_MAX, HIT, MISS, NODE, RAY, TLAS_NODE, BvhGpuError, ptr)
+
+
+class Context:
+    """One bvhgpu context on one CUDA device (not thread-safe, like the reference's Rc model)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = _lib.load()
+        h = ctypes.c_void_p()
+        rc = self.lib.bvhgpu_create(ctypes.byref(h), device)
+        if rc != 0:
+            raise BvhGpuError(rc, "bvhgpu_create failed (is a CUDA device present?)")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.bvhgpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def check(self, rc: int):
+        if rc != 0:
+            msg = self.lib.bvhgpu_last_error(self.h)
+            raise BvhGpuError(rc, msg.decode() if msg else "")
+
+    def sync(self):
+        self.check(self.lib.bvhgpu_sync(self.h))
+
+    @property
+    def stream(self):
+        return self.lib.bvhgpu_get_stream(self.h)
+
+    def launch_count(self) -> int:
+        return int(self.lib.bvhgpu_launch_count())
+
+    # -- memory ---------------------------------------------------------------------------
+    def device_buffer(self, nbytes: int) -> "DeviceBuffer":
+        return DeviceBuffer(self, nbytes)
+
+    def to_device(self, arr: np.ndarray) -> "DeviceBuffer":
+        arr = np.ascontiguousarray(arr)
+        buf = DeviceBuffer(self, arr.nbytes)
+        buf.upload(arr)
+        return buf
+
+    def pinned(self, shape, dtype) -> "PinnedArray":
+        return PinnedArray(self, shape, dtype)
+
+    def flush_l2(self, stream=None):
+        self.check(self.lib.bvhgpu_flush_l2(self.h, stream))
+
+    def event(self) -> "Event":
+        return Event(self)
+
+    def profile(self, enable: bool):
+        self.check(self.lib.bvhgpu_profile_enable(self.h, int(enable)))
+
+    def profile_read(self) -> dict:
+        ms = np.zeros(len(_lib.KERNELS), np.float64)
+        n = np.zeros(len(_lib.KERNELS), np.uint64)
+        self.check(self.lib.bvhgpu_profile_read(self.h, ptr(ms), ptr(n)))
+        return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(_lib.KERNELS) if n[i]}
+
+    # -- objects --------------------------------------------------------------------------
+    def upload_blas(self, bvh: "Bvh", tris: np.ndarray) -> "Blas":
+        return Blas(self, bvh, tris)
+
+    def scene(self, blases, transforms=None, inverses=None) -> "Scene":
+        return Scene(self, blases, transforms, inverses)
+
+    def trace_batch(self, items, rays: np.ndarray, mode: int) -> np.ndarray:
+        items = np.ascontiguousarray(items, BATCH_ITEM)
+        rays = np.ascontiguousarray(rays, RAY)
+        hits = np.zeros(len(rays), HIT)
+        self.check(self.lib.bvhgpu_trace_batch(self.h, ptr(items), len(items), ptr(rays), len(rays), mode,
+                                               ptr(hits)))
+        return hits
+
+    def trace_batch_async(self, items, d_rays: "DeviceBuffer", nrays: int, mode: int, d_hits: "DeviceBuffer",
+                          stream=None):
+        items = np.ascontiguousarray(items, BATCH_ITEM)
+        self.check(self.lib.bvhgpu_trace_batch_async(self.h, ptr(items), len(items), d_rays.ptr, nrays, mode,
+                                                     d_hits.ptr, stream))
+
+
+class DeviceBuffer:
+    def __init__(self, ctx: Context, nbytes: int):
+        self.ctx = ctx
+        self.nbytes = int(nbytes)
+        p = ctypes.c_void_p()
+        ctx.check(ctx.lib.bvhgpu_device_alloc(ctx.h, max(self.nbytes, 16), ctypes.byref(p)))
+        self.p = p
+
+    @property
+    def ptr(self):
+        return self.p
+
+    def upload(self, arr: np.ndarray, stream=None, sync: bool = True):
+        arr = np.ascontiguousarray(arr)
+        assert arr.nbytes <= self.nbytes
+        self.ctx.check(self.ctx.lib.bvhgpu_copy_to_device(self.ctx.h, self.p, ptr(arr), arr.nbytes, stream))
+        if sync:
+            self.ctx.sync()
+
+    def download(self, out: np.ndarray, stream=None, sync: bool = True) -> np.ndarray:
+        assert out.flags.c_contiguous and out.nbytes <= self.nbytes
+        self.ctx.check(self.ctx.lib.bvhgpu_copy_to_host(self.ctx.h, ptr(out), self.p, out.nbytes, stream))
+        if sync:
+            self.ctx.sync()
+        return out
+
+    def zero(self, stream=None):
+        self.ctx.check(self.ctx.lib.bvhgpu_memset_device(self.ctx.h, self.p, 0, self.nbytes, stream))
+
+    def free(self):
+        if self.p:
+            self.ctx.lib.bvhgpu_device_free(self.ctx.h, self.p)
+            self.p = None
+
+    def __del__(self):
+        try:
+            if self.ctx.h:
+                self.free()
+        except Exception:
+            pass
+
+
+class PinnedArray:
+    """A numpy view over page-locked host memory (for asynchronous copies)."""
+
+    def __init__(self, ctx: Context, shape, dtype):
+        self.ctx = ctx
+        dtype = np.dtype(dtype)
+        n = int(np.prod(shape)) * dtype.itemsize
+        p = ctypes.c_void_p()
+        ctx.check(ctx.lib.bvhgpu_host_alloc(ctx.h, max(n, 16), ctypes.byref(p)))
+        self.p = p
+        buf = (ctypes.c_char * max(n, 16)).from_address(p.value)
+        self.array = np.frombuffer(buf, dtype=np.uint8, count=n).view(dtype).reshape(shape)
+
+    def free(self):
+        if self.p:
+            self.array = None
+            self.ctx.lib.bvhgpu_host_free(self.ctx.h, self.p)
+            self.p = None
+
+
+class Event:
+    def __init__(self, ctx: Context):
+        self.ctx = ctx
+        p = ctypes.c_void_p()
+        ctx.check(ctx.lib.bvhgpu_event_create(ctx.h, ctypes.byref(p)))
+        self.p = p
+
+    def record(self, stream=None):
+        self.ctx.check(self.ctx.lib.bvhgpu_event_record(self.ctx.h, self.p, stream))
+
+    def elapsed_ms(self, later: "Event") -> float:
+        ms = ctypes.c_float()
+        self.ctx.check(self.ctx.lib.bvhgpu_event_elapsed_ms(self.ctx.h, self.p, later.p, ctypes.byref(ms)))
+        return float(ms.value)
+
+
+# ---- BVH build (host) -----------------------------------------------------------------------
+
+class Bvh:
+    """The reference's Bvh node array (bvh.rs:227-233): nodes[2n], nodes_used."""
+
+    def __init__(self, nodes: np.ndarray, nodes_used: int):
+        self.nodes = nodes
+        self.nodes_used = int(nodes_used)
+
+    def bounds(self):
+        """Bvh::bounds (bvh.rs:499-501)."""
+        return self.nodes[0]["bounds_min"].copy(), self.nodes[0]["bounds_max"].copy()
+
+
+class BvhBuilder:
+    """BvhBuilder::build_for (bvh.rs:524-541): SAH binned build on the host (8 bins)."""
+
+    def build_for(self, mesh: np.ndarray) -> Bvh:
+        """Builds the BVH and reorders ``mesh`` ([n, 9] float32, C-contiguous) in place."""
+        if mesh.dtype != np.float32 or not mesh.flags.c_contiguous or mesh.ndim != 2 or mesh.shape[1] != 9:
+            raise ValueError("mesh must be a C-contiguous float32 array of shape [n, 9]")
+        n = mesh.shape[0]
+        nodes = np.zeros(max(2 * n, 1), NODE)
+        used = ctypes.c_uint32()
+        lib = _lib.load()
+        rc = lib.bvhgpu_build_bvh_host(ptr(mesh), n, ptr(nodes), ctypes.byref(used))
+        if rc != 0:
+            raise BvhGpuError(rc, "BvhBuilder::build_for: the reference build would panic on this mesh"
+                              if rc == 6 else "bad mesh")
+        return Bvh(nodes, used.value)
+
+
+# ---- BLAS on the GPU --------------------------------------------------------------------------
+
+class Blas:
+    """A BVH + its triangles resident on the GPU: ModelInstance's intersect / refit."""
+
+    def __init__(self, ctx: Context, bvh: Bvh, tris: np.ndarray):
+        self.ctx = ctx
+        tris = np.ascontiguousarray(tris, np.float32).reshape(-1, 9)
+        nodes = np.ascontiguousarray(bvh.nodes[:bvh.nodes_used])
+        bid = ctypes.c_uint32()
+        ctx.check(ctx.lib.bvhgpu_blas_upload(ctx.h, ptr(nodes), bvh.nodes_used, ptr(tris), len(tris),
+                                             ctypes.byref(bid)))
+        self.id = bid.value
+        self.nodes_used = bvh.nodes_used
+        self.ntris = len(tris)
+        nu, nt, depth = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint32()
+        ctx.check(ctx.lib.bvhgpu_blas_info(ctx.h, self.id, ctypes.byref(nu), ctypes.byref(nt), ctypes.byref(depth)))
+        self.depth = depth.value
+
+    def intersect(self, rays: np.ndarray) -> np.ndarray:
+        """Bvh::intersect for every ray (host arrays in, host hits out)."""
+        rays = np.ascontiguousarray(rays, RAY)
+        hits = np.zeros(len(rays), HIT)
+        self.ctx.check(self.ctx.lib.bvhgpu_blas_intersect(self.ctx.h, self.id, ptr(rays), len(rays), ptr(hits)))
+        return hits
+
+    def intersect_async(self, d_rays: DeviceBuffer, n: int, d_hits: DeviceBuffer, stream=None):
+        self.ctx.check(self.ctx.lib.bvhgpu_blas_intersect_async(self.ctx.h, self.id, d_rays.ptr, n, d_hits.ptr,
+                                                                stream))
+
+    def trace_bounce(self, rays: np.ndarray, seed: int, mode: int):
+        rays = np.ascontiguousarray(rays, RAY)
+        h0 = np.zeros(len(rays), HIT)
+        h1 = np.zeros(len(rays), HIT)
+        nb = ctypes.c_uint32()
+        self.ctx.check(self.ctx.lib.bvhgpu_blas_trace_bounce(self.ctx.h, self.id, ptr(rays), len(rays), seed, mode,
+                                                             ptr(h0), ptr(h1), ctypes.byref(nb)))
+        return h0, h1, nb.value
+
+    def trace_bounce_async(self, d_rays, n, seed, mode, d_h0, d_h1, stream=None):
+        self.ctx.check(self.ctx.lib.bvhgpu_blas_trace_bounce_async(self.ctx.h, self.id, d_rays.ptr, n, seed, mode,
+                                                                   d_h0.ptr, d_h1.ptr, stream))
+
+    def bounce_rays(self, rays: np.ndarray, seed: int):
+        rays = np.ascontiguousarray(rays, RAY)
+        out = np.zeros(len(rays), RAY)
+        valid = np.zeros(len(rays), np.uint8)
+        self.ctx.check(self.ctx.lib.bvhgpu_blas_bounce_rays(self.ctx.h, self.id, ptr(rays), len(rays), seed,
+                                                            ptr(out), ptr(valid)))
+        return out, valid.astype(bool)
+
+    def update_vertices(self, tris: np.ndarray):
+        tris = np.ascontiguousarray(tris, np.float32).reshape(-1, 9)
+        assert len(tris) == self.ntris
+        self.ctx.check(self.ctx.lib.bvhgpu_blas_update_vertices(self.ctx.h, self.id, ptr(tris)))
+
+    def update_vertices_async(self, d_tris: DeviceBuffer, stream=None):
+        self.ctx.check(self.ctx.lib.bvhgpu_blas_update_vertices_async(self.ctx.h, self.id, d_tris.ptr, stream))
+
+    def refit(self):
+        """Bvh::refit (bvh.rs:469-493) on the GPU."""
+        self.ctx.check(self.ctx.lib.bvhgpu_blas_refit(self.ctx.h, self.id))
+
+    def refit_async(self, stream=None):
+        self.ctx.check(self.ctx.lib.bvhgpu_blas_refit_async(self.ctx.h, self.id, stream))
+
+    def download_nodes(self) -> np.ndarray:
+        out = np.zeros(self.nodes_used, NODE)
+        self.ctx.check(self.ctx.lib.bvhgpu_blas_download_nodes(self.ctx.h, self.id, ptr(out)))
+        return out
+
+    def render(self, camera: "Camera", width: int, height: int, accumulator: int, shader: int,
+               acc_params=None, shader_params=None, normals=None):
+        """PathTracer::evaluate on this BLAS: returns (rgba [h, w, 4] uint8, rays traced)."""
+        cam = camera.to_struct()
+        rgba = np.zeros((height, width, 4), np.uint8)
+        ap = None if acc_params is None else np.ascontiguousarray(acc_params, np.float32)
+        sp = None if shader_params is None else np.ascontiguousarray(shader_params, np.float32)
+        nrm = None if normals is None else np.ascontiguousarray(normals, np.float32).reshape(-1, 9)
+        rays = ctypes.c_uint64()
+        self.ctx.check(self.ctx.lib.bvhgpu_render(self.ctx.h, self.id, ptr(cam), width, height, accumulator,
+                                                  ptr(ap), shader, ptr(sp), ptr(nrm), ptr(rgba),
+                                                  ctypes.byref(rays)))
+        return rgba, rays.value
+
+    def free(self):
+        if self.id:
+            self.ctx.lib.bvhgpu_blas_free(self.ctx.h, self.id)
+            self.id = 0
+
+
+class Scene:
+    """Scene over instanced BLASes with a GPU-rebuilt TLAS (scene.rs, tlas.rs, scene_object.rs)."""
+
+    def __init__(self, ctx: Context, blases, transforms=None, inverses=None):
+        self.ctx = ctx
+        ids = np.ascontiguousarray([b.id for b in blases], np.uint32)
+        sid = ctypes.c_uint32()
+        ctx.check(ctx.lib.bvhgpu_scene_create(ctx.h, ptr(ids), len(ids), ctypes.byref(sid)))
+        self.id = sid.value
+        self.nobjects = len(ids)
+        if transforms is not None:
+            self.set_transforms(transforms, inverses)
+            self.rebuild()
+
+    def set_transforms(self, xf, inv):
+        """SceneObject::set_transform for every object: 4x4 column-major transforms + inverses."""
+        xf = np.ascontiguousarray(xf, np.float32).reshape(self.nobjects, 16)
+        inv = np.ascontiguousarray(inv, np.float32).reshape(self.nobjects, 16)
+        self.ctx.check(self.ctx.lib.bvhgpu_scene_set_transforms(self.ctx.h, self.id, ptr(xf), ptr(inv)))
+
+    def set_transforms_async(self, d_xf: DeviceBuffer, d_inv: DeviceBuffer, stream=None):
+        self.ctx.check(self.ctx.lib.bvhgpu_scene_set_transforms_async(self.ctx.h, self.id, d_xf.ptr, d_inv.ptr,
+                                                                      stream))
+
+    def rebuild(self):
+        """Scene::rebuild (TLAS rebuild on the GPU)."""
+        self.ctx.check(self.ctx.lib.bvhgpu_scene_rebuild(self.ctx.h, self.id))
+
+    def rebuild_async(self, stream=None):
+        self.ctx.check(self.ctx.lib.bvhgpu_scene_rebuild_async(self.ctx.h, self.id, stream))
+
+    def download_tlas(self):
+        nodes = np.zeros(2 * self.nobjects, TLAS_NODE)
+        used = ctypes.c_uint32()
+        self.ctx.check(self.ctx.lib.bvhgpu_scene_download_tlas(self.ctx.h, self.id, ptr(nodes), ctypes.byref(used)))
+        return nodes, used.value
+
+    def intersect(self, rays: np.ndarray) -> np.ndarray:
+        rays = np.ascontiguousarray(rays, RAY)
+        hits = np.zeros(len(rays), HIT)
+        self.ctx.check(self.ctx.lib.bvhgpu_scene_intersect(self.ctx.h, self.id, ptr(rays), len(rays), ptr(hits)))
+        return hits
+
+    def intersect_async(self, d_rays: DeviceBuffer, n: int, d_hits: DeviceBuffer, stream=None):
+        self.ctx.check(self.ctx.lib.bvhgpu_scene_intersect_async(self.ctx.h, self.id, d_rays.ptr, n, d_hits.ptr,
+                                                                 stream))
+
+    def free(self):
+        if self.id:
+            self.ctx.lib.bvhgpu_scene_free(self.ctx.h, self.id)
+            self.id = 0
+
+
+# ---- camera ---------------------------------------------------------------------------------
+
+CAMERA = np.dtype([("top_left", "<f4", 3), ("top_right", "<f4", 3), ("bottom_left", "<f4", 3),
+                   ("view_inv", "<f4", 16)])
+
+
+class Camera:
+    """Camera<f32, PerspectiveProjection> reduced to what get_ray_world needs (camera.rs:994-1010).
+
+    ``box_spec`` = (left, right, bottom, top, near, far) as BoxSpec (camera.rs:343-368);
+    attitude = position, forward, right, up (CameraAttitudeSpec, camera.rs:652-700).
+    view_matrix_inv is the inverse of rotation * translation(-position) (camera.rs:809-834),
+    computed in float64 and rounded to float32.
+    """
+
+    def __init__(self, box_spec, position, forward, right, up):
+        left, rgt, bottom, top, near, _far = [np.float32(x) for x in box_spec]
+        ext_x = rgt - left
+        ext_y = top - bottom
+        self.top_left = np.array([left, top, -near], np.float32)
+        self.top_right = np.array([left + ext_x, top, -near], np.float32)
+        self.bottom_left = np.array([left, top - ext_y, -near], np.float32)
+        r = np.asarray(right, np.float64)
+        u = np.asarray(up, np.float64)
+        f = np.asarray(forward, np.float64)
+        p = np.asarray(position, np.float64)
+        rot = np.eye(4)
+        rot[0, :3], rot[1, :3], rot[2, :3] = r, u, -f     # rows: right, up, -forward
+        trans = np.eye(4)
+        trans[:3, 3] = -p
+        view = rot @ trans
+        inv = np.linalg.inv(view)
+        self.view_inv = np.ascontiguousarray(inv.T.astype(np.float32)).reshape(16)  # column-major
+
+    @staticmethod
+    def symmetric_fov(fovy_deg, aspect, near, far, position, forward, right, up) -> "Camera":
+        """SymmetricFovSpec -> frustum (camera.rs:219-252)."""
+        top = np.float32(near) * np.float32(np.tan(np.radians(fovy_deg) / 2.0))
+        right_x = np.float32(aspect) * top
+        return Camera((-right_x, right_x, -top, top, near, far), position, forward, right, up)
+
+    def corners(self) -> np.ndarray:
+        return np.concatenate([self.top_left, self.top_right, self.bottom_left]).astype(np.float32)
+
+    def to_struct(self) -> np.ndarray:
+        s = np.zeros(1, CAMERA)
+        s["top_left"] = self.top_left
+        s["top_right"] = self.top_right
+        s["bottom_left"] = self.bottom_left
+        s["view_inv"] = self.view_inv
+        return s
+
+
+__all__ = ["Context", "DeviceBuffer", "PinnedArray", "Event", "Bvh", "BvhBuilder", "Blas", "Scene", "Camera",
+           "RAY", "HIT", "NODE", "TLAS_NODE", "BATCH_ITEM", "MISS", "FLT_MAX"]

@@ -1,0 +1,813 @@
+// C ABI of the bvhgpu library (include/bvhgpu.h): context, memory helpers, timing, BLAS and
+// scene management, and the trace / refit / rebuild / render entry points.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "common.cuh"
+#include "internal.hpp"
+
+namespace bvhgpu {
+
+std::atomic<uint64_t> g_launches{0};
+
+LaunchScope::LaunchScope(bvhgpu_ctx* c, int k, cudaStream_t st) : ctx(c), kernel(k), s(st) {
+    if (!ctx->profiling) return;
+    if (ctx->event_pool.size() >= 2) {
+        e1 = ctx->event_pool.back();
+        ctx->event_pool.pop_back();
+        e0 = ctx->event_pool.back();
+        ctx->event_pool.pop_back();
+    } else {
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+    }
+    cudaEventRecord(e0, s);
+}
+
+LaunchScope::~LaunchScope() {
+    if (!e0) return;
+    cudaEventRecord(e1, s);
+    ctx->prof.push_back(ProfileRec{kernel, e0, e1});
+}
+
+}  // namespace bvhgpu
+
+using namespace bvhgpu;
+
+namespace {
+
+static_assert(sizeof(bvhgpu_node) == 32, "bvhgpu_node layout");
+static_assert(sizeof(bvhgpu_triangle) == 36, "bvhgpu_triangle layout");
+static_assert(sizeof(bvhgpu_ray) == 32, "bvhgpu_ray layout");
+static_assert(sizeof(bvhgpu_hit) == 20, "bvhgpu_hit layout");
+static_assert(sizeof(bvhgpu_tlas_node) == 32, "bvhgpu_tlas_node layout");
+static_assert(sizeof(bvhgpu_batch_item) == 16, "bvhgpu_batch_item layout");
+
+int fail(bvhgpu_ctx* ctx, int code, const char* fmt, ...) {
+    if (ctx) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof(buf), fmt, ap);
+        va_end(ap);
+        ctx->last_error = buf;
+    }
+    return code;
+}
+
+int cuda_fail(bvhgpu_ctx* ctx, cudaError_t e, const char* what) {
+    return fail(ctx, BVHGPU_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CK(expr, what)                                    \
+    do {                                                  \
+        cudaError_t _e = (expr);                          \
+        if (_e != cudaSuccess) return cuda_fail(ctx, _e, what); \
+    } while (0)
+
+cudaStream_t pick(bvhgpu_ctx* ctx, bvhgpu_stream s) { return s ? static_cast<cudaStream_t>(s) : ctx->stream; }
+
+int ensure(bvhgpu_ctx* ctx, void** buf, size_t* cap, size_t need) {
+    if (*cap >= need) return BVHGPU_OK;
+    if (*buf) cudaFree(*buf);
+    *buf = nullptr;
+    *cap = 0;
+    size_t want = std::max<size_t>(need, 1 << 20);
+    cudaError_t e = cudaMalloc(buf, want);
+    if (e != cudaSuccess) return fail(ctx, BVHGPU_ERR_OUT_OF_MEMORY, "cudaMalloc(%zu): %s", want, cudaGetErrorString(e));
+    *cap = want;
+    return BVHGPU_OK;
+}
+
+int read_errors(bvhgpu_ctx* ctx) {
+    uint32_t flags = 0;
+    CK(cudaMemcpy(&flags, ctx->d_err, sizeof(flags), cudaMemcpyDeviceToHost), "read error flags");
+    if (flags) {
+        CK(cudaMemset(ctx->d_err, 0, sizeof(uint32_t)), "reset error flags");
+        if (flags & kErrStack) return fail(ctx, BVHGPU_ERR_STACK_DEPTH, "traversal stack overflow (tree too deep)");
+        return fail(ctx, BVHGPU_ERR_STEP_CAP, "traversal step cap exceeded (malformed tree)");
+    }
+    return BVHGPU_OK;
+}
+
+int finish(bvhgpu_ctx* ctx) {
+    CK(cudaStreamSynchronize(ctx->stream), "stream synchronize");
+    return read_errors(ctx);
+}
+
+DeviceBlas* find_blas(bvhgpu_ctx* ctx, uint32_t id) {
+    auto it = ctx->blas.find(id);
+    return it == ctx->blas.end() ? nullptr : &it->second;
+}
+DeviceScene* find_scene(bvhgpu_ctx* ctx, uint32_t id) {
+    auto it = ctx->scenes.find(id);
+    return it == ctx->scenes.end() ? nullptr : &it->second;
+}
+
+void free_blas(DeviceBlas& b) {
+    cudaFree(b.nodes);
+    cudaFree(b.tris);
+    cudaFree(b.parent);
+    cudaFree(b.leaves);
+    cudaFree(b.counters);
+    b = DeviceBlas();
+}
+
+void free_scene(DeviceScene& s) {
+    cudaFree(s.xf);
+    cudaFree(s.inv);
+    cudaFree(s.obj_blas);
+    cudaFree(s.blas_table);
+    cudaFree(s.tlas);
+    s = DeviceScene();
+}
+
+// Validates a reference node array and derives parent links, leaf list and depth.
+int analyse_nodes(bvhgpu_ctx* ctx, const bvhgpu_node* nodes, uint32_t nodes_used, uint32_t ntris,
+                  std::vector<uint32_t>& parent, std::vector<uint32_t>& leaves, uint32_t* depth) {
+    parent.assign(nodes_used, 0xFFFFFFFFu);
+    leaves.clear();
+    std::vector<uint32_t> seen(nodes_used, 0);
+    std::vector<std::pair<uint32_t, uint32_t>> st;
+    st.push_back({0u, 1u});
+    seen[0] = 1;
+    uint32_t maxd = 0;
+    uint64_t covered = 0;
+    while (!st.empty()) {
+        auto [i, d] = st.back();
+        st.pop_back();
+        maxd = std::max(maxd, d);
+        const bvhgpu_node& n = nodes[i];
+        if (n.primitive_count > 0) {
+            if ((uint64_t)n.left_first + n.primitive_count > ntris)
+                return fail(ctx, BVHGPU_ERR_INVALID_ARG, "leaf %u addresses triangles past %u", i, ntris);
+            leaves.push_back(i);
+            covered += n.primitive_count;
+        } else {
+            uint32_t l = n.left_first;
+            if (l < 2 || (uint64_t)l + 1 >= nodes_used || l <= i)
+                return fail(ctx, BVHGPU_ERR_INVALID_ARG, "branch %u has bad child index %u", i, l);
+            if (seen[l] || seen[l + 1]) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "node %u reached twice", l);
+            seen[l] = seen[l + 1] = 1;
+            parent[l] = i;
+            parent[l + 1] = i;
+            st.push_back({l, d + 1});
+            st.push_back({l + 1, d + 1});
+        }
+    }
+    (void)covered;
+    *depth = maxd;
+    return BVHGPU_OK;
+}
+
+void pack_nodes(const bvhgpu_node* nodes, uint32_t n, std::vector<float>& out) {
+    out.resize(8ull * n);
+    for (uint32_t i = 0; i < n; ++i) {
+        float* o = &out[8ull * i];
+        o[0] = nodes[i].bounds_min[0];
+        o[1] = nodes[i].bounds_min[1];
+        o[2] = nodes[i].bounds_min[2];
+        std::memcpy(&o[3], &nodes[i].left_first, 4);
+        o[4] = nodes[i].bounds_max[0];
+        o[5] = nodes[i].bounds_max[1];
+        o[6] = nodes[i].bounds_max[2];
+        std::memcpy(&o[7], &nodes[i].primitive_count, 4);
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int bvhgpu_create(bvhgpu_ctx** out, int device) {
+    if (!out) return BVHGPU_ERR_INVALID_ARG;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return BVHGPU_ERR_NO_DEVICE;
+    if (device < 0 || device >= ndev) return BVHGPU_ERR_INVALID_ARG;
+    if (cudaSetDevice(device) != cudaSuccess) return BVHGPU_ERR_CUDA;
+    bvhgpu_ctx* ctx = new bvhgpu_ctx();
+    ctx->device = device;
+    cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMalloc(&ctx->d_err, sizeof(uint32_t)) != cudaSuccess ||
+        cudaMalloc(&ctx->d_scratch, 64 * sizeof(uint32_t)) != cudaSuccess) {
+        delete ctx;
+        return BVHGPU_ERR_CUDA;
+    }
+    cudaMemset(ctx->d_err, 0, sizeof(uint32_t));
+    cudaMemset(ctx->d_scratch, 0, 64 * sizeof(uint32_t));
+    cudaDeviceSynchronize();
+    *out = ctx;
+    return BVHGPU_OK;
+}
+
+int bvhgpu_destroy(bvhgpu_ctx* ctx) {
+    if (!ctx) return BVHGPU_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    for (auto& kv : ctx->blas) free_blas(kv.second);
+    for (auto& kv : ctx->scenes) free_scene(kv.second);
+    for (auto& r : ctx->prof) {
+        cudaEventDestroy(r.start);
+        cudaEventDestroy(r.stop);
+    }
+    for (auto e : ctx->event_pool) cudaEventDestroy(e);
+    cudaFree(ctx->d_err);
+    cudaFree(ctx->d_scratch);
+    cudaFree(ctx->l2_flush);
+    cudaFree(ctx->stage_in);
+    cudaFree(ctx->stage_out);
+    cudaFree(ctx->stage_out2);
+    cudaFree(ctx->bounce_rays);
+    cudaFree(ctx->bounce_pix);
+    cudaFree(ctx->batch_table);
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return BVHGPU_OK;
+}
+
+const char* bvhgpu_last_error(const bvhgpu_ctx* ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }
+
+uint64_t bvhgpu_launch_count(void) { return g_launches.load(); }
+
+int bvhgpu_sync(bvhgpu_ctx* ctx) {
+    if (!ctx) return BVHGPU_ERR_INVALID_ARG;
+    return finish(ctx);
+}
+
+bvhgpu_stream bvhgpu_get_stream(bvhgpu_ctx* ctx) { return ctx ? ctx->stream : nullptr; }
+
+// ---- memory helpers -------------------------------------------------------------------------
+
+int bvhgpu_device_alloc(bvhgpu_ctx* ctx, size_t bytes, void** out) {
+    if (!ctx || !out) return BVHGPU_ERR_INVALID_ARG;
+    cudaError_t e = cudaMalloc(out, std::max<size_t>(bytes, 16));
+    if (e != cudaSuccess) return fail(ctx, BVHGPU_ERR_OUT_OF_MEMORY, "cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e));
+    return BVHGPU_OK;
+}
+int bvhgpu_device_free(bvhgpu_ctx* ctx, void* p) {
+    if (!ctx) return BVHGPU_ERR_INVALID_ARG;
+    CK(cudaFree(p), "cudaFree");
+    return BVHGPU_OK;
+}
+int bvhgpu_host_alloc(bvhgpu_ctx* ctx, size_t bytes, void** out) {
+    if (!ctx || !out) return BVHGPU_ERR_INVALID_ARG;
+    cudaError_t e = cudaMallocHost(out, std::max<size_t>(bytes, 16));
+    if (e != cudaSuccess) return fail(ctx, BVHGPU_ERR_OUT_OF_MEMORY, "cudaMallocHost(%zu): %s", bytes, cudaGetErrorString(e));
+    return BVHGPU_OK;
+}
+int bvhgpu_host_free(bvhgpu_ctx* ctx, void* p) {
+    if (!ctx) return BVHGPU_ERR_INVALID_ARG;
+    CK(cudaFreeHost(p), "cudaFreeHost");
+    return BVHGPU_OK;
+}
+int bvhgpu_copy_to_device(bvhgpu_ctx* ctx, void* dst, const void* src, size_t bytes, bvhgpu_stream s) {
+    if (!ctx || (bytes && (!dst || !src))) return BVHGPU_ERR_INVALID_ARG;
+    CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, pick(ctx, s)), "copy to device");
+    return BVHGPU_OK;
+}
+int bvhgpu_copy_to_host(bvhgpu_ctx* ctx, void* dst, const void* src, size_t bytes, bvhgpu_stream s) {
+    if (!ctx || (bytes && (!dst || !src))) return BVHGPU_ERR_INVALID_ARG;
+    CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, pick(ctx, s)), "copy to host");
+    return BVHGPU_OK;
+}
+int bvhgpu_memset_device(bvhgpu_ctx* ctx, void* dst, int value, size_t bytes, bvhgpu_stream s) {
+    if (!ctx || (bytes && !dst)) return BVHGPU_ERR_INVALID_ARG;
+    CK(cudaMemsetAsync(dst, value, bytes, pick(ctx, s)), "memset");
+    return BVHGPU_OK;
+}
+int bvhgpu_flush_l2(bvhgpu_ctx* ctx, bvhgpu_stream s) {
+    if (!ctx) return BVHGPU_ERR_INVALID_ARG;
+    if (!ctx->l2_flush) {
+        int l2 = 0;
+        cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, ctx->device);
+        ctx->l2_flush_bytes = std::max<size_t>((size_t)l2 * 2, 256ull << 20);
+        CK(cudaMalloc(&ctx->l2_flush, ctx->l2_flush_bytes), "alloc L2 flush buffer");
+    }
+    static int flip = 0;
+    flip ^= 1;
+    CK(cudaMemsetAsync(ctx->l2_flush, flip, ctx->l2_flush_bytes, pick(ctx, s)), "L2 flush");
+    return BVHGPU_OK;
+}
+
+// ---- timing -------------------------------------------------------------------------------------
+
+int bvhgpu_event_create(bvhgpu_ctx* ctx, void** ev) {
+    if (!ctx || !ev) return BVHGPU_ERR_INVALID_ARG;
+    cudaEvent_t e;
+    CK(cudaEventCreate(&e), "event create");
+    *ev = e;
+    return BVHGPU_OK;
+}
+int bvhgpu_event_destroy(bvhgpu_ctx* ctx, void* ev) {
+    if (!ctx || !ev) return BVHGPU_ERR_INVALID_ARG;
+    CK(cudaEventDestroy(static_cast<cudaEvent_t>(ev)), "event destroy");
+    return BVHGPU_OK;
+}
+int bvhgpu_event_record(bvhgpu_ctx* ctx, void* ev, bvhgpu_stream s) {
+    if (!ctx || !ev) return BVHGPU_ERR_INVALID_ARG;
+    CK(cudaEventRecord(static_cast<cudaEvent_t>(ev), pick(ctx, s)), "event record");
+    return BVHGPU_OK;
+}
+int bvhgpu_event_elapsed_ms(bvhgpu_ctx* ctx, void* start, void* stop, float* ms) {
+    if (!ctx || !start || !stop || !ms) return BVHGPU_ERR_INVALID_ARG;
+    CK(cudaEventSynchronize(static_cast<cudaEvent_t>(stop)), "event synchronize");
+    CK(cudaEventElapsedTime(ms, static_cast<cudaEvent_t>(start), static_cast<cudaEvent_t>(stop)), "event elapsed");
+    return BVHGPU_OK;
+}
+int bvhgpu_profile_enable(bvhgpu_ctx* ctx, int enable) {
+    if (!ctx) return BVHGPU_ERR_INVALID_ARG;
+    ctx->profiling = enable != 0;
+    return BVHGPU_OK;
+}
+int bvhgpu_profile_read(bvhgpu_ctx* ctx, double* ms, uint64_t* launches) {
+    if (!ctx) return BVHGPU_ERR_INVALID_ARG;
+    for (int k = 0; k < BVHGPU_KERNEL_COUNT; ++k) {
+        if (ms) ms[k] = 0.0;
+        if (launches) launches[k] = 0;
+    }
+    for (auto& r : ctx->prof) {
+        CK(cudaEventSynchronize(r.stop), "event synchronize");
+        float t = 0.0f;
+        CK(cudaEventElapsedTime(&t, r.start, r.stop), "event elapsed");
+        if (ms) ms[r.kernel] += t;
+        if (launches) launches[r.kernel] += 1;
+        ctx->event_pool.push_back(r.start);
+        ctx->event_pool.push_back(r.stop);
+    }
+    ctx->prof.clear();
+    return BVHGPU_OK;
+}
+
+// ---- BLAS -------------------------------------------------------------------------------------
+
+int bvhgpu_build_bvh_host(bvhgpu_triangle* mesh, uint32_t n, bvhgpu_node* nodes_out, uint32_t* nodes_used) {
+    return build_bvh_host(mesh, n, nodes_out, nodes_used);
+}
+
+int bvhgpu_blas_upload(bvhgpu_ctx* ctx, const bvhgpu_node* nodes, uint32_t nodes_used, const bvhgpu_triangle* tris,
+                       uint32_t ntris, uint32_t* blas_id) {
+    if (!ctx || !nodes || !tris || !blas_id || nodes_used < 1 || ntris == 0)
+        return fail(ctx, BVHGPU_ERR_INVALID_ARG, "blas_upload: null pointer or empty mesh");
+    std::vector<uint32_t> parent, leaves;
+    uint32_t depth = 0;
+    int rc = analyse_nodes(ctx, nodes, nodes_used, ntris, parent, leaves, &depth);
+    if (rc) return rc;
+    DeviceBlas b;
+    b.nodes_used = nodes_used;
+    b.ntris = ntris;
+    b.nleaves = (uint32_t)leaves.size();
+    b.depth = depth;
+    b.root_count = nodes[0].primitive_count;
+    b.root_first = nodes[0].left_first;
+    std::vector<float> packed;
+    pack_nodes(nodes, nodes_used, packed);
+    void* d_tris9 = nullptr;
+    cudaError_t e = cudaSuccess;
+    auto cleanup = [&]() {
+        cudaFree(d_tris9);
+        free_blas(b);
+    };
+    if ((e = cudaMalloc(&b.nodes, 32ull * nodes_used)) != cudaSuccess ||
+        (e = cudaMalloc(&b.tris, 48ull * ntris)) != cudaSuccess ||
+        (e = cudaMalloc(&b.parent, 4ull * nodes_used)) != cudaSuccess ||
+        (e = cudaMalloc(&b.leaves, 4ull * std::max<size_t>(1, leaves.size()))) != cudaSuccess ||
+        (e = cudaMalloc(&b.counters, 4ull * nodes_used)) != cudaSuccess ||
+        (e = cudaMalloc(&d_tris9, 36ull * ntris)) != cudaSuccess) {
+        cleanup();
+        return fail(ctx, BVHGPU_ERR_OUT_OF_MEMORY, "blas_upload: %s", cudaGetErrorString(e));
+    }
+    if ((e = cudaMemcpy(b.nodes, packed.data(), 32ull * nodes_used, cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(b.parent, parent.data(), 4ull * nodes_used, cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(b.leaves, leaves.data(), 4ull * leaves.size(), cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemset(b.counters, 0, 4ull * nodes_used)) != cudaSuccess ||
+        (e = cudaMemcpy(d_tris9, tris, 36ull * ntris, cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = launch_write_tris(ctx, b, static_cast<const float*>(d_tris9), ctx->stream)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess) {
+        cleanup();
+        return cuda_fail(ctx, e, "blas_upload");
+    }
+    cudaFree(d_tris9);
+    uint32_t id = ctx->next_blas++;
+    ctx->blas[id] = b;
+    *blas_id = id;
+    return BVHGPU_OK;
+}
+
+int bvhgpu_blas_free(bvhgpu_ctx* ctx, uint32_t blas_id) {
+    if (!ctx) return BVHGPU_ERR_INVALID_ARG;
+    DeviceBlas* b = find_blas(ctx, blas_id);
+    if (!b) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown BLAS %u", blas_id);
+    cudaStreamSynchronize(ctx->stream);
+    free_blas(*b);
+    ctx->blas.erase(blas_id);
+    return BVHGPU_OK;
+}
+
+int bvhgpu_blas_info(bvhgpu_ctx* ctx, uint32_t blas_id, uint32_t* nodes_used, uint32_t* ntris, uint32_t* depth) {
+    if (!ctx) return BVHGPU_ERR_INVALID_ARG;
+    DeviceBlas* b = find_blas(ctx, blas_id);
+    if (!b) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown BLAS %u", blas_id);
+    if (nodes_used) *nodes_used = b->nodes_used;
+    if (ntris) *ntris = b->ntris;
+    if (depth) *depth = b->depth;
+    return BVHGPU_OK;
+}
+
+int bvhgpu_blas_update_vertices_async(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhgpu_triangle* d_tris,
+                                      bvhgpu_stream s) {
+    if (!ctx || !d_tris) return BVHGPU_ERR_INVALID_ARG;
+    DeviceBlas* b = find_blas(ctx, blas_id);
+    if (!b) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown BLAS %u", blas_id);
+    CK(launch_write_tris(ctx, *b, reinterpret_cast<const float*>(d_tris), pick(ctx, s)), "write triangles");
+    return BVHGPU_OK;
+}
+
+int bvhgpu_blas_update_vertices(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhgpu_triangle* tris) {
+    if (!ctx || !tris) return BVHGPU_ERR_INVALID_ARG;
+    DeviceBlas* b = find_blas(ctx, blas_id);
+    if (!b) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown BLAS %u", blas_id);
+    int rc = ensure(ctx, &ctx->stage_in, &ctx->stage_in_bytes, 36ull * b->ntris);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(ctx->stage_in, tris, 36ull * b->ntris, cudaMemcpyHostToDevice, ctx->stream), "upload vertices");
+    CK(launch_write_tris(ctx, *b, static_cast<const float*>(ctx->stage_in), ctx->stream), "write triangles");
+    return finish(ctx);
+}
+
+int bvhgpu_blas_refit_async(bvhgpu_ctx* ctx, uint32_t blas_id, bvhgpu_stream s) {
+    if (!ctx) return BVHGPU_ERR_INVALID_ARG;
+    DeviceBlas* b = find_blas(ctx, blas_id);
+    if (!b) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown BLAS %u", blas_id);
+    CK(launch_refit(ctx, *b, pick(ctx, s)), "refit");
+    return BVHGPU_OK;
+}
+
+int bvhgpu_blas_refit(bvhgpu_ctx* ctx, uint32_t blas_id) {
+    int rc = bvhgpu_blas_refit_async(ctx, blas_id, nullptr);
+    if (rc) return rc;
+    return finish(ctx);
+}
+
+int bvhgpu_blas_download_nodes(bvhgpu_ctx* ctx, uint32_t blas_id, bvhgpu_node* nodes) {
+    if (!ctx || !nodes) return BVHGPU_ERR_INVALID_ARG;
+    DeviceBlas* b = find_blas(ctx, blas_id);
+    if (!b) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown BLAS %u", blas_id);
+    std::vector<float> packed(8ull * b->nodes_used);
+    CK(cudaStreamSynchronize(ctx->stream), "stream synchronize");
+    CK(cudaMemcpy(packed.data(), b->nodes, 32ull * b->nodes_used, cudaMemcpyDeviceToHost), "download nodes");
+    for (uint32_t i = 0; i < b->nodes_used; ++i) {
+        const float* o = &packed[8ull * i];
+        nodes[i].bounds_min[0] = o[0];
+        nodes[i].bounds_min[1] = o[1];
+        nodes[i].bounds_min[2] = o[2];
+        std::memcpy(&nodes[i].left_first, &o[3], 4);
+        nodes[i].bounds_max[0] = o[4];
+        nodes[i].bounds_max[1] = o[5];
+        nodes[i].bounds_max[2] = o[6];
+        std::memcpy(&nodes[i].primitive_count, &o[7], 4);
+    }
+    return BVHGPU_OK;
+}
+
+int bvhgpu_blas_intersect_async(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhgpu_ray* d_rays, uint32_t n,
+                                bvhgpu_hit* d_hits, bvhgpu_stream s) {
+    if (!ctx || (n && (!d_rays || !d_hits))) return BVHGPU_ERR_INVALID_ARG;
+    DeviceBlas* b = find_blas(ctx, blas_id);
+    if (!b) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown BLAS %u", blas_id);
+    CK(launch_trace_blas(ctx, *b, reinterpret_cast<const float4*>(d_rays), n, d_hits, pick(ctx, s)), "trace");
+    return BVHGPU_OK;
+}
+
+int bvhgpu_blas_intersect(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhgpu_ray* rays, uint32_t n, bvhgpu_hit* hits) {
+    if (!ctx || (n && (!rays || !hits))) return BVHGPU_ERR_INVALID_ARG;
+    DeviceBlas* b = find_blas(ctx, blas_id);
+    if (!b) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown BLAS %u", blas_id);
+    if (n == 0) return BVHGPU_OK;
+    int rc = ensure(ctx, &ctx->stage_in, &ctx->stage_in_bytes, 32ull * n);
+    if (!rc) rc = ensure(ctx, &ctx->stage_out, &ctx->stage_out_bytes, 20ull * n);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(ctx->stage_in, rays, 32ull * n, cudaMemcpyHostToDevice, ctx->stream), "upload rays");
+    CK(launch_trace_blas(ctx, *b, static_cast<const float4*>(ctx->stage_in), n, ctx->stage_out, ctx->stream), "trace");
+    CK(cudaMemcpyAsync(hits, ctx->stage_out, 20ull * n, cudaMemcpyDeviceToHost, ctx->stream), "download hits");
+    return finish(ctx);
+}
+
+static int ensure_bounce(bvhgpu_ctx* ctx, uint32_t n) {
+    if (ctx->bounce_cap >= n) return BVHGPU_OK;
+    cudaFree(ctx->bounce_rays);
+    cudaFree(ctx->bounce_pix);
+    ctx->bounce_rays = nullptr;
+    ctx->bounce_pix = nullptr;
+    ctx->bounce_cap = 0;
+    if (cudaMalloc(&ctx->bounce_rays, 32ull * n) != cudaSuccess ||
+        cudaMalloc(&ctx->bounce_pix, 4ull * n) != cudaSuccess)
+        return fail(ctx, BVHGPU_ERR_OUT_OF_MEMORY, "bounce queue of %u rays", n);
+    ctx->bounce_cap = n;
+    return BVHGPU_OK;
+}
+
+int bvhgpu_blas_trace_bounce_async(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhgpu_ray* d_rays, uint32_t n,
+                                   uint32_t seed, int mode, bvhgpu_hit* d_hits0, bvhgpu_hit* d_hits1,
+                                   bvhgpu_stream s) {
+    if (!ctx || (n && (!d_rays || !d_hits0 || !d_hits1))) return BVHGPU_ERR_INVALID_ARG;
+    DeviceBlas* b = find_blas(ctx, blas_id);
+    if (!b) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown BLAS %u", blas_id);
+    const float4* r = reinterpret_cast<const float4*>(d_rays);
+    if (mode == BVHGPU_MODE_PLAIN) {
+        int rc = ensure_bounce(ctx, n);
+        if (rc) return rc;
+        CK(launch_bounce_plain(ctx, *b, r, n, seed, d_hits0, d_hits1, pick(ctx, s)), "bounce (plain)");
+    } else if (mode == BVHGPU_MODE_PERSISTENT) {
+        CK(launch_bounce_persistent(ctx, *b, r, n, seed, d_hits0, d_hits1, pick(ctx, s)), "bounce (persistent)");
+    } else {
+        return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown mode %d", mode);
+    }
+    return BVHGPU_OK;
+}
+
+int bvhgpu_blas_trace_bounce(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhgpu_ray* rays, uint32_t n, uint32_t seed,
+                             int mode, bvhgpu_hit* hits0, bvhgpu_hit* hits1, uint32_t* n_bounce) {
+    if (!ctx || (n && (!rays || !hits0 || !hits1))) return BVHGPU_ERR_INVALID_ARG;
+    if (n == 0) {
+        if (n_bounce) *n_bounce = 0;
+        return BVHGPU_OK;
+    }
+    int rc = ensure(ctx, &ctx->stage_in, &ctx->stage_in_bytes, 32ull * n);
+    if (!rc) rc = ensure(ctx, &ctx->stage_out, &ctx->stage_out_bytes, 20ull * n);
+    if (!rc) rc = ensure(ctx, &ctx->stage_out2, &ctx->stage_out2_bytes, 20ull * n);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(ctx->stage_in, rays, 32ull * n, cudaMemcpyHostToDevice, ctx->stream), "upload rays");
+    rc = bvhgpu_blas_trace_bounce_async(ctx, blas_id, static_cast<const bvhgpu_ray*>(ctx->stage_in), n, seed, mode,
+                                        static_cast<bvhgpu_hit*>(ctx->stage_out),
+                                        static_cast<bvhgpu_hit*>(ctx->stage_out2), nullptr);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(hits0, ctx->stage_out, 20ull * n, cudaMemcpyDeviceToHost, ctx->stream), "download hits");
+    CK(cudaMemcpyAsync(hits1, ctx->stage_out2, 20ull * n, cudaMemcpyDeviceToHost, ctx->stream), "download hits");
+    rc = finish(ctx);
+    if (rc) return rc;
+    if (n_bounce) {
+        uint32_t c = 0;
+        for (uint32_t i = 0; i < n; ++i) c += hits0[i].prim != BVHGPU_MISS;
+        *n_bounce = c;
+    }
+    return BVHGPU_OK;
+}
+
+int bvhgpu_blas_bounce_rays(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhgpu_ray* rays, uint32_t n, uint32_t seed,
+                            bvhgpu_ray* out, uint8_t* valid) {
+    if (!ctx || (n && (!rays || !out || !valid))) return BVHGPU_ERR_INVALID_ARG;
+    DeviceBlas* b = find_blas(ctx, blas_id);
+    if (!b) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown BLAS %u", blas_id);
+    if (n == 0) return BVHGPU_OK;
+    void *d_rays = nullptr, *d_hits = nullptr, *d_out = nullptr, *d_valid = nullptr;
+    auto done = [&]() {
+        cudaFree(d_rays);
+        cudaFree(d_hits);
+        cudaFree(d_out);
+        cudaFree(d_valid);
+    };
+    if (cudaMalloc(&d_rays, 32ull * n) != cudaSuccess || cudaMalloc(&d_hits, 20ull * n) != cudaSuccess ||
+        cudaMalloc(&d_out, 32ull * n) != cudaSuccess || cudaMalloc(&d_valid, n) != cudaSuccess) {
+        done();
+        return fail(ctx, BVHGPU_ERR_OUT_OF_MEMORY, "bounce_rays buffers");
+    }
+    cudaError_t e;
+    if ((e = cudaMemcpyAsync(d_rays, rays, 32ull * n, cudaMemcpyHostToDevice, ctx->stream)) != cudaSuccess ||
+        (e = launch_trace_blas(ctx, *b, static_cast<const float4*>(d_rays), n, d_hits, ctx->stream)) != cudaSuccess ||
+        (e = launch_bounce_rays(ctx, *b, static_cast<const float4*>(d_rays), d_hits, n, seed,
+                                static_cast<float4*>(d_out), static_cast<uint8_t*>(d_valid), ctx->stream)) !=
+            cudaSuccess ||
+        (e = cudaMemcpyAsync(out, d_out, 32ull * n, cudaMemcpyDeviceToHost, ctx->stream)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(valid, d_valid, n, cudaMemcpyDeviceToHost, ctx->stream)) != cudaSuccess) {
+        done();
+        return cuda_fail(ctx, e, "bounce_rays");
+    }
+    int rc = finish(ctx);
+    done();
+    return rc;
+}
+
+int bvhgpu_trace_batch_async(bvhgpu_ctx* ctx, const bvhgpu_batch_item* items, uint32_t nitems,
+                             const bvhgpu_ray* d_rays, uint32_t nrays, int mode, bvhgpu_hit* d_hits, bvhgpu_stream s) {
+    if (!ctx || (nitems && (!items || !d_rays || !d_hits))) return BVHGPU_ERR_INVALID_ARG;
+    if (mode != BVHGPU_MODE_PLAIN && mode != BVHGPU_MODE_PERSISTENT)
+        return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown mode %d", mode);
+    std::vector<const DeviceBlas*> blases(nitems);
+    for (uint32_t i = 0; i < nitems; ++i) {
+        blases[i] = find_blas(ctx, items[i].blas);
+        if (!blases[i]) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "batch item %u: unknown BLAS %u", i, items[i].blas);
+        if ((uint64_t)items[i].ray_offset + items[i].ray_count > nrays)
+            return fail(ctx, BVHGPU_ERR_INVALID_ARG, "batch item %u: rays past %u", i, nrays);
+    }
+    CK(launch_trace_batch(ctx, blases, items, nitems, reinterpret_cast<const float4*>(d_rays), nrays, mode, d_hits,
+                          pick(ctx, s)),
+       "trace batch");
+    return BVHGPU_OK;
+}
+
+int bvhgpu_trace_batch(bvhgpu_ctx* ctx, const bvhgpu_batch_item* items, uint32_t nitems, const bvhgpu_ray* rays,
+                       uint32_t nrays, int mode, bvhgpu_hit* hits) {
+    if (!ctx || (nrays && (!rays || !hits))) return BVHGPU_ERR_INVALID_ARG;
+    if (nrays == 0) return BVHGPU_OK;
+    int rc = ensure(ctx, &ctx->stage_in, &ctx->stage_in_bytes, 32ull * nrays);
+    if (!rc) rc = ensure(ctx, &ctx->stage_out, &ctx->stage_out_bytes, 20ull * nrays);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(ctx->stage_in, rays, 32ull * nrays, cudaMemcpyHostToDevice, ctx->stream), "upload rays");
+    rc = bvhgpu_trace_batch_async(ctx, items, nitems, static_cast<const bvhgpu_ray*>(ctx->stage_in), nrays, mode,
+                                  static_cast<bvhgpu_hit*>(ctx->stage_out), nullptr);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(hits, ctx->stage_out, 20ull * nrays, cudaMemcpyDeviceToHost, ctx->stream), "download hits");
+    return finish(ctx);
+}
+
+// ---- scenes --------------------------------------------------------------------------------------
+
+int bvhgpu_scene_create(bvhgpu_ctx* ctx, const uint32_t* blas_ids, uint32_t nobjects, uint32_t* scene_id) {
+    if (!ctx || !blas_ids || !scene_id || nobjects == 0)
+        return fail(ctx, BVHGPU_ERR_INVALID_ARG, "scene_create: empty scene");
+    if (nobjects > 4096) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "scene_create: at most 4096 objects");
+    DeviceScene sc;
+    sc.nobjects = nobjects;
+    sc.blas_ids.assign(blas_ids, blas_ids + nobjects);
+    std::vector<uint32_t> obj_blas(nobjects);
+    std::vector<GBlas> table;
+    for (uint32_t i = 0; i < nobjects; ++i) {
+        DeviceBlas* b = find_blas(ctx, blas_ids[i]);
+        if (!b) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "scene_create: unknown BLAS %u", blas_ids[i]);
+        auto it = std::find(sc.table_blas.begin(), sc.table_blas.end(), blas_ids[i]);
+        if (it == sc.table_blas.end()) {
+            sc.table_blas.push_back(blas_ids[i]);
+            GBlas g;
+            g.nodes = b->nodes;
+            g.tris = b->tris;
+            g.nodes_used = b->nodes_used;
+            g.ntris = b->ntris;
+            g.root_count = b->root_count;
+            g.root_first = b->root_first;
+            table.push_back(g);
+            obj_blas[i] = (uint32_t)table.size() - 1;
+        } else {
+            obj_blas[i] = (uint32_t)(it - sc.table_blas.begin());
+        }
+    }
+    sc.nblas = (uint32_t)table.size();
+    std::vector<float> ident(16ull * nobjects, 0.0f);
+    for (uint32_t i = 0; i < nobjects; ++i)
+        for (int k = 0; k < 4; ++k) ident[16ull * i + 5 * k] = 1.0f;
+    cudaError_t e;
+    if ((e = cudaMalloc(&sc.xf, 64ull * nobjects)) != cudaSuccess ||
+        (e = cudaMalloc(&sc.inv, 64ull * nobjects)) != cudaSuccess ||
+        (e = cudaMalloc(&sc.obj_blas, 4ull * nobjects)) != cudaSuccess ||
+        (e = cudaMalloc(&sc.blas_table, sizeof(GBlas) * table.size())) != cudaSuccess ||
+        (e = cudaMalloc(&sc.tlas, 64ull * nobjects)) != cudaSuccess) {
+        free_scene(sc);
+        return fail(ctx, BVHGPU_ERR_OUT_OF_MEMORY, "scene_create: %s", cudaGetErrorString(e));
+    }
+    if ((e = cudaMemcpy(sc.xf, ident.data(), 64ull * nobjects, cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(sc.inv, ident.data(), 64ull * nobjects, cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(sc.obj_blas, obj_blas.data(), 4ull * nobjects, cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(sc.blas_table, table.data(), sizeof(GBlas) * table.size(), cudaMemcpyHostToDevice)) !=
+            cudaSuccess) {
+        free_scene(sc);
+        return cuda_fail(ctx, e, "scene_create");
+    }
+    uint32_t id = ctx->next_scene++;
+    ctx->scenes[id] = sc;
+    *scene_id = id;
+    return bvhgpu_scene_rebuild(ctx, id);
+}
+
+int bvhgpu_scene_free(bvhgpu_ctx* ctx, uint32_t scene_id) {
+    if (!ctx) return BVHGPU_ERR_INVALID_ARG;
+    DeviceScene* sc = find_scene(ctx, scene_id);
+    if (!sc) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown scene %u", scene_id);
+    cudaStreamSynchronize(ctx->stream);
+    free_scene(*sc);
+    ctx->scenes.erase(scene_id);
+    return BVHGPU_OK;
+}
+
+int bvhgpu_scene_set_transforms_async(bvhgpu_ctx* ctx, uint32_t scene_id, const float* d_xf, const float* d_inv,
+                                      bvhgpu_stream s) {
+    if (!ctx || !d_xf || !d_inv) return BVHGPU_ERR_INVALID_ARG;
+    DeviceScene* sc = find_scene(ctx, scene_id);
+    if (!sc) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown scene %u", scene_id);
+    CK(cudaMemcpyAsync(sc->xf, d_xf, 64ull * sc->nobjects, cudaMemcpyDeviceToDevice, pick(ctx, s)), "transforms");
+    CK(cudaMemcpyAsync(sc->inv, d_inv, 64ull * sc->nobjects, cudaMemcpyDeviceToDevice, pick(ctx, s)), "inverses");
+    return BVHGPU_OK;
+}
+
+int bvhgpu_scene_set_transforms(bvhgpu_ctx* ctx, uint32_t scene_id, const float* xf, const float* inv) {
+    if (!ctx || !xf || !inv) return BVHGPU_ERR_INVALID_ARG;
+    DeviceScene* sc = find_scene(ctx, scene_id);
+    if (!sc) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown scene %u", scene_id);
+    CK(cudaStreamSynchronize(ctx->stream), "stream synchronize");
+    CK(cudaMemcpy(sc->xf, xf, 64ull * sc->nobjects, cudaMemcpyHostToDevice), "transforms");
+    CK(cudaMemcpy(sc->inv, inv, 64ull * sc->nobjects, cudaMemcpyHostToDevice), "inverses");
+    return BVHGPU_OK;
+}
+
+int bvhgpu_scene_rebuild_async(bvhgpu_ctx* ctx, uint32_t scene_id, bvhgpu_stream s) {
+    if (!ctx) return BVHGPU_ERR_INVALID_ARG;
+    DeviceScene* sc = find_scene(ctx, scene_id);
+    if (!sc) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown scene %u", scene_id);
+    CK(launch_tlas_rebuild(ctx, *sc, pick(ctx, s)), "TLAS rebuild");
+    sc->tlas_nodes_used = 2 * sc->nobjects;
+    return BVHGPU_OK;
+}
+
+int bvhgpu_scene_rebuild(bvhgpu_ctx* ctx, uint32_t scene_id) {
+    int rc = bvhgpu_scene_rebuild_async(ctx, scene_id, nullptr);
+    if (rc) return rc;
+    rc = finish(ctx);
+    if (rc) return rc;
+    uint32_t status[2] = {0, 0};
+    CK(cudaMemcpy(status, ctx->d_scratch + 8, sizeof(status), cudaMemcpyDeviceToHost), "TLAS status");
+    if (status[1]) return fail(ctx, BVHGPU_ERR_BUILD, "TLAS rebuild: the reference would panic (NaN bounds)");
+    find_scene(ctx, scene_id)->tlas_nodes_used = status[0];
+    return BVHGPU_OK;
+}
+
+int bvhgpu_scene_download_tlas(bvhgpu_ctx* ctx, uint32_t scene_id, bvhgpu_tlas_node* nodes, uint32_t* nodes_used) {
+    if (!ctx || !nodes) return BVHGPU_ERR_INVALID_ARG;
+    DeviceScene* sc = find_scene(ctx, scene_id);
+    if (!sc) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown scene %u", scene_id);
+    std::vector<float> packed(16ull * sc->nobjects);
+    CK(cudaStreamSynchronize(ctx->stream), "stream synchronize");
+    CK(cudaMemcpy(packed.data(), sc->tlas, 64ull * sc->nobjects, cudaMemcpyDeviceToHost), "download TLAS");
+    for (uint32_t i = 0; i < 2 * sc->nobjects; ++i) {
+        const float* o = &packed[8ull * i];
+        for (int k = 0; k < 3; ++k) {
+            nodes[i].bounds_min[k] = o[k];
+            nodes[i].bounds_max[k] = o[4 + k];
+        }
+        std::memcpy(&nodes[i].left_right, &o[3], 4);
+        std::memcpy(&nodes[i].blas, &o[7], 4);
+    }
+    if (nodes_used) *nodes_used = sc->tlas_nodes_used;
+    return BVHGPU_OK;
+}
+
+int bvhgpu_scene_intersect_async(bvhgpu_ctx* ctx, uint32_t scene_id, const bvhgpu_ray* d_rays, uint32_t n,
+                                 bvhgpu_hit* d_hits, bvhgpu_stream s) {
+    if (!ctx || (n && (!d_rays || !d_hits))) return BVHGPU_ERR_INVALID_ARG;
+    DeviceScene* sc = find_scene(ctx, scene_id);
+    if (!sc) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown scene %u", scene_id);
+    CK(launch_trace_scene(ctx, *sc, reinterpret_cast<const float4*>(d_rays), n, d_hits, pick(ctx, s)), "trace scene");
+    return BVHGPU_OK;
+}
+
+int bvhgpu_scene_intersect(bvhgpu_ctx* ctx, uint32_t scene_id, const bvhgpu_ray* rays, uint32_t n, bvhgpu_hit* hits) {
+    if (!ctx || (n && (!rays || !hits))) return BVHGPU_ERR_INVALID_ARG;
+    if (n == 0) return BVHGPU_OK;
+    int rc = ensure(ctx, &ctx->stage_in, &ctx->stage_in_bytes, 32ull * n);
+    if (!rc) rc = ensure(ctx, &ctx->stage_out, &ctx->stage_out_bytes, 20ull * n);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(ctx->stage_in, rays, 32ull * n, cudaMemcpyHostToDevice, ctx->stream), "upload rays");
+    rc = bvhgpu_scene_intersect_async(ctx, scene_id, static_cast<const bvhgpu_ray*>(ctx->stage_in), n,
+                                      static_cast<bvhgpu_hit*>(ctx->stage_out), nullptr);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(hits, ctx->stage_out, 20ull * n, cudaMemcpyDeviceToHost, ctx->stream), "download hits");
+    return finish(ctx);
+}
+
+// ---- render -------------------------------------------------------------------------------------
+
+int bvhgpu_render(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhgpu_camera* camera, int width, int height,
+                  int accumulator, const float* acc_params, int shader, const float* shader_params,
+                  const float* normals, uint8_t* rgba, uint64_t* rays_traced) {
+    if (!ctx || !camera || !rgba || width <= 0 || height <= 0) return BVHGPU_ERR_INVALID_ARG;
+    if (accumulator < 0 || accumulator > 3 || shader < 0 || shader > 2)
+        return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown accumulator %d or shader %d", accumulator, shader);
+    if ((accumulator == BVHGPU_ACC_INTERSECTION || accumulator == BVHGPU_ACC_NORMAL) && !acc_params)
+        return fail(ctx, BVHGPU_ERR_INVALID_ARG, "accumulator needs parameters");
+    if ((shader == BVHGPU_SHADER_INTERSECTION || shader == BVHGPU_SHADER_DEPTH) && !shader_params)
+        return fail(ctx, BVHGPU_ERR_INVALID_ARG, "shader needs parameters");
+    DeviceBlas* b = find_blas(ctx, blas_id);
+    if (!b) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown BLAS %u", blas_id);
+    if (accumulator == BVHGPU_ACC_NORMAL && !normals) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "normals required");
+    size_t px = (size_t)width * height;
+    int rc = ensure(ctx, &ctx->stage_out, &ctx->stage_out_bytes, 4 * px);
+    if (!rc && normals) rc = ensure(ctx, &ctx->stage_in, &ctx->stage_in_bytes, 36ull * b->ntris);
+    if (rc) return rc;
+    if (normals)
+        CK(cudaMemcpyAsync(ctx->stage_in, normals, 36ull * b->ntris, cudaMemcpyHostToDevice, ctx->stream), "normals");
+    CK(launch_render(ctx, *b, *camera, width, height, accumulator, acc_params, shader, shader_params,
+                     normals ? static_cast<const float*>(ctx->stage_in) : nullptr,
+                     static_cast<uint8_t*>(ctx->stage_out), ctx->stream),
+       "render");
+    CK(cudaMemcpyAsync(rgba, ctx->stage_out, 4 * px, cudaMemcpyDeviceToHost, ctx->stream), "download frame");
+    rc = finish(ctx);
+    if (rc) return rc;
+    if (rays_traced) *rays_traced = px;
+    return BVHGPU_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,272 @@
+// Device-side building blocks shared by the bvhgpu kernels.
+//
+// Parity rule: every floating-point step that decides a hit follows the reference's
+// Rust operation order (BT/src/geometry/{aabb,triangle}.rs) with explicit
+// round-to-nearest intrinsics, so no multiply-add is ever fused and every division /
+// square root is the correctly rounded IEEE one.  The library is also compiled with
+// -fmad=false -prec-div=true -prec-sqrt=true -ftz=false.
+#pragma once
+
+#include <cfloat>
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+namespace bvhgpu {
+
+// Device error flags (OR-ed into the context's error word).
+constexpr uint32_t kErrStack = 1u;
+constexpr uint32_t kErrSteps = 2u;
+
+constexpr uint32_t kMiss = 0xFFFFFFFFu;
+constexpr float kThreshold = 0.0001f;  // num_traits::cast(0.0001_f64) (triangle.rs:47)
+
+// GPU node: two float4, {bmin.xyz, left_first bits}, {bmax.xyz, count bits}.  A branch's two
+// children are adjacent (right = left + 1, bvh.rs:111-113), so one child pair is 64 bytes.
+struct GBlas {
+    const float4* nodes;  // 2 float4 per node
+    const float4* tris;   // 3 float4 per triangle: {v0, 0}, {v1, 0}, {v2, 0}
+    uint32_t nodes_used;
+    uint32_t ntris;
+    uint32_t root_count;  // root node meta (node 0)
+    uint32_t root_first;
+};
+
+struct GHit {
+    float t, u, v;
+    uint32_t prim, inst;
+};
+static_assert(sizeof(GHit) == 20, "hit record layout");
+
+__device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
+
+// cglinalg Vector3::dot: (x*x' + y*y') + z*z'.
+__device__ __forceinline__ float dot3(float ax, float ay, float az, float bx, float by, float bz) {
+    return fadd(fadd(fmul(ax, bx), fmul(ay, by)), fmul(az, bz));
+}
+
+// Ray::new recomputes 1/d with an IEEE division (ray.rs:23-31).
+__device__ __forceinline__ float3 recip3(float3 d) {
+    return make_float3(__frcp_rn(d.x), __frcp_rn(d.y), __frcp_rn(d.z));
+}
+
+// Aabb::intersect (aabb.rs:65-84).  fminf/fmaxf ignore a NaN operand exactly like Rust's
+// f32::min/max; the result only feeds comparisons, so the sign of a zero is irrelevant.
+__device__ __forceinline__ bool slab(float4 lo, float4 hi, float3 o, float3 rd, float t, float& tmin_out) {
+    float tx1 = fmul(fsub(lo.x, o.x), rd.x);
+    float tx2 = fmul(fsub(hi.x, o.x), rd.x);
+    float tmin = fminf(tx1, tx2);
+    float tmax = fmaxf(tx1, tx2);
+    float ty1 = fmul(fsub(lo.y, o.y), rd.y);
+    float ty2 = fmul(fsub(hi.y, o.y), rd.y);
+    tmin = fmaxf(tmin, fminf(ty1, ty2));
+    tmax = fminf(tmax, fmaxf(ty1, ty2));
+    float tz1 = fmul(fsub(lo.z, o.z), rd.z);
+    float tz2 = fmul(fsub(hi.z, o.z), rd.z);
+    tmin = fmaxf(tmin, fminf(tz1, tz2));
+    tmax = fminf(tmax, fmaxf(tz1, tz2));
+    tmin_out = tmin;
+    return (tmax >= tmin) && (tmin < t) && (tmax > 0.0f);
+}
+
+// Triangle::intersect (triangle.rs:42-72), Moeller-Trumbore in the reference's order, but
+// evaluated without early exits (same decision, less divergence).  Returns the raw t; the
+// caller accepts it iff t < closest_t, which equals the reference's
+// `min(ray.t, t) < closest_ray.t` test because closest_ray.t never exceeds ray.t.
+__device__ __forceinline__ bool tri_test(float4 v0, float4 e1, float4 e2, float3 o, float3 d, float& t,
+                                         float& u, float& v) {
+    float nx = fsub(fmul(d.y, e2.z), fmul(d.z, e2.y));
+    float ny = fsub(fmul(d.z, e2.x), fmul(d.x, e2.z));
+    float nz = fsub(fmul(d.x, e2.y), fmul(d.y, e2.x));
+    float area = dot3(e1.x, e1.y, e1.z, nx, ny, nz);
+    float f = __frcp_rn(area);
+    float sx = fsub(o.x, v0.x);
+    float sy = fsub(o.y, v0.y);
+    float sz = fsub(o.z, v0.z);
+    u = fmul(f, dot3(sx, sy, sz, nx, ny, nz));
+    float qx = fsub(fmul(sy, e1.z), fmul(sz, e1.y));
+    float qy = fsub(fmul(sz, e1.x), fmul(sx, e1.z));
+    float qz = fsub(fmul(sx, e1.y), fmul(sy, e1.x));
+    v = fmul(f, dot3(d.x, d.y, d.z, qx, qy, qz));
+    t = fmul(f, dot3(e2.x, e2.y, e2.z, qx, qy, qz));
+    bool ok = !(fabsf(area) < kThreshold);
+    ok = ok && !(u < 0.0f || u > 1.0f);
+    ok = ok && !(v < 0.0f || fadd(u, v) > 1.0f);
+    ok = ok && (t > kThreshold);
+    return ok;
+}
+
+__device__ __forceinline__ uint32_t ubits(float f) { return __float_as_uint(f); }
+
+// Closest-hit traversal of one BLAS (bvh.rs:242-305), one node per step: DFS with the far
+// child pushed, near child = strictly smaller entry distance (ties -> right child), popped
+// nodes are not re-culled (the reference does not re-test a popped node's box), leaf
+// triangles in primitive order with a strict `<` update.  The visit order is identical to
+// the reference's, so equal-t ties resolve to the same primitive.  The stack holds the far
+// child's (count, first), so a pop needs no memory load.  Triangles are stored as three
+// float4 vertices and the edges are recomputed here exactly as triangle.rs:44-45 does.
+template <int STACK>
+struct Trav {
+    uint2 stack[STACK];
+    int sp;
+    uint32_t cnt, first, steps, max_steps;
+
+    __device__ __forceinline__ void init(const GBlas& b) {
+        sp = 0;
+        cnt = b.root_count;
+        first = b.root_first;
+        steps = 0;
+        max_steps = 2u * b.nodes_used + 16u;
+    }
+
+    __device__ __forceinline__ bool pop() {
+        if (sp == 0) return true;
+        --sp;
+        cnt = stack[sp].x;
+        first = stack[sp].y;
+        return false;
+    }
+
+    // Processes one node.  Returns true when the traversal has finished.
+    __device__ __forceinline__ bool step(const GBlas& b, float3 o, float3 d, float3 rd, float& closest_t, float& hu,
+                                         float& hv, uint32_t& hprim, bool& hit, uint32_t* err) {
+        if (++steps > max_steps) {
+            atomicOr(err, kErrSteps);
+            return true;
+        }
+        if (cnt > 0) {
+            const float4* T = b.tris + 3ull * first;
+            for (uint32_t k = 0; k < cnt; ++k) {
+                float4 a = __ldg(T + 3 * k);
+                float4 p1 = __ldg(T + 3 * k + 1);
+                float4 p2 = __ldg(T + 3 * k + 2);
+                float4 e1 = make_float4(fsub(p1.x, a.x), fsub(p1.y, a.y), fsub(p1.z, a.z), 0.0f);
+                float4 e2 = make_float4(fsub(p2.x, a.x), fsub(p2.y, a.y), fsub(p2.z, a.z), 0.0f);
+                float t, u, v;
+                if (tri_test(a, e1, e2, o, d, t, u, v) && t < closest_t) {
+                    closest_t = t;
+                    hu = u;
+                    hv = v;
+                    hprim = first + k;
+                    hit = true;
+                }
+            }
+            return pop();
+        }
+        const float4* N = b.nodes + 2ull * first;
+        float4 l0 = __ldg(N);
+        float4 l1 = __ldg(N + 1);
+        float4 r0 = __ldg(N + 2);
+        float4 r1 = __ldg(N + 3);
+        float dl, dr;
+        bool hl = slab(l0, l1, o, rd, closest_t, dl);
+        bool hr = slab(r0, r1, o, rd, closest_t, dr);
+        float kl = hl ? dl : FLT_MAX;
+        float kr = hr ? dr : FLT_MAX;
+        bool left_near = kl < kr;
+        bool near_hit = left_near ? hl : hr;
+        bool far_hit = left_near ? hr : hl;
+        if (near_hit) {
+            if (far_hit) {
+                if (sp >= STACK) {
+                    atomicOr(err, kErrStack);
+                    return true;
+                }
+                stack[sp++] = left_near ? make_uint2(ubits(r1.w), ubits(r0.w)) : make_uint2(ubits(l1.w), ubits(l0.w));
+            }
+            cnt = left_near ? ubits(l1.w) : ubits(r1.w);
+            first = left_near ? ubits(l0.w) : ubits(r0.w);
+            return false;
+        }
+        return pop();
+    }
+};
+
+template <int STACK>
+__device__ __forceinline__ bool trace_blas(const GBlas& b, float3 o, float3 d, float3 rd, float& closest_t,
+                                           float& hu, float& hv, uint32_t& hprim, uint32_t* err) {
+    Trav<STACK> tr;
+    tr.init(b);
+    bool hit = false;
+    while (!tr.step(b, o, d, rd, closest_t, hu, hv, hprim, hit, err)) {
+    }
+    return hit;
+}
+
+__device__ __forceinline__ void load_ray(const float4* rays, uint32_t i, float3& o, float3& d, float& t) {
+    float4 a = __ldg(rays + 2ull * i);
+    float4 b = __ldg(rays + 2ull * i + 1);
+    o = make_float3(a.x, a.y, a.z);
+    t = a.w;
+    d = make_float3(b.x, b.y, b.z);
+}
+
+__device__ __forceinline__ void store_hit(GHit* hits, uint32_t i, bool hit, float t, float u, float v,
+                                          uint32_t prim, uint32_t inst) {
+    GHit h;
+    if (hit) {
+        h.t = t; h.u = u; h.v = v; h.prim = prim; h.inst = inst;
+    } else {
+        h.t = FLT_MAX; h.u = 0.0f; h.v = 0.0f; h.prim = kMiss; h.inst = kMiss;
+    }
+    hits[i] = h;
+}
+
+// ---- bounce rays (not in the reference) ------------------------------------------------
+// Same definition as the CPU oracle: lowbias32 hash, Marsaglia sphere point, direction
+// normalize(n + q) around the face-forward geometric normal.  Only IEEE + - * / sqrt.
+__device__ __forceinline__ uint32_t hash32(uint32_t x) {
+    x ^= x >> 16;
+    x *= 0x7feb352du;
+    x ^= x >> 15;
+    x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return x;
+}
+__device__ __forceinline__ float rng_uniform(uint32_t key, uint32_t k) {
+    uint32_t h = hash32(key + k * 0x9E3779B9u);
+    return fmul((float)(h >> 8), 1.0f / 16777216.0f);
+}
+
+// p = o + d*t (Ray::interpolate, ray.rs:37-39); triangle given as v0, e1, e2.
+__device__ __forceinline__ bool bounce_dir(float3 o, float3 d, float t, float4 v0, float4 e1, float4 e2,
+                                           uint32_t seed, uint32_t pixel, float3& po, float3& pd) {
+    po = make_float3(fadd(o.x, fmul(d.x, t)), fadd(o.y, fmul(d.y, t)), fadd(o.z, fmul(d.z, t)));
+    float nx = fsub(fmul(e1.y, e2.z), fmul(e1.z, e2.y));
+    float ny = fsub(fmul(e1.z, e2.x), fmul(e1.x, e2.z));
+    float nz = fsub(fmul(e1.x, e2.y), fmul(e1.y, e2.x));
+    float nl = __fsqrt_rn(dot3(nx, ny, nz, nx, ny, nz));
+    if (!(nl > 0.0f) || !(nl <= FLT_MAX)) return false;
+    nx = __fdiv_rn(nx, nl);
+    ny = __fdiv_rn(ny, nl);
+    nz = __fdiv_rn(nz, nl);
+    if (dot3(nx, ny, nz, d.x, d.y, d.z) > 0.0f) {
+        nx = -nx; ny = -ny; nz = -nz;
+    }
+    uint32_t key = hash32(seed ^ hash32(pixel));
+    float qx = nx, qy = ny, qz = nz;
+    for (uint32_t k = 0; k < 32u; ++k) {
+        float x1 = fsub(fmul(2.0f, rng_uniform(key, 2u * k)), 1.0f);
+        float x2 = fsub(fmul(2.0f, rng_uniform(key, 2u * k + 1u)), 1.0f);
+        float s = fadd(fmul(x1, x1), fmul(x2, x2));
+        if (s < 1.0f && s > 0.0f) {
+            float r = __fsqrt_rn(fsub(1.0f, s));
+            qx = fmul(fmul(2.0f, x1), r);
+            qy = fmul(fmul(2.0f, x2), r);
+            qz = fsub(1.0f, fmul(2.0f, s));
+            break;
+        }
+    }
+    float dx = fadd(nx, qx), dy = fadd(ny, qy), dz = fadd(nz, qz);
+    float dl = __fsqrt_rn(dot3(dx, dy, dz, dx, dy, dz));
+    if (dl < 1e-6f) {
+        pd = make_float3(nx, ny, nz);
+    } else {
+        pd = make_float3(__fdiv_rn(dx, dl), __fdiv_rn(dy, dl), __fdiv_rn(dz, dl));
+    }
+    return true;
+}
+
+}  // namespace bvhgpu

@@ -1,0 +1,128 @@
+// Host-side internals of the bvhgpu library: the context, BLAS / scene records and the
+// kernel launchers (defined in the kernel translation units, called from api.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdint>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/bvhgpu.h"
+
+namespace bvhgpu {
+
+extern std::atomic<uint64_t> g_launches;
+
+struct DeviceBlas {
+    float4* nodes = nullptr;     // 2 float4 per node (nodes_used nodes)
+    float4* tris = nullptr;      // 3 float4 per triangle (v0, e1, e2)
+    uint32_t* parent = nullptr;  // parent index per node (refit), 0xFFFFFFFF for root/filler
+    uint32_t* leaves = nullptr;  // indices of leaf nodes (refit start points)
+    uint32_t* counters = nullptr;// refit arrival counters, one per node (kept zeroed)
+    uint32_t nodes_used = 0;
+    uint32_t ntris = 0;
+    uint32_t nleaves = 0;
+    uint32_t depth = 0;
+    uint32_t root_count = 0;
+    uint32_t root_first = 0;
+};
+
+struct DeviceScene {
+    std::vector<uint32_t> blas_ids;  // per object
+    uint32_t nobjects = 0;
+    float* xf = nullptr;       // 16 per object
+    float* inv = nullptr;      // 16 per object
+    uint32_t* obj_blas = nullptr;       // per object: index into the scene's BLAS table
+    void* blas_table = nullptr;         // GBlas per distinct BLAS used (device)
+    uint32_t nblas = 0;
+    std::vector<uint32_t> table_blas;   // context BLAS id of each table entry
+    float4* tlas = nullptr;    // 2 float4 per TLAS node (2*nobjects nodes)
+    uint32_t tlas_nodes_used = 0;
+    uint32_t tlas_depth_cap = 0;
+};
+
+struct ProfileRec {
+    int kernel;
+    cudaEvent_t start, stop;
+};
+
+}  // namespace bvhgpu
+
+struct bvhgpu_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    uint32_t* d_err = nullptr;       // device error flags
+    uint32_t* d_scratch = nullptr;   // small device scratch: queue counters etc. (64 words)
+    void* l2_flush = nullptr;
+    size_t l2_flush_bytes = 0;
+    int num_sms = 0;
+    std::string last_error;
+    std::map<uint32_t, bvhgpu::DeviceBlas> blas;
+    std::map<uint32_t, bvhgpu::DeviceScene> scenes;
+    uint32_t next_blas = 1;
+    uint32_t next_scene = 1;
+    // staging buffers for host-pointer entry points (grown on demand)
+    void* stage_in = nullptr;
+    size_t stage_in_bytes = 0;
+    void* stage_out = nullptr;
+    size_t stage_out_bytes = 0;
+    void* stage_out2 = nullptr;
+    size_t stage_out2_bytes = 0;
+    // plain-bounce work buffers
+    void* bounce_rays = nullptr;     // compacted bounce rays (2 float4 each)
+    uint32_t* bounce_pix = nullptr;  // pixel index of each compacted bounce ray
+    size_t bounce_cap = 0;
+    // persistent batch: device table of the last item list (rebuilt when the items change)
+    void* batch_table = nullptr;
+    size_t batch_table_bytes = 0;
+    std::vector<bvhgpu_batch_item> batch_items;
+    uint32_t batch_total = 0;
+    uint32_t batch_depth = 1;
+    // profiling
+    bool profiling = false;
+    std::vector<bvhgpu::ProfileRec> prof;
+    std::vector<cudaEvent_t> event_pool;
+};
+
+namespace bvhgpu {
+
+// Launch bracket for per-kernel timing.
+struct LaunchScope {
+    bvhgpu_ctx* ctx;
+    int kernel;
+    cudaStream_t s;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    LaunchScope(bvhgpu_ctx* c, int k, cudaStream_t st);
+    ~LaunchScope();
+};
+
+// ---- launchers (kernels_trace.cu) ------------------------------------------------------
+cudaError_t launch_trace_blas(bvhgpu_ctx* ctx, const DeviceBlas& b, const float4* rays, uint32_t n, void* hits,
+                              cudaStream_t s);
+cudaError_t launch_bounce_plain(bvhgpu_ctx* ctx, const DeviceBlas& b, const float4* rays, uint32_t n, uint32_t seed,
+                                void* hits0, void* hits1, cudaStream_t s);
+cudaError_t launch_bounce_persistent(bvhgpu_ctx* ctx, const DeviceBlas& b, const float4* rays, uint32_t n,
+                                     uint32_t seed, void* hits0, void* hits1, cudaStream_t s);
+cudaError_t launch_bounce_rays(bvhgpu_ctx* ctx, const DeviceBlas& b, const float4* rays, const void* hits0,
+                               uint32_t n, uint32_t seed, float4* out, uint8_t* valid, cudaStream_t s);
+cudaError_t launch_trace_batch(bvhgpu_ctx* ctx, const std::vector<const DeviceBlas*>& blases,
+                               const bvhgpu_batch_item* items, uint32_t nitems, const float4* rays, uint32_t nrays,
+                               int mode, void* hits, cudaStream_t s);
+cudaError_t launch_render(bvhgpu_ctx* ctx, const DeviceBlas& b, const bvhgpu_camera& cam, int w, int h, int acc,
+                          const float* acc_params, int shader, const float* shader_params, const float* d_normals,
+                          uint8_t* d_rgba, cudaStream_t s);
+
+// ---- launchers (kernels_scene.cu) ------------------------------------------------------
+cudaError_t launch_write_tris(bvhgpu_ctx* ctx, DeviceBlas& b, const float* d_tris9, cudaStream_t s);
+cudaError_t launch_refit(bvhgpu_ctx* ctx, DeviceBlas& b, cudaStream_t s);
+cudaError_t launch_tlas_rebuild(bvhgpu_ctx* ctx, DeviceScene& sc, cudaStream_t s);
+cudaError_t launch_trace_scene(bvhgpu_ctx* ctx, DeviceScene& sc, const float4* rays, uint32_t n, void* hits,
+                               cudaStream_t s);
+
+// ---- host SAH build (host_build.cpp) ----------------------------------------------------
+int build_bvh_host(bvhgpu_triangle* mesh, uint32_t n, bvhgpu_node* nodes_out, uint32_t* nodes_used);
+
+}  // namespace bvhgpu

@@ -1,0 +1,614 @@
+// Ray traversal kernels: plain one-thread-per-ray BLAS traversal, the primary + diffuse
+// bounce pipeline (plain and persistent), the uneven multi-scene batch (plain and
+// persistent) and the tiled render.
+//
+// Persistent kernels: each warp keeps 32 ray slots; lanes whose ray finished are refilled
+// together (ballot -> one atomicAdd per warp on a global queue -> shfl broadcast), so
+// the SMs stay busy across scenes of very different sizes and across the incoherent
+// bounce rays, and no lane idles while a neighbour finishes a long traversal.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <vector>
+
+#include "common.cuh"
+#include "internal.hpp"
+
+namespace bvhgpu {
+
+namespace {
+
+constexpr int kBlock = 128;
+constexpr unsigned kFull = 0xFFFFFFFFu;
+
+inline GBlas to_gblas(const DeviceBlas& b) {
+    GBlas g;
+    g.nodes = b.nodes;
+    g.tris = b.tris;
+    g.nodes_used = b.nodes_used;
+    g.ntris = b.ntris;
+    g.root_count = b.root_count;
+    g.root_first = b.root_first;
+    return g;
+}
+
+// Smallest compiled stack that holds `depth - 1` pending far children.
+inline int stack_variant(uint32_t depth) {
+    if (depth <= 33) return 32;
+    if (depth <= 65) return 64;
+    if (depth <= 129) return 128;
+    return 256;
+}
+
+inline unsigned grid_for(uint32_t n, int block) { return (unsigned)((n + block - 1) / block); }
+
+// ---- plain -------------------------------------------------------------------------------
+
+template <int STACK>
+__global__ void __launch_bounds__(kBlock) k_trace_blas(GBlas b, const float4* __restrict__ rays, uint32_t n,
+                                                       GHit* __restrict__ hits, uint32_t* err) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float3 o, d;
+    float t;
+    load_ray(rays, i, o, d, t);
+    float3 rd = recip3(d);
+    float hu = 0.0f, hv = 0.0f;
+    uint32_t hp = 0;
+    bool hit = trace_blas<STACK>(b, o, d, rd, t, hu, hv, hp, err);
+    // bvh.rs:295: a hit needs closest_ray.t < f32::MAX as well.
+    store_hit(hits, i, hit && t < FLT_MAX, t, hu, hv, hp, 0u);
+}
+
+// Bounce generation with warp-aggregated compaction: one atomicAdd per warp appends the
+// warp's bounce rays to a dense queue (slot order is irrelevant: results go to pixels).
+__global__ void __launch_bounds__(kBlock) k_bounce_gen(GBlas b, const float4* __restrict__ rays,
+                                                       const GHit* __restrict__ hits0, uint32_t n, uint32_t seed,
+                                                       float4* __restrict__ queue_rays, uint32_t* __restrict__ queue_pix,
+                                                       uint32_t* queue_count, GHit* __restrict__ hits1) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    bool have = false;
+    float3 po = make_float3(0, 0, 0), pd = make_float3(0, 0, 0);
+    if (i < n) {
+        GHit h = hits0[i];
+        store_hit(hits1, i, false, 0, 0, 0, 0, 0);
+        if (h.prim != kMiss) {
+            float3 o, d;
+            float t0;
+            load_ray(rays, i, o, d, t0);
+            const float4* T = b.tris + 3ull * h.prim;
+            float4 v0 = __ldg(T), v1 = __ldg(T + 1), v2 = __ldg(T + 2);
+            float4 e1 = make_float4(fsub(v1.x, v0.x), fsub(v1.y, v0.y), fsub(v1.z, v0.z), 0.f);
+            float4 e2 = make_float4(fsub(v2.x, v0.x), fsub(v2.y, v0.y), fsub(v2.z, v0.z), 0.f);
+            have = bounce_dir(o, d, h.t, v0, e1, e2, seed, i, po, pd);
+        }
+    }
+    unsigned mask = __ballot_sync(kFull, have);
+    if (mask == 0) return;
+    unsigned lane = threadIdx.x & 31u;
+    int leader = __ffs(mask) - 1;
+    uint32_t base = 0;
+    if ((int)lane == leader) base = atomicAdd(queue_count, (uint32_t)__popc(mask));
+    base = __shfl_sync(kFull, base, leader);
+    if (have) {
+        uint32_t slot = base + __popc(mask & ((1u << lane) - 1u));
+        queue_rays[2ull * slot] = make_float4(po.x, po.y, po.z, FLT_MAX);
+        queue_rays[2ull * slot + 1] = make_float4(pd.x, pd.y, pd.z, 0.0f);
+        queue_pix[slot] = i;
+    }
+}
+
+template <int STACK>
+__global__ void __launch_bounds__(kBlock) k_trace_queue(GBlas b, const float4* __restrict__ qrays,
+                                                        const uint32_t* __restrict__ qpix, const uint32_t* qcount,
+                                                        GHit* __restrict__ hits, uint32_t* err) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= *qcount) return;
+    float3 o, d;
+    float t;
+    load_ray(qrays, i, o, d, t);
+    float3 rd = recip3(d);
+    float hu = 0.0f, hv = 0.0f;
+    uint32_t hp = 0;
+    bool hit = trace_blas<STACK>(b, o, d, rd, t, hu, hv, hp, err);
+    store_hit(hits, qpix[i], hit && t < FLT_MAX, t, hu, hv, hp, 0u);
+}
+
+// Bounce rays in pixel order (for checking the bounce generation against the oracle).
+__global__ void k_bounce_rays(GBlas b, const float4* __restrict__ rays, const GHit* __restrict__ hits0, uint32_t n,
+                              uint32_t seed, float4* __restrict__ out, uint8_t* __restrict__ valid) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    GHit h = hits0[i];
+    bool have = false;
+    float3 po = make_float3(0, 0, 0), pd = make_float3(0, 0, 0);
+    if (h.prim != kMiss) {
+        float3 o, d;
+        float t0;
+        load_ray(rays, i, o, d, t0);
+        const float4* T = b.tris + 3ull * h.prim;
+        float4 v0 = __ldg(T), v1 = __ldg(T + 1), v2 = __ldg(T + 2);
+        float4 e1 = make_float4(fsub(v1.x, v0.x), fsub(v1.y, v0.y), fsub(v1.z, v0.z), 0.f);
+        float4 e2 = make_float4(fsub(v2.x, v0.x), fsub(v2.y, v0.y), fsub(v2.z, v0.z), 0.f);
+        have = bounce_dir(o, d, h.t, v0, e1, e2, seed, i, po, pd);
+    }
+    out[2ull * i] = make_float4(po.x, po.y, po.z, FLT_MAX);
+    out[2ull * i + 1] = make_float4(pd.x, pd.y, pd.z, 0.0f);
+    valid[i] = have ? 1 : 0;
+}
+
+// ---- persistent: primary + bounce in one launch -------------------------------------------
+
+// Lanes are refilled when fewer than this many of the warp's 32 lanes still have work.
+constexpr int kRefillBelow = 24;
+
+template <int STACK>
+__global__ void __launch_bounds__(kBlock) k_persistent_bounce(GBlas b, const float4* __restrict__ rays, uint32_t n,
+                                                              uint32_t seed, GHit* __restrict__ hits0,
+                                                              GHit* __restrict__ hits1, uint32_t* queue,
+                                                              uint32_t* err) {
+    const unsigned lane = threadIdx.x & 31u;
+    // phase: 0 needs work, 1 primary ray, 2 bounce ray, 3 retired
+    int phase = 0;
+    uint32_t idx = 0;
+    float3 o = make_float3(0, 0, 0), d = o, rd = o;
+    float ct = 0.0f, hu = 0.0f, hv = 0.0f;
+    uint32_t hp = 0;
+    bool hit = false;
+    bool queue_open = true;
+    Trav<STACK> tr;
+    for (;;) {
+        unsigned need = __ballot_sync(kFull, phase == 0);
+        if (need != 0u) {
+            int leader = __ffs(need) - 1;
+            uint32_t base = 0;
+            if ((int)lane == leader) base = atomicAdd(queue, (uint32_t)__popc(need));
+            base = __shfl_sync(kFull, base, leader);
+            if (base + (uint32_t)__popc(need) > n) queue_open = false;
+            if (phase == 0) {
+                uint32_t my = base + __popc(need & ((1u << lane) - 1u));
+                if (my < n) {
+                    idx = my;
+                    float t0;
+                    load_ray(rays, idx, o, d, t0);
+                    rd = recip3(d);
+                    ct = t0;
+                    hu = hv = 0.0f;
+                    hp = 0;
+                    hit = false;
+                    tr.init(b);
+                    phase = 1;
+                } else {
+                    phase = 3;
+                }
+            }
+        }
+        unsigned busy = __ballot_sync(kFull, phase == 1 || phase == 2);
+        if (busy == 0u) {
+            if (!queue_open) break;
+            continue;
+        }
+        for (;;) {
+            if (phase == 1 || phase == 2) {
+                if (tr.step(b, o, d, rd, ct, hu, hv, hp, hit, err)) {
+                    bool h = hit && ct < FLT_MAX;
+                    if (phase == 1) {
+                        store_hit(hits0, idx, h, ct, hu, hv, hp, 0u);
+                        float3 po, pd;
+                        bool have = false;
+                        if (h) {
+                            const float4* T = b.tris + 3ull * hp;
+                            float4 v0 = __ldg(T), v1 = __ldg(T + 1), v2 = __ldg(T + 2);
+                            float4 e1 = make_float4(fsub(v1.x, v0.x), fsub(v1.y, v0.y), fsub(v1.z, v0.z), 0.f);
+                            float4 e2 = make_float4(fsub(v2.x, v0.x), fsub(v2.y, v0.y), fsub(v2.z, v0.z), 0.f);
+                            have = bounce_dir(o, d, ct, v0, e1, e2, seed, idx, po, pd);
+                        }
+                        if (have) {
+                            o = po;
+                            d = pd;
+                            rd = recip3(d);
+                            ct = FLT_MAX;
+                            hu = hv = 0.0f;
+                            hp = 0;
+                            hit = false;
+                            tr.init(b);
+                            phase = 2;
+                        } else {
+                            store_hit(hits1, idx, false, 0, 0, 0, 0, 0);
+                            phase = 0;
+                        }
+                    } else {
+                        store_hit(hits1, idx, h, ct, hu, hv, hp, 0u);
+                        phase = 0;
+                    }
+                }
+            }
+            unsigned act = __ballot_sync(kFull, phase == 1 || phase == 2);
+            if (act == 0u) break;
+            if (queue_open && __popc(act) < kRefillBelow) break;
+        }
+    }
+}
+
+// ---- uneven batch ----------------------------------------------------------------------------
+
+struct BatchEntry {
+    GBlas blas;
+    uint32_t ray_offset;
+    uint32_t work_begin;  // prefix sum of ray counts
+    uint32_t pad0, pad1;
+};
+
+template <int STACK>
+__global__ void __launch_bounds__(kBlock) k_trace_batch_persistent(const BatchEntry* __restrict__ table,
+                                                                   uint32_t nitems, uint32_t total,
+                                                                   const float4* __restrict__ rays,
+                                                                   GHit* __restrict__ hits, uint32_t* queue,
+                                                                   uint32_t* err) {
+    const unsigned lane = threadIdx.x & 31u;
+    int phase = 0;  // 0 needs work, 1 tracing, 3 retired
+    uint32_t ray = 0;
+    GBlas b;
+    b.nodes = nullptr;
+    b.tris = nullptr;
+    b.nodes_used = b.ntris = b.root_count = b.root_first = 0;
+    float3 o = make_float3(0, 0, 0), d = o, rd = o;
+    float ct = 0.0f, hu = 0.0f, hv = 0.0f;
+    uint32_t hp = 0;
+    bool hit = false;
+    bool queue_open = true;
+    Trav<STACK> tr;
+    for (;;) {
+        unsigned need = __ballot_sync(kFull, phase == 0);
+        if (need != 0u) {
+            int leader = __ffs(need) - 1;
+            uint32_t base = 0;
+            if ((int)lane == leader) base = atomicAdd(queue, (uint32_t)__popc(need));
+            base = __shfl_sync(kFull, base, leader);
+            if (base + (uint32_t)__popc(need) > total) queue_open = false;
+            if (phase == 0) {
+                uint32_t w = base + __popc(need & ((1u << lane) - 1u));
+                if (w < total) {
+                    // binary search: last item with work_begin <= w
+                    uint32_t lo = 0, hi = nitems;
+                    while (hi - lo > 1) {
+                        uint32_t mid = (lo + hi) >> 1;
+                        if (__ldg(&table[mid].work_begin) <= w) lo = mid; else hi = mid;
+                    }
+                    const BatchEntry& e = table[lo];
+                    b.nodes = e.blas.nodes;
+                    b.tris = e.blas.tris;
+                    b.nodes_used = e.blas.nodes_used;
+                    b.ntris = e.blas.ntris;
+                    b.root_count = e.blas.root_count;
+                    b.root_first = e.blas.root_first;
+                    ray = e.ray_offset + (w - e.work_begin);
+                    float t0;
+                    load_ray(rays, ray, o, d, t0);
+                    rd = recip3(d);
+                    ct = t0;
+                    hu = hv = 0.0f;
+                    hp = 0;
+                    hit = false;
+                    tr.init(b);
+                    phase = 1;
+                } else {
+                    phase = 3;
+                }
+            }
+        }
+        unsigned busy = __ballot_sync(kFull, phase == 1);
+        if (busy == 0u) {
+            if (!queue_open) break;
+            continue;
+        }
+        for (;;) {
+            if (phase == 1) {
+                if (tr.step(b, o, d, rd, ct, hu, hv, hp, hit, err)) {
+                    store_hit(hits, ray, hit && ct < FLT_MAX, ct, hu, hv, hp, 0u);
+                    phase = 0;
+                }
+            }
+            unsigned act = __ballot_sync(kFull, phase == 1);
+            if (act == 0u) break;
+            if (queue_open && __popc(act) < kRefillBelow) break;
+        }
+    }
+}
+
+// ---- tiled render --------------------------------------------------------------------------
+
+__device__ __forceinline__ float3 xf_point(const float* m, float3 p) {
+    return make_float3(fadd(fadd(fadd(fmul(m[0], p.x), fmul(m[4], p.y)), fmul(m[8], p.z)), fmul(m[12], 1.0f)),
+                       fadd(fadd(fadd(fmul(m[1], p.x), fmul(m[5], p.y)), fmul(m[9], p.z)), fmul(m[13], 1.0f)),
+                       fadd(fadd(fadd(fmul(m[2], p.x), fmul(m[6], p.y)), fmul(m[10], p.z)), fmul(m[14], 1.0f)));
+}
+__device__ __forceinline__ float3 xf_vector(const float* m, float3 p) {
+    return make_float3(fadd(fadd(fadd(fmul(m[0], p.x), fmul(m[4], p.y)), fmul(m[8], p.z)), fmul(m[12], 0.0f)),
+                       fadd(fadd(fadd(fmul(m[1], p.x), fmul(m[5], p.y)), fmul(m[9], p.z)), fmul(m[13], 0.0f)),
+                       fadd(fadd(fadd(fmul(m[2], p.x), fmul(m[6], p.y)), fmul(m[10], p.z)), fmul(m[14], 0.0f)));
+}
+__device__ __forceinline__ float3 normalize3(float3 v) {
+    float m = __fsqrt_rn(dot3(v.x, v.y, v.z, v.x, v.y, v.z));
+    return make_float3(__fdiv_rn(v.x, m), __fdiv_rn(v.y, m), __fdiv_rn(v.z, m));
+}
+
+struct RenderParams {
+    float cam[9 + 16];
+    float acc[16];
+    float sh[8];
+    int width, height, acc_kind, shader_kind;
+};
+
+__device__ __forceinline__ uint8_t f32_as_u8(float x) {  // Rust `as u8`: saturating, NaN -> 0
+    if (!(x > 0.0f)) return 0;
+    if (x >= 255.0f) return 255;
+    return (uint8_t)x;
+}
+__device__ __forceinline__ int32_t f32_as_i32(float x) {  // Rust `as i32`: saturating, NaN -> 0
+    if (x != x) return 0;
+    if (x >= 2147483648.0f) return INT32_MAX;
+    if (x <= -2147483648.0f) return INT32_MIN;
+    return (int32_t)x;
+}
+
+// PathTracer::evaluate (renderer.rs:345-384): one 64-thread block per 8x8 tile; the camera ray
+// goes through the pixel's top-left corner u = x / w, v = y / h (renderer.rs:358-361).
+template <int STACK>
+__global__ void __launch_bounds__(64) k_render(GBlas b, RenderParams P, const float* __restrict__ normals,
+                                               uint8_t* __restrict__ rgba, uint32_t* err) {
+    const int tiles_x = (P.width + 7) / 8;
+    const int tile = blockIdx.x;
+    const int x = (tile % tiles_x) * 8 + (threadIdx.x & 7);
+    const int y = (tile / tiles_x) * 8 + (threadIdx.x >> 3);
+    if (x >= P.width || y >= P.height) return;
+    const float* C = P.cam;
+    float u = __fdiv_rn((float)x, (float)P.width);
+    float v = __fdiv_rn((float)y, (float)P.height);
+    // Camera::get_ray_eye (camera.rs:994-1002)
+    float3 tl = make_float3(C[0], C[1], C[2]), tr = make_float3(C[3], C[4], C[5]), bl = make_float3(C[6], C[7], C[8]);
+    float3 org = make_float3(0.0f, 0.0f, 0.0f);
+    float3 p = make_float3(fadd(org.x, tl.x), fadd(org.y, tl.y), fadd(org.z, tl.z));
+    p = make_float3(fadd(p.x, fmul(fsub(tr.x, tl.x), u)), fadd(p.y, fmul(fsub(tr.y, tl.y), u)),
+                    fadd(p.z, fmul(fsub(tr.z, tl.z), u)));
+    p = make_float3(fadd(p.x, fmul(fsub(bl.x, tl.x), v)), fadd(p.y, fmul(fsub(bl.y, tl.y), v)),
+                    fadd(p.z, fmul(fsub(bl.z, tl.z), v)));
+    float3 dir = normalize3(make_float3(fsub(p.x, org.x), fsub(p.y, org.y), fsub(p.z, org.z)));
+    // Camera::get_ray_world (camera.rs:1004-1010)
+    float3 o = xf_point(C + 9, org);
+    float3 d = xf_vector(C + 9, dir);
+    float3 rd = recip3(d);
+    float t = FLT_MAX, hu = 0.0f, hv = 0.0f;
+    uint32_t hp = 0;
+    bool hit = trace_blas<STACK>(b, o, d, rd, t, hu, hv, hp, err) && t < FLT_MAX;
+    float3 rad = make_float3(0.0f, 0.0f, 0.0f);
+    switch (P.acc_kind) {
+        case BVHGPU_ACC_INTERSECTION:  // renderer.rs:145-153
+            rad = hit ? make_float3(P.acc[0], P.acc[1], P.acc[2]) : make_float3(P.acc[3], P.acc[4], P.acc[5]);
+            break;
+        case BVHGPU_ACC_DEPTH: {  // renderer.rs:184-193
+            float tt = hit ? t : FLT_MAX;
+            rad = make_float3(tt, tt, tt);
+            break;
+        }
+        case BVHGPU_ACC_UV:  // renderer.rs:233-244
+            if (hit) rad = make_float3(hu, hv, fsub(1.0f, fadd(hu, hv)));
+            break;
+        case BVHGPU_ACC_NORMAL:  // renderer.rs:256-285
+            if (hit) {
+                const float* nn = normals + 9ull * hp;
+                float w0 = fsub(fsub(1.0f, hu), hv);
+                float3 nm;
+                nm.x = fadd(fadd(fmul(nn[0], w0), fmul(nn[3], hu)), fmul(nn[6], hv));
+                nm.y = fadd(fadd(fmul(nn[1], w0), fmul(nn[4], hu)), fmul(nn[7], hv));
+                nm.z = fadd(fadd(fmul(nn[2], w0), fmul(nn[5], hu)), fmul(nn[8], hv));
+                float3 nz = normalize3(xf_vector(P.acc, nm));
+                rad = make_float3(fmul(fadd(nz.x, 1.0f), 0.5f), fmul(fadd(nz.y, 1.0f), 0.5f),
+                                  fmul(fadd(nz.z, 1.0f), 0.5f));
+            }
+            break;
+        default:
+            break;
+    }
+    uchar4 c;
+    switch (P.shader_kind) {
+        case BVHGPU_SHADER_INTERSECTION: {  // renderer.rs:166-173
+            bool nz = !(rad.x == 0.0f && rad.y == 0.0f && rad.z == 0.0f);
+            const float* s = nz ? P.sh : P.sh + 4;
+            c = make_uchar4((uint8_t)s[0], (uint8_t)s[1], (uint8_t)s[2], (uint8_t)s[3]);
+            break;
+        }
+        case BVHGPU_SHADER_DEPTH: {  // renderer.rs:207-221 (u32 arithmetic wraps)
+            if (rad.x < FLT_MAX) {
+                uint32_t col = 255u - (uint32_t)f32_as_i32(fmul(fsub(rad.x, P.sh[1]), P.sh[0]));
+                uint32_t cc = col * 0x010101u;
+                c = make_uchar4((uint8_t)((cc & 0x00FF0000u) >> 16), (uint8_t)((cc & 0x0000FF00u) >> 8),
+                                (uint8_t)(cc & 0xFFu), 255);
+            } else {
+                c = make_uchar4(0, 0, 0, 255);
+            }
+            break;
+        }
+        default:  // RadianceToRgbShader (renderer.rs:124-131)
+            c = make_uchar4(f32_as_u8(fmul(255.0f, rad.x)), f32_as_u8(fmul(255.0f, rad.y)),
+                            f32_as_u8(fmul(255.0f, rad.z)), 255);
+            break;
+    }
+    reinterpret_cast<uchar4*>(rgba)[(size_t)y * P.width + x] = c;
+}
+
+int persistent_grid(bvhgpu_ctx* ctx, const void* kernel) {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kBlock, 0);
+    if (per_sm < 1) per_sm = 1;
+    return per_sm * ctx->num_sms;
+}
+
+}  // namespace
+
+#define BVHGPU_DISPATCH_STACK(depth, ...)                         \
+    switch (stack_variant(depth)) {                               \
+        case 32: { constexpr int S = 32; __VA_ARGS__; break; }    \
+        case 64: { constexpr int S = 64; __VA_ARGS__; break; }    \
+        case 128: { constexpr int S = 128; __VA_ARGS__; break; }  \
+        default: { constexpr int S = 256; __VA_ARGS__; break; }   \
+    }
+
+cudaError_t launch_trace_blas(bvhgpu_ctx* ctx, const DeviceBlas& b, const float4* rays, uint32_t n, void* hits,
+                              cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    GBlas g = to_gblas(b);
+    LaunchScope scope(ctx, BVHGPU_K_TRACE_BLAS, s);
+    BVHGPU_DISPATCH_STACK(b.depth, (k_trace_blas<S><<<grid_for(n, kBlock), kBlock, 0, s>>>(
+                                       g, rays, n, static_cast<GHit*>(hits), ctx->d_err)));
+    g_launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bounce_plain(bvhgpu_ctx* ctx, const DeviceBlas& b, const float4* rays, uint32_t n, uint32_t seed,
+                                void* hits0, void* hits1, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    cudaError_t e = launch_trace_blas(ctx, b, rays, n, hits0, s);
+    if (e != cudaSuccess) return e;
+    uint32_t* qcount = ctx->d_scratch + 1;
+    e = cudaMemsetAsync(qcount, 0, sizeof(uint32_t), s);
+    if (e != cudaSuccess) return e;
+    GBlas g = to_gblas(b);
+    {
+        LaunchScope scope(ctx, BVHGPU_K_BOUNCE_GEN, s);
+        k_bounce_gen<<<grid_for(n, kBlock), kBlock, 0, s>>>(g, rays, static_cast<const GHit*>(hits0), n, seed,
+                                                            static_cast<float4*>(ctx->bounce_rays), ctx->bounce_pix,
+                                                            qcount, static_cast<GHit*>(hits1));
+        g_launches++;
+    }
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    {
+        LaunchScope scope(ctx, BVHGPU_K_TRACE_QUEUE, s);
+        BVHGPU_DISPATCH_STACK(b.depth, (k_trace_queue<S><<<grid_for(n, kBlock), kBlock, 0, s>>>(
+                                           g, static_cast<const float4*>(ctx->bounce_rays), ctx->bounce_pix, qcount,
+                                           static_cast<GHit*>(hits1), ctx->d_err)));
+        g_launches++;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bounce_persistent(bvhgpu_ctx* ctx, const DeviceBlas& b, const float4* rays, uint32_t n,
+                                     uint32_t seed, void* hits0, void* hits1, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    uint32_t* queue = ctx->d_scratch + 2;
+    cudaError_t e = cudaMemsetAsync(queue, 0, sizeof(uint32_t), s);
+    if (e != cudaSuccess) return e;
+    GBlas g = to_gblas(b);
+    LaunchScope scope(ctx, BVHGPU_K_PERSISTENT_BOUNCE, s);
+    BVHGPU_DISPATCH_STACK(b.depth, {
+        int grid = persistent_grid(ctx, (const void*)k_persistent_bounce<S>);
+        k_persistent_bounce<S><<<grid, kBlock, 0, s>>>(g, rays, n, seed, static_cast<GHit*>(hits0),
+                                                         static_cast<GHit*>(hits1), queue, ctx->d_err);
+    });
+    g_launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bounce_rays(bvhgpu_ctx* ctx, const DeviceBlas& b, const float4* rays, const void* hits0,
+                               uint32_t n, uint32_t seed, float4* out, uint8_t* valid, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    GBlas g = to_gblas(b);
+    LaunchScope scope(ctx, BVHGPU_K_OTHER, s);
+    k_bounce_rays<<<grid_for(n, kBlock), kBlock, 0, s>>>(g, rays, static_cast<const GHit*>(hits0), n, seed, out,
+                                                         valid);
+    g_launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_trace_batch(bvhgpu_ctx* ctx, const std::vector<const DeviceBlas*>& blases,
+                               const bvhgpu_batch_item* items, uint32_t nitems, const float4* rays, uint32_t nrays,
+                               int mode, void* hits, cudaStream_t s) {
+    (void)nrays;
+    if (nitems == 0) return cudaSuccess;
+    if (mode == BVHGPU_MODE_PLAIN) {
+        for (uint32_t i = 0; i < nitems; ++i) {
+            cudaError_t e = launch_trace_blas(ctx, *blases[i], rays + 2ull * items[i].ray_offset, items[i].ray_count,
+                                              static_cast<GHit*>(hits) + items[i].ray_offset, s);
+            if (e != cudaSuccess) return e;
+        }
+        return cudaSuccess;
+    }
+    // persistent: a device table of (BLAS, ray offset, work prefix), cached across calls
+    bool same = ctx->batch_items.size() == nitems && ctx->batch_table != nullptr &&
+                std::equal(items, items + nitems, ctx->batch_items.begin(),
+                           [](const bvhgpu_batch_item& a, const bvhgpu_batch_item& b) {
+                               return a.blas == b.blas && a.ray_offset == b.ray_offset && a.ray_count == b.ray_count;
+                           });
+    if (!same) {
+        std::vector<BatchEntry> table(nitems);
+        uint32_t total = 0;
+        uint32_t depth = 1;
+        for (uint32_t i = 0; i < nitems; ++i) {
+            table[i].blas = to_gblas(*blases[i]);
+            table[i].ray_offset = items[i].ray_offset;
+            table[i].work_begin = total;
+            table[i].pad0 = table[i].pad1 = 0;
+            total += items[i].ray_count;
+            depth = std::max(depth, blases[i]->depth);
+        }
+        size_t bytes = sizeof(BatchEntry) * nitems;
+        // the previous table may still be read by work queued on the stream
+        cudaError_t e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return e;
+        if (ctx->batch_table_bytes < bytes) {
+            cudaFree(ctx->batch_table);
+            ctx->batch_table = nullptr;
+            ctx->batch_table_bytes = 0;
+            e = cudaMalloc(&ctx->batch_table, bytes);
+            if (e != cudaSuccess) return e;
+            ctx->batch_table_bytes = bytes;
+        }
+        e = cudaMemcpy(ctx->batch_table, table.data(), bytes, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return e;
+        ctx->batch_items.assign(items, items + nitems);
+        ctx->batch_total = total;
+        ctx->batch_depth = depth;
+    }
+    uint32_t* queue = ctx->d_scratch + 3;
+    cudaError_t e = cudaMemsetAsync(queue, 0, sizeof(uint32_t), s);
+    if (e != cudaSuccess) return e;
+    const uint32_t total = ctx->batch_total;
+    LaunchScope scope(ctx, BVHGPU_K_TRACE_BATCH, s);
+    BVHGPU_DISPATCH_STACK(ctx->batch_depth, {
+        int grid = persistent_grid(ctx, (const void*)k_trace_batch_persistent<S>);
+        k_trace_batch_persistent<S><<<grid, kBlock, 0, s>>>(static_cast<const BatchEntry*>(ctx->batch_table), nitems,
+                                                            total, rays, static_cast<GHit*>(hits), queue, ctx->d_err);
+    });
+    g_launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_render(bvhgpu_ctx* ctx, const DeviceBlas& b, const bvhgpu_camera& cam, int w, int h, int acc,
+                          const float* acc_params, int shader, const float* shader_params, const float* d_normals,
+                          uint8_t* d_rgba, cudaStream_t s) {
+    RenderParams P;
+    std::copy(cam.top_left, cam.top_left + 3, P.cam);
+    std::copy(cam.top_right, cam.top_right + 3, P.cam + 3);
+    std::copy(cam.bottom_left, cam.bottom_left + 3, P.cam + 6);
+    std::copy(cam.view_inv, cam.view_inv + 16, P.cam + 9);
+    std::fill(P.acc, P.acc + 16, 0.0f);
+    std::fill(P.sh, P.sh + 8, 0.0f);
+    if (acc == BVHGPU_ACC_INTERSECTION && acc_params) std::copy(acc_params, acc_params + 6, P.acc);
+    if (acc == BVHGPU_ACC_NORMAL && acc_params) std::copy(acc_params, acc_params + 16, P.acc);
+    if (shader == BVHGPU_SHADER_INTERSECTION && shader_params) std::copy(shader_params, shader_params + 8, P.sh);
+    if (shader == BVHGPU_SHADER_DEPTH && shader_params) std::copy(shader_params, shader_params + 2, P.sh);
+    P.width = w;
+    P.height = h;
+    P.acc_kind = acc;
+    P.shader_kind = shader;
+    GBlas g = to_gblas(b);
+    unsigned tiles = (unsigned)(((w + 7) / 8) * ((h + 7) / 8));
+    LaunchScope scope(ctx, BVHGPU_K_RENDER, s);
+    BVHGPU_DISPATCH_STACK(b.depth, (k_render<S><<<tiles, 64, 0, s>>>(g, P, d_normals, d_rgba, ctx->d_err)));
+    g_launches++;
+    return cudaGetLastError();
+}
+
+}  // namespace bvhgpu

@@ -1,0 +1,250 @@
+/*
+ * bvhgpu -- GB300 (sm_103a) ray-BVH hot path of lambdaxymox/bvhtracer behind a C ABI.
+ *
+ * The reference is a Rust crate with no FFI of its own; the entry points below are
+ * what a Rust `extern "C"` block (bvhgpu-sys) binds to put the GPU path behind the
+ * crate's own plug-in points.  Each declaration names the reference interface it
+ * replaces (paths relative to the reference repository; BT = bvhtracer/).
+ *
+ * Conventions
+ *  - Every function returns an int status (BVHGPU_OK == 0); no exception or abort
+ *    crosses the ABI.  bvhgpu_last_error(ctx) gives a message for the last failure.
+ *  - Plain C structs with fixed layouts (sizes asserted in the implementation).
+ *  - Host pointers are caller-owned and only read/written during the call.  Device
+ *    buffers behind BLAS / scene handles are owned by the context.
+ *  - "_async" entry points take DEVICE pointers and a stream (NULL = the context's
+ *    stream) and return before the work finishes; the others take HOST pointers and
+ *    return after the results are in host memory.
+ *  - A context is not thread-safe (one per host thread), like the reference's
+ *    single-threaded Rc<RefCell<Model>> ownership (BT/src/model/model.rs:16-24).
+ *  - There is no CPU fallback: without a usable CUDA device bvhgpu_create fails.
+ */
+#ifndef BVHGPU_H
+#define BVHGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes --------------------------------------------------------------- */
+#define BVHGPU_OK 0
+#define BVHGPU_ERR_INVALID_ARG 1   /* bad pointer, size, handle or malformed node array */
+#define BVHGPU_ERR_OUT_OF_MEMORY 2
+#define BVHGPU_ERR_CUDA 3          /* a CUDA runtime call failed */
+#define BVHGPU_ERR_STACK_DEPTH 4   /* tree deeper than the traversal stack (device flag) */
+#define BVHGPU_ERR_STEP_CAP 5      /* a traversal exceeded its step cap (corrupt tree) */
+#define BVHGPU_ERR_BUILD 6         /* the reference's BvhBuilder would panic on this mesh */
+#define BVHGPU_ERR_NO_DEVICE 7
+
+/* ---- data layouts ------------------------------------------------------------------- */
+
+/* BvhNode (BT/src/model/bvh.rs:129-134): 32 bytes, leaf iff primitive_count > 0; for a
+ * branch left_first is the left child (right = left + 1, bvh.rs:111-113), for a leaf the
+ * first primitive.  Node 0 is the root, node 1 an unused filler (bvh.rs:514-517). */
+typedef struct bvhgpu_node {
+    float bounds_min[3];
+    float bounds_max[3];
+    uint32_t primitive_count;
+    uint32_t left_first;
+} bvhgpu_node;
+
+/* Triangle<f32> (BT/src/geometry/triangle.rs:11-17): three vertices, 36 bytes. */
+typedef struct bvhgpu_triangle {
+    float vertices[9];
+} bvhgpu_triangle;
+
+/* Ray<f32> (BT/src/query/ray.rs:9-35) without the derived reciprocal direction (the
+ * kernels recompute 1/d with the same IEEE division).  t = FLT_MAX for Ray::from_origin_dir. */
+typedef struct bvhgpu_ray {
+    float origin[3];
+    float t;
+    float direction[3];
+    uint32_t reserved;
+} bvhgpu_ray;
+
+/* Intersection (BT/src/query/intersection.rs:83-92) reduced to the hit record: t, u, v of
+ * SurfaceInteraction and separate 32-bit primitive / instance ids (the reference packs
+ * them in 20 + 12 bits, intersection.rs:41-66).  A miss (Option::None) is
+ * t = FLT_MAX, u = v = 0, prim = inst = BVHGPU_MISS. */
+typedef struct bvhgpu_hit {
+    float t, u, v;
+    uint32_t prim;
+    uint32_t inst;
+} bvhgpu_hit;
+#define BVHGPU_MISS 0xFFFFFFFFu
+
+/* TlasNode (BT/src/scene/tlas.rs:41-46): left_right packs two 16-bit node indices with the
+ * reference's swapped getters (tlas.rs:17-32); leaf iff left_right == 0. */
+typedef struct bvhgpu_tlas_node {
+    float bounds_min[3];
+    float bounds_max[3];
+    uint32_t left_right;
+    uint32_t blas;
+} bvhgpu_tlas_node;
+
+/* Camera::get_ray_world inputs (BT/src/camera/camera.rs:994-1010): the eye-space frustum
+ * corners (top-left, top-right, bottom-left) and view_matrix_inv, column-major. */
+typedef struct bvhgpu_camera {
+    float top_left[3];
+    float top_right[3];
+    float bottom_left[3];
+    float view_inv[16];
+} bvhgpu_camera;
+
+/* One scene of an uneven batch: rays [ray_offset, ray_offset + ray_count) of the batch's
+ * ray array are traced against BLAS `blas`. */
+typedef struct bvhgpu_batch_item {
+    uint32_t blas;
+    uint32_t ray_offset;
+    uint32_t ray_count;
+    uint32_t reserved;
+} bvhgpu_batch_item;
+
+/* Accumulators (BT/src/renderer.rs:108-110, 134-286) and pixel shaders (:112-222). */
+#define BVHGPU_ACC_INTERSECTION 0  /* IntersectionAccumulator: params hit rgb, miss rgb */
+#define BVHGPU_ACC_DEPTH 1         /* DepthAccumulator */
+#define BVHGPU_ACC_UV 2            /* UvMappingAccumulator */
+#define BVHGPU_ACC_NORMAL 3        /* NormalMappingAccumulator: params = object transform (16) */
+#define BVHGPU_SHADER_RADIANCE 0      /* RadianceToRgbShader */
+#define BVHGPU_SHADER_INTERSECTION 1  /* IntersectionShader: params hit rgba, miss rgba */
+#define BVHGPU_SHADER_DEPTH 2         /* DepthMappingShader: params scale, offset */
+
+/* Trace modes for the bounce and batch entry points. */
+#define BVHGPU_MODE_PLAIN 0       /* one launch per scene / pass */
+#define BVHGPU_MODE_PERSISTENT 1  /* one persistent work-stealing launch */
+
+typedef struct bvhgpu_ctx bvhgpu_ctx;
+typedef void* bvhgpu_stream; /* a cudaStream_t */
+
+/* ---- context ------------------------------------------------------------------------ */
+/* Replaces nothing in the reference (it has no device); owns the stream and buffers. */
+int bvhgpu_create(bvhgpu_ctx** out, int device);
+int bvhgpu_destroy(bvhgpu_ctx* ctx);
+const char* bvhgpu_last_error(const bvhgpu_ctx* ctx);
+/* Number of kernels this library launched since load (all contexts). */
+uint64_t bvhgpu_launch_count(void);
+/* Waits for the context's stream and reports any device-side error flag. */
+int bvhgpu_sync(bvhgpu_ctx* ctx);
+bvhgpu_stream bvhgpu_get_stream(bvhgpu_ctx* ctx);
+
+/* ---- memory helpers (for callers without their own CUDA allocator) ------------------- */
+int bvhgpu_device_alloc(bvhgpu_ctx* ctx, size_t bytes, void** out);
+int bvhgpu_device_free(bvhgpu_ctx* ctx, void* p);
+int bvhgpu_host_alloc(bvhgpu_ctx* ctx, size_t bytes, void** out); /* pinned */
+int bvhgpu_host_free(bvhgpu_ctx* ctx, void* p);
+int bvhgpu_copy_to_device(bvhgpu_ctx* ctx, void* dst, const void* src, size_t bytes, bvhgpu_stream s);
+int bvhgpu_copy_to_host(bvhgpu_ctx* ctx, void* dst, const void* src, size_t bytes, bvhgpu_stream s);
+int bvhgpu_memset_device(bvhgpu_ctx* ctx, void* dst, int value, size_t bytes, bvhgpu_stream s);
+/* Writes a buffer larger than L2 so the next launch starts with a cold cache. */
+int bvhgpu_flush_l2(bvhgpu_ctx* ctx, bvhgpu_stream s);
+
+/* ---- timing ---------------------------------------------------------------------------- */
+int bvhgpu_event_create(bvhgpu_ctx* ctx, void** ev);
+int bvhgpu_event_destroy(bvhgpu_ctx* ctx, void* ev);
+int bvhgpu_event_record(bvhgpu_ctx* ctx, void* ev, bvhgpu_stream s);
+int bvhgpu_event_elapsed_ms(bvhgpu_ctx* ctx, void* start, void* stop, float* ms);
+/* Per-kernel timing: while enabled, every launch is bracketed by events on its own stream.
+ * bvhgpu_profile_read waits and fills per-kernel total ms and launch counts (arrays of
+ * BVHGPU_KERNEL_COUNT entries, indexed by the BVHGPU_K_* ids) and resets the table. */
+#define BVHGPU_K_TRACE_BLAS 0
+#define BVHGPU_K_TRACE_SCENE 1
+#define BVHGPU_K_PERSISTENT_BOUNCE 2
+#define BVHGPU_K_BOUNCE_GEN 3
+#define BVHGPU_K_TRACE_QUEUE 4
+#define BVHGPU_K_TRACE_BATCH 5
+#define BVHGPU_K_REFIT 6
+#define BVHGPU_K_TLAS_BUILD 7
+#define BVHGPU_K_RENDER 8
+#define BVHGPU_K_OTHER 9
+#define BVHGPU_KERNEL_COUNT 10
+int bvhgpu_profile_enable(bvhgpu_ctx* ctx, int enable);
+int bvhgpu_profile_read(bvhgpu_ctx* ctx, double* ms, uint64_t* launches);
+
+/* ---- BLAS -------------------------------------------------------------------------------- */
+/* BvhBuilder::build_for (BT/src/model/bvh.rs:524-541) on the host: the reference's SAH binned
+ * build (8 bins), reordering `mesh` in place.  nodes_out must hold 2*n nodes. */
+int bvhgpu_build_bvh_host(bvhgpu_triangle* mesh, uint32_t n, bvhgpu_node* nodes_out, uint32_t* nodes_used);
+
+/* Upload a reference-built BVH as-is (the node array of Bvh, bvh.rs:227-233, and the mesh's
+ * primitives, BT/src/mesh/mesh.rs:126-134).  Validates the tree; the handle replaces
+ * ModelInstance's Bvh + mesh pair (BT/src/model/model.rs:16-33). */
+int bvhgpu_blas_upload(bvhgpu_ctx* ctx, const bvhgpu_node* nodes, uint32_t nodes_used,
+                       const bvhgpu_triangle* tris, uint32_t ntris, uint32_t* blas_id);
+int bvhgpu_blas_free(bvhgpu_ctx* ctx, uint32_t blas_id);
+int bvhgpu_blas_info(bvhgpu_ctx* ctx, uint32_t blas_id, uint32_t* nodes_used, uint32_t* ntris, uint32_t* depth);
+/* New vertex positions (same triangle order), e.g. an animated mesh before refit. */
+int bvhgpu_blas_update_vertices(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhgpu_triangle* tris);
+int bvhgpu_blas_update_vertices_async(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhgpu_triangle* d_tris,
+                                      bvhgpu_stream s);
+/* Bvh::refit (bvh.rs:469-493) / ModelInstance::refit (model.rs:31-33) on the GPU. */
+int bvhgpu_blas_refit(bvhgpu_ctx* ctx, uint32_t blas_id);
+int bvhgpu_blas_refit_async(bvhgpu_ctx* ctx, uint32_t blas_id, bvhgpu_stream s);
+/* Read the node array back in the reference layout (nodes_used entries). */
+int bvhgpu_blas_download_nodes(bvhgpu_ctx* ctx, uint32_t blas_id, bvhgpu_node* nodes);
+/* Bvh::intersect (bvh.rs:307-309) / ModelInstance::intersect (model.rs:27-29) for a batch. */
+int bvhgpu_blas_intersect(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhgpu_ray* rays, uint32_t n,
+                          bvhgpu_hit* hits);
+int bvhgpu_blas_intersect_async(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhgpu_ray* d_rays, uint32_t n,
+                                bvhgpu_hit* d_hits, bvhgpu_stream s);
+
+/* Primary rays + one cosine-weighted diffuse bounce per hit (not in the reference; the frame
+ * pattern of its demos).  hits0[i] is ray i's closest hit, hits1[i] the hit of its bounce
+ * (miss when ray i missed).  mode: BVHGPU_MODE_PLAIN (trace, compact, trace) or
+ * BVHGPU_MODE_PERSISTENT (one work-stealing launch).  n_bounce (may be NULL) receives the
+ * number of bounce rays traced. */
+int bvhgpu_blas_trace_bounce(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhgpu_ray* rays, uint32_t n,
+                             uint32_t seed, int mode, bvhgpu_hit* hits0, bvhgpu_hit* hits1, uint32_t* n_bounce);
+int bvhgpu_blas_trace_bounce_async(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhgpu_ray* d_rays, uint32_t n,
+                                   uint32_t seed, int mode, bvhgpu_hit* d_hits0, bvhgpu_hit* d_hits1,
+                                   bvhgpu_stream s);
+/* The bounce rays the plain mode traced, in pixel order (valid[i] = 0 where none). */
+int bvhgpu_blas_bounce_rays(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhgpu_ray* rays, uint32_t n,
+                            uint32_t seed, bvhgpu_ray* out, uint8_t* valid);
+
+/* Uneven batch of scenes in one call: Scene::intersect repeated over many scenes.
+ * mode BVHGPU_MODE_PLAIN launches once per item; BVHGPU_MODE_PERSISTENT runs one
+ * work-stealing launch over all items. */
+int bvhgpu_trace_batch(bvhgpu_ctx* ctx, const bvhgpu_batch_item* items, uint32_t nitems,
+                       const bvhgpu_ray* rays, uint32_t nrays, int mode, bvhgpu_hit* hits);
+int bvhgpu_trace_batch_async(bvhgpu_ctx* ctx, const bvhgpu_batch_item* items, uint32_t nitems,
+                             const bvhgpu_ray* d_rays, uint32_t nrays, int mode, bvhgpu_hit* d_hits,
+                             bvhgpu_stream s);
+
+/* ---- scene / TLAS ----------------------------------------------------------------------- */
+/* SceneBuilder::build (BT/src/scene/scene.rs:224-234): objects i = 0..n-1 instance BLAS
+ * blas_ids[i].  Transforms start as identity. */
+int bvhgpu_scene_create(bvhgpu_ctx* ctx, const uint32_t* blas_ids, uint32_t nobjects, uint32_t* scene_id);
+int bvhgpu_scene_free(bvhgpu_ctx* ctx, uint32_t scene_id);
+/* SceneObject::set_transform (BT/src/scene/scene_object.rs:60-75) for all objects: the
+ * transform and its cached inverse (TransformComponent3, BT/src/transform_component.rs:24-27),
+ * 16 floats each, column-major.  World bounds are recomputed on the GPU at rebuild. */
+int bvhgpu_scene_set_transforms(bvhgpu_ctx* ctx, uint32_t scene_id, const float* xf, const float* inv);
+int bvhgpu_scene_set_transforms_async(bvhgpu_ctx* ctx, uint32_t scene_id, const float* d_xf,
+                                      const float* d_inv, bvhgpu_stream s);
+/* Scene::rebuild / Tlas::rebuild (scene.rs:36-38, tlas.rs:204-250) on the GPU. */
+int bvhgpu_scene_rebuild(bvhgpu_ctx* ctx, uint32_t scene_id);
+int bvhgpu_scene_rebuild_async(bvhgpu_ctx* ctx, uint32_t scene_id, bvhgpu_stream s);
+int bvhgpu_scene_download_tlas(bvhgpu_ctx* ctx, uint32_t scene_id, bvhgpu_tlas_node* nodes, uint32_t* nodes_used);
+/* Scene::intersect (scene.rs:32-34, tlas.rs:123-177, scene_object.rs:78-89).  Unlike the
+ * reference (which always reports instance 0) hit.inst is the object index. */
+int bvhgpu_scene_intersect(bvhgpu_ctx* ctx, uint32_t scene_id, const bvhgpu_ray* rays, uint32_t n,
+                           bvhgpu_hit* hits);
+int bvhgpu_scene_intersect_async(bvhgpu_ctx* ctx, uint32_t scene_id, const bvhgpu_ray* d_rays, uint32_t n,
+                                 bvhgpu_hit* d_hits, bvhgpu_stream s);
+
+/* ---- tiled render ----------------------------------------------------------------------- */
+/* Integrator::evaluate for PathTracer (BT/src/renderer.rs:104-106, 345-384) on one BLAS:
+ * 8x8 tiles, one ray per pixel through the pixel's top-left corner, accumulator + shader ->
+ * RGBA8 (row-major, w*h*4 bytes, not flipped).  normals (9 floats per triangle, in the BLAS's
+ * triangle order) only for BVHGPU_ACC_NORMAL.  Returns rays traced in *rays_traced. */
+int bvhgpu_render(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhgpu_camera* camera, int width, int height,
+                  int accumulator, const float* acc_params, int shader, const float* shader_params,
+                  const float* normals, uint8_t* rgba, uint64_t* rays_traced);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BVHGPU_H */

@@ -1,0 +1,53 @@
+"""The C-ABI library loads and exports every entry point include/bvhgpu.h declares.
+CPU only: no compute call needs a GPU here."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from bvhtracer_gb300 import _lib
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared():
+    with open(os.path.join(ROOT, "include", "bvhgpu.h")) as f:
+        text = f.read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(bvhgpu_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_header_declares_entry_points():
+    names = declared()
+    assert "bvhgpu_blas_intersect" in names and "bvhgpu_scene_rebuild" in names
+    assert len(names) >= 40
+
+
+def test_library_exports_every_declared_symbol():
+    lib = _lib.load()
+    missing = [n for n in declared() if not hasattr(lib, n)]
+    assert not missing, f"missing exports: {missing}"
+
+
+def test_binding_covers_header():
+    assert set(declared()) <= set(_lib.SIGNATURES), set(declared()) - set(_lib.SIGNATURES)
+
+
+def test_create_without_device_fails_cleanly():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a CUDA device is present")
+    lib = _lib.load()
+    h = ctypes.c_void_p()
+    rc = lib.bvhgpu_create(ctypes.byref(h), 0)
+    assert rc in (3, 7)
+    assert not h.value
+
+
+def test_host_entry_points_validate_arguments():
+    lib = _lib.load()
+    used = ctypes.c_uint32()
+    assert lib.bvhgpu_build_bvh_host(None, 0, None, ctypes.byref(used)) == 1
+    assert lib.bvhgpu_destroy(None) == 1
+    assert lib.bvhgpu_sync(None) == 1

@@ -1,0 +1,58 @@
+"""The product's host SAH build (BvhBuilder::build_for) against the oracle: identical node
+arrays and identical triangle order, bit for bit.  CPU only."""
+import numpy as np
+import pytest
+
+import bvhtracer_gb300 as bt
+from bvhtracer_gb300 import scenes
+from oracle import oracle as orc
+
+
+def build_both(tris):
+    tris = np.ascontiguousarray(tris, np.float32).reshape(-1, 9)
+    mine = tris.copy()
+    bvh = bt.BvhBuilder().build_for(mine)
+    ref_tris, ref_nodes, ref_used = orc.bvh_build(tris)
+    return mine, bvh, ref_tris, ref_nodes, ref_used
+
+
+def assert_same(tris):
+    mine, bvh, ref_tris, ref_nodes, ref_used = build_both(tris)
+    assert bvh.nodes_used == ref_used
+    assert mine.tobytes() == ref_tris.tobytes()
+    assert bvh.nodes.tobytes() == ref_nodes.tobytes()
+
+
+@pytest.mark.parametrize("n,seed", [(1, 0), (2, 1), (3, 2), (17, 3), (4096, 0), (4096, 11), (20000, 5)])
+def test_soup(n, seed):
+    assert_same(scenes.soup(n, seed))
+
+
+@pytest.mark.parametrize("level", [0, 1, 3, 5])
+def test_displaced_icosphere(level):
+    assert_same(scenes.displaced_icosphere(level, seed=level).triangles())
+
+
+def test_degenerate_meshes():
+    # identical triangles: every axis is skipped (bounds_min == bounds_max), one leaf
+    t = np.tile(np.array([0, 0, 0, 1, 0, 0, 0, 1, 0], np.float32), (64, 1))
+    assert_same(t)
+    # all centroids negative: the 1e-30 initial maximum of the reference is inside the range
+    assert_same(scenes.soup(300, 9) - np.float32(20))
+    # collinear centroids along one axis, zero extent on the others
+    line = np.zeros((100, 9), np.float32)
+    line[:, 0::3] = np.arange(100, dtype=np.float32)[:, None]
+    assert_same(line)
+
+
+def test_cube_fixture():
+    import os
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "cube.npz"))
+    assert_same(d["tris"])
+
+
+def test_rejects_bad_mesh():
+    with pytest.raises(ValueError):
+        bt.BvhBuilder().build_for(np.zeros((4, 9), np.float64))
+    with pytest.raises(bt.BvhGpuError):
+        bt.BvhBuilder().build_for(np.zeros((0, 9), np.float32))
