@@ -113,6 +113,7 @@ DeviceScene* find_scene(bvhgpu_ctx* ctx, uint32_t id) {
 void free_blas(DeviceBlas& b) {
     cudaFree(b.nodes);
     cudaFree(b.tris);
+    cudaFree(b.verts);
     cudaFree(b.parent);
     cudaFree(b.leaves);
     cudaFree(b.counters);
@@ -377,6 +378,7 @@ int bvhgpu_blas_upload(bvhgpu_ctx* ctx, const bvhgpu_node* nodes, uint32_t nodes
     };
     if ((e = cudaMalloc(&b.nodes, 32ull * nodes_used)) != cudaSuccess ||
         (e = cudaMalloc(&b.tris, 48ull * ntris)) != cudaSuccess ||
+        (e = cudaMalloc(&b.verts, 48ull * ntris)) != cudaSuccess ||
         (e = cudaMalloc(&b.parent, 4ull * nodes_used)) != cudaSuccess ||
         (e = cudaMalloc(&b.leaves, 4ull * std::max<size_t>(1, leaves.size()))) != cudaSuccess ||
         (e = cudaMalloc(&b.counters, 4ull * nodes_used)) != cudaSuccess ||

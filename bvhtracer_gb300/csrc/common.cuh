@@ -25,7 +25,7 @@ constexpr float kThreshold = 0.0001f;  // num_traits::cast(0.0001_f64) (triangle
 // children are adjacent (right = left + 1, bvh.rs:111-113), so one child pair is 64 bytes.
 struct GBlas {
     const float4* nodes;  // 2 float4 per node
-    const float4* tris;   // 3 float4 per triangle: {v0, 0}, {v1, 0}, {v2, 0}
+    const float4* tris;   // 3 float4 per triangle: {v0, 0}, {e1 = v1 - v0, 0}, {e2 = v2 - v0, 0}
     uint32_t nodes_used;
     uint32_t ntris;
     uint32_t root_count;  // root node meta (node 0)
@@ -100,13 +100,43 @@ __device__ __forceinline__ bool tri_test(float4 v0, float4 e1, float4 e2, float3
 
 __device__ __forceinline__ uint32_t ubits(float f) { return __float_as_uint(f); }
 
-// Closest-hit traversal of one BLAS (bvh.rs:242-305), one node per step: DFS with the far
-// child pushed, near child = strictly smaller entry distance (ties -> right child), popped
-// nodes are not re-culled (the reference does not re-test a popped node's box), leaf
-// triangles in primitive order with a strict `<` update.  The visit order is identical to
-// the reference's, so equal-t ties resolve to the same primitive.  The stack holds the far
-// child's (count, first), so a pop needs no memory load.  Triangles are stored as three
-// float4 vertices and the edges are recomputed here exactly as triangle.rs:44-45 does.
+// Closest-hit traversal of one BLAS (bvh.rs:242-305): DFS with the far child pushed, near
+// child = strictly smaller entry distance (ties -> right child), popped nodes are not
+// re-culled (the reference does not re-test a popped node's box), leaf triangles in
+// primitive order with a strict `<` update.  The visit order is identical to the
+// reference's, so equal-t ties resolve to the same primitive.  The stack holds the far
+// child's (count, first), so a pop needs no memory load.  Triangles are stored as
+// {v0, e1 = v1 - v0, e2 = v2 - v0}; each edge is the single IEEE subtraction of
+// triangle.rs:44-45, so precomputing it changes no bit.
+enum StepResult { kStepContinue = 0, kStepFinished = 1, kStepBigLeaf = 2 };
+
+// One lane's ray (world or model space) and its running closest hit.
+struct LaneRay {
+    float3 o, d, rd;
+    float ct;  // closest_ray.t
+    float hu, hv;
+    uint32_t hp;
+    bool hit;
+};
+
+__device__ __forceinline__ void test_leaf_lane(const float4* __restrict__ tris, uint32_t first, uint32_t cnt,
+                                               LaneRay& r) {
+    const float4* T = tris + 3ull * first;
+    for (uint32_t k = 0; k < cnt; ++k) {
+        float4 a = __ldg(T + 3 * k);
+        float4 e1 = __ldg(T + 3 * k + 1);
+        float4 e2 = __ldg(T + 3 * k + 2);
+        float t, u, v;
+        if (tri_test(a, e1, e2, r.o, r.d, t, u, v) && t < r.ct) {
+            r.ct = t;
+            r.hu = u;
+            r.hv = v;
+            r.hp = first + k;
+            r.hit = true;
+        }
+    }
+}
+
 template <int STACK>
 struct Trav {
     uint2 stack[STACK];
@@ -129,31 +159,18 @@ struct Trav {
         return false;
     }
 
-    // Processes one node.  Returns true when the traversal has finished.
-    __device__ __forceinline__ bool step(const GBlas& b, float3 o, float3 d, float3 rd, float& closest_t, float& hu,
-                                         float& hv, uint32_t& hprim, bool& hit, uint32_t* err) {
+    // Processes one node.  Leaves with more than `big_leaf` triangles are not tested here:
+    // the step returns kStepBigLeaf with (first, cnt) describing the leaf, and the caller
+    // tests it (warp-cooperatively) and then calls pop().
+    __device__ __forceinline__ StepResult step(const GBlas& b, LaneRay& r, uint32_t big_leaf, uint32_t* err) {
         if (++steps > max_steps) {
             atomicOr(err, kErrSteps);
-            return true;
+            return kStepFinished;
         }
         if (cnt > 0) {
-            const float4* T = b.tris + 3ull * first;
-            for (uint32_t k = 0; k < cnt; ++k) {
-                float4 a = __ldg(T + 3 * k);
-                float4 p1 = __ldg(T + 3 * k + 1);
-                float4 p2 = __ldg(T + 3 * k + 2);
-                float4 e1 = make_float4(fsub(p1.x, a.x), fsub(p1.y, a.y), fsub(p1.z, a.z), 0.0f);
-                float4 e2 = make_float4(fsub(p2.x, a.x), fsub(p2.y, a.y), fsub(p2.z, a.z), 0.0f);
-                float t, u, v;
-                if (tri_test(a, e1, e2, o, d, t, u, v) && t < closest_t) {
-                    closest_t = t;
-                    hu = u;
-                    hv = v;
-                    hprim = first + k;
-                    hit = true;
-                }
-            }
-            return pop();
+            if (cnt > big_leaf) return kStepBigLeaf;
+            test_leaf_lane(b.tris, first, cnt, r);
+            return pop() ? kStepFinished : kStepContinue;
         }
         const float4* N = b.nodes + 2ull * first;
         float4 l0 = __ldg(N);
@@ -161,8 +178,8 @@ struct Trav {
         float4 r0 = __ldg(N + 2);
         float4 r1 = __ldg(N + 3);
         float dl, dr;
-        bool hl = slab(l0, l1, o, rd, closest_t, dl);
-        bool hr = slab(r0, r1, o, rd, closest_t, dr);
+        bool hl = slab(l0, l1, r.o, r.rd, r.ct, dl);
+        bool hr = slab(r0, r1, r.o, r.rd, r.ct, dr);
         float kl = hl ? dl : FLT_MAX;
         float kr = hr ? dr : FLT_MAX;
         bool left_near = kl < kr;
@@ -172,27 +189,104 @@ struct Trav {
             if (far_hit) {
                 if (sp >= STACK) {
                     atomicOr(err, kErrStack);
-                    return true;
+                    return kStepFinished;
                 }
                 stack[sp++] = left_near ? make_uint2(ubits(r1.w), ubits(r0.w)) : make_uint2(ubits(l1.w), ubits(l0.w));
             }
             cnt = left_near ? ubits(l1.w) : ubits(r1.w);
             first = left_near ? ubits(l0.w) : ubits(r0.w);
-            return false;
+            return kStepContinue;
         }
-        return pop();
+        return pop() ? kStepFinished : kStepContinue;
+    }
+
+    // Steps until the lane finishes or stops at a big leaf.
+    __device__ __forceinline__ StepResult advance(const GBlas& b, LaneRay& r, uint32_t big_leaf, uint32_t* err) {
+        for (;;) {
+            StepResult s = step(b, r, big_leaf, err);
+            if (s != kStepContinue) return s;
+        }
     }
 };
 
+// Whole traversal by one lane, every leaf tested by the lane itself.
 template <int STACK>
 __device__ __forceinline__ bool trace_blas(const GBlas& b, float3 o, float3 d, float3 rd, float& closest_t,
                                            float& hu, float& hv, uint32_t& hprim, uint32_t* err) {
     Trav<STACK> tr;
     tr.init(b);
-    bool hit = false;
-    while (!tr.step(b, o, d, rd, closest_t, hu, hv, hprim, hit, err)) {
+    LaneRay r;
+    r.o = o;
+    r.d = d;
+    r.rd = rd;
+    r.ct = closest_t;
+    r.hu = hu;
+    r.hv = hv;
+    r.hp = hprim;
+    r.hit = false;
+    tr.advance(b, r, 0xFFFFFFFFu, err);
+    closest_t = r.ct;
+    hu = r.hu;
+    hv = r.hv;
+    hprim = r.hp;
+    return r.hit;
+}
+
+// ---- warp-cooperative big-leaf test ------------------------------------------------------
+// All 32 lanes test the ray of lane `src` against the leaf [first, first + cnt): lane k takes
+// triangles first + k, first + k + 32, ... (coalesced loads), keeps its first strictly
+// smallest t below the ray's closest t, and the warp reduces to the minimum t with ties
+// going to the lowest triangle index -- exactly the triangle the reference's sequential
+// loop (bvh.rs:250-258, strict `<` in index order) keeps.  Lane `src` then takes the hit.
+// Must be called by all 32 lanes with the same src / first / cnt / tris.
+__device__ __forceinline__ void coop_leaf(const float4* __restrict__ tris, uint32_t first, uint32_t cnt, int src,
+                                          LaneRay& r) {
+    const unsigned kAll = 0xFFFFFFFFu;
+    const unsigned lane = threadIdx.x & 31u;
+    float3 o, d;
+    o.x = __shfl_sync(kAll, r.o.x, src);
+    o.y = __shfl_sync(kAll, r.o.y, src);
+    o.z = __shfl_sync(kAll, r.o.z, src);
+    d.x = __shfl_sync(kAll, r.d.x, src);
+    d.y = __shfl_sync(kAll, r.d.y, src);
+    d.z = __shfl_sync(kAll, r.d.z, src);
+    const float ct = __shfl_sync(kAll, r.ct, src);
+    float bt = ct, bu = 0.0f, bv = 0.0f;
+    uint32_t bk = 0xFFFFFFFFu;
+    const float4* T = tris + 3ull * first;
+#pragma unroll 2
+    for (uint32_t k = lane; k < cnt; k += 32u) {
+        float4 a = __ldg(T + 3ull * k);
+        float4 e1 = __ldg(T + 3ull * k + 1);
+        float4 e2 = __ldg(T + 3ull * k + 2);
+        float t, u, v;
+        if (tri_test(a, e1, e2, o, d, t, u, v) && t < bt) {
+            bt = t;
+            bu = u;
+            bv = v;
+            bk = k;
+        }
     }
-    return hit;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        float ot = __shfl_xor_sync(kAll, bt, off);
+        uint32_t ok = __shfl_xor_sync(kAll, bk, off);
+        if (ok != 0xFFFFFFFFu && (bk == 0xFFFFFFFFu || ot < bt || (ot == bt && ok < bk))) {
+            bt = ot;
+            bk = ok;
+        }
+    }
+    if (bk != 0xFFFFFFFFu) {
+        float wu = __shfl_sync(kAll, bu, (int)(bk & 31u));
+        float wv = __shfl_sync(kAll, bv, (int)(bk & 31u));
+        if ((int)lane == src) {
+            r.ct = bt;
+            r.hu = wu;
+            r.hv = wv;
+            r.hp = first + bk;
+            r.hit = true;
+        }
+    }
 }
 
 __device__ __forceinline__ void load_ray(const float4* rays, uint32_t i, float3& o, float3& d, float& t) {

@@ -37,13 +37,22 @@ __device__ __forceinline__ float max_ni(float a, float b) {
     return (b > a) ? b : a;
 }
 
-__global__ void k_write_tris(const float* __restrict__ tris9, uint32_t n, float4* __restrict__ out) {
+// Writes the traversal layout {v0, e1 = v1 - v0, e2 = v2 - v0} (the subtractions of
+// triangle.rs:44-45, so no bit changes) and the raw vertices used by refit.
+__global__ void k_write_tris(const float* __restrict__ tris9, uint32_t n, float4* __restrict__ out,
+                             float4* __restrict__ verts) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float* t = tris9 + 9ull * i;
-    out[3ull * i] = make_float4(t[0], t[1], t[2], 0.0f);
-    out[3ull * i + 1] = make_float4(t[3], t[4], t[5], 0.0f);
-    out[3ull * i + 2] = make_float4(t[6], t[7], t[8], 0.0f);
+    float4 v0 = make_float4(t[0], t[1], t[2], 0.0f);
+    float4 v1 = make_float4(t[3], t[4], t[5], 0.0f);
+    float4 v2 = make_float4(t[6], t[7], t[8], 0.0f);
+    out[3ull * i] = v0;
+    out[3ull * i + 1] = make_float4(fsub(v1.x, v0.x), fsub(v1.y, v0.y), fsub(v1.z, v0.z), 0.0f);
+    out[3ull * i + 2] = make_float4(fsub(v2.x, v0.x), fsub(v2.y, v0.y), fsub(v2.z, v0.z), 0.0f);
+    verts[3ull * i] = v0;
+    verts[3ull * i + 1] = v1;
+    verts[3ull * i + 2] = v2;
 }
 
 __global__ void __launch_bounds__(kBlock) k_refit(float4* nodes, const float4* __restrict__ tris,
@@ -330,7 +339,7 @@ inline unsigned grid_for(uint32_t n, int block) { return (unsigned)((n + block -
 cudaError_t launch_write_tris(bvhgpu_ctx* ctx, DeviceBlas& b, const float* d_tris9, cudaStream_t s) {
     if (b.ntris == 0) return cudaSuccess;
     LaunchScope scope(ctx, BVHGPU_K_OTHER, s);
-    k_write_tris<<<grid_for(b.ntris, 256), 256, 0, s>>>(d_tris9, b.ntris, b.tris);
+    k_write_tris<<<grid_for(b.ntris, 256), 256, 0, s>>>(d_tris9, b.ntris, b.tris, b.verts);
     g_launches++;
     return cudaGetLastError();
 }
@@ -338,7 +347,7 @@ cudaError_t launch_write_tris(bvhgpu_ctx* ctx, DeviceBlas& b, const float* d_tri
 cudaError_t launch_refit(bvhgpu_ctx* ctx, DeviceBlas& b, cudaStream_t s) {
     if (b.nleaves == 0) return cudaSuccess;
     LaunchScope scope(ctx, BVHGPU_K_REFIT, s);
-    k_refit<<<grid_for(b.nleaves, kBlock), kBlock, 0, s>>>(b.nodes, b.tris, b.leaves, b.nleaves, b.parent,
+    k_refit<<<grid_for(b.nleaves, kBlock), kBlock, 0, s>>>(b.nodes, b.verts, b.leaves, b.nleaves, b.parent,
                                                            b.counters);
     g_launches++;
     return cudaGetLastError();

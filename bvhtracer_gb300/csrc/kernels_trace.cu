@@ -21,6 +21,9 @@ namespace {
 
 constexpr int kBlock = 128;
 constexpr unsigned kFull = 0xFFFFFFFFu;
+// Leaves with more triangles than this are tested by the whole warp (coop_leaf); smaller
+// ones by the lane that reached them.
+constexpr uint32_t kBigLeaf = 16;
 
 inline GBlas to_gblas(const DeviceBlas& b) {
     GBlas g;
@@ -43,22 +46,74 @@ inline int stack_variant(uint32_t depth) {
 
 inline unsigned grid_for(uint32_t n, int block) { return (unsigned)((n + block - 1) / block); }
 
+// ---- warp-synchronous traversal ----------------------------------------------------------
+// Every lane walks its own ray through the interior nodes (and tests small leaves itself);
+// a leaf with more than `big_leaf` triangles is tested by the whole warp together
+// (coop_leaf), one waiting ray at a time.  All 32 lanes stay in the loop until every ray of
+// the warp has finished, so the cooperative step always has the full warp.
+
+// Lane-level state machine of the traversal loop.
+template <int STACK>
+__device__ __forceinline__ void coop_leaf_phase(unsigned pend, const GBlas& b, Trav<STACK>& tr, LaneRay& r,
+                                                StepResult& st) {
+    const unsigned lane = threadIdx.x & 31u;
+    while (pend) {
+        int src = __ffs(pend) - 1;
+        pend &= pend - 1u;
+        uint32_t f = __shfl_sync(kFull, tr.first, src);
+        uint32_t c = __shfl_sync(kFull, tr.cnt, src);
+        coop_leaf(b.tris, f, c, src, r);
+        if ((int)lane == src) st = tr.pop() ? kStepFinished : kStepContinue;
+    }
+}
+
+// Traces the rays of one warp (inactive lanes take part in the cooperative steps only).
+template <int STACK>
+__device__ __forceinline__ void warp_trace(const GBlas& b, bool active, LaneRay& r, uint32_t big_leaf,
+                                           uint32_t* err) {
+    Trav<STACK> tr;
+    if (active) tr.init(b);
+    StepResult st = active ? kStepContinue : kStepFinished;
+    for (;;) {
+        if (st == kStepContinue) st = tr.advance(b, r, big_leaf, err);
+        unsigned pend = __ballot_sync(kFull, st == kStepBigLeaf);
+        if (pend == 0u) break;
+        coop_leaf_phase<STACK>(pend, b, tr, r, st);
+    }
+}
+
+__device__ __forceinline__ void init_lane_ray(LaneRay& r, float3 o, float3 d, float t) {
+    r.o = o;
+    r.d = d;
+    r.rd = recip3(d);
+    r.ct = t;
+    r.hu = r.hv = 0.0f;
+    r.hp = 0;
+    r.hit = false;
+}
+
 // ---- plain -------------------------------------------------------------------------------
 
+// One thread per ray.  `count` (device, may be null) overrides n; `out_index` (may be null)
+// maps ray i to its hit slot (the compacted bounce queue writes hits at pixel positions).
 template <int STACK>
 __global__ void __launch_bounds__(kBlock) k_trace_blas(GBlas b, const float4* __restrict__ rays, uint32_t n,
-                                                       GHit* __restrict__ hits, uint32_t* err) {
+                                                       const uint32_t* count, const uint32_t* __restrict__ out_index,
+                                                       GHit* __restrict__ hits, uint32_t big_leaf, uint32_t* err) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    float3 o, d;
-    float t;
-    load_ray(rays, i, o, d, t);
-    float3 rd = recip3(d);
-    float hu = 0.0f, hv = 0.0f;
-    uint32_t hp = 0;
-    bool hit = trace_blas<STACK>(b, o, d, rd, t, hu, hv, hp, err);
+    if (count) n = *count;
+    if (__all_sync(kFull, i >= n)) return;  // whole warp idle
+    bool active = i < n;
+    LaneRay r;
+    if (active) {
+        float3 o, d;
+        float t;
+        load_ray(rays, i, o, d, t);
+        init_lane_ray(r, o, d, t);
+    }
+    warp_trace<STACK>(b, active, r, big_leaf, err);
     // bvh.rs:295: a hit needs closest_ray.t < f32::MAX as well.
-    store_hit(hits, i, hit && t < FLT_MAX, t, hu, hv, hp, 0u);
+    if (active) store_hit(hits, out_index ? out_index[i] : i, r.hit && r.ct < FLT_MAX, r.ct, r.hu, r.hv, r.hp, 0u);
 }
 
 // Bounce generation with warp-aggregated compaction: one atomicAdd per warp appends the
@@ -78,10 +133,7 @@ __global__ void __launch_bounds__(kBlock) k_bounce_gen(GBlas b, const float4* __
             float t0;
             load_ray(rays, i, o, d, t0);
             const float4* T = b.tris + 3ull * h.prim;
-            float4 v0 = __ldg(T), v1 = __ldg(T + 1), v2 = __ldg(T + 2);
-            float4 e1 = make_float4(fsub(v1.x, v0.x), fsub(v1.y, v0.y), fsub(v1.z, v0.z), 0.f);
-            float4 e2 = make_float4(fsub(v2.x, v0.x), fsub(v2.y, v0.y), fsub(v2.z, v0.z), 0.f);
-            have = bounce_dir(o, d, h.t, v0, e1, e2, seed, i, po, pd);
+            have = bounce_dir(o, d, h.t, __ldg(T), __ldg(T + 1), __ldg(T + 2), seed, i, po, pd);
         }
     }
     unsigned mask = __ballot_sync(kFull, have);
@@ -99,22 +151,6 @@ __global__ void __launch_bounds__(kBlock) k_bounce_gen(GBlas b, const float4* __
     }
 }
 
-template <int STACK>
-__global__ void __launch_bounds__(kBlock) k_trace_queue(GBlas b, const float4* __restrict__ qrays,
-                                                        const uint32_t* __restrict__ qpix, const uint32_t* qcount,
-                                                        GHit* __restrict__ hits, uint32_t* err) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= *qcount) return;
-    float3 o, d;
-    float t;
-    load_ray(qrays, i, o, d, t);
-    float3 rd = recip3(d);
-    float hu = 0.0f, hv = 0.0f;
-    uint32_t hp = 0;
-    bool hit = trace_blas<STACK>(b, o, d, rd, t, hu, hv, hp, err);
-    store_hit(hits, qpix[i], hit && t < FLT_MAX, t, hu, hv, hp, 0u);
-}
-
 // Bounce rays in pixel order (for checking the bounce generation against the oracle).
 __global__ void k_bounce_rays(GBlas b, const float4* __restrict__ rays, const GHit* __restrict__ hits0, uint32_t n,
                               uint32_t seed, float4* __restrict__ out, uint8_t* __restrict__ valid) {
@@ -128,10 +164,7 @@ __global__ void k_bounce_rays(GBlas b, const float4* __restrict__ rays, const GH
         float t0;
         load_ray(rays, i, o, d, t0);
         const float4* T = b.tris + 3ull * h.prim;
-        float4 v0 = __ldg(T), v1 = __ldg(T + 1), v2 = __ldg(T + 2);
-        float4 e1 = make_float4(fsub(v1.x, v0.x), fsub(v1.y, v0.y), fsub(v1.z, v0.z), 0.f);
-        float4 e2 = make_float4(fsub(v2.x, v0.x), fsub(v2.y, v0.y), fsub(v2.z, v0.z), 0.f);
-        have = bounce_dir(o, d, h.t, v0, e1, e2, seed, i, po, pd);
+        have = bounce_dir(o, d, h.t, __ldg(T), __ldg(T + 1), __ldg(T + 2), seed, i, po, pd);
     }
     out[2ull * i] = make_float4(po.x, po.y, po.z, FLT_MAX);
     out[2ull * i + 1] = make_float4(pd.x, pd.y, pd.z, 0.0f);
@@ -139,25 +172,22 @@ __global__ void k_bounce_rays(GBlas b, const float4* __restrict__ rays, const GH
 }
 
 // ---- persistent: primary + bounce in one launch -------------------------------------------
-
-// Lanes are refilled when fewer than this many of the warp's 32 lanes still have work.
-constexpr int kRefillBelow = 24;
+// Each warp keeps 32 ray slots.  A slot whose ray finished is refilled from the global queue
+// (ballot -> one atomicAdd per warp -> shfl); a primary that hit continues in the same slot
+// with its bounce ray, so no compaction pass and no second launch are needed.
 
 template <int STACK>
 __global__ void __launch_bounds__(kBlock) k_persistent_bounce(GBlas b, const float4* __restrict__ rays, uint32_t n,
                                                               uint32_t seed, GHit* __restrict__ hits0,
                                                               GHit* __restrict__ hits1, uint32_t* queue,
-                                                              uint32_t* err) {
+                                                              uint32_t big_leaf, uint32_t* err) {
     const unsigned lane = threadIdx.x & 31u;
-    // phase: 0 needs work, 1 primary ray, 2 bounce ray, 3 retired
-    int phase = 0;
+    int phase = 0;  // 0 needs work, 1 primary ray, 2 bounce ray, 3 retired
     uint32_t idx = 0;
-    float3 o = make_float3(0, 0, 0), d = o, rd = o;
-    float ct = 0.0f, hu = 0.0f, hv = 0.0f;
-    uint32_t hp = 0;
-    bool hit = false;
-    bool queue_open = true;
+    LaneRay r;
     Trav<STACK> tr;
+    StepResult st = kStepFinished;
+    bool queue_open = true;
     for (;;) {
         unsigned need = __ballot_sync(kFull, phase == 0);
         if (need != 0u) {
@@ -165,69 +195,56 @@ __global__ void __launch_bounds__(kBlock) k_persistent_bounce(GBlas b, const flo
             uint32_t base = 0;
             if ((int)lane == leader) base = atomicAdd(queue, (uint32_t)__popc(need));
             base = __shfl_sync(kFull, base, leader);
-            if (base + (uint32_t)__popc(need) > n) queue_open = false;
+            if (base + (uint32_t)__popc(need) >= n) queue_open = false;
             if (phase == 0) {
                 uint32_t my = base + __popc(need & ((1u << lane) - 1u));
                 if (my < n) {
                     idx = my;
+                    float3 o, d;
                     float t0;
                     load_ray(rays, idx, o, d, t0);
-                    rd = recip3(d);
-                    ct = t0;
-                    hu = hv = 0.0f;
-                    hp = 0;
-                    hit = false;
+                    init_lane_ray(r, o, d, t0);
                     tr.init(b);
+                    st = kStepContinue;
                     phase = 1;
                 } else {
                     phase = 3;
                 }
             }
         }
-        unsigned busy = __ballot_sync(kFull, phase == 1 || phase == 2);
-        if (busy == 0u) {
-            if (!queue_open) break;
+        // advance this lane; finished rays are completed (a primary hit starts its bounce)
+        while (phase == 1 || phase == 2) {
+            if (st == kStepContinue) st = tr.advance(b, r, big_leaf, err);
+            if (st != kStepFinished) break;
+            bool h = r.hit && r.ct < FLT_MAX;
+            if (phase == 2) {
+                store_hit(hits1, idx, h, r.ct, r.hu, r.hv, r.hp, 0u);
+                phase = 0;
+                break;
+            }
+            store_hit(hits0, idx, h, r.ct, r.hu, r.hv, r.hp, 0u);
+            float3 po, pd;
+            bool have = false;
+            if (h) {
+                const float4* T = b.tris + 3ull * r.hp;
+                have = bounce_dir(r.o, r.d, r.ct, __ldg(T), __ldg(T + 1), __ldg(T + 2), seed, idx, po, pd);
+            }
+            if (!have) {
+                store_hit(hits1, idx, false, 0, 0, 0, 0, 0);
+                phase = 0;
+                break;
+            }
+            init_lane_ray(r, po, pd, FLT_MAX);
+            tr.init(b);
+            st = kStepContinue;
+            phase = 2;
+        }
+        unsigned pend = __ballot_sync(kFull, (phase == 1 || phase == 2) && st == kStepBigLeaf);
+        if (pend == 0u) {
+            if (!queue_open && __ballot_sync(kFull, phase == 0 || phase == 1 || phase == 2) == 0u) break;
             continue;
         }
-        for (;;) {
-            if (phase == 1 || phase == 2) {
-                if (tr.step(b, o, d, rd, ct, hu, hv, hp, hit, err)) {
-                    bool h = hit && ct < FLT_MAX;
-                    if (phase == 1) {
-                        store_hit(hits0, idx, h, ct, hu, hv, hp, 0u);
-                        float3 po, pd;
-                        bool have = false;
-                        if (h) {
-                            const float4* T = b.tris + 3ull * hp;
-                            float4 v0 = __ldg(T), v1 = __ldg(T + 1), v2 = __ldg(T + 2);
-                            float4 e1 = make_float4(fsub(v1.x, v0.x), fsub(v1.y, v0.y), fsub(v1.z, v0.z), 0.f);
-                            float4 e2 = make_float4(fsub(v2.x, v0.x), fsub(v2.y, v0.y), fsub(v2.z, v0.z), 0.f);
-                            have = bounce_dir(o, d, ct, v0, e1, e2, seed, idx, po, pd);
-                        }
-                        if (have) {
-                            o = po;
-                            d = pd;
-                            rd = recip3(d);
-                            ct = FLT_MAX;
-                            hu = hv = 0.0f;
-                            hp = 0;
-                            hit = false;
-                            tr.init(b);
-                            phase = 2;
-                        } else {
-                            store_hit(hits1, idx, false, 0, 0, 0, 0, 0);
-                            phase = 0;
-                        }
-                    } else {
-                        store_hit(hits1, idx, h, ct, hu, hv, hp, 0u);
-                        phase = 0;
-                    }
-                }
-            }
-            unsigned act = __ballot_sync(kFull, phase == 1 || phase == 2);
-            if (act == 0u) break;
-            if (queue_open && __popc(act) < kRefillBelow) break;
-        }
+        coop_leaf_phase<STACK>(pend, b, tr, r, st);
     }
 }
 
@@ -240,12 +257,19 @@ struct BatchEntry {
     uint32_t pad0, pad1;
 };
 
+__device__ __forceinline__ const float4* shfl_ptr(const float4* p, int src) {
+    unsigned long long v = reinterpret_cast<unsigned long long>(p);
+    unsigned lo = __shfl_sync(kFull, (unsigned)(v & 0xFFFFFFFFull), src);
+    unsigned hi = __shfl_sync(kFull, (unsigned)(v >> 32), src);
+    return reinterpret_cast<const float4*>((unsigned long long)lo | ((unsigned long long)hi << 32));
+}
+
 template <int STACK>
 __global__ void __launch_bounds__(kBlock) k_trace_batch_persistent(const BatchEntry* __restrict__ table,
                                                                    uint32_t nitems, uint32_t total,
                                                                    const float4* __restrict__ rays,
                                                                    GHit* __restrict__ hits, uint32_t* queue,
-                                                                   uint32_t* err) {
+                                                                   uint32_t big_leaf, uint32_t* err) {
     const unsigned lane = threadIdx.x & 31u;
     int phase = 0;  // 0 needs work, 1 tracing, 3 retired
     uint32_t ray = 0;
@@ -253,12 +277,10 @@ __global__ void __launch_bounds__(kBlock) k_trace_batch_persistent(const BatchEn
     b.nodes = nullptr;
     b.tris = nullptr;
     b.nodes_used = b.ntris = b.root_count = b.root_first = 0;
-    float3 o = make_float3(0, 0, 0), d = o, rd = o;
-    float ct = 0.0f, hu = 0.0f, hv = 0.0f;
-    uint32_t hp = 0;
-    bool hit = false;
-    bool queue_open = true;
+    LaneRay r;
     Trav<STACK> tr;
+    StepResult st = kStepFinished;
+    bool queue_open = true;
     for (;;) {
         unsigned need = __ballot_sync(kFull, phase == 0);
         if (need != 0u) {
@@ -266,53 +288,49 @@ __global__ void __launch_bounds__(kBlock) k_trace_batch_persistent(const BatchEn
             uint32_t base = 0;
             if ((int)lane == leader) base = atomicAdd(queue, (uint32_t)__popc(need));
             base = __shfl_sync(kFull, base, leader);
-            if (base + (uint32_t)__popc(need) > total) queue_open = false;
+            if (base + (uint32_t)__popc(need) >= total) queue_open = false;
             if (phase == 0) {
                 uint32_t w = base + __popc(need & ((1u << lane) - 1u));
                 if (w < total) {
-                    // binary search: last item with work_begin <= w
-                    uint32_t lo = 0, hi = nitems;
+                    uint32_t lo = 0, hi = nitems;  // last item with work_begin <= w
                     while (hi - lo > 1) {
                         uint32_t mid = (lo + hi) >> 1;
                         if (__ldg(&table[mid].work_begin) <= w) lo = mid; else hi = mid;
                     }
-                    const BatchEntry& e = table[lo];
-                    b.nodes = e.blas.nodes;
-                    b.tris = e.blas.tris;
-                    b.nodes_used = e.blas.nodes_used;
-                    b.ntris = e.blas.ntris;
-                    b.root_count = e.blas.root_count;
-                    b.root_first = e.blas.root_first;
-                    ray = e.ray_offset + (w - e.work_begin);
+                    b = table[lo].blas;
+                    ray = table[lo].ray_offset + (w - table[lo].work_begin);
+                    float3 o, d;
                     float t0;
                     load_ray(rays, ray, o, d, t0);
-                    rd = recip3(d);
-                    ct = t0;
-                    hu = hv = 0.0f;
-                    hp = 0;
-                    hit = false;
+                    init_lane_ray(r, o, d, t0);
                     tr.init(b);
+                    st = kStepContinue;
                     phase = 1;
                 } else {
                     phase = 3;
                 }
             }
         }
-        unsigned busy = __ballot_sync(kFull, phase == 1);
-        if (busy == 0u) {
-            if (!queue_open) break;
+        if (phase == 1) {
+            if (st == kStepContinue) st = tr.advance(b, r, big_leaf, err);
+            if (st == kStepFinished) {
+                store_hit(hits, ray, r.hit && r.ct < FLT_MAX, r.ct, r.hu, r.hv, r.hp, 0u);
+                phase = 0;
+            }
+        }
+        unsigned pend = __ballot_sync(kFull, phase == 1 && st == kStepBigLeaf);
+        if (pend == 0u) {
+            if (!queue_open && __ballot_sync(kFull, phase == 0 || phase == 1) == 0u) break;
             continue;
         }
-        for (;;) {
-            if (phase == 1) {
-                if (tr.step(b, o, d, rd, ct, hu, hv, hp, hit, err)) {
-                    store_hit(hits, ray, hit && ct < FLT_MAX, ct, hu, hv, hp, 0u);
-                    phase = 0;
-                }
-            }
-            unsigned act = __ballot_sync(kFull, phase == 1);
-            if (act == 0u) break;
-            if (queue_open && __popc(act) < kRefillBelow) break;
+        while (pend) {
+            int src = __ffs(pend) - 1;
+            pend &= pend - 1u;
+            const float4* T = shfl_ptr(b.tris, src);
+            uint32_t f = __shfl_sync(kFull, tr.first, src);
+            uint32_t c = __shfl_sync(kFull, tr.cnt, src);
+            coop_leaf(T, f, c, src, r);
+            if ((int)lane == src) st = tr.pop() ? kStepFinished : kStepContinue;
         }
     }
 }
@@ -357,12 +375,12 @@ __device__ __forceinline__ int32_t f32_as_i32(float x) {  // Rust `as i32`: satu
 // goes through the pixel's top-left corner u = x / w, v = y / h (renderer.rs:358-361).
 template <int STACK>
 __global__ void __launch_bounds__(64) k_render(GBlas b, RenderParams P, const float* __restrict__ normals,
-                                               uint8_t* __restrict__ rgba, uint32_t* err) {
+                                               uint8_t* __restrict__ rgba, uint32_t big_leaf, uint32_t* err) {
     const int tiles_x = (P.width + 7) / 8;
     const int tile = blockIdx.x;
     const int x = (tile % tiles_x) * 8 + (threadIdx.x & 7);
     const int y = (tile / tiles_x) * 8 + (threadIdx.x >> 3);
-    if (x >= P.width || y >= P.height) return;
+    const bool active = x < P.width && y < P.height;  // all lanes stay for the cooperative leaf steps
     const float* C = P.cam;
     float u = __fdiv_rn((float)x, (float)P.width);
     float v = __fdiv_rn((float)y, (float)P.height);
@@ -378,10 +396,13 @@ __global__ void __launch_bounds__(64) k_render(GBlas b, RenderParams P, const fl
     // Camera::get_ray_world (camera.rs:1004-1010)
     float3 o = xf_point(C + 9, org);
     float3 d = xf_vector(C + 9, dir);
-    float3 rd = recip3(d);
-    float t = FLT_MAX, hu = 0.0f, hv = 0.0f;
-    uint32_t hp = 0;
-    bool hit = trace_blas<STACK>(b, o, d, rd, t, hu, hv, hp, err) && t < FLT_MAX;
+    LaneRay lr;
+    init_lane_ray(lr, o, d, FLT_MAX);
+    warp_trace<STACK>(b, active, lr, big_leaf, err);
+    if (!active) return;
+    const float t = lr.ct, hu = lr.hu, hv = lr.hv;
+    const uint32_t hp = lr.hp;
+    const bool hit = lr.hit && t < FLT_MAX;
     float3 rad = make_float3(0.0f, 0.0f, 0.0f);
     switch (P.acc_kind) {
         case BVHGPU_ACC_INTERSECTION:  // renderer.rs:145-153
@@ -461,7 +482,7 @@ cudaError_t launch_trace_blas(bvhgpu_ctx* ctx, const DeviceBlas& b, const float4
     GBlas g = to_gblas(b);
     LaunchScope scope(ctx, BVHGPU_K_TRACE_BLAS, s);
     BVHGPU_DISPATCH_STACK(b.depth, (k_trace_blas<S><<<grid_for(n, kBlock), kBlock, 0, s>>>(
-                                       g, rays, n, static_cast<GHit*>(hits), ctx->d_err)));
+                                       g, rays, n, nullptr, nullptr, static_cast<GHit*>(hits), kBigLeaf, ctx->d_err)));
     g_launches++;
     return cudaGetLastError();
 }
@@ -486,9 +507,9 @@ cudaError_t launch_bounce_plain(bvhgpu_ctx* ctx, const DeviceBlas& b, const floa
     if (e != cudaSuccess) return e;
     {
         LaunchScope scope(ctx, BVHGPU_K_TRACE_QUEUE, s);
-        BVHGPU_DISPATCH_STACK(b.depth, (k_trace_queue<S><<<grid_for(n, kBlock), kBlock, 0, s>>>(
-                                           g, static_cast<const float4*>(ctx->bounce_rays), ctx->bounce_pix, qcount,
-                                           static_cast<GHit*>(hits1), ctx->d_err)));
+        BVHGPU_DISPATCH_STACK(b.depth, (k_trace_blas<S><<<grid_for(n, kBlock), kBlock, 0, s>>>(
+                                           g, static_cast<const float4*>(ctx->bounce_rays), n, qcount, ctx->bounce_pix,
+                                           static_cast<GHit*>(hits1), kBigLeaf, ctx->d_err)));
         g_launches++;
     }
     return cudaGetLastError();
@@ -505,7 +526,7 @@ cudaError_t launch_bounce_persistent(bvhgpu_ctx* ctx, const DeviceBlas& b, const
     BVHGPU_DISPATCH_STACK(b.depth, {
         int grid = persistent_grid(ctx, (const void*)k_persistent_bounce<S>);
         k_persistent_bounce<S><<<grid, kBlock, 0, s>>>(g, rays, n, seed, static_cast<GHit*>(hits0),
-                                                         static_cast<GHit*>(hits1), queue, ctx->d_err);
+                                                         static_cast<GHit*>(hits1), queue, kBigLeaf, ctx->d_err);
     });
     g_launches++;
     return cudaGetLastError();
@@ -579,7 +600,8 @@ cudaError_t launch_trace_batch(bvhgpu_ctx* ctx, const std::vector<const DeviceBl
     BVHGPU_DISPATCH_STACK(ctx->batch_depth, {
         int grid = persistent_grid(ctx, (const void*)k_trace_batch_persistent<S>);
         k_trace_batch_persistent<S><<<grid, kBlock, 0, s>>>(static_cast<const BatchEntry*>(ctx->batch_table), nitems,
-                                                            total, rays, static_cast<GHit*>(hits), queue, ctx->d_err);
+                                                            total, rays, static_cast<GHit*>(hits), queue, kBigLeaf,
+                                                            ctx->d_err);
     });
     g_launches++;
     return cudaGetLastError();
@@ -606,7 +628,7 @@ cudaError_t launch_render(bvhgpu_ctx* ctx, const DeviceBlas& b, const bvhgpu_cam
     GBlas g = to_gblas(b);
     unsigned tiles = (unsigned)(((w + 7) / 8) * ((h + 7) / 8));
     LaunchScope scope(ctx, BVHGPU_K_RENDER, s);
-    BVHGPU_DISPATCH_STACK(b.depth, (k_render<S><<<tiles, 64, 0, s>>>(g, P, d_normals, d_rgba, ctx->d_err)));
+    BVHGPU_DISPATCH_STACK(b.depth, (k_render<S><<<tiles, 64, 0, s>>>(g, P, d_normals, d_rgba, kBigLeaf, ctx->d_err)));
     g_launches++;
     return cudaGetLastError();
 }

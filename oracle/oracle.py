@@ -23,7 +23,7 @@ LIB_PATH = os.path.join(HERE, "_build", "liborc.so")
 
 NODE = np.dtype([("bounds_min", "<f4", 3), ("bounds_max", "<f4", 3),
                  ("primitive_count", "<u4"), ("left_first", "<u4")])
-RAY = np.dtype([("origin", "<f4", 3), ("t", "<f4"), ("direction", "<f4", 3), ("pad", "<u4")])
+RAY = np.dtype([("origin", "<f4", 3), ("t", "<f4"), ("direction", "<f4", 3), ("reserved", "<u4")])
 HIT = np.dtype([("t", "<f4"), ("u", "<f4"), ("v", "<f4"), ("prim", "<u4"), ("inst", "<u4")])
 TLAS_NODE = np.dtype([("bounds_min", "<f4", 3), ("bounds_max", "<f4", 3),
                       ("left_right", "<u4"), ("blas", "<u4")])

@@ -326,23 +326,26 @@ def test_invalid_inputs_are_rejected(ctx):
 
 def test_stack_overflow_is_reported_not_faulted(ctx):
     # A valid but degenerate tree deeper than the largest compiled stack (256): a chain of
-    # nested identical boxes whose far child is always pushed.
+    # nested identical boxes whose far child is always pushed (the leaf triangles lie off the
+    # ray, so no hit ever shrinks the ray and culls the chain).
     depth = 300
     nodes = np.zeros(2 * depth + 2, bt.NODE)
-    tri = np.array([[-1, -1, 0, 1, -1, 0, 0, 1, 0]], np.float32)
+    tri = np.array([[5, 5, 0, 6, 5, 0, 5, 6, 0]], np.float32)
     tris = np.repeat(tri, depth + 1, axis=0)
     box_min, box_max = np.array([-1, -1, 0], np.float32), np.array([1, 1, 0], np.float32)
     used = 2
     cur = 0
     for lvl in range(depth):
+        # equal entry distances send the traversal to the right child first (bvh.rs:271-275),
+        # so the chain continues on the right and every left leaf is pushed
         l, r = used, used + 1
         used += 2
         nodes[cur]["left_first"] = l
         nodes[cur]["primitive_count"] = 0
         nodes[cur]["bounds_min"], nodes[cur]["bounds_max"] = box_min, box_max
-        nodes[r]["left_first"], nodes[r]["primitive_count"] = lvl, 1
-        nodes[r]["bounds_min"], nodes[r]["bounds_max"] = box_min, box_max
-        cur = l
+        nodes[l]["left_first"], nodes[l]["primitive_count"] = lvl, 1
+        nodes[l]["bounds_min"], nodes[l]["bounds_max"] = box_min, box_max
+        cur = r
     nodes[cur]["left_first"], nodes[cur]["primitive_count"] = depth, 1
     nodes[cur]["bounds_min"], nodes[cur]["bounds_max"] = box_min, box_max
     blas = ctx.upload_blas(bt.Bvh(nodes, used), tris)
