@@ -114,6 +114,7 @@ void free_blas(DeviceBlas& b) {
     cudaFree(b.nodes);
     cudaFree(b.tris);
     cudaFree(b.verts);
+    cudaFree(b.pairs);
     cudaFree(b.parent);
     cudaFree(b.leaves);
     cudaFree(b.counters);
@@ -379,6 +380,7 @@ int bvhgpu_blas_upload(bvhgpu_ctx* ctx, const bvhgpu_node* nodes, uint32_t nodes
     if ((e = cudaMalloc(&b.nodes, 32ull * nodes_used)) != cudaSuccess ||
         (e = cudaMalloc(&b.tris, 48ull * ntris)) != cudaSuccess ||
         (e = cudaMalloc(&b.verts, 48ull * ntris)) != cudaSuccess ||
+        (e = cudaMalloc(&b.pairs, 80ull * ((ntris + 1) / 2))) != cudaSuccess ||
         (e = cudaMalloc(&b.parent, 4ull * nodes_used)) != cudaSuccess ||
         (e = cudaMalloc(&b.leaves, 4ull * std::max<size_t>(1, leaves.size()))) != cudaSuccess ||
         (e = cudaMalloc(&b.counters, 4ull * nodes_used)) != cudaSuccess ||
@@ -390,6 +392,7 @@ int bvhgpu_blas_upload(bvhgpu_ctx* ctx, const bvhgpu_node* nodes, uint32_t nodes
         (e = cudaMemcpy(b.parent, parent.data(), 4ull * nodes_used, cudaMemcpyHostToDevice)) != cudaSuccess ||
         (e = cudaMemcpy(b.leaves, leaves.data(), 4ull * leaves.size(), cudaMemcpyHostToDevice)) != cudaSuccess ||
         (e = cudaMemset(b.counters, 0, 4ull * nodes_used)) != cudaSuccess ||
+        (e = cudaMemset(b.pairs, 0, 80ull * ((ntris + 1) / 2))) != cudaSuccess ||
         (e = cudaMemcpy(d_tris9, tris, 36ull * ntris, cudaMemcpyHostToDevice)) != cudaSuccess ||
         (e = launch_write_tris(ctx, b, static_cast<const float*>(d_tris9), ctx->stream)) != cudaSuccess ||
         (e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess) {
@@ -649,6 +652,7 @@ int bvhgpu_scene_create(bvhgpu_ctx* ctx, const uint32_t* blas_ids, uint32_t nobj
             GBlas g;
             g.nodes = b->nodes;
             g.tris = b->tris;
+            g.pairs = b->pairs;
             g.nodes_used = b->nodes_used;
             g.ntris = b->ntris;
             g.root_count = b->root_count;

@@ -26,6 +26,9 @@ constexpr float kThreshold = 0.0001f;  // num_traits::cast(0.0001_f64) (triangle
 struct GBlas {
     const float4* nodes;  // 2 float4 per node
     const float4* tris;   // 3 float4 per triangle: {v0, 0}, {e1 = v1 - v0, 0}, {e2 = v2 - v0, 0}
+    // Triangle pairs (2p, 2p+1) interleaved for packed f32x2 math: 20 floats per pair, component
+    // c of {v0x v0y v0z e1x e1y e1z e2x e2y e2z} of triangle 2p + h at float 2c + h.
+    const ulonglong2* pairs;
     uint32_t nodes_used;
     uint32_t ntris;
     uint32_t root_count;  // root node meta (node 0)
@@ -232,39 +235,110 @@ __device__ __forceinline__ bool trace_blas(const GBlas& b, float3 o, float3 d, f
     return r.hit;
 }
 
+// ---- packed f32x2 arithmetic (Blackwell) ---------------------------------------------------
+// add/sub/mul.rn.f32x2 operate on two IEEE binary32 values with round-to-nearest each, i.e.
+// exactly two of the scalar __fadd_rn / __fsub_rn / __fmul_rn above; no multiply-add is fused.
+typedef unsigned long long f2;
+
+__device__ __forceinline__ f2 f2_add(f2 a, f2 b) {
+    f2 d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2 f2_sub(f2 a, f2 b) {
+    f2 d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+// Packed product RN(a*b) computed as fma.rn(a, b, z) with z = (-0, -0): a*b + (-0) is exactly a*b for
+// every input (signed zeros included), so the result equals __fmul_rn per element.  z is read at run
+// time so the compiler cannot prove it is -0: ptxas contracts a packed mul.rn.f32x2 that feeds an
+// add/sub into one fused multiply-add (even with --fmad=false), which would change the rounding.
+static __device__ unsigned long long g_neg_zero2 = 0x8000000080000000ull;
+__device__ __forceinline__ f2 f2_neg_zero() { return *reinterpret_cast<volatile unsigned long long*>(&g_neg_zero2); }
+__device__ __forceinline__ f2 f2_mul(f2 a, f2 b, f2 z) {
+    f2 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(z));
+    return d;
+}
+__device__ __forceinline__ f2 f2_pack(float lo, float hi) {
+    f2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ void f2_unpack(f2 v, float& lo, float& hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+
+// Moeller-Trumbore (triangle.rs:42-72) on the two triangles of a pair at once, every step in
+// the reference's order.  ok[h] is the reference's accept decision for triangle h.
+__device__ __forceinline__ void tri_test_pair(const ulonglong2* __restrict__ P, f2 OX, f2 OY, f2 OZ, f2 DX, f2 DY,
+                                              f2 DZ, f2 Z, bool okA_in, bool okB_in, bool& okA, bool& okB, float& tA,
+                                              float& tB, float& uA, float& uB, float& vA, float& vB) {
+    ulonglong2 q0 = __ldg(P), q1 = __ldg(P + 1), q2 = __ldg(P + 2), q3 = __ldg(P + 3), q4 = __ldg(P + 4);
+    const f2 V0X = q0.x, V0Y = q0.y, V0Z = q1.x, E1X = q1.y, E1Y = q2.x, E1Z = q2.y, E2X = q3.x, E2Y = q3.y,
+             E2Z = q4.x;
+    // n = cross(d, e2)
+    f2 NX = f2_sub(f2_mul(DY, E2Z, Z), f2_mul(DZ, E2Y, Z));
+    f2 NY = f2_sub(f2_mul(DZ, E2X, Z), f2_mul(DX, E2Z, Z));
+    f2 NZ = f2_sub(f2_mul(DX, E2Y, Z), f2_mul(DY, E2X, Z));
+    f2 A = f2_add(f2_add(f2_mul(E1X, NX, Z), f2_mul(E1Y, NY, Z)), f2_mul(E1Z, NZ, Z));
+    float aA, aB;
+    f2_unpack(A, aA, aB);
+    f2 F = f2_pack(__frcp_rn(aA), __frcp_rn(aB));
+    f2 SX = f2_sub(OX, V0X), SY = f2_sub(OY, V0Y), SZ = f2_sub(OZ, V0Z);
+    f2 U = f2_mul(F, f2_add(f2_add(f2_mul(SX, NX, Z), f2_mul(SY, NY, Z)), f2_mul(SZ, NZ, Z)), Z);
+    f2 QX = f2_sub(f2_mul(SY, E1Z, Z), f2_mul(SZ, E1Y, Z));
+    f2 QY = f2_sub(f2_mul(SZ, E1X, Z), f2_mul(SX, E1Z, Z));
+    f2 QZ = f2_sub(f2_mul(SX, E1Y, Z), f2_mul(SY, E1X, Z));
+    f2 V = f2_mul(F, f2_add(f2_add(f2_mul(DX, QX, Z), f2_mul(DY, QY, Z)), f2_mul(DZ, QZ, Z)), Z);
+    f2 T = f2_mul(F, f2_add(f2_add(f2_mul(E2X, QX, Z), f2_mul(E2Y, QY, Z)), f2_mul(E2Z, QZ, Z)), Z);
+    f2 UV = f2_add(U, V);
+    float uvA, uvB;
+    f2_unpack(U, uA, uB);
+    f2_unpack(V, vA, vB);
+    f2_unpack(T, tA, tB);
+    f2_unpack(UV, uvA, uvB);
+    okA = okA_in && !(fabsf(aA) < kThreshold) && !(uA < 0.0f || uA > 1.0f) && !(vA < 0.0f || uvA > 1.0f) &&
+          (tA > kThreshold);
+    okB = okB_in && !(fabsf(aB) < kThreshold) && !(uB < 0.0f || uB > 1.0f) && !(vB < 0.0f || uvB > 1.0f) &&
+          (tB > kThreshold);
+}
+
 // ---- warp-cooperative big-leaf test ------------------------------------------------------
 // All 32 lanes test the ray of lane `src` against the leaf [first, first + cnt): lane k takes
-// triangles first + k, first + k + 32, ... (coalesced loads), keeps its first strictly
-// smallest t below the ray's closest t, and the warp reduces to the minimum t with ties
-// going to the lowest triangle index -- exactly the triangle the reference's sequential
-// loop (bvh.rs:250-258, strict `<` in index order) keeps.  Lane `src` then takes the hit.
-// Must be called by all 32 lanes with the same src / first / cnt / tris.
-__device__ __forceinline__ void coop_leaf(const float4* __restrict__ tris, uint32_t first, uint32_t cnt, int src,
-                                          LaneRay& r) {
+// the triangle pairs pbeg + k, pbeg + k + 32, ... (coalesced 80-byte loads, two triangles per
+// packed instruction), keeps its first strictly smallest t below the ray's closest t, and the
+// warp reduces to the minimum t with ties going to the lowest triangle index -- exactly the
+// triangle the reference's sequential loop (bvh.rs:250-258, strict `<` in index order) keeps.
+// Lane `src` then takes the hit.  Must be called by all 32 lanes with the same arguments.
+__device__ __forceinline__ void coop_leaf(const ulonglong2* __restrict__ pairs, uint32_t first, uint32_t cnt,
+                                          int src, LaneRay& r) {
     const unsigned kAll = 0xFFFFFFFFu;
     const unsigned lane = threadIdx.x & 31u;
-    float3 o, d;
-    o.x = __shfl_sync(kAll, r.o.x, src);
-    o.y = __shfl_sync(kAll, r.o.y, src);
-    o.z = __shfl_sync(kAll, r.o.z, src);
-    d.x = __shfl_sync(kAll, r.d.x, src);
-    d.y = __shfl_sync(kAll, r.d.y, src);
-    d.z = __shfl_sync(kAll, r.d.z, src);
+    const float ox = __shfl_sync(kAll, r.o.x, src), oy = __shfl_sync(kAll, r.o.y, src),
+                oz = __shfl_sync(kAll, r.o.z, src);
+    const float dx = __shfl_sync(kAll, r.d.x, src), dy = __shfl_sync(kAll, r.d.y, src),
+                dz = __shfl_sync(kAll, r.d.z, src);
     const float ct = __shfl_sync(kAll, r.ct, src);
+    const f2 OX = f2_pack(ox, ox), OY = f2_pack(oy, oy), OZ = f2_pack(oz, oz);
+    const f2 DX = f2_pack(dx, dx), DY = f2_pack(dy, dy), DZ = f2_pack(dz, dz);
+    const f2 Z = f2_neg_zero();
+    const uint32_t end = first + cnt;
+    const uint32_t pbeg = first >> 1, pend = (end + 1) >> 1;
     float bt = ct, bu = 0.0f, bv = 0.0f;
     uint32_t bk = 0xFFFFFFFFu;
-    const float4* T = tris + 3ull * first;
-#pragma unroll 2
-    for (uint32_t k = lane; k < cnt; k += 32u) {
-        float4 a = __ldg(T + 3ull * k);
-        float4 e1 = __ldg(T + 3ull * k + 1);
-        float4 e2 = __ldg(T + 3ull * k + 2);
-        float t, u, v;
-        if (tri_test(a, e1, e2, o, d, t, u, v) && t < bt) {
-            bt = t;
-            bu = u;
-            bv = v;
-            bk = k;
+    for (uint32_t p = pbeg + lane; p < pend; p += 32u) {
+        const uint32_t kA = 2u * p, kB = kA + 1u;
+        bool okA, okB;
+        float tA, tB, uA, uB, vA, vB;
+        tri_test_pair(pairs + 5ull * p, OX, OY, OZ, DX, DY, DZ, Z, kA >= first, kB < end, okA, okB, tA, tB, uA,
+                      uB, vA, vB);
+        if (okA && tA < bt) {
+            bt = tA; bu = uA; bv = vA; bk = kA;
+        }
+        if (okB && tB < bt) {
+            bt = tB; bu = uB; bv = vB; bk = kB;
         }
     }
 #pragma unroll
@@ -277,13 +351,14 @@ __device__ __forceinline__ void coop_leaf(const float4* __restrict__ tris, uint3
         }
     }
     if (bk != 0xFFFFFFFFu) {
-        float wu = __shfl_sync(kAll, bu, (int)(bk & 31u));
-        float wv = __shfl_sync(kAll, bv, (int)(bk & 31u));
+        const int owner = (int)(((bk >> 1) - pbeg) & 31u);
+        float wu = __shfl_sync(kAll, bu, owner);
+        float wv = __shfl_sync(kAll, bv, owner);
         if ((int)lane == src) {
             r.ct = bt;
             r.hu = wu;
             r.hv = wv;
-            r.hp = first + bk;
+            r.hp = bk;
             r.hit = true;
         }
     }

@@ -20,6 +20,7 @@ struct DeviceBlas {
     float4* nodes = nullptr;     // 2 float4 per node (nodes_used nodes)
     float4* tris = nullptr;      // 3 float4 per triangle (v0, e1, e2): traversal layout
     float4* verts = nullptr;     // 3 float4 per triangle (v0, v1, v2): refit input
+    ulonglong2* pairs = nullptr; // 5 x 16 bytes per triangle pair: packed traversal layout
     uint32_t* parent = nullptr;  // parent index per node (refit), 0xFFFFFFFF for root/filler
     uint32_t* leaves = nullptr;  // indices of leaf nodes (refit start points)
     uint32_t* counters = nullptr;// refit arrival counters, one per node (kept zeroed)

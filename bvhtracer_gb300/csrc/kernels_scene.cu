@@ -40,7 +40,7 @@ __device__ __forceinline__ float max_ni(float a, float b) {
 // Writes the traversal layout {v0, e1 = v1 - v0, e2 = v2 - v0} (the subtractions of
 // triangle.rs:44-45, so no bit changes) and the raw vertices used by refit.
 __global__ void k_write_tris(const float* __restrict__ tris9, uint32_t n, float4* __restrict__ out,
-                             float4* __restrict__ verts) {
+                             float4* __restrict__ verts, float* __restrict__ pairs) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float* t = tris9 + 9ull * i;
@@ -53,6 +53,12 @@ __global__ void k_write_tris(const float* __restrict__ tris9, uint32_t n, float4
     verts[3ull * i] = v0;
     verts[3ull * i + 1] = v1;
     verts[3ull * i + 2] = v2;
+    // pair layout: component c of triangle i at float 20 * (i / 2) + 2c + (i & 1)
+    float c[9] = {v0.x, v0.y, v0.z, fsub(v1.x, v0.x), fsub(v1.y, v0.y), fsub(v1.z, v0.z),
+                  fsub(v2.x, v0.x), fsub(v2.y, v0.y), fsub(v2.z, v0.z)};
+    float* P = pairs + 20ull * (i >> 1) + (i & 1u);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) P[2 * k] = c[k];
 }
 
 __global__ void __launch_bounds__(kBlock) k_refit(float4* nodes, const float4* __restrict__ tris,
@@ -339,7 +345,8 @@ inline unsigned grid_for(uint32_t n, int block) { return (unsigned)((n + block -
 cudaError_t launch_write_tris(bvhgpu_ctx* ctx, DeviceBlas& b, const float* d_tris9, cudaStream_t s) {
     if (b.ntris == 0) return cudaSuccess;
     LaunchScope scope(ctx, BVHGPU_K_OTHER, s);
-    k_write_tris<<<grid_for(b.ntris, 256), 256, 0, s>>>(d_tris9, b.ntris, b.tris, b.verts);
+    k_write_tris<<<grid_for(b.ntris, 256), 256, 0, s>>>(d_tris9, b.ntris, b.tris, b.verts,
+                                                        reinterpret_cast<float*>(b.pairs));
     g_launches++;
     return cudaGetLastError();
 }

@@ -29,6 +29,7 @@ inline GBlas to_gblas(const DeviceBlas& b) {
     GBlas g;
     g.nodes = b.nodes;
     g.tris = b.tris;
+    g.pairs = b.pairs;
     g.nodes_used = b.nodes_used;
     g.ntris = b.ntris;
     g.root_count = b.root_count;
@@ -62,7 +63,7 @@ __device__ __forceinline__ void coop_leaf_phase(unsigned pend, const GBlas& b, T
         pend &= pend - 1u;
         uint32_t f = __shfl_sync(kFull, tr.first, src);
         uint32_t c = __shfl_sync(kFull, tr.cnt, src);
-        coop_leaf(b.tris, f, c, src, r);
+        coop_leaf(b.pairs, f, c, src, r);
         if ((int)lane == src) st = tr.pop() ? kStepFinished : kStepContinue;
     }
 }
@@ -257,11 +258,11 @@ struct BatchEntry {
     uint32_t pad0, pad1;
 };
 
-__device__ __forceinline__ const float4* shfl_ptr(const float4* p, int src) {
+__device__ __forceinline__ const ulonglong2* shfl_ptr(const ulonglong2* p, int src) {
     unsigned long long v = reinterpret_cast<unsigned long long>(p);
     unsigned lo = __shfl_sync(kFull, (unsigned)(v & 0xFFFFFFFFull), src);
     unsigned hi = __shfl_sync(kFull, (unsigned)(v >> 32), src);
-    return reinterpret_cast<const float4*>((unsigned long long)lo | ((unsigned long long)hi << 32));
+    return reinterpret_cast<const ulonglong2*>((unsigned long long)lo | ((unsigned long long)hi << 32));
 }
 
 template <int STACK>
@@ -276,6 +277,7 @@ __global__ void __launch_bounds__(kBlock) k_trace_batch_persistent(const BatchEn
     GBlas b;
     b.nodes = nullptr;
     b.tris = nullptr;
+    b.pairs = nullptr;
     b.nodes_used = b.ntris = b.root_count = b.root_first = 0;
     LaneRay r;
     Trav<STACK> tr;
@@ -326,7 +328,7 @@ __global__ void __launch_bounds__(kBlock) k_trace_batch_persistent(const BatchEn
         while (pend) {
             int src = __ffs(pend) - 1;
             pend &= pend - 1u;
-            const float4* T = shfl_ptr(b.tris, src);
+            const ulonglong2* T = shfl_ptr(b.pairs, src);
             uint32_t f = __shfl_sync(kFull, tr.first, src);
             uint32_t c = __shfl_sync(kFull, tr.cnt, src);
             coop_leaf(T, f, c, src, r);
