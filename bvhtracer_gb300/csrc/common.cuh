@@ -272,75 +272,106 @@ __device__ __forceinline__ void f2_unpack(f2 v, float& lo, float& hi) {
 
 // Moeller-Trumbore (triangle.rs:42-72) on the two triangles of a pair at once, every step in
 // the reference's order.  ok[h] is the reference's accept decision for triangle h.
-__device__ __forceinline__ void tri_test_pair(const ulonglong2* __restrict__ P, f2 OX, f2 OY, f2 OZ, f2 DX, f2 DY,
-                                              f2 DZ, f2 Z, bool okA_in, bool okB_in, bool& okA, bool& okB, float& tA,
-                                              float& tB, float& uA, float& uB, float& vA, float& vB) {
+// Moeller-Trumbore (triangle.rs:42-72) on the two triangles of a pair at once, every step in
+// the reference's order, split in three parts so that several rays can share a loaded pair and
+// rays with the same origin can share the origin terms s = o - v0, q = s x e1 and e2 . q (the
+// same operations, computed once).
+struct PairData {
+    f2 V0X, V0Y, V0Z, E1X, E1Y, E1Z, E2X, E2Y, E2Z;
+};
+struct OriginTerms {
+    f2 SX, SY, SZ, QX, QY, QZ, TN;
+};
+struct PairHit {
+    bool okA, okB;
+    float tA, tB, uA, uB, vA, vB;
+};
+
+__device__ __forceinline__ PairData load_pair(const ulonglong2* __restrict__ P) {
     ulonglong2 q0 = __ldg(P), q1 = __ldg(P + 1), q2 = __ldg(P + 2), q3 = __ldg(P + 3), q4 = __ldg(P + 4);
-    const f2 V0X = q0.x, V0Y = q0.y, V0Z = q1.x, E1X = q1.y, E1Y = q2.x, E1Z = q2.y, E2X = q3.x, E2Y = q3.y,
-             E2Z = q4.x;
-    // n = cross(d, e2)
-    f2 NX = f2_sub(f2_mul(DY, E2Z, Z), f2_mul(DZ, E2Y, Z));
-    f2 NY = f2_sub(f2_mul(DZ, E2X, Z), f2_mul(DX, E2Z, Z));
-    f2 NZ = f2_sub(f2_mul(DX, E2Y, Z), f2_mul(DY, E2X, Z));
-    f2 A = f2_add(f2_add(f2_mul(E1X, NX, Z), f2_mul(E1Y, NY, Z)), f2_mul(E1Z, NZ, Z));
+    PairData d;
+    d.V0X = q0.x; d.V0Y = q0.y; d.V0Z = q1.x; d.E1X = q1.y; d.E1Y = q2.x;
+    d.E1Z = q2.y; d.E2X = q3.x; d.E2Y = q3.y; d.E2Z = q4.x;
+    return d;
+}
+
+__device__ __forceinline__ OriginTerms origin_terms(const PairData& p, f2 OX, f2 OY, f2 OZ, f2 Z) {
+    OriginTerms o;
+    o.SX = f2_sub(OX, p.V0X);  // s = ray.origin - v0
+    o.SY = f2_sub(OY, p.V0Y);
+    o.SZ = f2_sub(OZ, p.V0Z);
+    o.QX = f2_sub(f2_mul(o.SY, p.E1Z, Z), f2_mul(o.SZ, p.E1Y, Z));  // q = s x e1
+    o.QY = f2_sub(f2_mul(o.SZ, p.E1X, Z), f2_mul(o.SX, p.E1Z, Z));
+    o.QZ = f2_sub(f2_mul(o.SX, p.E1Y, Z), f2_mul(o.SY, p.E1X, Z));
+    o.TN = f2_add(f2_add(f2_mul(p.E2X, o.QX, Z), f2_mul(p.E2Y, o.QY, Z)), f2_mul(p.E2Z, o.QZ, Z));  // e2 . q
+    return o;
+}
+
+__device__ __forceinline__ PairHit ray_terms(const PairData& p, const OriginTerms& o, f2 DX, f2 DY, f2 DZ, f2 Z,
+                                             bool okA_in, bool okB_in) {
+    f2 NX = f2_sub(f2_mul(DY, p.E2Z, Z), f2_mul(DZ, p.E2Y, Z));  // n = d x e2
+    f2 NY = f2_sub(f2_mul(DZ, p.E2X, Z), f2_mul(DX, p.E2Z, Z));
+    f2 NZ = f2_sub(f2_mul(DX, p.E2Y, Z), f2_mul(DY, p.E2X, Z));
+    f2 A = f2_add(f2_add(f2_mul(p.E1X, NX, Z), f2_mul(p.E1Y, NY, Z)), f2_mul(p.E1Z, NZ, Z));  // e1 . n
     float aA, aB;
     f2_unpack(A, aA, aB);
     f2 F = f2_pack(__frcp_rn(aA), __frcp_rn(aB));
-    f2 SX = f2_sub(OX, V0X), SY = f2_sub(OY, V0Y), SZ = f2_sub(OZ, V0Z);
-    f2 U = f2_mul(F, f2_add(f2_add(f2_mul(SX, NX, Z), f2_mul(SY, NY, Z)), f2_mul(SZ, NZ, Z)), Z);
-    f2 QX = f2_sub(f2_mul(SY, E1Z, Z), f2_mul(SZ, E1Y, Z));
-    f2 QY = f2_sub(f2_mul(SZ, E1X, Z), f2_mul(SX, E1Z, Z));
-    f2 QZ = f2_sub(f2_mul(SX, E1Y, Z), f2_mul(SY, E1X, Z));
-    f2 V = f2_mul(F, f2_add(f2_add(f2_mul(DX, QX, Z), f2_mul(DY, QY, Z)), f2_mul(DZ, QZ, Z)), Z);
-    f2 T = f2_mul(F, f2_add(f2_add(f2_mul(E2X, QX, Z), f2_mul(E2Y, QY, Z)), f2_mul(E2Z, QZ, Z)), Z);
+    f2 U = f2_mul(F, f2_add(f2_add(f2_mul(o.SX, NX, Z), f2_mul(o.SY, NY, Z)), f2_mul(o.SZ, NZ, Z)), Z);
+    f2 V = f2_mul(F, f2_add(f2_add(f2_mul(DX, o.QX, Z), f2_mul(DY, o.QY, Z)), f2_mul(DZ, o.QZ, Z)), Z);
+    f2 T = f2_mul(F, o.TN, Z);
     f2 UV = f2_add(U, V);
+    PairHit h;
     float uvA, uvB;
-    f2_unpack(U, uA, uB);
-    f2_unpack(V, vA, vB);
-    f2_unpack(T, tA, tB);
+    f2_unpack(U, h.uA, h.uB);
+    f2_unpack(V, h.vA, h.vB);
+    f2_unpack(T, h.tA, h.tB);
     f2_unpack(UV, uvA, uvB);
-    okA = okA_in && !(fabsf(aA) < kThreshold) && !(uA < 0.0f || uA > 1.0f) && !(vA < 0.0f || uvA > 1.0f) &&
-          (tA > kThreshold);
-    okB = okB_in && !(fabsf(aB) < kThreshold) && !(uB < 0.0f || uB > 1.0f) && !(vB < 0.0f || uvB > 1.0f) &&
-          (tB > kThreshold);
+    h.okA = okA_in && !(fabsf(aA) < kThreshold) && !(h.uA < 0.0f || h.uA > 1.0f) && !(h.vA < 0.0f || uvA > 1.0f) &&
+            (h.tA > kThreshold);
+    h.okB = okB_in && !(fabsf(aB) < kThreshold) && !(h.uB < 0.0f || h.uB > 1.0f) && !(h.vB < 0.0f || uvB > 1.0f) &&
+            (h.tB > kThreshold);
+    return h;
 }
 
-// ---- warp-cooperative big-leaf test ------------------------------------------------------
-// All 32 lanes test the ray of lane `src` against the leaf [first, first + cnt): lane k takes
-// the triangle pairs pbeg + k, pbeg + k + 32, ... (coalesced 80-byte loads, two triangles per
-// packed instruction), keeps its first strictly smallest t below the ray's closest t, and the
-// warp reduces to the minimum t with ties going to the lowest triangle index -- exactly the
-// triangle the reference's sequential loop (bvh.rs:250-258, strict `<` in index order) keeps.
-// Lane `src` then takes the hit.  Must be called by all 32 lanes with the same arguments.
-__device__ __forceinline__ void coop_leaf(const ulonglong2* __restrict__ pairs, uint32_t first, uint32_t cnt,
-                                          int src, LaneRay& r) {
-    const unsigned kAll = 0xFFFFFFFFu;
-    const unsigned lane = threadIdx.x & 31u;
-    const float ox = __shfl_sync(kAll, r.o.x, src), oy = __shfl_sync(kAll, r.o.y, src),
-                oz = __shfl_sync(kAll, r.o.z, src);
-    const float dx = __shfl_sync(kAll, r.d.x, src), dy = __shfl_sync(kAll, r.d.y, src),
-                dz = __shfl_sync(kAll, r.d.z, src);
-    const float ct = __shfl_sync(kAll, r.ct, src);
-    const f2 OX = f2_pack(ox, ox), OY = f2_pack(oy, oy), OZ = f2_pack(oz, oz);
-    const f2 DX = f2_pack(dx, dx), DY = f2_pack(dy, dy), DZ = f2_pack(dz, dz);
-    const f2 Z = f2_neg_zero();
-    const uint32_t end = first + cnt;
-    const uint32_t pbeg = first >> 1, pend = (end + 1) >> 1;
-    float bt = ct, bu = 0.0f, bv = 0.0f;
-    uint32_t bk = 0xFFFFFFFFu;
-    for (uint32_t p = pbeg + lane; p < pend; p += 32u) {
-        const uint32_t kA = 2u * p, kB = kA + 1u;
-        bool okA, okB;
-        float tA, tB, uA, uB, vA, vB;
-        tri_test_pair(pairs + 5ull * p, OX, OY, OZ, DX, DY, DZ, Z, kA >= first, kB < end, okA, okB, tA, tB, uA,
-                      uB, vA, vB);
-        if (okA && tA < bt) {
-            bt = tA; bu = uA; bv = vA; bk = kA;
+// Running best of one ray inside a cooperative leaf test (triangle index order kept: a pair's
+// triangle A before B, strict `<`).
+struct Best {
+    float t, u, v;
+    uint32_t k;
+    __device__ __forceinline__ void take(const PairHit& h, uint32_t kA) {
+        if (h.okA && h.tA < t) {
+            t = h.tA; u = h.uA; v = h.vA; k = kA;
         }
-        if (okB && tB < bt) {
-            bt = tB; bu = uB; bv = vB; bk = kB;
+        if (h.okB && h.tB < t) {
+            t = h.tB; u = h.uB; v = h.vB; k = kA + 1u;
         }
     }
+};
+
+struct CoopRay {
+    float ox, oy, oz, dx, dy, dz, ct;
+};
+
+__device__ __forceinline__ CoopRay bcast_ray(const LaneRay& r, int src) {
+    const unsigned kAll = 0xFFFFFFFFu;
+    CoopRay c;
+    c.ox = __shfl_sync(kAll, r.o.x, src);
+    c.oy = __shfl_sync(kAll, r.o.y, src);
+    c.oz = __shfl_sync(kAll, r.o.z, src);
+    c.dx = __shfl_sync(kAll, r.d.x, src);
+    c.dy = __shfl_sync(kAll, r.d.y, src);
+    c.dz = __shfl_sync(kAll, r.d.z, src);
+    c.ct = __shfl_sync(kAll, r.ct, src);
+    return c;
+}
+
+// Warp argmin of (t, k) -- minimum t, ties to the lowest triangle index -- then lane `src` takes
+// the hit (u, v come from the lane that tested the winning triangle).
+__device__ __forceinline__ void reduce_and_take(Best b, uint32_t pbeg, int src, LaneRay& r) {
+    const unsigned kAll = 0xFFFFFFFFu;
+    const unsigned lane = threadIdx.x & 31u;
+    float bt = b.t;
+    uint32_t bk = b.k;
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
         float ot = __shfl_xor_sync(kAll, bt, off);
@@ -352,8 +383,8 @@ __device__ __forceinline__ void coop_leaf(const ulonglong2* __restrict__ pairs, 
     }
     if (bk != 0xFFFFFFFFu) {
         const int owner = (int)(((bk >> 1) - pbeg) & 31u);
-        float wu = __shfl_sync(kAll, bu, owner);
-        float wv = __shfl_sync(kAll, bv, owner);
+        float wu = __shfl_sync(kAll, b.u, owner);
+        float wv = __shfl_sync(kAll, b.v, owner);
         if ((int)lane == src) {
             r.ct = bt;
             r.hu = wu;
@@ -362,6 +393,73 @@ __device__ __forceinline__ void coop_leaf(const ulonglong2* __restrict__ pairs, 
             r.hit = true;
         }
     }
+}
+
+// ---- warp-cooperative big-leaf test ------------------------------------------------------
+// All 32 lanes test the ray(s) of lane(s) `src` against the leaf [first, first + cnt): lane k
+// takes the triangle pairs pbeg + k, pbeg + k + 32, ... (coalesced 80-byte loads, two triangles
+// per packed instruction), keeps its first strictly smallest t below the ray's closest t, and
+// the warp reduces to the minimum t with ties going to the lowest triangle index -- exactly the
+// triangle the reference's sequential loop (bvh.rs:250-258, strict `<` in index order) keeps.
+// Must be called by all 32 lanes with the same arguments.
+__device__ __forceinline__ void coop_leaf(const ulonglong2* __restrict__ pairs, uint32_t first, uint32_t cnt,
+                                          int src, LaneRay& r) {
+    const unsigned lane = threadIdx.x & 31u;
+    const CoopRay c = bcast_ray(r, src);
+    const f2 OX = f2_pack(c.ox, c.ox), OY = f2_pack(c.oy, c.oy), OZ = f2_pack(c.oz, c.oz);
+    const f2 DX = f2_pack(c.dx, c.dx), DY = f2_pack(c.dy, c.dy), DZ = f2_pack(c.dz, c.dz);
+    const f2 Z = f2_neg_zero();
+    const uint32_t end = first + cnt;
+    const uint32_t pbeg = first >> 1, pend = (end + 1) >> 1;
+    Best b{c.ct, 0.0f, 0.0f, 0xFFFFFFFFu};
+    for (uint32_t p = pbeg + lane; p < pend; p += 32u) {
+        const uint32_t kA = 2u * p;
+        PairData pd = load_pair(pairs + 5ull * p);
+        OriginTerms ot = origin_terms(pd, OX, OY, OZ, Z);
+        b.take(ray_terms(pd, ot, DX, DY, DZ, Z, kA >= first, kA + 1u < end), kA);
+    }
+    reduce_and_take(b, pbeg, src, r);
+}
+
+// Two rays (lanes srcA, srcB) waiting on the same leaf: each loaded pair is tested against both,
+// and when the rays share their origin bit for bit the origin terms are computed once.
+__device__ __forceinline__ void coop_leaf2(const ulonglong2* __restrict__ pairs, uint32_t first, uint32_t cnt,
+                                           int srcA, int srcB, LaneRay& r) {
+    const unsigned lane = threadIdx.x & 31u;
+    const CoopRay ca = bcast_ray(r, srcA);
+    const CoopRay cb = bcast_ray(r, srcB);
+    const bool same_o = __float_as_uint(ca.ox) == __float_as_uint(cb.ox) &&
+                        __float_as_uint(ca.oy) == __float_as_uint(cb.oy) &&
+                        __float_as_uint(ca.oz) == __float_as_uint(cb.oz);
+    const f2 AOX = f2_pack(ca.ox, ca.ox), AOY = f2_pack(ca.oy, ca.oy), AOZ = f2_pack(ca.oz, ca.oz);
+    const f2 ADX = f2_pack(ca.dx, ca.dx), ADY = f2_pack(ca.dy, ca.dy), ADZ = f2_pack(ca.dz, ca.dz);
+    const f2 BOX = f2_pack(cb.ox, cb.ox), BOY = f2_pack(cb.oy, cb.oy), BOZ = f2_pack(cb.oz, cb.oz);
+    const f2 BDX = f2_pack(cb.dx, cb.dx), BDY = f2_pack(cb.dy, cb.dy), BDZ = f2_pack(cb.dz, cb.dz);
+    const f2 Z = f2_neg_zero();
+    const uint32_t end = first + cnt;
+    const uint32_t pbeg = first >> 1, pend = (end + 1) >> 1;
+    Best ba{ca.ct, 0.0f, 0.0f, 0xFFFFFFFFu};
+    Best bb{cb.ct, 0.0f, 0.0f, 0xFFFFFFFFu};
+    if (same_o) {
+        for (uint32_t p = pbeg + lane; p < pend; p += 32u) {
+            const uint32_t kA = 2u * p;
+            const bool va = kA >= first, vb = kA + 1u < end;
+            PairData pd = load_pair(pairs + 5ull * p);
+            OriginTerms ot = origin_terms(pd, AOX, AOY, AOZ, Z);
+            ba.take(ray_terms(pd, ot, ADX, ADY, ADZ, Z, va, vb), kA);
+            bb.take(ray_terms(pd, ot, BDX, BDY, BDZ, Z, va, vb), kA);
+        }
+    } else {
+        for (uint32_t p = pbeg + lane; p < pend; p += 32u) {
+            const uint32_t kA = 2u * p;
+            const bool va = kA >= first, vb = kA + 1u < end;
+            PairData pd = load_pair(pairs + 5ull * p);
+            ba.take(ray_terms(pd, origin_terms(pd, AOX, AOY, AOZ, Z), ADX, ADY, ADZ, Z, va, vb), kA);
+            bb.take(ray_terms(pd, origin_terms(pd, BOX, BOY, BOZ, Z), BDX, BDY, BDZ, Z, va, vb), kA);
+        }
+    }
+    reduce_and_take(ba, pbeg, srcA, r);
+    reduce_and_take(bb, pbeg, srcB, r);
 }
 
 __device__ __forceinline__ void load_ray(const float4* rays, uint32_t i, float3& o, float3& d, float& t) {

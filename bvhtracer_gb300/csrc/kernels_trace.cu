@@ -53,18 +53,36 @@ inline unsigned grid_for(uint32_t n, int block) { return (unsigned)((n + block -
 // (coop_leaf), one waiting ray at a time.  All 32 lanes stay in the loop until every ray of
 // the warp has finished, so the cooperative step always has the full warp.
 
-// Lane-level state machine of the traversal loop.
+// Cooperative leaf phase: lanes waiting on the same leaf form a group; the group's rays are
+// tested two at a time (coop_leaf2 shares each loaded triangle pair between the two rays), an
+// odd one alone.  `key` identifies the BLAS (pairs pointer) so that different scenes of a batch
+// never share a leaf.
 template <int STACK>
-__device__ __forceinline__ void coop_leaf_phase(unsigned pend, const GBlas& b, Trav<STACK>& tr, LaneRay& r,
+__device__ __forceinline__ void coop_leaf_phase(unsigned pend, const ulonglong2* pairs, Trav<STACK>& tr, LaneRay& r,
                                                 StepResult& st) {
     const unsigned lane = threadIdx.x & 31u;
+    const unsigned long long key = reinterpret_cast<unsigned long long>(pairs);
     while (pend) {
-        int src = __ffs(pend) - 1;
-        pend &= pend - 1u;
-        uint32_t f = __shfl_sync(kFull, tr.first, src);
-        uint32_t c = __shfl_sync(kFull, tr.cnt, src);
-        coop_leaf(b.pairs, f, c, src, r);
-        if ((int)lane == src) st = tr.pop() ? kStepFinished : kStepContinue;
+        const int leader = __ffs(pend) - 1;
+        const uint32_t f = __shfl_sync(kFull, tr.first, leader);
+        const uint32_t c = __shfl_sync(kFull, tr.cnt, leader);
+        const unsigned long long lk = __shfl_sync(kFull, key, leader);
+        const ulonglong2* P = reinterpret_cast<const ulonglong2*>(lk);
+        unsigned group = __ballot_sync(kFull, ((pend >> lane) & 1u) && tr.first == f && key == lk);
+        pend &= ~group;
+        while (group) {
+            const int a = __ffs(group) - 1;
+            group &= group - 1u;
+            if (group) {
+                const int b = __ffs(group) - 1;
+                group &= group - 1u;
+                coop_leaf2(P, f, c, a, b, r);
+                if ((int)lane == a || (int)lane == b) st = tr.pop() ? kStepFinished : kStepContinue;
+            } else {
+                coop_leaf(P, f, c, a, r);
+                if ((int)lane == a) st = tr.pop() ? kStepFinished : kStepContinue;
+            }
+        }
     }
 }
 
@@ -79,7 +97,7 @@ __device__ __forceinline__ void warp_trace(const GBlas& b, bool active, LaneRay&
         if (st == kStepContinue) st = tr.advance(b, r, big_leaf, err);
         unsigned pend = __ballot_sync(kFull, st == kStepBigLeaf);
         if (pend == 0u) break;
-        coop_leaf_phase<STACK>(pend, b, tr, r, st);
+        coop_leaf_phase<STACK>(pend, b.pairs, tr, r, st);
     }
 }
 
@@ -245,7 +263,7 @@ __global__ void __launch_bounds__(kBlock) k_persistent_bounce(GBlas b, const flo
             if (!queue_open && __ballot_sync(kFull, phase == 0 || phase == 1 || phase == 2) == 0u) break;
             continue;
         }
-        coop_leaf_phase<STACK>(pend, b, tr, r, st);
+        coop_leaf_phase<STACK>(pend, b.pairs, tr, r, st);
     }
 }
 
@@ -257,13 +275,6 @@ struct BatchEntry {
     uint32_t work_begin;  // prefix sum of ray counts
     uint32_t pad0, pad1;
 };
-
-__device__ __forceinline__ const ulonglong2* shfl_ptr(const ulonglong2* p, int src) {
-    unsigned long long v = reinterpret_cast<unsigned long long>(p);
-    unsigned lo = __shfl_sync(kFull, (unsigned)(v & 0xFFFFFFFFull), src);
-    unsigned hi = __shfl_sync(kFull, (unsigned)(v >> 32), src);
-    return reinterpret_cast<const ulonglong2*>((unsigned long long)lo | ((unsigned long long)hi << 32));
-}
 
 template <int STACK>
 __global__ void __launch_bounds__(kBlock) k_trace_batch_persistent(const BatchEntry* __restrict__ table,
@@ -325,15 +336,7 @@ __global__ void __launch_bounds__(kBlock) k_trace_batch_persistent(const BatchEn
             if (!queue_open && __ballot_sync(kFull, phase == 0 || phase == 1) == 0u) break;
             continue;
         }
-        while (pend) {
-            int src = __ffs(pend) - 1;
-            pend &= pend - 1u;
-            const ulonglong2* T = shfl_ptr(b.pairs, src);
-            uint32_t f = __shfl_sync(kFull, tr.first, src);
-            uint32_t c = __shfl_sync(kFull, tr.cnt, src);
-            coop_leaf(T, f, c, src, r);
-            if ((int)lane == src) st = tr.pop() ? kStepFinished : kStepContinue;
-        }
+        coop_leaf_phase<STACK>(pend, b.pairs, tr, r, st);
     }
 }
 
