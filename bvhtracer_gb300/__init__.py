@@ -4,6 +4,7 @@ The compute path is the CUDA library ``libbvhgpu.so`` (C ABI in include/bvhgpu.h
 this package is its host-side mirror of the reference's interface (see ``api``) plus
 the seeded synthetic workloads (``scenes``).
 """
+from . import scenes  # noqa: F401
 from .api import (BATCH_ITEM, FLT_MAX, HIT, MISS, NODE, RAY, TLAS_NODE, Blas, Bvh, BvhBuilder, Camera, Context,
                   DeviceBuffer, Event, PinnedArray, Scene)
 from ._lib import (ACC_DEPTH, ACC_INTERSECTION, ACC_NORMAL, ACC_UV, MODE_PERSISTENT, MODE_PLAIN, SHADER_DEPTH,
