@@ -28,7 +28,8 @@ FLT_MAX = np.float32(np.finfo(np.float32).max)
 
 OK = 0
 ERRORS = {1: "invalid argument", 2: "out of memory", 3: "CUDA error", 4: "stack depth exceeded",
-          5: "step cap exceeded", 6: "build would panic", 7: "no CUDA device"}
+          5: "step cap exceeded", 6: "build would panic", 7: "no CUDA device",
+          8: "input larger than the entry point's fixed maximum"}
 
 ACC_INTERSECTION, ACC_DEPTH, ACC_UV, ACC_NORMAL = 0, 1, 2, 3
 SHADER_RADIANCE, SHADER_INTERSECTION, SHADER_DEPTH = 0, 1, 2
@@ -89,6 +90,7 @@ SIGNATURES = {
     "bvhgpu_scene_intersect": (_I, [_P, _U32, _P, _U32, _P]),
     "bvhgpu_scene_intersect_async": (_I, [_P, _U32, _P, _U32, _P, _P]),
     "bvhgpu_render": (_I, [_P, _U32, _P, _I, _I, _I, _P, _I, _P, _P, _P, _P]),
+    "bvhgpu_refit_noalloc": (_I, [_P, _U32, _P, _U32, _P, _P]),
 }
 
 _lib = None

@@ -38,6 +38,7 @@ extern "C" {
 #define BVHGPU_ERR_STEP_CAP 5      /* a traversal exceeded its step cap (corrupt tree) */
 #define BVHGPU_ERR_BUILD 6         /* the reference's BvhBuilder would panic on this mesh */
 #define BVHGPU_ERR_NO_DEVICE 7
+#define BVHGPU_ERR_TOO_LARGE 8     /* input larger than a fixed-size entry point accepts */
 
 /* ---- data layouts ------------------------------------------------------------------- */
 
@@ -243,6 +244,26 @@ int bvhgpu_scene_intersect_async(bvhgpu_ctx* ctx, uint32_t scene_id, const bvhgp
 int bvhgpu_render(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhgpu_camera* camera, int width, int height,
                   int accumulator, const float* acc_params, int shader, const float* shader_params,
                   const float* normals, uint8_t* rgba, uint64_t* rays_traced);
+
+/* ---- refit without allocation ----------------------------------------------------------------- */
+/* No counterpart in the reference.  For callers that cannot call cudaMalloc: engines that own all
+ * device memory through a pool reserved at start-up, or latency-critical threads on which a driver
+ * allocation (which can synchronise the device) is not allowed.  Refits, in place, a node array the
+ * caller owns on the device (reference layout, nodes_used entries) against the caller's device
+ * triangles (ntris x 36 bytes), with the same results as bvhgpu_blas_refit.  Allocates nothing and
+ * needs no context: its scratch is a fixed device array of 8 MiB that every GPU which loads the
+ * library holds until the process exits, so nodes_used may be at most BVHGPU_NOALLOC_MAX_NODES
+ * (larger arrays return BVHGPU_ERR_TOO_LARGE).  Runs asynchronously on `stream` (NULL = legacy
+ * default stream) on the current device.  The first call on a device looks up the scratch array's
+ * device address (cudaGetSymbolAddress) with that device current; make that first call before any
+ * stream capture.  Every call shares the one scratch array and resets the part it uses, so calls
+ * whose work overlaps on the GPU (different streams, or different threads with the same device)
+ * race and must be serialised by the caller.  If d_status (device, caller-owned, may be NULL) is
+ * given, bit 1 is OR-ed in for a branch with a bad child index and bit 2 for a leaf addressing
+ * triangles past ntris (such nodes are skipped); the caller clears it. */
+#define BVHGPU_NOALLOC_MAX_NODES (1u << 20)
+int bvhgpu_refit_noalloc(bvhgpu_node* d_nodes, uint32_t nodes_used, const bvhgpu_triangle* d_tris, uint32_t ntris,
+                         bvhgpu_stream stream, uint32_t* d_status);
 
 #ifdef __cplusplus
 }
