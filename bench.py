@@ -345,6 +345,156 @@ def run_ours(args):
     return 0
 
 
+WORKLOAD3 = ("uneven batch: 64 scenes, triangles log-uniform in [1k, 2M] (soup / displaced icosphere), "
+             "rays log-uniform in [64k, 4M] (half pinhole primaries, half random)")
+
+
+def setup_batch(nscenes: int = 64, seed: int = SEED):
+    """The 64 scenes of the uneven batch, generated and built (reference SAH) on host threads."""
+    import bvhtracer_gb300 as bt
+    from concurrent.futures import ThreadPoolExecutor
+    from bvhtracer_gb300 import scenes
+    ntris, nrays = scenes.config3_specs(seed, nscenes)
+
+    def make(i):
+        tris, rays = scenes.config3_scene(i, int(ntris[i]), int(nrays[i]), seed)
+        bvh = bt.BvhBuilder().build_for(tris)
+        return tris, bvh, rays
+
+    with ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 1)) as ex:
+        return list(ex.map(make, range(nscenes)))
+
+
+def batch_cpu_baseline(built, per_scene: int = 8192, threads: int | None = None):
+    """The oracle on a bounded sample of every scene (the first `per_scene` primaries and the
+    first `per_scene` random rays of each), the scenes spread over all host threads; plus
+    single-thread per-ray counters for the algorithmic bytes."""
+    from concurrent.futures import ThreadPoolExecutor
+    from oracle import oracle as orc
+    threads = threads or os.cpu_count() or 1
+
+    def sample_of(rays, k):
+        half = len(rays) // 2
+        return np.concatenate([rays[:k], rays[half:half + k]])
+
+    def run(item):
+        tris, bvh, rays = item
+        return orc.bvh_intersect(bvh.nodes, bvh.nodes_used, tris, sample_of(rays, per_scene))
+
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        done = list(ex.map(run, built))
+    secs = time.perf_counter() - t0
+    total_rays = sum(len(h) for h in done)
+    bytes_sum, counted = 0.0, 0
+    for tris, bvh, rays in built:
+        _, c = orc.bvh_intersect(bvh.nodes, bvh.nodes_used, tris, sample_of(rays, 16), counters=True)
+        bytes_sum += float(orc.bytes_per_ray(c).mean()) * len(rays)  # weighted by the scene's ray count
+        counted += len(rays)
+    return {"value": total_rays / secs / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "port",
+            "sample": f"{per_scene} primaries + {per_scene} random rays of each of the {len(built)} scenes, "
+                      f"scenes spread over {threads} threads", "seconds": secs}, bytes_sum / counted
+
+
+def run_batch(args):
+    import bvhtracer_gb300 as bt
+    rank, world, local_rank = dist_env()
+    t0 = time.perf_counter()
+    built = setup_batch()
+    setup_s = time.perf_counter() - t0
+    ctx = bt.Context(local_rank)
+    blases = [ctx.upload_blas(bvh, tris) for tris, bvh, _ in built]
+    rays = np.concatenate([r for _, _, r in built])
+    items = np.zeros(len(built), bt.BATCH_ITEM)
+    off = 0
+    for i, (b, (_, _, r)) in enumerate(zip(blases, built)):
+        items[i] = (b.id, off, len(r), 0)
+        off += len(r)
+    n = len(rays)
+    d_rays = ctx.to_device(rays)
+    d_hits = ctx.device_buffer(n * bt.HIT.itemsize)
+    d_hits2 = ctx.device_buffer(n * bt.HIT.itemsize)
+    ev = [(ctx.event(), ctx.event()) for _ in range(args.steps)]
+
+    def timed(mode, out):
+        for _ in range(args.warmup):
+            ctx.flush_l2()
+            ctx.trace_batch_async(items, d_rays, n, mode, out)
+        ctx.sync()
+        ctx.profile(True)
+        ctx.profile_read()
+        for s in range(args.steps):
+            ctx.flush_l2()
+            ev[s][0].record()
+            ctx.trace_batch_async(items, d_rays, n, mode, out)
+            ev[s][1].record()
+        ctx.sync()
+        ms = [a.elapsed_ms(b) for a, b in ev]
+        prof = ctx.profile_read()
+        ctx.profile(False)
+        return ms, prof
+
+    clocks = Clocks(local_rank)
+    clocks.start()
+    ms_p, prof_p = timed(bt.MODE_PERSISTENT, d_hits)
+    clk = clocks.stop()
+    ms_plain, prof_plain = timed(bt.MODE_PLAIN, d_hits2)
+    h1 = d_hits.download(np.zeros(n, bt.HIT))
+    h2 = d_hits2.download(np.zeros(n, bt.HIT))
+    identical = bool(h1.tobytes() == h2.tobytes())
+    value = n * args.steps / (sum(ms_p) / 1e3) / 1e6
+    plain = n * args.steps / (sum(ms_plain) / 1e3) / 1e6
+    # e2e: bvhgpu_trace_batch with pinned host buffers
+    pin_r = ctx.pinned((n,), bt.RAY)
+    pin_r.array[:] = rays
+    pin_h = ctx.pinned((n,), bt.HIT)
+    import ctypes
+    from bvhtracer_gb300._lib import ptr
+    its = np.ascontiguousarray(items)
+
+    def e2e_once():
+        ctx.check(ctx.lib.bvhgpu_trace_batch(ctx.h, ptr(its), len(its), ptr(pin_r.array), n, bt.MODE_PERSISTENT,
+                                             ptr(pin_h.array)))
+    e2e_once()
+    t0 = time.perf_counter()
+    for _ in range(max(1, args.steps // 2)):
+        e2e_once()
+    e2e_value = n * max(1, args.steps // 2) / (time.perf_counter() - t0) / 1e6
+    if rank != 0:
+        return 0
+    result = {
+        "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": sum(ms_p) / len(ms_p), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD3, "scenes": len(built), "rays": n,
+                   "triangles": int(sum(len(t) for t, _, _ in built)), "setup_s": setup_s,
+                   "l2": "flushed between steps (256 MB memset)", "parallelism": f"replicas x{world}", "seed": SEED},
+        "plain_vs_persistent": {"persistent": value, "plain": plain, "ratio_persistent_over_plain": value / plain,
+                                "hit_records_identical": identical},
+        "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": n * bt.RAY.itemsize,
+                "d2h_bytes_per_step": n * bt.HIT.itemsize},
+        "gpu_launches": sum(v[1] for v in prof_p.values()),
+        "clocks": clk,
+        "kernel_ms": {k: {"ms_total": v[0], "launches": v[1]} for k, v in prof_p.items()},
+        "kernel_ms_plain": {k: {"ms_total": v[0], "launches": v[1]} for k, v in prof_plain.items()},
+    }
+    if args.no_cpu_baseline:
+        result["cpu_baseline"] = None
+        result["roofline"] = None
+    else:
+        base, bytes_per_ray = batch_cpu_baseline(built)
+        result["cpu_baseline"] = base
+        peak, peak_kind = measured_peaks()
+        dom_ms, dom_n = prof_p["trace_batch"]
+        per_launch_s = dom_ms / dom_n / 1e3
+        achieved = n * bytes_per_ray / per_launch_s / 1e9
+        result["roofline"] = {"bound": "hbm", "kernel": "trace_batch", "achieved": achieved, "peak": peak,
+                              "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                              "algorithmic_bytes_per_launch": n * bytes_per_ray, "launch_ms": per_launch_s * 1e3}
+    print(json.dumps(result), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -352,6 +502,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--mode", choices=["persistent", "plain"], default="persistent")
+    ap.add_argument("--config", type=int, choices=[1, 3], default=1,
+                    help="1: displaced icosphere frame + bounce (default); 3: uneven 64-scene batch")
     ap.add_argument("--no-cpu-baseline", action="store_true",
                     help="skip the CPU-baseline leg (outside the timed region), e.g. under a profiler")
     args = ap.parse_args()
@@ -359,6 +511,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.config == 3:
+        return run_batch(args)
     return run_ours(args)
 
 

@@ -210,3 +210,36 @@ def config1(seed: int = 0, width: int = 1920, height: int = 1080):
     tris = mesh.triangles()
     rays = look_at_rays(width, height, (0.0, 0.0, -3.0), (0.0, 0.0, 0.0), 45.0)
     return tris, rays, mesh
+
+
+def config3_specs(seed: int = 0, nscenes: int = 64, tri_range=(1_000, 2_000_000), ray_range=(65_536, 4_194_304)):
+    """Sizes of the uneven batch: triangle and ray counts log-uniform in the given ranges."""
+    u_t = uniform(seed, 30, nscenes)
+    u_r = uniform(seed, 31, nscenes)
+    lt = np.log(tri_range[0]) + u_t * (np.log(tri_range[1]) - np.log(tri_range[0]))
+    lr = np.log(ray_range[0]) + u_r * (np.log(ray_range[1]) - np.log(ray_range[0]))
+    return np.round(np.exp(lt)).astype(np.int64), np.round(np.exp(lr)).astype(np.int64)
+
+
+def config3_scene(i: int, ntris: int, nrays: int, seed: int = 0):
+    """Scene i of the uneven batch: even i a config-0-style soup grown to `ntris` triangles
+    (box scaled by (ntris/4096)^(1/3)), odd i a displaced icosphere at the subdivision level
+    nearest to `ntris`; rays: half pinhole primaries (tile order), half origins
+    U[-10, 10]^3 (times the scene scale) with uniform-sphere directions."""
+    sseed = seed * 1000 + i
+    if i % 2 == 0:
+        scale = (ntris / 4096.0) ** (1.0 / 3.0)
+        tris = soup(int(ntris), sseed, scale=scale)
+        n_prim = nrays // 2
+        side = int(np.ceil(np.sqrt(n_prim) / 8.0) * 8)
+        prim = plane_rays(side, side, (0.0, 0.0, -18.0 * scale), -15.0 * scale, scale, scale)[:n_prim]
+        box = 10.0 * scale
+    else:
+        level = int(np.clip(np.round(np.log(ntris / 20.0) / np.log(4.0)), 1, 8))
+        tris = displaced_icosphere(level, sseed).triangles()
+        n_prim = nrays // 2
+        side = int(np.ceil(np.sqrt(n_prim) / 8.0) * 8)
+        prim = look_at_rays(side, side, (0.0, 0.0, -3.0), (0.0, 0.0, 0.0), 45.0)[:n_prim]
+        box = 10.0
+    rnd = sphere_rays(int(nrays - n_prim), sseed + 7, box=box)
+    return tris, np.concatenate([prim, rnd])
