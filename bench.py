@@ -495,6 +495,103 @@ def run_batch(args):
     return 0
 
 
+WORKLOAD4 = ("differentiable Lambertian render: displaced icosphere, 7 subdivisions (327,680 tris, "
+             "163,842 vertices), 512x512, light (2,2,-3), target from N(0, 0.01^2) radial noise, all lengths x10 "
+             "(the reference's |det| < 1e-4 test rejects every triangle of the unit sphere); "
+             "step = update+refit, forward, adjoint, SGD (lr 1e-2)")
+
+
+def run_adjoint(args):
+    import bvhtracer_gb300 as bt
+    from bvhtracer_gb300 import scenes
+    rank, world, local_rank = dist_env()
+    verts, faces, vn, tverts, rays, light = scenes.config4(seed=SEED)
+    n = len(rays)
+    ctx = bt.Context(local_rank)
+    m = bt.DiffMesh(ctx, verts, faces, vn)
+    d_rays = ctx.to_device(rays)
+    d_img = ctx.device_buffer(4 * n)
+    d_tgt = ctx.device_buffer(4 * n)
+    d_hits = ctx.device_buffer(bt.HIT.itemsize * n)
+    d_grad = ctx.device_buffer(12 * len(verts))
+    d_grad.zero()
+    m.set_vertices(tverts)
+    m.forward_async(d_rays, n, light, d_tgt, d_hits)
+    m.set_vertices(verts)
+    lr = 1e-2
+
+    def step(evs=None):
+        if evs:
+            evs[0].record()
+        m.update_async()
+        if evs:
+            evs[1].record()
+        m.forward_async(d_rays, n, light, d_img, d_hits)
+        if evs:
+            evs[2].record()
+        m.adjoint_async(d_rays, n, light, d_hits, d_img, d_tgt, d_grad)
+        if evs:
+            evs[3].record()
+        m.sgd_step_async(d_grad, lr)
+        if evs:
+            evs[4].record()
+
+    for _ in range(args.warmup):
+        ctx.flush_l2()
+        step()
+    ctx.sync()
+    evs = [[ctx.event() for _ in range(5)] for _ in range(args.steps)]
+    clocks = Clocks(local_rank)
+    clocks.start()
+    ctx.profile(True)
+    ctx.profile_read()
+    for s in range(args.steps):
+        ctx.flush_l2()
+        step(evs[s])
+    ctx.sync()
+    clk = clocks.stop()
+    prof = ctx.profile_read()
+    ctx.profile(False)
+    upd = [e[0].elapsed_ms(e[1]) for e in evs]
+    fwd = [e[1].elapsed_ms(e[2]) for e in evs]
+    adj = [e[2].elapsed_ms(e[3]) for e in evs]
+    tot = [e[0].elapsed_ms(e[4]) for e in evs]
+    # the 100-step descent from the start (outside the timed region): loss every 10 steps
+    m.set_vertices(verts)
+    d_grad.zero()
+    losses = []
+    for it in range(101):
+        m.update_async()
+        m.forward_async(d_rays, n, light, d_img, d_hits)
+        if it % 10 == 0:
+            losses.append(bt.mse_loss(ctx, d_img, d_tgt, n))
+        if it == 100:
+            break
+        m.adjoint_async(d_rays, n, light, d_hits, d_img, d_tgt, d_grad)
+        m.sgd_step_async(d_grad, lr)
+    ctx.sync()
+    if rank != 0:
+        return 0
+    adj_ms = sum(adj) / len(adj)
+    fwd_ms = sum(fwd) / len(fwd)
+    result = {
+        "metric": METRIC, "value": adj_ms, "unit": "ms/step (adjoint kernel)", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": sum(tot) / len(tot), "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD4, "pixels": n, "triangles": int(len(faces)), "vertices": int(len(verts)),
+                   "bvh_nodes": m.bvh.nodes_used, "l2": "flushed between steps (256 MB memset)", "seed": SEED},
+        "adjoint": {"forward_ms": fwd_ms, "adjoint_ms": adj_ms, "update_refit_ms": sum(upd) / len(upd),
+                    "step_ms": sum(tot) / len(tot), "adjoint_over_forward": adj_ms / fwd_ms,
+                    "forward_mrays_per_s": n / fwd_ms / 1e3,
+                    "loss_every_10_steps": losses},
+        "e2e": None, "gpu_launches": sum(v[1] for v in prof.values()) // max(1, args.steps), "clocks": clk,
+        "kernel_ms": {k: {"ms_total": v[0], "launches": v[1]} for k, v in prof.items()},
+        "cpu_baseline": None, "roofline": None,
+    }
+    print(json.dumps(result), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -502,8 +599,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--mode", choices=["persistent", "plain"], default="persistent")
-    ap.add_argument("--config", type=int, choices=[1, 3], default=1,
-                    help="1: displaced icosphere frame + bounce (default); 3: uneven 64-scene batch")
+    ap.add_argument("--config", type=int, choices=[1, 3, 4], default=1,
+                    help="1: displaced icosphere frame + bounce (default); 3: uneven 64-scene batch; "
+                         "4: differentiable render (adjoint ms/step)")
     ap.add_argument("--no-cpu-baseline", action="store_true",
                     help="skip the CPU-baseline leg (outside the timed region), e.g. under a profiler")
     args = ap.parse_args()
@@ -513,6 +611,8 @@ def main():
         return run_reference(args)
     if args.config == 3:
         return run_batch(args)
+    if args.config == 4:
+        return run_adjoint(args)
     return run_ours(args)
 
 

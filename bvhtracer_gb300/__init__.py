@@ -6,11 +6,12 @@ the seeded synthetic workloads (``scenes``).
 """
 from . import scenes  # noqa: F401
 from .api import (BATCH_ITEM, FLT_MAX, HIT, MISS, NODE, RAY, TLAS_NODE, Blas, Bvh, BvhBuilder, Camera, Context,
-                  DeviceBuffer, Event, PinnedArray, Scene)
+                  DeviceBuffer, DiffMesh, Event, PinnedArray, Scene, mse_loss)
 from ._lib import (ACC_DEPTH, ACC_INTERSECTION, ACC_NORMAL, ACC_UV, MODE_PERSISTENT, MODE_PLAIN, SHADER_DEPTH,
                    SHADER_INTERSECTION, SHADER_RADIANCE, BvhGpuError)
 
 __all__ = ["Context", "DeviceBuffer", "PinnedArray", "Event", "Bvh", "BvhBuilder", "Blas", "Scene", "Camera",
+           "DiffMesh", "mse_loss",
            "RAY", "HIT", "NODE", "TLAS_NODE", "BATCH_ITEM", "MISS", "FLT_MAX", "BvhGpuError",
            "ACC_INTERSECTION", "ACC_DEPTH", "ACC_UV", "ACC_NORMAL", "SHADER_RADIANCE", "SHADER_INTERSECTION",
            "SHADER_DEPTH", "MODE_PLAIN", "MODE_PERSISTENT"]

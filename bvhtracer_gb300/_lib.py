@@ -36,7 +36,7 @@ SHADER_RADIANCE, SHADER_INTERSECTION, SHADER_DEPTH = 0, 1, 2
 MODE_PLAIN, MODE_PERSISTENT = 0, 1
 
 KERNELS = ["trace_blas", "trace_scene", "persistent_bounce", "bounce_gen", "trace_queue", "trace_batch",
-           "refit", "tlas_build", "render", "other"]
+           "refit", "tlas_build", "render", "other", "lambert_forward", "lambert_adjoint"]
 
 # Exported symbols and their ctypes signatures (kept in the order of include/bvhgpu.h).
 _P = ctypes.c_void_p
@@ -65,6 +65,7 @@ SIGNATURES = {
     "bvhgpu_profile_enable": (_I, [_P, _I]),
     "bvhgpu_profile_read": (_I, [_P, _P, _P]),
     "bvhgpu_build_bvh_host": (_I, [_P, _U32, _P, _P]),
+    "bvhgpu_build_bvh_host_indexed": (_I, [_P, _U32, _P, _P, _P]),
     "bvhgpu_blas_upload": (_I, [_P, _P, _U32, _P, _U32, _P]),
     "bvhgpu_blas_free": (_I, [_P, _U32]),
     "bvhgpu_blas_info": (_I, [_P, _U32, _P, _P, _P]),
@@ -90,6 +91,15 @@ SIGNATURES = {
     "bvhgpu_scene_intersect": (_I, [_P, _U32, _P, _U32, _P]),
     "bvhgpu_scene_intersect_async": (_I, [_P, _U32, _P, _U32, _P, _P]),
     "bvhgpu_render": (_I, [_P, _U32, _P, _I, _I, _I, _P, _I, _P, _P, _P, _P]),
+    "bvhgpu_mesh_create": (_I, [_P, _U32, _P, _U32, _P, _P, _U32, _P]),
+    "bvhgpu_mesh_free": (_I, [_P, _U32]),
+    "bvhgpu_mesh_vertices": (_I, [_P, _U32, _P]),
+    "bvhgpu_mesh_set_vertices": (_I, [_P, _U32, _P]),
+    "bvhgpu_mesh_update_async": (_I, [_P, _U32, _P]),
+    "bvhgpu_lambert_forward_async": (_I, [_P, _U32, _P, _U32, _P, _P, _P, _P]),
+    "bvhgpu_mse_loss": (_I, [_P, _P, _P, _U32, _P]),
+    "bvhgpu_lambert_adjoint_async": (_I, [_P, _U32, _P, _U32, _P, _P, _P, _P, _P, _P]),
+    "bvhgpu_mesh_sgd_step_async": (_I, [_P, _U32, _P, ctypes.c_float, _P]),
     "bvhgpu_refit_noalloc": (_I, [_P, _U32, _P, _U32, _P, _P]),
 }
 

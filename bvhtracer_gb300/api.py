@@ -365,6 +365,75 @@ class Scene:
             self.id = 0
 
 
+# ---- differentiable Lambertian render ------------------------------------------------------------
+
+class DiffMesh:
+    """Indexed mesh for the differentiable Lambertian render: a BLAS built by the reference's SAH
+    build over the mesh's triangles, the face list permuted the way that build reordered the
+    triangles, and device vertices / shading normals."""
+
+    def __init__(self, ctx: Context, verts: np.ndarray, faces: np.ndarray, vnormals: np.ndarray):
+        self.ctx = ctx
+        verts = np.ascontiguousarray(verts, np.float32).reshape(-1, 3)
+        faces = np.ascontiguousarray(faces, np.uint32).reshape(-1, 3)
+        vnormals = np.ascontiguousarray(vnormals, np.float32).reshape(-1, 3)
+        tris = np.ascontiguousarray(verts[faces].reshape(-1, 9), np.float32)
+        n = len(tris)
+        nodes = np.zeros(2 * n, NODE)
+        perm = np.zeros(n, np.uint32)
+        used = ctypes.c_uint32()
+        rc = ctx.lib.bvhgpu_build_bvh_host_indexed(ptr(tris), n, ptr(nodes), ctypes.byref(used), ptr(perm))
+        if rc != 0:
+            raise BvhGpuError(rc, "build of the mesh's BVH failed")
+        self.bvh = Bvh(nodes, used.value)
+        self.tris = tris
+        self.faces = np.ascontiguousarray(faces[perm], np.uint32)
+        self.nverts = len(verts)
+        self.blas = Blas(ctx, self.bvh, tris)
+        mid = ctypes.c_uint32()
+        ctx.check(ctx.lib.bvhgpu_mesh_create(ctx.h, self.blas.id, ptr(self.faces), n, ptr(verts), ptr(vnormals),
+                                             self.nverts, ctypes.byref(mid)))
+        self.id = mid.value
+
+    def set_vertices(self, verts: np.ndarray):
+        verts = np.ascontiguousarray(verts, np.float32).reshape(self.nverts, 3)
+        self.ctx.check(self.ctx.lib.bvhgpu_mesh_set_vertices(self.ctx.h, self.id, ptr(verts)))
+
+    def vertices(self) -> np.ndarray:
+        p = ctypes.c_void_p()
+        self.ctx.check(self.ctx.lib.bvhgpu_mesh_vertices(self.ctx.h, self.id, ctypes.byref(p)))
+        out = np.zeros((self.nverts, 3), np.float32)
+        self.ctx.sync()
+        self.ctx.check(self.ctx.lib.bvhgpu_copy_to_host(self.ctx.h, ptr(out), p, out.nbytes, None))
+        self.ctx.sync()
+        return out
+
+    def update_async(self, stream=None):
+        self.ctx.check(self.ctx.lib.bvhgpu_mesh_update_async(self.ctx.h, self.id, stream))
+
+    def forward_async(self, d_rays: DeviceBuffer, n: int, light, d_image: DeviceBuffer, d_hits: DeviceBuffer,
+                      stream=None):
+        L = np.ascontiguousarray(light, np.float32)
+        self.ctx.check(self.ctx.lib.bvhgpu_lambert_forward_async(self.ctx.h, self.id, d_rays.ptr, n, ptr(L),
+                                                                 d_image.ptr, d_hits.ptr, stream))
+
+    def adjoint_async(self, d_rays: DeviceBuffer, n: int, light, d_hits: DeviceBuffer, d_image: DeviceBuffer,
+                      d_target: DeviceBuffer, d_grad: DeviceBuffer, stream=None):
+        L = np.ascontiguousarray(light, np.float32)
+        self.ctx.check(self.ctx.lib.bvhgpu_lambert_adjoint_async(self.ctx.h, self.id, d_rays.ptr, n, ptr(L),
+                                                                 d_hits.ptr, d_image.ptr, d_target.ptr, d_grad.ptr,
+                                                                 stream))
+
+    def sgd_step_async(self, d_grad: DeviceBuffer, lr: float, stream=None):
+        self.ctx.check(self.ctx.lib.bvhgpu_mesh_sgd_step_async(self.ctx.h, self.id, d_grad.ptr, float(lr), stream))
+
+
+def mse_loss(ctx: Context, d_image: DeviceBuffer, d_target: DeviceBuffer, n: int) -> float:
+    loss = ctypes.c_double()
+    ctx.check(ctx.lib.bvhgpu_mse_loss(ctx.h, d_image.ptr, d_target.ptr, n, ctypes.byref(loss)))
+    return loss.value
+
+
 # ---- camera ---------------------------------------------------------------------------------
 
 CAMERA = np.dtype([("top_left", "<f4", 3), ("top_right", "<f4", 3), ("bottom_left", "<f4", 3),
@@ -419,4 +488,5 @@ class Camera:
 
 
 __all__ = ["Context", "DeviceBuffer", "PinnedArray", "Event", "Bvh", "BvhBuilder", "Blas", "Scene", "Camera",
+           "DiffMesh", "mse_loss",
            "RAY", "HIT", "NODE", "TLAS_NODE", "BATCH_ITEM", "MISS", "FLT_MAX"]

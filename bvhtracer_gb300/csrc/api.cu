@@ -118,7 +118,21 @@ void free_blas(DeviceBlas& b) {
     cudaFree(b.parent);
     cudaFree(b.leaves);
     cudaFree(b.counters);
+    cudaFree(b.tri_leaf);
+    cudaFree(b.leaf_keys);
     b = DeviceBlas();
+}
+
+void free_mesh(DeviceMesh& m) {
+    cudaFree(m.faces);
+    cudaFree(m.verts);
+    cudaFree(m.vnormals);
+    m = DeviceMesh();
+}
+
+DeviceMesh* find_mesh(bvhgpu_ctx* ctx, uint32_t id) {
+    auto it = ctx->meshes.find(id);
+    return it == ctx->meshes.end() ? nullptr : &it->second;
 }
 
 void free_scene(DeviceScene& s) {
@@ -132,7 +146,8 @@ void free_scene(DeviceScene& s) {
 
 // Validates a reference node array and derives parent links, leaf list and depth.
 int analyse_nodes(bvhgpu_ctx* ctx, const bvhgpu_node* nodes, uint32_t nodes_used, uint32_t ntris,
-                  std::vector<uint32_t>& parent, std::vector<uint32_t>& leaves, uint32_t* depth) {
+                  std::vector<uint32_t>& parent, std::vector<uint32_t>& leaves, uint32_t* depth,
+                  std::vector<uint32_t>& tri_leaf) {
     parent.assign(nodes_used, 0xFFFFFFFFu);
     leaves.clear();
     std::vector<uint32_t> seen(nodes_used, 0);
@@ -165,6 +180,15 @@ int analyse_nodes(bvhgpu_ctx* ctx, const bvhgpu_node* nodes, uint32_t nodes_used
     }
     (void)covered;
     *depth = maxd;
+    tri_leaf.assign(ntris, 0xFFFFFFFFu);
+    for (uint32_t li = 0; li < leaves.size(); ++li) {
+        const bvhgpu_node& n = nodes[leaves[li]];
+        for (uint32_t t = n.left_first; t < n.left_first + n.primitive_count; ++t) {
+            if (tri_leaf[t] != 0xFFFFFFFFu)
+                return fail(ctx, BVHGPU_ERR_INVALID_ARG, "triangle %u belongs to two leaves", t);
+            tri_leaf[t] = li;
+        }
+    }
     return BVHGPU_OK;
 }
 
@@ -216,6 +240,8 @@ int bvhgpu_destroy(bvhgpu_ctx* ctx) {
     cudaStreamSynchronize(ctx->stream);
     for (auto& kv : ctx->blas) free_blas(kv.second);
     for (auto& kv : ctx->scenes) free_scene(kv.second);
+    for (auto& kv : ctx->meshes) free_mesh(kv.second);
+    cudaFree(ctx->mse_partials);
     for (auto& r : ctx->prof) {
         cudaEventDestroy(r.start);
         cudaEventDestroy(r.stop);
@@ -351,16 +377,22 @@ int bvhgpu_profile_read(bvhgpu_ctx* ctx, double* ms, uint64_t* launches) {
 // ---- BLAS -------------------------------------------------------------------------------------
 
 int bvhgpu_build_bvh_host(bvhgpu_triangle* mesh, uint32_t n, bvhgpu_node* nodes_out, uint32_t* nodes_used) {
-    return build_bvh_host(mesh, n, nodes_out, nodes_used);
+    return build_bvh_host(mesh, n, nodes_out, nodes_used, nullptr);
+}
+
+int bvhgpu_build_bvh_host_indexed(bvhgpu_triangle* mesh, uint32_t n, bvhgpu_node* nodes_out, uint32_t* nodes_used,
+                                  uint32_t* perm_out) {
+    if (!perm_out) return BVHGPU_ERR_INVALID_ARG;
+    return build_bvh_host(mesh, n, nodes_out, nodes_used, perm_out);
 }
 
 int bvhgpu_blas_upload(bvhgpu_ctx* ctx, const bvhgpu_node* nodes, uint32_t nodes_used, const bvhgpu_triangle* tris,
                        uint32_t ntris, uint32_t* blas_id) {
     if (!ctx || !nodes || !tris || !blas_id || nodes_used < 1 || ntris == 0)
         return fail(ctx, BVHGPU_ERR_INVALID_ARG, "blas_upload: null pointer or empty mesh");
-    std::vector<uint32_t> parent, leaves;
+    std::vector<uint32_t> parent, leaves, tri_leaf;
     uint32_t depth = 0;
-    int rc = analyse_nodes(ctx, nodes, nodes_used, ntris, parent, leaves, &depth);
+    int rc = analyse_nodes(ctx, nodes, nodes_used, ntris, parent, leaves, &depth, tri_leaf);
     if (rc) return rc;
     DeviceBlas b;
     b.nodes_used = nodes_used;
@@ -371,6 +403,10 @@ int bvhgpu_blas_upload(bvhgpu_ctx* ctx, const bvhgpu_node* nodes, uint32_t nodes
     b.root_first = nodes[0].left_first;
     std::vector<float> packed;
     pack_nodes(nodes, nodes_used, packed);
+    // refit keys start at the identities: min keys all-ones, max keys zero (6 per leaf)
+    std::vector<unsigned long long> key_init(6 * std::max<size_t>(1, leaves.size()), 0ull);
+    for (size_t li = 0; li < key_init.size() / 6; ++li)
+        for (int k = 0; k < 3; ++k) key_init[6 * li + k] = 0xFFFFFFFFFFFFFFFFull;
     void* d_tris9 = nullptr;
     cudaError_t e = cudaSuccess;
     auto cleanup = [&]() {
@@ -384,6 +420,8 @@ int bvhgpu_blas_upload(bvhgpu_ctx* ctx, const bvhgpu_node* nodes, uint32_t nodes
         (e = cudaMalloc(&b.parent, 4ull * nodes_used)) != cudaSuccess ||
         (e = cudaMalloc(&b.leaves, 4ull * std::max<size_t>(1, leaves.size()))) != cudaSuccess ||
         (e = cudaMalloc(&b.counters, 4ull * nodes_used)) != cudaSuccess ||
+        (e = cudaMalloc(&b.tri_leaf, 4ull * ntris)) != cudaSuccess ||
+        (e = cudaMalloc(&b.leaf_keys, 48ull * std::max<size_t>(1, leaves.size()))) != cudaSuccess ||
         (e = cudaMalloc(&d_tris9, 36ull * ntris)) != cudaSuccess) {
         cleanup();
         return fail(ctx, BVHGPU_ERR_OUT_OF_MEMORY, "blas_upload: %s", cudaGetErrorString(e));
@@ -392,6 +430,8 @@ int bvhgpu_blas_upload(bvhgpu_ctx* ctx, const bvhgpu_node* nodes, uint32_t nodes
         (e = cudaMemcpy(b.parent, parent.data(), 4ull * nodes_used, cudaMemcpyHostToDevice)) != cudaSuccess ||
         (e = cudaMemcpy(b.leaves, leaves.data(), 4ull * leaves.size(), cudaMemcpyHostToDevice)) != cudaSuccess ||
         (e = cudaMemset(b.counters, 0, 4ull * nodes_used)) != cudaSuccess ||
+        (e = cudaMemcpy(b.tri_leaf, tri_leaf.data(), 4ull * ntris, cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(b.leaf_keys, key_init.data(), 8ull * key_init.size(), cudaMemcpyHostToDevice)) != cudaSuccess ||
         (e = cudaMemset(b.pairs, 0, 80ull * ((ntris + 1) / 2))) != cudaSuccess ||
         (e = cudaMemcpy(d_tris9, tris, 36ull * ntris, cudaMemcpyHostToDevice)) != cudaSuccess ||
         (e = launch_write_tris(ctx, b, static_cast<const float*>(d_tris9), ctx->stream)) != cudaSuccess ||
@@ -782,6 +822,135 @@ int bvhgpu_scene_intersect(bvhgpu_ctx* ctx, uint32_t scene_id, const bvhgpu_ray*
     if (rc) return rc;
     CK(cudaMemcpyAsync(hits, ctx->stage_out, 20ull * n, cudaMemcpyDeviceToHost, ctx->stream), "download hits");
     return finish(ctx);
+}
+
+// ---- differentiable Lambertian render ---------------------------------------------------------------
+
+int bvhgpu_mesh_create(bvhgpu_ctx* ctx, uint32_t blas_id, const uint32_t* faces, uint32_t nfaces, const float* verts,
+                       const float* vnormals, uint32_t nverts, uint32_t* mesh_id) {
+    if (!ctx || !faces || !verts || !vnormals || !mesh_id || nverts == 0) return BVHGPU_ERR_INVALID_ARG;
+    DeviceBlas* b = find_blas(ctx, blas_id);
+    if (!b) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown BLAS %u", blas_id);
+    if (nfaces != b->ntris) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "mesh has %u faces, BLAS %u triangles", nfaces, b->ntris);
+    for (uint64_t i = 0; i < 3ull * nfaces; ++i)
+        if (faces[i] >= nverts) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "face index %u past %u vertices", faces[i], nverts);
+    DeviceMesh m;
+    m.blas = blas_id;
+    m.nfaces = nfaces;
+    m.nverts = nverts;
+    cudaError_t e;
+    if ((e = cudaMalloc(&m.faces, 12ull * nfaces)) != cudaSuccess || (e = cudaMalloc(&m.verts, 12ull * nverts)) != cudaSuccess ||
+        (e = cudaMalloc(&m.vnormals, 12ull * nverts)) != cudaSuccess) {
+        free_mesh(m);
+        return fail(ctx, BVHGPU_ERR_OUT_OF_MEMORY, "mesh_create: %s", cudaGetErrorString(e));
+    }
+    if ((e = cudaMemcpy(m.faces, faces, 12ull * nfaces, cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(m.verts, verts, 12ull * nverts, cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(m.vnormals, vnormals, 12ull * nverts, cudaMemcpyHostToDevice)) != cudaSuccess) {
+        free_mesh(m);
+        return cuda_fail(ctx, e, "mesh_create");
+    }
+    uint32_t id = ctx->next_mesh++;
+    ctx->meshes[id] = m;
+    *mesh_id = id;
+    return BVHGPU_OK;
+}
+
+int bvhgpu_mesh_free(bvhgpu_ctx* ctx, uint32_t mesh_id) {
+    if (!ctx) return BVHGPU_ERR_INVALID_ARG;
+    DeviceMesh* m = find_mesh(ctx, mesh_id);
+    if (!m) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown mesh %u", mesh_id);
+    cudaStreamSynchronize(ctx->stream);
+    free_mesh(*m);
+    ctx->meshes.erase(mesh_id);
+    return BVHGPU_OK;
+}
+
+int bvhgpu_mesh_vertices(bvhgpu_ctx* ctx, uint32_t mesh_id, float** d_verts) {
+    if (!ctx || !d_verts) return BVHGPU_ERR_INVALID_ARG;
+    DeviceMesh* m = find_mesh(ctx, mesh_id);
+    if (!m) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown mesh %u", mesh_id);
+    *d_verts = m->verts;
+    return BVHGPU_OK;
+}
+
+int bvhgpu_mesh_update_async(bvhgpu_ctx* ctx, uint32_t mesh_id, bvhgpu_stream s) {
+    if (!ctx) return BVHGPU_ERR_INVALID_ARG;
+    DeviceMesh* m = find_mesh(ctx, mesh_id);
+    if (!m) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown mesh %u", mesh_id);
+    DeviceBlas* b = find_blas(ctx, m->blas);
+    if (!b) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "mesh %u: BLAS %u was freed", mesh_id, m->blas);
+    CK(launch_mesh_update(ctx, *m, *b, pick(ctx, s)), "mesh update");
+    return BVHGPU_OK;
+}
+
+int bvhgpu_mesh_set_vertices(bvhgpu_ctx* ctx, uint32_t mesh_id, const float* verts) {
+    if (!ctx || !verts) return BVHGPU_ERR_INVALID_ARG;
+    DeviceMesh* m = find_mesh(ctx, mesh_id);
+    if (!m) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown mesh %u", mesh_id);
+    CK(cudaStreamSynchronize(ctx->stream), "stream synchronize");
+    CK(cudaMemcpy(m->verts, verts, 12ull * m->nverts, cudaMemcpyHostToDevice), "upload vertices");
+    int rc = bvhgpu_mesh_update_async(ctx, mesh_id, nullptr);
+    if (rc) return rc;
+    return finish(ctx);
+}
+
+int bvhgpu_lambert_forward_async(bvhgpu_ctx* ctx, uint32_t mesh_id, const bvhgpu_ray* d_rays, uint32_t n,
+                                 const float light[3], float* d_image, bvhgpu_hit* d_hits, bvhgpu_stream s) {
+    if (!ctx || !light || (n && (!d_rays || !d_image || !d_hits))) return BVHGPU_ERR_INVALID_ARG;
+    DeviceMesh* m = find_mesh(ctx, mesh_id);
+    if (!m) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown mesh %u", mesh_id);
+    DeviceBlas* b = find_blas(ctx, m->blas);
+    if (!b) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "mesh %u: BLAS %u was freed", mesh_id, m->blas);
+    CK(launch_lambert_forward(ctx, *m, *b, reinterpret_cast<const float4*>(d_rays), n, light, d_image, d_hits,
+                              pick(ctx, s)),
+       "lambert forward");
+    return BVHGPU_OK;
+}
+
+int bvhgpu_mse_loss(bvhgpu_ctx* ctx, const float* d_image, const float* d_target, uint32_t n, double* loss) {
+    if (!ctx || !loss || (n && (!d_image || !d_target))) return BVHGPU_ERR_INVALID_ARG;
+    if (n == 0) {
+        *loss = 0.0;
+        return BVHGPU_OK;
+    }
+    size_t nb = (n + 255) / 256;
+    if (ctx->mse_partials_cap < nb) {
+        cudaFree(ctx->mse_partials);
+        ctx->mse_partials = nullptr;
+        ctx->mse_partials_cap = 0;
+        CK(cudaMalloc(&ctx->mse_partials, 8 * nb), "loss partials");
+        ctx->mse_partials_cap = nb;
+    }
+    CK(launch_mse_partials(ctx, d_image, d_target, n, ctx->mse_partials, ctx->stream), "loss");
+    std::vector<double> parts(nb);
+    CK(cudaMemcpyAsync(parts.data(), ctx->mse_partials, 8 * nb, cudaMemcpyDeviceToHost, ctx->stream), "loss copy");
+    int rc = finish(ctx);
+    if (rc) return rc;
+    double sum = 0.0;
+    for (double p : parts) sum += p;
+    *loss = sum / (double)n;
+    return BVHGPU_OK;
+}
+
+int bvhgpu_lambert_adjoint_async(bvhgpu_ctx* ctx, uint32_t mesh_id, const bvhgpu_ray* d_rays, uint32_t n,
+                                 const float light[3], const bvhgpu_hit* d_hits, const float* d_image,
+                                 const float* d_target, float* d_grad, bvhgpu_stream s) {
+    if (!ctx || !light || (n && (!d_rays || !d_hits || !d_image || !d_target || !d_grad))) return BVHGPU_ERR_INVALID_ARG;
+    DeviceMesh* m = find_mesh(ctx, mesh_id);
+    if (!m) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown mesh %u", mesh_id);
+    CK(launch_lambert_adjoint(ctx, *m, reinterpret_cast<const float4*>(d_rays), n, light, d_hits, d_image, d_target,
+                              d_grad, pick(ctx, s)),
+       "lambert adjoint");
+    return BVHGPU_OK;
+}
+
+int bvhgpu_mesh_sgd_step_async(bvhgpu_ctx* ctx, uint32_t mesh_id, float* d_grad, float lr, bvhgpu_stream s) {
+    if (!ctx || !d_grad) return BVHGPU_ERR_INVALID_ARG;
+    DeviceMesh* m = find_mesh(ctx, mesh_id);
+    if (!m) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown mesh %u", mesh_id);
+    CK(launch_sgd(ctx, *m, d_grad, lr, pick(ctx, s)), "sgd step");
+    return BVHGPU_OK;
 }
 
 // ---- render -------------------------------------------------------------------------------------

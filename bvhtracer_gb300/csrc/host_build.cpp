@@ -61,6 +61,7 @@ inline uint64_t f32_to_usize(float f) {
 
 struct Builder {
     float* tris;       // n x 9, permuted in place
+    uint32_t* perm = nullptr;  // optional: original index of the triangle at each position
     uint32_t n;
     std::vector<float> cent;  // n x 3
     bvhgpu_node* nodes;
@@ -179,6 +180,7 @@ struct Builder {
         std::memcpy(tris + 9ull * a, tris + 9ull * b, sizeof(tmp));
         std::memcpy(tris + 9ull * b, tmp, sizeof(tmp));
         for (int k = 0; k < 3; ++k) std::swap(cent[3ull * a + k], cent[3ull * b + k]);
+        if (perm) std::swap(perm[a], perm[b]);
     }
 
     // subdivide (bvh.rs:396-467) as a work list.  Returns false where the reference panics.
@@ -229,7 +231,8 @@ struct Builder {
 
 }  // namespace
 
-int build_bvh_host(bvhgpu_triangle* mesh, uint32_t n, bvhgpu_node* nodes_out, uint32_t* nodes_used) {
+int build_bvh_host(bvhgpu_triangle* mesh, uint32_t n, bvhgpu_node* nodes_out, uint32_t* nodes_used,
+                   uint32_t* perm_out) {
     static_assert(sizeof(bvhgpu_node) == 32, "node layout");
     static_assert(sizeof(bvhgpu_triangle) == 36, "triangle layout");
     if (!mesh || !nodes_out || !nodes_used || n == 0 || n > 0x7FFFFFFFu) return BVHGPU_ERR_INVALID_ARG;
@@ -238,6 +241,10 @@ int build_bvh_host(bvhgpu_triangle* mesh, uint32_t n, bvhgpu_node* nodes_out, ui
     b.tris = reinterpret_cast<float*>(mesh);
     b.n = n;
     b.nodes = nodes_out;
+    if (perm_out) {
+        for (uint32_t i = 0; i < n; ++i) perm_out[i] = i;
+        b.perm = perm_out;
+    }
     b.compute_centroids();
     nodes_out[0].left_first = 0;
     nodes_out[0].primitive_count = n;

@@ -24,6 +24,8 @@ struct DeviceBlas {
     uint32_t* parent = nullptr;  // parent index per node (refit), 0xFFFFFFFF for root/filler
     uint32_t* leaves = nullptr;  // indices of leaf nodes (refit start points)
     uint32_t* counters = nullptr;// refit arrival counters, one per node (kept zeroed)
+    uint32_t* tri_leaf = nullptr;        // leaf slot (index into `leaves`) of each triangle, or none
+    unsigned long long* leaf_keys = nullptr;  // refit reduction keys, 6 per leaf (kept at identity)
     uint32_t nodes_used = 0;
     uint32_t ntris = 0;
     uint32_t nleaves = 0;
@@ -46,6 +48,15 @@ struct DeviceScene {
     uint32_t tlas_depth_cap = 0;
 };
 
+struct DeviceMesh {
+    uint32_t blas = 0;           // BLAS whose triangle i is face i
+    uint32_t* faces = nullptr;   // 3 vertex ids per face, in the BLAS's triangle order
+    float* verts = nullptr;      // 3 floats per vertex
+    float* vnormals = nullptr;   // 3 floats per vertex (fixed shading normals)
+    uint32_t nfaces = 0;
+    uint32_t nverts = 0;
+};
+
 struct ProfileRec {
     int kernel;
     cudaEvent_t start, stop;
@@ -64,8 +75,12 @@ struct bvhgpu_ctx {
     std::string last_error;
     std::map<uint32_t, bvhgpu::DeviceBlas> blas;
     std::map<uint32_t, bvhgpu::DeviceScene> scenes;
+    std::map<uint32_t, bvhgpu::DeviceMesh> meshes;
     uint32_t next_blas = 1;
     uint32_t next_scene = 1;
+    uint32_t next_mesh = 1;
+    double* mse_partials = nullptr;  // per-block partial sums of the loss
+    size_t mse_partials_cap = 0;
     // staging buffers for host-pointer entry points (grown on demand)
     void* stage_in = nullptr;
     size_t stage_in_bytes = 0;
@@ -124,7 +139,19 @@ cudaError_t launch_tlas_rebuild(bvhgpu_ctx* ctx, DeviceScene& sc, cudaStream_t s
 cudaError_t launch_trace_scene(bvhgpu_ctx* ctx, DeviceScene& sc, const float4* rays, uint32_t n, void* hits,
                                cudaStream_t s);
 
+// ---- launchers (kernels_adjoint.cu) ----------------------------------------------------
+cudaError_t launch_mesh_update(bvhgpu_ctx* ctx, DeviceMesh& m, DeviceBlas& b, cudaStream_t s);
+cudaError_t launch_lambert_forward(bvhgpu_ctx* ctx, DeviceMesh& m, const DeviceBlas& b, const float4* rays, uint32_t n,
+                                   const float* light, float* image, void* hits, cudaStream_t s);
+cudaError_t launch_mse_partials(bvhgpu_ctx* ctx, const float* image, const float* target, uint32_t n, double* partials,
+                                cudaStream_t s);
+cudaError_t launch_lambert_adjoint(bvhgpu_ctx* ctx, DeviceMesh& m, const float4* rays, uint32_t n, const float* light,
+                                   const void* hits, const float* image, const float* target, float* grad,
+                                   cudaStream_t s);
+cudaError_t launch_sgd(bvhgpu_ctx* ctx, DeviceMesh& m, float* grad, float lr, cudaStream_t s);
+
 // ---- host SAH build (host_build.cpp) ----------------------------------------------------
-int build_bvh_host(bvhgpu_triangle* mesh, uint32_t n, bvhgpu_node* nodes_out, uint32_t* nodes_used);
+int build_bvh_host(bvhgpu_triangle* mesh, uint32_t n, bvhgpu_node* nodes_out, uint32_t* nodes_used,
+                   uint32_t* perm_out);
 
 }  // namespace bvhgpu

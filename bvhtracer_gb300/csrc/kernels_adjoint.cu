@@ -1,0 +1,312 @@
+// Differentiable Lambertian render on an indexed mesh (not in the reference).
+//
+// Forward, per camera ray: closest hit through the reference-built BLAS (same traversal as
+// every other trace), hit record {t, u, v, prim} checkpointed, and
+//     p = o + d t,  l = L - p,  n = n0 (1 - u - v) + n1 u + n2 v  (renderer.rs:268-272),
+//     I = max(0, normalize(n) . normalize(l))
+// with the vertex normals n_i held fixed.  Adjoint, per pixel, from the checkpointed record
+// (no re-trace, visibility fixed): dLoss/dI -> dI/d(t, u, v) -> vertices.  For the
+// Moeller-Trumbore solution x = (t, u, v) of M x = o - v0 with M = [-d | e1 | e2],
+//     dx/dv0 = -(1 - u - v) M^-1,  dx/dv1 = -u M^-1,  dx/dv2 = -v M^-1,
+// so dLoss/dv_k = -w_k y with y = M^-T dLoss/dx = (g_t (e1 x e2) + g_u (d x e2) + g_v (e1 x d)) / a,
+// a = e1 . (d x e2) being the Moeller-Trumbore determinant.  Vertex gradients are accumulated
+// with atomicAdd through the face index map.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "common.cuh"
+#include "internal.hpp"
+
+namespace bvhgpu {
+
+// Defined in kernels_trace.cu (same translation-unit-local helpers re-declared here).
+namespace {
+
+constexpr int kBlock = 128;
+constexpr unsigned kFull = 0xFFFFFFFFu;
+constexpr uint32_t kBigLeaf = 16;
+
+inline unsigned grid_for(uint32_t n, int block) { return (unsigned)((n + block - 1) / block); }
+
+inline GBlas to_gblas(const DeviceBlas& b) {
+    GBlas g;
+    g.nodes = b.nodes;
+    g.tris = b.tris;
+    g.pairs = b.pairs;
+    g.nodes_used = b.nodes_used;
+    g.ntris = b.ntris;
+    g.root_count = b.root_count;
+    g.root_first = b.root_first;
+    return g;
+}
+
+template <int STACK>
+__device__ __forceinline__ void warp_trace_local(const GBlas& b, bool active, LaneRay& r, uint32_t* err) {
+    Trav<STACK> tr;
+    if (active) tr.init(b);
+    StepResult st = active ? kStepContinue : kStepFinished;
+    const unsigned lane = threadIdx.x & 31u;
+    for (;;) {
+        if (st == kStepContinue) st = tr.advance(b, r, kBigLeaf, err);
+        unsigned pend = __ballot_sync(kFull, st == kStepBigLeaf);
+        if (pend == 0u) break;
+        while (pend) {
+            const int leader = __ffs(pend) - 1;
+            const uint32_t f = __shfl_sync(kFull, tr.first, leader);
+            const uint32_t c = __shfl_sync(kFull, tr.cnt, leader);
+            unsigned group = __ballot_sync(kFull, ((pend >> lane) & 1u) && tr.first == f);
+            pend &= ~group;
+            while (group) {
+                const int a = __ffs(group) - 1;
+                group &= group - 1u;
+                if (group) {
+                    const int bb = __ffs(group) - 1;
+                    group &= group - 1u;
+                    coop_leaf2(b.pairs, f, c, a, bb, r);
+                    if ((int)lane == a || (int)lane == bb) st = tr.pop() ? kStepFinished : kStepContinue;
+                } else {
+                    coop_leaf(b.pairs, f, c, a, r);
+                    if ((int)lane == a) st = tr.pop() ? kStepFinished : kStepContinue;
+                }
+            }
+        }
+    }
+}
+
+struct Shade {
+    float3 d, lh, nh, n0, n1, n2, e1, e2;
+    float ll, nl, c;
+};
+
+__device__ __forceinline__ float3 ld3(const float* p) { return make_float3(p[0], p[1], p[2]); }
+__device__ __forceinline__ float3 sub3(float3 a, float3 b) { return make_float3(fsub(a.x, b.x), fsub(a.y, b.y), fsub(a.z, b.z)); }
+__device__ __forceinline__ float3 add3(float3 a, float3 b) { return make_float3(fadd(a.x, b.x), fadd(a.y, b.y), fadd(a.z, b.z)); }
+__device__ __forceinline__ float3 scale3(float3 a, float s) { return make_float3(fmul(a.x, s), fmul(a.y, s), fmul(a.z, s)); }
+__device__ __forceinline__ float dotv(float3 a, float3 b) { return dot3(a.x, a.y, a.z, b.x, b.y, b.z); }
+__device__ __forceinline__ float3 crossv(float3 a, float3 b) {
+    return make_float3(fsub(fmul(a.y, b.z), fmul(a.z, b.y)), fsub(fmul(a.z, b.x), fmul(a.x, b.z)),
+                       fsub(fmul(a.x, b.y), fmul(a.y, b.x)));
+}
+
+// Shading of a hit (t, u, v) on face f.  Returns the clamped intensity and the intermediates.
+__device__ __forceinline__ float shade(float3 o, float3 d, float t, float u, float v, const uint32_t* faces,
+                                       uint32_t f, const float* verts, const float* vnormals, float3 light,
+                                       Shade& s) {
+    const uint32_t i0 = faces[3ull * f], i1 = faces[3ull * f + 1], i2 = faces[3ull * f + 2];
+    float3 p = add3(o, scale3(d, t));
+    float3 l = sub3(light, p);
+    s.ll = __fsqrt_rn(dotv(l, l));
+    s.lh = make_float3(__fdiv_rn(l.x, s.ll), __fdiv_rn(l.y, s.ll), __fdiv_rn(l.z, s.ll));
+    s.n0 = ld3(vnormals + 3ull * i0);
+    s.n1 = ld3(vnormals + 3ull * i1);
+    s.n2 = ld3(vnormals + 3ull * i2);
+    float w0 = fsub(fsub(1.0f, u), v);
+    float3 n = add3(add3(scale3(s.n0, w0), scale3(s.n1, u)), scale3(s.n2, v));
+    s.nl = __fsqrt_rn(dotv(n, n));
+    s.nh = make_float3(__fdiv_rn(n.x, s.nl), __fdiv_rn(n.y, s.nl), __fdiv_rn(n.z, s.nl));
+    s.c = dotv(s.nh, s.lh);
+    s.d = d;
+    float3 v0 = ld3(verts + 3ull * i0);
+    s.e1 = sub3(ld3(verts + 3ull * i1), v0);
+    s.e2 = sub3(ld3(verts + 3ull * i2), v0);
+    return s.c > 0.0f ? s.c : 0.0f;
+}
+
+__global__ void k_mesh_tris(const float* __restrict__ verts, const uint32_t* __restrict__ faces, uint32_t nf,
+                            float4* __restrict__ tris, float4* __restrict__ tverts, float* __restrict__ pairs) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nf) return;
+    const float* a = verts + 3ull * faces[3ull * i];
+    const float* b = verts + 3ull * faces[3ull * i + 1];
+    const float* c = verts + 3ull * faces[3ull * i + 2];
+    float4 v0 = make_float4(a[0], a[1], a[2], 0.0f), v1 = make_float4(b[0], b[1], b[2], 0.0f),
+           v2 = make_float4(c[0], c[1], c[2], 0.0f);
+    float4 e1 = make_float4(fsub(v1.x, v0.x), fsub(v1.y, v0.y), fsub(v1.z, v0.z), 0.0f);
+    float4 e2 = make_float4(fsub(v2.x, v0.x), fsub(v2.y, v0.y), fsub(v2.z, v0.z), 0.0f);
+    tris[3ull * i] = v0;
+    tris[3ull * i + 1] = e1;
+    tris[3ull * i + 2] = e2;
+    tverts[3ull * i] = v0;
+    tverts[3ull * i + 1] = v1;
+    tverts[3ull * i + 2] = v2;
+    float comp[9] = {v0.x, v0.y, v0.z, e1.x, e1.y, e1.z, e2.x, e2.y, e2.z};
+    float* P = pairs + 20ull * (i >> 1) + (i & 1u);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) P[2 * k] = comp[k];
+}
+
+template <int STACK>
+__global__ void __launch_bounds__(kBlock) k_lambert_forward(GBlas b, const float4* __restrict__ rays, uint32_t n,
+                                                            const uint32_t* __restrict__ faces,
+                                                            const float* __restrict__ verts,
+                                                            const float* __restrict__ vnormals, float3 light,
+                                                            float* __restrict__ image, GHit* __restrict__ hits,
+                                                            uint32_t* err) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (__all_sync(kFull, i >= n)) return;
+    const bool active = i < n;
+    LaneRay r;
+    float3 o = make_float3(0, 0, 0), d = o;
+    if (active) {
+        float t0;
+        load_ray(rays, i, o, d, t0);
+        r.o = o;
+        r.d = d;
+        r.rd = recip3(d);
+        r.ct = t0;
+        r.hu = r.hv = 0.0f;
+        r.hp = 0;
+        r.hit = false;
+    }
+    warp_trace_local<STACK>(b, active, r, err);
+    if (!active) return;
+    const bool hit = r.hit && r.ct < FLT_MAX;
+    store_hit(hits, i, hit, r.ct, r.hu, r.hv, r.hp, 0u);
+    float I = 0.0f;
+    if (hit) {
+        Shade s;
+        I = shade(o, d, r.ct, r.hu, r.hv, faces, r.hp, verts, vnormals, light, s);
+    }
+    image[i] = I;
+}
+
+// Per-block partial sums of (I - T)^2 in double.
+__global__ void k_mse_partials(const float* __restrict__ image, const float* __restrict__ target, uint32_t n,
+                               double* __restrict__ partials) {
+    __shared__ double sh[256];
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    double v = 0.0;
+    if (i < n) {
+        double e = (double)image[i] - (double)target[i];
+        v = e * e;
+    }
+    sh[threadIdx.x] = v;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if ((int)threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partials[blockIdx.x] = sh[0];
+}
+
+__global__ void __launch_bounds__(kBlock) k_lambert_adjoint(const float4* __restrict__ rays, uint32_t n,
+                                                            const GHit* __restrict__ hits,
+                                                            const float* __restrict__ image,
+                                                            const float* __restrict__ target,
+                                                            const uint32_t* __restrict__ faces,
+                                                            const float* __restrict__ verts,
+                                                            const float* __restrict__ vnormals, float3 light,
+                                                            float scale, float* __restrict__ grad) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const GHit h = hits[i];
+    if (h.prim == kMiss) return;
+    float3 o, d;
+    float t0;
+    load_ray(rays, i, o, d, t0);
+    Shade s;
+    float I = shade(o, d, h.t, h.u, h.v, faces, h.prim, verts, vnormals, light, s);
+    if (!(s.c > 0.0f)) return;  // max(0, .) is flat there
+    const float g = fmul(scale, fsub(image[i], target[i]));  // dLoss/dI of the mean squared error
+    (void)I;
+    // dI/dn = (lh - c nh) / |n|,  dI/dl = (nh - c lh) / |l|
+    float3 dn = scale3(sub3(s.lh, scale3(s.nh, s.c)), __frcp_rn(s.nl));
+    float3 dl = scale3(sub3(s.nh, scale3(s.lh, s.c)), __frcp_rn(s.ll));
+    const float gt = fmul(g, -dotv(dl, d));                 // l = L - o - t d
+    const float gu = fmul(g, dotv(dn, sub3(s.n1, s.n0)));
+    const float gv = fmul(g, dotv(dn, sub3(s.n2, s.n0)));
+    const float a = dotv(s.e1, crossv(d, s.e2));
+    const float f = __frcp_rn(a);
+    float3 y = add3(add3(scale3(crossv(s.e1, s.e2), gt), scale3(crossv(d, s.e2), gu)), scale3(crossv(s.e1, d), gv));
+    y = scale3(y, f);
+    const float w[3] = {fsub(fsub(1.0f, h.u), h.v), h.u, h.v};
+    for (int k = 0; k < 3; ++k) {
+        const uint32_t vid = faces[3ull * h.prim + k];
+        const float m = -w[k];
+        atomicAdd(grad + 3ull * vid, fmul(m, y.x));
+        atomicAdd(grad + 3ull * vid + 1, fmul(m, y.y));
+        atomicAdd(grad + 3ull * vid + 2, fmul(m, y.z));
+    }
+}
+
+__global__ void k_sgd(float* __restrict__ verts, float* __restrict__ grad, uint32_t count, float lr) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    verts[i] = fsub(verts[i], fmul(lr, grad[i]));
+    grad[i] = 0.0f;
+}
+
+inline int stack_variant(uint32_t depth) {
+    if (depth <= 33) return 32;
+    if (depth <= 65) return 64;
+    if (depth <= 129) return 128;
+    return 256;
+}
+
+}  // namespace
+
+cudaError_t launch_mesh_update(bvhgpu_ctx* ctx, DeviceMesh& m, DeviceBlas& b, cudaStream_t s) {
+    {
+        LaunchScope scope(ctx, BVHGPU_K_OTHER, s);
+        k_mesh_tris<<<grid_for(m.nfaces, 256), 256, 0, s>>>(m.verts, m.faces, m.nfaces, b.tris, b.verts,
+                                                            reinterpret_cast<float*>(b.pairs));
+        g_launches++;
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    return launch_refit(ctx, b, s);
+}
+
+cudaError_t launch_lambert_forward(bvhgpu_ctx* ctx, DeviceMesh& m, const DeviceBlas& b, const float4* rays, uint32_t n,
+                                   const float* light, float* image, void* hits, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    GBlas g = to_gblas(b);
+    float3 L = make_float3(light[0], light[1], light[2]);
+    LaunchScope scope(ctx, BVHGPU_K_LAMBERT_FORWARD, s);
+    switch (stack_variant(b.depth)) {
+        case 32:
+            k_lambert_forward<32><<<grid_for(n, kBlock), kBlock, 0, s>>>(g, rays, n, m.faces, m.verts, m.vnormals, L,
+                                                                         image, static_cast<GHit*>(hits), ctx->d_err);
+            break;
+        case 64:
+            k_lambert_forward<64><<<grid_for(n, kBlock), kBlock, 0, s>>>(g, rays, n, m.faces, m.verts, m.vnormals, L,
+                                                                         image, static_cast<GHit*>(hits), ctx->d_err);
+            break;
+        default:
+            k_lambert_forward<256><<<grid_for(n, kBlock), kBlock, 0, s>>>(g, rays, n, m.faces, m.verts, m.vnormals, L,
+                                                                          image, static_cast<GHit*>(hits), ctx->d_err);
+            break;
+    }
+    g_launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mse_partials(bvhgpu_ctx* ctx, const float* image, const float* target, uint32_t n, double* partials,
+                                cudaStream_t s) {
+    LaunchScope scope(ctx, BVHGPU_K_OTHER, s);
+    k_mse_partials<<<grid_for(n, 256), 256, 0, s>>>(image, target, n, partials);
+    g_launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_lambert_adjoint(bvhgpu_ctx* ctx, DeviceMesh& m, const float4* rays, uint32_t n, const float* light,
+                                   const void* hits, const float* image, const float* target, float* grad,
+                                   cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    float3 L = make_float3(light[0], light[1], light[2]);
+    LaunchScope scope(ctx, BVHGPU_K_LAMBERT_ADJOINT, s);
+    k_lambert_adjoint<<<grid_for(n, kBlock), kBlock, 0, s>>>(rays, n, static_cast<const GHit*>(hits), image, target,
+                                                             m.faces, m.verts, m.vnormals, L, 2.0f / (float)n, grad);
+    g_launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sgd(bvhgpu_ctx* ctx, DeviceMesh& m, float* grad, float lr, cudaStream_t s) {
+    LaunchScope scope(ctx, BVHGPU_K_OTHER, s);
+    k_sgd<<<grid_for(3 * m.nverts, 256), 256, 0, s>>>(m.verts, grad, 3 * m.nverts, lr);
+    g_launches++;
+    return cudaGetLastError();
+}
+
+}  // namespace bvhgpu

@@ -61,30 +61,116 @@ __global__ void k_write_tris(const float* __restrict__ tris9, uint32_t n, float4
     for (int k = 0; k < 9; ++k) P[2 * k] = c[k];
 }
 
-__global__ void __launch_bounds__(kBlock) k_refit(float4* nodes, const float4* __restrict__ tris,
-                                                  const uint32_t* __restrict__ leaves, uint32_t nleaves,
-                                                  const uint32_t* __restrict__ parent, uint32_t* counters) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nleaves) return;
-    uint32_t ni = leaves[i];
-    float4 lo = nodes[2ull * ni];
-    float4 hi = nodes[2ull * ni + 1];
-    uint32_t first = __float_as_uint(lo.w);
-    uint32_t cnt = __float_as_uint(hi.w);
-    // update_node_bounds (bvh.rs:317-330)
-    float mnx = FLT_MAX, mny = FLT_MAX, mnz = FLT_MAX, mxx = -FLT_MAX, mxy = -FLT_MAX, mxz = -FLT_MAX;
-    for (uint32_t k = 0; k < cnt; ++k) {
-        const float4* T = tris + 3ull * (first + k);
-        float4 a = T[0], b = T[1], c = T[2];
-        mnx = min_ni(min_ni(min_ni(mnx, a.x), b.x), c.x);
-        mny = min_ni(min_ni(min_ni(mny, a.y), b.y), c.y);
-        mnz = min_ni(min_ni(min_ni(mnz, a.z), b.z), c.z);
-        mxx = max_ni(max_ni(max_ni(mxx, a.x), b.x), c.x);
-        mxy = max_ni(max_ni(max_ni(mxy, a.y), b.y), c.y);
-        mxz = max_ni(max_ni(max_ni(mxz, a.z), b.z), c.z);
+// ---- refit, parallel over triangles --------------------------------------------------------
+// update_node_bounds (bvh.rs:317-330) folds a leaf's vertices in order v0, v1, v2 of triangle
+// first, first+1, ... with f32::min / f32::max.  The fold's result is the minimum (maximum)
+// value, and among equal values (only +0 / -0 differ in bits) the first one in that order.  The
+// same result is computed in parallel with 64-bit keys: an order-preserving map of the value
+// with both zeros mapped to one rank, then the position in the fold order (lower wins on a tie).
+// NaNs are skipped, as f32::min skips them.  The reduced key names the winning vertex, whose
+// actual bits are read back.
+__device__ __forceinline__ uint32_t ordered(float f) {
+    uint32_t b = __float_as_uint(f);
+    if (f == 0.0f) return 0x80000000u;
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+
+// Segmented min of 64-bit keys over consecutive lanes with the same segment id (leaf): the
+// first lane of each segment ends up holding the segment's minimum.
+__device__ __forceinline__ unsigned long long seg_min(unsigned long long k, uint32_t seg) {
+    const unsigned lane = threadIdx.x & 31u;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        unsigned long long o = __shfl_down_sync(kFull, k, off);
+        uint32_t os = __shfl_down_sync(kFull, seg, off);
+        if (lane + off < 32u && os == seg && o < k) k = o;
     }
-    nodes[2ull * ni] = make_float4(mnx, mny, mnz, lo.w);
-    nodes[2ull * ni + 1] = make_float4(mxx, mxy, mxz, hi.w);
+    return k;
+}
+__device__ __forceinline__ unsigned long long seg_max(unsigned long long k, uint32_t seg) {
+    const unsigned lane = threadIdx.x & 31u;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        unsigned long long o = __shfl_down_sync(kFull, k, off);
+        uint32_t os = __shfl_down_sync(kFull, seg, off);
+        if (lane + off < 32u && os == seg && o > k) k = o;
+    }
+    return k;
+}
+
+constexpr unsigned long long kKeyMinIdentity = 0xFFFFFFFFFFFFFFFFull;
+constexpr unsigned long long kKeyMaxIdentity = 0ull;
+
+// One thread per triangle: keys of its three vertices per axis, reduced over the warp's lanes of
+// the same leaf, then one atomicMin / atomicMax per (leaf, axis) from the segment's first lane.
+// keys: 6 per leaf slot (min x y z, max x y z), at the identity before the launch.
+__global__ void __launch_bounds__(256) k_refit_tris(const float4* __restrict__ verts, uint32_t ntris,
+                                                    const uint32_t* __restrict__ tri_leaf,
+                                                    unsigned long long* keys) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned lane = threadIdx.x & 31u;
+    uint32_t slot = kNone;
+    float4 v[3];
+    if (i < ntris) {
+        slot = tri_leaf[i];
+        v[0] = verts[3ull * i];
+        v[1] = verts[3ull * i + 1];
+        v[2] = verts[3ull * i + 2];
+    }
+    const uint32_t prev = __shfl_up_sync(kFull, slot, 1);
+    const bool head = slot != kNone && (lane == 0u || prev != slot);
+#pragma unroll
+    for (int axis = 0; axis < 3; ++axis) {
+        unsigned long long kmin = kKeyMinIdentity, kmax = kKeyMaxIdentity;
+        if (slot != kNone) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const float x = axis == 0 ? v[c].x : (axis == 1 ? v[c].y : v[c].z);
+                if (x != x) continue;
+                const uint32_t pos = 3u * i + (uint32_t)c;
+                const unsigned long long r = (unsigned long long)ordered(x) << 32;
+                const unsigned long long a = r | pos, b = r | (0xFFFFFFFFu - pos);
+                if (a < kmin) kmin = a;
+                if (b > kmax) kmax = b;
+            }
+        }
+        kmin = seg_min(kmin, slot);
+        kmax = seg_max(kmax, slot);
+        if (head) {
+            if (kmin != kKeyMinIdentity) atomicMin(&keys[6ull * slot + axis], kmin);
+            if (kmax != kKeyMaxIdentity) atomicMax(&keys[6ull * slot + 3 + axis], kmax);
+        }
+    }
+}
+
+// One thread per leaf: decode the keys into the winning vertices' values (identity = the fold's
+// start value FLT_MAX / -FLT_MAX), reset the keys, write the leaf, then walk up: the second child
+// to arrive at a parent computes it (bvh.rs:490-491: min(left, right), max(left, right)).
+__global__ void __launch_bounds__(kBlock) k_refit_leaves(float4* nodes, const float4* __restrict__ verts,
+                                                         const uint32_t* __restrict__ leaves, uint32_t nleaves,
+                                                         const uint32_t* __restrict__ parent, uint32_t* counters,
+                                                         unsigned long long* keys) {
+    uint32_t li = blockIdx.x * blockDim.x + threadIdx.x;
+    if (li >= nleaves) return;
+    const uint32_t ni = leaves[li];
+    float b[6];
+    for (int k = 0; k < 6; ++k) {
+        const unsigned long long key = keys[6ull * li + k];
+        const bool is_min = k < 3;
+        keys[6ull * li + k] = is_min ? kKeyMinIdentity : kKeyMaxIdentity;
+        if (key == (is_min ? kKeyMinIdentity : kKeyMaxIdentity)) {
+            b[k] = is_min ? FLT_MAX : -FLT_MAX;
+            continue;
+        }
+        uint32_t pos = (uint32_t)(key & 0xFFFFFFFFull);
+        if (!is_min) pos = 0xFFFFFFFFu - pos;
+        const float4 vv = verts[pos];  // pos = 3 * triangle + vertex indexes the float4 vertex array
+        const int axis = k % 3;
+        b[k] = axis == 0 ? vv.x : (axis == 1 ? vv.y : vv.z);
+    }
+    const float4 lo = nodes[2ull * ni], hi = nodes[2ull * ni + 1];
+    nodes[2ull * ni] = make_float4(b[0], b[1], b[2], lo.w);
+    nodes[2ull * ni + 1] = make_float4(b[3], b[4], b[5], hi.w);
     __threadfence();
     uint32_t p = parent[ni];
     while (p != kNone) {
@@ -97,7 +183,6 @@ __global__ void __launch_bounds__(kBlock) k_refit(float4* nodes, const float4* _
         uint32_t l = __float_as_uint(plo.w);
         float4 llo = __ldcg(&nodes[2ull * l]), lhi = __ldcg(&nodes[2ull * l + 1]);
         float4 rlo = __ldcg(&nodes[2ull * l + 2]), rhi = __ldcg(&nodes[2ull * l + 3]);
-        // bvh.rs:490-491: __min(left, right), __max(left, right)
         __stcg(&nodes[2ull * p], make_float4(min_ni(llo.x, rlo.x), min_ni(llo.y, rlo.y), min_ni(llo.z, rlo.z), plo.w));
         __stcg(&nodes[2ull * p + 1],
                make_float4(max_ni(lhi.x, rhi.x), max_ni(lhi.y, rhi.y), max_ni(lhi.z, rhi.z), phi.w));
@@ -354,9 +439,10 @@ cudaError_t launch_write_tris(bvhgpu_ctx* ctx, DeviceBlas& b, const float* d_tri
 cudaError_t launch_refit(bvhgpu_ctx* ctx, DeviceBlas& b, cudaStream_t s) {
     if (b.nleaves == 0) return cudaSuccess;
     LaunchScope scope(ctx, BVHGPU_K_REFIT, s);
-    k_refit<<<grid_for(b.nleaves, kBlock), kBlock, 0, s>>>(b.nodes, b.verts, b.leaves, b.nleaves, b.parent,
-                                                           b.counters);
-    g_launches++;
+    k_refit_tris<<<grid_for(b.ntris, 256), 256, 0, s>>>(b.verts, b.ntris, b.tri_leaf, b.leaf_keys);
+    k_refit_leaves<<<grid_for(b.nleaves, kBlock), kBlock, 0, s>>>(b.nodes, b.verts, b.leaves, b.nleaves, b.parent,
+                                                                  b.counters, b.leaf_keys);
+    g_launches += 2;
     return cudaGetLastError();
 }
 

@@ -243,3 +243,24 @@ def config3_scene(i: int, ntris: int, nrays: int, seed: int = 0):
         box = 10.0
     rnd = sphere_rays(int(nrays - n_prim), sseed + 7, box=box)
     return tris, np.concatenate([prim, rnd])
+
+
+def config4(seed: int = 0, level: int = 7, width: int = 512, height: int = 512, sigma: float = 0.01,
+            scale: float = 10.0):
+    """Differentiable-render workload: displaced icosphere (config-1 displacement) with `level`
+    subdivisions, its radial unit directions as fixed vertex normals, a target mesh whose vertices
+    are moved radially by N(0, sigma^2), a point light at (2, 2, -3), and width x height
+    pixel-centre primaries from distance 3 (tile order) -- all lengths multiplied by `scale`.
+
+    The scale exists because the reference's Moeller-Trumbore test rejects |e1 . (d x e2)| < 1e-4
+    (triangle.rs:47-51), an absolute threshold on a quantity proportional to the triangle's area:
+    at unit radius the 7-subdivision sphere's triangles (edges ~0.01) are all rejected.  A uniform
+    scale leaves the Lambertian image unchanged up to rounding."""
+    mesh = displaced_icosphere(level, seed)
+    verts = (mesh.dirs * (scale * mesh.radius)[:, None]).astype(np.float32)
+    vnormals = mesh.dirs.astype(np.float32)
+    target_r = scale * (mesh.radius + sigma * normal(seed, 40, len(mesh.radius)))
+    target_verts = (mesh.dirs * target_r[:, None]).astype(np.float32)
+    rays = look_at_rays(width, height, (0.0, 0.0, -3.0 * scale), (0.0, 0.0, 0.0), 45.0)
+    light = np.array([2.0 * scale, 2.0 * scale, -3.0 * scale], np.float32)
+    return verts, mesh.faces.astype(np.uint32), vnormals, target_verts, rays, light

@@ -160,7 +160,9 @@ int bvhgpu_event_elapsed_ms(bvhgpu_ctx* ctx, void* start, void* stop, float* ms)
 #define BVHGPU_K_TLAS_BUILD 7
 #define BVHGPU_K_RENDER 8
 #define BVHGPU_K_OTHER 9
-#define BVHGPU_KERNEL_COUNT 10
+#define BVHGPU_K_LAMBERT_FORWARD 10
+#define BVHGPU_K_LAMBERT_ADJOINT 11
+#define BVHGPU_KERNEL_COUNT 12
 int bvhgpu_profile_enable(bvhgpu_ctx* ctx, int enable);
 int bvhgpu_profile_read(bvhgpu_ctx* ctx, double* ms, uint64_t* launches);
 
@@ -168,6 +170,11 @@ int bvhgpu_profile_read(bvhgpu_ctx* ctx, double* ms, uint64_t* launches);
 /* BvhBuilder::build_for (BT/src/model/bvh.rs:524-541) on the host: the reference's SAH binned
  * build (8 bins), reordering `mesh` in place.  nodes_out must hold 2*n nodes. */
 int bvhgpu_build_bvh_host(bvhgpu_triangle* mesh, uint32_t n, bvhgpu_node* nodes_out, uint32_t* nodes_used);
+
+/* Same build, also writing perm_out[i] = the input index of the triangle that ends at position i
+ * (n entries), so that an indexed mesh's faces can follow the reordering. */
+int bvhgpu_build_bvh_host_indexed(bvhgpu_triangle* mesh, uint32_t n, bvhgpu_node* nodes_out, uint32_t* nodes_used,
+                                  uint32_t* perm_out);
 
 /* Upload a reference-built BVH as-is (the node array of Bvh, bvh.rs:227-233, and the mesh's
  * primitives, BT/src/mesh/mesh.rs:126-134).  Validates the tree; the handle replaces
@@ -244,6 +251,37 @@ int bvhgpu_scene_intersect_async(bvhgpu_ctx* ctx, uint32_t scene_id, const bvhgp
 int bvhgpu_render(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhgpu_camera* camera, int width, int height,
                   int accumulator, const float* acc_params, int shader, const float* shader_params,
                   const float* normals, uint8_t* rgba, uint64_t* rays_traced);
+
+/* ---- differentiable Lambertian render (not in the reference) ----------------------------------- */
+/* Indexed mesh over a BLAS: triangle i of the BLAS is (verts[faces[3i]], verts[faces[3i+1]],
+ * verts[faces[3i+2]]), i.e. faces are given in the BLAS's triangle order (see
+ * bvhgpu_build_bvh_host_indexed).  vnormals are per-vertex shading normals, interpolated with the
+ * hit's barycentrics like NormalMappingAccumulator (BT/src/renderer.rs:268-272) and held fixed. */
+int bvhgpu_mesh_create(bvhgpu_ctx* ctx, uint32_t blas_id, const uint32_t* faces, uint32_t nfaces, const float* verts,
+                       const float* vnormals, uint32_t nverts, uint32_t* mesh_id);
+int bvhgpu_mesh_free(bvhgpu_ctx* ctx, uint32_t mesh_id);
+/* Device pointer of the mesh's vertex array (3 floats per vertex), e.g. for a custom update. */
+int bvhgpu_mesh_vertices(bvhgpu_ctx* ctx, uint32_t mesh_id, float** d_verts);
+/* New vertex positions from the host; the BLAS triangles are regenerated and refit. */
+int bvhgpu_mesh_set_vertices(bvhgpu_ctx* ctx, uint32_t mesh_id, const float* verts);
+/* Regenerate the BLAS triangles from the mesh's device vertices and refit (Bvh::refit). */
+int bvhgpu_mesh_update_async(bvhgpu_ctx* ctx, uint32_t mesh_id, bvhgpu_stream s);
+/* Forward: closest hit per ray, hit records {t, u, v, prim} written to d_hits (the checkpoint the
+ * adjoint reuses), image[i] = max(0, n_hat . l_hat) with n the barycentric vertex normal and l the
+ * direction from the hit point to the point light `light` (0 for a miss). */
+int bvhgpu_lambert_forward_async(bvhgpu_ctx* ctx, uint32_t mesh_id, const bvhgpu_ray* d_rays, uint32_t n,
+                                 const float light[3], float* d_image, bvhgpu_hit* d_hits, bvhgpu_stream s);
+/* Mean squared error between image and target (n floats each, device), computed on the device in
+ * double precision; waits for the stream. */
+int bvhgpu_mse_loss(bvhgpu_ctx* ctx, const float* d_image, const float* d_target, uint32_t n, double* loss);
+/* Adjoint of forward + mean squared error: adds dLoss/dvertex (3 floats per vertex) into d_grad,
+ * from the checkpointed hit records (no re-trace; visibility held fixed). */
+int bvhgpu_lambert_adjoint_async(bvhgpu_ctx* ctx, uint32_t mesh_id, const bvhgpu_ray* d_rays, uint32_t n,
+                                 const float light[3], const bvhgpu_hit* d_hits, const float* d_image,
+                                 const float* d_target, float* d_grad, bvhgpu_stream s);
+/* Gradient-descent step on the mesh vertices: verts -= lr * grad, then grad = 0 (call
+ * bvhgpu_mesh_update_async before the next forward). */
+int bvhgpu_mesh_sgd_step_async(bvhgpu_ctx* ctx, uint32_t mesh_id, float* d_grad, float lr, bvhgpu_stream s);
 
 /* ---- refit without allocation ----------------------------------------------------------------- */
 /* No counterpart in the reference.  For callers that cannot call cudaMalloc: engines that own all
