@@ -36,7 +36,7 @@ SHADER_RADIANCE, SHADER_INTERSECTION, SHADER_DEPTH = 0, 1, 2
 MODE_PLAIN, MODE_PERSISTENT = 0, 1
 
 KERNELS = ["trace_blas", "trace_scene", "persistent_bounce", "bounce_gen", "trace_queue", "trace_batch",
-           "refit", "tlas_build", "render", "other", "lambert_forward", "lambert_adjoint"]
+           "refit", "tlas_build", "render", "other", "lambert_forward", "lambert_adjoint", "scene_bounce"]
 
 # Exported symbols and their ctypes signatures (kept in the order of include/bvhgpu.h).
 _P = ctypes.c_void_p
@@ -90,6 +90,16 @@ SIGNATURES = {
     "bvhgpu_scene_download_tlas": (_I, [_P, _U32, _P, _P]),
     "bvhgpu_scene_intersect": (_I, [_P, _U32, _P, _U32, _P]),
     "bvhgpu_scene_intersect_async": (_I, [_P, _U32, _P, _U32, _P, _P]),
+    "bvhgpu_scene_trace_bounce_async": (_I, [_P, _U32, _P, _U32, _U32, _P, _P, _P]),
+    "bvhgpu_scene_bounce_rays": (_I, [_P, _U32, _P, _U32, _U32, _P, _P]),
+    "bvhgpu_scene_download_transforms": (_I, [_P, _U32, _P, _P]),
+    "bvhgpu_mesh_wobble_async": (_I, [_P, _U32, _P, _P, _P, ctypes.c_float, ctypes.c_float, _P, _P]),
+    "bvhgpu_scene_animate_async": (_I, [_P, _U32, _P, _P, _P, _P, _P, _P, _P]),
+    "bvhgpu_advance_time_async": (_I, [_P, _P, ctypes.c_float, _P]),
+    "bvhgpu_graph_begin": (_I, [_P]),
+    "bvhgpu_graph_end": (_I, [_P, _P]),
+    "bvhgpu_graph_launch": (_I, [_P, _U32]),
+    "bvhgpu_graph_free": (_I, [_P, _U32]),
     "bvhgpu_render": (_I, [_P, _U32, _P, _I, _I, _I, _P, _I, _P, _P, _P, _P]),
     "bvhgpu_mesh_create": (_I, [_P, _U32, _P, _U32, _P, _P, _U32, _P]),
     "bvhgpu_mesh_free": (_I, [_P, _U32]),

@@ -96,6 +96,24 @@ class Context:
     def scene(self, blases, transforms=None, inverses=None) -> "Scene":
         return Scene(self, blases, transforms, inverses)
 
+    # -- frame graphs -------------------------------------------------------------------
+    def advance_time_async(self, d_time: "DeviceBuffer", dt: float, stream=None):
+        self.check(self.lib.bvhgpu_advance_time_async(self.h, d_time.ptr, float(dt), stream))
+
+    def graph_begin(self):
+        self.check(self.lib.bvhgpu_graph_begin(self.h))
+
+    def graph_end(self) -> int:
+        gid = ctypes.c_uint32()
+        self.check(self.lib.bvhgpu_graph_end(self.h, ctypes.byref(gid)))
+        return gid.value
+
+    def graph_launch(self, graph_id: int):
+        self.check(self.lib.bvhgpu_graph_launch(self.h, graph_id))
+
+    def graph_free(self, graph_id: int):
+        self.check(self.lib.bvhgpu_graph_free(self.h, graph_id))
+
     def trace_batch(self, items, rays: np.ndarray, mode: int) -> np.ndarray:
         items = np.ascontiguousarray(items, BATCH_ITEM)
         rays = np.ascontiguousarray(rays, RAY)
@@ -343,6 +361,30 @@ class Scene:
     def rebuild_async(self, stream=None):
         self.ctx.check(self.ctx.lib.bvhgpu_scene_rebuild_async(self.ctx.h, self.id, stream))
 
+    def trace_bounce_async(self, d_rays: DeviceBuffer, n: int, seed: int, d_hits0: DeviceBuffer,
+                           d_hits1: DeviceBuffer, stream=None):
+        self.ctx.check(self.ctx.lib.bvhgpu_scene_trace_bounce_async(self.ctx.h, self.id, d_rays.ptr, n, seed,
+                                                                    d_hits0.ptr, d_hits1.ptr, stream))
+
+    def bounce_rays(self, rays: np.ndarray, seed: int):
+        rays = np.ascontiguousarray(rays, RAY)
+        out = np.zeros(len(rays), RAY)
+        valid = np.zeros(len(rays), np.uint8)
+        self.ctx.check(self.ctx.lib.bvhgpu_scene_bounce_rays(self.ctx.h, self.id, ptr(rays), len(rays), seed,
+                                                             ptr(out), ptr(valid)))
+        return out, valid.astype(bool)
+
+    def download_transforms(self):
+        xf = np.zeros((self.nobjects, 16), np.float32)
+        inv = np.zeros((self.nobjects, 16), np.float32)
+        self.ctx.check(self.ctx.lib.bvhgpu_scene_download_transforms(self.ctx.h, self.id, ptr(xf), ptr(inv)))
+        return xf, inv
+
+    def animate_async(self, d_rot0, d_axis, d_omega, d_scale, d_trans, d_time, stream=None):
+        self.ctx.check(self.ctx.lib.bvhgpu_scene_animate_async(self.ctx.h, self.id, d_rot0.ptr, d_axis.ptr,
+                                                               d_omega.ptr, d_scale.ptr, d_trans.ptr, d_time.ptr,
+                                                               stream))
+
     def download_tlas(self):
         nodes = np.zeros(2 * self.nobjects, TLAS_NODE)
         used = ctypes.c_uint32()
@@ -423,6 +465,11 @@ class DiffMesh:
         self.ctx.check(self.ctx.lib.bvhgpu_lambert_adjoint_async(self.ctx.h, self.id, d_rays.ptr, n, ptr(L),
                                                                  d_hits.ptr, d_image.ptr, d_target.ptr, d_grad.ptr,
                                                                  stream))
+
+    def wobble_async(self, d_dirs: DeviceBuffer, d_r0: DeviceBuffer, d_phase: DeviceBuffer, amp: float,
+                     freq: float, d_time: DeviceBuffer, stream=None):
+        self.ctx.check(self.ctx.lib.bvhgpu_mesh_wobble_async(self.ctx.h, self.id, d_dirs.ptr, d_r0.ptr, d_phase.ptr,
+                                                             float(amp), float(freq), d_time.ptr, stream))
 
     def sgd_step_async(self, d_grad: DeviceBuffer, lr: float, stream=None):
         self.ctx.check(self.ctx.lib.bvhgpu_mesh_sgd_step_async(self.ctx.h, self.id, d_grad.ptr, float(lr), stream))

@@ -241,6 +241,10 @@ int bvhgpu_destroy(bvhgpu_ctx* ctx) {
     for (auto& kv : ctx->blas) free_blas(kv.second);
     for (auto& kv : ctx->scenes) free_scene(kv.second);
     for (auto& kv : ctx->meshes) free_mesh(kv.second);
+    for (auto& kv : ctx->graphs) {
+        cudaGraphExecDestroy(kv.second.second);
+        cudaGraphDestroy(kv.second.first);
+    }
     cudaFree(ctx->mse_partials);
     for (auto& r : ctx->prof) {
         cudaEventDestroy(r.start);
@@ -950,6 +954,137 @@ int bvhgpu_mesh_sgd_step_async(bvhgpu_ctx* ctx, uint32_t mesh_id, float* d_grad,
     DeviceMesh* m = find_mesh(ctx, mesh_id);
     if (!m) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown mesh %u", mesh_id);
     CK(launch_sgd(ctx, *m, d_grad, lr, pick(ctx, s)), "sgd step");
+    return BVHGPU_OK;
+}
+
+// ---- instanced frames ----------------------------------------------------------------------------
+
+int bvhgpu_scene_trace_bounce_async(bvhgpu_ctx* ctx, uint32_t scene_id, const bvhgpu_ray* d_rays, uint32_t n,
+                                    uint32_t seed, bvhgpu_hit* d_hits0, bvhgpu_hit* d_hits1, bvhgpu_stream s) {
+    if (!ctx || (n && (!d_rays || !d_hits0 || !d_hits1))) return BVHGPU_ERR_INVALID_ARG;
+    DeviceScene* sc = find_scene(ctx, scene_id);
+    if (!sc) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown scene %u", scene_id);
+    CK(launch_scene_bounce(ctx, *sc, reinterpret_cast<const float4*>(d_rays), n, seed, d_hits0, d_hits1, pick(ctx, s)),
+       "scene bounce");
+    return BVHGPU_OK;
+}
+
+int bvhgpu_scene_bounce_rays(bvhgpu_ctx* ctx, uint32_t scene_id, const bvhgpu_ray* rays, uint32_t n, uint32_t seed,
+                             bvhgpu_ray* out, uint8_t* valid) {
+    if (!ctx || (n && (!rays || !out || !valid))) return BVHGPU_ERR_INVALID_ARG;
+    DeviceScene* sc = find_scene(ctx, scene_id);
+    if (!sc) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown scene %u", scene_id);
+    if (n == 0) return BVHGPU_OK;
+    void *d_rays = nullptr, *d_hits = nullptr, *d_out = nullptr, *d_valid = nullptr;
+    auto done = [&]() {
+        cudaFree(d_rays);
+        cudaFree(d_hits);
+        cudaFree(d_out);
+        cudaFree(d_valid);
+    };
+    if (cudaMalloc(&d_rays, 32ull * n) != cudaSuccess || cudaMalloc(&d_hits, 20ull * n) != cudaSuccess ||
+        cudaMalloc(&d_out, 32ull * n) != cudaSuccess || cudaMalloc(&d_valid, n) != cudaSuccess) {
+        done();
+        return fail(ctx, BVHGPU_ERR_OUT_OF_MEMORY, "scene_bounce_rays buffers");
+    }
+    cudaError_t e;
+    if ((e = cudaMemcpyAsync(d_rays, rays, 32ull * n, cudaMemcpyHostToDevice, ctx->stream)) != cudaSuccess ||
+        (e = launch_trace_scene(ctx, *sc, static_cast<const float4*>(d_rays), n, d_hits, ctx->stream)) != cudaSuccess ||
+        (e = launch_scene_bounce_rays(ctx, *sc, static_cast<const float4*>(d_rays), d_hits, n, seed,
+                                      static_cast<float4*>(d_out), static_cast<uint8_t*>(d_valid), ctx->stream)) !=
+            cudaSuccess ||
+        (e = cudaMemcpyAsync(out, d_out, 32ull * n, cudaMemcpyDeviceToHost, ctx->stream)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(valid, d_valid, n, cudaMemcpyDeviceToHost, ctx->stream)) != cudaSuccess) {
+        done();
+        return cuda_fail(ctx, e, "scene_bounce_rays");
+    }
+    int rc = finish(ctx);
+    done();
+    return rc;
+}
+
+int bvhgpu_scene_download_transforms(bvhgpu_ctx* ctx, uint32_t scene_id, float* xf, float* inv) {
+    if (!ctx || !xf || !inv) return BVHGPU_ERR_INVALID_ARG;
+    DeviceScene* sc = find_scene(ctx, scene_id);
+    if (!sc) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown scene %u", scene_id);
+    CK(cudaStreamSynchronize(ctx->stream), "stream synchronize");
+    CK(cudaMemcpy(xf, sc->xf, 64ull * sc->nobjects, cudaMemcpyDeviceToHost), "download transforms");
+    CK(cudaMemcpy(inv, sc->inv, 64ull * sc->nobjects, cudaMemcpyDeviceToHost), "download inverses");
+    return BVHGPU_OK;
+}
+
+int bvhgpu_mesh_wobble_async(bvhgpu_ctx* ctx, uint32_t mesh_id, const float* d_dirs, const float* d_r0,
+                             const float* d_phase, float amp, float freq, const float* d_time, bvhgpu_stream s) {
+    if (!ctx || !d_dirs || !d_r0 || !d_phase || !d_time) return BVHGPU_ERR_INVALID_ARG;
+    DeviceMesh* m = find_mesh(ctx, mesh_id);
+    if (!m) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown mesh %u", mesh_id);
+    CK(launch_wobble(ctx, m->verts, d_dirs, d_r0, d_phase, m->nverts, amp, freq, d_time, pick(ctx, s)), "wobble");
+    return BVHGPU_OK;
+}
+
+int bvhgpu_scene_animate_async(bvhgpu_ctx* ctx, uint32_t scene_id, const float* d_rot0, const float* d_axis,
+                               const float* d_omega, const float* d_scale, const float* d_trans, const float* d_time,
+                               bvhgpu_stream s) {
+    if (!ctx || !d_rot0 || !d_axis || !d_omega || !d_scale || !d_trans || !d_time) return BVHGPU_ERR_INVALID_ARG;
+    DeviceScene* sc = find_scene(ctx, scene_id);
+    if (!sc) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown scene %u", scene_id);
+    CK(launch_animate_instances(ctx, *sc, d_rot0, d_axis, d_omega, d_scale, d_trans, d_time, pick(ctx, s)),
+       "animate instances");
+    return BVHGPU_OK;
+}
+
+int bvhgpu_advance_time_async(bvhgpu_ctx* ctx, float* d_time, float dt, bvhgpu_stream s) {
+    if (!ctx || !d_time) return BVHGPU_ERR_INVALID_ARG;
+    CK(launch_advance_time(ctx, d_time, dt, pick(ctx, s)), "advance time");
+    return BVHGPU_OK;
+}
+
+int bvhgpu_graph_begin(bvhgpu_ctx* ctx) {
+    if (!ctx || ctx->capturing) return BVHGPU_ERR_INVALID_ARG;
+    CK(cudaStreamSynchronize(ctx->stream), "stream synchronize");
+    ctx->profiling_before_capture = ctx->profiling;
+    ctx->profiling = false;  // no timing events inside a captured graph
+    CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+    ctx->capturing = true;
+    return BVHGPU_OK;
+}
+
+int bvhgpu_graph_end(bvhgpu_ctx* ctx, uint32_t* graph_id) {
+    if (!ctx || !graph_id || !ctx->capturing) return BVHGPU_ERR_INVALID_ARG;
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+    ctx->capturing = false;
+    ctx->profiling = ctx->profiling_before_capture;
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "end capture");
+    cudaGraphExec_t ex = nullptr;
+    e = cudaGraphInstantiate(&ex, g, 0);
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(g);
+        return cuda_fail(ctx, e, "instantiate graph");
+    }
+    uint32_t id = ctx->next_graph++;
+    ctx->graphs[id] = {g, ex};
+    *graph_id = id;
+    return BVHGPU_OK;
+}
+
+int bvhgpu_graph_launch(bvhgpu_ctx* ctx, uint32_t graph_id) {
+    if (!ctx) return BVHGPU_ERR_INVALID_ARG;
+    auto it = ctx->graphs.find(graph_id);
+    if (it == ctx->graphs.end()) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown graph %u", graph_id);
+    CK(cudaGraphLaunch(it->second.second, ctx->stream), "graph launch");
+    g_launches++;
+    return BVHGPU_OK;
+}
+
+int bvhgpu_graph_free(bvhgpu_ctx* ctx, uint32_t graph_id) {
+    if (!ctx) return BVHGPU_ERR_INVALID_ARG;
+    auto it = ctx->graphs.find(graph_id);
+    if (it == ctx->graphs.end()) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown graph %u", graph_id);
+    cudaStreamSynchronize(ctx->stream);
+    cudaGraphExecDestroy(it->second.second);
+    cudaGraphDestroy(it->second.first);
+    ctx->graphs.erase(it);
     return BVHGPU_OK;
 }
 

@@ -120,6 +120,8 @@ struct LaneRay {
     float hu, hv;
     uint32_t hp;
     bool hit;
+    uint32_t inst_cur = 0;  // instance whose BLAS is being traversed (two-level traversal)
+    uint32_t inst = 0;      // instance of the closest hit
 };
 
 __device__ __forceinline__ void test_leaf_lane(const float4* __restrict__ tris, uint32_t first, uint32_t cnt,
@@ -136,6 +138,7 @@ __device__ __forceinline__ void test_leaf_lane(const float4* __restrict__ tris, 
             r.hv = v;
             r.hp = first + k;
             r.hit = true;
+            r.inst = r.inst_cur;
         }
     }
 }
@@ -391,6 +394,7 @@ __device__ __forceinline__ void reduce_and_take(Best b, uint32_t pbeg, int src, 
             r.hv = wv;
             r.hp = bk;
             r.hit = true;
+            r.inst = r.inst_cur;
         }
     }
 }
@@ -504,6 +508,52 @@ __device__ __forceinline__ bool bounce_dir(float3 o, float3 d, float t, float4 v
     float nx = fsub(fmul(e1.y, e2.z), fmul(e1.z, e2.y));
     float ny = fsub(fmul(e1.z, e2.x), fmul(e1.x, e2.z));
     float nz = fsub(fmul(e1.x, e2.y), fmul(e1.y, e2.x));
+    float nl = __fsqrt_rn(dot3(nx, ny, nz, nx, ny, nz));
+    if (!(nl > 0.0f) || !(nl <= FLT_MAX)) return false;
+    nx = __fdiv_rn(nx, nl);
+    ny = __fdiv_rn(ny, nl);
+    nz = __fdiv_rn(nz, nl);
+    if (dot3(nx, ny, nz, d.x, d.y, d.z) > 0.0f) {
+        nx = -nx; ny = -ny; nz = -nz;
+    }
+    uint32_t key = hash32(seed ^ hash32(pixel));
+    float qx = nx, qy = ny, qz = nz;
+    for (uint32_t k = 0; k < 32u; ++k) {
+        float x1 = fsub(fmul(2.0f, rng_uniform(key, 2u * k)), 1.0f);
+        float x2 = fsub(fmul(2.0f, rng_uniform(key, 2u * k + 1u)), 1.0f);
+        float s = fadd(fmul(x1, x1), fmul(x2, x2));
+        if (s < 1.0f && s > 0.0f) {
+            float r = __fsqrt_rn(fsub(1.0f, s));
+            qx = fmul(fmul(2.0f, x1), r);
+            qy = fmul(fmul(2.0f, x2), r);
+            qz = fsub(1.0f, fmul(2.0f, s));
+            break;
+        }
+    }
+    float dx = fadd(nx, qx), dy = fadd(ny, qy), dz = fadd(nz, qz);
+    float dl = __fsqrt_rn(dot3(dx, dy, dz, dx, dy, dz));
+    if (dl < 1e-6f) {
+        pd = make_float3(nx, ny, nz);
+    } else {
+        pd = make_float3(__fdiv_rn(dx, dl), __fdiv_rn(dy, dl), __fdiv_rn(dz, dl));
+    }
+    return true;
+}
+
+// Bounce for an instanced hit: world hit point p = o + d t (o, d world space), geometric normal
+// of the model-space triangle (e1 x e2) taken to world space with the inverse-transpose of the
+// instance transform (row r of inv^T is column r of the column-major inverse), then the same
+// face-forward + Marsaglia sampling as bounce_dir.  Identical on the CPU oracle.
+__device__ __forceinline__ bool bounce_dir_instanced(float3 o, float3 d, float t, float4 e1, float4 e2,
+                                                     const float* inv, uint32_t seed, uint32_t pixel, float3& po,
+                                                     float3& pd) {
+    po = make_float3(fadd(o.x, fmul(d.x, t)), fadd(o.y, fmul(d.y, t)), fadd(o.z, fmul(d.z, t)));
+    const float mx = fsub(fmul(e1.y, e2.z), fmul(e1.z, e2.y));
+    const float my = fsub(fmul(e1.z, e2.x), fmul(e1.x, e2.z));
+    const float mz = fsub(fmul(e1.x, e2.y), fmul(e1.y, e2.x));
+    float nx = fadd(fadd(fmul(inv[0], mx), fmul(inv[1], my)), fmul(inv[2], mz));
+    float ny = fadd(fadd(fmul(inv[4], mx), fmul(inv[5], my)), fmul(inv[6], mz));
+    float nz = fadd(fadd(fmul(inv[8], mx), fmul(inv[9], my)), fmul(inv[10], mz));
     float nl = __fsqrt_rn(dot3(nx, ny, nz, nx, ny, nz));
     if (!(nl > 0.0f) || !(nl <= FLT_MAX)) return false;
     nx = __fdiv_rn(nx, nl);

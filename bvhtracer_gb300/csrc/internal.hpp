@@ -98,6 +98,11 @@ struct bvhgpu_ctx {
     std::vector<bvhgpu_batch_item> batch_items;
     uint32_t batch_total = 0;
     uint32_t batch_depth = 1;
+    // captured frame graphs
+    std::map<uint32_t, std::pair<cudaGraph_t, cudaGraphExec_t>> graphs;
+    uint32_t next_graph = 1;
+    bool capturing = false;
+    bool profiling_before_capture = false;
     // profiling
     bool profiling = false;
     std::vector<bvhgpu::ProfileRec> prof;
@@ -138,6 +143,16 @@ cudaError_t launch_refit(bvhgpu_ctx* ctx, DeviceBlas& b, cudaStream_t s);
 cudaError_t launch_tlas_rebuild(bvhgpu_ctx* ctx, DeviceScene& sc, cudaStream_t s);
 cudaError_t launch_trace_scene(bvhgpu_ctx* ctx, DeviceScene& sc, const float4* rays, uint32_t n, void* hits,
                                cudaStream_t s);
+cudaError_t launch_scene_bounce(bvhgpu_ctx* ctx, DeviceScene& sc, const float4* rays, uint32_t n, uint32_t seed,
+                                void* hits0, void* hits1, cudaStream_t s);
+cudaError_t launch_scene_bounce_rays(bvhgpu_ctx* ctx, DeviceScene& sc, const float4* rays, const void* hits0,
+                                     uint32_t n, uint32_t seed, float4* out, uint8_t* valid, cudaStream_t s);
+cudaError_t launch_wobble(bvhgpu_ctx* ctx, float* verts, const float* dirs, const float* r0, const float* phase,
+                          uint32_t nv, float amp, float freq, const float* time, cudaStream_t s);
+cudaError_t launch_animate_instances(bvhgpu_ctx* ctx, DeviceScene& sc, const float* rot0, const float* axis,
+                                     const float* omega, const float* scale, const float* trans, const float* time,
+                                     cudaStream_t s);
+cudaError_t launch_advance_time(bvhgpu_ctx* ctx, float* time, float dt, cudaStream_t s);
 
 // ---- launchers (kernels_adjoint.cu) ----------------------------------------------------
 cudaError_t launch_mesh_update(bvhgpu_ctx* ctx, DeviceMesh& m, DeviceBlas& b, cudaStream_t s);

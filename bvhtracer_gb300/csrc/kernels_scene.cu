@@ -336,92 +336,355 @@ __global__ void k_tlas_rebuild(const GBlas* __restrict__ blas_table, const uint3
     }
 }
 
-// Tlas::intersect (tlas.rs:123-177) with SceneObject::intersect (scene_object.rs:78-89) at
-// the leaves: the ray goes to model space through the cached inverse, 1/d' is recomputed
-// (Ray::new), and the BLAS traversal shares the TLAS's closest t.
+// ---- two-level traversal ------------------------------------------------------------------
+// Tlas::intersect (tlas.rs:123-177) with SceneObject::intersect (scene_object.rs:78-89) at the
+// leaves: the ray goes to model space through the cached inverse, 1/d' is recomputed (Ray::new)
+// and the BLAS traversal (Trav, the same as for a single BLAS) shares the TLAS's closest t.  The
+// LaneRay holds the model-space ray while a BLAS is traversed; the world ray is kept here.  Big
+// BLAS leaves are handed to the warp-cooperative leaf phase, keyed by (BLAS, leaf), so rays in
+// different instances of the same BLAS share the loaded triangle pairs.
+struct SceneData {
+    const float4* tlas;
+    const GBlas* blas_table;
+    const uint32_t* obj_blas;
+    const float* inv;
+    uint32_t tlas_nodes;
+};
+
 template <int STACK, int TSTACK>
-__global__ void __launch_bounds__(kBlock) k_trace_scene(const float4* __restrict__ tlas,
-                                                        const GBlas* __restrict__ blas_table,
-                                                        const uint32_t* __restrict__ obj_blas,
-                                                        const float* __restrict__ inv, const float4* __restrict__ rays,
-                                                        uint32_t n, GHit* __restrict__ hits, uint32_t* err) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    float3 o, d;
-    float ct;
-    load_ray(rays, i, o, d, ct);
+struct SceneTrav {
+    Trav<STACK> bt;
+    GBlas blas;
     uint2 tstack[TSTACK];  // pending far TLAS nodes: (left_right, blas)
-    int tsp = 0;
-    float4 cur_lo = __ldg(tlas), cur_hi = __ldg(tlas + 1);
-    uint32_t lr = __float_as_uint(cur_lo.w), bl = __float_as_uint(cur_hi.w);
-    bool hit = false;
-    float hu = 0.0f, hv = 0.0f;
-    uint32_t hp = 0, hinst = 0;
-    float3 rd = recip3(d);
-    for (;;) {
-        if (lr == 0u) {
-            // leaf: SceneObject::intersect
-            const float* m = inv + 16ull * bl;
-            float3 mo, md;
-            mo.x = fadd(fadd(fadd(fmul(__ldg(m + 0), o.x), fmul(__ldg(m + 4), o.y)), fmul(__ldg(m + 8), o.z)),
-                        fmul(__ldg(m + 12), 1.0f));
-            mo.y = fadd(fadd(fadd(fmul(__ldg(m + 1), o.x), fmul(__ldg(m + 5), o.y)), fmul(__ldg(m + 9), o.z)),
-                        fmul(__ldg(m + 13), 1.0f));
-            mo.z = fadd(fadd(fadd(fmul(__ldg(m + 2), o.x), fmul(__ldg(m + 6), o.y)), fmul(__ldg(m + 10), o.z)),
-                        fmul(__ldg(m + 14), 1.0f));
-            md.x = fadd(fadd(fadd(fmul(__ldg(m + 0), d.x), fmul(__ldg(m + 4), d.y)), fmul(__ldg(m + 8), d.z)),
-                        fmul(__ldg(m + 12), 0.0f));
-            md.y = fadd(fadd(fadd(fmul(__ldg(m + 1), d.x), fmul(__ldg(m + 5), d.y)), fmul(__ldg(m + 9), d.z)),
-                        fmul(__ldg(m + 13), 0.0f));
-            md.z = fadd(fadd(fadd(fmul(__ldg(m + 2), d.x), fmul(__ldg(m + 6), d.y)), fmul(__ldg(m + 10), d.z)),
-                        fmul(__ldg(m + 14), 0.0f));
-            GBlas b = blas_table[__ldg(obj_blas + bl)];
-            float u2 = 0.0f, v2 = 0.0f;
-            uint32_t p2 = 0;
-            if (trace_blas<STACK>(b, mo, md, recip3(md), ct, u2, v2, p2, err)) {
-                hit = true;
-                hu = u2;
-                hv = v2;
-                hp = p2;
-                hinst = bl;
-            }
-            if (tsp == 0) break;
-            --tsp;
-            lr = tstack[tsp].x;
-            bl = tstack[tsp].y;
-            continue;
-        }
-        // LeftRightIndex getters are swapped (tlas.rs:24-32): left() is the high half.
-        uint32_t li = (lr & 0xFFFF0000u) >> 16, ri = lr & 0xFFFFu;
-        float4 l0 = __ldg(tlas + 2ull * li), l1 = __ldg(tlas + 2ull * li + 1);
-        float4 r0 = __ldg(tlas + 2ull * ri), r1 = __ldg(tlas + 2ull * ri + 1);
-        float dl, dr;
-        bool hl = slab(l0, l1, o, rd, ct, dl);
-        bool hr = slab(r0, r1, o, rd, ct, dr);
-        float kl = hl ? dl : FLT_MAX;
-        float kr = hr ? dr : FLT_MAX;
-        bool left_near = kl < kr;
-        bool near_hit = left_near ? hl : hr;
-        bool far_hit = left_near ? hr : hl;
-        if (near_hit) {
-            if (far_hit) {
-                if (tsp >= TSTACK) {
-                    atomicOr(err, kErrStack);
-                    break;
-                }
-                tstack[tsp++] = left_near ? make_uint2(ubits(r0.w), ubits(r1.w)) : make_uint2(ubits(l0.w), ubits(l1.w));
-            }
-            lr = left_near ? ubits(l0.w) : ubits(r0.w);
-            bl = left_near ? ubits(l1.w) : ubits(r1.w);
-            continue;
-        }
-        if (tsp == 0) break;
+    int tsp;
+    uint32_t lr, bl, tsteps;
+    bool in_blas;
+    float3 wo, wd, wrd;
+
+    __device__ __forceinline__ void init(const SceneData& sd, LaneRay& r) {
+        const float4 lo = __ldg(sd.tlas), hi = __ldg(sd.tlas + 1);
+        lr = __float_as_uint(lo.w);
+        bl = __float_as_uint(hi.w);
+        tsp = 0;
+        tsteps = 0;
+        in_blas = false;
+        wo = r.o;
+        wd = r.d;
+        wrd = r.rd;
+        blas.nodes = nullptr;
+        blas.tris = nullptr;
+        blas.pairs = nullptr;
+        blas.nodes_used = blas.ntris = blas.root_count = blas.root_first = 0;
+    }
+
+    __device__ __forceinline__ bool tpop() {
+        if (tsp == 0) return true;
         --tsp;
         lr = tstack[tsp].x;
         bl = tstack[tsp].y;
+        return false;
     }
-    store_hit(hits, i, hit && ct < FLT_MAX, ct, hu, hv, hp, hinst);
+
+    // After the cooperative test of the current big BLAS leaf.
+    __device__ __forceinline__ StepResult after_leaf() {
+        if (!bt.pop()) return kStepContinue;
+        in_blas = false;
+        return tpop() ? kStepFinished : kStepContinue;
+    }
+
+    __device__ __forceinline__ StepResult advance(const SceneData& sd, LaneRay& r, uint32_t big_leaf, uint32_t* err) {
+        for (;;) {
+            if (in_blas) {
+                const StepResult st = bt.step(blas, r, big_leaf, err);
+                if (st == kStepContinue) continue;
+                if (st == kStepBigLeaf) return st;
+                in_blas = false;
+                if (tpop()) return kStepFinished;
+                continue;
+            }
+            if (++tsteps > 2u * sd.tlas_nodes + 16u) {
+                atomicOr(err, kErrSteps);
+                return kStepFinished;
+            }
+            if (lr == 0u) {  // TLAS leaf: SceneObject::intersect
+                const float* m = sd.inv + 16ull * bl;
+                r.o.x = fadd(fadd(fadd(fmul(__ldg(m + 0), wo.x), fmul(__ldg(m + 4), wo.y)), fmul(__ldg(m + 8), wo.z)),
+                             fmul(__ldg(m + 12), 1.0f));
+                r.o.y = fadd(fadd(fadd(fmul(__ldg(m + 1), wo.x), fmul(__ldg(m + 5), wo.y)), fmul(__ldg(m + 9), wo.z)),
+                             fmul(__ldg(m + 13), 1.0f));
+                r.o.z = fadd(fadd(fadd(fmul(__ldg(m + 2), wo.x), fmul(__ldg(m + 6), wo.y)), fmul(__ldg(m + 10), wo.z)),
+                             fmul(__ldg(m + 14), 1.0f));
+                r.d.x = fadd(fadd(fadd(fmul(__ldg(m + 0), wd.x), fmul(__ldg(m + 4), wd.y)), fmul(__ldg(m + 8), wd.z)),
+                             fmul(__ldg(m + 12), 0.0f));
+                r.d.y = fadd(fadd(fadd(fmul(__ldg(m + 1), wd.x), fmul(__ldg(m + 5), wd.y)), fmul(__ldg(m + 9), wd.z)),
+                             fmul(__ldg(m + 13), 0.0f));
+                r.d.z = fadd(fadd(fadd(fmul(__ldg(m + 2), wd.x), fmul(__ldg(m + 6), wd.y)), fmul(__ldg(m + 10), wd.z)),
+                             fmul(__ldg(m + 14), 0.0f));
+                r.rd = recip3(r.d);
+                r.inst_cur = bl;
+                blas = sd.blas_table[__ldg(sd.obj_blas + bl)];
+                bt.init(blas);
+                in_blas = true;
+                continue;
+            }
+            // LeftRightIndex getters are swapped (tlas.rs:24-32): left() is the high half.
+            const uint32_t li = (lr & 0xFFFF0000u) >> 16, ri = lr & 0xFFFFu;
+            const float4 l0 = __ldg(sd.tlas + 2ull * li), l1 = __ldg(sd.tlas + 2ull * li + 1);
+            const float4 r0 = __ldg(sd.tlas + 2ull * ri), r1 = __ldg(sd.tlas + 2ull * ri + 1);
+            float dl, dr;
+            const bool hl = slab(l0, l1, wo, wrd, r.ct, dl);
+            const bool hr = slab(r0, r1, wo, wrd, r.ct, dr);
+            const float kl = hl ? dl : FLT_MAX;
+            const float kr = hr ? dr : FLT_MAX;
+            const bool left_near = kl < kr;
+            const bool near_hit = left_near ? hl : hr;
+            const bool far_hit = left_near ? hr : hl;
+            if (near_hit) {
+                if (far_hit) {
+                    if (tsp >= TSTACK) {
+                        atomicOr(err, kErrStack);
+                        return kStepFinished;
+                    }
+                    tstack[tsp++] = left_near ? make_uint2(ubits(r0.w), ubits(r1.w)) : make_uint2(ubits(l0.w), ubits(l1.w));
+                }
+                lr = left_near ? ubits(l0.w) : ubits(r0.w);
+                bl = left_near ? ubits(l1.w) : ubits(r1.w);
+                continue;
+            }
+            if (tpop()) return kStepFinished;
+        }
+    }
+};
+
+// Cooperative phase of the two-level traversal (same grouping as the single-BLAS kernels).
+template <int STACK, int TSTACK>
+__device__ __forceinline__ void scene_coop_phase(unsigned pend, SceneTrav<STACK, TSTACK>& tr, LaneRay& r,
+                                                 StepResult& st) {
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned long long key = reinterpret_cast<unsigned long long>(tr.blas.pairs);
+    while (pend) {
+        const int leader = __ffs(pend) - 1;
+        const uint32_t f = __shfl_sync(kFull, tr.bt.first, leader);
+        const uint32_t c = __shfl_sync(kFull, tr.bt.cnt, leader);
+        const unsigned long long lk = __shfl_sync(kFull, key, leader);
+        const ulonglong2* P = reinterpret_cast<const ulonglong2*>(lk);
+        unsigned group = __ballot_sync(kFull, ((pend >> lane) & 1u) && tr.bt.first == f && key == lk);
+        pend &= ~group;
+        while (group) {
+            const int a = __ffs(group) - 1;
+            group &= group - 1u;
+            if (group) {
+                const int b = __ffs(group) - 1;
+                group &= group - 1u;
+                coop_leaf2(P, f, c, a, b, r);
+                if ((int)lane == a || (int)lane == b) st = tr.after_leaf();
+            } else {
+                coop_leaf(P, f, c, a, r);
+                if ((int)lane == a) st = tr.after_leaf();
+            }
+        }
+    }
 }
+
+constexpr uint32_t kBigLeaf = 16;
+
+template <int STACK, int TSTACK>
+__global__ void __launch_bounds__(kBlock) k_trace_scene(SceneData sd, const float4* __restrict__ rays, uint32_t n,
+                                                        GHit* __restrict__ hits, uint32_t* err) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (__all_sync(kFull, i >= n)) return;
+    const bool active = i < n;
+    LaneRay r;
+    SceneTrav<STACK, TSTACK> tr;
+    StepResult st = kStepFinished;
+    if (active) {
+        float3 o, d;
+        float t0;
+        load_ray(rays, i, o, d, t0);
+        r.o = o;
+        r.d = d;
+        r.rd = recip3(d);
+        r.ct = t0;
+        r.hu = r.hv = 0.0f;
+        r.hp = 0;
+        r.hit = false;
+        r.inst = r.inst_cur = 0;
+        tr.init(sd, r);
+        st = kStepContinue;
+    }
+    for (;;) {
+        if (st == kStepContinue) st = tr.advance(sd, r, kBigLeaf, err);
+        const unsigned pend = __ballot_sync(kFull, st == kStepBigLeaf);
+        if (pend == 0u) break;
+        scene_coop_phase(pend, tr, r, st);
+    }
+    if (active) store_hit(hits, i, r.hit && r.ct < FLT_MAX, r.ct, r.hu, r.hv, r.hp, r.inst);
+}
+
+// Persistent primary + bounce over a scene (the instanced frame): idle lanes are refilled from
+// the queue; a primary that hits continues in its lane with the bounce ray of its hit.
+template <int STACK, int TSTACK>
+__global__ void __launch_bounds__(kBlock) k_scene_persistent_bounce(SceneData sd, const float4* __restrict__ rays,
+                                                                    uint32_t n, uint32_t seed,
+                                                                    GHit* __restrict__ hits0, GHit* __restrict__ hits1,
+                                                                    uint32_t* queue, uint32_t* err) {
+    const unsigned lane = threadIdx.x & 31u;
+    int phase = 0;  // 0 needs work, 1 primary, 2 bounce, 3 retired
+    uint32_t idx = 0;
+    LaneRay r;
+    SceneTrav<STACK, TSTACK> tr;
+    StepResult st = kStepFinished;
+    bool queue_open = true;
+    for (;;) {
+        const unsigned need = __ballot_sync(kFull, phase == 0);
+        if (need != 0u) {
+            const int leader = __ffs(need) - 1;
+            uint32_t base = 0;
+            if ((int)lane == leader) base = atomicAdd(queue, (uint32_t)__popc(need));
+            base = __shfl_sync(kFull, base, leader);
+            if (base + (uint32_t)__popc(need) >= n) queue_open = false;
+            if (phase == 0) {
+                const uint32_t my = base + __popc(need & ((1u << lane) - 1u));
+                if (my < n) {
+                    idx = my;
+                    float3 o, d;
+                    float t0;
+                    load_ray(rays, idx, o, d, t0);
+                    r.o = o;
+                    r.d = d;
+                    r.rd = recip3(d);
+                    r.ct = t0;
+                    r.hu = r.hv = 0.0f;
+                    r.hp = 0;
+                    r.hit = false;
+                    r.inst = r.inst_cur = 0;
+                    tr.init(sd, r);
+                    st = kStepContinue;
+                    phase = 1;
+                } else {
+                    phase = 3;
+                }
+            }
+        }
+        while (phase == 1 || phase == 2) {
+            if (st == kStepContinue) st = tr.advance(sd, r, kBigLeaf, err);
+            if (st != kStepFinished) break;
+            const bool h = r.hit && r.ct < FLT_MAX;
+            if (phase == 2) {
+                store_hit(hits1, idx, h, r.ct, r.hu, r.hv, r.hp, r.inst);
+                phase = 0;
+                break;
+            }
+            store_hit(hits0, idx, h, r.ct, r.hu, r.hv, r.hp, r.inst);
+            float3 po, pd;
+            bool have = false;
+            if (h) {
+                const GBlas hb = sd.blas_table[__ldg(sd.obj_blas + r.inst)];
+                const float4* T = hb.tris + 3ull * r.hp;
+                have = bounce_dir_instanced(tr.wo, tr.wd, r.ct, __ldg(T + 1), __ldg(T + 2), sd.inv + 16ull * r.inst,
+                                            seed, idx, po, pd);
+            }
+            if (!have) {
+                store_hit(hits1, idx, false, 0, 0, 0, 0, 0);
+                phase = 0;
+                break;
+            }
+            r.o = po;
+            r.d = pd;
+            r.rd = recip3(pd);
+            r.ct = FLT_MAX;
+            r.hu = r.hv = 0.0f;
+            r.hp = 0;
+            r.hit = false;
+            r.inst = r.inst_cur = 0;
+            tr.init(sd, r);
+            st = kStepContinue;
+            phase = 2;
+        }
+        const unsigned pend = __ballot_sync(kFull, (phase == 1 || phase == 2) && st == kStepBigLeaf);
+        if (pend == 0u) {
+            if (!queue_open && __ballot_sync(kFull, phase == 0 || phase == 1 || phase == 2) == 0u) break;
+            continue;
+        }
+        scene_coop_phase(pend, tr, r, st);
+    }
+}
+
+// Bounce rays of an instanced frame in pixel order (for checking against the oracle).
+__global__ void k_scene_bounce_rays(SceneData sd, const float4* __restrict__ rays, const GHit* __restrict__ hits0,
+                                    uint32_t n, uint32_t seed, float4* __restrict__ out, uint8_t* __restrict__ valid) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const GHit h = hits0[i];
+    bool have = false;
+    float3 po = make_float3(0, 0, 0), pd = po;
+    if (h.prim != kMiss) {
+        float3 o, d;
+        float t0;
+        load_ray(rays, i, o, d, t0);
+        const GBlas hb = sd.blas_table[sd.obj_blas[h.inst]];
+        const float4* T = hb.tris + 3ull * h.prim;
+        have = bounce_dir_instanced(o, d, h.t, T[1], T[2], sd.inv + 16ull * h.inst, seed, i, po, pd);
+    }
+    out[2ull * i] = make_float4(po.x, po.y, po.z, FLT_MAX);
+    out[2ull * i + 1] = make_float4(pd.x, pd.y, pd.z, 0.0f);
+    valid[i] = have ? 1 : 0;
+}
+
+// ---- animation (the frame pattern of the reference's demos, closed form) --------------------
+// Radial vertex wobble: v = dir * (r0 + amp * sin(freq * t + phase)), t read from device memory
+// so that a captured frame graph replays with the current time.
+__global__ void k_wobble(float* __restrict__ verts, const float* __restrict__ dirs, const float* __restrict__ r0,
+                         const float* __restrict__ phase, uint32_t nv, float amp, float freq,
+                         const float* __restrict__ time) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nv) return;
+    const float t = *time;
+    const float r = r0[i] + amp * sinf(freq * t + phase[i]);
+    verts[3ull * i] = dirs[3ull * i] * r;
+    verts[3ull * i + 1] = dirs[3ull * i + 1] * r;
+    verts[3ull * i + 2] = dirs[3ull * i + 2] * r;
+}
+
+// Instance i at time t: rotation R_i = R0_i * Rot(axis_i, omega_i t) (Rodrigues), uniform scale
+// s_i, translation T_i; xf = [s R | T] and its inverse [R^T / s | -R^T T / s], column-major.
+__global__ void k_animate_instances(float* __restrict__ xf, float* __restrict__ inv, const float* __restrict__ rot0,
+                                    const float* __restrict__ axis, const float* __restrict__ omega,
+                                    const float* __restrict__ scale, const float* __restrict__ trans, uint32_t n,
+                                    const float* __restrict__ time) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float t = *time;
+    const float ang = omega[i] * t;
+    float sn, cs;
+    sincosf(ang, &sn, &cs);
+    const float kx = axis[3 * i], ky = axis[3 * i + 1], kz = axis[3 * i + 2];
+    const float oc = 1.0f - cs;
+    // Rot(axis, ang), row-major A[r][c]
+    float A[3][3] = {{cs + kx * kx * oc, kx * ky * oc - kz * sn, kx * kz * oc + ky * sn},
+                     {ky * kx * oc + kz * sn, cs + ky * ky * oc, ky * kz * oc - kx * sn},
+                     {kz * kx * oc - ky * sn, kz * ky * oc + kx * sn, cs + kz * kz * oc}};
+    const float* B = rot0 + 9ull * i;  // row-major R0
+    float R[3][3];
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) R[r][c] = B[3 * r] * A[0][c] + B[3 * r + 1] * A[1][c] + B[3 * r + 2] * A[2][c];
+    const float s = scale[i], is = 1.0f / s;
+    const float tx = trans[3 * i], ty = trans[3 * i + 1], tz = trans[3 * i + 2];
+    float* X = xf + 16ull * i;
+    float* I = inv + 16ull * i;
+    for (int c = 0; c < 3; ++c)
+        for (int r = 0; r < 3; ++r) {
+            X[4 * c + r] = s * R[r][c];
+            I[4 * c + r] = is * R[c][r];
+        }
+    X[3] = X[7] = X[11] = 0.0f;
+    X[12] = tx; X[13] = ty; X[14] = tz; X[15] = 1.0f;
+    I[3] = I[7] = I[11] = 0.0f;
+    for (int r = 0; r < 3; ++r) I[12 + r] = -(is * (R[0][r] * tx + R[1][r] * ty + R[2][r] * tz));
+    I[15] = 1.0f;
+}
+
+__global__ void k_advance_time(float* time, float dt) { *time += dt; }
 
 inline unsigned grid_for(uint32_t n, int block) { return (unsigned)((n + block - 1) / block); }
 
@@ -462,21 +725,99 @@ cudaError_t launch_tlas_rebuild(bvhgpu_ctx* ctx, DeviceScene& sc, cudaStream_t s
     return cudaGetLastError();
 }
 
+static SceneData scene_data(bvhgpu_ctx* ctx, DeviceScene& sc, uint32_t* depth) {
+    SceneData sd;
+    sd.tlas = sc.tlas;
+    sd.blas_table = static_cast<const GBlas*>(sc.blas_table);
+    sd.obj_blas = sc.obj_blas;
+    sd.inv = sc.inv;
+    sd.tlas_nodes = 2 * sc.nobjects;
+    uint32_t d = 1;
+    for (uint32_t id : sc.table_blas) d = std::max(d, ctx->blas[id].depth);
+    *depth = d;
+    return sd;
+}
+
 cudaError_t launch_trace_scene(bvhgpu_ctx* ctx, DeviceScene& sc, const float4* rays, uint32_t n, void* hits,
                                cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     uint32_t depth = 1;
-    for (uint32_t id : sc.table_blas) depth = std::max(depth, ctx->blas[id].depth);
+    SceneData sd = scene_data(ctx, sc, &depth);
     LaunchScope scope(ctx, BVHGPU_K_TRACE_SCENE, s);
-    const GBlas* table = static_cast<const GBlas*>(sc.blas_table);
     GHit* h = static_cast<GHit*>(hits);
-    unsigned grid = grid_for(n, kBlock);
+    const unsigned grid = grid_for(n, kBlock);
     if (depth <= 33)
-        k_trace_scene<32, 64><<<grid, kBlock, 0, s>>>(sc.tlas, table, sc.obj_blas, sc.inv, rays, n, h, ctx->d_err);
+        k_trace_scene<32, 64><<<grid, kBlock, 0, s>>>(sd, rays, n, h, ctx->d_err);
     else if (depth <= 65)
-        k_trace_scene<64, 64><<<grid, kBlock, 0, s>>>(sc.tlas, table, sc.obj_blas, sc.inv, rays, n, h, ctx->d_err);
+        k_trace_scene<64, 64><<<grid, kBlock, 0, s>>>(sd, rays, n, h, ctx->d_err);
     else
-        k_trace_scene<256, 64><<<grid, kBlock, 0, s>>>(sc.tlas, table, sc.obj_blas, sc.inv, rays, n, h, ctx->d_err);
+        k_trace_scene<256, 64><<<grid, kBlock, 0, s>>>(sd, rays, n, h, ctx->d_err);
+    g_launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scene_bounce(bvhgpu_ctx* ctx, DeviceScene& sc, const float4* rays, uint32_t n, uint32_t seed,
+                                void* hits0, void* hits1, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    uint32_t depth = 1;
+    SceneData sd = scene_data(ctx, sc, &depth);
+    uint32_t* queue = ctx->d_scratch + 4;
+    cudaError_t e = cudaMemsetAsync(queue, 0, sizeof(uint32_t), s);
+    if (e != cudaSuccess) return e;
+    LaunchScope scope(ctx, BVHGPU_K_SCENE_BOUNCE, s);
+    GHit* h0 = static_cast<GHit*>(hits0);
+    GHit* h1 = static_cast<GHit*>(hits1);
+    int per_sm = 0;
+    if (depth <= 33) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_scene_persistent_bounce<32, 64>, kBlock, 0);
+        k_scene_persistent_bounce<32, 64><<<std::max(1, per_sm) * ctx->num_sms, kBlock, 0, s>>>(
+            sd, rays, n, seed, h0, h1, queue, ctx->d_err);
+    } else if (depth <= 65) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_scene_persistent_bounce<64, 64>, kBlock, 0);
+        k_scene_persistent_bounce<64, 64><<<std::max(1, per_sm) * ctx->num_sms, kBlock, 0, s>>>(
+            sd, rays, n, seed, h0, h1, queue, ctx->d_err);
+    } else {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_scene_persistent_bounce<256, 64>, kBlock, 0);
+        k_scene_persistent_bounce<256, 64><<<std::max(1, per_sm) * ctx->num_sms, kBlock, 0, s>>>(
+            sd, rays, n, seed, h0, h1, queue, ctx->d_err);
+    }
+    g_launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scene_bounce_rays(bvhgpu_ctx* ctx, DeviceScene& sc, const float4* rays, const void* hits0,
+                                     uint32_t n, uint32_t seed, float4* out, uint8_t* valid, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    uint32_t depth = 1;
+    SceneData sd = scene_data(ctx, sc, &depth);
+    LaunchScope scope(ctx, BVHGPU_K_OTHER, s);
+    k_scene_bounce_rays<<<grid_for(n, kBlock), kBlock, 0, s>>>(sd, rays, static_cast<const GHit*>(hits0), n, seed,
+                                                               out, valid);
+    g_launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_wobble(bvhgpu_ctx* ctx, float* verts, const float* dirs, const float* r0, const float* phase,
+                          uint32_t nv, float amp, float freq, const float* time, cudaStream_t s) {
+    LaunchScope scope(ctx, BVHGPU_K_OTHER, s);
+    k_wobble<<<grid_for(nv, 256), 256, 0, s>>>(verts, dirs, r0, phase, nv, amp, freq, time);
+    g_launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_animate_instances(bvhgpu_ctx* ctx, DeviceScene& sc, const float* rot0, const float* axis,
+                                     const float* omega, const float* scale, const float* trans, const float* time,
+                                     cudaStream_t s) {
+    LaunchScope scope(ctx, BVHGPU_K_OTHER, s);
+    k_animate_instances<<<grid_for(sc.nobjects, 128), 128, 0, s>>>(sc.xf, sc.inv, rot0, axis, omega, scale, trans,
+                                                                   sc.nobjects, time);
+    g_launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_advance_time(bvhgpu_ctx* ctx, float* time, float dt, cudaStream_t s) {
+    LaunchScope scope(ctx, BVHGPU_K_OTHER, s);
+    k_advance_time<<<1, 1, 0, s>>>(time, dt);
     g_launches++;
     return cudaGetLastError();
 }

@@ -264,3 +264,36 @@ def config4(seed: int = 0, level: int = 7, width: int = 512, height: int = 512, 
     rays = look_at_rays(width, height, (0.0, 0.0, -3.0 * scale), (0.0, 0.0, 0.0), 45.0)
     light = np.array([2.0 * scale, 2.0 * scale, -3.0 * scale], np.float32)
     return verts, mesh.faces.astype(np.uint32), vnormals, target_verts, rays, light
+
+
+def config2(seed: int = 0, ninstances: int = 256, width: int = 1280, height: int = 720, levels=(4, 5, 6)):
+    """Instanced animated scene: three displaced icospheres (config-1 displacement) at the given
+    subdivision levels, `ninstances` instances (instance i uses mesh i % 3) with a seeded random
+    rotation, uniform scale U[0.5, 2] and translation in a 40^3 box; per frame (dt = 1/30 s) each
+    instance turns about a seeded axis at U[-1, 1] rad/s and every vertex wobbles radially by
+    0.02 sin(3 t + phase_v).  Camera: width x height pixel-centre primaries from (0, 0, -60),
+    60 degree field of view, tile order."""
+    meshes = []
+    for k, lvl in enumerate(levels):
+        m = displaced_icosphere(lvl, seed * 100 + k)
+        phase = 2.0 * np.pi * uniform(seed * 100 + k, 50, len(m.radius))
+        meshes.append({"verts": m.vertices, "faces": m.faces.astype(np.uint32),
+                       "dirs": m.dirs.astype(np.float32), "r0": m.radius.astype(np.float32),
+                       "phase": phase.astype(np.float32)})
+    n = ninstances
+    q = normal(seed, 60, 4 * n).reshape(n, 4)
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    w, x, y, z = q.T
+    rot0 = np.stack([np.stack([1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)], -1),
+                     np.stack([2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)], -1),
+                     np.stack([2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)], -1)], 1)
+    axis = normal(seed, 61, 3 * n).reshape(n, 3)
+    axis /= np.linalg.norm(axis, axis=1, keepdims=True)
+    inst = {"blas_of": (np.arange(n) % len(levels)).astype(np.uint32),
+            "rot0": np.ascontiguousarray(rot0.astype(np.float32)),
+            "axis": np.ascontiguousarray(axis.astype(np.float32)),
+            "omega": (2.0 * uniform(seed, 62, n) - 1.0).astype(np.float32),
+            "scale": (0.5 + 1.5 * uniform(seed, 63, n)).astype(np.float32),
+            "trans": ((2.0 * uniform(seed, 64, 3 * n) - 1.0) * 20.0).reshape(n, 3).astype(np.float32)}
+    rays = look_at_rays(width, height, (0.0, 0.0, -60.0), (0.0, 0.0, 0.0), 60.0)
+    return {"meshes": meshes, "instances": inst, "rays": rays, "dt": 1.0 / 30.0, "amp": 0.02, "freq": 3.0}

@@ -162,7 +162,8 @@ int bvhgpu_event_elapsed_ms(bvhgpu_ctx* ctx, void* start, void* stop, float* ms)
 #define BVHGPU_K_OTHER 9
 #define BVHGPU_K_LAMBERT_FORWARD 10
 #define BVHGPU_K_LAMBERT_ADJOINT 11
-#define BVHGPU_KERNEL_COUNT 12
+#define BVHGPU_K_SCENE_BOUNCE 12
+#define BVHGPU_KERNEL_COUNT 13
 int bvhgpu_profile_enable(bvhgpu_ctx* ctx, int enable);
 int bvhgpu_profile_read(bvhgpu_ctx* ctx, double* ms, uint64_t* launches);
 
@@ -242,6 +243,35 @@ int bvhgpu_scene_intersect(bvhgpu_ctx* ctx, uint32_t scene_id, const bvhgpu_ray*
                            bvhgpu_hit* hits);
 int bvhgpu_scene_intersect_async(bvhgpu_ctx* ctx, uint32_t scene_id, const bvhgpu_ray* d_rays, uint32_t n,
                                  bvhgpu_hit* d_hits, bvhgpu_stream s);
+
+/* Primary rays + one cosine-weighted bounce per hit over a scene (the instanced frame), one
+ * persistent launch; as bvhgpu_blas_trace_bounce_async but two-level, hits carry the instance. */
+int bvhgpu_scene_trace_bounce_async(bvhgpu_ctx* ctx, uint32_t scene_id, const bvhgpu_ray* d_rays, uint32_t n,
+                                    uint32_t seed, bvhgpu_hit* d_hits0, bvhgpu_hit* d_hits1, bvhgpu_stream s);
+/* The bounce rays of a scene frame in pixel order (host in/out; valid[i] = 0 where none). */
+int bvhgpu_scene_bounce_rays(bvhgpu_ctx* ctx, uint32_t scene_id, const bvhgpu_ray* rays, uint32_t n, uint32_t seed,
+                             bvhgpu_ray* out, uint8_t* valid);
+/* Current object transforms and cached inverses (16 floats each, column-major). */
+int bvhgpu_scene_download_transforms(bvhgpu_ctx* ctx, uint32_t scene_id, float* xf, float* inv);
+
+/* ---- animated frames in a CUDA graph (the per-frame pattern of the reference's demos) ------------ */
+/* Closed-form animation driven by a time value in device memory (so that a captured graph replays
+ * with the current time): radial vertex wobble v = dir * (r0 + amp * sin(freq * t + phase)) of a
+ * mesh (then bvhgpu_mesh_update_async regenerates and refits its BLAS), and per-instance rotation
+ * R_i(t) = R0_i * Rot(axis_i, omega_i * t) with uniform scale and translation, written as the
+ * scene's transforms and inverses (then bvhgpu_scene_rebuild_async). */
+int bvhgpu_mesh_wobble_async(bvhgpu_ctx* ctx, uint32_t mesh_id, const float* d_dirs, const float* d_r0,
+                             const float* d_phase, float amp, float freq, const float* d_time, bvhgpu_stream s);
+int bvhgpu_scene_animate_async(bvhgpu_ctx* ctx, uint32_t scene_id, const float* d_rot0, const float* d_axis,
+                               const float* d_omega, const float* d_scale, const float* d_trans, const float* d_time,
+                               bvhgpu_stream s);
+int bvhgpu_advance_time_async(bvhgpu_ctx* ctx, float* d_time, float dt, bvhgpu_stream s);
+/* Stream capture of the context's stream: every _async call with a NULL stream between begin and
+ * end is recorded (no work runs), end instantiates the graph; launch replays it. */
+int bvhgpu_graph_begin(bvhgpu_ctx* ctx);
+int bvhgpu_graph_end(bvhgpu_ctx* ctx, uint32_t* graph_id);
+int bvhgpu_graph_launch(bvhgpu_ctx* ctx, uint32_t graph_id);
+int bvhgpu_graph_free(bvhgpu_ctx* ctx, uint32_t graph_id);
 
 /* ---- tiled render ----------------------------------------------------------------------- */
 /* Integrator::evaluate for PathTracer (BT/src/renderer.rs:104-106, 345-384) on one BLAS:

@@ -640,15 +640,13 @@ inline float rng_uniform(uint32_t key, uint32_t k) {
     return (float)(h >> 8) * (1.0f / 16777216.0f);
 }
 
-bool bounce_one(const Ray& prim, float t, const Tri& tri, uint32_t seed, uint32_t pixel, orc_ray* out) {
-    V3 p = add(prim.o, muls(prim.d, t));  // Ray::interpolate (ray.rs:37-39)
-    V3 e1 = sub(tri.v[1], tri.v[0]);
-    V3 e2 = sub(tri.v[2], tri.v[0]);
-    V3 n = cross(e1, e2);
+// From the hit point p and the (unnormalised) geometric normal n onward: normalise, face-forward
+// against d, Marsaglia sphere point, direction normalize(n + q).
+bool finish_bounce(V3 p, V3 n, V3 d_in, uint32_t seed, uint32_t pixel, orc_ray* out) {
     float nl = std::sqrt(dot(n, n));
     if (!(nl > 0.0f) || !(nl <= FLT_MAX)) return false;
     n = mk(n.x / nl, n.y / nl, n.z / nl);
-    if (dot(n, prim.d) > 0.0f) n = neg(n);
+    if (dot(n, d_in) > 0.0f) n = neg(n);
     uint32_t key = hash32(seed ^ hash32(pixel));
     V3 q = n;
     bool found = false;
@@ -674,6 +672,26 @@ bool bounce_one(const Ray& prim, float t, const Tri& tri, uint32_t seed, uint32_
     out->t = FLT_MAX;
     out->pad = 0;
     return true;
+}
+
+bool bounce_one(const Ray& prim, float t, const Tri& tri, uint32_t seed, uint32_t pixel, orc_ray* out) {
+    V3 p = add(prim.o, muls(prim.d, t));  // Ray::interpolate (ray.rs:37-39)
+    V3 e1 = sub(tri.v[1], tri.v[0]);
+    V3 e2 = sub(tri.v[2], tri.v[0]);
+    return finish_bounce(p, cross(e1, e2), prim.d, seed, pixel, out);
+}
+
+// Instanced hit: the model-space geometric normal goes to world space with the inverse-transpose
+// of the instance transform (row r of inv^T is column r of the column-major inverse).
+bool bounce_instanced(const Ray& prim, float t, const Tri& tri, const float* inv, uint32_t seed, uint32_t pixel,
+                      orc_ray* out) {
+    V3 p = add(prim.o, muls(prim.d, t));
+    V3 e1 = sub(tri.v[1], tri.v[0]);
+    V3 e2 = sub(tri.v[2], tri.v[0]);
+    V3 m = cross(e1, e2);
+    V3 n = mk((inv[0] * m.x + inv[1] * m.y) + inv[2] * m.z, (inv[4] * m.x + inv[5] * m.y) + inv[6] * m.z,
+              (inv[8] * m.x + inv[9] * m.y) + inv[10] * m.z);
+    return finish_bounce(p, n, prim.d, seed, pixel, out);
 }
 
 template <class F>
@@ -1008,6 +1026,20 @@ int orc_bounce_ray(const orc_ray* primary, const orc_hit* hit, const orc_tri* tr
                    orc_ray* out) {
     if (hit->prim == 0xFFFFFFFFu) return 0;
     return bounce_one(load_ray(*primary), hit->t, load_tri(*tri), seed, pixel, out) ? 1 : 0;
+}
+
+int orc_scene_bounce_rays(const uint32_t* blas_of, const float* inv, const orc_tri* tris, const uint32_t* tri_off,
+                          const orc_ray* primaries, const orc_hit* hits, uint32_t nrays, uint32_t seed, orc_ray* out,
+                          uint8_t* valid) {
+    for (uint32_t i = 0; i < nrays; ++i) {
+        valid[i] = 0;
+        if (hits[i].prim == 0xFFFFFFFFu) continue;
+        const uint32_t obj = hits[i].inst;
+        const orc_tri* tb = tris + tri_off[blas_of[obj]];
+        valid[i] = bounce_instanced(load_ray(primaries[i]), hits[i].t, load_tri(tb[hits[i].prim]), inv + 16 * obj,
+                                    seed, i, &out[i]) ? 1 : 0;
+    }
+    return ORC_OK;
 }
 
 int orc_bounce_rays(const orc_ray* primaries, const orc_hit* hits, uint32_t nrays, const orc_tri* tris,

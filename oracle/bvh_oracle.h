@@ -97,6 +97,10 @@ int orc_bounce_ray(const orc_ray* primary, const orc_hit* hit, const orc_tri* tr
                    uint32_t pixel, orc_ray* out);
 int orc_bounce_rays(const orc_ray* primaries, const orc_hit* hits, uint32_t nrays, const orc_tri* tris,
                     uint32_t seed, orc_ray* out, uint8_t* valid);
+/* Bounce rays of instanced hits (hit.inst selects the object, tri_off / blas_of as for the scene). */
+int orc_scene_bounce_rays(const uint32_t* blas_of, const float* inv, const orc_tri* tris, const uint32_t* tri_off,
+                          const orc_ray* primaries, const orc_hit* hits, uint32_t nrays, uint32_t seed, orc_ray* out,
+                          uint8_t* valid);
 
 #ifdef __cplusplus
 }

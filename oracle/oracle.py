@@ -89,6 +89,7 @@ def lib():
         L.orc_render.argtypes = [P, P, i32, i32, i32, P, i32, P, P, u32, P, u32, P, P, P]
         L.orc_bounce_ray.argtypes = [P, P, P, u32, u32, P]
         L.orc_bounce_rays.argtypes = [P, P, u32, P, u32, P, P]
+        L.orc_scene_bounce_rays.argtypes = [P, P, P, P, P, P, u32, u32, P, P]
         _lib = L
     return _lib
 
@@ -286,6 +287,17 @@ def bounce_rays(primaries, hits, tris, seed):
     out = np.zeros(len(primaries), RAY)
     valid = np.zeros(len(primaries), np.uint8)
     rc = lib().orc_bounce_rays(_p(primaries), _p(hits), len(primaries), _p(tris), seed, _p(out), _p(valid))
+    assert rc == 0
+    return out, valid.astype(bool)
+
+
+def scene_bounce_rays(sa: SceneArrays, primaries, hits, seed):
+    primaries = _c(primaries, RAY)
+    hits = _c(hits, HIT)
+    out = np.zeros(len(primaries), RAY)
+    valid = np.zeros(len(primaries), np.uint8)
+    rc = lib().orc_scene_bounce_rays(_p(sa.blas_of), _p(sa.inv), _p(sa.tris), _p(sa.tri_off), _p(primaries),
+                                     _p(hits), len(primaries), seed, _p(out), _p(valid))
     assert rc == 0
     return out, valid.astype(bool)
 
