@@ -681,7 +681,7 @@ int bvhgpu_trace_batch(bvhgpu_ctx* ctx, const bvhgpu_batch_item* items, uint32_t
 int bvhgpu_scene_create(bvhgpu_ctx* ctx, const uint32_t* blas_ids, uint32_t nobjects, uint32_t* scene_id) {
     if (!ctx || !blas_ids || !scene_id || nobjects == 0)
         return fail(ctx, BVHGPU_ERR_INVALID_ARG, "scene_create: empty scene");
-    if (nobjects > 4096) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "scene_create: at most 4096 objects");
+    if (nobjects > kMaxSceneObjects) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "scene_create: at most 4096 objects");
     DeviceScene sc;
     sc.nobjects = nobjects;
     sc.blas_ids.assign(blas_ids, blas_ids + nobjects);

@@ -1,15 +1,12 @@
 // BLAS vertex upload + refit, TLAS rebuild and instanced (two-level) traversal.
 //
-// Refit (Bvh::refit, bvh.rs:469-493) runs bottom-up with one thread per leaf and one
-// arrival counter per node: the second child to finish computes its parent, so every
-// node is written once, after both children, with the reference's min/max order
-// (left child first).  The counters are reset by the thread that consumes them, so they
-// are all zero again when the kernel ends.
+// Refit (Bvh::refit, bvh.rs:469-493): leaf boxes by a reduction over the triangles (exact
+// order-preserving keys, so the min/max and its ties are the reference's), then the inner
+// nodes bottom-up with one arrival counter per node: the second child to finish computes its
+// parent with the reference's min/max order (left child first).
 //
-// TLAS rebuild (Tlas::rebuild, tlas.rs:204-250) is the reference's agglomerative
-// clustering itself, run by one warp over the nodes held in shared memory: each
-// find_best_match (tlas.rs:179-202) is a warp-wide argmin, so the resulting TLAS is
-// bit-identical to the reference's.
+// TLAS rebuild (Tlas::rebuild, tlas.rs:204-250): the reference's agglomerative clustering with
+// find_best_match results cached per list position in shared memory (see k_tlas_rebuild).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -192,47 +189,76 @@ __global__ void __launch_bounds__(kBlock) k_refit_leaves(float4* nodes, const fl
 }
 
 // ---- TLAS ------------------------------------------------------------------------------------
+// Tlas::rebuild (tlas.rs:204-250) walks nearest neighbours over a list of node indices and
+// calls find_best_match (tlas.rs:179-202) -- a full scan of the list -- at every step.  Here
+// each list position keeps the result find_best_match would give for it (surface area and
+// position) in shared memory, and a merge updates only what it can change:
+//  - the merged node lands on position a, the last node moves to position b, the list shrinks;
+//  - a position whose cached best was a, b or the old last position is rescanned in full
+//    (one warp per position);
+//  - any other position keeps its cached best, which is still the first minimum over the
+//    positions whose node did not change, and compares it with the two changed positions.
+// The walk then reads the cache.  Minimum first, ties to the lower position, only areas below
+// FLT_MAX taken: exactly the reference's strict `<` scan from FLT_MAX, so the TLAS is bit for
+// bit Tlas::rebuild's, including the case where position a itself leaves the list.
 
-struct SNode {  // shared-memory TLAS node
-    float lo[3];
-    float hi[3];
-    uint32_t left_right;
-    uint32_t blas;
+constexpr int kTlasThreads = 512;
+
+struct TlasSmem {  // one entry per list position
+    float *lx, *ly, *lz, *hx, *hy, *hz;  // node bounds (nodes[list[p]].aabb)
+    int* node;                            // list[p]: node index
+    float* csa;                           // cached find_best_match(p): surface area
+    int* cpos;                            //   and position (-1: none)
+    int* inval;                           // positions to rescan after a merge
 };
 
-__device__ __forceinline__ float sa_merge(const SNode& a, const SNode& b) {
-    // find_best_match (tlas.rs:184-193): component_max / component_min with a's first
-    float ex = fsub(max_ni(a.hi[0], b.hi[0]), min_ni(a.lo[0], b.lo[0]));
-    float ey = fsub(max_ni(a.hi[1], b.hi[1]), min_ni(a.lo[1], b.lo[1]));
-    float ez = fsub(max_ni(a.hi[2], b.hi[2]), min_ni(a.lo[2], b.lo[2]));
+struct Box6 {
+    float lx, ly, lz, hx, hy, hz;
+};
+
+__device__ __forceinline__ Box6 load_box(const TlasSmem& S, int p) {
+    return Box6{S.lx[p], S.ly[p], S.lz[p], S.hx[p], S.hy[p], S.hz[p]};
+}
+
+// find_best_match's area (tlas.rs:184-193): component_max / component_min with the query
+// node's coordinate first, then ex*ey + ey*ez + ez*ex.
+__device__ __forceinline__ float sa_merge(const Box6& a, const TlasSmem& S, int r) {
+    float ex = fsub(max_ni(a.hx, S.hx[r]), min_ni(a.lx, S.lx[r]));
+    float ey = fsub(max_ni(a.hy, S.hy[r]), min_ni(a.ly, S.ly[r]));
+    float ez = fsub(max_ni(a.hz, S.hz[r]), min_ni(a.lz, S.lz[r]));
     return fadd(fadd(fmul(ex, ey), fmul(ey, ez)), fmul(ez, ex));
 }
 
-// Warp-wide find_best_match: the first b (in index order) with the strictly smallest
-// surface area below FLT_MAX, or -1.
-__device__ __forceinline__ int warp_best_match(const SNode* nodes, const int* list, int n, int a) {
-    const unsigned lane = threadIdx.x & 31u;
-    float best = FLT_MAX;
-    int best_b = -1;
-    const SNode& na = nodes[list[a]];
-    for (int b = (int)lane; b < n; b += 32) {
-        if (b == a) continue;
-        float sa = sa_merge(na, nodes[list[b]]);
-        if (sa < best) {
-            best = sa;
-            best_b = b;
+// (s, r) beats the current best (bs, bq): the area is taken at all only below FLT_MAX, and ties
+// go to the lower position.
+__device__ __forceinline__ bool better(float s, int r, float bs, int bq) {
+    return s < FLT_MAX && (bq < 0 || s < bs || (s == bs && r < bq));
+}
+
+// Full find_best_match for position p over positions [0, count) by one warp.
+__device__ __forceinline__ void warp_best_match(const TlasSmem& S, int p, int count, float& out_s, int& out_q) {
+    const int lane = (int)(threadIdx.x & 31u);
+    const Box6 P = load_box(S, p);
+    float bs = FLT_MAX;
+    int bq = -1;
+    for (int r = lane; r < count; r += 32) {
+        if (r == p) continue;
+        float s = sa_merge(P, S, r);
+        if (s < bs) {  // strict, from FLT_MAX: this lane's first minimum
+            bs = s;
+            bq = r;
         }
     }
     for (int off = 16; off > 0; off >>= 1) {
-        float ob = __shfl_xor_sync(kFull, best, off);
-        int obb = __shfl_xor_sync(kFull, best_b, off);
-        bool take = (obb >= 0) && (best_b < 0 || ob < best || (ob == best && obb < best_b));
-        if (take) {
-            best = ob;
-            best_b = obb;
+        float os = __shfl_xor_sync(kFull, bs, off);
+        int oq = __shfl_xor_sync(kFull, bq, off);
+        if (oq >= 0 && better(os, oq, bs, bq)) {
+            bs = os;
+            bq = oq;
         }
     }
-    return best_b;
+    out_s = bs;
+    out_q = bq;
 }
 
 __device__ __forceinline__ void xf_point_g(const float* m, float x, float y, float z, float* out) {
@@ -241,23 +267,38 @@ __device__ __forceinline__ void xf_point_g(const float* m, float x, float y, flo
     out[2] = fadd(fadd(fadd(fmul(m[2], x), fmul(m[6], y)), fmul(m[10], z)), fmul(m[14], 1.0f));
 }
 
-// One block: object world bounds (SceneObject::set_transform, scene_object.rs:60-75) in
-// parallel, then warp 0 runs Tlas::rebuild.  status[0] gets nodes_used, status[1] an error.
-__global__ void k_tlas_rebuild(const GBlas* __restrict__ blas_table, const uint32_t* __restrict__ obj_blas,
-                               const float* __restrict__ xf, uint32_t nobj, float4* __restrict__ tlas_out,
-                               uint32_t* status) {
-    extern __shared__ unsigned char smem[];
-    SNode* nodes = reinterpret_cast<SNode*>(smem);
-    int* list = reinterpret_cast<int*>(nodes + 2 * nobj);
-    for (uint32_t i = threadIdx.x; i < 2 * nobj; i += blockDim.x) {  // TlasNode::default
-        SNode& s = nodes[i];
-        s.lo[0] = s.lo[1] = s.lo[2] = FLT_MAX;
-        s.hi[0] = s.hi[1] = s.hi[2] = -FLT_MAX;
-        s.left_right = 0;
-        s.blas = 0;
-    }
-    __syncthreads();
-    for (uint32_t i = threadIdx.x; i < nobj; i += blockDim.x) {
+__device__ __forceinline__ void store_tlas_node(float4* out, uint32_t i, const Box6& b, uint32_t left_right,
+                                                uint32_t blas) {
+    out[2ull * i] = make_float4(b.lx, b.ly, b.lz, __uint_as_float(left_right));
+    out[2ull * i + 1] = make_float4(b.hx, b.hy, b.hz, __uint_as_float(blas));
+}
+
+// One block.  Object world bounds (SceneObject::set_transform, scene_object.rs:60-75) in
+// parallel, the cache filled one warp per position, then the walk: every thread follows it
+// (it only reads shared memory), thread 0 writes the merged nodes, all threads update the
+// cache.  status[0] gets nodes_used, status[1] an error (the reference would panic).
+__global__ void __launch_bounds__(kTlasThreads) k_tlas_rebuild(const GBlas* __restrict__ blas_table,
+                                                               const uint32_t* __restrict__ obj_blas,
+                                                               const float* __restrict__ xf, uint32_t nobj,
+                                                               float4* __restrict__ tlas_out, uint32_t* status) {
+    extern __shared__ float tsm[];
+    __shared__ int s_ninval, s_best_a;
+    const int n = (int)nobj;
+    TlasSmem S;
+    S.lx = tsm;
+    S.ly = tsm + n;
+    S.lz = tsm + 2 * n;
+    S.hx = tsm + 3 * n;
+    S.hy = tsm + 4 * n;
+    S.hz = tsm + 5 * n;
+    S.node = reinterpret_cast<int*>(tsm + 6 * n);
+    S.csa = tsm + 7 * n;
+    S.cpos = reinterpret_cast<int*>(tsm + 8 * n);
+    S.inval = reinterpret_cast<int*>(tsm + 9 * n);
+    const int tid = (int)threadIdx.x;
+    const int warp = tid >> 5, lane = tid & 31, nwarps = (int)(blockDim.x >> 5);
+
+    for (int i = tid; i < n; i += (int)blockDim.x) {
         const GBlas& b = blas_table[obj_blas[i]];
         float4 rlo = b.nodes[0], rhi = b.nodes[1];  // Bvh::bounds = nodes[0].aabb (bvh.rs:499-501)
         const float* m = xf + 16ull * i;
@@ -271,66 +312,123 @@ __global__ void k_tlas_rebuild(const GBlas* __restrict__ blas_table, const uint3
                 hi[k] = max_ni(hi[k], p[k]);
             }
         }
-        SNode& s = nodes[1 + i];  // leaves at 1..nobj (tlas.rs:210-218)
-        for (int k = 0; k < 3; ++k) {
-            s.lo[k] = lo[k];
-            s.hi[k] = hi[k];
-        }
-        s.blas = i;
-        s.left_right = 0;
-        list[i] = (int)(1 + i);
+        S.lx[i] = lo[0];
+        S.ly[i] = lo[1];
+        S.lz[i] = lo[2];
+        S.hx[i] = hi[0];
+        S.hy[i] = hi[1];
+        S.hz[i] = hi[2];
+        S.node[i] = 1 + i;  // leaves at 1..nobj (tlas.rs:210-218)
+        store_tlas_node(tlas_out, 1u + (uint32_t)i, Box6{lo[0], lo[1], lo[2], hi[0], hi[1], hi[2]}, 0u, (uint32_t)i);
     }
     __syncthreads();
-    if (threadIdx.x >= 32) return;
-    const unsigned lane = threadIdx.x;
-    int count = (int)nobj;
-    int used = 1 + (int)nobj;
-    int a = 0;
-    int b = warp_best_match(nodes, list, count, a);
+    for (int p = warp; p < n; p += nwarps) {
+        float s;
+        int q;
+        warp_best_match(S, p, n, s, q);
+        if (lane == 0) {
+            S.csa[p] = s;
+            S.cpos[p] = q;
+        }
+    }
+    __syncthreads();
+
+    int count = n, used = 1 + n, a = 0;
+    int b = S.cpos[0];
     uint32_t err = 0;
-    uint64_t iters = 0;
-    const uint64_t max_iters = 4ull * nobj * nobj + 64;
+    uint64_t steps = 0;
+    const uint64_t max_steps = 4ull * nobj * nobj + 64;
     while (count > 1) {
-        if (b < 0 || ++iters > max_iters) {
+        if (b < 0 || ++steps > max_steps) {
             err = 1;
             break;
         }
-        int c = warp_best_match(nodes, list, count, b);
-        if (a == c) {
-            int ia = list[a], ib = list[b];
-            if (lane == 0) {
-                SNode na = nodes[ia], nb = nodes[ib];
-                SNode& nn = nodes[used];
-                nn.left_right = (uint32_t)ia + ((uint32_t)ib << 16);  // LeftRightIndex::new (tlas.rs:18-22)
-                for (int k = 0; k < 3; ++k) {
-                    nn.lo[k] = min_ni(na.lo[k], nb.lo[k]);
-                    nn.hi[k] = max_ni(na.hi[k], nb.hi[k]);
-                }
-                list[a] = used;
-                list[b] = list[count - 1];
-            }
-            __syncwarp();
-            used += 1;
-            count -= 1;
-            b = warp_best_match(nodes, list, count, a);
-        } else {
-            if (c < 0) {
-                err = 1;
-                break;
-            }
+        const int c = S.cpos[b];
+        if (a != c) {
             a = b;
             b = c;
+            continue;
         }
+        const int last = count - 1;
+        __syncthreads();  // everyone has read the cache before it changes
+        if (tid == 0) {
+            const Box6 A = load_box(S, a), B = load_box(S, b);
+            const Box6 M{min_ni(A.lx, B.lx), min_ni(A.ly, B.ly), min_ni(A.lz, B.lz),
+                         max_ni(A.hx, B.hx), max_ni(A.hy, B.hy), max_ni(A.hz, B.hz)};
+            // LeftRightIndex::new(a, b) = a + (b << 16) (tlas.rs:18-22)
+            store_tlas_node(tlas_out, (uint32_t)used, M, (uint32_t)S.node[a] + ((uint32_t)S.node[b] << 16), 0u);
+            S.lx[a] = M.lx;
+            S.ly[a] = M.ly;
+            S.lz[a] = M.lz;
+            S.hx[a] = M.hx;
+            S.hy[a] = M.hy;
+            S.hz[a] = M.hz;
+            S.node[a] = used;
+            S.lx[b] = S.lx[last];  // list[b] = list[count - 1], after list[a] (tlas.rs:238-240)
+            S.ly[b] = S.ly[last];
+            S.lz[b] = S.lz[last];
+            S.hx[b] = S.hx[last];
+            S.hy[b] = S.hy[last];
+            S.hz[b] = S.hz[last];
+            S.node[b] = S.node[last];
+            s_ninval = 0;
+        }
+        count = last;
+        used += 1;
+        __syncthreads();
+        for (int p = tid; p < count; p += (int)blockDim.x) {
+            int q = S.cpos[p];
+            if (p == a || p == b || q == a || q == b || q == last) {
+                S.inval[atomicAdd(&s_ninval, 1)] = p;
+                continue;
+            }
+            const Box6 P = load_box(S, p);
+            float bs = S.csa[p];
+            if (a < count) {
+                float s = sa_merge(P, S, a);
+                if (better(s, a, bs, q)) {
+                    bs = s;
+                    q = a;
+                }
+            }
+            if (b < count) {
+                float s = sa_merge(P, S, b);
+                if (better(s, b, bs, q)) {
+                    bs = s;
+                    q = b;
+                }
+            }
+            S.csa[p] = bs;
+            S.cpos[p] = q;
+        }
+        __syncthreads();
+        const int ninval = s_ninval;
+        for (int k = warp; k < ninval; k += nwarps) {
+            const int p = S.inval[k];
+            float s;
+            int q;
+            warp_best_match(S, p, count, s, q);
+            if (lane == 0) {
+                S.csa[p] = s;
+                S.cpos[p] = q;
+            }
+        }
+        if (a >= count && warp == 0) {  // position a left the list; its stale entry is still read
+            float s;
+            int q;
+            warp_best_match(S, a, count, s, q);
+            if (lane == 0) s_best_a = q;
+        }
+        __syncthreads();
+        b = (a < count) ? S.cpos[a] : s_best_a;
     }
-    __syncwarp();
-    if (lane == 0 && err == 0) nodes[0] = nodes[list[a]];  // tlas.rs:248
-    __syncwarp();
-    for (uint32_t i = lane; i < 2 * nobj; i += 32) {
-        const SNode& s = nodes[i];
-        tlas_out[2ull * i] = make_float4(s.lo[0], s.lo[1], s.lo[2], __uint_as_float(s.left_right));
-        tlas_out[2ull * i + 1] = make_float4(s.hi[0], s.hi[1], s.hi[2], __uint_as_float(s.blas));
-    }
-    if (lane == 0) {
+    if (tid == 0) {
+        if (err == 0) {  // nodes[0] = nodes[list[a]] (tlas.rs:248); thread 0 wrote that node
+            const uint32_t r = (uint32_t)S.node[a];
+            const float4 r0 = tlas_out[2ull * r], r1 = tlas_out[2ull * r + 1];
+            tlas_out[0] = r0;
+            tlas_out[1] = r1;
+        }
         status[0] = (uint32_t)used;
         status[1] = err;
     }
@@ -709,18 +807,19 @@ cudaError_t launch_refit(bvhgpu_ctx* ctx, DeviceBlas& b, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-size_t tlas_smem_bytes(uint32_t nobj) { return sizeof(SNode) * 2ull * nobj + sizeof(int) * nobj; }
+size_t tlas_smem_bytes(uint32_t nobj) { return 10ull * sizeof(float) * nobj; }
 
 cudaError_t launch_tlas_rebuild(bvhgpu_ctx* ctx, DeviceScene& sc, cudaStream_t s) {
     size_t smem = tlas_smem_bytes(sc.nobjects);
-    static bool attr_set = false;
+    static bool attr_set = false;  // set outside graph capture: the first rebuild is scene_create's
     if (!attr_set) {
-        cudaFuncSetAttribute(k_tlas_rebuild, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(k_tlas_rebuild, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)tlas_smem_bytes(kMaxSceneObjects));
         attr_set = true;
     }
     LaunchScope scope(ctx, BVHGPU_K_TLAS_BUILD, s);
-    k_tlas_rebuild<<<1, 256, smem, s>>>(static_cast<const GBlas*>(sc.blas_table), sc.obj_blas, sc.xf, sc.nobjects,
-                                        sc.tlas, ctx->d_scratch + 8);
+    k_tlas_rebuild<<<1, kTlasThreads, smem, s>>>(static_cast<const GBlas*>(sc.blas_table), sc.obj_blas, sc.xf,
+                                                  sc.nobjects, sc.tlas, ctx->d_scratch + 8);
     g_launches++;
     return cudaGetLastError();
 }

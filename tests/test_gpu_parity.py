@@ -244,6 +244,30 @@ def test_tlas_rebuild_and_scene_trace(ctx):
     assert (ref["prim"] != bt.MISS).sum() > 1000
 
 
+@pytest.mark.parametrize("n,dup", [(1, 0), (2, 0), (3, 0), (37, 0), (300, 3), (1000, 0), (1000, 2), (4096, 0)])
+def test_tlas_rebuild_sizes_and_ties(ctx, n, dup):
+    """TLAS nodes bit-identical to Tlas::rebuild from 1 to the 4,096-object maximum; with dup > 0
+    every dup-th object copies object 0's transform, so find_best_match meets exact area ties
+    (decided by list position) and zero-area merges."""
+    tris, bvh = build(scenes.displaced_icosphere(2, 5).triangles())
+    blas = ctx.upload_blas(bvh, tris)
+    xf, inv = random_instances(n, 100 + n)
+    if dup:
+        xf[::dup] = xf[0]
+        inv[::dup] = inv[0]
+    sc = ctx.scene([blas] * n, xf, inv)
+    gpu_nodes, gpu_used = sc.download_tlas()
+    root = bvh.nodes[0]
+    omin = np.zeros((n, 3), np.float32)
+    omax = np.zeros((n, 3), np.float32)
+    for i in range(n):
+        omin[i], omax[i] = orc.object_bounds(root["bounds_min"], root["bounds_max"], xf[i])
+    ref_nodes, ref_used = orc.tlas_build(omin, omax)
+    assert gpu_used == ref_used
+    assert gpu_nodes.tobytes() == ref_nodes.tobytes(), "TLAS not bit-identical to Tlas::rebuild"
+    sc.free()
+
+
 # ---- render ----------------------------------------------------------------------------------------
 
 def test_render_quad_viewport_matches_oracle(ctx):
