@@ -229,6 +229,17 @@ def run_ours(args):
     n_bounce = int((h0["prim"] != bt.MISS).sum())
     rays_per_step = n + n_bounce
 
+    # autotune both pipelines on this frame (configs never change results, only speed)
+    tuned, tune_s = {}, 0.0
+    if not args.no_tune:
+        t0 = time.perf_counter()
+        cfg, ms_ = ctx.autotune(bt.K_PERSISTENT_BOUNCE, d_rays, n, d_h0, d_h1, target=blas.id, seed=BOUNCE_SEED,
+                                reps=3)
+        tuned["persistent_bounce"] = dict(cfg, ms=ms_)
+        cfg, ms_ = ctx.autotune(bt.K_TRACE_BLAS, d_rays, n, d_h0, target=blas.id, reps=3)
+        tuned["trace_blas"] = dict(cfg, ms=ms_)
+        tune_s = time.perf_counter() - t0
+
     ev = [(ctx.event(), ctx.event()) for _ in range(args.steps)]
 
     def timed(m, profile=False):
@@ -304,7 +315,7 @@ def run_ours(args):
         "config": {"workload": WORKLOAD, "mode": args.mode, "primary_rays": n, "bounce_rays": n_bounce,
                    "rays_per_step": rays_per_step, "triangles": int(len(tris)), "bvh_nodes": bvh.nodes_used,
                    "bvh_depth": blas.depth, "l2": "flushed between steps (256 MB memset)",
-                   "parallelism": f"replicas x{world}", "seed": SEED},
+                   "parallelism": f"replicas x{world}", "seed": SEED, "tuned": tuned, "tune_s": tune_s},
         "plain_vs_persistent": {
             args.mode: value / world,
             ("plain" if mode == bt.MODE_PERSISTENT else "persistent"): other_value,
@@ -416,20 +427,42 @@ def run_batch(args):
     d_hits2 = ctx.device_buffer(n * bt.HIT.itemsize)
     ev = [(ctx.event(), ctx.event()) for _ in range(args.steps)]
 
-    def timed(mode, out):
+    # autotune on a 1/16 sample of every scene (its first primaries and first random rays)
+    tuned, tune_s = {}, 0.0
+    if not args.no_tune:
+        t0 = time.perf_counter()
+        s_items = np.zeros(len(built), bt.BATCH_ITEM)
+        s_rays, off = [], 0
+        for i, (b, (_, _, r)) in enumerate(zip(blases, built)):
+            k, half = max(32, len(r) // 32), len(r) // 2
+            sr = np.concatenate([r[:k], r[half:half + k]])
+            s_items[i] = (b.id, off, len(sr), 0)
+            s_rays.append(sr)
+            off += len(sr)
+        s_rays = np.concatenate(s_rays)
+        d_srays = ctx.to_device(s_rays)
+        for kernel, name in ((bt.K_TRACE_BATCH, "trace_batch"), (bt.K_TRACE_BLAS, "trace_blas")):
+            cfg, ms_ = ctx.autotune(kernel, d_srays, len(s_rays), d_hits, items=s_items, reps=2)
+            tuned[name] = dict(cfg, ms_on_sample=ms_)
+        tuned["sample_rays"] = int(len(s_rays))
+        del d_srays
+        tune_s = time.perf_counter() - t0
+
+    def timed(mode, out, steps=None):
+        steps = steps or args.steps
         for _ in range(args.warmup):
             ctx.flush_l2()
             ctx.trace_batch_async(items, d_rays, n, mode, out)
         ctx.sync()
         ctx.profile(True)
         ctx.profile_read()
-        for s in range(args.steps):
+        for s in range(steps):
             ctx.flush_l2()
             ev[s][0].record()
             ctx.trace_batch_async(items, d_rays, n, mode, out)
             ev[s][1].record()
         ctx.sync()
-        ms = [a.elapsed_ms(b) for a, b in ev]
+        ms = [a.elapsed_ms(b) for a, b in ev[:steps]]
         prof = ctx.profile_read()
         ctx.profile(False)
         return ms, prof
@@ -444,6 +477,16 @@ def run_batch(args):
     identical = bool(h1.tobytes() == h2.tobytes())
     value = n * args.steps / (sum(ms_p) / 1e3) / 1e6
     plain = n * args.steps / (sum(ms_plain) / 1e3) / 1e6
+    # the textbook plain traversal: one launch per scene, one thread per ray, every leaf tested by
+    # its own lane (no warp-cooperative leaves), launch shape as tuned for the plain kernel
+    tb_cfg = ctx.tune_get(bt.K_TRACE_BLAS)
+    ctx.tune_set(bt.K_TRACE_BLAS, big_leaf=bt.BIG_LEAF_NEVER)
+    tb_steps = max(1, min(3, args.steps))
+    ms_tb, _ = timed(bt.MODE_PLAIN, d_hits2, steps=tb_steps)
+    ctx.tune_set(bt.K_TRACE_BLAS, **tb_cfg)
+    h3 = d_hits2.download(np.zeros(n, bt.HIT))
+    identical = identical and bool(h1.tobytes() == h3.tobytes())
+    textbook = n * tb_steps / (sum(ms_tb) / 1e3) / 1e6
     # e2e: bvhgpu_trace_batch with pinned host buffers
     pin_r = ctx.pinned((n,), bt.RAY)
     pin_r.array[:] = rays
@@ -468,8 +511,11 @@ def run_batch(args):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
         "config": {"workload": WORKLOAD3, "scenes": len(built), "rays": n,
                    "triangles": int(sum(len(t) for t, _, _ in built)), "setup_s": setup_s,
-                   "l2": "flushed between steps (256 MB memset)", "parallelism": f"replicas x{world}", "seed": SEED},
+                   "l2": "flushed between steps (256 MB memset)", "parallelism": f"replicas x{world}", "seed": SEED,
+                   "tuned": tuned, "tune_s": tune_s},
         "plain_vs_persistent": {"persistent": value, "plain": plain, "ratio_persistent_over_plain": value / plain,
+                                "plain_per_lane_leaves": textbook,
+                                "ratio_persistent_over_plain_per_lane_leaves": value / textbook,
                                 "hit_records_identical": identical},
         "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": n * bt.RAY.itemsize,
                 "d2h_bytes_per_step": n * bt.HIT.itemsize},
@@ -617,6 +663,19 @@ def run_frames(args):
     ctx.sync()
     prof = ctx.profile_read()
     ctx.profile(False)
+    tuned, tune_s = {}, 0.0
+    if not args.no_tune:  # tune the frame's trace kernel before the graph captures its launch
+        t0 = time.perf_counter()
+        cfg_t, ms_ = ctx.autotune(bt.K_SCENE_BOUNCE, sc.d_rays, n, sc.d_hits0, sc.d_hits1, target=sc.scene.id,
+                                  seed=sc.seed, reps=3)
+        tuned["scene_bounce"] = dict(cfg_t, ms=ms_)
+        tune_s = time.perf_counter() - t0
+        ctx.profile(True)
+        ctx.profile_read()
+        sc.frame_async()
+        ctx.sync()
+        prof = ctx.profile_read()
+        ctx.profile(False)
     sc.capture()
     # rays per frame: primaries + the bounces of that frame's primary hits (counted in a first pass)
     sc.set_time(0.0)
@@ -655,7 +714,7 @@ def run_frames(args):
         "config": {"workload": WORKLOAD2, "frames": nframes, "primary_rays_per_frame": n,
                    "bounce_rays_total": sum(bounces), "instances": len(sc.blas_of),
                    "l2": "flushed between frames (256 MB memset)", "step": "one frame = one CUDA graph launch",
-                   "seed": SEED},
+                   "seed": SEED, "tuned": tuned, "tune_s": tune_s},
         "frame_ms": {"mean": total_ms / nframes, "max": max(best), "min": min(best)},
         "e2e": None, "gpu_launches": 1, "clocks": clk,
         "kernel_ms_one_frame": {k: {"ms_total": v[0], "launches": v[1]} for k, v in prof.items()},
@@ -675,6 +734,7 @@ def main():
     ap.add_argument("--config", type=int, choices=[1, 2, 3, 4], default=1,
                     help="1: displaced icosphere frame + bounce (default); 2: instanced animated frames in a CUDA "
                          "graph; 3: uneven 64-scene batch; 4: differentiable render (adjoint ms/step)")
+    ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (use the default launch configs)")
     ap.add_argument("--no-cpu-baseline", action="store_true",
                     help="skip the CPU-baseline leg (outside the timed region), e.g. under a profiler")
     args = ap.parse_args()

@@ -22,6 +22,17 @@ TLAS_NODE = np.dtype([("bounds_min", "<f4", 3), ("bounds_max", "<f4", 3),
 BATCH_ITEM = np.dtype([("blas", "<u4"), ("ray_offset", "<u4"), ("ray_count", "<u4"), ("reserved", "<u4")])
 assert NODE.itemsize == 32 and RAY.itemsize == 32 and HIT.itemsize == 20
 assert TLAS_NODE.itemsize == 32 and BATCH_ITEM.itemsize == 16
+TUNE_CONFIG = np.dtype([("block", "<u4"), ("min_blocks", "<u4"), ("stack", "<u4"), ("big_leaf", "<u4"),
+                        ("refill", "<u4"), ("reserved", "<u4")])
+BIG_LEAF_NEVER = 0xFFFFFFFF
+
+
+class TuneJob(ctypes.Structure):
+    """bvhgpu_tune_job."""
+    _fields_ = [("kernel", ctypes.c_int), ("target", ctypes.c_uint32), ("d_rays", ctypes.c_void_p),
+                ("n", ctypes.c_uint32), ("seed", ctypes.c_uint32), ("d_hits0", ctypes.c_void_p),
+                ("d_hits1", ctypes.c_void_p), ("items", ctypes.c_void_p), ("nitems", ctypes.c_uint32)]
+
 
 MISS = 0xFFFFFFFF
 FLT_MAX = np.float32(np.finfo(np.float32).max)
@@ -110,6 +121,10 @@ SIGNATURES = {
     "bvhgpu_mse_loss": (_I, [_P, _P, _P, _U32, _P]),
     "bvhgpu_lambert_adjoint_async": (_I, [_P, _U32, _P, _U32, _P, _P, _P, _P, _P, _P]),
     "bvhgpu_mesh_sgd_step_async": (_I, [_P, _U32, _P, ctypes.c_float, _P]),
+    "bvhgpu_tune_get": (_I, [_P, _I, _P]),
+    "bvhgpu_tune_set": (_I, [_P, _I, _P]),
+    "bvhgpu_tune_space": (_I, [_I, _P, _U32, _P]),
+    "bvhgpu_autotune": (_I, [_P, _P, _U32, _P, _P]),
     "bvhgpu_refit_noalloc": (_I, [_P, _U32, _P, _U32, _P, _P]),
 }
 

@@ -129,6 +129,54 @@ class Context:
                                                      d_hits.ptr, stream))
 
 
+    # ---- launch configuration / autotuning (bvhgpu_tune_*, bvhgpu_autotune) ----
+    def tune_get(self, kernel: int) -> dict:
+        c = np.zeros(1, _lib.TUNE_CONFIG)
+        self.check(self.lib.bvhgpu_tune_get(self.h, kernel, ptr(c)))
+        return {k: int(c[0][k]) for k in _lib.TUNE_CONFIG.names if k != "reserved"}
+
+    def tune_set(self, kernel: int, **cfg):
+        c = np.zeros(1, _lib.TUNE_CONFIG)
+        cur = self.tune_get(kernel)
+        cur.update(cfg)
+        for k, v in cur.items():
+            c[0][k] = v
+        self.check(self.lib.bvhgpu_tune_set(self.h, kernel, ptr(c)))
+
+    @staticmethod
+    def tune_space(kernel: int) -> list:
+        lib = _lib.load()
+        n = ctypes.c_uint32()
+        rc = lib.bvhgpu_tune_space(kernel, None, 0, ctypes.byref(n))
+        if rc:
+            raise _lib.BvhGpuError(rc, "tune_space")
+        out = np.zeros(n.value, _lib.TUNE_CONFIG)
+        lib.bvhgpu_tune_space(kernel, ptr(out), n.value, ctypes.byref(n))
+        return [{k: int(r[k]) for k in _lib.TUNE_CONFIG.names if k != "reserved"} for r in out]
+
+    def autotune(self, kernel: int, d_rays: "DeviceBuffer", n: int, d_hits0: "DeviceBuffer", d_hits1=None,
+                 target: int = 0, seed: int = 0, items=None, reps: int = 3):
+        """Runs bvhgpu_autotune on one call of `kernel`; returns (config dict, ms per call)."""
+        job = _lib.TuneJob()
+        job.kernel = kernel
+        job.target = target
+        job.d_rays = d_rays.ptr.value if isinstance(d_rays.ptr, ctypes.c_void_p) else d_rays.ptr
+        job.n = n
+        job.seed = seed
+        job.d_hits0 = d_hits0.ptr.value if isinstance(d_hits0.ptr, ctypes.c_void_p) else d_hits0.ptr
+        if d_hits1 is not None:
+            job.d_hits1 = d_hits1.ptr.value if isinstance(d_hits1.ptr, ctypes.c_void_p) else d_hits1.ptr
+        keep = None
+        if items is not None:
+            keep = np.ascontiguousarray(items, BATCH_ITEM)
+            job.items = keep.ctypes.data
+            job.nitems = len(keep)
+        best = np.zeros(1, _lib.TUNE_CONFIG)
+        ms = ctypes.c_float()
+        self.check(self.lib.bvhgpu_autotune(self.h, ctypes.byref(job), reps, ptr(best), ctypes.byref(ms)))
+        return {k: int(best[0][k]) for k in _lib.TUNE_CONFIG.names if k != "reserved"}, float(ms.value)
+
+
 class DeviceBuffer:
     def __init__(self, ctx: Context, nbytes: int):
         self.ctx = ctx

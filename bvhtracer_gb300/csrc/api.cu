@@ -61,6 +61,12 @@ int fail(bvhgpu_ctx* ctx, int code, const char* fmt, ...) {
     return code;
 }
 
+}  // namespace
+
+int bvhgpu::record_error(bvhgpu_ctx* ctx, int code, const char* msg) { return fail(ctx, code, "%s", msg); }
+
+namespace {
+
 int cuda_fail(bvhgpu_ctx* ctx, cudaError_t e, const char* what) {
     return fail(ctx, BVHGPU_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
 }

@@ -143,14 +143,67 @@ __device__ __forceinline__ void test_leaf_lane(const float4* __restrict__ tris, 
     }
 }
 
-template <int STACK>
-struct Trav {
-    uint2 stack[STACK];
+// ---- traversal stacks -------------------------------------------------------------------------
+// An entry is a pending far child, (count, first) of its node.
+//
+// SplitStack: the newest RK entries live in registers as a shift register (every index is a
+// compile-time constant, so nothing goes to local memory); older entries spill to this thread's
+// column of a shared-memory array (entry k at col[k * blockDim.x]: consecutive lanes hit
+// consecutive 8-byte words, no bank conflicts).  A kernel using it takes
+// kSharedEntries * 8 * blockDim.x bytes of dynamic shared memory and calls bind() once.
+template <int RK, int SK>
+struct SplitStack {
+    static_assert(RK >= 1, "at least one register entry");
+    static constexpr int kCap = RK + SK;
+    static constexpr int kSharedEntries = SK;
+    uint2 reg[RK];
+    uint2* col;
     int sp;
+
+    __device__ __forceinline__ void bind(uint2* smem) { col = smem + threadIdx.x; }
+    __device__ __forceinline__ void clear() { sp = 0; }
+    __device__ __forceinline__ bool empty() const { return sp == 0; }
+    __device__ __forceinline__ bool full() const { return sp >= kCap; }
+    __device__ __forceinline__ void push(uint2 e) {
+        if (SK > 0 && sp >= RK) col[(sp - RK) * blockDim.x] = reg[RK - 1];
+#pragma unroll
+        for (int k = RK - 1; k > 0; --k) reg[k] = reg[k - 1];
+        reg[0] = e;
+        ++sp;
+    }
+    __device__ __forceinline__ uint2 pop() {
+        const uint2 e = reg[0];
+#pragma unroll
+        for (int k = 0; k < RK - 1; ++k) reg[k] = reg[k + 1];
+        if (SK > 0 && sp > RK) reg[RK - 1] = col[(sp - RK - 1) * blockDim.x];
+        --sp;
+        return e;
+    }
+};
+
+// LocalStack: a plain per-thread array (local memory, cached in L1), for the rare deep trees.
+template <int N>
+struct LocalStack {
+    static constexpr int kCap = N;
+    static constexpr int kSharedEntries = 0;
+    uint2 s[N];
+    int sp;
+
+    __device__ __forceinline__ void bind(uint2*) {}
+    __device__ __forceinline__ void clear() { sp = 0; }
+    __device__ __forceinline__ bool empty() const { return sp == 0; }
+    __device__ __forceinline__ bool full() const { return sp >= N; }
+    __device__ __forceinline__ void push(uint2 e) { s[sp++] = e; }
+    __device__ __forceinline__ uint2 pop() { return s[--sp]; }
+};
+
+template <class STK>
+struct TravT {
+    STK stk;
     uint32_t cnt, first, steps, max_steps;
 
     __device__ __forceinline__ void init(const GBlas& b) {
-        sp = 0;
+        stk.clear();
         cnt = b.root_count;
         first = b.root_first;
         steps = 0;
@@ -158,10 +211,10 @@ struct Trav {
     }
 
     __device__ __forceinline__ bool pop() {
-        if (sp == 0) return true;
-        --sp;
-        cnt = stack[sp].x;
-        first = stack[sp].y;
+        if (stk.empty()) return true;
+        const uint2 e = stk.pop();
+        cnt = e.x;
+        first = e.y;
         return false;
     }
 
@@ -193,11 +246,11 @@ struct Trav {
         bool far_hit = left_near ? hr : hl;
         if (near_hit) {
             if (far_hit) {
-                if (sp >= STACK) {
+                if (stk.full()) {
                     atomicOr(err, kErrStack);
                     return kStepFinished;
                 }
-                stack[sp++] = left_near ? make_uint2(ubits(r1.w), ubits(r0.w)) : make_uint2(ubits(l1.w), ubits(l0.w));
+                stk.push(left_near ? make_uint2(ubits(r1.w), ubits(r0.w)) : make_uint2(ubits(l1.w), ubits(l0.w)));
             }
             cnt = left_near ? ubits(l1.w) : ubits(r1.w);
             first = left_near ? ubits(l0.w) : ubits(r0.w);
@@ -214,6 +267,10 @@ struct Trav {
         }
     }
 };
+
+// The local-memory traversal used where no tuned variant applies (render, adjoint).
+template <int STACK>
+using Trav = TravT<LocalStack<STACK>>;
 
 // Whole traversal by one lane, every leaf tested by the lane itself.
 template <int STACK>

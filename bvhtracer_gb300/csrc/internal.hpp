@@ -107,6 +107,15 @@ struct bvhgpu_ctx {
     bool profiling = false;
     std::vector<bvhgpu::ProfileRec> prof;
     std::vector<cudaEvent_t> event_pool;
+    // launch configuration per kernel id (only the tunable kernels read theirs)
+    bvhgpu_tune_config tune[BVHGPU_KERNEL_COUNT];
+    bvhgpu_ctx() {
+        // defaults: the configs the autotuner picked on GB300 for the displaced-icosphere frame
+        // (single BLAS) and the instanced frame (two-level)
+        for (auto& t : tune) t = bvhgpu_tune_config{128u, 5u, 0u, 16u, 1u, 0u};
+        tune[BVHGPU_K_TRACE_SCENE] = bvhgpu_tune_config{64u, 1u, 256u, 16u, 1u, 0u};
+        tune[BVHGPU_K_SCENE_BOUNCE] = bvhgpu_tune_config{64u, 1u, 256u, 16u, 8u, 0u};
+    }
 };
 
 namespace bvhgpu {
@@ -140,6 +149,8 @@ cudaError_t launch_render(bvhgpu_ctx* ctx, const DeviceBlas& b, const bvhgpu_cam
 // ---- launchers (kernels_scene.cu) ------------------------------------------------------
 cudaError_t launch_write_tris(bvhgpu_ctx* ctx, DeviceBlas& b, const float* d_tris9, cudaStream_t s);
 cudaError_t launch_refit(bvhgpu_ctx* ctx, DeviceBlas& b, cudaStream_t s);
+// Sets ctx->last_error to msg and returns code (the ABI's error path).
+int record_error(bvhgpu_ctx* ctx, int code, const char* msg);
 constexpr uint32_t kMaxSceneObjects = 4096;  // TLAS rebuild shared memory: 40 B per object
 cudaError_t launch_tlas_rebuild(bvhgpu_ctx* ctx, DeviceScene& sc, cudaStream_t s);
 cudaError_t launch_trace_scene(bvhgpu_ctx* ctx, DeviceScene& sc, const float4* rays, uint32_t n, void* hits,

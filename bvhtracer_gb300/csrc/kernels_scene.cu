@@ -14,6 +14,7 @@
 
 #include "common.cuh"
 #include "internal.hpp"
+#include "variants.cuh"
 
 namespace bvhgpu {
 namespace {
@@ -449,9 +450,9 @@ struct SceneData {
     uint32_t tlas_nodes;
 };
 
-template <int STACK, int TSTACK>
+template <class STK, int TSTACK>
 struct SceneTrav {
-    Trav<STACK> bt;
+    TravT<STK> bt;
     GBlas blas;
     uint2 tstack[TSTACK];  // pending far TLAS nodes: (left_right, blas)
     int tsp;
@@ -555,8 +556,8 @@ struct SceneTrav {
 };
 
 // Cooperative phase of the two-level traversal (same grouping as the single-BLAS kernels).
-template <int STACK, int TSTACK>
-__device__ __forceinline__ void scene_coop_phase(unsigned pend, SceneTrav<STACK, TSTACK>& tr, LaneRay& r,
+template <class STK, int TSTACK>
+__device__ __forceinline__ void scene_coop_phase(unsigned pend, SceneTrav<STK, TSTACK>& tr, LaneRay& r,
                                                  StepResult& st) {
     const unsigned lane = threadIdx.x & 31u;
     const unsigned long long key = reinterpret_cast<unsigned long long>(tr.blas.pairs);
@@ -584,16 +585,19 @@ __device__ __forceinline__ void scene_coop_phase(unsigned pend, SceneTrav<STACK,
     }
 }
 
-constexpr uint32_t kBigLeaf = 16;
+constexpr int kTlasStack = 64;
 
-template <int STACK, int TSTACK>
-__global__ void __launch_bounds__(kBlock) k_trace_scene(SceneData sd, const float4* __restrict__ rays, uint32_t n,
-                                                        GHit* __restrict__ hits, uint32_t* err) {
+template <int BLOCK, int MINB, class STK>
+__global__ void __launch_bounds__(BLOCK, MINB) k_trace_scene(SceneData sd, const float4* __restrict__ rays,
+                                                             uint32_t n, GHit* __restrict__ hits, uint32_t big_leaf,
+                                                             uint32_t* err) {
+    extern __shared__ uint2 stack_smem[];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (__all_sync(kFull, i >= n)) return;
     const bool active = i < n;
     LaneRay r;
-    SceneTrav<STACK, TSTACK> tr;
+    SceneTrav<STK, kTlasStack> tr;
+    tr.bt.stk.bind(stack_smem);
     StepResult st = kStepFinished;
     if (active) {
         float3 o, d;
@@ -611,7 +615,7 @@ __global__ void __launch_bounds__(kBlock) k_trace_scene(SceneData sd, const floa
         st = kStepContinue;
     }
     for (;;) {
-        if (st == kStepContinue) st = tr.advance(sd, r, kBigLeaf, err);
+        if (st == kStepContinue) st = tr.advance(sd, r, big_leaf, err);
         const unsigned pend = __ballot_sync(kFull, st == kStepBigLeaf);
         if (pend == 0u) break;
         scene_coop_phase(pend, tr, r, st);
@@ -621,21 +625,26 @@ __global__ void __launch_bounds__(kBlock) k_trace_scene(SceneData sd, const floa
 
 // Persistent primary + bounce over a scene (the instanced frame): idle lanes are refilled from
 // the queue; a primary that hits continues in its lane with the bounce ray of its hit.
-template <int STACK, int TSTACK>
-__global__ void __launch_bounds__(kBlock) k_scene_persistent_bounce(SceneData sd, const float4* __restrict__ rays,
-                                                                    uint32_t n, uint32_t seed,
-                                                                    GHit* __restrict__ hits0, GHit* __restrict__ hits1,
-                                                                    uint32_t* queue, uint32_t* err) {
+template <int BLOCK, int MINB, class STK>
+__global__ void __launch_bounds__(BLOCK, MINB) k_scene_persistent_bounce(SceneData sd, const float4* __restrict__ rays,
+                                                                         uint32_t n, uint32_t seed,
+                                                                         GHit* __restrict__ hits0,
+                                                                         GHit* __restrict__ hits1, uint32_t* queue,
+                                                                         uint32_t big_leaf, uint32_t refill,
+                                                                         uint32_t* err) {
+    extern __shared__ uint2 stack_smem[];
     const unsigned lane = threadIdx.x & 31u;
     int phase = 0;  // 0 needs work, 1 primary, 2 bounce, 3 retired
     uint32_t idx = 0;
     LaneRay r;
-    SceneTrav<STACK, TSTACK> tr;
+    SceneTrav<STK, kTlasStack> tr;
+    tr.bt.stk.bind(stack_smem);
     StepResult st = kStepFinished;
     bool queue_open = true;
     for (;;) {
         const unsigned need = __ballot_sync(kFull, phase == 0);
-        if (need != 0u) {
+        const unsigned busy = __ballot_sync(kFull, phase == 1 || phase == 2);
+        if (need != 0u && ((uint32_t)__popc(need) >= refill || busy == 0u)) {
             const int leader = __ffs(need) - 1;
             uint32_t base = 0;
             if ((int)lane == leader) base = atomicAdd(queue, (uint32_t)__popc(need));
@@ -665,7 +674,7 @@ __global__ void __launch_bounds__(kBlock) k_scene_persistent_bounce(SceneData sd
             }
         }
         while (phase == 1 || phase == 2) {
-            if (st == kStepContinue) st = tr.advance(sd, r, kBigLeaf, err);
+            if (st == kStepContinue) st = tr.advance(sd, r, big_leaf, err);
             if (st != kStepFinished) break;
             const bool h = r.hit && r.ct < FLT_MAX;
             if (phase == 2) {
@@ -843,16 +852,17 @@ cudaError_t launch_trace_scene(bvhgpu_ctx* ctx, DeviceScene& sc, const float4* r
     uint32_t depth = 1;
     SceneData sd = scene_data(ctx, sc, &depth);
     LaunchScope scope(ctx, BVHGPU_K_TRACE_SCENE, s);
-    GHit* h = static_cast<GHit*>(hits);
-    const unsigned grid = grid_for(n, kBlock);
-    if (depth <= 33)
-        k_trace_scene<32, 64><<<grid, kBlock, 0, s>>>(sd, rays, n, h, ctx->d_err);
-    else if (depth <= 65)
-        k_trace_scene<64, 64><<<grid, kBlock, 0, s>>>(sd, rays, n, h, ctx->d_err);
-    else
-        k_trace_scene<256, 64><<<grid, kBlock, 0, s>>>(sd, rays, n, h, ctx->d_err);
+    const Variant v = resolve(ctx->tune[BVHGPU_K_TRACE_SCENE], depth);
+    cudaError_t e = with_variant(v.shape, v.stack, [&](auto sh, auto tg) {
+        using SH = decltype(sh);
+        using STK = typename decltype(tg)::type;
+        k_trace_scene<SH::block, SH::minb, STK><<<grid_for(n, SH::block), SH::block,
+                                                  stack_smem_bytes<STK>(SH::block), s>>>(
+            sd, rays, n, static_cast<GHit*>(hits), v.big_leaf, ctx->d_err);
+        return cudaGetLastError();
+    });
     g_launches++;
-    return cudaGetLastError();
+    return e;
 }
 
 cudaError_t launch_scene_bounce(bvhgpu_ctx* ctx, DeviceScene& sc, const float4* rays, uint32_t n, uint32_t seed,
@@ -864,24 +874,21 @@ cudaError_t launch_scene_bounce(bvhgpu_ctx* ctx, DeviceScene& sc, const float4* 
     cudaError_t e = cudaMemsetAsync(queue, 0, sizeof(uint32_t), s);
     if (e != cudaSuccess) return e;
     LaunchScope scope(ctx, BVHGPU_K_SCENE_BOUNCE, s);
-    GHit* h0 = static_cast<GHit*>(hits0);
-    GHit* h1 = static_cast<GHit*>(hits1);
-    int per_sm = 0;
-    if (depth <= 33) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_scene_persistent_bounce<32, 64>, kBlock, 0);
-        k_scene_persistent_bounce<32, 64><<<std::max(1, per_sm) * ctx->num_sms, kBlock, 0, s>>>(
-            sd, rays, n, seed, h0, h1, queue, ctx->d_err);
-    } else if (depth <= 65) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_scene_persistent_bounce<64, 64>, kBlock, 0);
-        k_scene_persistent_bounce<64, 64><<<std::max(1, per_sm) * ctx->num_sms, kBlock, 0, s>>>(
-            sd, rays, n, seed, h0, h1, queue, ctx->d_err);
-    } else {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_scene_persistent_bounce<256, 64>, kBlock, 0);
-        k_scene_persistent_bounce<256, 64><<<std::max(1, per_sm) * ctx->num_sms, kBlock, 0, s>>>(
-            sd, rays, n, seed, h0, h1, queue, ctx->d_err);
-    }
+    const Variant v = resolve(ctx->tune[BVHGPU_K_SCENE_BOUNCE], depth);
+    e = with_variant(v.shape, v.stack, [&](auto sh, auto tg) {
+        using SH = decltype(sh);
+        using STK = typename decltype(tg)::type;
+        auto* k = k_scene_persistent_bounce<SH::block, SH::minb, STK>;
+        const size_t smem = stack_smem_bytes<STK>(SH::block);
+        int per_sm = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, SH::block, smem);
+        k<<<std::max(1, per_sm) * ctx->num_sms, SH::block, smem, s>>>(sd, rays, n, seed, static_cast<GHit*>(hits0),
+                                                                     static_cast<GHit*>(hits1), queue, v.big_leaf,
+                                                                     v.refill, ctx->d_err);
+        return cudaGetLastError();
+    });
     g_launches++;
-    return cudaGetLastError();
+    return e;
 }
 
 cudaError_t launch_scene_bounce_rays(bvhgpu_ctx* ctx, DeviceScene& sc, const float4* rays, const void* hits0,

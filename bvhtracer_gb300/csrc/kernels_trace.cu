@@ -14,6 +14,7 @@
 
 #include "common.cuh"
 #include "internal.hpp"
+#include "variants.cuh"
 
 namespace bvhgpu {
 
@@ -57,8 +58,8 @@ inline unsigned grid_for(uint32_t n, int block) { return (unsigned)((n + block -
 // tested two at a time (coop_leaf2 shares each loaded triangle pair between the two rays), an
 // odd one alone.  `key` identifies the BLAS (pairs pointer) so that different scenes of a batch
 // never share a leaf.
-template <int STACK>
-__device__ __forceinline__ void coop_leaf_phase(unsigned pend, const ulonglong2* pairs, Trav<STACK>& tr, LaneRay& r,
+template <class TR>
+__device__ __forceinline__ void coop_leaf_phase(unsigned pend, const ulonglong2* pairs, TR& tr, LaneRay& r,
                                                 StepResult& st) {
     const unsigned lane = threadIdx.x & 31u;
     const unsigned long long key = reinterpret_cast<unsigned long long>(pairs);
@@ -87,17 +88,18 @@ __device__ __forceinline__ void coop_leaf_phase(unsigned pend, const ulonglong2*
 }
 
 // Traces the rays of one warp (inactive lanes take part in the cooperative steps only).
-template <int STACK>
-__device__ __forceinline__ void warp_trace(const GBlas& b, bool active, LaneRay& r, uint32_t big_leaf,
-                                           uint32_t* err) {
-    Trav<STACK> tr;
+template <class STK>
+__device__ __forceinline__ void warp_trace(const GBlas& b, bool active, LaneRay& r, uint32_t big_leaf, uint32_t* err,
+                                           uint2* stack_smem) {
+    TravT<STK> tr;
+    tr.stk.bind(stack_smem);
     if (active) tr.init(b);
     StepResult st = active ? kStepContinue : kStepFinished;
     for (;;) {
         if (st == kStepContinue) st = tr.advance(b, r, big_leaf, err);
         unsigned pend = __ballot_sync(kFull, st == kStepBigLeaf);
         if (pend == 0u) break;
-        coop_leaf_phase<STACK>(pend, b.pairs, tr, r, st);
+        coop_leaf_phase(pend, b.pairs, tr, r, st);
     }
 }
 
@@ -115,10 +117,13 @@ __device__ __forceinline__ void init_lane_ray(LaneRay& r, float3 o, float3 d, fl
 
 // One thread per ray.  `count` (device, may be null) overrides n; `out_index` (may be null)
 // maps ray i to its hit slot (the compacted bounce queue writes hits at pixel positions).
-template <int STACK>
-__global__ void __launch_bounds__(kBlock) k_trace_blas(GBlas b, const float4* __restrict__ rays, uint32_t n,
-                                                       const uint32_t* count, const uint32_t* __restrict__ out_index,
-                                                       GHit* __restrict__ hits, uint32_t big_leaf, uint32_t* err) {
+template <int BLOCK, int MINB, class STK>
+__global__ void __launch_bounds__(BLOCK, MINB) k_trace_blas(GBlas b, const float4* __restrict__ rays, uint32_t n,
+                                                            const uint32_t* count,
+                                                            const uint32_t* __restrict__ out_index,
+                                                            GHit* __restrict__ hits, uint32_t big_leaf,
+                                                            uint32_t* err) {
+    extern __shared__ uint2 stack_smem[];
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (count) n = *count;
     if (__all_sync(kFull, i >= n)) return;  // whole warp idle
@@ -130,7 +135,7 @@ __global__ void __launch_bounds__(kBlock) k_trace_blas(GBlas b, const float4* __
         load_ray(rays, i, o, d, t);
         init_lane_ray(r, o, d, t);
     }
-    warp_trace<STACK>(b, active, r, big_leaf, err);
+    warp_trace<STK>(b, active, r, big_leaf, err, stack_smem);
     // bvh.rs:295: a hit needs closest_ray.t < f32::MAX as well.
     if (active) store_hit(hits, out_index ? out_index[i] : i, r.hit && r.ct < FLT_MAX, r.ct, r.hu, r.hv, r.hp, 0u);
 }
@@ -195,21 +200,26 @@ __global__ void k_bounce_rays(GBlas b, const float4* __restrict__ rays, const GH
 // (ballot -> one atomicAdd per warp -> shfl); a primary that hit continues in the same slot
 // with its bounce ray, so no compaction pass and no second launch are needed.
 
-template <int STACK>
-__global__ void __launch_bounds__(kBlock) k_persistent_bounce(GBlas b, const float4* __restrict__ rays, uint32_t n,
-                                                              uint32_t seed, GHit* __restrict__ hits0,
-                                                              GHit* __restrict__ hits1, uint32_t* queue,
-                                                              uint32_t big_leaf, uint32_t* err) {
+template <int BLOCK, int MINB, class STK>
+__global__ void __launch_bounds__(BLOCK, MINB) k_persistent_bounce(GBlas b, const float4* __restrict__ rays,
+                                                                   uint32_t n, uint32_t seed,
+                                                                   GHit* __restrict__ hits0, GHit* __restrict__ hits1,
+                                                                   uint32_t* queue, uint32_t big_leaf, uint32_t refill,
+                                                                   uint32_t* err) {
+    extern __shared__ uint2 stack_smem[];
     const unsigned lane = threadIdx.x & 31u;
     int phase = 0;  // 0 needs work, 1 primary ray, 2 bounce ray, 3 retired
     uint32_t idx = 0;
     LaneRay r;
-    Trav<STACK> tr;
+    TravT<STK> tr;
+    tr.stk.bind(stack_smem);
     StepResult st = kStepFinished;
     bool queue_open = true;
     for (;;) {
-        unsigned need = __ballot_sync(kFull, phase == 0);
-        if (need != 0u) {
+        const unsigned need = __ballot_sync(kFull, phase == 0);
+        const unsigned busy = __ballot_sync(kFull, phase == 1 || phase == 2);
+        // refill once `refill` lanes are idle (or none is busy)
+        if (need != 0u && ((uint32_t)__popc(need) >= refill || busy == 0u)) {
             int leader = __ffs(need) - 1;
             uint32_t base = 0;
             if ((int)lane == leader) base = atomicAdd(queue, (uint32_t)__popc(need));
@@ -263,7 +273,7 @@ __global__ void __launch_bounds__(kBlock) k_persistent_bounce(GBlas b, const flo
             if (!queue_open && __ballot_sync(kFull, phase == 0 || phase == 1 || phase == 2) == 0u) break;
             continue;
         }
-        coop_leaf_phase<STACK>(pend, b.pairs, tr, r, st);
+        coop_leaf_phase(pend, b.pairs, tr, r, st);
     }
 }
 
@@ -276,12 +286,14 @@ struct BatchEntry {
     uint32_t pad0, pad1;
 };
 
-template <int STACK>
-__global__ void __launch_bounds__(kBlock) k_trace_batch_persistent(const BatchEntry* __restrict__ table,
-                                                                   uint32_t nitems, uint32_t total,
-                                                                   const float4* __restrict__ rays,
-                                                                   GHit* __restrict__ hits, uint32_t* queue,
-                                                                   uint32_t big_leaf, uint32_t* err) {
+template <int BLOCK, int MINB, class STK>
+__global__ void __launch_bounds__(BLOCK, MINB) k_trace_batch_persistent(const BatchEntry* __restrict__ table,
+                                                                        uint32_t nitems, uint32_t total,
+                                                                        const float4* __restrict__ rays,
+                                                                        GHit* __restrict__ hits, uint32_t* queue,
+                                                                        uint32_t big_leaf, uint32_t refill,
+                                                                        uint32_t* err) {
+    extern __shared__ uint2 stack_smem[];
     const unsigned lane = threadIdx.x & 31u;
     int phase = 0;  // 0 needs work, 1 tracing, 3 retired
     uint32_t ray = 0;
@@ -291,12 +303,14 @@ __global__ void __launch_bounds__(kBlock) k_trace_batch_persistent(const BatchEn
     b.pairs = nullptr;
     b.nodes_used = b.ntris = b.root_count = b.root_first = 0;
     LaneRay r;
-    Trav<STACK> tr;
+    TravT<STK> tr;
+    tr.stk.bind(stack_smem);
     StepResult st = kStepFinished;
     bool queue_open = true;
     for (;;) {
-        unsigned need = __ballot_sync(kFull, phase == 0);
-        if (need != 0u) {
+        const unsigned need = __ballot_sync(kFull, phase == 0);
+        const unsigned busy = __ballot_sync(kFull, phase == 1);
+        if (need != 0u && ((uint32_t)__popc(need) >= refill || busy == 0u)) {
             int leader = __ffs(need) - 1;
             uint32_t base = 0;
             if ((int)lane == leader) base = atomicAdd(queue, (uint32_t)__popc(need));
@@ -336,7 +350,7 @@ __global__ void __launch_bounds__(kBlock) k_trace_batch_persistent(const BatchEn
             if (!queue_open && __ballot_sync(kFull, phase == 0 || phase == 1) == 0u) break;
             continue;
         }
-        coop_leaf_phase<STACK>(pend, b.pairs, tr, r, st);
+        coop_leaf_phase(pend, b.pairs, tr, r, st);
     }
 }
 
@@ -403,7 +417,7 @@ __global__ void __launch_bounds__(64) k_render(GBlas b, RenderParams P, const fl
     float3 d = xf_vector(C + 9, dir);
     LaneRay lr;
     init_lane_ray(lr, o, d, FLT_MAX);
-    warp_trace<STACK>(b, active, lr, big_leaf, err);
+    warp_trace<LocalStack<STACK>>(b, active, lr, big_leaf, err, nullptr);
     if (!active) return;
     const float t = lr.ct, hu = lr.hu, hv = lr.hv;
     const uint32_t hp = lr.hp;
@@ -464,9 +478,10 @@ __global__ void __launch_bounds__(64) k_render(GBlas b, RenderParams P, const fl
     reinterpret_cast<uchar4*>(rgba)[(size_t)y * P.width + x] = c;
 }
 
-int persistent_grid(bvhgpu_ctx* ctx, const void* kernel) {
+template <class K>
+int persistent_grid(bvhgpu_ctx* ctx, K kernel, int block, size_t smem) {
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, smem);
     if (per_sm < 1) per_sm = 1;
     return per_sm * ctx->num_sms;
 }
@@ -481,15 +496,29 @@ int persistent_grid(bvhgpu_ctx* ctx, const void* kernel) {
         default: { constexpr int S = 256; __VA_ARGS__; break; }   \
     }
 
+// Plain one-thread-per-ray launch; `count` (device) and `out_index` as in k_trace_blas.
+static cudaError_t trace_blas_variant(bvhgpu_ctx* ctx, const Variant& v, const GBlas& g, const float4* rays,
+                                      uint32_t n, const uint32_t* count, const uint32_t* out_index, GHit* hits,
+                                      cudaStream_t s) {
+    return with_variant(v.shape, v.stack, [&](auto sh, auto tg) {
+        using SH = decltype(sh);
+        using STK = typename decltype(tg)::type;
+        k_trace_blas<SH::block, SH::minb, STK><<<grid_for(n, SH::block), SH::block,
+                                                 stack_smem_bytes<STK>(SH::block), s>>>(g, rays, n, count, out_index,
+                                                                                       hits, v.big_leaf, ctx->d_err);
+        return cudaGetLastError();
+    });
+}
+
 cudaError_t launch_trace_blas(bvhgpu_ctx* ctx, const DeviceBlas& b, const float4* rays, uint32_t n, void* hits,
                               cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     GBlas g = to_gblas(b);
     LaunchScope scope(ctx, BVHGPU_K_TRACE_BLAS, s);
-    BVHGPU_DISPATCH_STACK(b.depth, (k_trace_blas<S><<<grid_for(n, kBlock), kBlock, 0, s>>>(
-                                       g, rays, n, nullptr, nullptr, static_cast<GHit*>(hits), kBigLeaf, ctx->d_err)));
+    const Variant v = resolve(ctx->tune[BVHGPU_K_TRACE_BLAS], b.depth);
+    cudaError_t e = trace_blas_variant(ctx, v, g, rays, n, nullptr, nullptr, static_cast<GHit*>(hits), s);
     g_launches++;
-    return cudaGetLastError();
+    return e;
 }
 
 cudaError_t launch_bounce_plain(bvhgpu_ctx* ctx, const DeviceBlas& b, const float4* rays, uint32_t n, uint32_t seed,
@@ -512,12 +541,12 @@ cudaError_t launch_bounce_plain(bvhgpu_ctx* ctx, const DeviceBlas& b, const floa
     if (e != cudaSuccess) return e;
     {
         LaunchScope scope(ctx, BVHGPU_K_TRACE_QUEUE, s);
-        BVHGPU_DISPATCH_STACK(b.depth, (k_trace_blas<S><<<grid_for(n, kBlock), kBlock, 0, s>>>(
-                                           g, static_cast<const float4*>(ctx->bounce_rays), n, qcount, ctx->bounce_pix,
-                                           static_cast<GHit*>(hits1), kBigLeaf, ctx->d_err)));
+        const Variant v = resolve(ctx->tune[BVHGPU_K_TRACE_BLAS], b.depth);
+        e = trace_blas_variant(ctx, v, g, static_cast<const float4*>(ctx->bounce_rays), n, qcount, ctx->bounce_pix,
+                               static_cast<GHit*>(hits1), s);
         g_launches++;
     }
-    return cudaGetLastError();
+    return e;
 }
 
 cudaError_t launch_bounce_persistent(bvhgpu_ctx* ctx, const DeviceBlas& b, const float4* rays, uint32_t n,
@@ -528,13 +557,19 @@ cudaError_t launch_bounce_persistent(bvhgpu_ctx* ctx, const DeviceBlas& b, const
     if (e != cudaSuccess) return e;
     GBlas g = to_gblas(b);
     LaunchScope scope(ctx, BVHGPU_K_PERSISTENT_BOUNCE, s);
-    BVHGPU_DISPATCH_STACK(b.depth, {
-        int grid = persistent_grid(ctx, (const void*)k_persistent_bounce<S>);
-        k_persistent_bounce<S><<<grid, kBlock, 0, s>>>(g, rays, n, seed, static_cast<GHit*>(hits0),
-                                                         static_cast<GHit*>(hits1), queue, kBigLeaf, ctx->d_err);
+    const Variant v = resolve(ctx->tune[BVHGPU_K_PERSISTENT_BOUNCE], b.depth);
+    e = with_variant(v.shape, v.stack, [&](auto sh, auto tg) {
+        using SH = decltype(sh);
+        using STK = typename decltype(tg)::type;
+        auto* k = k_persistent_bounce<SH::block, SH::minb, STK>;
+        const size_t smem = stack_smem_bytes<STK>(SH::block);
+        k<<<persistent_grid(ctx, k, SH::block, smem), SH::block, smem, s>>>(
+            g, rays, n, seed, static_cast<GHit*>(hits0), static_cast<GHit*>(hits1), queue, v.big_leaf, v.refill,
+            ctx->d_err);
+        return cudaGetLastError();
     });
     g_launches++;
-    return cudaGetLastError();
+    return e;
 }
 
 cudaError_t launch_bounce_rays(bvhgpu_ctx* ctx, const DeviceBlas& b, const float4* rays, const void* hits0,
@@ -602,14 +637,19 @@ cudaError_t launch_trace_batch(bvhgpu_ctx* ctx, const std::vector<const DeviceBl
     if (e != cudaSuccess) return e;
     const uint32_t total = ctx->batch_total;
     LaunchScope scope(ctx, BVHGPU_K_TRACE_BATCH, s);
-    BVHGPU_DISPATCH_STACK(ctx->batch_depth, {
-        int grid = persistent_grid(ctx, (const void*)k_trace_batch_persistent<S>);
-        k_trace_batch_persistent<S><<<grid, kBlock, 0, s>>>(static_cast<const BatchEntry*>(ctx->batch_table), nitems,
-                                                            total, rays, static_cast<GHit*>(hits), queue, kBigLeaf,
-                                                            ctx->d_err);
+    const Variant v = resolve(ctx->tune[BVHGPU_K_TRACE_BATCH], ctx->batch_depth);
+    e = with_variant(v.shape, v.stack, [&](auto sh, auto tg) {
+        using SH = decltype(sh);
+        using STK = typename decltype(tg)::type;
+        auto* k = k_trace_batch_persistent<SH::block, SH::minb, STK>;
+        const size_t smem = stack_smem_bytes<STK>(SH::block);
+        k<<<persistent_grid(ctx, k, SH::block, smem), SH::block, smem, s>>>(
+            static_cast<const BatchEntry*>(ctx->batch_table), nitems, total, rays, static_cast<GHit*>(hits), queue,
+            v.big_leaf, v.refill, ctx->d_err);
+        return cudaGetLastError();
     });
     g_launches++;
-    return cudaGetLastError();
+    return e;
 }
 
 cudaError_t launch_render(bvhgpu_ctx* ctx, const DeviceBlas& b, const bvhgpu_camera& cam, int w, int h, int acc,

@@ -313,6 +313,66 @@ int bvhgpu_lambert_adjoint_async(bvhgpu_ctx* ctx, uint32_t mesh_id, const bvhgpu
  * bvhgpu_mesh_update_async before the next forward). */
 int bvhgpu_mesh_sgd_step_async(bvhgpu_ctx* ctx, uint32_t mesh_id, float* d_grad, float lr, bvhgpu_stream s);
 
+/* ---- launch configuration and autotuning (not in the reference) ------------------------------ */
+/* The traversal kernels BVHGPU_K_TRACE_BLAS (also the bounce pass of BVHGPU_MODE_PLAIN and the
+ * per-scene launches of a plain batch), BVHGPU_K_TRACE_SCENE, BVHGPU_K_PERSISTENT_BOUNCE,
+ * BVHGPU_K_TRACE_BATCH and BVHGPU_K_SCENE_BOUNCE are compiled in several variants, and a context
+ * holds one config per kernel.  Every config gives bit-identical results; it only changes speed. */
+#define BVHGPU_BIG_LEAF_NEVER 0xFFFFFFFFu
+typedef struct bvhgpu_tune_config {
+    /* launch shape: threads per block and the blocks per SM that __launch_bounds__ sizes the
+     * register budget for (65536 / (block * min_blocks) registers per thread).  Compiled shapes:
+     * (128, 1), (128, 5), (128, 6), (128, 8), (64, 1). */
+    uint32_t block;
+    uint32_t min_blocks;
+    /* traversal stack entries per ray: 8 or 32 (the newest 4 in registers, the rest in shared
+     * memory) or 256 (local memory).  0, or fewer than the tree needs: the smallest that holds it. */
+    uint32_t stack;
+    /* leaf layout: a leaf with more triangles than this is tested by the whole warp on the paired
+     * f32x2 triangle layout, smaller ones by their own lane on the float4 layout;
+     * BVHGPU_BIG_LEAF_NEVER = every leaf by its lane. */
+    uint32_t big_leaf;
+    /* ray batch of the persistent kernels: a warp fetches new rays once this many of its lanes
+     * are idle (1..32; a warp whose lanes are all idle always fetches). */
+    uint32_t refill;
+    uint32_t reserved; /* 0 */
+} bvhgpu_tune_config;
+/* Defaults: block 128, min_blocks 5, stack 0, big_leaf 16, refill 1; for the two-level kernels
+ * (TRACE_SCENE, SCENE_BOUNCE) block 64, min_blocks 1, stack 256, refill 1 / 8. */
+int bvhgpu_tune_get(bvhgpu_ctx* ctx, int kernel, bvhgpu_tune_config* out);
+/* BVHGPU_ERR_INVALID_ARG for a kernel that is not tunable or a shape / stack not compiled. */
+int bvhgpu_tune_set(bvhgpu_ctx* ctx, int kernel, const bvhgpu_tune_config* cfg);
+/* The candidate values the tuner searches, as a list of configs (cap entries at most; *count
+ * gets the full number): every compiled shape x stack, big_leaf in {8, 16, 32, 64, NEVER} and
+ * refill in {1, 8, 16} (refill only for the persistent kernels). */
+int bvhgpu_tune_space(int kernel, bvhgpu_tune_config* out, uint32_t cap, uint32_t* count);
+
+/* One call for the tuner to time: the fields a kernel needs, others 0 / NULL.
+ *   TRACE_BLAS:        target = BLAS id, d_rays, n, d_hits0 (bvhgpu_blas_intersect_async); or,
+ *                      with nitems > 0, the plain batch of `items` (one launch per item)
+ *   PERSISTENT_BOUNCE: target = BLAS id, d_rays, n, seed, d_hits0, d_hits1
+ *   TRACE_SCENE:       target = scene id, d_rays, n, d_hits0
+ *   SCENE_BOUNCE:      target = scene id, d_rays, n, seed, d_hits0, d_hits1
+ *   TRACE_BATCH:       items, nitems, d_rays, n (= total rays), d_hits0 */
+typedef struct bvhgpu_tune_job {
+    int kernel;
+    uint32_t target;
+    const bvhgpu_ray* d_rays;
+    uint32_t n;
+    uint32_t seed;
+    bvhgpu_hit* d_hits0;
+    bvhgpu_hit* d_hits1;
+    const bvhgpu_batch_item* items;
+    uint32_t nitems;
+} bvhgpu_tune_job;
+/* Times the job under candidate configs -- a coordinate search from the current config over
+ * launch shape, stack, big_leaf and refill, two sweeps; each candidate runs once untimed, then
+ * `reps` times bracketed by events on the context's stream (median kept) -- stores the fastest
+ * in the context and returns it with its ms per call (either pointer may be NULL).  The job's
+ * outputs are overwritten.  Synchronous; not allowed during graph capture. */
+int bvhgpu_autotune(bvhgpu_ctx* ctx, const bvhgpu_tune_job* job, uint32_t reps, bvhgpu_tune_config* best,
+                    float* best_ms);
+
 /* ---- refit without allocation ----------------------------------------------------------------- */
 /* No counterpart in the reference.  For callers that cannot call cudaMalloc: engines that own all
  * device memory through a pool reserved at start-up, or latency-critical threads on which a driver
