@@ -45,6 +45,7 @@ ERRORS = {1: "invalid argument", 2: "out of memory", 3: "CUDA error", 4: "stack 
 ACC_INTERSECTION, ACC_DEPTH, ACC_UV, ACC_NORMAL = 0, 1, 2, 3
 SHADER_RADIANCE, SHADER_INTERSECTION, SHADER_DEPTH = 0, 1, 2
 MODE_PLAIN, MODE_PERSISTENT = 0, 1
+LIST_CLOSEST, LIST_MUT = 0, 1
 
 KERNELS = ["trace_blas", "trace_scene", "persistent_bounce", "bounce_gen", "trace_queue", "trace_batch",
            "refit", "tlas_build", "render", "other", "lambert_forward", "lambert_adjoint", "scene_bounce"]
@@ -121,6 +122,8 @@ SIGNATURES = {
     "bvhgpu_mse_loss": (_I, [_P, _P, _P, _U32, _P]),
     "bvhgpu_lambert_adjoint_async": (_I, [_P, _U32, _P, _U32, _P, _P, _P, _P, _P, _P]),
     "bvhgpu_mesh_sgd_step_async": (_I, [_P, _U32, _P, ctypes.c_float, _P]),
+    "bvhgpu_triangles_intersect": (_I, [_P, _P, _U32, _P, _U32, _I, _P]),
+    "bvhgpu_triangles_intersect_async": (_I, [_P, _P, _U32, _P, _U32, _I, _P, _P]),
     "bvhgpu_tune_get": (_I, [_P, _I, _P]),
     "bvhgpu_tune_set": (_I, [_P, _I, _P]),
     "bvhgpu_tune_space": (_I, [_I, _P, _U32, _P]),

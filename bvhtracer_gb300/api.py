@@ -129,6 +129,16 @@ class Context:
                                                      d_hits.ptr, stream))
 
 
+    def triangles_intersect(self, tris: np.ndarray, rays: np.ndarray, mode: int = _lib.LIST_CLOSEST) -> np.ndarray:
+        """Triangle::intersect (mode LIST_CLOSEST) or Triangle::intersect_mut (LIST_MUT) of every ray
+        against a triangle list in index order, no BVH."""
+        tris = np.ascontiguousarray(tris, np.float32).reshape(-1, 9)
+        rays = np.ascontiguousarray(rays, RAY)
+        hits = np.zeros(len(rays), HIT)
+        self.check(self.lib.bvhgpu_triangles_intersect(self.h, ptr(tris), len(tris), ptr(rays), len(rays), mode,
+                                                       ptr(hits)))
+        return hits
+
     # ---- launch configuration / autotuning (bvhgpu_tune_*, bvhgpu_autotune) ----
     def tune_get(self, kernel: int) -> dict:
         c = np.zeros(1, _lib.TUNE_CONFIG)

@@ -554,6 +554,38 @@ int bvhgpu_blas_intersect(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhgpu_ray* r
     return finish(ctx);
 }
 
+int bvhgpu_triangles_intersect_async(bvhgpu_ctx* ctx, const bvhgpu_triangle* d_tris, uint32_t ntris,
+                                     const bvhgpu_ray* d_rays, uint32_t n, int mode, bvhgpu_hit* d_hits,
+                                     bvhgpu_stream s) {
+    if (!ctx || (n && (!d_rays || !d_hits)) || (ntris && !d_tris)) return BVHGPU_ERR_INVALID_ARG;
+    if (mode != BVHGPU_LIST_CLOSEST && mode != BVHGPU_LIST_MUT)
+        return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown triangle-list mode %d", mode);
+    CK(launch_triangle_list(ctx, reinterpret_cast<const float*>(d_tris), ntris,
+                            reinterpret_cast<const float4*>(d_rays), n, mode, d_hits, pick(ctx, s)),
+       "triangle list");
+    return BVHGPU_OK;
+}
+
+int bvhgpu_triangles_intersect(bvhgpu_ctx* ctx, const bvhgpu_triangle* tris, uint32_t ntris, const bvhgpu_ray* rays,
+                               uint32_t n, int mode, bvhgpu_hit* hits) {
+    if (!ctx || (n && (!rays || !hits)) || (ntris && !tris)) return BVHGPU_ERR_INVALID_ARG;
+    if (n == 0) return BVHGPU_OK;
+    int rc = ensure(ctx, &ctx->stage_in, &ctx->stage_in_bytes, 32ull * n);
+    if (!rc) rc = ensure(ctx, &ctx->stage_out, &ctx->stage_out_bytes, 20ull * n);
+    if (!rc) rc = ensure(ctx, &ctx->stage_out2, &ctx->stage_out2_bytes, 36ull * ntris + 16);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(ctx->stage_in, rays, 32ull * n, cudaMemcpyHostToDevice, ctx->stream), "upload rays");
+    if (ntris)
+        CK(cudaMemcpyAsync(ctx->stage_out2, tris, 36ull * ntris, cudaMemcpyHostToDevice, ctx->stream),
+           "upload triangles");
+    rc = bvhgpu_triangles_intersect_async(ctx, static_cast<const bvhgpu_triangle*>(ctx->stage_out2), ntris,
+                                          static_cast<const bvhgpu_ray*>(ctx->stage_in), n, mode,
+                                          static_cast<bvhgpu_hit*>(ctx->stage_out), nullptr);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(hits, ctx->stage_out, 20ull * n, cudaMemcpyDeviceToHost, ctx->stream), "download hits");
+    return finish(ctx);
+}
+
 static int ensure_bounce(bvhgpu_ctx* ctx, uint32_t n) {
     if (ctx->bounce_cap >= n) return BVHGPU_OK;
     cudaFree(ctx->bounce_rays);

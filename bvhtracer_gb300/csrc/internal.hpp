@@ -142,6 +142,8 @@ cudaError_t launch_bounce_rays(bvhgpu_ctx* ctx, const DeviceBlas& b, const float
 cudaError_t launch_trace_batch(bvhgpu_ctx* ctx, const std::vector<const DeviceBlas*>& blases,
                                const bvhgpu_batch_item* items, uint32_t nitems, const float4* rays, uint32_t nrays,
                                int mode, void* hits, cudaStream_t s);
+cudaError_t launch_triangle_list(bvhgpu_ctx* ctx, const float* tris, uint32_t ntris, const float4* rays, uint32_t n,
+                                 int mode, void* hits, cudaStream_t s);
 cudaError_t launch_render(bvhgpu_ctx* ctx, const DeviceBlas& b, const bvhgpu_camera& cam, int w, int h, int acc,
                           const float* acc_params, int shader, const float* shader_params, const float* d_normals,
                           uint8_t* d_rgba, cudaStream_t s);

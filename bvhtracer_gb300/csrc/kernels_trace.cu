@@ -354,6 +354,68 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_trace_batch_persistent(const Ba
     }
 }
 
+// ---- triangle list, no BVH (Triangle::intersect / intersect_mut) ---------------------------
+// One thread per ray; the block stages 128 triangles at a time in shared memory (each loaded
+// once per block, then read by every lane) and tests them in index order.  Edges are formed on
+// load with the single IEEE subtractions of triangle.rs:44-45 / 77-78.
+//  kListClosest: Triangle::intersect with the strict `<` of a BVH leaf (first smallest t wins).
+//  kListMut:     Triangle::intersect_mut on one Intersection per ray: each triangle that reports
+//                a hit sets ray.t = min(ray.t, t) and overwrites u, v even when its t is larger.
+constexpr int kListClosest = 0;
+constexpr int kListMut = 1;
+constexpr int kListTile = 128;
+
+__device__ __forceinline__ float rmin_f(float a, float b) {  // f32::min: NaN-ignoring, first on ties
+    if (a != a) return b;
+    if (b != b) return a;
+    return (b < a) ? b : a;
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(kListTile) k_triangle_list(const float* __restrict__ tris, uint32_t ntris,
+                                                             const float4* __restrict__ rays, uint32_t n,
+                                                             GHit* __restrict__ hits) {
+    __shared__ float4 tile[3 * kListTile];
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool active = i < n;
+    float3 o = make_float3(0, 0, 0), d = o;
+    float ct = FLT_MAX, hu = 0.0f, hv = 0.0f;
+    uint32_t hp = kMiss;
+    if (active) load_ray(rays, i, o, d, ct);
+    for (uint32_t base = 0; base < ntris; base += kListTile) {
+        __syncthreads();
+        const uint32_t k = base + threadIdx.x;
+        if (k < ntris) {
+            const float* T = tris + 9ull * k;
+            const float v0x = T[0], v0y = T[1], v0z = T[2];
+            tile[3 * threadIdx.x] = make_float4(v0x, v0y, v0z, 0.0f);
+            tile[3 * threadIdx.x + 1] = make_float4(fsub(T[3], v0x), fsub(T[4], v0y), fsub(T[5], v0z), 0.0f);
+            tile[3 * threadIdx.x + 2] = make_float4(fsub(T[6], v0x), fsub(T[7], v0y), fsub(T[8], v0z), 0.0f);
+        }
+        __syncthreads();
+        if (!active) continue;
+        const uint32_t m = min((uint32_t)kListTile, ntris - base);
+        for (uint32_t j = 0; j < m; ++j) {
+            float t, u, v;
+            if (!tri_test(tile[3 * j], tile[3 * j + 1], tile[3 * j + 2], o, d, t, u, v)) continue;
+            if (MODE == kListClosest) {
+                if (t < ct) {
+                    ct = t;
+                    hu = u;
+                    hv = v;
+                    hp = base + j;
+                }
+            } else {
+                ct = rmin_f(ct, t);
+                hu = u;
+                hv = v;
+                hp = base + j;
+            }
+        }
+    }
+    if (active) store_hit(hits, i, hp != kMiss && (MODE == kListMut || ct < FLT_MAX), ct, hu, hv, hp, 0u);
+}
+
 // ---- tiled render --------------------------------------------------------------------------
 
 __device__ __forceinline__ float3 xf_point(const float* m, float3 p) {
@@ -650,6 +712,20 @@ cudaError_t launch_trace_batch(bvhgpu_ctx* ctx, const std::vector<const DeviceBl
     });
     g_launches++;
     return e;
+}
+
+cudaError_t launch_triangle_list(bvhgpu_ctx* ctx, const float* tris, uint32_t ntris, const float4* rays, uint32_t n,
+                                 int mode, void* hits, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    LaunchScope scope(ctx, BVHGPU_K_OTHER, s);
+    if (mode == BVHGPU_LIST_MUT)
+        k_triangle_list<kListMut><<<grid_for(n, kListTile), kListTile, 0, s>>>(tris, ntris, rays, n,
+                                                                             static_cast<GHit*>(hits));
+    else
+        k_triangle_list<kListClosest><<<grid_for(n, kListTile), kListTile, 0, s>>>(tris, ntris, rays, n,
+                                                                                 static_cast<GHit*>(hits));
+    g_launches++;
+    return cudaGetLastError();
 }
 
 cudaError_t launch_render(bvhgpu_ctx* ctx, const DeviceBlas& b, const bvhgpu_camera& cam, int w, int h, int acc,

@@ -167,6 +167,23 @@ int bvhgpu_event_elapsed_ms(bvhgpu_ctx* ctx, void* start, void* stop, float* ms)
 int bvhgpu_profile_enable(bvhgpu_ctx* ctx, int enable);
 int bvhgpu_profile_read(bvhgpu_ctx* ctx, double* ms, uint64_t* launches);
 
+/* ---- triangle list, no BVH ----------------------------------------------------------------- */
+/* Triangle::intersect / Triangle::intersect_mut (BT/src/geometry/triangle.rs:42-108) of every
+ * ray against every triangle of a list, in index order (brute force, tiled through shared memory).
+ *  BVHGPU_LIST_CLOSEST: Triangle::intersect with a BVH leaf's strict `<`: the first triangle with
+ *                       the smallest t; a miss is the sentinel.
+ *  BVHGPU_LIST_MUT:     Triangle::intersect_mut applied in order to one Intersection per ray:
+ *                       every triangle that reports a hit sets t = min(t, its t) and overwrites
+ *                       u and v (also when its t is larger); prim = the last such triangle.
+ * Hit records carry inst = 0 for a hit. */
+#define BVHGPU_LIST_CLOSEST 0
+#define BVHGPU_LIST_MUT 1
+int bvhgpu_triangles_intersect(bvhgpu_ctx* ctx, const bvhgpu_triangle* tris, uint32_t ntris, const bvhgpu_ray* rays,
+                               uint32_t n, int mode, bvhgpu_hit* hits);
+int bvhgpu_triangles_intersect_async(bvhgpu_ctx* ctx, const bvhgpu_triangle* d_tris, uint32_t ntris,
+                                     const bvhgpu_ray* d_rays, uint32_t n, int mode, bvhgpu_hit* d_hits,
+                                     bvhgpu_stream s);
+
 /* ---- BLAS -------------------------------------------------------------------------------- */
 /* BvhBuilder::build_for (BT/src/model/bvh.rs:524-541) on the host: the reference's SAH binned
  * build (8 bins), reordering `mesh` in place.  nodes_out must hold 2*n nodes. */

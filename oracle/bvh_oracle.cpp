@@ -782,6 +782,101 @@ int orc_bvh_intersect_mt(const orc_node* nodes, uint32_t nodes_used, const orc_t
     return ORC_OK;
 }
 
+// The two smallest distances at which `ray` meets a triangle of the BVH (the parity rule's
+// near-tie check: rays whose two nearest hits lie within a relative 1e-5 are reported apart).
+// Every node whose box the ray enters before the current second-best distance is visited
+// (Aabb::intersect against a ray whose t is that distance), leaf triangles are tested with
+// Triangle::intersect, and the two smallest t are kept; FLT_MAX where there is none.
+void two_nearest(const orc_node* nodes, const orc_tri* mesh, const Ray& ray, float* t1, float* t2) {
+    float a = FLT_MAX, b = FLT_MAX;
+    std::vector<uint32_t> stack;
+    stack.push_back(0);
+    while (!stack.empty()) {
+        const Node n = load_node(nodes[stack.back()]);
+        stack.pop_back();
+        Ray cull = ray;
+        cull.t = b;
+        float tmin = 0;
+        if (!aabb_intersect(n.aabb, cull, &tmin)) continue;
+        if (n.count > 0) {
+            for (uint32_t k = 0; k < n.count; ++k) {
+                float t, u, v;
+                if (!tri_intersect(load_tri(mesh[n.left_first + k]), ray, &t, &u, &v)) continue;
+                if (t < a) {
+                    b = a;
+                    a = t;
+                } else if (t < b) {
+                    b = t;
+                }
+            }
+        } else {
+            stack.push_back(n.left_first);
+            stack.push_back(n.left_first + 1);
+        }
+    }
+    *t1 = a;
+    *t2 = b;
+}
+
+int orc_two_nearest_mt(const orc_node* nodes, const orc_tri* mesh, const orc_ray* rays, uint32_t nrays, float* t1,
+                       float* t2, int nthreads) {
+    if (!nodes || !mesh || (nrays && (!rays || !t1 || !t2))) return ORC_ERR_ARG;
+    parallel_for(nrays, nthreads, [&](uint32_t b, uint32_t e) {
+        for (uint32_t i = b; i < e; ++i) two_nearest(nodes, mesh, load_ray(rays[i]), &t1[i], &t2[i]);
+    });
+    return ORC_OK;
+}
+
+// Triangle::intersect_mut (triangle.rs:75-108) on an Intersection: same test, and on a hit
+// ray.t = min(ray.t, t), interaction.{t, u, v} overwritten (u, v also when t is larger).
+inline bool tri_intersect_mut(const Tri& tri, Ray& ray, float* it, float* iu, float* iv) {
+    float t, u, v;
+    Ray probe = ray;
+    probe.t = INFINITY;  // min(inf, t) == t: the raw t, to which intersect_mut applies its own min
+    if (!tri_intersect(tri, probe, &t, &u, &v)) return false;
+    ray.t = rmin(ray.t, t);
+    *it = ray.t;
+    *iu = u;
+    *iv = v;
+    return true;
+}
+
+// Every ray against a triangle list in index order: mode 0 Triangle::intersect with a strict `<`
+// (first smallest t), mode 1 Triangle::intersect_mut on one Intersection per ray (prim = last
+// triangle that reported a hit).
+int orc_triangles_intersect(const orc_tri* mesh, uint32_t ntris, const orc_ray* rays, uint32_t nrays, int mode,
+                            orc_hit* hits) {
+    if ((ntris && !mesh) || (nrays && (!rays || !hits))) return ORC_ERR_ARG;
+    for (uint32_t i = 0; i < nrays; ++i) {
+        Ray r = load_ray(rays[i]);
+        float ct = r.t, hu = 0, hv = 0;
+        uint32_t hp = 0xFFFFFFFFu;
+        for (uint32_t k = 0; k < ntris; ++k) {
+            const Tri tri = load_tri(mesh[k]);
+            if (mode == 0) {
+                float t, u, v;
+                if (tri_intersect(tri, r, &t, &u, &v) && t < ct) {
+                    ct = t;
+                    hu = u;
+                    hv = v;
+                    hp = k;
+                }
+            } else {
+                float t, u, v;
+                if (tri_intersect_mut(tri, r, &t, &u, &v)) {
+                    ct = t;
+                    hu = u;
+                    hv = v;
+                    hp = k;
+                }
+            }
+        }
+        const bool hit = hp != 0xFFFFFFFFu && (mode == 1 || ct < FLT_MAX);
+        hits[i] = hit ? orc_hit{ct, hu, hv, hp, 0u} : MISS;
+    }
+    return ORC_OK;
+}
+
 // bvh.rs:469-493
 int orc_bvh_refit(orc_node* nodes, uint32_t nodes_used, const orc_tri* mesh, uint32_t n) {
     if (!nodes || !mesh) return ORC_ERR_ARG;

@@ -50,6 +50,13 @@ int orc_bvh_build(orc_tri* mesh, uint32_t n, orc_node* nodes_out, uint32_t* node
 int orc_bvh_intersect(const orc_node* nodes, uint32_t nodes_used, const orc_tri* mesh, uint32_t n,
                       const orc_ray* rays, uint32_t nrays, orc_hit* hits, orc_counters* counters);
 /* Same, split over nthreads host threads. */
+/* Every ray against a triangle list: mode 0 Triangle::intersect (first smallest t), mode 1
+ * Triangle::intersect_mut on one Intersection per ray. */
+int orc_triangles_intersect(const orc_tri* mesh, uint32_t ntris, const orc_ray* rays, uint32_t nrays, int mode,
+                            orc_hit* hits);
+/* Two smallest hit distances per ray over the whole BVH (FLT_MAX where there is none). */
+int orc_two_nearest_mt(const orc_node* nodes, const orc_tri* mesh, const orc_ray* rays, uint32_t nrays, float* t1,
+                       float* t2, int nthreads);
 int orc_bvh_intersect_mt(const orc_node* nodes, uint32_t nodes_used, const orc_tri* mesh, uint32_t n,
                          const orc_ray* rays, uint32_t nrays, orc_hit* hits, int nthreads);
 /* Bvh::refit, in place. */

@@ -76,6 +76,8 @@ def lib():
         L.orc_bvh_build.argtypes = [P, u32, P, P]
         L.orc_bvh_intersect.argtypes = [P, u32, P, u32, P, u32, P, P]
         L.orc_bvh_intersect_mt.argtypes = [P, u32, P, u32, P, u32, P, i32]
+        L.orc_two_nearest_mt.argtypes = [P, P, P, u32, P, P, i32]
+        L.orc_triangles_intersect.argtypes = [P, u32, P, u32, i32, P]
         L.orc_bvh_refit.argtypes = [P, u32, P, u32]
         L.orc_bvh_depth.argtypes = [P, u32]
         L.orc_bvh_depth.restype = u32
@@ -175,6 +177,36 @@ def bvh_intersect(nodes, nodes_used, tris, rays, counters=False, threads=1):
                                  _p(cnt))
     assert rc == 0
     return (hits, cnt) if counters else hits
+
+
+def triangles_intersect(tris, rays, mode=0):
+    """Triangle::intersect (mode 0, first smallest t) or Triangle::intersect_mut (mode 1) of every
+    ray against the triangle list in order."""
+    tris = _c(tris, np.float32).reshape(-1, 9)
+    rays = _c(rays, RAY)
+    hits = np.zeros(len(rays), HIT)
+    assert lib().orc_triangles_intersect(_p(tris), len(tris), _p(rays), len(rays), mode, _p(hits)) == 0
+    return hits
+
+
+def two_nearest(nodes, tris, rays, threads=8):
+    """The two smallest hit distances of every ray over the whole BVH (FLT_MAX: none)."""
+    nodes = _c(nodes, NODE)
+    tris = _c(tris, np.float32).reshape(-1, 9)
+    rays = _c(rays, RAY)
+    t1 = np.zeros(len(rays), np.float32)
+    t2 = np.zeros(len(rays), np.float32)
+    assert lib().orc_two_nearest_mt(_p(nodes), _p(tris), _p(rays), len(rays), _p(t1), _p(t2), threads) == 0
+    return t1, t2
+
+
+def near_ties(nodes, tris, rays, rel=1e-5, threads=8):
+    """Mask of the rays whose two nearest hits lie within `rel` relative in t (the parity rule
+    counts them apart: a 1-ulp difference in t could swap which triangle is closest)."""
+    t1, t2 = two_nearest(nodes, tris, rays, threads)
+    fmax = np.finfo(np.float32).max
+    both = (t1 < fmax) & (t2 < fmax)
+    return both & ((t2.astype(np.float64) - t1) <= rel * np.abs(t1.astype(np.float64)))
 
 
 def bvh_refit(nodes, nodes_used, tris):

@@ -159,6 +159,43 @@ def test_bounce_rays_and_hits(ctx):
         assert nb == int((ref0["prim"] != bt.MISS).sum())
 
 
+def test_near_tie_rays_counted_and_identical(ctx):
+    """The parity rule counts rays whose two nearest hits lie within 1e-5 relative in t apart.  The
+    traversal keeps the reference's visit order and strict `<`, so even exact ties (duplicated
+    triangles) resolve to the reference's primitive: near-tie rays match bit for bit too."""
+    base = scenes.soup(3000, 21)
+    tris, bvh = build(np.concatenate([base, base[::7], base[5::11]]))
+    blas = ctx.upload_blas(bvh, tris)
+    rays = np.concatenate([scenes.plane_rays(320, 320, (0.0, 0.0, -18.0), -15.0, 1.0, 1.0),
+                           scenes.sphere_rays(20000, 4, box=6.0)])
+    ref = orc.bvh_intersect(bvh.nodes, bvh.nodes_used, tris, rays, threads=8)
+    ties = orc.near_ties(bvh.nodes, tris, rays)
+    print(f"near-tie rays: {int(ties.sum())} of {int((ref['prim'] != bt.MISS).sum())} hits")
+    assert ties.sum() > 1000
+    gpu = blas.intersect(rays)
+    assert_hits_equal(gpu[~ties], ref[~ties], "rays without a near tie")
+    assert_hits_equal(gpu[ties], ref[ties], "near-tie rays")
+
+
+@pytest.mark.parametrize("mode", [bt.LIST_CLOSEST, bt.LIST_MUT])
+def test_triangle_list_matches_oracle(ctx, mode):
+    """Triangle::intersect / intersect_mut over a list (no BVH), incl. duplicated triangles and a
+    list that is not a multiple of the 128-triangle tile; LIST_MUT keeps the reference's
+    overwrite of u, v by a later, farther hit."""
+    base = scenes.soup(700, 9)
+    tris = np.ascontiguousarray(np.concatenate([base, base[::13]]), np.float32)
+    rays = np.concatenate([scenes.plane_rays(96, 96, (0.0, 0.0, -18.0), -15.0, 1.0, 1.0),
+                           scenes.sphere_rays(3000, 2, box=6.0)])
+    ref = orc.triangles_intersect(tris, rays, mode)
+    gpu = ctx.triangles_intersect(tris, rays, mode)
+    assert (ref["prim"] != bt.MISS).sum() > 1000
+    assert gpu.tobytes() == ref.tobytes()
+    if mode == bt.LIST_MUT:
+        closest = orc.triangles_intersect(tris, rays, 0)
+        assert (closest["prim"] != ref["prim"]).sum() > 0  # the overwrite quirk is exercised
+    assert ctx.triangles_intersect(tris[:0], rays[:5], mode)["prim"].tolist() == [bt.MISS] * 5
+
+
 # ---- refit -------------------------------------------------------------------------------------
 
 def test_refit_bit_exact(ctx):
