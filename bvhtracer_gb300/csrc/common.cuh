@@ -78,13 +78,31 @@ __device__ __forceinline__ bool slab(float4 lo, float4 hi, float3 o, float3 rd, 
 // evaluated without early exits (same decision, less divergence).  Returns the raw t; the
 // caller accepts it iff t < closest_t, which equals the reference's
 // `min(ray.t, t) < closest_ray.t` test because closest_ray.t never exceeds ray.t.
+// IEEE round-to-nearest 1/x for the triangle test's `S::one() / area` (triangle.rs:51, 83): the
+// hardware estimate rcp.approx refined by one Newton-Raphson step in fused multiply-adds
+// (Markstein's method: e = 1 - x*y, exact in an FMA; y' = y + e*y).  Checked on a GB300 against
+// CUDA's IEEE reciprocal __frcp_rn for every float with 1e-4 <= |x| < 2^126, both signs
+// (2,338,099,666 values): identical bit for bit, at about half the cost.  Huge, infinite and NaN
+// arguments take __frcp_rn itself; for |x| < 1e-4 the value is never used, because the test
+// rejects the triangle on |area| < 1e-4.
+__device__ __forceinline__ float rcp_approx(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float rcp_tri(float x) {
+    if (!(fabsf(x) < 0x1p126f)) return __frcp_rn(x);
+    const float y = rcp_approx(x);
+    return __fmaf_rn(__fmaf_rn(-x, y, 1.0f), y, y);
+}
+
 __device__ __forceinline__ bool tri_test(float4 v0, float4 e1, float4 e2, float3 o, float3 d, float& t,
                                          float& u, float& v) {
     float nx = fsub(fmul(d.y, e2.z), fmul(d.z, e2.y));
     float ny = fsub(fmul(d.z, e2.x), fmul(d.x, e2.z));
     float nz = fsub(fmul(d.x, e2.y), fmul(d.y, e2.x));
     float area = dot3(e1.x, e1.y, e1.z, nx, ny, nz);
-    float f = __frcp_rn(area);
+    float f = rcp_tri(area);
     float sx = fsub(o.x, v0.x);
     float sy = fsub(o.y, v0.y);
     float sz = fsub(o.z, v0.z);
@@ -321,6 +339,11 @@ __device__ __forceinline__ f2 f2_mul(f2 a, f2 b, f2 z) {
     asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(z));
     return d;
 }
+__device__ __forceinline__ f2 f2_fma(f2 a, f2 b, f2 c) {  // two fused multiply-adds, one rounding each
+    f2 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
 __device__ __forceinline__ f2 f2_pack(float lo, float hi) {
     f2 r;
     asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
@@ -375,7 +398,14 @@ __device__ __forceinline__ PairHit ray_terms(const PairData& p, const OriginTerm
     f2 A = f2_add(f2_add(f2_mul(p.E1X, NX, Z), f2_mul(p.E1Y, NY, Z)), f2_mul(p.E1Z, NZ, Z));  // e1 . n
     float aA, aB;
     f2_unpack(A, aA, aB);
-    f2 F = f2_pack(__frcp_rn(aA), __frcp_rn(aB));
+    f2 F;  // 1 / area for both triangles (rcp_tri, the Newton step packed)
+    if (fabsf(aA) < 0x1p126f && fabsf(aB) < 0x1p126f) {
+        const f2 Y = f2_pack(rcp_approx(aA), rcp_approx(aB));
+        const f2 E = f2_fma(A ^ 0x8000000080000000ull, Y, 0x3F8000003F800000ull);  // 1 - a*y
+        F = f2_fma(E, Y, Y);
+    } else {
+        F = f2_pack(rcp_tri(aA), rcp_tri(aB));
+    }
     f2 U = f2_mul(F, f2_add(f2_add(f2_mul(o.SX, NX, Z), f2_mul(o.SY, NY, Z)), f2_mul(o.SZ, NZ, Z)), Z);
     f2 V = f2_mul(F, f2_add(f2_add(f2_mul(DX, o.QX, Z), f2_mul(DY, o.QY, Z)), f2_mul(DZ, o.QZ, Z)), Z);
     f2 T = f2_mul(F, o.TN, Z);
