@@ -411,7 +411,7 @@ def run_batch(args):
     import bvhtracer_gb300 as bt
     rank, world, local_rank = dist_env()
     t0 = time.perf_counter()
-    built = setup_batch()
+    built = setup_batch(args.scenes)
     setup_s = time.perf_counter() - t0
     ctx = bt.Context(local_rank)
     blases = [ctx.upload_blas(bvh, tris) for tris, bvh, _ in built]
@@ -734,6 +734,8 @@ def main():
     ap.add_argument("--config", type=int, choices=[1, 2, 3, 4], default=1,
                     help="1: displaced icosphere frame + bounce (default); 2: instanced animated frames in a CUDA "
                          "graph; 3: uneven 64-scene batch; 4: differentiable render (adjoint ms/step)")
+    ap.add_argument("--scenes", type=int, default=64,
+                    help="config 3: number of scenes (64 = the workload; fewer only for small profiling runs)")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (use the default launch configs)")
     ap.add_argument("--no-cpu-baseline", action="store_true",
                     help="skip the CPU-baseline leg (outside the timed region), e.g. under a profiler")

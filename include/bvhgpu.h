@@ -354,8 +354,8 @@ typedef struct bvhgpu_tune_config {
     uint32_t refill;
     uint32_t reserved; /* 0 */
 } bvhgpu_tune_config;
-/* Defaults: block 128, min_blocks 5, stack 0, big_leaf 16, refill 1; for the two-level kernels
- * (TRACE_SCENE, SCENE_BOUNCE) block 64, min_blocks 1, stack 256, refill 1 / 8. */
+/* Defaults (the tuner's picks on GB300): block 128, min_blocks 6, stack 0, big_leaf 16, refill 1;
+ * for the two-level kernels (TRACE_SCENE, SCENE_BOUNCE) stack 256 and refill 1 / 8. */
 int bvhgpu_tune_get(bvhgpu_ctx* ctx, int kernel, bvhgpu_tune_config* out);
 /* BVHGPU_ERR_INVALID_ARG for a kernel that is not tunable or a shape / stack not compiled. */
 int bvhgpu_tune_set(bvhgpu_ctx* ctx, int kernel, const bvhgpu_tune_config* cfg);
