@@ -386,11 +386,14 @@ def setup_batch(nscenes: int = 64, seed: int = SEED):
 
     def make(i):
         tris, rays = scenes.config3_scene(i, int(ntris[i]), int(nrays[i]), seed)
+        original = tris.copy()
         bvh = bt.BvhBuilder().build_for(tris)
-        return tris, bvh, rays
+        return tris, bvh, rays, original
 
     with ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 1)) as ex:
-        return list(ex.map(make, range(nscenes)))
+        out = list(ex.map(make, range(nscenes)))
+    setup_batch.originals = [o for *_, o in out]
+    return [(t, b, r) for t, b, r, _ in out]
 
 
 def batch_cpu_baseline(built, per_scene: int = 8192, threads: int | None = None):
@@ -431,6 +434,18 @@ def run_batch(args):
     built = setup_batch(args.scenes)
     setup_s = time.perf_counter() - t0
     ctx = bt.Context(local_rank)
+    # the same 64 SAH builds on the GPU (BvhBuilder::build_for on the device), checked bit for bit
+    # against the host builds above
+    t0 = time.perf_counter()
+    gpu_builds = []
+    for orig in setup_batch.originals:
+        mesh = orig.copy()
+        gpu_builds.append((mesh, ctx.build_bvh(mesh)))
+    gpu_build_s = time.perf_counter() - t0
+    gpu_build_identical = all(m.tobytes() == t.tobytes() and g.nodes_used == b.nodes_used and
+                              g.nodes.tobytes() == b.nodes.tobytes()
+                              for (m, g), (t, b, _) in zip(gpu_builds, built))
+    del gpu_builds
     blases = [ctx.upload_blas(bvh, tris) for tris, bvh, _ in built]
     rays = np.concatenate([r for _, _, r in built])
     items = np.zeros(len(built), bt.BATCH_ITEM)
@@ -528,6 +543,8 @@ def run_batch(args):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
         "config": {"workload": WORKLOAD3, "scenes": len(built), "rays": n,
                    "triangles": int(sum(len(t) for t, _, _ in built)), "setup_s": setup_s,
+                   "sah_build": {"host_s_16_threads_incl_generation": setup_s, "gpu_s": gpu_build_s,
+                                 "gpu_identical_to_host": gpu_build_identical},
                    "l2": "flushed between steps (256 MB memset)", "parallelism": f"replicas x{world}", "seed": SEED,
                    "tuned": tuned, "tune_s": tune_s},
         "plain_vs_persistent": {"persistent": value, "plain": plain, "ratio_persistent_over_plain": value / plain,

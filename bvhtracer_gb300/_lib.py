@@ -122,6 +122,8 @@ SIGNATURES = {
     "bvhgpu_mse_loss": (_I, [_P, _P, _P, _U32, _P]),
     "bvhgpu_lambert_adjoint_async": (_I, [_P, _U32, _P, _U32, _P, _P, _P, _P, _P, _P]),
     "bvhgpu_mesh_sgd_step_async": (_I, [_P, _U32, _P, ctypes.c_float, _P]),
+    "bvhgpu_build_bvh_device": (_I, [_P, _P, _U32, _P, _P, _P]),
+    "bvhgpu_blas_build": (_I, [_P, _P, _U32, _P]),
     "bvhgpu_triangles_intersect": (_I, [_P, _P, _U32, _P, _U32, _I, _P]),
     "bvhgpu_triangles_intersect_async": (_I, [_P, _P, _U32, _P, _U32, _I, _P, _P]),
     "bvhgpu_tune_get": (_I, [_P, _I, _P]),

@@ -129,6 +129,20 @@ class Context:
                                                      d_hits.ptr, stream))
 
 
+    def build_bvh(self, mesh: np.ndarray, perm: bool = False):
+        """BvhBuilder::build_for on the GPU (same result as BvhBuilder().build_for); reorders ``mesh``
+        ([n, 9] float32, C-contiguous) in place.  With perm=True also returns the input index of the
+        triangle at each position."""
+        if mesh.dtype != np.float32 or not mesh.flags.c_contiguous or mesh.ndim != 2 or mesh.shape[1] != 9:
+            raise ValueError("mesh must be a C-contiguous float32 array of shape [n, 9]")
+        n = mesh.shape[0]
+        nodes = np.zeros(max(2 * n, 1), NODE)
+        used = ctypes.c_uint32()
+        p = np.zeros(n, np.uint32) if perm else None
+        self.check(self.lib.bvhgpu_build_bvh_device(self.h, ptr(mesh), n, ptr(nodes), ctypes.byref(used), ptr(p)))
+        bvh = Bvh(nodes, used.value)
+        return (bvh, p) if perm else bvh
+
     def triangles_intersect(self, tris: np.ndarray, rays: np.ndarray, mode: int = _lib.LIST_CLOSEST) -> np.ndarray:
         """Triangle::intersect (mode LIST_CLOSEST) or Triangle::intersect_mut (LIST_MUT) of every ray
         against a triangle list in index order, no BVH."""

@@ -554,6 +554,25 @@ int bvhgpu_blas_intersect(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhgpu_ray* r
     return finish(ctx);
 }
 
+int bvhgpu_build_bvh_device(bvhgpu_ctx* ctx, bvhgpu_triangle* mesh, uint32_t n, bvhgpu_node* nodes_out,
+                            uint32_t* nodes_used, uint32_t* perm_out) {
+    if (!ctx || !mesh || !nodes_out || !nodes_used || n == 0 || n > 0x55555554u) return BVHGPU_ERR_INVALID_ARG;
+    if (ctx->capturing) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "build_bvh_device: not allowed during capture");
+    const char* what = "";
+    int rc = build_bvh_device(ctx, reinterpret_cast<float*>(mesh), n, nodes_out, nodes_used, perm_out, &what);
+    if (rc) return fail(ctx, rc, "GPU SAH build: %s", what);
+    return BVHGPU_OK;
+}
+
+int bvhgpu_blas_build(bvhgpu_ctx* ctx, bvhgpu_triangle* mesh, uint32_t n, uint32_t* blas_id) {
+    if (!ctx || !mesh || !blas_id || n == 0) return BVHGPU_ERR_INVALID_ARG;
+    std::vector<bvhgpu_node> nodes(2ull * n);
+    uint32_t used = 0;
+    int rc = bvhgpu_build_bvh_device(ctx, mesh, n, nodes.data(), &used, nullptr);
+    if (rc) return rc;
+    return bvhgpu_blas_upload(ctx, nodes.data(), used, mesh, n, blas_id);
+}
+
 int bvhgpu_triangles_intersect_async(bvhgpu_ctx* ctx, const bvhgpu_triangle* d_tris, uint32_t ntris,
                                      const bvhgpu_ray* d_rays, uint32_t n, int mode, bvhgpu_hit* d_hits,
                                      bvhgpu_stream s) {

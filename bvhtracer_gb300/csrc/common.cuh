@@ -121,6 +121,35 @@ __device__ __forceinline__ bool tri_test(float4 v0, float4 e1, float4 e2, float3
 
 __device__ __forceinline__ uint32_t ubits(float f) { return __float_as_uint(f); }
 
+// f32::min / f32::max: a NaN operand is ignored, and on equality the first operand is kept
+// (the host build and the oracle use the same rule; it decides the sign of a zero result).
+__device__ __forceinline__ float min_ni(float a, float b) {
+    if (a != a) return b;
+    if (b != b) return a;
+    return (b < a) ? b : a;
+}
+__device__ __forceinline__ float max_ni(float a, float b) {
+    if (a != a) return b;
+    if (b != b) return a;
+    return (b > a) ? b : a;
+}
+
+// Order-preserving map of a float to 32 bits with both zeros at one rank: the high half of the
+// 64-bit keys with which the min / max folds of the reference (update_node_bounds, the SAH bins)
+// are reduced in parallel -- the low half is the position in the fold's order, so among equal
+// values the first in that order wins, as the sequential f32::min / f32::max keeps it.
+__device__ __forceinline__ uint32_t ordered(float f) {
+    uint32_t b = __float_as_uint(f);
+    if (f == 0.0f) return 0x80000000u;
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ unsigned long long key_min(float f, uint32_t pos) {
+    return ((unsigned long long)ordered(f) << 32) | pos;
+}
+__device__ __forceinline__ unsigned long long key_max(float f, uint32_t pos) {
+    return ((unsigned long long)ordered(f) << 32) | (0xFFFFFFFFu - pos);
+}
+
 // Closest-hit traversal of one BLAS (bvh.rs:242-305): DFS with the far child pushed, near
 // child = strictly smaller entry distance (ties -> right child), popped nodes are not
 // re-culled (the reference does not re-test a popped node's box), leaf triangles in

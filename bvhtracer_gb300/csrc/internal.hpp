@@ -151,6 +151,10 @@ cudaError_t launch_render(bvhgpu_ctx* ctx, const DeviceBlas& b, const bvhgpu_cam
 // ---- launchers (kernels_scene.cu) ------------------------------------------------------
 cudaError_t launch_write_tris(bvhgpu_ctx* ctx, DeviceBlas& b, const float* d_tris9, cudaStream_t s);
 cudaError_t launch_refit(bvhgpu_ctx* ctx, DeviceBlas& b, cudaStream_t s);
+// BvhBuilder::build_for on the device (build_gpu.cu): mesh (host, n x 9 floats) is reordered in
+// place, nodes_out (2n) and perm_out (optional) written; *what names a failure.
+int build_bvh_device(bvhgpu_ctx* ctx, float* mesh, uint32_t n, bvhgpu_node* nodes_out, uint32_t* nodes_used,
+                     uint32_t* perm_out, const char** what);
 // Sets ctx->last_error to msg and returns code (the ABI's error path).
 int record_error(bvhgpu_ctx* ctx, int code, const char* msg);
 constexpr uint32_t kMaxSceneObjects = 4096;  // TLAS rebuild shared memory: 40 B per object

@@ -23,18 +23,6 @@ constexpr int kBlock = 128;
 constexpr uint32_t kNone = 0xFFFFFFFFu;
 constexpr unsigned kFull = 0xFFFFFFFFu;
 
-// f32::min / f32::max with the first operand kept on equality (same rule as the host build).
-__device__ __forceinline__ float min_ni(float a, float b) {
-    if (a != a) return b;
-    if (b != b) return a;
-    return (b < a) ? b : a;
-}
-__device__ __forceinline__ float max_ni(float a, float b) {
-    if (a != a) return b;
-    if (b != b) return a;
-    return (b > a) ? b : a;
-}
-
 // Writes the traversal layout {v0, e1 = v1 - v0, e2 = v2 - v0} (the subtractions of
 // triangle.rs:44-45, so no bit changes) and the raw vertices used by refit.
 __global__ void k_write_tris(const float* __restrict__ tris9, uint32_t n, float4* __restrict__ out,
@@ -67,11 +55,6 @@ __global__ void k_write_tris(const float* __restrict__ tris9, uint32_t n, float4
 // with both zeros mapped to one rank, then the position in the fold order (lower wins on a tie).
 // NaNs are skipped, as f32::min skips them.  The reduced key names the winning vertex, whose
 // actual bits are read back.
-__device__ __forceinline__ uint32_t ordered(float f) {
-    uint32_t b = __float_as_uint(f);
-    if (f == 0.0f) return 0x80000000u;
-    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
-}
 
 // Segmented min of 64-bit keys over consecutive lanes with the same segment id (leaf): the
 // first lane of each segment ends up holding the segment's minimum.

@@ -365,12 +365,6 @@ constexpr int kListClosest = 0;
 constexpr int kListMut = 1;
 constexpr int kListTile = 128;
 
-__device__ __forceinline__ float rmin_f(float a, float b) {  // f32::min: NaN-ignoring, first on ties
-    if (a != a) return b;
-    if (b != b) return a;
-    return (b < a) ? b : a;
-}
-
 template <int MODE>
 __global__ void __launch_bounds__(kListTile) k_triangle_list(const float* __restrict__ tris, uint32_t ntris,
                                                              const float4* __restrict__ rays, uint32_t n,
@@ -406,7 +400,7 @@ __global__ void __launch_bounds__(kListTile) k_triangle_list(const float* __rest
                     hp = base + j;
                 }
             } else {
-                ct = rmin_f(ct, t);
+                ct = min_ni(ct, t);
                 hu = u;
                 hv = v;
                 hp = base + j;

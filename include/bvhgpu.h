@@ -167,6 +167,15 @@ int bvhgpu_event_elapsed_ms(bvhgpu_ctx* ctx, void* start, void* stop, float* ms)
 int bvhgpu_profile_enable(bvhgpu_ctx* ctx, int enable);
 int bvhgpu_profile_read(bvhgpu_ctx* ctx, double* ms, uint64_t* launches);
 
+/* BvhBuilder::build_for on the GPU: the same nodes, triangle order and permutation as
+ * bvhgpu_build_bvh_host / bvhgpu_build_bvh_host_indexed, bit for bit (BVHGPU_ERR_BUILD where the
+ * reference panics).  mesh (host) is reordered in place; nodes_out holds 2n nodes; perm_out (n
+ * entries, may be NULL) gets the input index of the triangle at each position.  Synchronous. */
+int bvhgpu_build_bvh_device(bvhgpu_ctx* ctx, bvhgpu_triangle* mesh, uint32_t n, bvhgpu_node* nodes_out,
+                            uint32_t* nodes_used, uint32_t* perm_out);
+/* Build on the GPU and upload as a BLAS in one call; mesh (host) is reordered in place. */
+int bvhgpu_blas_build(bvhgpu_ctx* ctx, bvhgpu_triangle* mesh, uint32_t n, uint32_t* blas_id);
+
 /* ---- triangle list, no BVH ----------------------------------------------------------------- */
 /* Triangle::intersect / Triangle::intersect_mut (BT/src/geometry/triangle.rs:42-108) of every
  * ray against every triangle of a list, in index order (brute force, tiled through shared memory).
