@@ -46,6 +46,7 @@ ACC_INTERSECTION, ACC_DEPTH, ACC_UV, ACC_NORMAL = 0, 1, 2, 3
 SHADER_RADIANCE, SHADER_INTERSECTION, SHADER_DEPTH = 0, 1, 2
 MODE_PLAIN, MODE_PERSISTENT = 0, 1
 LIST_CLOSEST, LIST_MUT = 0, 1
+MESH_TRI, MESH_OBJ = 0, 1
 
 KERNELS = ["trace_blas", "trace_scene", "persistent_bounce", "bounce_gen", "trace_queue", "trace_batch",
            "refit", "tlas_build", "render", "other", "lambert_forward", "lambert_adjoint", "scene_bounce"]
@@ -122,6 +123,8 @@ SIGNATURES = {
     "bvhgpu_mse_loss": (_I, [_P, _P, _P, _U32, _P]),
     "bvhgpu_lambert_adjoint_async": (_I, [_P, _U32, _P, _U32, _P, _P, _P, _P, _P, _P]),
     "bvhgpu_mesh_sgd_step_async": (_I, [_P, _U32, _P, ctypes.c_float, _P]),
+    "bvhgpu_mesh_decode": (_I, [ctypes.c_char_p, _SZ, _I, _P, _P, _P, _U32, _P, ctypes.c_char_p, _SZ]),
+    "bvhgpu_mesh_decode_file": (_I, [ctypes.c_char_p, _I, _P, _P, _P, _U32, _P, ctypes.c_char_p, _SZ]),
     "bvhgpu_build_bvh_device": (_I, [_P, _P, _U32, _P, _P, _P]),
     "bvhgpu_blas_build": (_I, [_P, _P, _U32, _P]),
     "bvhgpu_triangles_intersect": (_I, [_P, _P, _U32, _P, _U32, _I, _P]),

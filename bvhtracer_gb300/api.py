@@ -201,6 +201,33 @@ class Context:
         return {k: int(best[0][k]) for k in _lib.TUNE_CONFIG.names if k != "reserved"}, float(ms.value)
 
 
+def decode_mesh(data, fmt: int = _lib.MESH_TRI):
+    """Decodes a `.tri` (MESH_TRI) or `.obj` (MESH_OBJ) mesh from text / bytes: returns
+    (tris [n, 9], normals [n, 9], uvs [n, 6]) float32 (bvhgpu_mesh_decode)."""
+    lib = _lib.load()
+    raw = data.encode() if isinstance(data, str) else bytes(data)
+    n = ctypes.c_uint32()
+    err = ctypes.create_string_buffer(512)
+    rc = lib.bvhgpu_mesh_decode(raw, len(raw), fmt, None, None, None, 0, ctypes.byref(n), err, 512)
+    if rc:
+        raise BvhGpuError(rc, err.value.decode(errors="replace"))
+    tris = np.zeros((n.value, 9), np.float32)
+    normals = np.zeros((n.value, 9), np.float32)
+    uvs = np.zeros((n.value, 6), np.float32)
+    rc = lib.bvhgpu_mesh_decode(raw, len(raw), fmt, ptr(tris), ptr(normals), ptr(uvs), n.value, ctypes.byref(n),
+                                err, 512)
+    if rc:
+        raise BvhGpuError(rc, err.value.decode(errors="replace"))
+    return tris, normals, uvs
+
+
+def load_mesh(path: str):
+    """decode_mesh of a file; the format from its extension (.tri / .obj)."""
+    fmt = _lib.MESH_OBJ if str(path).lower().endswith(".obj") else _lib.MESH_TRI
+    with open(path, "rb") as f:
+        return decode_mesh(f.read(), fmt)
+
+
 class DeviceBuffer:
     def __init__(self, ctx: Context, nbytes: int):
         self.ctx = ctx

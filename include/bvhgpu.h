@@ -176,6 +176,22 @@ int bvhgpu_build_bvh_device(bvhgpu_ctx* ctx, bvhgpu_triangle* mesh, uint32_t n, 
 /* Build on the GPU and upload as a BLAS in one call; mesh (host) is reordered in place. */
 int bvhgpu_blas_build(bvhgpu_ctx* ctx, bvhgpu_triangle* mesh, uint32_t n, uint32_t* blas_id);
 
+/* ---- mesh decoders (host; no context needed) ------------------------------------------------ */
+/* BVHGPU_MESH_TRI: the reference's `.tri` loader (BT/tri_loader/src/loader.rs, lexer.rs) and
+ * TriMeshDecoder (BT/src/mesh/decoders.rs:108-133): nine floats per triangle, the face normal
+ * normalize(normalize(v2-v0) x normalize(v1-v0)) at every corner, zero texture coordinates.
+ * BVHGPU_MESH_OBJ: Wavefront `.obj`, first object only, with ObjMeshDecoder's per-corner normals
+ * and texture coordinates (decoders.rs:157-215; f64 values cast to f32; polygons as fans).
+ * Writes min(cap, n) triangles (36 B), normals (9 floats) and uvs (6 floats) where the pointers
+ * are not NULL and *ntris = n; call with cap = 0 to size the buffers.  A decoding error returns
+ * BVHGPU_ERR_INVALID_ARG with the line and reason in err (errlen bytes, may be NULL). */
+#define BVHGPU_MESH_TRI 0
+#define BVHGPU_MESH_OBJ 1
+int bvhgpu_mesh_decode(const char* text, size_t len, int format, bvhgpu_triangle* tris, float* normals, float* uvs,
+                       uint32_t cap, uint32_t* ntris, char* err, size_t errlen);
+int bvhgpu_mesh_decode_file(const char* path, int format, bvhgpu_triangle* tris, float* normals, float* uvs,
+                            uint32_t cap, uint32_t* ntris, char* err, size_t errlen);
+
 /* ---- triangle list, no BVH ----------------------------------------------------------------- */
 /* Triangle::intersect / Triangle::intersect_mut (BT/src/geometry/triangle.rs:42-108) of every
  * ray against every triangle of a list, in index order (brute force, tiled through shared memory).

@@ -106,3 +106,21 @@ def test_blas_built_on_the_gpu_traces_like_the_host_built_one(ctx):
     hits = np.zeros(len(rays), bt.HIT)
     ctx.check(ctx.lib.bvhgpu_blas_intersect(ctx.h, bid.value, ptr(np.ascontiguousarray(rays)), len(rays), ptr(hits)))
     assert hits.tobytes() == ref.tobytes()
+
+
+def test_decoded_tri_file_builds_and_traces_on_the_gpu(ctx):
+    """`.tri` text -> bvhgpu_mesh_decode -> GPU SAH build -> upload -> trace, against the oracle's
+    build and traversal of the same decoded mesh."""
+    from oracle import oracle as orc
+    src = scenes.displaced_icosphere(4, seed=12).triangles()
+    text = "\n".join(" ".join("{:.9g}".format(float(x)) for x in row) for row in src) + "\n"
+    tris, normals, _ = bt.decode_mesh(text)
+    assert tris.tobytes() == np.ascontiguousarray(src, np.float32).tobytes()
+    mesh = tris.copy()
+    bvh = ctx.build_bvh(mesh)
+    blas = ctx.upload_blas(bvh, mesh)
+    rays = scenes.look_at_rays(128, 96, (0.0, 0.0, -3.0), (0.0, 0.0, 0.0), 45.0)
+    ref_tris, ref_nodes, ref_used = orc.bvh_build(tris)
+    ref = orc.bvh_intersect(ref_nodes, ref_used, ref_tris, rays, threads=8)
+    assert blas.intersect(rays).tobytes() == ref.tobytes()
+    assert (ref["prim"] != bt.MISS).sum() > 1000
