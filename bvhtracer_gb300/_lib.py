@@ -42,7 +42,7 @@ ERRORS = {1: "invalid argument", 2: "out of memory", 3: "CUDA error", 4: "stack 
           5: "step cap exceeded", 6: "build would panic", 7: "no CUDA device",
           8: "input larger than the entry point's fixed maximum"}
 
-ACC_INTERSECTION, ACC_DEPTH, ACC_UV, ACC_NORMAL = 0, 1, 2, 3
+ACC_INTERSECTION, ACC_DEPTH, ACC_UV, ACC_NORMAL, ACC_TEXTURE = 0, 1, 2, 3, 4
 SHADER_RADIANCE, SHADER_INTERSECTION, SHADER_DEPTH = 0, 1, 2
 MODE_PLAIN, MODE_PERSISTENT = 0, 1
 LIST_CLOSEST, LIST_MUT = 0, 1
@@ -114,6 +114,7 @@ SIGNATURES = {
     "bvhgpu_graph_launch": (_I, [_P, _U32]),
     "bvhgpu_graph_free": (_I, [_P, _U32]),
     "bvhgpu_render": (_I, [_P, _U32, _P, _I, _I, _I, _P, _I, _P, _P, _P, _P]),
+    "bvhgpu_render_textured": (_I, [_P, _U32, _P, _I, _I, _P, _P, _U32, _U32, _I, _P, _P, _P]),
     "bvhgpu_mesh_create": (_I, [_P, _U32, _P, _U32, _P, _P, _U32, _P]),
     "bvhgpu_mesh_free": (_I, [_P, _U32]),
     "bvhgpu_mesh_vertices": (_I, [_P, _U32, _P]),

@@ -423,6 +423,21 @@ class Blas:
                                                   ctypes.byref(rays)))
         return rgba, rays.value
 
+    def render_textured(self, camera: "Camera", width: int, height: int, tex_coords, texels, shader: int = 0,
+                        shader_params=None):
+        """TextureMaterialAccumulator + shader: tex_coords [n, 6] (per-corner u, v, in this BLAS's
+        triangle order), texels [h, w, 3] uint8.  Returns (rgba [h, w, 4], rays traced)."""
+        cam = camera.to_struct()
+        rgba = np.zeros((height, width, 4), np.uint8)
+        tc = np.ascontiguousarray(tex_coords, np.float32).reshape(-1, 6)
+        tx = np.ascontiguousarray(texels, np.uint8)
+        sp = None if shader_params is None else np.ascontiguousarray(shader_params, np.float32)
+        rays = ctypes.c_uint64()
+        self.ctx.check(self.ctx.lib.bvhgpu_render_textured(self.ctx.h, self.id, ptr(cam), width, height, ptr(tc),
+                                                           ptr(tx), tx.shape[1], tx.shape[0], shader, ptr(sp),
+                                                           ptr(rgba), ctypes.byref(rays)))
+        return rgba, rays.value
+
     def free(self):
         if self.id:
             self.ctx.lib.bvhgpu_blas_free(self.ctx.h, self.id)

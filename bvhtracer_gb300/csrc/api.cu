@@ -1167,8 +1167,37 @@ int bvhgpu_render(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhgpu_camera* camera
     if (normals)
         CK(cudaMemcpyAsync(ctx->stage_in, normals, 36ull * b->ntris, cudaMemcpyHostToDevice, ctx->stream), "normals");
     CK(launch_render(ctx, *b, *camera, width, height, accumulator, acc_params, shader, shader_params,
-                     normals ? static_cast<const float*>(ctx->stage_in) : nullptr,
+                     normals ? static_cast<const float*>(ctx->stage_in) : nullptr, nullptr, nullptr, 0, 0,
                      static_cast<uint8_t*>(ctx->stage_out), ctx->stream),
+       "render");
+    CK(cudaMemcpyAsync(rgba, ctx->stage_out, 4 * px, cudaMemcpyDeviceToHost, ctx->stream), "download frame");
+    rc = finish(ctx);
+    if (rc) return rc;
+    if (rays_traced) *rays_traced = px;
+    return BVHGPU_OK;
+}
+
+int bvhgpu_render_textured(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhgpu_camera* camera, int width, int height,
+                           const float* tex_coords, const uint8_t* texels, uint32_t tex_w, uint32_t tex_h,
+                           int shader, const float* shader_params, uint8_t* rgba, uint64_t* rays_traced) {
+    if (!ctx || !camera || !rgba || width <= 0 || height <= 0 || !tex_coords || !texels || tex_w == 0 ||
+        tex_h == 0)
+        return BVHGPU_ERR_INVALID_ARG;
+    if (shader < 0 || shader > 2) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown shader %d", shader);
+    if ((shader == BVHGPU_SHADER_INTERSECTION || shader == BVHGPU_SHADER_DEPTH) && !shader_params)
+        return fail(ctx, BVHGPU_ERR_INVALID_ARG, "shader needs parameters");
+    DeviceBlas* b = find_blas(ctx, blas_id);
+    if (!b) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown BLAS %u", blas_id);
+    const size_t px = (size_t)width * height, tc_bytes = 24ull * b->ntris, tex_bytes = 3ull * tex_w * tex_h;
+    int rc = ensure(ctx, &ctx->stage_out, &ctx->stage_out_bytes, 4 * px);
+    if (!rc) rc = ensure(ctx, &ctx->stage_in, &ctx->stage_in_bytes, tc_bytes + tex_bytes + 16);
+    if (rc) return rc;
+    float* d_tc = static_cast<float*>(ctx->stage_in);
+    uint8_t* d_tex = static_cast<uint8_t*>(ctx->stage_in) + tc_bytes;
+    CK(cudaMemcpyAsync(d_tc, tex_coords, tc_bytes, cudaMemcpyHostToDevice, ctx->stream), "texture coordinates");
+    CK(cudaMemcpyAsync(d_tex, texels, tex_bytes, cudaMemcpyHostToDevice, ctx->stream), "texture");
+    CK(launch_render(ctx, *b, *camera, width, height, BVHGPU_ACC_TEXTURE, nullptr, shader, shader_params, nullptr,
+                     d_tc, d_tex, tex_w, tex_h, static_cast<uint8_t*>(ctx->stage_out), ctx->stream),
        "render");
     CK(cudaMemcpyAsync(rgba, ctx->stage_out, 4 * px, cudaMemcpyDeviceToHost, ctx->stream), "download frame");
     rc = finish(ctx);

@@ -146,6 +146,7 @@ cudaError_t launch_triangle_list(bvhgpu_ctx* ctx, const float* tris, uint32_t nt
                                  int mode, void* hits, cudaStream_t s);
 cudaError_t launch_render(bvhgpu_ctx* ctx, const DeviceBlas& b, const bvhgpu_camera& cam, int w, int h, int acc,
                           const float* acc_params, int shader, const float* shader_params, const float* d_normals,
+                          const float* d_tex_coords, const uint8_t* d_texels, uint32_t tex_w, uint32_t tex_h,
                           uint8_t* d_rgba, cudaStream_t s);
 
 // ---- launchers (kernels_scene.cu) ------------------------------------------------------

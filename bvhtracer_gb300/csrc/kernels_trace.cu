@@ -432,7 +432,16 @@ struct RenderParams {
     float acc[16];
     float sh[8];
     int width, height, acc_kind, shader_kind;
+    const float* tex_coords;  // BVHGPU_ACC_TEXTURE: 6 floats per triangle (per-corner u, v)
+    const uint8_t* texels;    //   RGB8, row-major
+    uint32_t tex_w, tex_h;
 };
+
+__device__ __forceinline__ unsigned long long f32_as_usize(float x) {  // Rust `as usize`: saturating
+    if (!(x > 0.0f)) return 0ull;
+    if (x >= 18446744073709551616.0f) return 0xFFFFFFFFFFFFFFFFull;
+    return (unsigned long long)x;
+}
 
 __device__ __forceinline__ uint8_t f32_as_u8(float x) {  // Rust `as u8`: saturating, NaN -> 0
     if (!(x > 0.0f)) return 0;
@@ -502,6 +511,21 @@ __global__ void __launch_bounds__(64) k_render(GBlas b, RenderParams P, const fl
                 float3 nz = normalize3(xf_vector(P.acc, nm));
                 rad = make_float3(fmul(fadd(nz.x, 1.0f), 0.5f), fmul(fadd(nz.y, 1.0f), 0.5f),
                                   fmul(fadd(nz.z, 1.0f), 0.5f));
+            }
+            break;
+        case BVHGPU_ACC_TEXTURE:  // TextureMaterialAccumulator, renderer.rs:289-334
+            if (hit) {
+                const float* tc = P.tex_coords + 6ull * hp;
+                const float w0 = fsub(fsub(1.0f, hu), hv);
+                const float uvx = fadd(fadd(fmul(tc[0], w0), fmul(tc[2], hu)), fmul(tc[4], hv));
+                const float uvy = fadd(fadd(fmul(tc[1], w0), fmul(tc[3], hu)), fmul(tc[5], hv));
+                // TextureMaterial::evaluate (materials/material.rs:44-52)
+                const unsigned long long iu = f32_as_usize(fmul(uvx, __uint2float_rn(P.tex_w))) % P.tex_w;
+                const unsigned long long iv = f32_as_usize(fmul(uvy, __uint2float_rn(P.tex_h))) % P.tex_h;
+                const uint8_t* px = P.texels + 3ull * (iv * P.tex_w + iu);
+                const float sc = 0.00390625f;  // 1 / 256, exact
+                rad = make_float3(fmul(__uint2float_rn(px[0]), sc), fmul(__uint2float_rn(px[1]), sc),
+                                  fmul(__uint2float_rn(px[2]), sc));
             }
             break;
         default:
@@ -724,6 +748,7 @@ cudaError_t launch_triangle_list(bvhgpu_ctx* ctx, const float* tris, uint32_t nt
 
 cudaError_t launch_render(bvhgpu_ctx* ctx, const DeviceBlas& b, const bvhgpu_camera& cam, int w, int h, int acc,
                           const float* acc_params, int shader, const float* shader_params, const float* d_normals,
+                          const float* d_tex_coords, const uint8_t* d_texels, uint32_t tex_w, uint32_t tex_h,
                           uint8_t* d_rgba, cudaStream_t s) {
     RenderParams P;
     std::copy(cam.top_left, cam.top_left + 3, P.cam);
@@ -740,6 +765,10 @@ cudaError_t launch_render(bvhgpu_ctx* ctx, const DeviceBlas& b, const bvhgpu_cam
     P.height = h;
     P.acc_kind = acc;
     P.shader_kind = shader;
+    P.tex_coords = d_tex_coords;
+    P.texels = d_texels;
+    P.tex_w = tex_w;
+    P.tex_h = tex_h;
     GBlas g = to_gblas(b);
     unsigned tiles = (unsigned)(((w + 7) / 8) * ((h + 7) / 8));
     LaunchScope scope(ctx, BVHGPU_K_RENDER, s);

@@ -109,6 +109,7 @@ typedef struct bvhgpu_batch_item {
 #define BVHGPU_ACC_DEPTH 1         /* DepthAccumulator */
 #define BVHGPU_ACC_UV 2            /* UvMappingAccumulator */
 #define BVHGPU_ACC_NORMAL 3        /* NormalMappingAccumulator: params = object transform (16) */
+#define BVHGPU_ACC_TEXTURE 4       /* TextureMaterialAccumulator: bvhgpu_render_textured only */
 #define BVHGPU_SHADER_RADIANCE 0      /* RadianceToRgbShader */
 #define BVHGPU_SHADER_INTERSECTION 1  /* IntersectionShader: params hit rgba, miss rgba */
 #define BVHGPU_SHADER_DEPTH 2         /* DepthMappingShader: params scale, offset */
@@ -323,6 +324,13 @@ int bvhgpu_graph_free(bvhgpu_ctx* ctx, uint32_t graph_id);
 int bvhgpu_render(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhgpu_camera* camera, int width, int height,
                   int accumulator, const float* acc_params, int shader, const float* shader_params,
                   const float* normals, uint8_t* rgba, uint64_t* rays_traced);
+/* TextureMaterialAccumulator (BT/src/renderer.rs:289-334) + shader: the hit's texture coordinate
+ * (per-corner tex_coords, 6 floats per triangle in the BLAS's triangle order, interpolated with the
+ * barycentrics) looks up an RGB8 texture (texels, tex_w x tex_h, row-major) as
+ * TextureMaterial::evaluate does (BT/src/materials/material.rs:44-52: (u * w) as usize % w). */
+int bvhgpu_render_textured(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhgpu_camera* camera, int width, int height,
+                           const float* tex_coords, const uint8_t* texels, uint32_t tex_w, uint32_t tex_h,
+                           int shader, const float* shader_params, uint8_t* rgba, uint64_t* rays_traced);
 
 /* ---- differentiable Lambertian render (not in the reference) ----------------------------------- */
 /* Indexed mesh over a BLAS: triangle i of the BLAS is (verts[faces[3i]], verts[faces[3i+1]],

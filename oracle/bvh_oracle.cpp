@@ -1007,13 +1007,18 @@ void orc_camera_ray(const float corners[9], const float view_inv[16], float u, f
 }
 
 // Accumulator / shader kinds (same values as include/bvhgpu.h).
-enum { ACC_INTERSECTION = 0, ACC_DEPTH = 1, ACC_UV = 2, ACC_NORMAL = 3 };
+enum { ACC_INTERSECTION = 0, ACC_DEPTH = 1, ACC_UV = 2, ACC_NORMAL = 3, ACC_TEXTURE = 4 };
 enum { SH_RADIANCE = 0, SH_INTERSECTION = 1, SH_DEPTH = 2 };
 
 static inline uint8_t rust_f32_as_u8(float x) {
     if (!(x > 0.0f)) return 0;  // NaN and negatives saturate to 0
     if (x >= 255.0f) return 255;
     return (uint8_t)x;
+}
+static inline uint64_t rust_f32_as_usize(float x) {  // saturating, NaN -> 0
+    if (!(x > 0.0f)) return 0;
+    if (x >= 18446744073709551616.0f) return UINT64_MAX;
+    return (uint64_t)x;
 }
 static inline int32_t rust_f32_as_i32(float x) {
     if (x != x) return 0;
@@ -1025,14 +1030,19 @@ static inline int32_t rust_f32_as_i32(float x) {
 // renderer.rs:345-384 (PathTracer::evaluate) with the accumulators of renderer.rs:134-286
 // and the shaders of renderer.rs:116-222.  The frame is w x h with 8x8 tiles; the
 // reference's fixed 80x80 tile grid is the w = h = 640 case.
-int orc_render(const float corners[9], const float view_inv[16], int width, int height, int accumulator,
-               const float* acc_params, int shader, const float* shader_params, const orc_node* nodes,
-               uint32_t nodes_used, const orc_tri* tris, uint32_t ntris, const float* normals, uint8_t* rgba,
-               float* radiance) {
+// TextureMaterialAccumulator (renderer.rs:289-334) reads per-corner texture coordinates (6 floats
+// per triangle) and an RGB8 texture (row-major, tex_w x tex_h) through TextureMaterial::evaluate
+// (materials/material.rs:44-52).
+int orc_render_textured(const float corners[9], const float view_inv[16], int width, int height, int accumulator,
+                        const float* acc_params, int shader, const float* shader_params, const orc_node* nodes,
+                        uint32_t nodes_used, const orc_tri* tris, uint32_t ntris, const float* normals,
+                        const float* tex_coords, const uint8_t* texels, uint32_t tex_w, uint32_t tex_h,
+                        uint8_t* rgba, float* radiance) {
     (void)nodes_used;
     (void)ntris;
     if (width <= 0 || height <= 0 || !nodes || !tris || !rgba) return ORC_ERR_ARG;
     if (accumulator == ACC_NORMAL && !normals) return ORC_ERR_ARG;
+    if (accumulator == ACC_TEXTURE && (!tex_coords || !texels || tex_w == 0 || tex_h == 0)) return ORC_ERR_ARG;
     auto node_at = [nodes](uint32_t i) { return load_node(nodes[i]); };
     auto tri_at = [tris](uint32_t i) { return load_tri(tris[i]); };
     const float* P = acc_params;
@@ -1069,6 +1079,21 @@ int orc_render(const float corners[9], const float view_inv[16], int width, int 
                         V3 nw = xf_vector(P, nm);
                         V3 nz = normalize(nw);
                         rad = muls(add(nz, mk(1.0f, 1.0f, 1.0f)), 0.5f);
+                    }
+                    break;
+                }
+                case ACC_TEXTURE: {
+                    if (hit) {
+                        const float* tc = tex_coords + 6 * (size_t)h.prim;
+                        const float w0 = 1.0f - h.u - h.v;
+                        // tex_coords[0] * (1 - u - v) + tex_coords[1] * u + tex_coords[2] * v
+                        const float uvx = (tc[0] * w0 + tc[2] * h.u) + tc[4] * h.v;
+                        const float uvy = (tc[1] * w0 + tc[3] * h.u) + tc[5] * h.v;
+                        const uint64_t iu = rust_f32_as_usize(uvx * (float)tex_w) % tex_w;
+                        const uint64_t iv = rust_f32_as_usize(uvy * (float)tex_h) % tex_h;
+                        const uint8_t* px = texels + 3 * (iv * tex_w + iu);
+                        const float sc = 1.0f / 256.0f;  // rgb8_to_rgb32f
+                        rad = mk((float)px[0] * sc, (float)px[1] * sc, (float)px[2] * sc);
                     }
                     break;
                 }
@@ -1115,6 +1140,15 @@ int orc_render(const float corners[9], const float view_inv[16], int width, int 
         }
     }
     return ORC_OK;
+}
+
+int orc_render(const float corners[9], const float view_inv[16], int width, int height, int accumulator,
+               const float* acc_params, int shader, const float* shader_params, const orc_node* nodes,
+               uint32_t nodes_used, const orc_tri* tris, uint32_t ntris, const float* normals, uint8_t* rgba,
+               float* radiance) {
+    if (accumulator == ACC_TEXTURE) return ORC_ERR_ARG;
+    return orc_render_textured(corners, view_inv, width, height, accumulator, acc_params, shader, shader_params,
+                               nodes, nodes_used, tris, ntris, normals, nullptr, nullptr, 0, 0, rgba, radiance);
 }
 
 int orc_bounce_ray(const orc_ray* primary, const orc_hit* hit, const orc_tri* tri, uint32_t seed, uint32_t pixel,

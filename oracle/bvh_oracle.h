@@ -93,6 +93,11 @@ int orc_scene_intersect_mt(const orc_tlas_node* tlas, uint32_t tlas_nodes_used,
 void orc_camera_ray(const float corners[9], const float view_inv[16], float u, float v, orc_ray* out);
 /* PathTracer::evaluate over a w x h frame (8x8 tiles, pixel top-left corner samples) on a
  * single BLAS (nobj == 0) or a scene; accumulator / shader kinds as in include/bvhgpu.h. */
+int orc_render_textured(const float corners[9], const float view_inv[16], int width, int height, int accumulator,
+                        const float* acc_params, int shader, const float* shader_params, const orc_node* nodes,
+                        uint32_t nodes_used, const orc_tri* tris, uint32_t ntris, const float* normals,
+                        const float* tex_coords, const uint8_t* texels, uint32_t tex_w, uint32_t tex_h,
+                        uint8_t* rgba, float* radiance);
 int orc_render(const float corners[9], const float view_inv[16], int width, int height,
                int accumulator, const float* acc_params, int shader, const float* shader_params,
                const orc_node* nodes, uint32_t nodes_used, const orc_tri* tris, uint32_t ntris,

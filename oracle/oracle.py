@@ -89,6 +89,7 @@ def lib():
         L.orc_camera_ray.argtypes = [P, P, f32, f32, P]
         L.orc_camera_ray.restype = None
         L.orc_render.argtypes = [P, P, i32, i32, i32, P, i32, P, P, u32, P, u32, P, P, P]
+        L.orc_render_textured.argtypes = [P, P, i32, i32, i32, P, i32, P, P, u32, P, u32, P, P, P, u32, u32, P, P]
         L.orc_bounce_ray.argtypes = [P, P, P, u32, u32, P]
         L.orc_bounce_rays.argtypes = [P, P, u32, P, u32, P, P]
         L.orc_scene_bounce_rays.argtypes = [P, P, P, P, P, P, u32, u32, P, P]
@@ -295,7 +296,8 @@ def camera_ray(corners, view_inv, u, v):
 
 
 def render(corners, view_inv, width, height, nodes, nodes_used, tris, accumulator, shader,
-           acc_params=None, shader_params=None, normals=None):
+           acc_params=None, shader_params=None, normals=None, tex_coords=None, texels=None):
+    """PathTracer::evaluate; texels ([h, w, 3] uint8) and tex_coords ([n, 6]) for accumulator 4."""
     corners = _c(corners, np.float32).reshape(9)
     view_inv = _c(view_inv, np.float32).reshape(16)
     nodes = _c(nodes, NODE)
@@ -305,8 +307,12 @@ def render(corners, view_inv, width, height, nodes, nodes_used, tris, accumulato
     nrm = None if normals is None else _c(normals, np.float32).reshape(-1, 9)
     rgba = np.zeros((height, width, 4), np.uint8)
     rad = np.zeros((height, width, 3), np.float32)
-    rc = lib().orc_render(_p(corners), _p(view_inv), width, height, accumulator, _p(ap), shader, _p(sp),
-                          _p(nodes), nodes_used, _p(tris), len(tris), _p(nrm), _p(rgba), _p(rad))
+    tc = None if tex_coords is None else _c(tex_coords, np.float32).reshape(-1, 6)
+    tx = None if texels is None else _c(texels, np.uint8)
+    th, tw = (0, 0) if tx is None else tx.shape[:2]
+    rc = lib().orc_render_textured(_p(corners), _p(view_inv), width, height, accumulator, _p(ap), shader, _p(sp),
+                                   _p(nodes), nodes_used, _p(tris), len(tris), _p(nrm), _p(tc), _p(tx), tw, th,
+                                   _p(rgba), _p(rad))
     if rc != 0:
         raise RuntimeError(f"oracle render failed ({rc})")
     return rgba, rad

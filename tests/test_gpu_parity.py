@@ -344,6 +344,31 @@ def test_render_shaders_match_oracle(ctx, acc, shader):
     assert (rgba[..., :3] != 0).any()
 
 
+def test_render_texture_material_matches_oracle(ctx):
+    """TextureMaterialAccumulator: per-corner spherical texture coordinates (some outside [0, 1],
+    exercising the `as usize` saturation and the modulo wrap) on an RGB8 texture."""
+    mesh = scenes.displaced_icosphere(4, seed=10)
+    tris0 = mesh.triangles()
+    d = mesh.dirs.astype(np.float64)
+    uv_v = np.stack([np.arctan2(d[:, 2], d[:, 0]) / (2 * np.pi) * 3.0 + 0.5,
+                     np.arccos(np.clip(d[:, 1], -1, 1)) / np.pi * 2.0 - 0.25], 1).astype(np.float32)
+    tc0 = np.ascontiguousarray(uv_v[mesh.faces].reshape(-1, 6))
+    tris = tris0.copy()
+    bvh = bt.BvhBuilder().build_for(tris)
+    order = {t.tobytes(): i for i, t in enumerate(tris0)}
+    tc = tc0[np.array([order[t.tobytes()] for t in tris])]
+    rng = np.random.default_rng(5)
+    texels = rng.integers(0, 256, (37, 53, 3), dtype=np.uint8)
+    blas = ctx.upload_blas(bvh, tris)
+    cam = bt.Camera((-0.5, 0.5, -0.5, 0.5, 1, 100), (0, 0, -3), (0, 0, 1), (-1, 0, 0), (0, 1, 0))
+    rgba, rays = blas.render_textured(cam, 200, 150, tc, texels)
+    ref, _ = orc.render(cam.corners(), cam.view_inv, 200, 150, bvh.nodes, bvh.nodes_used, tris,
+                        bt.ACC_TEXTURE, bt.SHADER_RADIANCE, tex_coords=tc, texels=texels)
+    assert rays == 200 * 150
+    assert np.array_equal(rgba, ref)
+    assert len(np.unique(rgba.reshape(-1, 4), axis=0)) > 100
+
+
 # ---- uneven batch ------------------------------------------------------------------------------------
 
 def test_uneven_batch_persistent_equals_plain_equals_oracle(ctx):
