@@ -25,6 +25,31 @@ assert TLAS_NODE.itemsize == 32 and BATCH_ITEM.itemsize == 16
 TUNE_CONFIG = np.dtype([("block", "<u4"), ("min_blocks", "<u4"), ("stack", "<u4"), ("big_leaf", "<u4"),
                         ("refill", "<u4"), ("reserved", "<u4")])
 BIG_LEAF_NEVER = 0xFFFFFFFF
+RIGID_BODY = np.dtype([("inverse_mass", "<f4"), ("inverse_inertia", "<f4", 9), ("linear_drag", "<f4"),
+                       ("angular_drag", "<f4"), ("position", "<f4", 3), ("orientation", "<f4", 4),
+                       ("velocity", "<f4", 3), ("rotation", "<f4", 3), ("inverse_inertia_world", "<f4", 9),
+                       ("motion", "<f4"), ("is_awake", "<u4"), ("can_sleep", "<u4"), ("transform", "<f4", 16),
+                       ("force_accum", "<f4", 3), ("torque_accum", "<f4", 3), ("acceleration", "<f4", 3),
+                       ("last_frame_acceleration", "<f4", 3)])
+FORCE_GENERATOR = np.dtype([("kind", "<u4"), ("body", "<u4"), ("other", "<u4"), ("reserved", "<u4"),
+                            ("gravity", "<f4", 3), ("spring_point", "<f4", 3), ("other_point", "<f4", 3),
+                            ("spring_constant", "<f4"), ("rest_length", "<f4")])
+assert RIGID_BODY.itemsize == 260 and FORCE_GENERATOR.itemsize == 60
+FORCE_GRAVITY, FORCE_SPRING = 0, 1
+
+
+def rigid_body_default(n=1):
+    """RigidBody::default (physics/rigid_body.rs:98-122): inverse mass f32::MAX, identity inertia,
+    drag 1, orientation unit_z, asleep, can sleep, identity transform."""
+    b = np.zeros(n, RIGID_BODY)
+    b["inverse_mass"] = np.finfo(np.float32).max
+    b["inverse_inertia"] = np.eye(3, dtype=np.float32).reshape(9)
+    b["inverse_inertia_world"] = np.eye(3, dtype=np.float32).reshape(9)
+    b["linear_drag"] = b["angular_drag"] = 1.0
+    b["orientation"] = (0.0, 0.0, 0.0, 1.0)
+    b["can_sleep"] = 1
+    b["transform"] = np.eye(4, dtype=np.float32).reshape(16)
+    return b
 
 
 class TuneJob(ctypes.Structure):
@@ -134,6 +159,13 @@ SIGNATURES = {
     "bvhgpu_tune_set": (_I, [_P, _I, _P]),
     "bvhgpu_tune_space": (_I, [_I, _P, _U32, _P]),
     "bvhgpu_autotune": (_I, [_P, _P, _U32, _P, _P]),
+    "bvhgpu_world_create": (_I, [_P, _P, _U32, _P, _U32, _P]),
+    "bvhgpu_world_free": (_I, [_P, _U32]),
+    "bvhgpu_world_start_frame_async": (_I, [_P, _U32, _P]),
+    "bvhgpu_world_step_async": (_I, [_P, _U32, ctypes.c_float, _P]),
+    "bvhgpu_world_download": (_I, [_P, _U32, _P]),
+    "bvhgpu_scene_bind_world": (_I, [_P, _U32, _U32, _P, _P]),
+    "bvhgpu_scene_run_async": (_I, [_P, _U32, ctypes.c_float, _P]),
     "bvhgpu_refit_noalloc": (_I, [_P, _U32, _P, _U32, _P, _P]),
 }
 

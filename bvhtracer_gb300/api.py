@@ -143,6 +143,9 @@ class Context:
         bvh = Bvh(nodes, used.value)
         return (bvh, p) if perm else bvh
 
+    def world(self, bodies, gens=None) -> "World":
+        return World(self, bodies, gens)
+
     def triangles_intersect(self, tris: np.ndarray, rays: np.ndarray, mode: int = _lib.LIST_CLOSEST) -> np.ndarray:
         """Triangle::intersect (mode LIST_CLOSEST) or Triangle::intersect_mut (LIST_MUT) of every ray
         against a triangle list in index order, no BVH."""
@@ -199,6 +202,36 @@ class Context:
         ms = ctypes.c_float()
         self.check(self.lib.bvhgpu_autotune(self.h, ctypes.byref(job), reps, ptr(best), ctypes.byref(ms)))
         return {k: int(best[0][k]) for k in _lib.TUNE_CONFIG.names if k != "reserved"}, float(ms.value)
+
+
+class World:
+    """World (physics/world.rs): rigid bodies and force generators on the device."""
+
+    def __init__(self, ctx: "Context", bodies, gens=None):
+        self.ctx = ctx
+        self.bodies = np.ascontiguousarray(bodies, _lib.RIGID_BODY)
+        g = np.ascontiguousarray(gens if gens is not None else np.zeros(0, _lib.FORCE_GENERATOR),
+                                 _lib.FORCE_GENERATOR)
+        wid = ctypes.c_uint32()
+        ctx.check(ctx.lib.bvhgpu_world_create(ctx.h, ptr(self.bodies), len(self.bodies), ptr(g), len(g),
+                                              ctypes.byref(wid)))
+        self.id = wid.value
+
+    def start_frame_async(self, stream=None):
+        self.ctx.check(self.ctx.lib.bvhgpu_world_start_frame_async(self.ctx.h, self.id, stream))
+
+    def step_async(self, dt: float, stream=None):
+        self.ctx.check(self.ctx.lib.bvhgpu_world_step_async(self.ctx.h, self.id, dt, stream))
+
+    def download(self) -> np.ndarray:
+        out = np.zeros(len(self.bodies), _lib.RIGID_BODY)
+        self.ctx.check(self.ctx.lib.bvhgpu_world_download(self.ctx.h, self.id, ptr(out)))
+        return out
+
+    def free(self):
+        if self.id:
+            self.ctx.lib.bvhgpu_world_free(self.ctx.h, self.id)
+            self.id = 0
 
 
 def decode_mesh(data, fmt: int = _lib.MESH_TRI):
@@ -498,6 +531,17 @@ class Scene:
         self.ctx.check(self.ctx.lib.bvhgpu_scene_animate_async(self.ctx.h, self.id, d_rot0.ptr, d_axis.ptr,
                                                                d_omega.ptr, d_scale.ptr, d_trans.ptr, d_time.ptr,
                                                                stream))
+
+    def bind_world(self, world: "World", body_of, transform_init):
+        """Object i follows body body_of[i] (0xFFFFFFFF: none) from initial transform
+        transform_init[i] (16 floats, column-major)."""
+        bo = np.ascontiguousarray(body_of, np.uint32)
+        ti = np.ascontiguousarray(transform_init, np.float32).reshape(-1, 16)
+        self.ctx.check(self.ctx.lib.bvhgpu_scene_bind_world(self.ctx.h, self.id, world.id, ptr(bo), ptr(ti)))
+
+    def run_async(self, dt: float, stream=None):
+        """Scene::run(dt): physics step, object transforms from the bodies, TLAS rebuild."""
+        self.ctx.check(self.ctx.lib.bvhgpu_scene_run_async(self.ctx.h, self.id, dt, stream))
 
     def download_tlas(self):
         nodes = np.zeros(2 * self.nobjects, TLAS_NODE)

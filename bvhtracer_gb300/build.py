@@ -21,7 +21,7 @@ GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-prec-div=true", "-prec-sqrt=true",
               "-ftz=false", "-Xcompiler", "-fPIC,-ffp-contract=off,-fno-fast-math", "-Xptxas", "-v"]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-Wall"]
-CU_SOURCES = ["api.cu", "kernels_trace.cu", "kernels_scene.cu", "kernels_adjoint.cu", "refit_noalloc.cu", "tune.cu", "build_gpu.cu"]
+CU_SOURCES = ["api.cu", "kernels_trace.cu", "kernels_scene.cu", "kernels_adjoint.cu", "refit_noalloc.cu", "tune.cu", "build_gpu.cu", "physics.cu"]
 CPP_SOURCES = ["host_build.cpp", "loaders.cpp"]
 
 

@@ -144,6 +144,8 @@ DeviceMesh* find_mesh(bvhgpu_ctx* ctx, uint32_t id) {
 void free_scene(DeviceScene& s) {
     cudaFree(s.xf);
     cudaFree(s.inv);
+    cudaFree(s.body_of);
+    cudaFree(s.transform_init);
     cudaFree(s.obj_blas);
     cudaFree(s.blas_table);
     cudaFree(s.tlas);
@@ -247,6 +249,7 @@ int bvhgpu_destroy(bvhgpu_ctx* ctx) {
     for (auto& kv : ctx->blas) free_blas(kv.second);
     for (auto& kv : ctx->scenes) free_scene(kv.second);
     for (auto& kv : ctx->meshes) free_mesh(kv.second);
+    bvhgpu_free_worlds(ctx);
     for (auto& kv : ctx->graphs) {
         cudaGraphExecDestroy(kv.second.second);
         cudaGraphDestroy(kv.second.first);

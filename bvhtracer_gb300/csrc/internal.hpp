@@ -46,6 +46,17 @@ struct DeviceScene {
     float4* tlas = nullptr;    // 2 float4 per TLAS node (2*nobjects nodes)
     uint32_t tlas_nodes_used = 0;
     uint32_t tlas_depth_cap = 0;
+    uint32_t world = 0;              // bound physics world (0: none)
+    uint32_t* body_of = nullptr;     // per object: body index or 0xFFFFFFFF
+    float* transform_init = nullptr; // 16 per object
+};
+
+struct DeviceWorld {
+    bvhgpu_rigid_body* bodies = nullptr;
+    uint32_t nbodies = 0;
+    bvhgpu_force_generator* gens = nullptr;  // grouped by body, registry order kept within a body
+    uint32_t* gen_off = nullptr;             // nbodies + 1
+    uint32_t ngens = 0;
 };
 
 struct DeviceMesh {
@@ -76,6 +87,8 @@ struct bvhgpu_ctx {
     std::map<uint32_t, bvhgpu::DeviceBlas> blas;
     std::map<uint32_t, bvhgpu::DeviceScene> scenes;
     std::map<uint32_t, bvhgpu::DeviceMesh> meshes;
+    std::map<uint32_t, bvhgpu::DeviceWorld> worlds;
+    uint32_t next_world = 1;
     uint32_t next_blas = 1;
     uint32_t next_scene = 1;
     uint32_t next_mesh = 1;
@@ -118,6 +131,9 @@ struct bvhgpu_ctx {
     }
 };
 
+// Frees every physics world of the context (physics.cu).
+void bvhgpu_free_worlds(bvhgpu_ctx* ctx);
+
 namespace bvhgpu {
 
 // Launch bracket for per-kernel timing.
@@ -152,6 +168,10 @@ cudaError_t launch_render(bvhgpu_ctx* ctx, const DeviceBlas& b, const bvhgpu_cam
 // ---- launchers (kernels_scene.cu) ------------------------------------------------------
 cudaError_t launch_write_tris(bvhgpu_ctx* ctx, DeviceBlas& b, const float* d_tris9, cudaStream_t s);
 cudaError_t launch_refit(bvhgpu_ctx* ctx, DeviceBlas& b, cudaStream_t s);
+// Physics (physics.cu).
+cudaError_t launch_world_start_frame(bvhgpu_ctx* ctx, DeviceWorld& w, cudaStream_t s);
+cudaError_t launch_world_step(bvhgpu_ctx* ctx, DeviceWorld& w, float dt, cudaStream_t s);
+cudaError_t launch_update_from_bodies(bvhgpu_ctx* ctx, DeviceScene& sc, const DeviceWorld& w, cudaStream_t s);
 // BvhBuilder::build_for on the device (build_gpu.cu): mesh (host, n x 9 floats) is reordered in
 // place, nodes_out (2n) and perm_out (optional) written; *what names a failure.
 int build_bvh_device(bvhgpu_ctx* ctx, float* mesh, uint32_t n, bvhgpu_node* nodes_out, uint32_t* nodes_used,

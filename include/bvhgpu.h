@@ -423,6 +423,51 @@ typedef struct bvhgpu_tune_job {
 int bvhgpu_autotune(bvhgpu_ctx* ctx, const bvhgpu_tune_job* job, uint32_t reps, bvhgpu_tune_config* best,
                     float* best_ms);
 
+/* ---- rigid-body physics driving instance transforms (BT/src/physics/, scene.rs:40-50) ---------- */
+/* RigidBody (physics/rigid_body.rs:74-122) as a plain struct; matrices column-major [col][row]. */
+typedef struct bvhgpu_rigid_body {
+    float inverse_mass;
+    float inverse_inertia[9];        /* body space */
+    float linear_drag, angular_drag;
+    float position[3];
+    float orientation[4];            /* quaternion s, x, y, z */
+    float velocity[3];
+    float rotation[3];               /* angular velocity */
+    float inverse_inertia_world[9];
+    float motion;
+    uint32_t is_awake, can_sleep;
+    float transform[16];             /* body space to world space */
+    float force_accum[3], torque_accum[3];
+    float acceleration[3], last_frame_acceleration[3];
+} bvhgpu_rigid_body;
+/* ForceGenerator (physics/force_generator.rs): Gravity (gravity), or Spring from `body`'s
+ * spring_point to `other`'s other_point (body-space points) with spring_constant, rest_length. */
+#define BVHGPU_FORCE_GRAVITY 0
+#define BVHGPU_FORCE_SPRING 1
+typedef struct bvhgpu_force_generator {
+    uint32_t kind, body, other, reserved;
+    float gravity[3];
+    float spring_point[3];
+    float other_point[3];
+    float spring_constant, rest_length;
+} bvhgpu_force_generator;
+/* World (physics/world.rs): bodies and the force registry, in registration order. */
+int bvhgpu_world_create(bvhgpu_ctx* ctx, const bvhgpu_rigid_body* bodies, uint32_t nbodies,
+                        const bvhgpu_force_generator* gens, uint32_t ngens, uint32_t* world_id);
+int bvhgpu_world_free(bvhgpu_ctx* ctx, uint32_t world_id);
+/* World::start_frame: clear the accumulators and RigidBody::calculate_derived_data. */
+int bvhgpu_world_start_frame_async(bvhgpu_ctx* ctx, uint32_t world_id, bvhgpu_stream s);
+/* World::run_physics(dt): the registry's forces, then RigidBody::integrate (Newton-Euler). */
+int bvhgpu_world_step_async(bvhgpu_ctx* ctx, uint32_t world_id, float dt, bvhgpu_stream s);
+int bvhgpu_world_download(bvhgpu_ctx* ctx, uint32_t world_id, bvhgpu_rigid_body* bodies_out);
+/* Binds scene objects to bodies: object i follows body body_of[i] (0xFFFFFFFF: none) with its
+ * initial transform transform_init[16 i..] (SceneObjectBuilder::with_transform). */
+int bvhgpu_scene_bind_world(bvhgpu_ctx* ctx, uint32_t scene_id, uint32_t world_id, const uint32_t* body_of,
+                            const float* transform_init);
+/* Scene::run(dt) (scene.rs:40-50): World::run_physics, SceneObject::update_transform of every bound
+ * object (body transform * initial transform, and its inverse), Scene::rebuild.  Capturable. */
+int bvhgpu_scene_run_async(bvhgpu_ctx* ctx, uint32_t scene_id, float dt, bvhgpu_stream s);
+
 /* ---- refit without allocation ----------------------------------------------------------------- */
 /* No counterpart in the reference.  For callers that cannot call cudaMalloc: engines that own all
  * device memory through a pool reserved at start-up, or latency-critical threads on which a driver

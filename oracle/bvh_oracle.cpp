@@ -877,6 +877,201 @@ int orc_triangles_intersect(const orc_tri* mesh, uint32_t ntris, const orc_ray* 
     return ORC_OK;
 }
 
+// ---- rigid-body physics (BT/src/physics/) -------------------------------------------------------
+// Same operation order as the reference; f32 throughout.  powf is the host math library's (the
+// reference calls f32::powf, i.e. the platform's powf); drag 1 and can_sleep false never reach it.
+
+static void rb_point_to_world(const float* m, const float* p, float* out) {  // Transform3::transform_point
+    for (int r = 0; r < 3; ++r) out[r] = ((m[r] * p[0] + m[4 + r] * p[1]) + m[8 + r] * p[2]) + m[12 + r] * 1.0f;
+}
+static float rb_mag(const float* v) { return std::sqrt((v[0] * v[0] + v[1] * v[1]) + v[2] * v[2]); }
+
+// RigidBody::apply_force_at_point (rigid_body.rs:434-440)
+static void rb_force_at_point(orc_rigid_body& b, const float* f, const float* p) {
+    const float cm[3] = {p[0] - b.position[0], p[1] - b.position[1], p[2] - b.position[2]};
+    for (int k = 0; k < 3; ++k) b.force_accum[k] += f[k];
+    const float t[3] = {cm[1] * f[2] - cm[2] * f[1], cm[2] * f[0] - cm[0] * f[2], cm[0] * f[1] - cm[1] * f[0]};
+    for (int k = 0; k < 3; ++k) b.torque_accum[k] += t[k];
+    b.is_awake = 1;
+}
+
+// RigidBody::calculate_derived_data (rigid_body.rs:132-146), Transform3::from_translation_rotation
+// (transform.rs:190-217), _transform_inertia_tensor (rigid_body.rs:30-70)
+static void rb_derived(orc_rigid_body& b) {
+    float* q = b.orientation;
+    const float m = std::sqrt(((q[0] * q[0] + q[1] * q[1]) + q[2] * q[2]) + q[3] * q[3]);
+    for (int k = 0; k < 4; ++k) q[k] = q[k] / m;
+    const float s = q[0], x = q[1], y = q[2], z = q[3], one = 1.0f, two = one + one, zero = 0.0f;
+    float rot[4][4];  // [col][row]
+    rot[0][0] = one - two * y * y - two * z * z;
+    rot[0][1] = two * x * y + two * s * z;
+    rot[0][2] = two * x * z - two * s * y;
+    rot[0][3] = zero;
+    rot[1][0] = two * x * y - two * s * z;
+    rot[1][1] = one - two * x * x - two * z * z;
+    rot[1][2] = two * y * z + two * s * x;
+    rot[1][3] = zero;
+    rot[2][0] = two * x * z + two * s * y;
+    rot[2][1] = two * y * z - two * s * x;
+    rot[2][2] = one - two * x * x - two * y * y;
+    rot[2][3] = zero;
+    rot[3][0] = b.position[0];
+    rot[3][1] = b.position[1];
+    rot[3][2] = b.position[2];
+    rot[3][3] = one;
+    for (int c = 0; c < 4; ++c)
+        for (int r = 0; r < 4; ++r) b.transform[4 * c + r] = rot[c][r];
+    float iit[3][3];  // [col][row]
+    for (int c = 0; c < 3; ++c)
+        for (int r = 0; r < 3; ++r) iit[c][r] = b.inverse_inertia[3 * c + r];
+    const float m00 = rot[0][0] * iit[0][0] + rot[1][0] * iit[0][1] + rot[2][0] * iit[0][2];
+    const float m10 = rot[0][0] * iit[1][0] + rot[1][0] * iit[1][1] + rot[2][0] * iit[1][2];
+    const float m20 = rot[0][0] * iit[2][0] + rot[1][0] * iit[2][1] + rot[2][0] * iit[2][2];
+    const float m01 = rot[0][1] * iit[0][0] + rot[1][1] * iit[0][1] + rot[2][1] * iit[0][2];
+    const float m11 = rot[0][1] * iit[1][0] + rot[1][1] * iit[1][1] + rot[2][1] * iit[1][2];
+    const float m21 = rot[0][1] * iit[2][0] + rot[1][1] * iit[2][1] + rot[2][1] * iit[2][2];
+    const float m02 = rot[0][2] * iit[0][0] + rot[1][2] * iit[0][1] + rot[2][2] * iit[0][2];
+    const float m12 = rot[0][2] * iit[1][0] + rot[1][2] * iit[1][1] + rot[2][2] * iit[1][2];
+    const float m22 = rot[0][2] * iit[2][0] + rot[1][2] * iit[2][1] + rot[2][2] * iit[2][2];
+    float w[3][3];
+    w[0][0] = m00 * rot[0][0] + m10 * rot[1][0] + m20 * rot[2][0];
+    w[1][0] = m00 * rot[0][1] + m10 * rot[1][1] + m20 * rot[2][1];
+    w[2][0] = m00 * rot[0][2] + m10 * rot[1][2] + m20 * rot[2][2];
+    w[0][1] = m01 * rot[0][0] + m11 * rot[1][0] + m21 * rot[2][0];
+    w[1][1] = m01 * rot[0][1] + m11 * rot[1][1] + m21 * rot[2][1];
+    w[2][1] = m01 * rot[0][2] + m11 * rot[1][2] + m21 * rot[2][2];
+    w[0][2] = m02 * rot[0][0] + m12 * rot[1][0] + m22 * rot[2][0];
+    w[1][2] = m02 * rot[0][1] + m12 * rot[1][1] + m22 * rot[2][1];
+    w[2][2] = m02 * rot[0][2] + m12 * rot[1][2] + m22 * rot[2][2];
+    for (int c = 0; c < 3; ++c)
+        for (int r = 0; r < 3; ++r) b.inverse_inertia_world[3 * c + r] = w[c][r];
+}
+
+int orc_world_start_frame(orc_rigid_body* bodies, uint32_t n) {  // world.rs:43-48
+    for (uint32_t i = 0; i < n; ++i) {
+        for (int k = 0; k < 3; ++k) bodies[i].force_accum[k] = bodies[i].torque_accum[k] = 0.0f;
+        rb_derived(bodies[i]);
+    }
+    return ORC_OK;
+}
+
+// World::run_physics (world.rs:56-59): ForceRegistry::apply_forces in registry order
+// (force_registry.rs:73-77, force_generator.rs:52-59, 133-154), then RigidBody::integrate
+// (rigid_body.rs:149-213) of every body.
+int orc_world_step(orc_rigid_body* bodies, uint32_t n, const orc_force_generator* gens, uint32_t ngens, float d) {
+    for (uint32_t g = 0; g < ngens; ++g) {
+        const orc_force_generator& G = gens[g];
+        if (G.body >= n) return ORC_ERR_ARG;
+        orc_rigid_body& b = bodies[G.body];
+        if (G.kind == 0) {
+            if (b.inverse_mass >= 0.0f) {
+                const float mass = b.inverse_mass == 0.0f ? FLT_MAX : 1.0f / b.inverse_mass;
+                for (int k = 0; k < 3; ++k) b.force_accum[k] += G.gravity[k] * mass;
+                b.is_awake = 1;
+            }
+        } else {
+            if (G.other >= n) return ORC_ERR_ARG;
+            float lws[3], ows[3];
+            rb_point_to_world(b.transform, G.spring_point, lws);
+            rb_point_to_world(bodies[G.other].transform, G.other_point, ows);
+            const float disp[3] = {lws[0] - ows[0], lws[1] - ows[1], lws[2] - ows[2]};
+            const float len = rb_mag(disp);
+            const float fm = G.spring_constant * std::fabs(len - G.rest_length);
+            const float m = rb_mag(disp);
+            const float f[3] = {(disp[0] / m) * (-fm), (disp[1] / m) * (-fm), (disp[2] / m) * (-fm)};
+            rb_force_at_point(b, f, lws);
+        }
+    }
+    for (uint32_t i = 0; i < n; ++i) {
+        orc_rigid_body& b = bodies[i];
+        if (!b.is_awake) continue;
+        for (int k = 0; k < 3; ++k) b.last_frame_acceleration[k] = b.acceleration[k] + b.force_accum[k] * b.inverse_mass;
+        const float* W = b.inverse_inertia_world;
+        float aa[3];
+        for (int r = 0; r < 3; ++r) aa[r] = (W[r] * b.torque_accum[0] + W[3 + r] * b.torque_accum[1]) + W[6 + r] * b.torque_accum[2];
+        for (int k = 0; k < 3; ++k) {
+            b.velocity[k] += b.last_frame_acceleration[k] * d;
+            b.rotation[k] += aa[k] * d;
+        }
+        const float ld = std::pow(b.linear_drag, d), ad = std::pow(b.angular_drag, d);
+        for (int k = 0; k < 3; ++k) {
+            b.velocity[k] *= ld;
+            b.rotation[k] *= ad;
+        }
+        for (int k = 0; k < 3; ++k) b.position[k] += b.velocity[k] * d;
+        // q = from_pure(rotation * d) * orientation (Hamilton product); orientation += q * 1/2
+        const float p1 = b.rotation[0] * d, p2 = b.rotation[1] * d, p3 = b.rotation[2] * d, p0 = 0.0f;
+        float* o = b.orientation;
+        const float s2 = o[0], x2 = o[1], y2 = o[2], z2 = o[3];
+        const float qs = p0 * s2 - p1 * x2 - p2 * y2 - p3 * z2;
+        const float qx = p0 * x2 + p1 * s2 + p2 * z2 - p3 * y2;
+        const float qy = p0 * y2 - p1 * z2 + p2 * s2 + p3 * x2;
+        const float qz = p0 * z2 + p1 * y2 - p2 * x2 + p3 * s2;
+        const float half = 0.5f;
+        o[0] += qs * half;
+        o[1] += qx * half;
+        o[2] += qy * half;
+        o[3] += qz * half;
+        rb_derived(b);
+        for (int k = 0; k < 3; ++k) b.force_accum[k] = b.torque_accum[k] = 0.0f;
+        if (b.can_sleep) {
+            const float* v = b.velocity;
+            const float* r = b.rotation;
+            const float cur = ((v[0] * v[0] + v[1] * v[1]) + v[2] * v[2]) + ((r[0] * r[0] + r[1] * r[1]) + r[2] * r[2]);
+            const float bias = std::pow(0.5f, d);
+            b.motion = bias * b.motion + (1.0f - bias) * cur;
+            const float thr = 0.3f, ten = 10.0f;
+            if (b.motion < thr) {
+                b.is_awake = 0;
+                for (int k = 0; k < 3; ++k) b.velocity[k] = b.rotation[k] = 0.0f;
+            } else if (b.motion > ten * thr) {
+                b.motion = ten * thr;
+            }
+        }
+    }
+    return ORC_OK;
+}
+
+// 3x3 determinant of rows rr, columns cc of a column-major 4x4, by the first row.
+static float rb_det3(const float* m, const int* rr, const int* cc) {
+    auto e = [&](int r, int c) { return m[4 * c + r]; };
+    return (e(rr[0], cc[0]) * (e(rr[1], cc[1]) * e(rr[2], cc[2]) - e(rr[1], cc[2]) * e(rr[2], cc[1])) -
+            e(rr[0], cc[1]) * (e(rr[1], cc[0]) * e(rr[2], cc[2]) - e(rr[1], cc[2]) * e(rr[2], cc[0]))) +
+           e(rr[0], cc[2]) * (e(rr[1], cc[0]) * e(rr[2], cc[1]) - e(rr[1], cc[1]) * e(rr[2], cc[0]));
+}
+
+// SceneObject::update_transform (scene_object.rs:52-58): body transform * initial transform; its
+// inverse by cofactors (the reference's Matrix4x4::inverse is not pinned by any test).
+int orc_object_transforms(const orc_rigid_body* bodies, const uint32_t* body_of, const float* init, uint32_t nobj,
+                          float* xf, float* inv) {
+    for (uint32_t i = 0; i < nobj; ++i) {
+        if (body_of[i] == 0xFFFFFFFFu) continue;
+        const float* A = bodies[body_of[i]].transform;
+        const float* B = init + 16 * (size_t)i;
+        float P[16];
+        for (int c = 0; c < 4; ++c)
+            for (int r = 0; r < 4; ++r)
+                P[4 * c + r] = ((A[r] * B[4 * c] + A[4 + r] * B[4 * c + 1]) + A[8 + r] * B[4 * c + 2]) +
+                               A[12 + r] * B[4 * c + 3];
+        float cof[16];
+        for (int r = 0; r < 4; ++r)
+            for (int c = 0; c < 4; ++c) {
+                int rr[3], cc[3];
+                for (int k = 0, j = 0; k < 4; ++k)
+                    if (k != r) rr[j++] = k;
+                for (int k = 0, j = 0; k < 4; ++k)
+                    if (k != c) cc[j++] = k;
+                const float d3 = rb_det3(P, rr, cc);
+                cof[4 * r + c] = ((r + c) & 1) ? -d3 : d3;
+            }
+        const float det = ((P[0] * cof[0] + P[1] * cof[4]) + P[2] * cof[8]) + P[3] * cof[12];
+        for (int k = 0; k < 16; ++k) xf[16 * (size_t)i + k] = P[k];
+        for (int r = 0; r < 4; ++r)
+            for (int c = 0; c < 4; ++c) inv[16 * (size_t)i + 4 * c + r] = cof[4 * c + r] / det;
+    }
+    return ORC_OK;
+}
+
 // bvh.rs:469-493
 int orc_bvh_refit(orc_node* nodes, uint32_t nodes_used, const orc_tri* mesh, uint32_t n) {
     if (!nodes || !mesh) return ORC_ERR_ARG;

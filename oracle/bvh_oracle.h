@@ -54,6 +54,35 @@ int orc_bvh_intersect(const orc_node* nodes, uint32_t nodes_used, const orc_tri*
  * Triangle::intersect_mut on one Intersection per ray. */
 int orc_triangles_intersect(const orc_tri* mesh, uint32_t ntris, const orc_ray* rays, uint32_t nrays, int mode,
                             orc_hit* hits);
+/* Rigid bodies (BT/src/physics/rigid_body.rs) and force generators (force_generator.rs); the same
+ * layout as the library's bvhgpu_rigid_body / bvhgpu_force_generator. */
+typedef struct {
+    float inverse_mass;
+    float inverse_inertia[9];
+    float linear_drag, angular_drag;
+    float position[3];
+    float orientation[4];
+    float velocity[3];
+    float rotation[3];
+    float inverse_inertia_world[9];
+    float motion;
+    uint32_t is_awake, can_sleep;
+    float transform[16];
+    float force_accum[3], torque_accum[3];
+    float acceleration[3], last_frame_acceleration[3];
+} orc_rigid_body;
+typedef struct {
+    uint32_t kind, body, other, reserved;
+    float gravity[3];
+    float spring_point[3];
+    float other_point[3];
+    float spring_constant, rest_length;
+} orc_force_generator;
+/* World::start_frame, World::run_physics(dt) (registry order), SceneObject::update_transform. */
+int orc_world_start_frame(orc_rigid_body* bodies, uint32_t n);
+int orc_world_step(orc_rigid_body* bodies, uint32_t n, const orc_force_generator* gens, uint32_t ngens, float dt);
+int orc_object_transforms(const orc_rigid_body* bodies, const uint32_t* body_of, const float* init, uint32_t nobj,
+                          float* xf, float* inv);
 /* Two smallest hit distances per ray over the whole BVH (FLT_MAX where there is none). */
 int orc_two_nearest_mt(const orc_node* nodes, const orc_tri* mesh, const orc_ray* rays, uint32_t nrays, float* t1,
                        float* t2, int nthreads);

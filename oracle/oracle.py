@@ -78,6 +78,9 @@ def lib():
         L.orc_bvh_intersect_mt.argtypes = [P, u32, P, u32, P, u32, P, i32]
         L.orc_two_nearest_mt.argtypes = [P, P, P, u32, P, P, i32]
         L.orc_triangles_intersect.argtypes = [P, u32, P, u32, i32, P]
+        L.orc_world_start_frame.argtypes = [P, u32]
+        L.orc_world_step.argtypes = [P, u32, P, u32, ctypes.c_float]
+        L.orc_object_transforms.argtypes = [P, P, P, u32, P, P]
         L.orc_bvh_refit.argtypes = [P, u32, P, u32]
         L.orc_bvh_depth.argtypes = [P, u32]
         L.orc_bvh_depth.restype = u32
@@ -188,6 +191,27 @@ def triangles_intersect(tris, rays, mode=0):
     hits = np.zeros(len(rays), HIT)
     assert lib().orc_triangles_intersect(_p(tris), len(tris), _p(rays), len(rays), mode, _p(hits)) == 0
     return hits
+
+
+def world_start_frame(bodies):
+    """World::start_frame on a structured array of rigid bodies (modified in place)."""
+    assert lib().orc_world_start_frame(_p(bodies), len(bodies)) == 0
+
+
+def world_step(bodies, gens, dt):
+    """World::run_physics(dt) in place: the registry's forces in order, then integrate."""
+    g = np.ascontiguousarray(gens)
+    assert lib().orc_world_step(_p(bodies), len(bodies), _p(g) if len(g) else None, len(g), float(dt)) == 0
+
+
+def object_transforms(bodies, body_of, init):
+    """SceneObject::update_transform: (xf, inv) [nobj, 16], body transform * initial transform."""
+    body_of = _c(body_of, np.uint32)
+    init = _c(init, np.float32).reshape(-1, 16)
+    xf = init.copy()
+    inv = np.zeros_like(init)
+    assert lib().orc_object_transforms(_p(bodies), _p(body_of), _p(init), len(body_of), _p(xf), _p(inv)) == 0
+    return xf, inv
 
 
 def two_nearest(nodes, tris, rays, threads=8):
