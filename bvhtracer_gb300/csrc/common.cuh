@@ -453,16 +453,19 @@ __device__ __forceinline__ PairHit ray_terms(const PairData& p, const OriginTerm
 }
 
 // Running best of one ray inside a cooperative leaf test (triangle index order kept: a pair's
-// triangle A before B, strict `<`).
+// triangle A before B, strict `<`).  Only t and the triangle are kept; the winner's u, v are
+// recomputed once after the warp reduction (reduce_and_take).
 struct Best {
-    float t, u, v;
+    float t;
     uint32_t k;
     __device__ __forceinline__ void take(const PairHit& h, uint32_t kA) {
         if (h.okA && h.tA < t) {
-            t = h.tA; u = h.uA; v = h.vA; k = kA;
+            t = h.tA;
+            k = kA;
         }
         if (h.okB && h.tB < t) {
-            t = h.tB; u = h.uB; v = h.vB; k = kA + 1u;
+            t = h.tB;
+            k = kA + 1u;
         }
     }
 };
@@ -484,9 +487,19 @@ __device__ __forceinline__ CoopRay bcast_ray(const LaneRay& r, int src) {
     return c;
 }
 
+// Triangle k of the pair layout as {v0, e1, e2} (component c of triangle k at float 20 (k/2) + 2c + k%2).
+__device__ __forceinline__ void load_pair_tri(const ulonglong2* __restrict__ pairs, uint32_t k, float4& v0, float4& e1,
+                                              float4& e2) {
+    const float* P = reinterpret_cast<const float*>(pairs) + 20ull * (k >> 1) + (k & 1u);
+    v0 = make_float4(__ldg(P), __ldg(P + 2), __ldg(P + 4), 0.0f);
+    e1 = make_float4(__ldg(P + 6), __ldg(P + 8), __ldg(P + 10), 0.0f);
+    e2 = make_float4(__ldg(P + 12), __ldg(P + 14), __ldg(P + 16), 0.0f);
+}
+
 // Warp argmin of (t, k) -- minimum t, ties to the lowest triangle index -- then lane `src` takes
-// the hit (u, v come from the lane that tested the winning triangle).
-__device__ __forceinline__ void reduce_and_take(Best b, uint32_t pbeg, int src, LaneRay& r) {
+// the hit.  Its u, v are recomputed by the scalar test (tri_test: per element the same
+// operations as the packed pair test, so t, u, v are the ones the loop saw).
+__device__ __forceinline__ void reduce_and_take(Best b, const ulonglong2* __restrict__ pairs, int src, LaneRay& r) {
     const unsigned kAll = 0xFFFFFFFFu;
     const unsigned lane = threadIdx.x & 31u;
     float bt = b.t;
@@ -500,18 +513,17 @@ __device__ __forceinline__ void reduce_and_take(Best b, uint32_t pbeg, int src, 
             bk = ok;
         }
     }
-    if (bk != 0xFFFFFFFFu) {
-        const int owner = (int)(((bk >> 1) - pbeg) & 31u);
-        float wu = __shfl_sync(kAll, b.u, owner);
-        float wv = __shfl_sync(kAll, b.v, owner);
-        if ((int)lane == src) {
-            r.ct = bt;
-            r.hu = wu;
-            r.hv = wv;
-            r.hp = bk;
-            r.hit = true;
-            r.inst = r.inst_cur;
-        }
+    if (bk != 0xFFFFFFFFu && (int)lane == src) {
+        float4 v0, e1, e2;
+        load_pair_tri(pairs, bk, v0, e1, e2);
+        float t, u, v;
+        tri_test(v0, e1, e2, r.o, r.d, t, u, v);
+        r.ct = bt;
+        r.hu = u;
+        r.hv = v;
+        r.hp = bk;
+        r.hit = true;
+        r.inst = r.inst_cur;
     }
 }
 
@@ -531,14 +543,14 @@ __device__ __forceinline__ void coop_leaf(const ulonglong2* __restrict__ pairs, 
     const f2 Z = f2_neg_zero();
     const uint32_t end = first + cnt;
     const uint32_t pbeg = first >> 1, pend = (end + 1) >> 1;
-    Best b{c.ct, 0.0f, 0.0f, 0xFFFFFFFFu};
+    Best b{c.ct, 0xFFFFFFFFu};
     for (uint32_t p = pbeg + lane; p < pend; p += 32u) {
         const uint32_t kA = 2u * p;
         PairData pd = load_pair(pairs + 5ull * p);
         OriginTerms ot = origin_terms(pd, OX, OY, OZ, Z);
         b.take(ray_terms(pd, ot, DX, DY, DZ, Z, kA >= first, kA + 1u < end), kA);
     }
-    reduce_and_take(b, pbeg, src, r);
+    reduce_and_take(b, pairs, src, r);
 }
 
 // Two rays (lanes srcA, srcB) waiting on the same leaf: each loaded pair is tested against both,
@@ -558,8 +570,8 @@ __device__ __forceinline__ void coop_leaf2(const ulonglong2* __restrict__ pairs,
     const f2 Z = f2_neg_zero();
     const uint32_t end = first + cnt;
     const uint32_t pbeg = first >> 1, pend = (end + 1) >> 1;
-    Best ba{ca.ct, 0.0f, 0.0f, 0xFFFFFFFFu};
-    Best bb{cb.ct, 0.0f, 0.0f, 0xFFFFFFFFu};
+    Best ba{ca.ct, 0xFFFFFFFFu};
+    Best bb{cb.ct, 0xFFFFFFFFu};
     if (same_o) {
         for (uint32_t p = pbeg + lane; p < pend; p += 32u) {
             const uint32_t kA = 2u * p;
@@ -578,8 +590,8 @@ __device__ __forceinline__ void coop_leaf2(const ulonglong2* __restrict__ pairs,
             bb.take(ray_terms(pd, origin_terms(pd, BOX, BOY, BOZ, Z), BDX, BDY, BDZ, Z, va, vb), kA);
         }
     }
-    reduce_and_take(ba, pbeg, srcA, r);
-    reduce_and_take(bb, pbeg, srcB, r);
+    reduce_and_take(ba, pairs, srcA, r);
+    reduce_and_take(bb, pairs, srcB, r);
 }
 
 __device__ __forceinline__ void load_ray(const float4* rays, uint32_t i, float3& o, float3& d, float& t) {
