@@ -175,24 +175,26 @@ __global__ void __launch_bounds__(kBlock) k_refit_leaves(float4* nodes, const fl
 // ---- TLAS ------------------------------------------------------------------------------------
 // Tlas::rebuild (tlas.rs:204-250) walks nearest neighbours over a list of node indices and
 // calls find_best_match (tlas.rs:179-202) -- a full scan of the list -- at every step.  Here
-// each list position keeps the result find_best_match would give for it (surface area and
-// position) in shared memory, and a merge updates only what it can change:
+// each list position keeps the result find_best_match would give for it as one 64-bit key in
+// shared memory: the area's order-preserving rank (both zeros one rank) above the position, so
+// the smallest key is the smallest area with ties to the lower position, as the reference's
+// strict `<` scan from FLT_MAX keeps it; areas not below FLT_MAX (and NaN) are never keys.  A
+// merge updates only what it can change:
 //  - the merged node lands on position a, the last node moves to position b, the list shrinks;
-//  - a position whose cached best was a, b or the old last position is rescanned in full
-//    (one warp per position);
+//  - a position whose cached best was a, b or the old last position is rescanned in full, by
+//    several warps at once (each a slice of the list, combined with a shared-memory atomicMin);
 //  - any other position keeps its cached best, which is still the first minimum over the
 //    positions whose node did not change, and compares it with the two changed positions.
-// The walk then reads the cache.  Minimum first, ties to the lower position, only areas below
-// FLT_MAX taken: exactly the reference's strict `<` scan from FLT_MAX, so the TLAS is bit for
-// bit Tlas::rebuild's, including the case where position a itself leaves the list.
+// The walk then reads the cache.  The TLAS is bit for bit Tlas::rebuild's, including the case
+// where position a itself leaves the list (its stale entry is then scanned like a rescan).
 
 constexpr int kTlasThreads = 512;
+constexpr unsigned long long kNoKey = 0xFFFFFFFFFFFFFFFFull;
 
 struct TlasSmem {  // one entry per list position
+    unsigned long long* key;              // cached find_best_match(p)
     float *lx, *ly, *lz, *hx, *hy, *hz;  // node bounds (nodes[list[p]].aabb)
     int* node;                            // list[p]: node index
-    float* csa;                           // cached find_best_match(p): surface area
-    int* cpos;                            //   and position (-1: none)
     int* inval;                           // positions to rescan after a merge
 };
 
@@ -204,45 +206,44 @@ __device__ __forceinline__ Box6 load_box(const TlasSmem& S, int p) {
     return Box6{S.lx[p], S.ly[p], S.lz[p], S.hx[p], S.hy[p], S.hz[p]};
 }
 
-// find_best_match's area (tlas.rs:184-193): component_max / component_min with the query
-// node's coordinate first, then ex*ey + ey*ez + ez*ex.
+// find_best_match's area (tlas.rs:184-193): component_max / component_min, then
+// ex*ey + ey*ez + ez*ex.  The area is only compared (as a key rank), never stored, so fmaxf /
+// fminf stand in for the first-operand-on-ties f32::max / f32::min: they ignore NaN the same way
+// and can differ only in the sign of a zero coordinate, which changes at most the sign of a zero
+// area -- the same rank.
 __device__ __forceinline__ float sa_merge(const Box6& a, const TlasSmem& S, int r) {
-    float ex = fsub(max_ni(a.hx, S.hx[r]), min_ni(a.lx, S.lx[r]));
-    float ey = fsub(max_ni(a.hy, S.hy[r]), min_ni(a.ly, S.ly[r]));
-    float ez = fsub(max_ni(a.hz, S.hz[r]), min_ni(a.lz, S.lz[r]));
+    float ex = fsub(fmaxf(a.hx, S.hx[r]), fminf(a.lx, S.lx[r]));
+    float ey = fsub(fmaxf(a.hy, S.hy[r]), fminf(a.ly, S.ly[r]));
+    float ez = fsub(fmaxf(a.hz, S.hz[r]), fminf(a.lz, S.lz[r]));
     return fadd(fadd(fmul(ex, ey), fmul(ey, ez)), fmul(ez, ex));
 }
 
-// (s, r) beats the current best (bs, bq): the area is taken at all only below FLT_MAX, and ties
-// go to the lower position.
-__device__ __forceinline__ bool better(float s, int r, float bs, int bq) {
-    return s < FLT_MAX && (bq < 0 || s < bs || (s == bs && r < bq));
+// The cache key of candidate r for query box P (kNoKey where the reference would not take it).
+__device__ __forceinline__ unsigned long long sa_key(const Box6& P, const TlasSmem& S, int r) {
+    const float s = sa_merge(P, S, r);
+    return s < FLT_MAX ? (((unsigned long long)ordered(s) << 32) | (uint32_t)r) : kNoKey;
 }
 
-// Full find_best_match for position p over positions [0, count) by one warp.
-__device__ __forceinline__ void warp_best_match(const TlasSmem& S, int p, int count, float& out_s, int& out_q) {
-    const int lane = (int)(threadIdx.x & 31u);
+__device__ __forceinline__ int key_pos(unsigned long long k) { return k == kNoKey ? -1 : (int)(uint32_t)k; }
+
+// Warp minimum of 64-bit keys as two 32-bit warp reductions: the smallest high half (area rank),
+// then the smallest low half (position) among the lanes holding that high half.
+__device__ __forceinline__ unsigned long long warp_min_key(unsigned long long k) {
+    const uint32_t hi = __reduce_min_sync(kFull, (uint32_t)(k >> 32));
+    const uint32_t lo = __reduce_min_sync(kFull, (uint32_t)(k >> 32) == hi ? (uint32_t)k : 0xFFFFFFFFu);
+    return ((unsigned long long)hi << 32) | lo;
+}
+
+// find_best_match for position p over positions [r0, r1) by one warp.
+__device__ __forceinline__ unsigned long long warp_best_key(const TlasSmem& S, int p, int r0, int r1) {
     const Box6 P = load_box(S, p);
-    float bs = FLT_MAX;
-    int bq = -1;
-    for (int r = lane; r < count; r += 32) {
+    unsigned long long best = kNoKey;
+    for (int r = r0 + (int)(threadIdx.x & 31u); r < r1; r += 32) {
         if (r == p) continue;
-        float s = sa_merge(P, S, r);
-        if (s < bs) {  // strict, from FLT_MAX: this lane's first minimum
-            bs = s;
-            bq = r;
-        }
+        const unsigned long long k = sa_key(P, S, r);
+        best = k < best ? k : best;
     }
-    for (int off = 16; off > 0; off >>= 1) {
-        float os = __shfl_xor_sync(kFull, bs, off);
-        int oq = __shfl_xor_sync(kFull, bq, off);
-        if (oq >= 0 && better(os, oq, bs, bq)) {
-            bs = os;
-            bq = oq;
-        }
-    }
-    out_s = bs;
-    out_q = bq;
+    return warp_min_key(best);
 }
 
 __device__ __forceinline__ void xf_point_g(const float* m, float x, float y, float z, float* out) {
@@ -259,26 +260,27 @@ __device__ __forceinline__ void store_tlas_node(float4* out, uint32_t i, const B
 
 // One block.  Object world bounds (SceneObject::set_transform, scene_object.rs:60-75) in
 // parallel, the cache filled one warp per position, then the walk: every thread follows it
-// (it only reads shared memory), thread 0 writes the merged nodes, all threads update the
-// cache.  status[0] gets nodes_used, status[1] an error (the reference would panic).
+// (it only reads the keys), warp 0 writes the merged nodes, all threads update the cache.
+// status[0] gets nodes_used, status[1] an error (the reference would panic).
 __global__ void __launch_bounds__(kTlasThreads) k_tlas_rebuild(const GBlas* __restrict__ blas_table,
                                                                const uint32_t* __restrict__ obj_blas,
                                                                const float* __restrict__ xf, uint32_t nobj,
                                                                float4* __restrict__ tlas_out, uint32_t* status) {
-    extern __shared__ float tsm[];
-    __shared__ int s_ninval, s_best_a;
+    extern __shared__ unsigned long long tsm_keys[];
+    __shared__ int s_ninval;
+    __shared__ unsigned long long s_key_a;
     const int n = (int)nobj;
     TlasSmem S;
-    S.lx = tsm;
-    S.ly = tsm + n;
-    S.lz = tsm + 2 * n;
-    S.hx = tsm + 3 * n;
-    S.hy = tsm + 4 * n;
-    S.hz = tsm + 5 * n;
-    S.node = reinterpret_cast<int*>(tsm + 6 * n);
-    S.csa = tsm + 7 * n;
-    S.cpos = reinterpret_cast<int*>(tsm + 8 * n);
-    S.inval = reinterpret_cast<int*>(tsm + 9 * n);
+    S.key = tsm_keys;
+    float* f = reinterpret_cast<float*>(tsm_keys + n);
+    S.lx = f;
+    S.ly = f + n;
+    S.lz = f + 2 * n;
+    S.hx = f + 3 * n;
+    S.hy = f + 4 * n;
+    S.hz = f + 5 * n;
+    S.node = reinterpret_cast<int*>(f + 6 * n);
+    S.inval = reinterpret_cast<int*>(f + 7 * n);
     const int tid = (int)threadIdx.x;
     const int warp = tid >> 5, lane = tid & 31, nwarps = (int)(blockDim.x >> 5);
 
@@ -307,18 +309,13 @@ __global__ void __launch_bounds__(kTlasThreads) k_tlas_rebuild(const GBlas* __re
     }
     __syncthreads();
     for (int p = warp; p < n; p += nwarps) {
-        float s;
-        int q;
-        warp_best_match(S, p, n, s, q);
-        if (lane == 0) {
-            S.csa[p] = s;
-            S.cpos[p] = q;
-        }
+        const unsigned long long k = warp_best_key(S, p, 0, n);
+        if (lane == 0) S.key[p] = k;
     }
     __syncthreads();
 
     int count = n, used = 1 + n, a = 0;
-    int b = S.cpos[0];
+    int b = key_pos(S.key[0]);
     uint32_t err = 0;
     uint64_t steps = 0;
     const uint64_t max_steps = 4ull * nobj * nobj + 64;
@@ -327,87 +324,80 @@ __global__ void __launch_bounds__(kTlasThreads) k_tlas_rebuild(const GBlas* __re
             err = 1;
             break;
         }
-        const int c = S.cpos[b];
+        const int c = key_pos(S.key[b]);
         if (a != c) {
             a = b;
             b = c;
             continue;
         }
         const int last = count - 1;
-        __syncthreads();  // everyone has read the cache before it changes
-        if (tid == 0) {
-            const Box6 A = load_box(S, a), B = load_box(S, b);
-            const Box6 M{min_ni(A.lx, B.lx), min_ni(A.ly, B.ly), min_ni(A.lz, B.lz),
-                         max_ni(A.hx, B.hx), max_ni(A.hy, B.hy), max_ni(A.hz, B.hz)};
-            // LeftRightIndex::new(a, b) = a + (b << 16) (tlas.rs:18-22)
-            store_tlas_node(tlas_out, (uint32_t)used, M, (uint32_t)S.node[a] + ((uint32_t)S.node[b] << 16), 0u);
-            S.lx[a] = M.lx;
-            S.ly[a] = M.ly;
-            S.lz[a] = M.lz;
-            S.hx[a] = M.hx;
-            S.hy[a] = M.hy;
-            S.hz[a] = M.hz;
-            S.node[a] = used;
-            S.lx[b] = S.lx[last];  // list[b] = list[count - 1], after list[a] (tlas.rs:238-240)
-            S.ly[b] = S.ly[last];
-            S.lz[b] = S.lz[last];
-            S.hx[b] = S.hx[last];
-            S.hy[b] = S.hy[last];
-            S.hz[b] = S.hz[last];
-            S.node[b] = S.node[last];
-            s_ninval = 0;
+        // Between the previous merge's last barrier and here the threads only read keys, so
+        // warp 0 may rewrite the boxes and the node list right away: lane c < 6 the c-th
+        // coordinate array, lane 6 the node list (each lane touches only its own array).
+        if (warp == 0 && lane < 7) {
+            // node `used` as 8 floats: lo.xyz, left_right, hi.xyz, blas (0 for an inner node)
+            float* out = reinterpret_cast<float*>(tlas_out) + 8ull * (uint32_t)used;
+            if (lane < 6) {
+                float* arr = S.lx + lane * n;  // lx, ly, lz, hx, hy, hz are consecutive arrays
+                const float va = arr[a], vb = arr[b];
+                const float m = lane < 3 ? min_ni(va, vb) : max_ni(va, vb);  // Aabb::new of a and b
+                arr[a] = m;
+                arr[b] = arr[last];  // list[b] = list[count - 1], after list[a] (tlas.rs:238-240)
+                out[lane < 3 ? lane : lane + 1] = m;
+            } else {
+                // LeftRightIndex::new(a, b) = a + (b << 16) (tlas.rs:18-22)
+                out[3] = __uint_as_float((uint32_t)S.node[a] + ((uint32_t)S.node[b] << 16));
+                out[7] = __uint_as_float(0u);
+                S.node[a] = used;
+                S.node[b] = S.node[last];
+                s_ninval = 0;  // last read before the previous merge's final barrier
+            }
         }
         count = last;
         used += 1;
         __syncthreads();
+        // s_key_a was read for the previous walk step by every thread before the barrier above
+        if (tid == 0) s_key_a = kNoKey;
         for (int p = tid; p < count; p += (int)blockDim.x) {
-            int q = S.cpos[p];
+            unsigned long long k = S.key[p];
+            const int q = key_pos(k);
             if (p == a || p == b || q == a || q == b || q == last) {
+                S.key[p] = kNoKey;
                 S.inval[atomicAdd(&s_ninval, 1)] = p;
                 continue;
             }
             const Box6 P = load_box(S, p);
-            float bs = S.csa[p];
             if (a < count) {
-                float s = sa_merge(P, S, a);
-                if (better(s, a, bs, q)) {
-                    bs = s;
-                    q = a;
-                }
+                const unsigned long long ka = sa_key(P, S, a);
+                k = ka < k ? ka : k;
             }
             if (b < count) {
-                float s = sa_merge(P, S, b);
-                if (better(s, b, bs, q)) {
-                    bs = s;
-                    q = b;
-                }
+                const unsigned long long kb = sa_key(P, S, b);
+                k = kb < k ? kb : k;
             }
-            S.csa[p] = bs;
-            S.cpos[p] = q;
+            S.key[p] = k;
         }
         __syncthreads();
+        // full rescans (and position a's stale entry if a left the list): every target split into
+        // slices over the warps, slices combined with atomicMin
         const int ninval = s_ninval;
-        for (int k = warp; k < ninval; k += nwarps) {
-            const int p = S.inval[k];
-            float s;
-            int q;
-            warp_best_match(S, p, count, s, q);
-            if (lane == 0) {
-                S.csa[p] = s;
-                S.cpos[p] = q;
+        const int ntarget = ninval + (a >= count ? 1 : 0);
+        if (ntarget > 0) {
+            const int slices = max(1, nwarps / ntarget);
+            for (int item = warp; item < ntarget * slices; item += nwarps) {
+                const int j = item / slices, sl = item - j * slices;
+                const int p = j < ninval ? S.inval[j] : a;
+                const int r0 = (int)((long long)count * sl / slices), r1 = (int)((long long)count * (sl + 1) / slices);
+                const unsigned long long k = warp_best_key(S, p, r0, r1);
+                if (lane == 0 && k != kNoKey) atomicMin(j < ninval ? &S.key[p] : &s_key_a, k);
             }
         }
-        if (a >= count && warp == 0) {  // position a left the list; its stale entry is still read
-            float s;
-            int q;
-            warp_best_match(S, a, count, s, q);
-            if (lane == 0) s_best_a = q;
-        }
         __syncthreads();
-        b = (a < count) ? S.cpos[a] : s_best_a;
+        b = key_pos(a < count ? S.key[a] : s_key_a);
     }
+    __syncthreads();  // the inner nodes written by warp 0's lanes are visible to thread 0
     if (tid == 0) {
-        if (err == 0) {  // nodes[0] = nodes[list[a]] (tlas.rs:248); thread 0 wrote that node
+        if (err == 0) {  // nodes[0] = nodes[list[a]] (tlas.rs:248)
             const uint32_t r = (uint32_t)S.node[a];
             const float4 r0 = tlas_out[2ull * r], r1 = tlas_out[2ull * r + 1];
             tlas_out[0] = r0;
@@ -799,7 +789,7 @@ cudaError_t launch_refit(bvhgpu_ctx* ctx, DeviceBlas& b, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-size_t tlas_smem_bytes(uint32_t nobj) { return 10ull * sizeof(float) * nobj; }
+size_t tlas_smem_bytes(uint32_t nobj) { return (8ull + 8ull * sizeof(float)) * nobj; }
 
 cudaError_t launch_tlas_rebuild(bvhgpu_ctx* ctx, DeviceScene& sc, cudaStream_t s) {
     size_t smem = tlas_smem_bytes(sc.nobjects);
