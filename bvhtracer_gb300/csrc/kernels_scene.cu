@@ -384,10 +384,11 @@ __global__ void __launch_bounds__(kTlasThreads) k_tlas_rebuild(const GBlas* __re
         const int ntarget = ninval + (a >= count ? 1 : 0);
         if (ntarget > 0) {
             const int slices = max(1, nwarps / ntarget);
+            const int chunk = (count + slices - 1) / slices;
             for (int item = warp; item < ntarget * slices; item += nwarps) {
                 const int j = item / slices, sl = item - j * slices;
                 const int p = j < ninval ? S.inval[j] : a;
-                const int r0 = (int)((long long)count * sl / slices), r1 = (int)((long long)count * (sl + 1) / slices);
+                const int r0 = sl * chunk, r1 = min(count, r0 + chunk);
                 const unsigned long long k = warp_best_key(S, p, r0, r1);
                 if (lane == 0 && k != kNoKey) atomicMin(j < ninval ? &S.key[p] : &s_key_a, k);
             }
