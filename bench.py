@@ -364,7 +364,7 @@ def run_ours(args):
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of each bench's dominant
 # kernel, from the ncu captures summarised under profiles/ (the command is in each summary).
 NCU_TRAFFIC = {
-    "persistent_bounce": (76.545024e6 + 48.692992e6, "ncu capture of the 1080p frame",
+    "persistent_bounce": (76.917504e6 + 46.391808e6, "ncu capture of the 1080p frame",
                           "profiles/k_persistent_bounce_config1_full.md"),
     # 8-scene capture (10,057,687 rays, 523.2 MB: 52 B of ray in + hit out per ray, the BVHs once)
     # scaled to the 64-scene launch: 52 B x rays + 88 B x triangles (tris + pairs, read once)
