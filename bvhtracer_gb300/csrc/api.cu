@@ -126,6 +126,7 @@ void free_blas(DeviceBlas& b) {
     cudaFree(b.counters);
     cudaFree(b.tri_leaf);
     cudaFree(b.leaf_keys);
+    cudaFree(b.cl);
     b = DeviceBlas();
 }
 
@@ -213,6 +214,66 @@ void pack_nodes(const bvhgpu_node* nodes, uint32_t n, std::vector<float>& out) {
         o[6] = nodes[i].bounds_max[2];
         std::memcpy(&o[7], &nodes[i].primitive_count, 4);
     }
+}
+
+// Spreads the low 10 bits of x to every third bit (Morton interleave).
+uint32_t spread3(uint32_t x) {
+    x &= 0x3FFu;
+    x = (x | (x << 16)) & 0x030000FFu;
+    x = (x | (x << 8)) & 0x0300F00Fu;
+    x = (x | (x << 4)) & 0x030C30C3u;
+    x = (x | (x << 2)) & 0x09249249u;
+    return x;
+}
+
+// Clusters of the leaves with at least kClusterMinLeaf triangles: each such leaf's triangles in
+// the Morton order of their centroids (10 bits per axis inside the leaf's box, ties by triangle
+// index), kClusterTris per cluster, the last one padded.  Returns the device image of GBlas::cl
+// with the table and the slot indices filled in (the refresh kernel writes boxes and pairs), or
+// an empty vector when no leaf is large enough.
+std::vector<uint4> plan_clusters(const bvhgpu_node* nodes, const std::vector<uint32_t>& leaves,
+                                 const bvhgpu_triangle* tris, uint32_t ntris, uint32_t* ncl_out) {
+    uint64_t ncl = 0;
+    for (uint32_t li : leaves)
+        if (nodes[li].primitive_count >= kClusterMinLeaf)
+            ncl += (nodes[li].primitive_count + kClusterTris - 1) / kClusterTris;
+    *ncl_out = (uint32_t)ncl;
+    if (ncl == 0) return {};
+    const uint64_t head = cluster_table_units(ntris);
+    std::vector<uint4> img(head + kClusterRec * ncl, make_uint4(0u, 0u, 0u, 0u));
+    uint2* table = reinterpret_cast<uint2*>(img.data());
+    std::vector<std::pair<uint32_t, uint32_t>> keys;
+    uint32_t c0 = 0;
+    for (uint32_t li : leaves) {
+        const bvhgpu_node& n = nodes[li];
+        if (n.primitive_count < kClusterMinLeaf) continue;
+        keys.clear();
+        for (uint32_t k = 0; k < n.primitive_count; ++k) {
+            const float* v = tris[n.left_first + k].vertices;
+            uint32_t code = 0;
+            for (int a = 0; a < 3; ++a) {
+                const float c = (v[a] + v[3 + a] + v[6 + a]) / 3.0f;
+                const float ext = n.bounds_max[a] - n.bounds_min[a];
+                const float x = ext > 0.0f ? (c - n.bounds_min[a]) / ext * 1024.0f : 0.0f;
+                const float q = std::min(1023.0f, std::max(0.0f, x));  // NaN -> 0
+                code |= spread3((uint32_t)q) << a;
+            }
+            keys.push_back({code, n.left_first + k});
+        }
+        std::sort(keys.begin(), keys.end());
+        table[n.left_first] = make_uint2(c0, n.primitive_count);
+        const uint32_t nc = (n.primitive_count + kClusterTris - 1) / kClusterTris;
+        for (uint32_t j = 0; j < nc; ++j) {
+            uint2* slots = reinterpret_cast<uint2*>(img.data() + head + (uint64_t)kClusterRec * (c0 + j) + kClusterIdx);
+            for (uint32_t p = 0; p < kClusterTris / 2; ++p) {
+                const uint64_t s0 = (uint64_t)j * kClusterTris + 2 * p;
+                slots[p].x = s0 < keys.size() ? keys[s0].second : kMiss;
+                slots[p].y = s0 + 1 < keys.size() ? keys[s0 + 1].second : kMiss;
+            }
+        }
+        c0 += nc;
+    }
+    return img;
 }
 
 }  // namespace
@@ -420,6 +481,7 @@ int bvhgpu_blas_upload(bvhgpu_ctx* ctx, const bvhgpu_node* nodes, uint32_t nodes
     std::vector<unsigned long long> key_init(6 * std::max<size_t>(1, leaves.size()), 0ull);
     for (size_t li = 0; li < key_init.size() / 6; ++li)
         for (int k = 0; k < 3; ++k) key_init[6 * li + k] = 0xFFFFFFFFFFFFFFFFull;
+    const std::vector<uint4> cl_img = plan_clusters(nodes, leaves, tris, ntris, &b.ncl);
     void* d_tris9 = nullptr;
     cudaError_t e = cudaSuccess;
     auto cleanup = [&]() {
@@ -435,7 +497,8 @@ int bvhgpu_blas_upload(bvhgpu_ctx* ctx, const bvhgpu_node* nodes, uint32_t nodes
         (e = cudaMalloc(&b.counters, 4ull * nodes_used)) != cudaSuccess ||
         (e = cudaMalloc(&b.tri_leaf, 4ull * ntris)) != cudaSuccess ||
         (e = cudaMalloc(&b.leaf_keys, 48ull * std::max<size_t>(1, leaves.size()))) != cudaSuccess ||
-        (e = cudaMalloc(&d_tris9, 36ull * ntris)) != cudaSuccess) {
+        (e = cudaMalloc(&d_tris9, 36ull * ntris)) != cudaSuccess ||
+        (b.ncl && (e = cudaMalloc(&b.cl, 16ull * cl_img.size())) != cudaSuccess)) {
         cleanup();
         return fail(ctx, BVHGPU_ERR_OUT_OF_MEMORY, "blas_upload: %s", cudaGetErrorString(e));
     }
@@ -447,6 +510,7 @@ int bvhgpu_blas_upload(bvhgpu_ctx* ctx, const bvhgpu_node* nodes, uint32_t nodes
         (e = cudaMemcpy(b.leaf_keys, key_init.data(), 8ull * key_init.size(), cudaMemcpyHostToDevice)) != cudaSuccess ||
         (e = cudaMemset(b.pairs, 0, 80ull * ((ntris + 1) / 2))) != cudaSuccess ||
         (e = cudaMemcpy(d_tris9, tris, 36ull * ntris, cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (b.ncl && (e = cudaMemcpy(b.cl, cl_img.data(), 16ull * cl_img.size(), cudaMemcpyHostToDevice)) != cudaSuccess) ||
         (e = launch_write_tris(ctx, b, static_cast<const float*>(d_tris9), ctx->stream)) != cudaSuccess ||
         (e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess) {
         cleanup();
@@ -476,6 +540,14 @@ int bvhgpu_blas_info(bvhgpu_ctx* ctx, uint32_t blas_id, uint32_t* nodes_used, ui
     if (nodes_used) *nodes_used = b->nodes_used;
     if (ntris) *ntris = b->ntris;
     if (depth) *depth = b->depth;
+    return BVHGPU_OK;
+}
+
+int bvhgpu_blas_clusters(bvhgpu_ctx* ctx, uint32_t blas_id, uint32_t* nclusters) {
+    if (!ctx || !nclusters) return BVHGPU_ERR_INVALID_ARG;
+    DeviceBlas* b = find_blas(ctx, blas_id);
+    if (!b) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown BLAS %u", blas_id);
+    *nclusters = b->ncl;
     return BVHGPU_OK;
 }
 
@@ -757,6 +829,7 @@ int bvhgpu_scene_create(bvhgpu_ctx* ctx, const uint32_t* blas_ids, uint32_t nobj
             g.nodes = b->nodes;
             g.tris = b->tris;
             g.pairs = b->pairs;
+            g.cl = b->cl;
             g.nodes_used = b->nodes_used;
             g.ntris = b->ntris;
             g.root_count = b->root_count;

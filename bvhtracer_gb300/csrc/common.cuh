@@ -12,6 +12,8 @@
 
 #include <cuda_runtime.h>
 
+#include "cull.cuh"
+
 namespace bvhgpu {
 
 // Device error flags (OR-ed into the context's error word).
@@ -29,11 +31,30 @@ struct GBlas {
     // Triangle pairs (2p, 2p+1) interleaved for packed f32x2 math: 20 floats per pair, component
     // c of {v0x v0y v0z e1x e1y e1z e2x e2y e2z} of triangle 2p + h at float 2c + h.
     const ulonglong2* pairs;
+    // Clusters of the large leaves (null when none): a table of ntris uint2 {first cluster, leaf
+    // triangle count} read at each leaf's first triangle ({0, 0}: not clustered; a count that
+    // differs from the leaf's: not this leaf's clusters), padded to 16 bytes, then one
+    // kClusterRec-uint4 record per cluster (cluster_rec), ceil(count / 64) clusters per leaf.
+    const uint4* cl;
     uint32_t nodes_used;
     uint32_t ntris;
     uint32_t root_count;  // root node meta (node 0)
     uint32_t root_first;
 };
+
+// Cluster record, in 16-byte units: [0, 2) ClusterBox; [2, 18) uint2 triangle index of slots
+// (2p, 2p + 1) for pair p = 0..31 (0xFFFFFFFF: padding); [18, 178) the 32 pairs in the packed
+// layout of GBlas::pairs (5 x 16 bytes each, padding slots all zero).
+constexpr uint32_t kClusterRec = 178;
+constexpr uint32_t kClusterIdx = 2;
+constexpr uint32_t kClusterPairs = 18;
+// Leaves with fewer triangles are not clustered.
+constexpr uint32_t kClusterMinLeaf = 128;
+
+__host__ __device__ __forceinline__ uint64_t cluster_table_units(uint32_t ntris) { return (ntris + 1ull) / 2ull; }
+__host__ __device__ __forceinline__ const uint4* cluster_rec(const uint4* cl, uint32_t ntris, uint32_t j) {
+    return cl + cluster_table_units(ntris) + (uint64_t)kClusterRec * j;
+}
 
 struct GHit {
     float t, u, v;
@@ -592,6 +613,179 @@ __device__ __forceinline__ void coop_leaf2(const ulonglong2* __restrict__ pairs,
     }
     reduce_and_take(ba, pairs, srcA, r);
     reduce_and_take(bb, pairs, srcB, r);
+}
+
+// ---- clustered big-leaf test --------------------------------------------------------------
+// A clustered leaf is tested cluster by cluster: lane j first decides for clusters j, j + 32, ...
+// whether the ray can have an accepted hit below its closest t there (cluster_culled, exact:
+// culled clusters hold none), then the warp tests each remaining cluster with one packed pair
+// per lane.  Cluster slots are in spatial (Morton) order, not triangle order, so the running best
+// is the smallest (t, triangle index): the same triangle the reference's in-order loop keeps.
+
+// Running best by (t, triangle).  Starts at (ray t, 0): a triangle is taken only with t below the
+// ray's closest t, and a tie in t goes to the lower triangle index.
+struct BestLex {
+    float t;
+    uint32_t k;
+    __device__ __forceinline__ void take(const PairHit& h, uint2 idx) {
+        if (h.okA && (h.tA < t || (h.tA == t && idx.x < k))) {
+            t = h.tA;
+            k = idx.x;
+        }
+        if (h.okB && (h.tB < t || (h.tB == t && idx.y < k))) {
+            t = h.tB;
+            k = idx.y;
+        }
+    }
+};
+
+__device__ __forceinline__ CullRay bcast_cull_ray(const CoopRay& c, const LaneRay& r, int src) {
+    const unsigned kAll = 0xFFFFFFFFu;
+    const float rx = __shfl_sync(kAll, r.rd.x, src), ry = __shfl_sync(kAll, r.rd.y, src),
+                rz = __shfl_sync(kAll, r.rd.z, src);
+    return cull_ray_rd(c.ox, c.oy, c.oz, c.dx, c.dy, c.dz, rx, ry, rz);
+}
+
+__device__ __forceinline__ bool cluster_live(const uint4* __restrict__ rec, const CullRay& cr, float t_best) {
+    const float4 a = __ldg(reinterpret_cast<const float4*>(rec));
+    const float4 b = __ldg(reinterpret_cast<const float4*>(rec) + 1);
+    ClusterBox box;
+    box.lo[0] = a.x; box.lo[1] = a.y; box.lo[2] = a.z; box.p = a.w;
+    box.hi[0] = b.x; box.hi[1] = b.y; box.hi[2] = b.z; box.q = b.w;
+    return !cluster_culled(box, cr, t_best);
+}
+
+// Warp argmin of (t, triangle); lane `src` takes the hit when the minimum t is below t0 (the
+// ray's closest t when the leaf test began), recomputing u, v as reduce_and_take does.
+__device__ __forceinline__ void reduce_and_take_lex(BestLex b, float t0, const ulonglong2* __restrict__ pairs, int src,
+                                                    LaneRay& r) {
+    const unsigned kAll = 0xFFFFFFFFu;
+    const unsigned lane = threadIdx.x & 31u;
+    float bt = b.t;
+    uint32_t bk = b.k;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const float ot = __shfl_xor_sync(kAll, bt, off);
+        const uint32_t ok = __shfl_xor_sync(kAll, bk, off);
+        if (ot < bt || (ot == bt && ok < bk)) {
+            bt = ot;
+            bk = ok;
+        }
+    }
+    if (bt < t0 && (int)lane == src) {
+        float4 v0, e1, e2;
+        load_pair_tri(pairs, bk, v0, e1, e2);
+        float t, u, v;
+        tri_test(v0, e1, e2, r.o, r.d, t, u, v);
+        r.ct = bt;
+        r.hu = u;
+        r.hv = v;
+        r.hp = bk;
+        r.hit = true;
+        r.inst = r.inst_cur;
+    }
+}
+
+// One ray (lane src) against the clusters [c0, c0 + nc) of records `cl` (cluster_rec(..., 0)).
+__device__ __forceinline__ void coop_leaf_cl(const uint4* __restrict__ cl, uint32_t c0, uint32_t nc,
+                                             const ulonglong2* __restrict__ pairs, int src, LaneRay& r) {
+    const unsigned kAll = 0xFFFFFFFFu;
+    const unsigned lane = threadIdx.x & 31u;
+    const CoopRay c = bcast_ray(r, src);
+    const CullRay cr = bcast_cull_ray(c, r, src);
+    const f2 OX = f2_pack(c.ox, c.ox), OY = f2_pack(c.oy, c.oy), OZ = f2_pack(c.oz, c.oz);
+    const f2 DX = f2_pack(c.dx, c.dx), DY = f2_pack(c.dy, c.dy), DZ = f2_pack(c.dz, c.dz);
+    const f2 Z = f2_neg_zero();
+    BestLex b{c.ct, 0u};
+    for (uint32_t base = 0; base < nc; base += 32u) {
+        const uint32_t j = base + lane;
+        const bool live = j < nc && cluster_live(cl + (uint64_t)kClusterRec * (c0 + j), cr, c.ct);
+        unsigned m = __ballot_sync(kAll, live);
+        while (m) {
+            const uint32_t i = (uint32_t)__ffs(m) - 1u;
+            m &= m - 1u;
+            const uint4* rec = cl + (uint64_t)kClusterRec * (c0 + base + i);
+            const uint2 idx = __ldg(reinterpret_cast<const uint2*>(rec + kClusterIdx) + lane);
+            const PairData pd = load_pair(reinterpret_cast<const ulonglong2*>(rec + kClusterPairs) + 5u * lane);
+            const OriginTerms ot = origin_terms(pd, OX, OY, OZ, Z);
+            b.take(ray_terms(pd, ot, DX, DY, DZ, Z, idx.x != kMiss, idx.y != kMiss), idx);
+        }
+    }
+    reduce_and_take_lex(b, c.ct, pairs, src, r);
+}
+
+// Two rays (lanes srcA, srcB) against the same clustered leaf: a cluster is loaded once when
+// either ray needs it, and tested for the rays that need it.
+__device__ __forceinline__ void coop_leaf2_cl(const uint4* __restrict__ cl, uint32_t c0, uint32_t nc,
+                                              const ulonglong2* __restrict__ pairs, int srcA, int srcB,
+                                              LaneRay& r) {
+    const unsigned kAll = 0xFFFFFFFFu;
+    const unsigned lane = threadIdx.x & 31u;
+    const CoopRay ca = bcast_ray(r, srcA);
+    const CoopRay cb = bcast_ray(r, srcB);
+    const CullRay cra = bcast_cull_ray(ca, r, srcA);
+    const CullRay crb = bcast_cull_ray(cb, r, srcB);
+    const bool same_o = __float_as_uint(ca.ox) == __float_as_uint(cb.ox) &&
+                        __float_as_uint(ca.oy) == __float_as_uint(cb.oy) &&
+                        __float_as_uint(ca.oz) == __float_as_uint(cb.oz);
+    const f2 AOX = f2_pack(ca.ox, ca.ox), AOY = f2_pack(ca.oy, ca.oy), AOZ = f2_pack(ca.oz, ca.oz);
+    const f2 ADX = f2_pack(ca.dx, ca.dx), ADY = f2_pack(ca.dy, ca.dy), ADZ = f2_pack(ca.dz, ca.dz);
+    const f2 BOX = f2_pack(cb.ox, cb.ox), BOY = f2_pack(cb.oy, cb.oy), BOZ = f2_pack(cb.oz, cb.oz);
+    const f2 BDX = f2_pack(cb.dx, cb.dx), BDY = f2_pack(cb.dy, cb.dy), BDZ = f2_pack(cb.dz, cb.dz);
+    const f2 Z = f2_neg_zero();
+    BestLex ba{ca.ct, 0u};
+    BestLex bb{cb.ct, 0u};
+    for (uint32_t base = 0; base < nc; base += 32u) {
+        const uint32_t j = base + lane;
+        bool la = false, lb = false;
+        if (j < nc) {
+            const uint4* rec = cl + (uint64_t)kClusterRec * (c0 + j);
+            la = cluster_live(rec, cra, ca.ct);
+            lb = cluster_live(rec, crb, cb.ct);
+        }
+        const unsigned ma = __ballot_sync(kAll, la), mb = __ballot_sync(kAll, lb);
+        unsigned m = ma | mb;
+        while (m) {
+            const uint32_t i = (uint32_t)__ffs(m) - 1u;
+            m &= m - 1u;
+            const bool ta = (ma >> i) & 1u, tb = (mb >> i) & 1u;
+            const uint4* rec = cl + (uint64_t)kClusterRec * (c0 + base + i);
+            const uint2 idx = __ldg(reinterpret_cast<const uint2*>(rec + kClusterIdx) + lane);
+            const bool va = idx.x != kMiss, vb = idx.y != kMiss;
+            const PairData pd = load_pair(reinterpret_cast<const ulonglong2*>(rec + kClusterPairs) + 5u * lane);
+            if (same_o) {
+                const OriginTerms ot = origin_terms(pd, AOX, AOY, AOZ, Z);
+                if (ta) ba.take(ray_terms(pd, ot, ADX, ADY, ADZ, Z, va, vb), idx);
+                if (tb) bb.take(ray_terms(pd, ot, BDX, BDY, BDZ, Z, va, vb), idx);
+            } else {
+                if (ta) ba.take(ray_terms(pd, origin_terms(pd, AOX, AOY, AOZ, Z), ADX, ADY, ADZ, Z, va, vb), idx);
+                if (tb) bb.take(ray_terms(pd, origin_terms(pd, BOX, BOY, BOZ, Z), BDX, BDY, BDZ, Z, va, vb), idx);
+            }
+        }
+    }
+    reduce_and_take_lex(ba, ca.ct, pairs, srcA, r);
+    reduce_and_take_lex(bb, cb.ct, pairs, srcB, r);
+}
+
+// Tests the big leaf [f, f + cnt) for one ray or two (srcB < 0: one): clustered when the BLAS has
+// clusters for it.  `cl` and `ntris` are those of the leaf's BLAS (the same on every lane).
+__device__ __forceinline__ void coop_leaf_any(const ulonglong2* __restrict__ pairs, const uint4* __restrict__ cl,
+                                              uint32_t ntris, uint32_t f, uint32_t cnt, int srcA, int srcB,
+                                              LaneRay& r) {
+    uint2 rec = make_uint2(0u, 0u);  // {first cluster, leaf triangle count}
+    if (cl != nullptr) rec = __ldg(reinterpret_cast<const uint2*>(cl) + f);
+    if (rec.y != 0u && rec.y == cnt) {
+        const uint4* C = cl + cluster_table_units(ntris);
+        const uint32_t nc = (cnt + kClusterTris - 1u) / kClusterTris;
+        if (srcB >= 0)
+            coop_leaf2_cl(C, rec.x, nc, pairs, srcA, srcB, r);
+        else
+            coop_leaf_cl(C, rec.x, nc, pairs, srcA, r);
+    } else if (srcB >= 0) {
+        coop_leaf2(pairs, f, cnt, srcA, srcB, r);
+    } else {
+        coop_leaf(pairs, f, cnt, srcA, r);
+    }
 }
 
 __device__ __forceinline__ void load_ray(const float4* rays, uint32_t i, float3& o, float3& d, float& t) {

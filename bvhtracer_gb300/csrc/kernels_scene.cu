@@ -47,6 +47,60 @@ __global__ void k_write_tris(const float* __restrict__ tris9, uint32_t n, float4
     for (int k = 0; k < 9; ++k) P[2 * k] = c[k];
 }
 
+// ---- cluster records of the large leaves, refreshed after every triangle write -------------
+// One warp per cluster: lane p copies the triangles of slots 2p, 2p + 1 (membership fixed at
+// upload) into the record's packed pair p and the warp reduces the cluster's box and edge bounds.
+__global__ void k_cluster_refresh(const float4* __restrict__ tris, uint4* __restrict__ recs, uint32_t ncl) {
+    const uint32_t j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const unsigned lane = threadIdx.x & 31u;
+    if (j >= ncl) return;  // whole warps leave together
+    uint4* rec = recs + (uint64_t)kClusterRec * j;
+    const uint2 idx = reinterpret_cast<const uint2*>(rec + kClusterIdx)[lane];
+    float c[2][9];
+    float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    float e1m = 0.0f, e2m = 0.0f;
+    bool finite = true;
+    for (int h = 0; h < 2; ++h) {
+        const uint32_t k = h ? idx.y : idx.x;
+        for (int q = 0; q < 9; ++q) c[h][q] = 0.0f;
+        if (k == kMiss) continue;
+        const float4 v0 = tris[3ull * k], e1 = tris[3ull * k + 1], e2 = tris[3ull * k + 2];
+        const float v[3] = {v0.x, v0.y, v0.z}, a[3] = {e1.x, e1.y, e1.z}, b[3] = {e2.x, e2.y, e2.z};
+        for (int i = 0; i < 3; ++i) {
+            c[h][i] = v[i];
+            c[h][3 + i] = a[i];
+            c[h][6 + i] = b[i];
+            const float p1 = fadd(v[i], a[i]), p2 = fadd(v[i], b[i]);
+            finite = finite && isfinite(v[i]) && isfinite(a[i]) && isfinite(b[i]) && isfinite(p1) && isfinite(p2);
+            lo[i] = fminf(lo[i], fminf(v[i], fminf(p1, p2)));
+            hi[i] = fmaxf(hi[i], fmaxf(v[i], fmaxf(p1, p2)));
+            e1m = fmaxf(e1m, fabsf(a[i]));
+            e2m = fmaxf(e2m, fabsf(b[i]));
+        }
+    }
+    float* P = reinterpret_cast<float*>(rec + kClusterPairs) + 20u * lane;
+    for (int q = 0; q < 9; ++q) {
+        P[2 * q] = c[0][q];
+        P[2 * q + 1] = c[1][q];
+    }
+    P[18] = P[19] = 0.0f;
+    for (int off = 16; off > 0; off >>= 1) {
+        for (int i = 0; i < 3; ++i) {
+            lo[i] = fminf(lo[i], __shfl_xor_sync(0xFFFFFFFFu, lo[i], off));
+            hi[i] = fmaxf(hi[i], __shfl_xor_sync(0xFFFFFFFFu, hi[i], off));
+        }
+        e1m = fmaxf(e1m, __shfl_xor_sync(0xFFFFFFFFu, e1m, off));
+        e2m = fmaxf(e2m, __shfl_xor_sync(0xFFFFFFFFu, e2m, off));
+    }
+    finite = __all_sync(0xFFFFFFFFu, finite);
+    if (lane == 0) {
+        const ClusterBox box = cluster_seal(lo, hi, e1m, e2m, finite);
+        float4* B = reinterpret_cast<float4*>(rec);
+        B[0] = make_float4(box.lo[0], box.lo[1], box.lo[2], box.p);
+        B[1] = make_float4(box.hi[0], box.hi[1], box.hi[2], box.q);
+    }
+}
+
 // ---- refit, parallel over triangles --------------------------------------------------------
 // update_node_bounds (bvh.rs:317-330) folds a leaf's vertices in order v0, v1, v2 of triangle
 // first, first+1, ... with f32::min / f32::max.  The fold's result is the minimum (maximum)
@@ -447,6 +501,7 @@ struct SceneTrav {
         blas.nodes = nullptr;
         blas.tris = nullptr;
         blas.pairs = nullptr;
+        blas.cl = nullptr;
         blas.nodes_used = blas.ntris = blas.root_count = blas.root_first = 0;
     }
 
@@ -535,12 +590,15 @@ __device__ __forceinline__ void scene_coop_phase(unsigned pend, SceneTrav<STK, T
                                                  StepResult& st) {
     const unsigned lane = threadIdx.x & 31u;
     const unsigned long long key = reinterpret_cast<unsigned long long>(tr.blas.pairs);
+    const unsigned long long ckey = reinterpret_cast<unsigned long long>(tr.blas.cl);
     while (pend) {
         const int leader = __ffs(pend) - 1;
         const uint32_t f = __shfl_sync(kFull, tr.bt.first, leader);
         const uint32_t c = __shfl_sync(kFull, tr.bt.cnt, leader);
         const unsigned long long lk = __shfl_sync(kFull, key, leader);
         const ulonglong2* P = reinterpret_cast<const ulonglong2*>(lk);
+        const uint4* C = reinterpret_cast<const uint4*>(__shfl_sync(kFull, ckey, leader));
+        const uint32_t nt = __shfl_sync(kFull, tr.blas.ntris, leader);
         unsigned group = __ballot_sync(kFull, ((pend >> lane) & 1u) && tr.bt.first == f && key == lk);
         pend &= ~group;
         while (group) {
@@ -549,10 +607,10 @@ __device__ __forceinline__ void scene_coop_phase(unsigned pend, SceneTrav<STK, T
             if (group) {
                 const int b = __ffs(group) - 1;
                 group &= group - 1u;
-                coop_leaf2(P, f, c, a, b, r);
+                coop_leaf_any(P, C, nt, f, c, a, b, r);
                 if ((int)lane == a || (int)lane == b) st = tr.after_leaf();
             } else {
-                coop_leaf(P, f, c, a, r);
+                coop_leaf_any(P, C, nt, f, c, a, -1, r);
                 if ((int)lane == a) st = tr.after_leaf();
             }
         }
@@ -776,6 +834,17 @@ cudaError_t launch_write_tris(bvhgpu_ctx* ctx, DeviceBlas& b, const float* d_tri
     LaunchScope scope(ctx, BVHGPU_K_OTHER, s);
     k_write_tris<<<grid_for(b.ntris, 256), 256, 0, s>>>(d_tris9, b.ntris, b.tris, b.verts,
                                                         reinterpret_cast<float*>(b.pairs));
+    g_launches++;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    return launch_cluster_refresh(ctx, b, s);
+}
+
+cudaError_t launch_cluster_refresh(bvhgpu_ctx* ctx, DeviceBlas& b, cudaStream_t s) {
+    if (b.ncl == 0) return cudaSuccess;
+    LaunchScope scope(ctx, BVHGPU_K_OTHER, s);
+    k_cluster_refresh<<<grid_for(32u * b.ncl, 128), 128, 0, s>>>(
+        b.tris, b.cl + cluster_table_units(b.ntris), b.ncl);
     g_launches++;
     return cudaGetLastError();
 }

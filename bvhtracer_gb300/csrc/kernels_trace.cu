@@ -31,6 +31,7 @@ inline GBlas to_gblas(const DeviceBlas& b) {
     g.nodes = b.nodes;
     g.tris = b.tris;
     g.pairs = b.pairs;
+    g.cl = b.cl;
     g.nodes_used = b.nodes_used;
     g.ntris = b.ntris;
     g.root_count = b.root_count;
@@ -59,16 +60,18 @@ inline unsigned grid_for(uint32_t n, int block) { return (unsigned)((n + block -
 // odd one alone.  `key` identifies the BLAS (pairs pointer) so that different scenes of a batch
 // never share a leaf.
 template <class TR>
-__device__ __forceinline__ void coop_leaf_phase(unsigned pend, const ulonglong2* pairs, TR& tr, LaneRay& r,
-                                                StepResult& st) {
+__device__ __forceinline__ void coop_leaf_phase(unsigned pend, const GBlas& blas, TR& tr, LaneRay& r, StepResult& st) {
     const unsigned lane = threadIdx.x & 31u;
-    const unsigned long long key = reinterpret_cast<unsigned long long>(pairs);
+    const unsigned long long key = reinterpret_cast<unsigned long long>(blas.pairs);
+    const unsigned long long ckey = reinterpret_cast<unsigned long long>(blas.cl);
     while (pend) {
         const int leader = __ffs(pend) - 1;
         const uint32_t f = __shfl_sync(kFull, tr.first, leader);
         const uint32_t c = __shfl_sync(kFull, tr.cnt, leader);
         const unsigned long long lk = __shfl_sync(kFull, key, leader);
         const ulonglong2* P = reinterpret_cast<const ulonglong2*>(lk);
+        const uint4* C = reinterpret_cast<const uint4*>(__shfl_sync(kFull, ckey, leader));
+        const uint32_t nt = __shfl_sync(kFull, blas.ntris, leader);
         unsigned group = __ballot_sync(kFull, ((pend >> lane) & 1u) && tr.first == f && key == lk);
         pend &= ~group;
         while (group) {
@@ -77,10 +80,10 @@ __device__ __forceinline__ void coop_leaf_phase(unsigned pend, const ulonglong2*
             if (group) {
                 const int b = __ffs(group) - 1;
                 group &= group - 1u;
-                coop_leaf2(P, f, c, a, b, r);
+                coop_leaf_any(P, C, nt, f, c, a, b, r);
                 if ((int)lane == a || (int)lane == b) st = tr.pop() ? kStepFinished : kStepContinue;
             } else {
-                coop_leaf(P, f, c, a, r);
+                coop_leaf_any(P, C, nt, f, c, a, -1, r);
                 if ((int)lane == a) st = tr.pop() ? kStepFinished : kStepContinue;
             }
         }
@@ -99,7 +102,7 @@ __device__ __forceinline__ void warp_trace(const GBlas& b, bool active, LaneRay&
         if (st == kStepContinue) st = tr.advance(b, r, big_leaf, err);
         unsigned pend = __ballot_sync(kFull, st == kStepBigLeaf);
         if (pend == 0u) break;
-        coop_leaf_phase(pend, b.pairs, tr, r, st);
+        coop_leaf_phase(pend, b, tr, r, st);
     }
 }
 
@@ -273,7 +276,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_persistent_bounce(GBlas b, cons
             if (!queue_open && __ballot_sync(kFull, phase == 0 || phase == 1 || phase == 2) == 0u) break;
             continue;
         }
-        coop_leaf_phase(pend, b.pairs, tr, r, st);
+        coop_leaf_phase(pend, b, tr, r, st);
     }
 }
 
@@ -301,6 +304,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_trace_batch_persistent(const Ba
     b.nodes = nullptr;
     b.tris = nullptr;
     b.pairs = nullptr;
+    b.cl = nullptr;
     b.nodes_used = b.ntris = b.root_count = b.root_first = 0;
     LaneRay r;
     TravT<STK> tr;
@@ -350,7 +354,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_trace_batch_persistent(const Ba
             if (!queue_open && __ballot_sync(kFull, phase == 0 || phase == 1) == 0u) break;
             continue;
         }
-        coop_leaf_phase(pend, b.pairs, tr, r, st);
+        coop_leaf_phase(pend, b, tr, r, st);
     }
 }
 

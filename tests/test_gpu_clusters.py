@@ -1,0 +1,186 @@
+"""Clustered big leaves: the exact in-leaf culling gives the reference's results bit for bit.
+
+Leaves of at least 128 triangles are split into 64-triangle clusters in spatial order, and a
+cluster is skipped for a ray only when provably no triangle of it is accepted below the ray's
+closest t.  These cases aim at what could break that: rays at edges and vertices, exact ties
+between duplicate triangles that land in different clusters (lowest triangle index must win),
+clusters refreshed after vertex updates and refits, non-finite vertices, axis-aligned and
+denormal directions, short rays, instanced (transformed) BLASes and the plain and persistent bounce
+kernels.  Everything is compared with the oracle's in-order leaf loop."""
+import numpy as np
+import pytest
+
+import bvhtracer_gb300 as bt
+from bvhtracer_gb300 import scenes
+from oracle import oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = bt.Context(0)
+    yield c
+    c.close()
+
+
+def same(gpu, ref, what):
+    bad = np.nonzero(gpu["prim"] != ref["prim"])[0]
+    assert len(bad) == 0, f"{what}: {len(bad)} rays with different primitives, first {bad[:8]}"
+    assert gpu.tobytes() == ref.tobytes(), f"{what}: hit records differ"
+
+
+def one_leaf_bvh(tris):
+    """A BVH whose root is one leaf holding every triangle (the reference's flat extreme)."""
+    nodes = np.zeros(2, bt.NODE)
+    v = tris.reshape(-1, 3)
+    nodes[0]["bounds_min"] = v.min(0)
+    nodes[0]["bounds_max"] = v.max(0)
+    nodes[0]["primitive_count"] = len(tris)
+    nodes[0]["left_first"] = 0
+    return bt.Bvh(nodes, 2)
+
+
+def edge_rays(tris, n, seed, eye_dist=6.0):
+    """Rays from random eyes aimed exactly at triangle vertices, edge midpoints and centroids."""
+    rng = np.random.default_rng(seed)
+    k = rng.integers(0, len(tris), n)
+    t = tris[k].reshape(n, 3, 3).astype(np.float64)
+    pick = rng.integers(0, 4, n)
+    a = np.where(pick[:, None] == 0, t[:, 0], np.where(pick[:, None] == 1, 0.5 * (t[:, 0] + t[:, 1]),
+                 np.where(pick[:, None] == 2, 0.5 * (t[:, 1] + t[:, 2]), t.mean(1))))
+    eye = rng.standard_normal((n, 3))
+    eye = eye / np.linalg.norm(eye, axis=1, keepdims=True) * eye_dist
+    d = a - eye
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    return orc.make_rays(eye.astype(np.float32), d.astype(np.float32))
+
+
+def test_flat_leaf_edges_vertices_and_random(ctx):
+    tris = scenes.displaced_icosphere(4, 7).triangles().copy()  # 5,120 triangles in one leaf
+    bvh = one_leaf_bvh(tris)
+    blas = ctx.upload_blas(bvh, tris)
+    assert blas.clusters() == (len(tris) + 63) // 64
+    rays = np.concatenate([edge_rays(tris, 20000, 1), scenes.sphere_rays(20000, 2, box=4.0)])
+    ref = orc.bvh_intersect(bvh.nodes, bvh.nodes_used, tris, rays, threads=8)
+    same(blas.intersect(rays), ref, "flat leaf")
+
+
+def test_reference_bvh_leaves_are_clustered(ctx):
+    tris = scenes.displaced_icosphere(6, 0).triangles().copy()
+    bvh = bt.BvhBuilder().build_for(tris)
+    blas = ctx.upload_blas(bvh, tris)
+    assert blas.clusters() > len(tris) // 64  # the reference's leaves of 1.7k-3.4k triangles
+    rays = edge_rays(tris, 30000, 3, eye_dist=4.0)
+    same(blas.intersect(rays), orc.bvh_intersect(bvh.nodes, bvh.nodes_used, tris, rays, threads=8), "ref bvh")
+
+
+def test_duplicate_triangles_in_different_clusters_tie_to_lowest_index(ctx):
+    rng = np.random.default_rng(5)
+    base = np.array([[-1, -1, 0, 1, -1, 0, 0, 1, 0]], np.float32)
+    other = rng.uniform(-3, 3, (600, 9)).astype(np.float32)
+    other[:, 2::3] += np.float32(2.0)  # behind the duplicates as seen from -z
+    tris = np.concatenate([other[:300], np.repeat(base, 200, 0), other[300:]])  # 200 exact copies
+    perm = rng.permutation(len(tris))
+    tris = np.ascontiguousarray(tris[perm])
+    bvh = one_leaf_bvh(tris)
+    blas = ctx.upload_blas(bvh, tris)
+    assert blas.clusters() >= 3
+    o = np.tile(np.array([0.05, -0.1, -5], np.float32), (64, 1))
+    d = np.tile(np.array([0, 0, 1], np.float32), (64, 1))
+    d[:, :2] = rng.uniform(-0.05, 0.05, (64, 2))
+    rays = orc.make_rays(o, np.array([orc.normalize(x) for x in d]))
+    ref = orc.bvh_intersect(bvh.nodes, bvh.nodes_used, tris, rays)
+    copies = np.nonzero((tris == base[0]).all(1))[0]
+    assert np.all(ref["prim"] == copies.min())
+    same(blas.intersect(rays), ref, "duplicates")
+
+
+def test_clusters_follow_vertex_updates_and_refit(ctx):
+    tris, bvh = scenes.displaced_icosphere(5, 2).triangles().copy(), None
+    bvh = bt.BvhBuilder().build_for(tris)
+    blas = ctx.upload_blas(bvh, tris)
+    rays = edge_rays(tris, 20000, 4)
+    rng = np.random.default_rng(8)
+    moved = (tris * np.float32(1.3) + rng.uniform(-0.02, 0.02, tris.shape).astype(np.float32)).astype(np.float32)
+    blas.update_vertices(moved)
+    blas.refit()
+    nodes = orc.bvh_refit(bvh.nodes, bvh.nodes_used, moved)
+    rays2 = edge_rays(moved, 20000, 5)
+    for r in (rays, rays2):
+        same(blas.intersect(r), orc.bvh_intersect(nodes, bvh.nodes_used, moved, r, threads=8), "after refit")
+
+
+def test_non_finite_vertices_and_odd_rays(ctx):
+    tris = scenes.displaced_icosphere(4, 3).triangles().copy()
+    tris[17, 0] = np.nan
+    tris[900, 4] = np.inf
+    tris[2000, 8] = -np.inf
+    tris[3001:3005] = np.float32(1e20)
+    bvh = one_leaf_bvh(np.nan_to_num(tris, nan=0.0, posinf=1e20, neginf=-1e20))
+    blas = ctx.upload_blas(bvh, tris)
+    rays = np.concatenate([scenes.sphere_rays(20000, 6, box=4.0), edge_rays(tris[:3000], 5000, 7)])
+    f32max = np.finfo(np.float32).max
+    extra = orc.make_rays([[0, 0, -10], [0, 0, -10], [0.1, 0.2, -10], [0, 0, -10], [0.3, 0.1, -10], [1e30, 0, 0],
+                           [0.2, 0.2, -3]],
+                          [[0, 0, 1], [1e-40, 0, 1], [-1e-30, 1e-38, 1], [0, 1, 0], [0, 0, 1], [-1, 0, 0], [0, 0, 1]],
+                          t=[f32max, f32max, f32max, 3.0, 9.3, f32max, 1e-5])
+    rays = np.concatenate([rays, extra])
+    ref = orc.bvh_intersect(bvh.nodes, bvh.nodes_used, tris, rays, threads=8)
+    same(blas.intersect(rays), ref, "non-finite")
+
+
+def test_short_rays_stop_at_their_t(ctx):
+    tris = scenes.displaced_icosphere(5, 4).triangles().copy()
+    bvh = bt.BvhBuilder().build_for(tris)
+    blas = ctx.upload_blas(bvh, tris)
+    rays = edge_rays(tris, 20000, 9)
+    full = orc.bvh_intersect(bvh.nodes, bvh.nodes_used, tris, rays, threads=8)
+    hit = full["prim"] != bt.MISS
+    # limit every ray to exactly its closest t, to just below it and to a random fraction
+    rng = np.random.default_rng(10)
+    for lim in (full["t"], np.nextafter(full["t"], np.float32(0)), full["t"] * rng.uniform(0.5, 1.5, len(rays))):
+        r = rays.copy()
+        r["t"] = np.where(hit, lim, np.finfo(np.float32).max).astype(np.float32)
+        same(blas.intersect(r), orc.bvh_intersect(bvh.nodes, bvh.nodes_used, tris, r, threads=8), "short rays")
+
+
+def test_bounce_kernels_with_clusters(ctx):
+    tris = scenes.displaced_icosphere(6, 1).triangles().copy()
+    bvh = bt.BvhBuilder().build_for(tris)
+    blas = ctx.upload_blas(bvh, tris)
+    prim = scenes.look_at_rays(160, 120, (0, 0, -3.2), (0, 0, 0), 50.0)
+    ref0 = orc.bvh_intersect(bvh.nodes, bvh.nodes_used, tris, prim, threads=8)
+    b2, valid = orc.bounce_rays(prim, ref0, tris, 99)
+    ref1 = np.zeros(len(prim), orc.HIT)
+    ref1["t"] = np.finfo(np.float32).max
+    ref1["prim"] = ref1["inst"] = bt.MISS
+    ref1[valid] = orc.bvh_intersect(bvh.nodes, bvh.nodes_used, tris, b2[valid], threads=8)
+    for mode in (bt.MODE_PLAIN, bt.MODE_PERSISTENT):
+        h0, h1, _ = blas.trace_bounce(prim, 99, mode)
+        same(h0, ref0, f"primaries, mode {mode}")
+        same(h1, ref1, f"bounces, mode {mode}")
+
+
+def test_instanced_scene_with_clusters(ctx):
+    tris = scenes.displaced_icosphere(5, 6).triangles().copy()
+    bvh = bt.BvhBuilder().build_for(tris)
+    blas = ctx.upload_blas(bvh, tris)
+    assert blas.clusters() > 0
+    n = 24
+    rng = np.random.default_rng(11)
+    xf = np.zeros((n, 16), np.float32)
+    inv = np.zeros((n, 16), np.float32)
+    for i in range(n):
+        s = rng.uniform(0.5, 2.0)
+        m = np.eye(4) * s
+        m[3, 3] = 1
+        m[:3, 3] = rng.uniform(-6, 6, 3)
+        xf[i] = m.T.reshape(16)
+        inv[i] = np.linalg.inv(m).T.reshape(16)
+    sc = ctx.scene([blas] * n, xf, inv)
+    tl, used = sc.download_tlas()
+    rays = scenes.sphere_rays(30000, 12, box=12.0)
+    sa = orc.SceneArrays([(bvh.nodes[:bvh.nodes_used], bvh.nodes_used, tris)], np.zeros(n, np.int64), inv)
+    ref = orc.scene_intersect(tl, used, sa, rays, threads=8)
+    same(sc.intersect(rays), ref, "scene")
