@@ -229,8 +229,8 @@ uint32_t spread3(uint32_t x) {
 // Clusters of the leaves with at least kClusterMinLeaf triangles: each such leaf's triangles in
 // the Morton order of their centroids (10 bits per axis inside the leaf's box, ties by triangle
 // index), kClusterTris per cluster, the last one padded.  Returns the device image of GBlas::cl
-// with the table and the slot indices filled in (the refresh kernel writes boxes and pairs), or
-// an empty vector when no leaf is large enough.
+// with the table, each record's leaf and the slot indices filled in (the refresh kernel writes
+// boxes, pairs and the leaves' Q and B), or an empty vector when no leaf is large enough.
 std::vector<uint4> plan_clusters(const bvhgpu_node* nodes, const std::vector<uint32_t>& leaves,
                                  const bvhgpu_triangle* tris, uint32_t ntris, uint32_t* ncl_out) {
     uint64_t ncl = 0;
@@ -241,7 +241,7 @@ std::vector<uint4> plan_clusters(const bvhgpu_node* nodes, const std::vector<uin
     if (ncl == 0) return {};
     const uint64_t head = cluster_table_units(ntris);
     std::vector<uint4> img(head + kClusterRec * ncl, make_uint4(0u, 0u, 0u, 0u));
-    uint2* table = reinterpret_cast<uint2*>(img.data());
+    uint4* table = img.data();
     std::vector<std::pair<uint32_t, uint32_t>> keys;
     uint32_t c0 = 0;
     for (uint32_t li : leaves) {
@@ -261,10 +261,12 @@ std::vector<uint4> plan_clusters(const bvhgpu_node* nodes, const std::vector<uin
             keys.push_back({code, n.left_first + k});
         }
         std::sort(keys.begin(), keys.end());
-        table[n.left_first] = make_uint2(c0, n.primitive_count);
+        table[n.left_first] = make_uint4(c0, n.primitive_count, 0u, 0u);
         const uint32_t nc = (n.primitive_count + kClusterTris - 1) / kClusterTris;
         for (uint32_t j = 0; j < nc; ++j) {
-            uint2* slots = reinterpret_cast<uint2*>(img.data() + head + (uint64_t)kClusterRec * (c0 + j) + kClusterIdx);
+            uint4* rec = img.data() + head + (uint64_t)kClusterRec * (c0 + j);
+            rec[0].w = n.left_first;  // the leaf's table entry (boxes, pairs, Q, B: refresh kernel)
+            uint2* slots = reinterpret_cast<uint2*>(rec + kClusterIdx);
             for (uint32_t p = 0; p < kClusterTris / 2; ++p) {
                 const uint64_t s0 = (uint64_t)j * kClusterTris + 2 * p;
                 slots[p].x = s0 < keys.size() ? keys[s0].second : kMiss;

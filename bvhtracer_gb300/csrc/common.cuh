@@ -31,10 +31,10 @@ struct GBlas {
     // Triangle pairs (2p, 2p+1) interleaved for packed f32x2 math: 20 floats per pair, component
     // c of {v0x v0y v0z e1x e1y e1z e2x e2y e2z} of triangle 2p + h at float 2c + h.
     const ulonglong2* pairs;
-    // Clusters of the large leaves (null when none): a table of ntris uint2 {first cluster, leaf
-    // triangle count} read at each leaf's first triangle ({0, 0}: not clustered; a count that
-    // differs from the leaf's: not this leaf's clusters), padded to 16 bytes, then one
-    // kClusterRec-uint4 record per cluster (cluster_rec), ceil(count / 64) clusters per leaf.
+    // Clusters of the large leaves (null when none): a table of ntris uint4 entries read at each
+    // leaf's first triangle, {first cluster, leaf triangle count, Q bits, B bits} ({0, 0, ...}:
+    // not clustered; a count that differs from the leaf's: not this leaf's clusters; Q and B as
+    // in cull.cuh), then one kClusterRec-uint4 record per cluster, ceil(count / 64) per leaf.
     const uint4* cl;
     uint32_t nodes_used;
     uint32_t ntris;
@@ -42,19 +42,17 @@ struct GBlas {
     uint32_t root_first;
 };
 
-// Cluster record, in 16-byte units: [0, 2) ClusterBox; [2, 18) uint2 triangle index of slots
-// (2p, 2p + 1) for pair p = 0..31 (0xFFFFFFFF: padding); [18, 178) the 32 pairs in the packed
-// layout of GBlas::pairs (5 x 16 bytes each, padding slots all zero).
+// Cluster record, in 16-byte units: [0, 2) the cluster's widened box {lo.xyz, table index of its
+// leaf (bits)}, {hi.xyz, 0}; [2, 18) uint2 triangle index of slots (2p, 2p + 1) for pair
+// p = 0..31 (0xFFFFFFFF: padding); [18, 178) the 32 pairs in the packed layout of GBlas::pairs
+// (5 x 16 bytes each, padding slots all zero).
 constexpr uint32_t kClusterRec = 178;
 constexpr uint32_t kClusterIdx = 2;
 constexpr uint32_t kClusterPairs = 18;
 // Leaves with fewer triangles are not clustered.
 constexpr uint32_t kClusterMinLeaf = 128;
 
-__host__ __device__ __forceinline__ uint64_t cluster_table_units(uint32_t ntris) { return (ntris + 1ull) / 2ull; }
-__host__ __device__ __forceinline__ const uint4* cluster_rec(const uint4* cl, uint32_t ntris, uint32_t j) {
-    return cl + cluster_table_units(ntris) + (uint64_t)kClusterRec * j;
-}
+__host__ __device__ __forceinline__ uint64_t cluster_table_units(uint32_t ntris) { return ntris; }
 
 struct GHit {
     float t, u, v;
@@ -616,10 +614,10 @@ __device__ __forceinline__ void coop_leaf2(const ulonglong2* __restrict__ pairs,
 }
 
 // ---- clustered big-leaf test --------------------------------------------------------------
-// A clustered leaf is tested cluster by cluster: lane j first decides for clusters j, j + 32, ...
-// whether the ray can have an accepted hit below its closest t there (cluster_culled, exact:
-// culled clusters hold none), then the warp tests each remaining cluster with one packed pair
-// per lane.  Cluster slots are in spatial (Morton) order, not triangle order, so the running best
+// A clustered leaf is tested cluster by cluster: the ray's margins for the leaf are computed once
+// (leaf_cull), lane j decides for clusters j, j + 32, ... whether the ray can have an accepted
+// hit below its closest t there (box_culled, exact: culled clusters hold none), then the warp
+// tests each remaining cluster with one packed pair per lane.  Cluster slots are in spatial (Morton) order, not triangle order, so the running best
 // is the smallest (t, triangle index): the same triangle the reference's in-order loop keeps.
 
 // Running best by (t, triangle).  Starts at (ray t, 0): a triangle is taken only with t below the
@@ -646,13 +644,13 @@ __device__ __forceinline__ CullRay bcast_cull_ray(const CoopRay& c, const LaneRa
     return cull_ray_rd(c.ox, c.oy, c.oz, c.dx, c.dy, c.dz, rx, ry, rz);
 }
 
-__device__ __forceinline__ bool cluster_live(const uint4* __restrict__ rec, const CullRay& cr, float t_best) {
+// Whether cluster `rec` may hold an accepted hit for the ray of `lc`.
+__device__ __forceinline__ bool cluster_live(const uint4* __restrict__ rec, const LeafCull& lc) {
+    if (!lc.on) return true;
     const float4 a = __ldg(reinterpret_cast<const float4*>(rec));
     const float4 b = __ldg(reinterpret_cast<const float4*>(rec) + 1);
-    ClusterBox box;
-    box.lo[0] = a.x; box.lo[1] = a.y; box.lo[2] = a.z; box.p = a.w;
-    box.hi[0] = b.x; box.hi[1] = b.y; box.hi[2] = b.z; box.q = b.w;
-    return !cluster_culled(box, cr, t_best);
+    const float lo[3] = {a.x, a.y, a.z}, hi[3] = {b.x, b.y, b.z};
+    return !box_culled(lo, hi, lc);
 }
 
 // Warp argmin of (t, triangle); lane `src` takes the hit when the minimum t is below t0 (the
@@ -687,19 +685,20 @@ __device__ __forceinline__ void reduce_and_take_lex(BestLex b, float t0, const u
 }
 
 // One ray (lane src) against the clusters [c0, c0 + nc) of records `cl` (cluster_rec(..., 0)).
-__device__ __forceinline__ void coop_leaf_cl(const uint4* __restrict__ cl, uint32_t c0, uint32_t nc,
+__device__ __forceinline__ void coop_leaf_cl(const uint4* __restrict__ cl, uint4 leaf,
                                              const ulonglong2* __restrict__ pairs, int src, LaneRay& r) {
     const unsigned kAll = 0xFFFFFFFFu;
     const unsigned lane = threadIdx.x & 31u;
+    const uint32_t c0 = leaf.x, nc = (leaf.y + kClusterTris - 1u) / kClusterTris;
     const CoopRay c = bcast_ray(r, src);
-    const CullRay cr = bcast_cull_ray(c, r, src);
+    const LeafCull lc = leaf_cull(bcast_cull_ray(c, r, src), __uint_as_float(leaf.z), __uint_as_float(leaf.w), c.ct);
     const f2 OX = f2_pack(c.ox, c.ox), OY = f2_pack(c.oy, c.oy), OZ = f2_pack(c.oz, c.oz);
     const f2 DX = f2_pack(c.dx, c.dx), DY = f2_pack(c.dy, c.dy), DZ = f2_pack(c.dz, c.dz);
     const f2 Z = f2_neg_zero();
     BestLex b{c.ct, 0u};
     for (uint32_t base = 0; base < nc; base += 32u) {
         const uint32_t j = base + lane;
-        const bool live = j < nc && cluster_live(cl + (uint64_t)kClusterRec * (c0 + j), cr, c.ct);
+        const bool live = j < nc && cluster_live(cl + (uint64_t)kClusterRec * (c0 + j), lc);
         unsigned m = __ballot_sync(kAll, live);
         while (m) {
             const uint32_t i = (uint32_t)__ffs(m) - 1u;
@@ -716,15 +715,17 @@ __device__ __forceinline__ void coop_leaf_cl(const uint4* __restrict__ cl, uint3
 
 // Two rays (lanes srcA, srcB) against the same clustered leaf: a cluster is loaded once when
 // either ray needs it, and tested for the rays that need it.
-__device__ __forceinline__ void coop_leaf2_cl(const uint4* __restrict__ cl, uint32_t c0, uint32_t nc,
+__device__ __forceinline__ void coop_leaf2_cl(const uint4* __restrict__ cl, uint4 leaf,
                                               const ulonglong2* __restrict__ pairs, int srcA, int srcB,
                                               LaneRay& r) {
     const unsigned kAll = 0xFFFFFFFFu;
     const unsigned lane = threadIdx.x & 31u;
+    const uint32_t c0 = leaf.x, nc = (leaf.y + kClusterTris - 1u) / kClusterTris;
+    const float Q = __uint_as_float(leaf.z), B = __uint_as_float(leaf.w);
     const CoopRay ca = bcast_ray(r, srcA);
     const CoopRay cb = bcast_ray(r, srcB);
-    const CullRay cra = bcast_cull_ray(ca, r, srcA);
-    const CullRay crb = bcast_cull_ray(cb, r, srcB);
+    const LeafCull lca = leaf_cull(bcast_cull_ray(ca, r, srcA), Q, B, ca.ct);
+    const LeafCull lcb = leaf_cull(bcast_cull_ray(cb, r, srcB), Q, B, cb.ct);
     const bool same_o = __float_as_uint(ca.ox) == __float_as_uint(cb.ox) &&
                         __float_as_uint(ca.oy) == __float_as_uint(cb.oy) &&
                         __float_as_uint(ca.oz) == __float_as_uint(cb.oz);
@@ -740,8 +741,8 @@ __device__ __forceinline__ void coop_leaf2_cl(const uint4* __restrict__ cl, uint
         bool la = false, lb = false;
         if (j < nc) {
             const uint4* rec = cl + (uint64_t)kClusterRec * (c0 + j);
-            la = cluster_live(rec, cra, ca.ct);
-            lb = cluster_live(rec, crb, cb.ct);
+            la = cluster_live(rec, lca);
+            lb = cluster_live(rec, lcb);
         }
         const unsigned ma = __ballot_sync(kAll, la), mb = __ballot_sync(kAll, lb);
         unsigned m = ma | mb;
@@ -772,15 +773,14 @@ __device__ __forceinline__ void coop_leaf2_cl(const uint4* __restrict__ cl, uint
 __device__ __forceinline__ void coop_leaf_any(const ulonglong2* __restrict__ pairs, const uint4* __restrict__ cl,
                                               uint32_t ntris, uint32_t f, uint32_t cnt, int srcA, int srcB,
                                               LaneRay& r) {
-    uint2 rec = make_uint2(0u, 0u);  // {first cluster, leaf triangle count}
-    if (cl != nullptr) rec = __ldg(reinterpret_cast<const uint2*>(cl) + f);
-    if (rec.y != 0u && rec.y == cnt) {
+    uint4 leaf = make_uint4(0u, 0u, 0u, 0u);  // {first cluster, leaf triangle count, Q, B}
+    if (cl != nullptr) leaf = __ldg(cl + f);
+    if (leaf.y != 0u && leaf.y == cnt) {
         const uint4* C = cl + cluster_table_units(ntris);
-        const uint32_t nc = (cnt + kClusterTris - 1u) / kClusterTris;
         if (srcB >= 0)
-            coop_leaf2_cl(C, rec.x, nc, pairs, srcA, srcB, r);
+            coop_leaf2_cl(C, leaf, pairs, srcA, srcB, r);
         else
-            coop_leaf_cl(C, rec.x, nc, pairs, srcA, r);
+            coop_leaf_cl(C, leaf, pairs, srcA, r);
     } else if (srcB >= 0) {
         coop_leaf2(pairs, f, cnt, srcA, srcB, r);
     } else {

@@ -16,25 +16,28 @@
 // P* = o + t* d = v0 + u* e1 + v* e2):
 //   |det - det*| <= E_det = 30 u0 E1 E2 D,  |s.n - s*.n*| <= E_u = 36 u0 S D E2,
 //   |d.q - d.q*| <= E_v = 36 u0 S D E1,     |e2.q - e2.q*| <= E_t = 36 u0 S E1 E2,
-// where D = max|d_i|, E1 / E2 bound |e1_i| / |e2_i| over the cluster and S bounds |o_i - x_i| over
-// the cluster's box.  An accepted triangle has |det| >= 1e-4, so with rho = E_det / 1e-4 < 1 its
-// exact barycentrics are within Du = ((E_u + E_det) / 1e-4 + 2 u0) / (1 - rho) and Dv of the
-// parameter triangle, hence P* lies within R = 2 (Du + Dv + u0) (|e1| + |e2|) of the triangle,
-// and t* <= t + Dt with Dt = ((E_t + t E_det) / 1e-4 + 2 u0 t) / (1 - rho).  P* is on the ray's
-// line: if the line, up to t_best + Dt(t_best), misses the cluster's box grown by R, no triangle
-// of the cluster is accepted below t_best.
+// where D = max|d_i|, E1 / E2 bound |e1_i| / |e2_i| and S bounds |o_i - x_i| over the triangles
+// of the leaf.  An accepted triangle has |det| >= 1e-4, so with rho = E_det / 1e-4 < 1 its exact
+// barycentrics are within Du = ((E_u + E_det) / 1e-4 + 2 u0) / (1 - rho) and Dv of the parameter
+// triangle, hence every coordinate of P* is within R = 2 (Du + Dv + u0) (E1 + E2) of the
+// triangle, and t* <= t + Dt with Dt = ((E_t + t E_det) / 1e-4 + 2 u0 t) / (1 - rho).  P* is on
+// the ray's line: if the line, up to t_best + Dt(t_best), misses a cluster's box grown by R, no
+// triangle of the cluster is accepted below t_best.
 //
-// The evaluation below never culls more than that argument allows: every error term carries a
-// factor 4, 1 / 1e-4 is rounded up to 10102 (>= 1 / 9.9e-5), 1 / (1 - x) is replaced by its upper
-// bound 1 + 2x (x < 1/2), the stored box is widened outward by a relative 4 u0 (it is computed
-// from rounded vertices v0 + e1, v0 + e2), and the grown box gets an extra absolute slack of
-// 8 u0 (|lo| + |hi| + |o| + R) per axis, which exceeds the rounding of the slab arithmetic
-// (lo - g - o) * (1 / d) with the IEEE reciprocal (<= 5.1 u0 (|lo| + R) + 3.1 u0 |o|).  Clusters
-// with non-finite or huge coordinates (sealed with q = +inf), rays with a non-finite or huge
-// component or a reciprocal 1 / d_i that overflows, and clusters where rho is not small are never
-// culled.  Both properties were audited on the CPU against the float test on adversarial rays
-// (aimed at edges, vertices and grazing the plane): no culled cluster held an accepted hit below
-// t_best, and the measured errors stayed below 5 % of the margins.
+// The leaf keeps Q >= E1 + E2 (so E1 E2 <= Q^2 / 4) and B >= every |coordinate| of its clusters'
+// boxes (so S <= |o|_inf + B); the margins are computed once per ray and leaf (leaf_cull) and each
+// cluster then costs one slab test of its box (box_culled).  The evaluation never culls more than
+// the argument allows: every error term carries a factor 4, R another factor 2, 1 / 1e-4 is
+// rounded up to 10102 (>= 1 / 9.9e-5), 1 / (1 - x) is replaced by its upper bound 1 + 2x
+// (x < 1/2), the stored boxes are widened outward by a relative 4 u0 (they are computed from the
+// rounded vertices v0 + e1, v0 + e2), and the grown box gets an extra slack of
+// 8 u0 (2 B + |o_i| + R) per axis, which exceeds the rounding of the slab arithmetic
+// fma(lo, 1 / d, -(o + g) / d) with the IEEE reciprocal (<= 5.1 u0 R + 4.1 u0 |o| + 2.1 u0 |lo|).
+// Leaves with a non-finite or huge coordinate (Q = +inf), rays with a non-finite or huge component
+// or a tiny non-zero d_i (|1 / d_i| >= 1e20), and leaves where rho is not small are never culled.
+// Both properties were audited on the CPU against the float test on adversarial rays (aimed at
+// edges and vertices, grazing the plane, axis-aligned): no culled cluster held an accepted hit
+// below t_best, and the measured errors stayed below 5 % of the margins.
 #pragma once
 
 #include <cfloat>
@@ -52,17 +55,6 @@ namespace bvhgpu {
 // Triangles per cluster: one packed pair per lane of a warp.
 constexpr uint32_t kClusterTris = 64;
 
-// One cluster as stored for the cull: its box (widened outward), p = E1 * E2 and q = E1 + E2,
-// where E1 / E2 are the largest |component| of the triangles' edges e1 = v1 - v0, e2 = v2 - v0.
-// q = +inf marks a cluster that is never culled.
-struct ClusterBox {
-    float lo[3];
-    float p;
-    float hi[3];
-    float q;
-};
-static_assert(sizeof(ClusterBox) == 32, "cluster box layout");
-
 constexpr float kCullUnit = 5.9604645e-8f;  // u0 = 2^-24
 constexpr float kCullSafety = 4.0f;
 constexpr float kCullInvDet = 10102.0f;     // >= 1 / 9.9e-5 > 1 / 1e-4
@@ -73,27 +65,39 @@ BVHGPU_HD float cull_fmin(float a, float b) { return a < b ? a : b; }
 BVHGPU_HD float cull_abs(float a) { return a < 0.0f ? -a : a; }
 BVHGPU_HD float cull_down(float t) { return t < 0.0f ? t * (1.0f + 4.0f * kCullUnit) : t * (1.0f - 4.0f * kCullUnit); }
 BVHGPU_HD float cull_up(float t) { return t < 0.0f ? t * (1.0f - 4.0f * kCullUnit) : t * (1.0f + 4.0f * kCullUnit); }
+#ifdef __CUDACC__
+BVHGPU_HD float cull_fma(float a, float b, float c) { return fmaf(a, b, c); }
+#else
+BVHGPU_HD float cull_fma(float a, float b, float c) { return std::fma(a, b, c); }
+#endif
 
-// Finishes a cluster from the raw min / max of its vertices v0, v0 + e1, v0 + e2 (as computed in
-// float) and the raw E1, E2.  `finite` is false when any input was non-finite.
-BVHGPU_HD ClusterBox cluster_seal(const float lo[3], const float hi[3], float e1max, float e2max, bool finite) {
-    ClusterBox c;
+// A cluster sealed for the cull: its box widened outward, and its contributions to the leaf's
+// Q (E1 + E2, rounded up; +inf for a non-finite or huge cluster) and B (largest |coordinate|).
+struct ClusterSeal {
+    float lo[3], hi[3];
+    float q, b;
+};
+
+// From the raw min / max of a cluster's vertices v0, v0 + e1, v0 + e2 (as computed in float) and
+// the raw largest |e1_i|, |e2_i|.  `finite` is false when any input was non-finite.
+BVHGPU_HD ClusterSeal cluster_seal(const float lo[3], const float hi[3], float e1max, float e2max, bool finite) {
+    ClusterSeal c;
     bool ok = finite && e1max < kCullHuge && e2max < kCullHuge;
+    float b = 0.0f;
     for (int i = 0; i < 3; ++i) {
         ok = ok && cull_abs(lo[i]) < kCullHuge && cull_abs(hi[i]) < kCullHuge;
         c.lo[i] = cull_down(lo[i]);
         c.hi[i] = cull_up(hi[i]);
+        b = cull_fmax(b, cull_fmax(cull_abs(c.lo[i]), cull_abs(c.hi[i])));
     }
-    c.p = e1max * e2max * (1.0f + 4.0f * kCullUnit);
     c.q = ok ? (e1max + e2max) * (1.0f + 4.0f * kCullUnit) : INFINITY;
-    if (!ok) {  // keep the box finite so the cull arithmetic never sees inf - inf
+    c.b = ok ? b : 0.0f;
+    if (!ok)  // keep the box finite: the leaf is never culled anyway (q = inf)
         for (int i = 0; i < 3; ++i) c.lo[i] = c.hi[i] = 0.0f;
-        c.p = 0.0f;
-    }
     return c;
 }
 
-// The per-ray part of the cull (origin, direction, IEEE reciprocal, D-scaled error factors).
+// The per-ray part of the cull.
 struct CullRay {
     float o[3], d[3], rd[3];
     float a_det;  // F 30 u0 D
@@ -111,9 +115,10 @@ BVHGPU_HD CullRay cull_ray_rd(float ox, float oy, float oz, float dx, float dy, 
     bool ok = true;
     float D = 0.0f;
     for (int i = 0; i < 3; ++i) {
-        // a zero component is handled exactly; any other must have a finite reciprocal
+        // a zero component is handled exactly; any other needs |1 / d_i| < 1e20 (with |o|, B below
+        // 1e15 no product of the slab arithmetic can overflow)
         ok = ok && cull_abs(r.o[i]) < kCullHuge && cull_abs(r.d[i]) < kCullHuge &&
-             (r.d[i] == 0.0f || cull_abs(r.rd[i]) < FLT_MAX);
+             (r.d[i] == 0.0f || cull_abs(r.rd[i]) < 1e20f);
         D = cull_fmax(D, cull_abs(r.d[i]));
     }
     r.ok = ok;
@@ -126,40 +131,73 @@ BVHGPU_HD CullRay cull_ray(float ox, float oy, float oz, float dx, float dy, flo
     return cull_ray_rd(ox, oy, oz, dx, dy, dz, 1.0f / dx, 1.0f / dy, 1.0f / dz);
 }
 
-// True when no triangle of cluster c can be accepted by the reference's test for the ray with a
-// t below t_best (t_best >= FLT_MAX, or NaN: no bound).
-BVHGPU_HD bool cluster_culled(const ClusterBox& c, const CullRay& r, float t_best) {
+// The per-(ray, leaf) part: the grown slab planes folded with the origin, c_lo = o + g and
+// c_hi = o - g per axis, pre-scaled by 1 / d for the axes where d is not zero, and the largest t
+// that still matters.  on = false: no cluster of this leaf is culled for this ray.
+struct LeafCull {
+    float rd[3], slo[3], shi[3];
+    float thi;
+    bool on;
+    bool zero[3];
+};
+
+BVHGPU_HD LeafCull leaf_cull(const CullRay& r, float Q, float B, float t_best) {
     const float u0 = kCullUnit, K = kCullInvDet;
-    if (!r.ok || !(c.q < kCullHuge)) return false;
-    float S = 0.0f;
-    for (int i = 0; i < 3; ++i)
-        S = cull_fmax(S, cull_fmax(cull_abs(r.o[i] - c.lo[i]), cull_abs(r.o[i] - c.hi[i])));
-    const float e_det = r.a_det * c.p;
-    const float rho = e_det * K;
-    if (!(rho < 0.25f)) return false;
-    const float inv = 1.0f + 2.0f * (rho + 8.0f * u0);  // >= 1 / (1 - rho - 8 u0)
-    const float e_uv = r.b_uv * S * c.q;                 // E_u + E_v
-    const float duv = ((e_uv + 2.0f * e_det) * K + 8.0f * u0) * inv;
-    const float R = 4.0f * (duv + 2.0f * u0) * c.q * 1.0001f + 1e-30f;
-    if (!(R < kCullHuge)) return false;
-    float thi = INFINITY;
-    if (t_best < FLT_MAX) {
-        const float e_t = kCullSafety * 36.0f * u0 * S * c.p;
-        thi = (t_best + ((e_t + t_best * e_det) * K + 4.0f * u0 * t_best) * inv) * (1.0f + 8.0f * u0) + 1e-30f;
-    }
-    float tlo = -INFINITY;
+    LeafCull lc;
+    lc.on = false;
     for (int i = 0; i < 3; ++i) {
-        const float g = R + 8.0f * u0 * (cull_abs(c.lo[i]) + cull_abs(c.hi[i]) + cull_abs(r.o[i]) + R) + 1e-30f;
-        const float lo = c.lo[i] - g, hi = c.hi[i] + g;
-        if (r.d[i] == 0.0f) {
-            if (r.o[i] < lo || r.o[i] > hi) return true;  // the line stays outside this slab
-            continue;
-        }
-        const float t1 = (lo - r.o[i]) * r.rd[i], t2 = (hi - r.o[i]) * r.rd[i];
-        tlo = cull_fmax(tlo, cull_fmin(t1, t2));
-        thi = cull_fmin(thi, cull_fmax(t1, t2));
+        lc.rd[i] = r.rd[i];
+        lc.zero[i] = r.d[i] == 0.0f;
+        lc.slo[i] = lc.shi[i] = 0.0f;
     }
-    return tlo > thi;
+    lc.thi = INFINITY;
+    if (!r.ok || !(Q < kCullHuge) || !(B < kCullHuge)) return lc;
+    const float oinf = cull_fmax(cull_abs(r.o[0]), cull_fmax(cull_abs(r.o[1]), cull_abs(r.o[2])));
+    const float S = (oinf + B) * (1.0f + 4.0f * u0);
+    const float P = 0.25f * Q * Q * (1.0f + 4.0f * u0);  // >= E1 E2
+    const float e_det = r.a_det * P;
+    const float rho = e_det * K;
+    if (!(rho < 0.25f)) return lc;
+    const float inv = 1.0f + 2.0f * (rho + 8.0f * u0);  // >= 1 / (1 - rho - 8 u0)
+    const float e_uv = r.b_uv * S * Q;                   // >= E_u + E_v
+    const float duv = ((e_uv + 2.0f * e_det) * K + 8.0f * u0) * inv;
+    const float R = 4.0f * (duv + 2.0f * u0) * Q * 1.0001f + 1e-30f;
+    if (!(R < kCullHuge)) return lc;
+    if (t_best < FLT_MAX) {
+        const float e_t = kCullSafety * 36.0f * u0 * S * P;
+        lc.thi = (t_best + ((e_t + t_best * e_det) * K + 4.0f * u0 * t_best) * inv) * (1.0f + 8.0f * u0) + 1e-30f;
+    }
+    for (int i = 0; i < 3; ++i) {
+        const float g = R + 8.0f * u0 * (2.0f * B + cull_abs(r.o[i]) + R) + 1e-30f;
+        const float clo = r.o[i] + g, chi = r.o[i] - g;
+        if (lc.zero[i]) {  // the line keeps o_i: culled when the grown slab does not contain it
+            lc.slo[i] = clo;
+            lc.shi[i] = chi;
+        } else {            // t = (lo - c_lo) / d = fma(lo, 1/d, -c_lo / d)
+            lc.slo[i] = -(clo * r.rd[i]);
+            lc.shi[i] = -(chi * r.rd[i]);
+        }
+    }
+    lc.on = true;
+    return lc;
+}
+
+// True when the line of the ray misses the cluster box [lo, hi] grown by the leaf's margins below
+// lc.thi (only meaningful when lc.on).
+BVHGPU_HD bool box_culled(const float lo[3], const float hi[3], const LeafCull& lc) {
+    float tlo = -INFINITY, thi = lc.thi;
+    bool out = false;
+    for (int i = 0; i < 3; ++i) {
+        if (lc.zero[i]) {
+            out = out || lo[i] > lc.slo[i] || hi[i] < lc.shi[i];
+        } else {
+            const float t1 = cull_fma(lo[i], lc.rd[i], lc.slo[i]);
+            const float t2 = cull_fma(hi[i], lc.rd[i], lc.shi[i]);
+            tlo = cull_fmax(tlo, cull_fmin(t1, t2));
+            thi = cull_fmin(thi, cull_fmax(t1, t2));
+        }
+    }
+    return out || tlo > thi;
 }
 
 }  // namespace bvhgpu

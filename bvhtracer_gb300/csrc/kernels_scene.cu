@@ -48,9 +48,22 @@ __global__ void k_write_tris(const float* __restrict__ tris9, uint32_t n, float4
 }
 
 // ---- cluster records of the large leaves, refreshed after every triangle write -------------
-// One warp per cluster: lane p copies the triangles of slots 2p, 2p + 1 (membership fixed at
-// upload) into the record's packed pair p and the warp reduces the cluster's box and edge bounds.
-__global__ void k_cluster_refresh(const float4* __restrict__ tris, uint4* __restrict__ recs, uint32_t ncl) {
+// Leaf maxima first reset by each leaf's first cluster, then one warp per cluster: lane p copies
+// the triangles of slots 2p, 2p + 1 (membership fixed at upload) into the record's packed pair p,
+// the warp reduces the cluster's box and edge bounds, and lane 0 raises its leaf's Q and B
+// (non-negative floats order like their bits, +inf above every finite value).
+__global__ void k_cluster_reset(uint4* __restrict__ table, const uint4* __restrict__ recs, uint32_t ncl) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= ncl) return;
+    const uint32_t f = recs[(uint64_t)kClusterRec * j].w;
+    if (table[f].x == j) {
+        table[f].z = 0u;
+        table[f].w = 0u;
+    }
+}
+
+__global__ void k_cluster_refresh(const float4* __restrict__ tris, uint4* __restrict__ table, uint4* __restrict__ recs,
+                                  uint32_t ncl) {
     const uint32_t j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const unsigned lane = threadIdx.x & 31u;
     if (j >= ncl) return;  // whole warps leave together
@@ -94,10 +107,13 @@ __global__ void k_cluster_refresh(const float4* __restrict__ tris, uint4* __rest
     }
     finite = __all_sync(0xFFFFFFFFu, finite);
     if (lane == 0) {
-        const ClusterBox box = cluster_seal(lo, hi, e1m, e2m, finite);
+        const ClusterSeal cs = cluster_seal(lo, hi, e1m, e2m, finite);
+        const uint32_t f = rec[0].w;
         float4* B = reinterpret_cast<float4*>(rec);
-        B[0] = make_float4(box.lo[0], box.lo[1], box.lo[2], box.p);
-        B[1] = make_float4(box.hi[0], box.hi[1], box.hi[2], box.q);
+        B[0] = make_float4(cs.lo[0], cs.lo[1], cs.lo[2], __uint_as_float(f));
+        B[1] = make_float4(cs.hi[0], cs.hi[1], cs.hi[2], 0.0f);
+        atomicMax(&table[f].z, __float_as_uint(cs.q));
+        atomicMax(&table[f].w, __float_as_uint(cs.b));
     }
 }
 
@@ -843,9 +859,10 @@ cudaError_t launch_write_tris(bvhgpu_ctx* ctx, DeviceBlas& b, const float* d_tri
 cudaError_t launch_cluster_refresh(bvhgpu_ctx* ctx, DeviceBlas& b, cudaStream_t s) {
     if (b.ncl == 0) return cudaSuccess;
     LaunchScope scope(ctx, BVHGPU_K_OTHER, s);
-    k_cluster_refresh<<<grid_for(32u * b.ncl, 128), 128, 0, s>>>(
-        b.tris, b.cl + cluster_table_units(b.ntris), b.ncl);
-    g_launches++;
+    uint4* recs = b.cl + cluster_table_units(b.ntris);
+    k_cluster_reset<<<grid_for(b.ncl, 128), 128, 0, s>>>(b.cl, recs, b.ncl);
+    k_cluster_refresh<<<grid_for(32u * b.ncl, 128), 128, 0, s>>>(b.tris, b.cl, recs, b.ncl);
+    g_launches += 2;
     return cudaGetLastError();
 }
 

@@ -79,7 +79,7 @@ def test_duplicate_triangles_in_different_clusters_tie_to_lowest_index(ctx):
     rng = np.random.default_rng(5)
     base = np.array([[-1, -1, 0, 1, -1, 0, 0, 1, 0]], np.float32)
     other = rng.uniform(-3, 3, (600, 9)).astype(np.float32)
-    other[:, 2::3] += np.float32(2.0)  # behind the duplicates as seen from -z
+    other[:, 2::3] += np.float32(4.0)  # all behind the duplicates (z = 0) as seen from -z
     tris = np.concatenate([other[:300], np.repeat(base, 200, 0), other[300:]])  # 200 exact copies
     perm = rng.permutation(len(tris))
     tris = np.ascontiguousarray(tris[perm])
