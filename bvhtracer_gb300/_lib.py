@@ -107,7 +107,7 @@ SIGNATURES = {
     "bvhgpu_blas_upload": (_I, [_P, _P, _U32, _P, _U32, _P]),
     "bvhgpu_blas_free": (_I, [_P, _U32]),
     "bvhgpu_blas_info": (_I, [_P, _U32, _P, _P, _P]),
-    "bvhgpu_blas_clusters": (_I, [_P, _U32, _P]),
+    "bvhgpu_blas_hidden": (_I, [_P, _U32, _P, _P, _P]),
     "bvhgpu_blas_update_vertices": (_I, [_P, _U32, _P]),
     "bvhgpu_blas_update_vertices_async": (_I, [_P, _U32, _P, _P]),
     "bvhgpu_blas_refit": (_I, [_P, _U32]),

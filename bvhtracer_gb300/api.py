@@ -390,11 +390,12 @@ class Blas:
         ctx.check(ctx.lib.bvhgpu_blas_info(ctx.h, self.id, ctypes.byref(nu), ctypes.byref(nt), ctypes.byref(depth)))
         self.depth = depth.value
 
-    def clusters(self) -> int:
-        """Number of 64-triangle clusters kept for the large leaves (exact culling inside leaves)."""
-        n = ctypes.c_uint32()
-        self.ctx.check(self.ctx.lib.bvhgpu_blas_clusters(self.ctx.h, self.id, ctypes.byref(n)))
-        return n.value
+    def hidden(self) -> dict:
+        """Size of the hidden trees under the large leaves: nodes, pairs, depth below the leaf."""
+        n, p, d = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint32()
+        self.ctx.check(self.ctx.lib.bvhgpu_blas_hidden(self.ctx.h, self.id, ctypes.byref(n), ctypes.byref(p),
+                                                       ctypes.byref(d)))
+        return {"nodes": n.value, "pairs": p.value, "depth": d.value}
 
     def intersect(self, rays: np.ndarray) -> np.ndarray:
         """Bvh::intersect for every ray (host arrays in, host hits out)."""

@@ -126,7 +126,8 @@ void free_blas(DeviceBlas& b) {
     cudaFree(b.counters);
     cudaFree(b.tri_leaf);
     cudaFree(b.leaf_keys);
-    cudaFree(b.cl);
+    cudaFree(b.hx);
+    cudaFree(b.hwork);
     b = DeviceBlas();
 }
 
@@ -226,27 +227,63 @@ uint32_t spread3(uint32_t x) {
     return x;
 }
 
-// Clusters of the leaves with at least kClusterMinLeaf triangles: each such leaf's triangles in
-// the Morton order of their centroids (10 bits per axis inside the leaf's box, ties by triangle
-// index), kClusterTris per cluster, the last one padded.  Returns the device image of GBlas::cl
-// with the table, each record's leaf and the slot indices filled in (the refresh kernel writes
-// boxes, pairs and the leaves' Q and B), or an empty vector when no leaf is large enough.
-std::vector<uint4> plan_clusters(const bvhgpu_node* nodes, const std::vector<uint32_t>& leaves,
-                                 const bvhgpu_triangle* tris, uint32_t ntris, uint32_t* ncl_out) {
-    uint64_t ncl = 0;
-    for (uint32_t li : leaves)
-        if (nodes[li].primitive_count >= kClusterMinLeaf)
-            ncl += (nodes[li].primitive_count + kClusterTris - 1) / kClusterTris;
-    *ncl_out = (uint32_t)ncl;
-    if (ncl == 0) return {};
-    const uint64_t head = cluster_table_units(ntris);
-    std::vector<uint4> img(head + kClusterRec * ncl, make_uint4(0u, 0u, 0u, 0u));
-    uint4* table = img.data();
+// Hidden trees over the leaves with at least kHiddenMinLeaf triangles.  A leaf's triangles are put
+// in the Morton order of their centroids (10 bits per axis inside the leaf's box, ties by
+// triangle index) and split in halves (the left half rounded up to an even size) down to at most
+// kHiddenLeafTris triangles, which are stored as packed pairs (a padding slot is all zero with
+// index 0xFFFFFFFF).  Hidden nodes get indices from nodes_used on, children adjacent, allocated
+// depth first; the boxes and the leaf bounds Q, B are written by the refresh kernel from `work`.
+struct HiddenPlan {
+    std::vector<float> nodes;  // 8 floats per hidden node (boxes 0 until refreshed)
+    std::vector<uint4> table;  // ntris entries (empty: no hidden tree)
+    std::vector<uint2> slots;  // per hidden pair
+    std::vector<uint4> work;   // per hidden node, then per hidden root
+    uint32_t nhid = 0, nhp = 0, depth = 0;
+};
+constexpr uint32_t kWorkRoot = 0x80000000u;
+
+void plan_hidden(const bvhgpu_node* nodes, uint32_t nodes_used, const std::vector<uint32_t>& leaves,
+                 const bvhgpu_triangle* tris, uint32_t ntris, HiddenPlan& hp) {
+    const uint32_t P0 = pairs_in_order(ntris);
     std::vector<std::pair<uint32_t, uint32_t>> keys;
-    uint32_t c0 = 0;
+    std::vector<uint4> roots;
+    // (first, count) of the subtree over keys[a, b); its pairs are allocated contiguously
+    auto make = [&](auto&& self, uint32_t a, uint32_t b, uint32_t depth) -> uint2 {
+        hp.depth = std::max(hp.depth, depth);
+        if (b - a <= kHiddenLeafTris) {
+            const uint32_t np = (b - a + 1) / 2;
+            const uint32_t p0 = P0 + hp.nhp;
+            for (uint32_t q = 0; q < np; ++q) {
+                const uint32_t s0 = a + 2 * q;
+                hp.slots.push_back(make_uint2(keys[s0].second, s0 + 1 < b ? keys[s0 + 1].second : kMiss));
+            }
+            hp.nhp += np;
+            return make_uint2(p0, kHiddenLeaf | np);
+        }
+        const uint32_t m = a + ((((b - a) / 2) + 1) & ~1u);
+        const uint32_t li = hp.nhid;
+        hp.nhid += 2;
+        hp.nodes.resize(8ull * hp.nhid, 0.0f);
+        hp.work.resize(hp.nhid);
+        const uint32_t pa = P0 + hp.nhp;
+        const uint2 L = self(self, a, m, depth + 1);
+        const uint32_t pm = P0 + hp.nhp;
+        const uint2 R = self(self, m, b, depth + 1);
+        const uint32_t pb = P0 + hp.nhp;
+        const uint2 meta[2] = {L, R};
+        for (int c = 0; c < 2; ++c) {
+            float* o = &hp.nodes[8ull * (li + c)];
+            std::memcpy(&o[3], &meta[c].x, 4);
+            std::memcpy(&o[7], &meta[c].y, 4);
+        }
+        hp.work[li] = make_uint4(pa, pm, nodes_used + li, 0u);
+        hp.work[li + 1] = make_uint4(pm, pb, nodes_used + li + 1, 0u);
+        return make_uint2(nodes_used + li, 0u);
+    };
     for (uint32_t li : leaves) {
         const bvhgpu_node& n = nodes[li];
-        if (n.primitive_count < kClusterMinLeaf) continue;
+        if (n.primitive_count < kHiddenMinLeaf) continue;
+        if (hp.table.empty()) hp.table.assign(ntris, make_uint4(0u, 0u, 0u, 0u));
         keys.clear();
         for (uint32_t k = 0; k < n.primitive_count; ++k) {
             const float* v = tris[n.left_first + k].vertices;
@@ -261,21 +298,12 @@ std::vector<uint4> plan_clusters(const bvhgpu_node* nodes, const std::vector<uin
             keys.push_back({code, n.left_first + k});
         }
         std::sort(keys.begin(), keys.end());
-        table[n.left_first] = make_uint4(c0, n.primitive_count, 0u, 0u);
-        const uint32_t nc = (n.primitive_count + kClusterTris - 1) / kClusterTris;
-        for (uint32_t j = 0; j < nc; ++j) {
-            uint4* rec = img.data() + head + (uint64_t)kClusterRec * (c0 + j);
-            rec[0].w = n.left_first;  // the leaf's table entry (boxes, pairs, Q, B: refresh kernel)
-            uint2* slots = reinterpret_cast<uint2*>(rec + kClusterIdx);
-            for (uint32_t p = 0; p < kClusterTris / 2; ++p) {
-                const uint64_t s0 = (uint64_t)j * kClusterTris + 2 * p;
-                slots[p].x = s0 < keys.size() ? keys[s0].second : kMiss;
-                slots[p].y = s0 + 1 < keys.size() ? keys[s0 + 1].second : kMiss;
-            }
-        }
-        c0 += nc;
+        const uint32_t pa = P0 + hp.nhp;
+        const uint2 root = make(make, 0, n.primitive_count, 0);
+        hp.table[n.left_first] = make_uint4(root.x, root.y, 0u, 0u);
+        roots.push_back(make_uint4(pa, P0 + hp.nhp, kWorkRoot | n.left_first, 0u));
     }
-    return img;
+    hp.work.insert(hp.work.end(), roots.begin(), roots.end());
 }
 
 }  // namespace
@@ -474,7 +502,6 @@ int bvhgpu_blas_upload(bvhgpu_ctx* ctx, const bvhgpu_node* nodes, uint32_t nodes
     b.nodes_used = nodes_used;
     b.ntris = ntris;
     b.nleaves = (uint32_t)leaves.size();
-    b.depth = depth;
     b.root_count = nodes[0].primitive_count;
     b.root_first = nodes[0].left_first;
     std::vector<float> packed;
@@ -483,24 +510,34 @@ int bvhgpu_blas_upload(bvhgpu_ctx* ctx, const bvhgpu_node* nodes, uint32_t nodes
     std::vector<unsigned long long> key_init(6 * std::max<size_t>(1, leaves.size()), 0ull);
     for (size_t li = 0; li < key_init.size() / 6; ++li)
         for (int k = 0; k < 3; ++k) key_init[6 * li + k] = 0xFFFFFFFFFFFFFFFFull;
-    const std::vector<uint4> cl_img = plan_clusters(nodes, leaves, tris, ntris, &b.ncl);
+    HiddenPlan hp;
+    plan_hidden(nodes, nodes_used, leaves, tris, ntris, hp);
+    b.nhid = hp.nhid;
+    b.nhp = hp.nhp;
+    b.nwork = (uint32_t)hp.work.size();
+    b.ref_depth = depth;
+    b.depth = depth + hp.depth;
+    const uint64_t nodes_all = (uint64_t)nodes_used + hp.nhid;
+    const uint64_t pairs_all = (uint64_t)pairs_in_order(ntris) + hp.nhp;
+    const uint64_t hx_bytes = hp.table.empty() ? 0 : 16ull * ntris + 8ull * std::max<uint32_t>(1, hp.nhp);
     void* d_tris9 = nullptr;
     cudaError_t e = cudaSuccess;
     auto cleanup = [&]() {
         cudaFree(d_tris9);
         free_blas(b);
     };
-    if ((e = cudaMalloc(&b.nodes, 32ull * nodes_used)) != cudaSuccess ||
+    if ((e = cudaMalloc(&b.nodes, 32ull * nodes_all)) != cudaSuccess ||
         (e = cudaMalloc(&b.tris, 48ull * ntris)) != cudaSuccess ||
         (e = cudaMalloc(&b.verts, 48ull * ntris)) != cudaSuccess ||
-        (e = cudaMalloc(&b.pairs, 80ull * ((ntris + 1) / 2))) != cudaSuccess ||
+        (e = cudaMalloc(&b.pairs, 80ull * pairs_all)) != cudaSuccess ||
         (e = cudaMalloc(&b.parent, 4ull * nodes_used)) != cudaSuccess ||
         (e = cudaMalloc(&b.leaves, 4ull * std::max<size_t>(1, leaves.size()))) != cudaSuccess ||
         (e = cudaMalloc(&b.counters, 4ull * nodes_used)) != cudaSuccess ||
         (e = cudaMalloc(&b.tri_leaf, 4ull * ntris)) != cudaSuccess ||
         (e = cudaMalloc(&b.leaf_keys, 48ull * std::max<size_t>(1, leaves.size()))) != cudaSuccess ||
         (e = cudaMalloc(&d_tris9, 36ull * ntris)) != cudaSuccess ||
-        (b.ncl && (e = cudaMalloc(&b.cl, 16ull * cl_img.size())) != cudaSuccess)) {
+        (hx_bytes && (e = cudaMalloc(&b.hx, hx_bytes)) != cudaSuccess) ||
+        (b.nwork && (e = cudaMalloc(&b.hwork, 16ull * b.nwork)) != cudaSuccess)) {
         cleanup();
         return fail(ctx, BVHGPU_ERR_OUT_OF_MEMORY, "blas_upload: %s", cudaGetErrorString(e));
     }
@@ -510,9 +547,14 @@ int bvhgpu_blas_upload(bvhgpu_ctx* ctx, const bvhgpu_node* nodes, uint32_t nodes
         (e = cudaMemset(b.counters, 0, 4ull * nodes_used)) != cudaSuccess ||
         (e = cudaMemcpy(b.tri_leaf, tri_leaf.data(), 4ull * ntris, cudaMemcpyHostToDevice)) != cudaSuccess ||
         (e = cudaMemcpy(b.leaf_keys, key_init.data(), 8ull * key_init.size(), cudaMemcpyHostToDevice)) != cudaSuccess ||
-        (e = cudaMemset(b.pairs, 0, 80ull * ((ntris + 1) / 2))) != cudaSuccess ||
+        (e = cudaMemset(b.pairs, 0, 80ull * pairs_all)) != cudaSuccess ||
         (e = cudaMemcpy(d_tris9, tris, 36ull * ntris, cudaMemcpyHostToDevice)) != cudaSuccess ||
-        (b.ncl && (e = cudaMemcpy(b.cl, cl_img.data(), 16ull * cl_img.size(), cudaMemcpyHostToDevice)) != cudaSuccess) ||
+        (hp.nhid && (e = cudaMemcpy(b.nodes + 2ull * nodes_used, hp.nodes.data(), 32ull * hp.nhid,
+                                    cudaMemcpyHostToDevice)) != cudaSuccess) ||
+        (hx_bytes && (e = cudaMemcpy(b.hx, hp.table.data(), 16ull * ntris, cudaMemcpyHostToDevice)) != cudaSuccess) ||
+        (hx_bytes && hp.nhp &&
+         (e = cudaMemcpy(b.hx + ntris, hp.slots.data(), 8ull * hp.nhp, cudaMemcpyHostToDevice)) != cudaSuccess) ||
+        (b.nwork && (e = cudaMemcpy(b.hwork, hp.work.data(), 16ull * b.nwork, cudaMemcpyHostToDevice)) != cudaSuccess) ||
         (e = launch_write_tris(ctx, b, static_cast<const float*>(d_tris9), ctx->stream)) != cudaSuccess ||
         (e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess) {
         cleanup();
@@ -541,15 +583,17 @@ int bvhgpu_blas_info(bvhgpu_ctx* ctx, uint32_t blas_id, uint32_t* nodes_used, ui
     if (!b) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown BLAS %u", blas_id);
     if (nodes_used) *nodes_used = b->nodes_used;
     if (ntris) *ntris = b->ntris;
-    if (depth) *depth = b->depth;
+    if (depth) *depth = b->ref_depth;
     return BVHGPU_OK;
 }
 
-int bvhgpu_blas_clusters(bvhgpu_ctx* ctx, uint32_t blas_id, uint32_t* nclusters) {
-    if (!ctx || !nclusters) return BVHGPU_ERR_INVALID_ARG;
+int bvhgpu_blas_hidden(bvhgpu_ctx* ctx, uint32_t blas_id, uint32_t* nodes, uint32_t* pairs, uint32_t* depth) {
+    if (!ctx) return BVHGPU_ERR_INVALID_ARG;
     DeviceBlas* b = find_blas(ctx, blas_id);
     if (!b) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown BLAS %u", blas_id);
-    *nclusters = b->ncl;
+    if (nodes) *nodes = b->nhid;
+    if (pairs) *pairs = b->nhp;
+    if (depth) *depth = b->depth - b->ref_depth;
     return BVHGPU_OK;
 }
 
@@ -831,7 +875,7 @@ int bvhgpu_scene_create(bvhgpu_ctx* ctx, const uint32_t* blas_ids, uint32_t nobj
             g.nodes = b->nodes;
             g.tris = b->tris;
             g.pairs = b->pairs;
-            g.cl = b->cl;
+            g.hx = b->hx;
             g.nodes_used = b->nodes_used;
             g.ntris = b->ntris;
             g.root_count = b->root_count;

@@ -31,28 +31,27 @@ struct GBlas {
     // Triangle pairs (2p, 2p+1) interleaved for packed f32x2 math: 20 floats per pair, component
     // c of {v0x v0y v0z e1x e1y e1z e2x e2y e2z} of triangle 2p + h at float 2c + h.
     const ulonglong2* pairs;
-    // Clusters of the large leaves (null when none): a table of ntris uint4 entries read at each
-    // leaf's first triangle, {first cluster, leaf triangle count, Q bits, B bits} ({0, 0, ...}:
-    // not clustered; a count that differs from the leaf's: not this leaf's clusters; Q and B as
-    // in cull.cuh), then one kClusterRec-uint4 record per cluster, ceil(count / 64) per leaf.
-    const uint4* cl;
+    // Hidden trees of the large leaves (null when none): ntris uint4 entries read at a leaf's first
+    // triangle, {first, count} of the hidden root node (both 0: no hidden tree) and the leaf's Q and
+    // B bits (cull.cuh), then one uint2 per hidden pair p >= (ntris + 1) / 2: the triangle indices
+    // of its two slots (0xFFFFFFFF: padding).  Hidden nodes follow the reference's nodes_used nodes
+    // in `nodes` (a node whose children start at or beyond nodes_used is hidden); a hidden leaf has
+    // count = kHiddenLeaf | pairs and first = its first pair in `pairs`, after the (ntris + 1) / 2
+    // pairs in triangle order.
+    const uint4* hx;
     uint32_t nodes_used;
     uint32_t ntris;
     uint32_t root_count;  // root node meta (node 0)
     uint32_t root_first;
 };
 
-// Cluster record, in 16-byte units: [0, 2) the cluster's widened box {lo.xyz, table index of its
-// leaf (bits)}, {hi.xyz, 0}; [2, 18) uint2 triangle index of slots (2p, 2p + 1) for pair
-// p = 0..31 (0xFFFFFFFF: padding); [18, 178) the 32 pairs in the packed layout of GBlas::pairs
-// (5 x 16 bytes each, padding slots all zero).
-constexpr uint32_t kClusterRec = 178;
-constexpr uint32_t kClusterIdx = 2;
-constexpr uint32_t kClusterPairs = 18;
-// Leaves with fewer triangles are not clustered.
-constexpr uint32_t kClusterMinLeaf = 128;
+constexpr uint32_t kHiddenLeaf = 0x80000000u;
+// Reference leaves with at least this many triangles get a hidden tree, whose leaves hold at most
+// kHiddenLeafTris triangles (two packed pairs).
+constexpr uint32_t kHiddenMinLeaf = 16;
+constexpr uint32_t kHiddenLeafTris = 4;
 
-__host__ __device__ __forceinline__ uint64_t cluster_table_units(uint32_t ntris) { return ntris; }
+__host__ __device__ __forceinline__ uint32_t pairs_in_order(uint32_t ntris) { return (ntris + 1u) / 2u; }
 
 struct GHit {
     float t, u, v;
@@ -209,158 +208,6 @@ __device__ __forceinline__ void test_leaf_lane(const float4* __restrict__ tris, 
     }
 }
 
-// ---- traversal stacks -------------------------------------------------------------------------
-// An entry is a pending far child, (count, first) of its node.
-//
-// SplitStack: the newest RK entries live in registers as a shift register (every index is a
-// compile-time constant, so nothing goes to local memory); older entries spill to this thread's
-// column of a shared-memory array (entry k at col[k * blockDim.x]: consecutive lanes hit
-// consecutive 8-byte words, no bank conflicts).  A kernel using it takes
-// kSharedEntries * 8 * blockDim.x bytes of dynamic shared memory and calls bind() once.
-template <int RK, int SK>
-struct SplitStack {
-    static_assert(RK >= 1, "at least one register entry");
-    static constexpr int kCap = RK + SK;
-    static constexpr int kSharedEntries = SK;
-    uint2 reg[RK];
-    uint2* col;
-    int sp;
-
-    __device__ __forceinline__ void bind(uint2* smem) { col = smem + threadIdx.x; }
-    __device__ __forceinline__ void clear() { sp = 0; }
-    __device__ __forceinline__ bool empty() const { return sp == 0; }
-    __device__ __forceinline__ bool full() const { return sp >= kCap; }
-    __device__ __forceinline__ void push(uint2 e) {
-        if (SK > 0 && sp >= RK) col[(sp - RK) * blockDim.x] = reg[RK - 1];
-#pragma unroll
-        for (int k = RK - 1; k > 0; --k) reg[k] = reg[k - 1];
-        reg[0] = e;
-        ++sp;
-    }
-    __device__ __forceinline__ uint2 pop() {
-        const uint2 e = reg[0];
-#pragma unroll
-        for (int k = 0; k < RK - 1; ++k) reg[k] = reg[k + 1];
-        if (SK > 0 && sp > RK) reg[RK - 1] = col[(sp - RK - 1) * blockDim.x];
-        --sp;
-        return e;
-    }
-};
-
-// LocalStack: a plain per-thread array (local memory, cached in L1), for the rare deep trees.
-template <int N>
-struct LocalStack {
-    static constexpr int kCap = N;
-    static constexpr int kSharedEntries = 0;
-    uint2 s[N];
-    int sp;
-
-    __device__ __forceinline__ void bind(uint2*) {}
-    __device__ __forceinline__ void clear() { sp = 0; }
-    __device__ __forceinline__ bool empty() const { return sp == 0; }
-    __device__ __forceinline__ bool full() const { return sp >= N; }
-    __device__ __forceinline__ void push(uint2 e) { s[sp++] = e; }
-    __device__ __forceinline__ uint2 pop() { return s[--sp]; }
-};
-
-template <class STK>
-struct TravT {
-    STK stk;
-    uint32_t cnt, first, steps, max_steps;
-
-    __device__ __forceinline__ void init(const GBlas& b) {
-        stk.clear();
-        cnt = b.root_count;
-        first = b.root_first;
-        steps = 0;
-        max_steps = 2u * b.nodes_used + 16u;
-    }
-
-    __device__ __forceinline__ bool pop() {
-        if (stk.empty()) return true;
-        const uint2 e = stk.pop();
-        cnt = e.x;
-        first = e.y;
-        return false;
-    }
-
-    // Processes one node.  Leaves with more than `big_leaf` triangles are not tested here:
-    // the step returns kStepBigLeaf with (first, cnt) describing the leaf, and the caller
-    // tests it (warp-cooperatively) and then calls pop().
-    __device__ __forceinline__ StepResult step(const GBlas& b, LaneRay& r, uint32_t big_leaf, uint32_t* err) {
-        if (++steps > max_steps) {
-            atomicOr(err, kErrSteps);
-            return kStepFinished;
-        }
-        if (cnt > 0) {
-            if (cnt > big_leaf) return kStepBigLeaf;
-            test_leaf_lane(b.tris, first, cnt, r);
-            return pop() ? kStepFinished : kStepContinue;
-        }
-        const float4* N = b.nodes + 2ull * first;
-        float4 l0 = __ldg(N);
-        float4 l1 = __ldg(N + 1);
-        float4 r0 = __ldg(N + 2);
-        float4 r1 = __ldg(N + 3);
-        float dl, dr;
-        bool hl = slab(l0, l1, r.o, r.rd, r.ct, dl);
-        bool hr = slab(r0, r1, r.o, r.rd, r.ct, dr);
-        float kl = hl ? dl : FLT_MAX;
-        float kr = hr ? dr : FLT_MAX;
-        bool left_near = kl < kr;
-        bool near_hit = left_near ? hl : hr;
-        bool far_hit = left_near ? hr : hl;
-        if (near_hit) {
-            if (far_hit) {
-                if (stk.full()) {
-                    atomicOr(err, kErrStack);
-                    return kStepFinished;
-                }
-                stk.push(left_near ? make_uint2(ubits(r1.w), ubits(r0.w)) : make_uint2(ubits(l1.w), ubits(l0.w)));
-            }
-            cnt = left_near ? ubits(l1.w) : ubits(r1.w);
-            first = left_near ? ubits(l0.w) : ubits(r0.w);
-            return kStepContinue;
-        }
-        return pop() ? kStepFinished : kStepContinue;
-    }
-
-    // Steps until the lane finishes or stops at a big leaf.
-    __device__ __forceinline__ StepResult advance(const GBlas& b, LaneRay& r, uint32_t big_leaf, uint32_t* err) {
-        for (;;) {
-            StepResult s = step(b, r, big_leaf, err);
-            if (s != kStepContinue) return s;
-        }
-    }
-};
-
-// The local-memory traversal used where no tuned variant applies (render, adjoint).
-template <int STACK>
-using Trav = TravT<LocalStack<STACK>>;
-
-// Whole traversal by one lane, every leaf tested by the lane itself.
-template <int STACK>
-__device__ __forceinline__ bool trace_blas(const GBlas& b, float3 o, float3 d, float3 rd, float& closest_t,
-                                           float& hu, float& hv, uint32_t& hprim, uint32_t* err) {
-    Trav<STACK> tr;
-    tr.init(b);
-    LaneRay r;
-    r.o = o;
-    r.d = d;
-    r.rd = rd;
-    r.ct = closest_t;
-    r.hu = hu;
-    r.hv = hv;
-    r.hp = hprim;
-    r.hit = false;
-    tr.advance(b, r, 0xFFFFFFFFu, err);
-    closest_t = r.ct;
-    hu = r.hu;
-    hv = r.hv;
-    hprim = r.hp;
-    return r.hit;
-}
-
 // ---- packed f32x2 arithmetic (Blackwell) ---------------------------------------------------
 // add/sub/mul.rn.f32x2 operate on two IEEE binary32 values with round-to-nearest each, i.e.
 // exactly two of the scalar __fadd_rn / __fsub_rn / __fmul_rn above; no multiply-add is fused.
@@ -469,6 +316,233 @@ __device__ __forceinline__ PairHit ray_terms(const PairData& p, const OriginTerm
     h.okB = okB_in && !(fabsf(aB) < kThreshold) && !(h.uB < 0.0f || h.uB > 1.0f) && !(h.vB < 0.0f || uvB > 1.0f) &&
             (h.tB > kThreshold);
     return h;
+}
+
+// ---- traversal stacks -------------------------------------------------------------------------
+// An entry is a pending far child, (count, first) of its node.
+//
+// SplitStack: the newest RK entries live in registers as a shift register (every index is a
+// compile-time constant, so nothing goes to local memory); older entries spill to this thread's
+// column of a shared-memory array (entry k at col[k * blockDim.x]: consecutive lanes hit
+// consecutive 8-byte words, no bank conflicts).  A kernel using it takes
+// kSharedEntries * 8 * blockDim.x bytes of dynamic shared memory and calls bind() once.
+template <int RK, int SK>
+struct SplitStack {
+    static_assert(RK >= 1, "at least one register entry");
+    static constexpr int kCap = RK + SK;
+    static constexpr int kSharedEntries = SK;
+    uint2 reg[RK];
+    uint2* col;
+    int sp;
+
+    __device__ __forceinline__ void bind(uint2* smem) { col = smem + threadIdx.x; }
+    __device__ __forceinline__ void clear() { sp = 0; }
+    __device__ __forceinline__ bool empty() const { return sp == 0; }
+    __device__ __forceinline__ bool full() const { return sp >= kCap; }
+    __device__ __forceinline__ void push(uint2 e) {
+        if (SK > 0 && sp >= RK) col[(sp - RK) * blockDim.x] = reg[RK - 1];
+#pragma unroll
+        for (int k = RK - 1; k > 0; --k) reg[k] = reg[k - 1];
+        reg[0] = e;
+        ++sp;
+    }
+    __device__ __forceinline__ uint2 pop() {
+        const uint2 e = reg[0];
+#pragma unroll
+        for (int k = 0; k < RK - 1; ++k) reg[k] = reg[k + 1];
+        if (SK > 0 && sp > RK) reg[RK - 1] = col[(sp - RK - 1) * blockDim.x];
+        --sp;
+        return e;
+    }
+};
+
+// LocalStack: a plain per-thread array (local memory, cached in L1), for the rare deep trees.
+template <int N>
+struct LocalStack {
+    static constexpr int kCap = N;
+    static constexpr int kSharedEntries = 0;
+    uint2 s[N];
+    int sp;
+
+    __device__ __forceinline__ void bind(uint2*) {}
+    __device__ __forceinline__ void clear() { sp = 0; }
+    __device__ __forceinline__ bool empty() const { return sp == 0; }
+    __device__ __forceinline__ bool full() const { return sp >= N; }
+    __device__ __forceinline__ void push(uint2 e) { s[sp++] = e; }
+    __device__ __forceinline__ uint2 pop() { return s[--sp]; }
+};
+
+// A hidden leaf (np packed pairs from `first`, in spatial order) against the lane's own ray.  A
+// triangle is taken when its t is below the closest t, or equal to it with a lower triangle index
+// while the held hit came from the same reference leaf (`held`): the reference's in-order leaf loop
+// keeps the lowest index among equal t, and a hit from an earlier leaf keeps equal t out.
+__device__ __forceinline__ bool test_hidden_leaf(const GBlas& b, uint32_t first, uint32_t np, LaneRay& r, bool& held) {
+    const uint2* hidx = reinterpret_cast<const uint2*>(b.hx + b.ntris) - pairs_in_order(b.ntris);
+    const f2 OX = f2_pack(r.o.x, r.o.x), OY = f2_pack(r.o.y, r.o.y), OZ = f2_pack(r.o.z, r.o.z);
+    const f2 DX = f2_pack(r.d.x, r.d.x), DY = f2_pack(r.d.y, r.d.y), DZ = f2_pack(r.d.z, r.d.z);
+    const f2 Z = f2_neg_zero();
+    bool better = false;
+    for (uint32_t q = 0; q < np; ++q) {
+        const uint32_t p = first + q;
+        const uint2 idx = __ldg(hidx + p);
+        const PairData pd = load_pair(b.pairs + 5ull * p);
+        const PairHit h = ray_terms(pd, origin_terms(pd, OX, OY, OZ, Z), DX, DY, DZ, Z, idx.x != kMiss, idx.y != kMiss);
+        if (h.okA && (h.tA < r.ct || (h.tA == r.ct && held && idx.x < r.hp))) {
+            r.ct = h.tA;
+            r.hu = h.uA;
+            r.hv = h.vA;
+            r.hp = idx.x;
+            held = true;
+            better = true;
+        }
+        if (h.okB && (h.tB < r.ct || (h.tB == r.ct && held && idx.y < r.hp))) {
+            r.ct = h.tB;
+            r.hu = h.uB;
+            r.hv = h.vB;
+            r.hp = idx.y;
+            held = true;
+            better = true;
+        }
+    }
+    if (better) {
+        r.hit = true;
+        r.inst = r.inst_cur;
+    }
+    return better;
+}
+
+__device__ __forceinline__ bool hidden_box(float4 lo, float4 hi, float3 rd, const LeafCull& lc, float& t_enter) {
+    const float l[3] = {lo.x, lo.y, lo.z}, h[3] = {hi.x, hi.y, hi.z}, d[3] = {rd.x, rd.y, rd.z};
+    return box_live(l, h, d, lc, t_enter);
+}
+
+template <class STK>
+struct TravT {
+    STK stk;
+    uint32_t cnt, first, steps, max_steps;
+    LeafCull lc;  // the ray's margins in the hidden tree being walked
+    bool held;    // the closest hit came from the reference leaf of that hidden tree
+
+    __device__ __forceinline__ void init(const GBlas& b) {
+        stk.clear();
+        cnt = b.root_count;
+        first = b.root_first;
+        steps = 0;
+        max_steps = 2u * (b.nodes_used + b.ntris) + 16u;  // hidden nodes: fewer than ntris
+        held = false;
+    }
+
+    __device__ __forceinline__ bool pop() {
+        if (stk.empty()) return true;
+        const uint2 e = stk.pop();
+        cnt = e.x;
+        first = e.y;
+        return false;
+    }
+
+    __device__ __forceinline__ bool push(uint2 e, uint32_t* err) {
+        if (stk.full()) {
+            atomicOr(err, kErrStack);
+            return false;
+        }
+        stk.push(e);
+        return true;
+    }
+
+    // Processes one node.  A reference leaf with a hidden tree continues at the tree's root (the
+    // ray's margins computed here); one without, with more than `big_leaf` triangles, is not
+    // tested here: the step returns kStepBigLeaf with (first, cnt) describing the leaf, and the
+    // caller tests it (warp-cooperatively) and then calls pop().
+    __device__ __forceinline__ StepResult step(const GBlas& b, LaneRay& r, uint32_t big_leaf, uint32_t* err) {
+        if (++steps > max_steps) {
+            atomicOr(err, kErrSteps);
+            return kStepFinished;
+        }
+        if (cnt > 0) {
+            if (cnt & kHiddenLeaf) {
+                if (test_hidden_leaf(b, first, cnt & ~kHiddenLeaf, r, held)) lc.thi = leaf_thi(lc, r.ct);
+                return pop() ? kStepFinished : kStepContinue;
+            }
+            if (b.hx != nullptr) {
+                const uint4 e = __ldg(b.hx + first);
+                if ((e.x | e.y) != 0u) {
+                    lc = leaf_cull(cull_ray_rd(r.o.x, r.o.y, r.o.z, r.d.x, r.d.y, r.d.z, r.rd.x, r.rd.y, r.rd.z),
+                                   __uint_as_float(e.z), __uint_as_float(e.w), r.ct);
+                    held = false;
+                    first = e.x;
+                    cnt = e.y;
+                    return kStepContinue;
+                }
+            }
+            if (cnt > big_leaf) return kStepBigLeaf;
+            test_leaf_lane(b.tris, first, cnt, r);
+            return pop() ? kStepFinished : kStepContinue;
+        }
+        const float4* N = b.nodes + 2ull * first;
+        float4 l0 = __ldg(N);
+        float4 l1 = __ldg(N + 1);
+        float4 r0 = __ldg(N + 2);
+        float4 r1 = __ldg(N + 3);
+        float dl, dr;
+        bool hl, hr, left_near;
+        if (first >= b.nodes_used) {  // hidden children: the margins' exact cull, any order
+            hl = hidden_box(l0, l1, r.rd, lc, dl);
+            hr = hidden_box(r0, r1, r.rd, lc, dr);
+            left_near = dl <= dr;
+        } else {
+            hl = slab(l0, l1, r.o, r.rd, r.ct, dl);
+            hr = slab(r0, r1, r.o, r.rd, r.ct, dr);
+            const float kl = hl ? dl : FLT_MAX;
+            const float kr = hr ? dr : FLT_MAX;
+            left_near = kl < kr;
+        }
+        const bool near_hit = left_near ? hl : hr;
+        const bool far_hit = left_near ? hr : hl;
+        if (near_hit) {
+            if (far_hit &&
+                !push(left_near ? make_uint2(ubits(r1.w), ubits(r0.w)) : make_uint2(ubits(l1.w), ubits(l0.w)), err))
+                return kStepFinished;
+            cnt = left_near ? ubits(l1.w) : ubits(r1.w);
+            first = left_near ? ubits(l0.w) : ubits(r0.w);
+            return kStepContinue;
+        }
+        return pop() ? kStepFinished : kStepContinue;
+    }
+
+    // Steps until the lane finishes or stops at a big leaf.
+    __device__ __forceinline__ StepResult advance(const GBlas& b, LaneRay& r, uint32_t big_leaf, uint32_t* err) {
+        for (;;) {
+            StepResult s = step(b, r, big_leaf, err);
+            if (s != kStepContinue) return s;
+        }
+    }
+};
+
+// The local-memory traversal used where no tuned variant applies (render, adjoint).
+template <int STACK>
+using Trav = TravT<LocalStack<STACK>>;
+
+// Whole traversal by one lane, every leaf tested by the lane itself.
+template <int STACK>
+__device__ __forceinline__ bool trace_blas(const GBlas& b, float3 o, float3 d, float3 rd, float& closest_t,
+                                           float& hu, float& hv, uint32_t& hprim, uint32_t* err) {
+    Trav<STACK> tr;
+    tr.init(b);
+    LaneRay r;
+    r.o = o;
+    r.d = d;
+    r.rd = rd;
+    r.ct = closest_t;
+    r.hu = hu;
+    r.hv = hv;
+    r.hp = hprim;
+    r.hit = false;
+    tr.advance(b, r, 0xFFFFFFFFu, err);
+    closest_t = r.ct;
+    hu = r.hu;
+    hv = r.hv;
+    hprim = r.hp;
+    return r.hit;
 }
 
 // Running best of one ray inside a cooperative leaf test (triangle index order kept: a pair's
@@ -611,181 +685,6 @@ __device__ __forceinline__ void coop_leaf2(const ulonglong2* __restrict__ pairs,
     }
     reduce_and_take(ba, pairs, srcA, r);
     reduce_and_take(bb, pairs, srcB, r);
-}
-
-// ---- clustered big-leaf test --------------------------------------------------------------
-// A clustered leaf is tested cluster by cluster: the ray's margins for the leaf are computed once
-// (leaf_cull), lane j decides for clusters j, j + 32, ... whether the ray can have an accepted
-// hit below its closest t there (box_culled, exact: culled clusters hold none), then the warp
-// tests each remaining cluster with one packed pair per lane.  Cluster slots are in spatial (Morton) order, not triangle order, so the running best
-// is the smallest (t, triangle index): the same triangle the reference's in-order loop keeps.
-
-// Running best by (t, triangle).  Starts at (ray t, 0): a triangle is taken only with t below the
-// ray's closest t, and a tie in t goes to the lower triangle index.
-struct BestLex {
-    float t;
-    uint32_t k;
-    __device__ __forceinline__ void take(const PairHit& h, uint2 idx) {
-        if (h.okA && (h.tA < t || (h.tA == t && idx.x < k))) {
-            t = h.tA;
-            k = idx.x;
-        }
-        if (h.okB && (h.tB < t || (h.tB == t && idx.y < k))) {
-            t = h.tB;
-            k = idx.y;
-        }
-    }
-};
-
-__device__ __forceinline__ CullRay bcast_cull_ray(const CoopRay& c, const LaneRay& r, int src) {
-    const unsigned kAll = 0xFFFFFFFFu;
-    const float rx = __shfl_sync(kAll, r.rd.x, src), ry = __shfl_sync(kAll, r.rd.y, src),
-                rz = __shfl_sync(kAll, r.rd.z, src);
-    return cull_ray_rd(c.ox, c.oy, c.oz, c.dx, c.dy, c.dz, rx, ry, rz);
-}
-
-// Whether cluster `rec` may hold an accepted hit for the ray of `lc`.
-__device__ __forceinline__ bool cluster_live(const uint4* __restrict__ rec, const LeafCull& lc) {
-    if (!lc.on) return true;
-    const float4 a = __ldg(reinterpret_cast<const float4*>(rec));
-    const float4 b = __ldg(reinterpret_cast<const float4*>(rec) + 1);
-    const float lo[3] = {a.x, a.y, a.z}, hi[3] = {b.x, b.y, b.z};
-    return !box_culled(lo, hi, lc);
-}
-
-// Warp argmin of (t, triangle); lane `src` takes the hit when the minimum t is below t0 (the
-// ray's closest t when the leaf test began), recomputing u, v as reduce_and_take does.
-__device__ __forceinline__ void reduce_and_take_lex(BestLex b, float t0, const ulonglong2* __restrict__ pairs, int src,
-                                                    LaneRay& r) {
-    const unsigned kAll = 0xFFFFFFFFu;
-    const unsigned lane = threadIdx.x & 31u;
-    float bt = b.t;
-    uint32_t bk = b.k;
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-        const float ot = __shfl_xor_sync(kAll, bt, off);
-        const uint32_t ok = __shfl_xor_sync(kAll, bk, off);
-        if (ot < bt || (ot == bt && ok < bk)) {
-            bt = ot;
-            bk = ok;
-        }
-    }
-    if (bt < t0 && (int)lane == src) {
-        float4 v0, e1, e2;
-        load_pair_tri(pairs, bk, v0, e1, e2);
-        float t, u, v;
-        tri_test(v0, e1, e2, r.o, r.d, t, u, v);
-        r.ct = bt;
-        r.hu = u;
-        r.hv = v;
-        r.hp = bk;
-        r.hit = true;
-        r.inst = r.inst_cur;
-    }
-}
-
-// One ray (lane src) against the clusters [c0, c0 + nc) of records `cl` (cluster_rec(..., 0)).
-__device__ __forceinline__ void coop_leaf_cl(const uint4* __restrict__ cl, uint4 leaf,
-                                             const ulonglong2* __restrict__ pairs, int src, LaneRay& r) {
-    const unsigned kAll = 0xFFFFFFFFu;
-    const unsigned lane = threadIdx.x & 31u;
-    const uint32_t c0 = leaf.x, nc = (leaf.y + kClusterTris - 1u) / kClusterTris;
-    const CoopRay c = bcast_ray(r, src);
-    const LeafCull lc = leaf_cull(bcast_cull_ray(c, r, src), __uint_as_float(leaf.z), __uint_as_float(leaf.w), c.ct);
-    const f2 OX = f2_pack(c.ox, c.ox), OY = f2_pack(c.oy, c.oy), OZ = f2_pack(c.oz, c.oz);
-    const f2 DX = f2_pack(c.dx, c.dx), DY = f2_pack(c.dy, c.dy), DZ = f2_pack(c.dz, c.dz);
-    const f2 Z = f2_neg_zero();
-    BestLex b{c.ct, 0u};
-    for (uint32_t base = 0; base < nc; base += 32u) {
-        const uint32_t j = base + lane;
-        const bool live = j < nc && cluster_live(cl + (uint64_t)kClusterRec * (c0 + j), lc);
-        unsigned m = __ballot_sync(kAll, live);
-        while (m) {
-            const uint32_t i = (uint32_t)__ffs(m) - 1u;
-            m &= m - 1u;
-            const uint4* rec = cl + (uint64_t)kClusterRec * (c0 + base + i);
-            const uint2 idx = __ldg(reinterpret_cast<const uint2*>(rec + kClusterIdx) + lane);
-            const PairData pd = load_pair(reinterpret_cast<const ulonglong2*>(rec + kClusterPairs) + 5u * lane);
-            const OriginTerms ot = origin_terms(pd, OX, OY, OZ, Z);
-            b.take(ray_terms(pd, ot, DX, DY, DZ, Z, idx.x != kMiss, idx.y != kMiss), idx);
-        }
-    }
-    reduce_and_take_lex(b, c.ct, pairs, src, r);
-}
-
-// Two rays (lanes srcA, srcB) against the same clustered leaf: a cluster is loaded once when
-// either ray needs it, and tested for the rays that need it.
-__device__ __forceinline__ void coop_leaf2_cl(const uint4* __restrict__ cl, uint4 leaf,
-                                              const ulonglong2* __restrict__ pairs, int srcA, int srcB,
-                                              LaneRay& r) {
-    const unsigned kAll = 0xFFFFFFFFu;
-    const unsigned lane = threadIdx.x & 31u;
-    const uint32_t c0 = leaf.x, nc = (leaf.y + kClusterTris - 1u) / kClusterTris;
-    const float Q = __uint_as_float(leaf.z), B = __uint_as_float(leaf.w);
-    const CoopRay ca = bcast_ray(r, srcA);
-    const CoopRay cb = bcast_ray(r, srcB);
-    const LeafCull lca = leaf_cull(bcast_cull_ray(ca, r, srcA), Q, B, ca.ct);
-    const LeafCull lcb = leaf_cull(bcast_cull_ray(cb, r, srcB), Q, B, cb.ct);
-    const bool same_o = __float_as_uint(ca.ox) == __float_as_uint(cb.ox) &&
-                        __float_as_uint(ca.oy) == __float_as_uint(cb.oy) &&
-                        __float_as_uint(ca.oz) == __float_as_uint(cb.oz);
-    const f2 AOX = f2_pack(ca.ox, ca.ox), AOY = f2_pack(ca.oy, ca.oy), AOZ = f2_pack(ca.oz, ca.oz);
-    const f2 ADX = f2_pack(ca.dx, ca.dx), ADY = f2_pack(ca.dy, ca.dy), ADZ = f2_pack(ca.dz, ca.dz);
-    const f2 BOX = f2_pack(cb.ox, cb.ox), BOY = f2_pack(cb.oy, cb.oy), BOZ = f2_pack(cb.oz, cb.oz);
-    const f2 BDX = f2_pack(cb.dx, cb.dx), BDY = f2_pack(cb.dy, cb.dy), BDZ = f2_pack(cb.dz, cb.dz);
-    const f2 Z = f2_neg_zero();
-    BestLex ba{ca.ct, 0u};
-    BestLex bb{cb.ct, 0u};
-    for (uint32_t base = 0; base < nc; base += 32u) {
-        const uint32_t j = base + lane;
-        bool la = false, lb = false;
-        if (j < nc) {
-            const uint4* rec = cl + (uint64_t)kClusterRec * (c0 + j);
-            la = cluster_live(rec, lca);
-            lb = cluster_live(rec, lcb);
-        }
-        const unsigned ma = __ballot_sync(kAll, la), mb = __ballot_sync(kAll, lb);
-        unsigned m = ma | mb;
-        while (m) {
-            const uint32_t i = (uint32_t)__ffs(m) - 1u;
-            m &= m - 1u;
-            const bool ta = (ma >> i) & 1u, tb = (mb >> i) & 1u;
-            const uint4* rec = cl + (uint64_t)kClusterRec * (c0 + base + i);
-            const uint2 idx = __ldg(reinterpret_cast<const uint2*>(rec + kClusterIdx) + lane);
-            const bool va = idx.x != kMiss, vb = idx.y != kMiss;
-            const PairData pd = load_pair(reinterpret_cast<const ulonglong2*>(rec + kClusterPairs) + 5u * lane);
-            if (same_o) {
-                const OriginTerms ot = origin_terms(pd, AOX, AOY, AOZ, Z);
-                if (ta) ba.take(ray_terms(pd, ot, ADX, ADY, ADZ, Z, va, vb), idx);
-                if (tb) bb.take(ray_terms(pd, ot, BDX, BDY, BDZ, Z, va, vb), idx);
-            } else {
-                if (ta) ba.take(ray_terms(pd, origin_terms(pd, AOX, AOY, AOZ, Z), ADX, ADY, ADZ, Z, va, vb), idx);
-                if (tb) bb.take(ray_terms(pd, origin_terms(pd, BOX, BOY, BOZ, Z), BDX, BDY, BDZ, Z, va, vb), idx);
-            }
-        }
-    }
-    reduce_and_take_lex(ba, ca.ct, pairs, srcA, r);
-    reduce_and_take_lex(bb, cb.ct, pairs, srcB, r);
-}
-
-// Tests the big leaf [f, f + cnt) for one ray or two (srcB < 0: one): clustered when the BLAS has
-// clusters for it.  `cl` and `ntris` are those of the leaf's BLAS (the same on every lane).
-__device__ __forceinline__ void coop_leaf_any(const ulonglong2* __restrict__ pairs, const uint4* __restrict__ cl,
-                                              uint32_t ntris, uint32_t f, uint32_t cnt, int srcA, int srcB,
-                                              LaneRay& r) {
-    uint4 leaf = make_uint4(0u, 0u, 0u, 0u);  // {first cluster, leaf triangle count, Q, B}
-    if (cl != nullptr) leaf = __ldg(cl + f);
-    if (leaf.y != 0u && leaf.y == cnt) {
-        const uint4* C = cl + cluster_table_units(ntris);
-        if (srcB >= 0)
-            coop_leaf2_cl(C, leaf, pairs, srcA, srcB, r);
-        else
-            coop_leaf_cl(C, leaf, pairs, srcA, r);
-    } else if (srcB >= 0) {
-        coop_leaf2(pairs, f, cnt, srcA, srcB, r);
-    } else {
-        coop_leaf(pairs, f, cnt, srcA, r);
-    }
 }
 
 __device__ __forceinline__ void load_ray(const float4* rays, uint32_t i, float3& o, float3& d, float& t) {

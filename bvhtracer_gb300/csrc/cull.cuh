@@ -1,11 +1,12 @@
-// Conservative culling of triangle clusters inside a leaf, with results identical to testing
+// Conservative culling of groups of triangles inside a leaf, with results identical to testing
 // every triangle.
 //
 // The reference tests every triangle of a leaf with its float Moeller-Trumbore test
-// (triangle.rs:42-72); its BVHs are nearly flat, so leaves hold thousands of triangles.  A leaf is
-// split into clusters of spatially close triangles, and a cluster is skipped for a ray only when
-// no triangle of it can be accepted by that float test with a t below the ray's current closest t
-// -- so the closest hit (and its ties, decided by triangle index) is unchanged.
+// (triangle.rs:42-72); its BVHs are nearly flat, so leaves hold thousands of triangles.  The
+// library puts a hidden tree of boxes over the triangles of each large leaf, and a box is skipped
+// for a ray only when no triangle in it can be accepted by that float test with a t at or below the
+// ray's current closest t -- so the closest hit (and its ties, decided by triangle index) is
+// unchanged.
 //
 // Why skipping is safe.  For float inputs o, d, v0, e1, e2 the test computes (each step rounded,
 // no fused multiply-add) n = d x e2, det = e1.n, s = o - v0, u = (s.n)/det, q = s x e1,
@@ -21,12 +22,15 @@
 // barycentrics are within Du = ((E_u + E_det) / 1e-4 + 2 u0) / (1 - rho) and Dv of the parameter
 // triangle, hence every coordinate of P* is within R = 2 (Du + Dv + u0) (E1 + E2) of the
 // triangle, and t* <= t + Dt with Dt = ((E_t + t E_det) / 1e-4 + 2 u0 t) / (1 - rho).  P* is on
-// the ray's line: if the line, up to t_best + Dt(t_best), misses a cluster's box grown by R, no
-// triangle of the cluster is accepted below t_best.
+// the ray's line: if the line, up to t_best + Dt(t_best), misses a box of triangles grown by R, no
+// triangle in it is accepted at or below t_best.
 //
-// The leaf keeps Q >= E1 + E2 (so E1 E2 <= Q^2 / 4) and B >= every |coordinate| of its clusters'
-// boxes (so S <= |o|_inf + B); the margins are computed once per ray and leaf (leaf_cull) and each
-// cluster then costs one slab test of its box (box_culled).  The evaluation never culls more than
+// Both bounds are symmetric (|t - t*| <= Dt(t)), so an accepted hit (t > 1e-4) also has
+// t* > 1e-4 - Dt(1e-4): parts of the line behind that need no test either.
+//
+// The leaf keeps Q >= E1 + E2 (so E1 E2 <= Q^2 / 4) and B >= every |coordinate| of its boxes (so
+// S <= |o|_inf + B); the margins are computed once per ray and leaf (leaf_cull) and each box then
+// costs one slab test (box_live).  The evaluation never culls more than
 // the argument allows: every error term carries a factor 4, R another factor 2, 1 / 1e-4 is
 // rounded up to 10102 (>= 1 / 9.9e-5), 1 / (1 - x) is replaced by its upper bound 1 + 2x
 // (x < 1/2), the stored boxes are widened outward by a relative 4 u0 (they are computed from the
@@ -36,7 +40,7 @@
 // Leaves with a non-finite or huge coordinate (Q = +inf), rays with a non-finite or huge component
 // or a tiny non-zero d_i (|1 / d_i| >= 1e20), and leaves where rho is not small are never culled.
 // Both properties were audited on the CPU against the float test on adversarial rays (aimed at
-// edges and vertices, grazing the plane, axis-aligned): no culled cluster held an accepted hit
+// edges and vertices, grazing the plane, axis-aligned): no culled box held an accepted hit at or
 // below t_best, and the measured errors stayed below 5 % of the margins.
 #pragma once
 
@@ -51,9 +55,6 @@
 #endif
 
 namespace bvhgpu {
-
-// Triangles per cluster: one packed pair per lane of a warp.
-constexpr uint32_t kClusterTris = 64;
 
 constexpr float kCullUnit = 5.9604645e-8f;  // u0 = 2^-24
 constexpr float kCullSafety = 4.0f;
@@ -71,17 +72,17 @@ BVHGPU_HD float cull_fma(float a, float b, float c) { return fmaf(a, b, c); }
 BVHGPU_HD float cull_fma(float a, float b, float c) { return std::fma(a, b, c); }
 #endif
 
-// A cluster sealed for the cull: its box widened outward, and its contributions to the leaf's
-// Q (E1 + E2, rounded up; +inf for a non-finite or huge cluster) and B (largest |coordinate|).
-struct ClusterSeal {
+// A group of triangles sealed for the cull: its box widened outward, and its contributions to the
+// leaf's Q (E1 + E2, rounded up; +inf for a non-finite or huge group) and B (largest |coordinate|).
+struct GroupSeal {
     float lo[3], hi[3];
     float q, b;
 };
 
-// From the raw min / max of a cluster's vertices v0, v0 + e1, v0 + e2 (as computed in float) and
+// From the raw min / max of a group's vertices v0, v0 + e1, v0 + e2 (as computed in float) and
 // the raw largest |e1_i|, |e2_i|.  `finite` is false when any input was non-finite.
-BVHGPU_HD ClusterSeal cluster_seal(const float lo[3], const float hi[3], float e1max, float e2max, bool finite) {
-    ClusterSeal c;
+BVHGPU_HD GroupSeal group_seal(const float lo[3], const float hi[3], float e1max, float e2max, bool finite) {
+    GroupSeal c;
     bool ok = finite && e1max < kCullHuge && e2max < kCullHuge;
     float b = 0.0f;
     for (int i = 0; i < 3; ++i) {
@@ -132,25 +133,35 @@ BVHGPU_HD CullRay cull_ray(float ox, float oy, float oz, float dx, float dy, flo
 }
 
 // The per-(ray, leaf) part: the grown slab planes folded with the origin, c_lo = o + g and
-// c_hi = o - g per axis, pre-scaled by 1 / d for the axes where d is not zero, and the largest t
-// that still matters.  on = false: no cluster of this leaf is culled for this ray.
+// c_hi = o - g per axis, pre-scaled by -1 / d where d is not zero (slab t = fma(x, 1/d, s)), the
+// largest t that still matters (thi, from the ray's closest t) and the smallest (tlo: accepted hits
+// have t > 1e-4, so t* > 1e-4 - Dt(1e-4)).  thi follows the closest t through leaf_thi.
+// on = false: nothing of this leaf is culled for this ray.  zero: bit i set when d_i == 0.
 struct LeafCull {
-    float rd[3], slo[3], shi[3];
-    float thi;
+    float slo[3], shi[3];
+    float thi, tlo;
+    float dt0, dt1;  // Dt(t) <= dt0 + t dt1 (rounded up)
     bool on;
-    bool zero[3];
+    uint32_t zero;
 };
+
+BVHGPU_HD float leaf_thi(const LeafCull& lc, float t_best) {
+    if (!(t_best < FLT_MAX)) return INFINITY;
+    return (t_best + (lc.dt0 + t_best * lc.dt1)) * (1.0f + 8.0f * kCullUnit) + 1e-30f;
+}
 
 BVHGPU_HD LeafCull leaf_cull(const CullRay& r, float Q, float B, float t_best) {
     const float u0 = kCullUnit, K = kCullInvDet;
     LeafCull lc;
     lc.on = false;
+    lc.zero = 0u;
     for (int i = 0; i < 3; ++i) {
-        lc.rd[i] = r.rd[i];
-        lc.zero[i] = r.d[i] == 0.0f;
+        if (r.d[i] == 0.0f) lc.zero |= 1u << i;
         lc.slo[i] = lc.shi[i] = 0.0f;
     }
     lc.thi = INFINITY;
+    lc.tlo = -INFINITY;
+    lc.dt0 = lc.dt1 = 0.0f;
     if (!r.ok || !(Q < kCullHuge) || !(B < kCullHuge)) return lc;
     const float oinf = cull_fmax(cull_abs(r.o[0]), cull_fmax(cull_abs(r.o[1]), cull_abs(r.o[2])));
     const float S = (oinf + B) * (1.0f + 4.0f * u0);
@@ -163,17 +174,20 @@ BVHGPU_HD LeafCull leaf_cull(const CullRay& r, float Q, float B, float t_best) {
     const float duv = ((e_uv + 2.0f * e_det) * K + 8.0f * u0) * inv;
     const float R = 4.0f * (duv + 2.0f * u0) * Q * 1.0001f + 1e-30f;
     if (!(R < kCullHuge)) return lc;
-    if (t_best < FLT_MAX) {
-        const float e_t = kCullSafety * 36.0f * u0 * S * P;
-        lc.thi = (t_best + ((e_t + t_best * e_det) * K + 4.0f * u0 * t_best) * inv) * (1.0f + 8.0f * u0) + 1e-30f;
-    }
+    const float e_t = kCullSafety * 36.0f * u0 * S * P;
+    // Dt(t) = ((E_t + t E_det) / 1e-4 + 2 u0 t) / (1 - rho) <= dt0 + t dt1
+    lc.dt0 = e_t * K * inv * (1.0f + 4.0f * u0);
+    lc.dt1 = (e_det * K + 4.0f * u0) * inv * (1.0f + 4.0f * u0);
+    lc.thi = leaf_thi(lc, t_best);
+    const float th = 0.0001f;  // the test's threshold (triangle.rs:47)
+    lc.tlo = cull_down(th - (lc.dt0 + th * lc.dt1) * (1.0f + 8.0f * u0)) - 1e-30f;
     for (int i = 0; i < 3; ++i) {
         const float g = R + 8.0f * u0 * (2.0f * B + cull_abs(r.o[i]) + R) + 1e-30f;
         const float clo = r.o[i] + g, chi = r.o[i] - g;
-        if (lc.zero[i]) {  // the line keeps o_i: culled when the grown slab does not contain it
+        if (lc.zero & (1u << i)) {  // the line keeps o_i: culled when the grown slab does not contain it
             lc.slo[i] = clo;
             lc.shi[i] = chi;
-        } else {            // t = (lo - c_lo) / d = fma(lo, 1/d, -c_lo / d)
+        } else {                    // t = (lo - c_lo) / d = fma(lo, 1/d, -c_lo / d)
             lc.slo[i] = -(clo * r.rd[i]);
             lc.shi[i] = -(chi * r.rd[i]);
         }
@@ -182,22 +196,25 @@ BVHGPU_HD LeafCull leaf_cull(const CullRay& r, float Q, float B, float t_best) {
     return lc;
 }
 
-// True when the line of the ray misses the cluster box [lo, hi] grown by the leaf's margins below
-// lc.thi (only meaningful when lc.on).
-BVHGPU_HD bool box_culled(const float lo[3], const float hi[3], const LeafCull& lc) {
-    float tlo = -INFINITY, thi = lc.thi;
+// Whether the line of the ray, between lc.tlo and lc.thi, meets the box [lo, hi] grown by the
+// leaf's margins (always true when !lc.on); t_enter: where it enters (for near-first order).
+BVHGPU_HD bool box_live(const float lo[3], const float hi[3], const float rd[3], const LeafCull& lc, float& t_enter) {
+    t_enter = 0.0f;
+    if (!lc.on) return true;
+    float tlo = lc.tlo, thi = lc.thi;
     bool out = false;
     for (int i = 0; i < 3; ++i) {
-        if (lc.zero[i]) {
+        if (lc.zero & (1u << i)) {
             out = out || lo[i] > lc.slo[i] || hi[i] < lc.shi[i];
         } else {
-            const float t1 = cull_fma(lo[i], lc.rd[i], lc.slo[i]);
-            const float t2 = cull_fma(hi[i], lc.rd[i], lc.shi[i]);
+            const float t1 = cull_fma(lo[i], rd[i], lc.slo[i]);
+            const float t2 = cull_fma(hi[i], rd[i], lc.shi[i]);
             tlo = cull_fmax(tlo, cull_fmin(t1, t2));
             thi = cull_fmin(thi, cull_fmax(t1, t2));
         }
     }
-    return out || tlo > thi;
+    t_enter = tlo;
+    return !out && !(tlo > thi);
 }
 
 }  // namespace bvhgpu

@@ -26,12 +26,16 @@ struct DeviceBlas {
     uint32_t* counters = nullptr;// refit arrival counters, one per node (kept zeroed)
     uint32_t* tri_leaf = nullptr;        // leaf slot (index into `leaves`) of each triangle, or none
     unsigned long long* leaf_keys = nullptr;  // refit reduction keys, 6 per leaf (kept at identity)
-    uint4* cl = nullptr;         // cluster table and records of the large leaves (GBlas::cl), or null
-    uint32_t ncl = 0;            // clusters
+    uint4* hx = nullptr;         // hidden-tree table and pair slots (GBlas::hx), or null
+    uint4* hwork = nullptr;      // refresh work: {first pair, end pair, node index | table index + flag, 0}
+    uint32_t nhid = 0;           // hidden nodes (after the nodes_used reference nodes)
+    uint32_t nhp = 0;            // hidden pairs (after the (ntris + 1) / 2 pairs in triangle order)
+    uint32_t nwork = 0;          // hidden nodes + hidden roots
+    uint32_t ref_depth = 0;      // depth of the reference tree (depth adds the hidden trees')
     uint32_t nodes_used = 0;
     uint32_t ntris = 0;
     uint32_t nleaves = 0;
-    uint32_t depth = 0;
+    uint32_t depth = 0;          // traversal depth: reference tree plus the deepest hidden tree
     uint32_t root_count = 0;
     uint32_t root_first = 0;
 };
@@ -169,8 +173,8 @@ cudaError_t launch_render(bvhgpu_ctx* ctx, const DeviceBlas& b, const bvhgpu_cam
 
 // ---- launchers (kernels_scene.cu) ------------------------------------------------------
 cudaError_t launch_write_tris(bvhgpu_ctx* ctx, DeviceBlas& b, const float* d_tris9, cudaStream_t s);
-// Rewrites the cluster records (pairs, boxes) from b.tris; part of every triangle write.
-cudaError_t launch_cluster_refresh(bvhgpu_ctx* ctx, DeviceBlas& b, cudaStream_t s);
+// Rewrites the hidden trees' pairs, boxes and leaf bounds from b.tris; part of every triangle write.
+cudaError_t launch_hidden_refresh(bvhgpu_ctx* ctx, DeviceBlas& b, cudaStream_t s);
 cudaError_t launch_refit(bvhgpu_ctx* ctx, DeviceBlas& b, cudaStream_t s);
 // Physics (physics.cu).
 cudaError_t launch_world_start_frame(bvhgpu_ctx* ctx, DeviceWorld& w, cudaStream_t s);

@@ -34,7 +34,7 @@ inline GBlas to_gblas(const DeviceBlas& b) {
     g.nodes = b.nodes;
     g.tris = b.tris;
     g.pairs = b.pairs;
-    g.cl = b.cl;
+    g.hx = b.hx;
     g.nodes_used = b.nodes_used;
     g.ntris = b.ntris;
     g.root_count = b.root_count;
@@ -64,10 +64,10 @@ __device__ __forceinline__ void warp_trace_local(const GBlas& b, bool active, La
                 if (group) {
                     const int bb = __ffs(group) - 1;
                     group &= group - 1u;
-                    coop_leaf_any(b.pairs, b.cl, b.ntris, f, c, a, bb, r);
+                    coop_leaf2(b.pairs, f, c, a, bb, r);
                     if ((int)lane == a || (int)lane == bb) st = tr.pop() ? kStepFinished : kStepContinue;
                 } else {
-                    coop_leaf_any(b.pairs, b.cl, b.ntris, f, c, a, -1, r);
+                    coop_leaf(b.pairs, f, c, a, r);
                     if ((int)lane == a) st = tr.pop() ? kStepFinished : kStepContinue;
                 }
             }
@@ -256,7 +256,7 @@ cudaError_t launch_mesh_update(bvhgpu_ctx* ctx, DeviceMesh& m, DeviceBlas& b, cu
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    if ((e = launch_cluster_refresh(ctx, b, s)) != cudaSuccess) return e;
+    if ((e = launch_hidden_refresh(ctx, b, s)) != cudaSuccess) return e;
     return launch_refit(ctx, b, s);
 }
 

@@ -47,56 +47,56 @@ __global__ void k_write_tris(const float* __restrict__ tris9, uint32_t n, float4
     for (int k = 0; k < 9; ++k) P[2 * k] = c[k];
 }
 
-// ---- cluster records of the large leaves, refreshed after every triangle write -------------
-// Leaf maxima first reset by each leaf's first cluster, then one warp per cluster: lane p copies
-// the triangles of slots 2p, 2p + 1 (membership fixed at upload) into the record's packed pair p,
-// the warp reduces the cluster's box and edge bounds, and lane 0 raises its leaf's Q and B
-// (non-negative floats order like their bits, +inf above every finite value).
-__global__ void k_cluster_reset(uint4* __restrict__ table, const uint4* __restrict__ recs, uint32_t ncl) {
+// ---- hidden trees of the large leaves, refreshed after every triangle write -----------------
+// Hidden pairs: the triangles of each pair's two slots (membership fixed at upload) copied into the
+// packed layout.  Then one warp per hidden node (and per hidden root): the widened box of the
+// node's pairs and, for a root, the leaf's bounds Q and B (cull.cuh).
+__global__ void k_hidden_pairs(const float4* __restrict__ tris, const uint2* __restrict__ slots, uint32_t nhp,
+                               float* __restrict__ pairs) {
     const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= ncl) return;
-    const uint32_t f = recs[(uint64_t)kClusterRec * j].w;
-    if (table[f].x == j) {
-        table[f].z = 0u;
-        table[f].w = 0u;
+    if (j >= nhp) return;
+    const uint2 idx = slots[j];
+    float* P = pairs + 20ull * j;
+    for (int h = 0; h < 2; ++h) {
+        const uint32_t k = h ? idx.y : idx.x;
+        float4 v0 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), e1 = v0, e2 = v0;
+        if (k != kMiss) {
+            v0 = tris[3ull * k];
+            e1 = tris[3ull * k + 1];
+            e2 = tris[3ull * k + 2];
+        }
+        const float c[9] = {v0.x, v0.y, v0.z, e1.x, e1.y, e1.z, e2.x, e2.y, e2.z};
+        for (int q = 0; q < 9; ++q) P[2 * q + h] = c[q];
     }
+    P[18] = P[19] = 0.0f;
 }
 
-__global__ void k_cluster_refresh(const float4* __restrict__ tris, uint4* __restrict__ table, uint4* __restrict__ recs,
-                                  uint32_t ncl) {
-    const uint32_t j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+__global__ void k_hidden_boxes(const uint4* __restrict__ work, uint32_t nwork, const float* __restrict__ pairs,
+                               const uint2* __restrict__ slots, uint32_t p0, float4* __restrict__ nodes,
+                               uint4* __restrict__ table) {
+    const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const unsigned lane = threadIdx.x & 31u;
-    if (j >= ncl) return;  // whole warps leave together
-    uint4* rec = recs + (uint64_t)kClusterRec * j;
-    const uint2 idx = reinterpret_cast<const uint2*>(rec + kClusterIdx)[lane];
-    float c[2][9];
+    if (w >= nwork) return;  // whole warps leave together
+    const uint4 job = work[w];
     float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
     float e1m = 0.0f, e2m = 0.0f;
     bool finite = true;
-    for (int h = 0; h < 2; ++h) {
-        const uint32_t k = h ? idx.y : idx.x;
-        for (int q = 0; q < 9; ++q) c[h][q] = 0.0f;
-        if (k == kMiss) continue;
-        const float4 v0 = tris[3ull * k], e1 = tris[3ull * k + 1], e2 = tris[3ull * k + 2];
-        const float v[3] = {v0.x, v0.y, v0.z}, a[3] = {e1.x, e1.y, e1.z}, b[3] = {e2.x, e2.y, e2.z};
-        for (int i = 0; i < 3; ++i) {
-            c[h][i] = v[i];
-            c[h][3 + i] = a[i];
-            c[h][6 + i] = b[i];
-            const float p1 = fadd(v[i], a[i]), p2 = fadd(v[i], b[i]);
-            finite = finite && isfinite(v[i]) && isfinite(a[i]) && isfinite(b[i]) && isfinite(p1) && isfinite(p2);
-            lo[i] = fminf(lo[i], fminf(v[i], fminf(p1, p2)));
-            hi[i] = fmaxf(hi[i], fmaxf(v[i], fmaxf(p1, p2)));
-            e1m = fmaxf(e1m, fabsf(a[i]));
-            e2m = fmaxf(e2m, fabsf(b[i]));
+    for (uint32_t p = job.x + lane; p < job.y; p += 32u) {
+        const uint2 idx = slots[p - p0];
+        const float* P = pairs + 20ull * p;
+        for (int h = 0; h < 2; ++h) {
+            if ((h ? idx.y : idx.x) == kMiss) continue;
+            for (int i = 0; i < 3; ++i) {
+                const float v = P[2 * i + h], a = P[2 * (3 + i) + h], b = P[2 * (6 + i) + h];
+                const float p1 = fadd(v, a), p2 = fadd(v, b);
+                finite = finite && isfinite(v) && isfinite(a) && isfinite(b) && isfinite(p1) && isfinite(p2);
+                lo[i] = fminf(lo[i], fminf(v, fminf(p1, p2)));
+                hi[i] = fmaxf(hi[i], fmaxf(v, fmaxf(p1, p2)));
+                e1m = fmaxf(e1m, fabsf(a));
+                e2m = fmaxf(e2m, fabsf(b));
+            }
         }
     }
-    float* P = reinterpret_cast<float*>(rec + kClusterPairs) + 20u * lane;
-    for (int q = 0; q < 9; ++q) {
-        P[2 * q] = c[0][q];
-        P[2 * q + 1] = c[1][q];
-    }
-    P[18] = P[19] = 0.0f;
     for (int off = 16; off > 0; off >>= 1) {
         for (int i = 0; i < 3; ++i) {
             lo[i] = fminf(lo[i], __shfl_xor_sync(0xFFFFFFFFu, lo[i], off));
@@ -106,14 +106,16 @@ __global__ void k_cluster_refresh(const float4* __restrict__ tris, uint4* __rest
         e2m = fmaxf(e2m, __shfl_xor_sync(0xFFFFFFFFu, e2m, off));
     }
     finite = __all_sync(0xFFFFFFFFu, finite);
-    if (lane == 0) {
-        const ClusterSeal cs = cluster_seal(lo, hi, e1m, e2m, finite);
-        const uint32_t f = rec[0].w;
-        float4* B = reinterpret_cast<float4*>(rec);
-        B[0] = make_float4(cs.lo[0], cs.lo[1], cs.lo[2], __uint_as_float(f));
-        B[1] = make_float4(cs.hi[0], cs.hi[1], cs.hi[2], 0.0f);
-        atomicMax(&table[f].z, __float_as_uint(cs.q));
-        atomicMax(&table[f].w, __float_as_uint(cs.b));
+    if (lane != 0) return;
+    const GroupSeal g = group_seal(lo, hi, e1m, e2m, finite);
+    if (job.z & 0x80000000u) {
+        uint4& e = table[job.z & 0x7FFFFFFFu];
+        e.z = __float_as_uint(g.q);
+        e.w = __float_as_uint(g.b);
+    } else {
+        float4* N = nodes + 2ull * job.z;
+        N[0] = make_float4(g.lo[0], g.lo[1], g.lo[2], N[0].w);
+        N[1] = make_float4(g.hi[0], g.hi[1], g.hi[2], N[1].w);
     }
 }
 
@@ -517,7 +519,7 @@ struct SceneTrav {
         blas.nodes = nullptr;
         blas.tris = nullptr;
         blas.pairs = nullptr;
-        blas.cl = nullptr;
+        blas.hx = nullptr;
         blas.nodes_used = blas.ntris = blas.root_count = blas.root_first = 0;
     }
 
@@ -606,15 +608,12 @@ __device__ __forceinline__ void scene_coop_phase(unsigned pend, SceneTrav<STK, T
                                                  StepResult& st) {
     const unsigned lane = threadIdx.x & 31u;
     const unsigned long long key = reinterpret_cast<unsigned long long>(tr.blas.pairs);
-    const unsigned long long ckey = reinterpret_cast<unsigned long long>(tr.blas.cl);
     while (pend) {
         const int leader = __ffs(pend) - 1;
         const uint32_t f = __shfl_sync(kFull, tr.bt.first, leader);
         const uint32_t c = __shfl_sync(kFull, tr.bt.cnt, leader);
         const unsigned long long lk = __shfl_sync(kFull, key, leader);
         const ulonglong2* P = reinterpret_cast<const ulonglong2*>(lk);
-        const uint4* C = reinterpret_cast<const uint4*>(__shfl_sync(kFull, ckey, leader));
-        const uint32_t nt = __shfl_sync(kFull, tr.blas.ntris, leader);
         unsigned group = __ballot_sync(kFull, ((pend >> lane) & 1u) && tr.bt.first == f && key == lk);
         pend &= ~group;
         while (group) {
@@ -623,10 +622,10 @@ __device__ __forceinline__ void scene_coop_phase(unsigned pend, SceneTrav<STK, T
             if (group) {
                 const int b = __ffs(group) - 1;
                 group &= group - 1u;
-                coop_leaf_any(P, C, nt, f, c, a, b, r);
+                coop_leaf2(P, f, c, a, b, r);
                 if ((int)lane == a || (int)lane == b) st = tr.after_leaf();
             } else {
-                coop_leaf_any(P, C, nt, f, c, a, -1, r);
+                coop_leaf(P, f, c, a, r);
                 if ((int)lane == a) st = tr.after_leaf();
             }
         }
@@ -853,15 +852,17 @@ cudaError_t launch_write_tris(bvhgpu_ctx* ctx, DeviceBlas& b, const float* d_tri
     g_launches++;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    return launch_cluster_refresh(ctx, b, s);
+    return launch_hidden_refresh(ctx, b, s);
 }
 
-cudaError_t launch_cluster_refresh(bvhgpu_ctx* ctx, DeviceBlas& b, cudaStream_t s) {
-    if (b.ncl == 0) return cudaSuccess;
+cudaError_t launch_hidden_refresh(bvhgpu_ctx* ctx, DeviceBlas& b, cudaStream_t s) {
+    if (b.nwork == 0) return cudaSuccess;
     LaunchScope scope(ctx, BVHGPU_K_OTHER, s);
-    uint4* recs = b.cl + cluster_table_units(b.ntris);
-    k_cluster_reset<<<grid_for(b.ncl, 128), 128, 0, s>>>(b.cl, recs, b.ncl);
-    k_cluster_refresh<<<grid_for(32u * b.ncl, 128), 128, 0, s>>>(b.tris, b.cl, recs, b.ncl);
+    const uint32_t p0 = pairs_in_order(b.ntris);
+    const uint2* slots = reinterpret_cast<const uint2*>(b.hx + b.ntris);
+    float* pairs = reinterpret_cast<float*>(b.pairs);
+    k_hidden_pairs<<<grid_for(b.nhp, 256), 256, 0, s>>>(b.tris, slots, b.nhp, pairs + 20ull * p0);
+    k_hidden_boxes<<<grid_for(32u * b.nwork, 128), 128, 0, s>>>(b.hwork, b.nwork, pairs, slots, p0, b.nodes, b.hx);
     g_launches += 2;
     return cudaGetLastError();
 }

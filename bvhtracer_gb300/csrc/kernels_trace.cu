@@ -31,7 +31,7 @@ inline GBlas to_gblas(const DeviceBlas& b) {
     g.nodes = b.nodes;
     g.tris = b.tris;
     g.pairs = b.pairs;
-    g.cl = b.cl;
+    g.hx = b.hx;
     g.nodes_used = b.nodes_used;
     g.ntris = b.ntris;
     g.root_count = b.root_count;
@@ -63,15 +63,12 @@ template <class TR>
 __device__ __forceinline__ void coop_leaf_phase(unsigned pend, const GBlas& blas, TR& tr, LaneRay& r, StepResult& st) {
     const unsigned lane = threadIdx.x & 31u;
     const unsigned long long key = reinterpret_cast<unsigned long long>(blas.pairs);
-    const unsigned long long ckey = reinterpret_cast<unsigned long long>(blas.cl);
     while (pend) {
         const int leader = __ffs(pend) - 1;
         const uint32_t f = __shfl_sync(kFull, tr.first, leader);
         const uint32_t c = __shfl_sync(kFull, tr.cnt, leader);
         const unsigned long long lk = __shfl_sync(kFull, key, leader);
         const ulonglong2* P = reinterpret_cast<const ulonglong2*>(lk);
-        const uint4* C = reinterpret_cast<const uint4*>(__shfl_sync(kFull, ckey, leader));
-        const uint32_t nt = __shfl_sync(kFull, blas.ntris, leader);
         unsigned group = __ballot_sync(kFull, ((pend >> lane) & 1u) && tr.first == f && key == lk);
         pend &= ~group;
         while (group) {
@@ -80,10 +77,10 @@ __device__ __forceinline__ void coop_leaf_phase(unsigned pend, const GBlas& blas
             if (group) {
                 const int b = __ffs(group) - 1;
                 group &= group - 1u;
-                coop_leaf_any(P, C, nt, f, c, a, b, r);
+                coop_leaf2(P, f, c, a, b, r);
                 if ((int)lane == a || (int)lane == b) st = tr.pop() ? kStepFinished : kStepContinue;
             } else {
-                coop_leaf_any(P, C, nt, f, c, a, -1, r);
+                coop_leaf(P, f, c, a, r);
                 if ((int)lane == a) st = tr.pop() ? kStepFinished : kStepContinue;
             }
         }
@@ -304,7 +301,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_trace_batch_persistent(const Ba
     b.nodes = nullptr;
     b.tris = nullptr;
     b.pairs = nullptr;
-    b.cl = nullptr;
+    b.hx = nullptr;
     b.nodes_used = b.ntris = b.root_count = b.root_first = 0;
     LaneRay r;
     TravT<STK> tr;

@@ -227,12 +227,13 @@ int bvhgpu_blas_upload(bvhgpu_ctx* ctx, const bvhgpu_node* nodes, uint32_t nodes
                        const bvhgpu_triangle* tris, uint32_t ntris, uint32_t* blas_id);
 int bvhgpu_blas_free(bvhgpu_ctx* ctx, uint32_t blas_id);
 int bvhgpu_blas_info(bvhgpu_ctx* ctx, uint32_t blas_id, uint32_t* nodes_used, uint32_t* ntris, uint32_t* depth);
-/* Number of 64-triangle clusters the library keeps for the BLAS's large leaves (leaves of at
- * least 128 triangles, split in the spatial order of their triangles).  A leaf's clusters are
- * skipped for a ray only when provably none of its triangles is accepted below the ray's closest
- * t, so results equal the reference's in-order leaf loop (bvh.rs:250-258).  No reference
- * counterpart: exposed for tests and tuning. */
-int bvhgpu_blas_clusters(bvhgpu_ctx* ctx, uint32_t blas_id, uint32_t* nclusters);
+/* Size of the hidden trees the library keeps under the BLAS's large leaves (leaves of at least 16
+ * triangles): nodes, triangle pairs and the deepest tree's depth below its leaf.  A hidden box is
+ * skipped for a ray only when provably no triangle in it is accepted at or below the ray's closest
+ * t, and ties keep the lowest triangle index, so results equal the reference's in-order leaf loop
+ * (bvh.rs:250-258).  No reference counterpart: exposed for tests and tuning.  Any pointer may be
+ * NULL. */
+int bvhgpu_blas_hidden(bvhgpu_ctx* ctx, uint32_t blas_id, uint32_t* nodes, uint32_t* pairs, uint32_t* depth);
 /* New vertex positions (same triangle order), e.g. an animated mesh before refit. */
 int bvhgpu_blas_update_vertices(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhgpu_triangle* tris);
 int bvhgpu_blas_update_vertices_async(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhgpu_triangle* d_tris,

@@ -1,10 +1,12 @@
-"""Clustered big leaves: the exact in-leaf culling gives the reference's results bit for bit.
+"""Hidden trees under large leaves: the exact in-leaf culling gives the reference's results bit for
+bit.
 
-Leaves of at least 128 triangles are split into 64-triangle clusters in spatial order, and a
-cluster is skipped for a ray only when provably no triangle of it is accepted below the ray's
-closest t.  These cases aim at what could break that: rays at edges and vertices, exact ties
-between duplicate triangles that land in different clusters (lowest triangle index must win),
-clusters refreshed after vertex updates and refits, non-finite vertices, axis-aligned and
+Leaves of at least 16 triangles get a hidden tree of boxes over their triangles (spatial order,
+leaves of at most 4 triangles), and a box is skipped for a ray only when provably no triangle in it
+is accepted at or below the ray's closest t.  These cases aim at what could break that: rays at
+edges and vertices, exact ties between duplicate triangles in different hidden leaves (lowest
+triangle index must win, but never against an equal t from an earlier leaf), boxes refreshed after
+vertex updates and refits, non-finite vertices, axis-aligned and
 denormal directions, short rays, instanced (transformed) BLASes and the plain and persistent bounce
 kernels.  Everything is compared with the oracle's in-order leaf loop."""
 import numpy as np
@@ -60,22 +62,23 @@ def test_flat_leaf_edges_vertices_and_random(ctx):
     tris = scenes.displaced_icosphere(4, 7).triangles().copy()  # 5,120 triangles in one leaf
     bvh = one_leaf_bvh(tris)
     blas = ctx.upload_blas(bvh, tris)
-    assert blas.clusters() == (len(tris) + 63) // 64
+    h = blas.hidden()
+    assert h["pairs"] >= len(tris) // 2 and h["depth"] >= 10
     rays = np.concatenate([edge_rays(tris, 20000, 1), scenes.sphere_rays(20000, 2, box=4.0)])
     ref = orc.bvh_intersect(bvh.nodes, bvh.nodes_used, tris, rays, threads=8)
     same(blas.intersect(rays), ref, "flat leaf")
 
 
-def test_reference_bvh_leaves_are_clustered(ctx):
+def test_reference_bvh_leaves_get_hidden_trees(ctx):
     tris = scenes.displaced_icosphere(6, 0).triangles().copy()
     bvh = bt.BvhBuilder().build_for(tris)
     blas = ctx.upload_blas(bvh, tris)
-    assert blas.clusters() > len(tris) // 64  # the reference's leaves of 1.7k-3.4k triangles
+    assert blas.hidden()["pairs"] >= len(tris) // 2  # the reference's leaves of 1.7k-3.4k triangles
     rays = edge_rays(tris, 30000, 3, eye_dist=4.0)
     same(blas.intersect(rays), orc.bvh_intersect(bvh.nodes, bvh.nodes_used, tris, rays, threads=8), "ref bvh")
 
 
-def test_duplicate_triangles_in_different_clusters_tie_to_lowest_index(ctx):
+def test_duplicate_triangles_in_different_hidden_leaves_tie_to_lowest_index(ctx):
     rng = np.random.default_rng(5)
     base = np.array([[-1, -1, 0, 1, -1, 0, 0, 1, 0]], np.float32)
     other = rng.uniform(-3, 3, (600, 9)).astype(np.float32)
@@ -85,7 +88,7 @@ def test_duplicate_triangles_in_different_clusters_tie_to_lowest_index(ctx):
     tris = np.ascontiguousarray(tris[perm])
     bvh = one_leaf_bvh(tris)
     blas = ctx.upload_blas(bvh, tris)
-    assert blas.clusters() >= 3
+    assert blas.hidden()["nodes"] > 100
     o = np.tile(np.array([0.05, -0.1, -5], np.float32), (64, 1))
     d = np.tile(np.array([0, 0, 1], np.float32), (64, 1))
     d[:, :2] = rng.uniform(-0.05, 0.05, (64, 2))
@@ -96,7 +99,37 @@ def test_duplicate_triangles_in_different_clusters_tie_to_lowest_index(ctx):
     same(blas.intersect(rays), ref, "duplicates")
 
 
-def test_clusters_follow_vertex_updates_and_refit(ctx):
+@pytest.mark.parametrize("left_nearer", [False, True])
+def test_equal_t_in_a_later_leaf_is_not_taken(ctx, left_nearer):
+    """The same triangle in two reference leaves (indices 20 and 45): the leaf visited first keeps
+    the hit, whatever the indices -- the reference's strict `<` across leaves."""
+    rng = np.random.default_rng(21)
+    tris = rng.uniform(-3, 3, (64, 9)).astype(np.float32)
+    tris[:, 2::3] = rng.uniform(2, 6, (64, 3)).astype(np.float32)  # behind z = 0
+    d = np.array([-1, -1, 0, 1, -1, 0, 0, 1, 0], np.float32)
+    tris[20] = d
+    tris[45] = d
+    v = tris.reshape(-1, 3)
+    nodes = np.zeros(4, bt.NODE)
+    nodes[0]["bounds_min"], nodes[0]["bounds_max"] = v.min(0), v.max(0)
+    nodes[0]["left_first"] = 2
+    for i, first in ((2, 0), (3, 32)):
+        nodes[i]["bounds_min"], nodes[i]["bounds_max"] = v.min(0), v.max(0)
+        nodes[i]["left_first"] = first
+        nodes[i]["primitive_count"] = 32
+    if left_nearer:
+        nodes[2]["bounds_min"][2] -= np.float32(0.5)
+    bvh = bt.Bvh(nodes, 4)
+    blas = ctx.upload_blas(bvh, tris)
+    assert blas.hidden()["pairs"] >= 32
+    rays = orc.make_rays(np.tile(np.array([0.05, -0.2, -5], np.float32), (8, 1)),
+                         np.tile(np.array([0, 0, 1], np.float32), (8, 1)))
+    ref = orc.bvh_intersect(bvh.nodes, bvh.nodes_used, tris, rays)
+    assert np.all(ref["prim"] == (20 if left_nearer else 45))
+    same(blas.intersect(rays), ref, "equal t across leaves")
+
+
+def test_hidden_boxes_follow_vertex_updates_and_refit(ctx):
     tris, bvh = scenes.displaced_icosphere(5, 2).triangles().copy(), None
     bvh = bt.BvhBuilder().build_for(tris)
     blas = ctx.upload_blas(bvh, tris)
@@ -145,7 +178,7 @@ def test_short_rays_stop_at_their_t(ctx):
         same(blas.intersect(r), orc.bvh_intersect(bvh.nodes, bvh.nodes_used, tris, r, threads=8), "short rays")
 
 
-def test_bounce_kernels_with_clusters(ctx):
+def test_bounce_kernels_with_hidden_trees(ctx):
     tris = scenes.displaced_icosphere(6, 1).triangles().copy()
     bvh = bt.BvhBuilder().build_for(tris)
     blas = ctx.upload_blas(bvh, tris)
@@ -162,11 +195,11 @@ def test_bounce_kernels_with_clusters(ctx):
         same(h1, ref1, f"bounces, mode {mode}")
 
 
-def test_instanced_scene_with_clusters(ctx):
+def test_instanced_scene_with_hidden_trees(ctx):
     tris = scenes.displaced_icosphere(5, 6).triangles().copy()
     bvh = bt.BvhBuilder().build_for(tris)
     blas = ctx.upload_blas(bvh, tris)
-    assert blas.clusters() > 0
+    assert blas.hidden()["pairs"] > 0
     n = 24
     rng = np.random.default_rng(11)
     xf = np.zeros((n, 16), np.float32)
