@@ -488,7 +488,7 @@ struct TravT {
         if (first >= b.nodes_used) {  // hidden children: the margins' exact cull, any order
             hl = hidden_box(l0, l1, r.rd, lc, dl);
             hr = hidden_box(r0, r1, r.rd, lc, dr);
-            left_near = dl <= dr;
+            left_near = hl && (!hr || dl <= dr);
         } else {
             hl = slab(l0, l1, r.o, r.rd, r.ct, dl);
             hr = slab(r0, r1, r.o, r.rd, r.ct, dr);
