@@ -449,9 +449,9 @@ struct TravT {
         return true;
     }
 
-    // Processes one node.  A reference leaf with a hidden tree continues at the tree's root (the
-    // ray's margins computed here); one without, with more than `big_leaf` triangles, is not
-    // tested here: the step returns kStepBigLeaf with (first, cnt) describing the leaf, and the
+    // Processes one node.  A reference leaf with a hidden tree continues at the tree's root when
+    // the ray's margins (computed here) are narrow enough to cull; other leaves with more than
+    // `big_leaf` triangles are not tested here: the step returns kStepBigLeaf with (first, cnt) describing the leaf, and the
     // caller tests it (warp-cooperatively) and then calls pop().
     __device__ __forceinline__ StepResult step(const GBlas& b, LaneRay& r, uint32_t big_leaf, uint32_t* err) {
         if (++steps > max_steps) {
@@ -468,10 +468,12 @@ struct TravT {
                 if ((e.x | e.y) != 0u) {
                     lc = leaf_cull(cull_ray_rd(r.o.x, r.o.y, r.o.z, r.d.x, r.d.y, r.d.z, r.rd.x, r.rd.y, r.rd.z),
                                    __uint_as_float(e.z), __uint_as_float(e.w), r.ct);
-                    held = false;
-                    first = e.x;
-                    cnt = e.y;
-                    return kStepContinue;
+                    if (lc.on) {  // else: margins too wide for this ray, the leaf is tested in order
+                        held = false;
+                        first = e.x;
+                        cnt = e.y;
+                        return kStepContinue;
+                    }
                 }
             }
             if (cnt > big_leaf) return kStepBigLeaf;

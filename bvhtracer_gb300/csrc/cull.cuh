@@ -150,7 +150,8 @@ BVHGPU_HD float leaf_thi(const LeafCull& lc, float t_best) {
     return (t_best + (lc.dt0 + t_best * lc.dt1)) * (1.0f + 8.0f * kCullUnit) + 1e-30f;
 }
 
-BVHGPU_HD LeafCull leaf_cull(const CullRay& r, float Q, float B, float t_best) {
+// max_duv: the largest barycentric margin (Du + Dv) worth culling with; on = false above it.
+BVHGPU_HD LeafCull leaf_cull(const CullRay& r, float Q, float B, float t_best, float max_duv = 0.5f) {
     const float u0 = kCullUnit, K = kCullInvDet;
     LeafCull lc;
     lc.on = false;
@@ -172,6 +173,8 @@ BVHGPU_HD LeafCull leaf_cull(const CullRay& r, float Q, float B, float t_best) {
     const float inv = 1.0f + 2.0f * (rho + 8.0f * u0);  // >= 1 / (1 - rho - 8 u0)
     const float e_uv = r.b_uv * S * Q;                   // >= E_u + E_v
     const float duv = ((e_uv + 2.0f * e_det) * K + 8.0f * u0) * inv;
+    // margins of half a triangle or more cull little: the caller tests the leaf in order instead
+    if (!(duv < max_duv)) return lc;
     const float R = 4.0f * (duv + 2.0f * u0) * Q * 1.0001f + 1e-30f;
     if (!(R < kCullHuge)) return lc;
     const float e_t = kCullSafety * 36.0f * u0 * S * P;
