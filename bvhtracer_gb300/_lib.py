@@ -23,7 +23,7 @@ BATCH_ITEM = np.dtype([("blas", "<u4"), ("ray_offset", "<u4"), ("ray_count", "<u
 assert NODE.itemsize == 32 and RAY.itemsize == 32 and HIT.itemsize == 20
 assert TLAS_NODE.itemsize == 32 and BATCH_ITEM.itemsize == 16
 TUNE_CONFIG = np.dtype([("block", "<u4"), ("min_blocks", "<u4"), ("stack", "<u4"), ("big_leaf", "<u4"),
-                        ("refill", "<u4"), ("reserved", "<u4")])
+                        ("refill", "<u4"), ("hidden", "<u4")])
 BIG_LEAF_NEVER = 0xFFFFFFFF
 RIGID_BODY = np.dtype([("inverse_mass", "<f4"), ("inverse_inertia", "<f4", 9), ("linear_drag", "<f4"),
                        ("angular_drag", "<f4"), ("position", "<f4", 3), ("orientation", "<f4", 4),

@@ -160,7 +160,7 @@ class Context:
     def tune_get(self, kernel: int) -> dict:
         c = np.zeros(1, _lib.TUNE_CONFIG)
         self.check(self.lib.bvhgpu_tune_get(self.h, kernel, ptr(c)))
-        return {k: int(c[0][k]) for k in _lib.TUNE_CONFIG.names if k != "reserved"}
+        return {k: int(c[0][k]) for k in _lib.TUNE_CONFIG.names}
 
     def tune_set(self, kernel: int, **cfg):
         c = np.zeros(1, _lib.TUNE_CONFIG)
@@ -179,7 +179,7 @@ class Context:
             raise _lib.BvhGpuError(rc, "tune_space")
         out = np.zeros(n.value, _lib.TUNE_CONFIG)
         lib.bvhgpu_tune_space(kernel, ptr(out), n.value, ctypes.byref(n))
-        return [{k: int(r[k]) for k in _lib.TUNE_CONFIG.names if k != "reserved"} for r in out]
+        return [{k: int(r[k]) for k in _lib.TUNE_CONFIG.names} for r in out]
 
     def autotune(self, kernel: int, d_rays: "DeviceBuffer", n: int, d_hits0: "DeviceBuffer", d_hits1=None,
                  target: int = 0, seed: int = 0, items=None, reps: int = 3):
@@ -201,7 +201,7 @@ class Context:
         best = np.zeros(1, _lib.TUNE_CONFIG)
         ms = ctypes.c_float()
         self.check(self.lib.bvhgpu_autotune(self.h, ctypes.byref(job), reps, ptr(best), ctypes.byref(ms)))
-        return {k: int(best[0][k]) for k in _lib.TUNE_CONFIG.names if k != "reserved"}, float(ms.value)
+        return {k: int(best[0][k]) for k in _lib.TUNE_CONFIG.names}, float(ms.value)
 
 
 class World:

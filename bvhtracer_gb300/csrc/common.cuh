@@ -178,6 +178,15 @@ __device__ __forceinline__ unsigned long long key_max(float f, uint32_t pos) {
 // triangle.rs:44-45, so precomputing it changes no bit.
 enum StepResult { kStepContinue = 0, kStepFinished = 1, kStepBigLeaf = 2 };
 
+// Leaf policy of a traversal launch (results never depend on it): a ray walks a leaf's hidden tree
+// when its barycentric margin there is below max_duv; other leaves with more than big_leaf
+// triangles are tested by the whole warp, smaller ones by their own lane.
+struct LeafPolicy {
+    uint32_t big_leaf;
+    float max_duv;
+};
+constexpr LeafPolicy kDefaultPolicy = {16u, 0.5f};
+
 // One lane's ray (world or model space) and its running closest hit.
 struct LaneRay {
     float3 o, d, rd;
@@ -451,9 +460,9 @@ struct TravT {
 
     // Processes one node.  A reference leaf with a hidden tree continues at the tree's root when
     // the ray's margins (computed here) are narrow enough to cull; other leaves with more than
-    // `big_leaf` triangles are not tested here: the step returns kStepBigLeaf with (first, cnt) describing the leaf, and the
+    // `pol.big_leaf` triangles are not tested here: the step returns kStepBigLeaf with (first, cnt) describing the leaf, and the
     // caller tests it (warp-cooperatively) and then calls pop().
-    __device__ __forceinline__ StepResult step(const GBlas& b, LaneRay& r, uint32_t big_leaf, uint32_t* err) {
+    __device__ __forceinline__ StepResult step(const GBlas& b, LaneRay& r, LeafPolicy pol, uint32_t* err) {
         if (++steps > max_steps) {
             atomicOr(err, kErrSteps);
             return kStepFinished;
@@ -467,7 +476,7 @@ struct TravT {
                 const uint4 e = __ldg(b.hx + first);
                 if ((e.x | e.y) != 0u) {
                     lc = leaf_cull(cull_ray_rd(r.o.x, r.o.y, r.o.z, r.d.x, r.d.y, r.d.z, r.rd.x, r.rd.y, r.rd.z),
-                                   __uint_as_float(e.z), __uint_as_float(e.w), r.ct);
+                                   __uint_as_float(e.z), __uint_as_float(e.w), r.ct, pol.max_duv);
                     if (lc.on) {  // else: margins too wide for this ray, the leaf is tested in order
                         held = false;
                         first = e.x;
@@ -476,7 +485,7 @@ struct TravT {
                     }
                 }
             }
-            if (cnt > big_leaf) return kStepBigLeaf;
+            if (cnt > pol.big_leaf) return kStepBigLeaf;
             test_leaf_lane(b.tris, first, cnt, r);
             return pop() ? kStepFinished : kStepContinue;
         }
@@ -512,9 +521,9 @@ struct TravT {
     }
 
     // Steps until the lane finishes or stops at a big leaf.
-    __device__ __forceinline__ StepResult advance(const GBlas& b, LaneRay& r, uint32_t big_leaf, uint32_t* err) {
+    __device__ __forceinline__ StepResult advance(const GBlas& b, LaneRay& r, LeafPolicy pol, uint32_t* err) {
         for (;;) {
-            StepResult s = step(b, r, big_leaf, err);
+            StepResult s = step(b, r, pol, err);
             if (s != kStepContinue) return s;
         }
     }
@@ -539,7 +548,7 @@ __device__ __forceinline__ bool trace_blas(const GBlas& b, float3 o, float3 d, f
     r.hv = hv;
     r.hp = hprim;
     r.hit = false;
-    tr.advance(b, r, 0xFFFFFFFFu, err);
+    tr.advance(b, r, LeafPolicy{0xFFFFFFFFu, kDefaultPolicy.max_duv}, err);
     closest_t = r.ct;
     hu = r.hu;
     hv = r.hv;

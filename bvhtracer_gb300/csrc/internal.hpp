@@ -131,9 +131,9 @@ struct bvhgpu_ctx {
     bvhgpu_ctx() {
         // defaults: the configs the autotuner picked on GB300 for the displaced-icosphere frame
         // (single BLAS) and the instanced frame (two-level)
-        for (auto& t : tune) t = bvhgpu_tune_config{128u, 6u, 0u, 16u, 1u, 0u};
-        tune[BVHGPU_K_TRACE_SCENE] = bvhgpu_tune_config{128u, 6u, 256u, 16u, 1u, 0u};
-        tune[BVHGPU_K_SCENE_BOUNCE] = bvhgpu_tune_config{128u, 6u, 256u, 16u, 8u, 0u};
+        for (auto& t : tune) t = bvhgpu_tune_config{128u, 5u, 256u, 16u, 8u, 500u};
+        tune[BVHGPU_K_TRACE_BLAS].refill = 1u;
+        tune[BVHGPU_K_TRACE_SCENE].refill = 1u;
     }
 };
 

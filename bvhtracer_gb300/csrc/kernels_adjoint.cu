@@ -25,7 +25,6 @@ namespace {
 
 constexpr int kBlock = 128;
 constexpr unsigned kFull = 0xFFFFFFFFu;
-constexpr uint32_t kBigLeaf = 16;
 
 inline unsigned grid_for(uint32_t n, int block) { return (unsigned)((n + block - 1) / block); }
 
@@ -49,7 +48,7 @@ __device__ __forceinline__ void warp_trace_local(const GBlas& b, bool active, La
     StepResult st = active ? kStepContinue : kStepFinished;
     const unsigned lane = threadIdx.x & 31u;
     for (;;) {
-        if (st == kStepContinue) st = tr.advance(b, r, kBigLeaf, err);
+        if (st == kStepContinue) st = tr.advance(b, r, kDefaultPolicy, err);
         unsigned pend = __ballot_sync(kFull, st == kStepBigLeaf);
         if (pend == 0u) break;
         while (pend) {

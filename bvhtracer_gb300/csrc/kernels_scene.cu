@@ -538,10 +538,10 @@ struct SceneTrav {
         return tpop() ? kStepFinished : kStepContinue;
     }
 
-    __device__ __forceinline__ StepResult advance(const SceneData& sd, LaneRay& r, uint32_t big_leaf, uint32_t* err) {
+    __device__ __forceinline__ StepResult advance(const SceneData& sd, LaneRay& r, LeafPolicy pol, uint32_t* err) {
         for (;;) {
             if (in_blas) {
-                const StepResult st = bt.step(blas, r, big_leaf, err);
+                const StepResult st = bt.step(blas, r, pol, err);
                 if (st == kStepContinue) continue;
                 if (st == kStepBigLeaf) return st;
                 in_blas = false;
@@ -636,7 +636,7 @@ constexpr int kTlasStack = 64;
 
 template <int BLOCK, int MINB, class STK>
 __global__ void __launch_bounds__(BLOCK, MINB) k_trace_scene(SceneData sd, const float4* __restrict__ rays,
-                                                             uint32_t n, GHit* __restrict__ hits, uint32_t big_leaf,
+                                                             uint32_t n, GHit* __restrict__ hits, LeafPolicy pol,
                                                              uint32_t* err) {
     extern __shared__ uint2 stack_smem[];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -662,7 +662,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_trace_scene(SceneData sd, const
         st = kStepContinue;
     }
     for (;;) {
-        if (st == kStepContinue) st = tr.advance(sd, r, big_leaf, err);
+        if (st == kStepContinue) st = tr.advance(sd, r, pol, err);
         const unsigned pend = __ballot_sync(kFull, st == kStepBigLeaf);
         if (pend == 0u) break;
         scene_coop_phase(pend, tr, r, st);
@@ -677,7 +677,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_scene_persistent_bounce(SceneDa
                                                                          uint32_t n, uint32_t seed,
                                                                          GHit* __restrict__ hits0,
                                                                          GHit* __restrict__ hits1, uint32_t* queue,
-                                                                         uint32_t big_leaf, uint32_t refill,
+                                                                         LeafPolicy pol, uint32_t refill,
                                                                          uint32_t* err) {
     extern __shared__ uint2 stack_smem[];
     const unsigned lane = threadIdx.x & 31u;
@@ -721,7 +721,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_scene_persistent_bounce(SceneDa
             }
         }
         while (phase == 1 || phase == 2) {
-            if (st == kStepContinue) st = tr.advance(sd, r, big_leaf, err);
+            if (st == kStepContinue) st = tr.advance(sd, r, pol, err);
             if (st != kStepFinished) break;
             const bool h = r.hit && r.ct < FLT_MAX;
             if (phase == 2) {
@@ -919,7 +919,7 @@ cudaError_t launch_trace_scene(bvhgpu_ctx* ctx, DeviceScene& sc, const float4* r
         using STK = typename decltype(tg)::type;
         k_trace_scene<SH::block, SH::minb, STK><<<grid_for(n, SH::block), SH::block,
                                                   stack_smem_bytes<STK>(SH::block), s>>>(
-            sd, rays, n, static_cast<GHit*>(hits), v.big_leaf, ctx->d_err);
+            sd, rays, n, static_cast<GHit*>(hits), v.pol, ctx->d_err);
         return cudaGetLastError();
     });
     g_launches++;
@@ -944,7 +944,7 @@ cudaError_t launch_scene_bounce(bvhgpu_ctx* ctx, DeviceScene& sc, const float4* 
         int per_sm = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, SH::block, smem);
         k<<<std::max(1, per_sm) * ctx->num_sms, SH::block, smem, s>>>(sd, rays, n, seed, static_cast<GHit*>(hits0),
-                                                                     static_cast<GHit*>(hits1), queue, v.big_leaf,
+                                                                     static_cast<GHit*>(hits1), queue, v.pol,
                                                                      v.refill, ctx->d_err);
         return cudaGetLastError();
     });

@@ -24,7 +24,6 @@ constexpr int kBlock = 128;
 constexpr unsigned kFull = 0xFFFFFFFFu;
 // Leaves with more triangles than this are tested by the whole warp (coop_leaf); smaller
 // ones by the lane that reached them.
-constexpr uint32_t kBigLeaf = 16;
 
 inline GBlas to_gblas(const DeviceBlas& b) {
     GBlas g;
@@ -51,7 +50,7 @@ inline unsigned grid_for(uint32_t n, int block) { return (unsigned)((n + block -
 
 // ---- warp-synchronous traversal ----------------------------------------------------------
 // Every lane walks its own ray through the interior nodes (and tests small leaves itself);
-// a leaf with more than `big_leaf` triangles is tested by the whole warp together
+// a leaf with more than `pol.big_leaf` triangles (and no hidden tree walk) is tested by the whole warp together
 // (coop_leaf), one waiting ray at a time.  All 32 lanes stay in the loop until every ray of
 // the warp has finished, so the cooperative step always has the full warp.
 
@@ -89,14 +88,14 @@ __device__ __forceinline__ void coop_leaf_phase(unsigned pend, const GBlas& blas
 
 // Traces the rays of one warp (inactive lanes take part in the cooperative steps only).
 template <class STK>
-__device__ __forceinline__ void warp_trace(const GBlas& b, bool active, LaneRay& r, uint32_t big_leaf, uint32_t* err,
+__device__ __forceinline__ void warp_trace(const GBlas& b, bool active, LaneRay& r, LeafPolicy pol, uint32_t* err,
                                            uint2* stack_smem) {
     TravT<STK> tr;
     tr.stk.bind(stack_smem);
     if (active) tr.init(b);
     StepResult st = active ? kStepContinue : kStepFinished;
     for (;;) {
-        if (st == kStepContinue) st = tr.advance(b, r, big_leaf, err);
+        if (st == kStepContinue) st = tr.advance(b, r, pol, err);
         unsigned pend = __ballot_sync(kFull, st == kStepBigLeaf);
         if (pend == 0u) break;
         coop_leaf_phase(pend, b, tr, r, st);
@@ -121,7 +120,7 @@ template <int BLOCK, int MINB, class STK>
 __global__ void __launch_bounds__(BLOCK, MINB) k_trace_blas(GBlas b, const float4* __restrict__ rays, uint32_t n,
                                                             const uint32_t* count,
                                                             const uint32_t* __restrict__ out_index,
-                                                            GHit* __restrict__ hits, uint32_t big_leaf,
+                                                            GHit* __restrict__ hits, LeafPolicy pol,
                                                             uint32_t* err) {
     extern __shared__ uint2 stack_smem[];
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -135,7 +134,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_trace_blas(GBlas b, const float
         load_ray(rays, i, o, d, t);
         init_lane_ray(r, o, d, t);
     }
-    warp_trace<STK>(b, active, r, big_leaf, err, stack_smem);
+    warp_trace<STK>(b, active, r, pol, err, stack_smem);
     // bvh.rs:295: a hit needs closest_ray.t < f32::MAX as well.
     if (active) store_hit(hits, out_index ? out_index[i] : i, r.hit && r.ct < FLT_MAX, r.ct, r.hu, r.hv, r.hp, 0u);
 }
@@ -204,7 +203,7 @@ template <int BLOCK, int MINB, class STK>
 __global__ void __launch_bounds__(BLOCK, MINB) k_persistent_bounce(GBlas b, const float4* __restrict__ rays,
                                                                    uint32_t n, uint32_t seed,
                                                                    GHit* __restrict__ hits0, GHit* __restrict__ hits1,
-                                                                   uint32_t* queue, uint32_t big_leaf, uint32_t refill,
+                                                                   uint32_t* queue, LeafPolicy pol, uint32_t refill,
                                                                    uint32_t* err) {
     extern __shared__ uint2 stack_smem[];
     const unsigned lane = threadIdx.x & 31u;
@@ -243,7 +242,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_persistent_bounce(GBlas b, cons
         }
         // advance this lane; finished rays are completed (a primary hit starts its bounce)
         while (phase == 1 || phase == 2) {
-            if (st == kStepContinue) st = tr.advance(b, r, big_leaf, err);
+            if (st == kStepContinue) st = tr.advance(b, r, pol, err);
             if (st != kStepFinished) break;
             bool h = r.hit && r.ct < FLT_MAX;
             if (phase == 2) {
@@ -291,7 +290,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_trace_batch_persistent(const Ba
                                                                         uint32_t nitems, uint32_t total,
                                                                         const float4* __restrict__ rays,
                                                                         GHit* __restrict__ hits, uint32_t* queue,
-                                                                        uint32_t big_leaf, uint32_t refill,
+                                                                        LeafPolicy pol, uint32_t refill,
                                                                         uint32_t* err) {
     extern __shared__ uint2 stack_smem[];
     const unsigned lane = threadIdx.x & 31u;
@@ -340,7 +339,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_trace_batch_persistent(const Ba
             }
         }
         if (phase == 1) {
-            if (st == kStepContinue) st = tr.advance(b, r, big_leaf, err);
+            if (st == kStepContinue) st = tr.advance(b, r, pol, err);
             if (st == kStepFinished) {
                 store_hit(hits, ray, r.hit && r.ct < FLT_MAX, r.ct, r.hu, r.hv, r.hp, 0u);
                 phase = 0;
@@ -460,7 +459,7 @@ __device__ __forceinline__ int32_t f32_as_i32(float x) {  // Rust `as i32`: satu
 // goes through the pixel's top-left corner u = x / w, v = y / h (renderer.rs:358-361).
 template <int STACK>
 __global__ void __launch_bounds__(64) k_render(GBlas b, RenderParams P, const float* __restrict__ normals,
-                                               uint8_t* __restrict__ rgba, uint32_t big_leaf, uint32_t* err) {
+                                               uint8_t* __restrict__ rgba, LeafPolicy pol, uint32_t* err) {
     const int tiles_x = (P.width + 7) / 8;
     const int tile = blockIdx.x;
     const int x = (tile % tiles_x) * 8 + (threadIdx.x & 7);
@@ -483,7 +482,7 @@ __global__ void __launch_bounds__(64) k_render(GBlas b, RenderParams P, const fl
     float3 d = xf_vector(C + 9, dir);
     LaneRay lr;
     init_lane_ray(lr, o, d, FLT_MAX);
-    warp_trace<LocalStack<STACK>>(b, active, lr, big_leaf, err, nullptr);
+    warp_trace<LocalStack<STACK>>(b, active, lr, pol, err, nullptr);
     if (!active) return;
     const float t = lr.ct, hu = lr.hu, hv = lr.hv;
     const uint32_t hp = lr.hp;
@@ -586,7 +585,7 @@ static cudaError_t trace_blas_variant(bvhgpu_ctx* ctx, const Variant& v, const G
         using STK = typename decltype(tg)::type;
         k_trace_blas<SH::block, SH::minb, STK><<<grid_for(n, SH::block), SH::block,
                                                  stack_smem_bytes<STK>(SH::block), s>>>(g, rays, n, count, out_index,
-                                                                                       hits, v.big_leaf, ctx->d_err);
+                                                                                       hits, v.pol, ctx->d_err);
         return cudaGetLastError();
     });
 }
@@ -645,7 +644,7 @@ cudaError_t launch_bounce_persistent(bvhgpu_ctx* ctx, const DeviceBlas& b, const
         auto* k = k_persistent_bounce<SH::block, SH::minb, STK>;
         const size_t smem = stack_smem_bytes<STK>(SH::block);
         k<<<persistent_grid(ctx, k, SH::block, smem), SH::block, smem, s>>>(
-            g, rays, n, seed, static_cast<GHit*>(hits0), static_cast<GHit*>(hits1), queue, v.big_leaf, v.refill,
+            g, rays, n, seed, static_cast<GHit*>(hits0), static_cast<GHit*>(hits1), queue, v.pol, v.refill,
             ctx->d_err);
         return cudaGetLastError();
     });
@@ -726,7 +725,7 @@ cudaError_t launch_trace_batch(bvhgpu_ctx* ctx, const std::vector<const DeviceBl
         const size_t smem = stack_smem_bytes<STK>(SH::block);
         k<<<persistent_grid(ctx, k, SH::block, smem), SH::block, smem, s>>>(
             static_cast<const BatchEntry*>(ctx->batch_table), nitems, total, rays, static_cast<GHit*>(hits), queue,
-            v.big_leaf, v.refill, ctx->d_err);
+            v.pol, v.refill, ctx->d_err);
         return cudaGetLastError();
     });
     g_launches++;
@@ -773,7 +772,7 @@ cudaError_t launch_render(bvhgpu_ctx* ctx, const DeviceBlas& b, const bvhgpu_cam
     GBlas g = to_gblas(b);
     unsigned tiles = (unsigned)(((w + 7) / 8) * ((h + 7) / 8));
     LaunchScope scope(ctx, BVHGPU_K_RENDER, s);
-    BVHGPU_DISPATCH_STACK(b.depth, (k_render<S><<<tiles, 64, 0, s>>>(g, P, d_normals, d_rgba, kBigLeaf, ctx->d_err)));
+    BVHGPU_DISPATCH_STACK(b.depth, (k_render<S><<<tiles, 64, 0, s>>>(g, P, d_normals, d_rgba, kDefaultPolicy, ctx->d_err)));
     g_launches++;
     return cudaGetLastError();
 }

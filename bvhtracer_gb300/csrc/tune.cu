@@ -2,7 +2,7 @@
 //
 // The tuner times a caller-supplied job (one of the library's own async calls) under candidate
 // configs: a coordinate search from the current config, one dimension at a time (launch shape,
-// stack, big-leaf threshold, refill), two sweeps, each candidate timed by events on the context
+// stack, big-leaf threshold, refill, hidden-tree margin), two sweeps, each candidate timed by events on the context
 // stream after an untimed run.  Configs never change results, only speed, so the job may be the
 // caller's real workload.
 #include <cuda_runtime.h>
@@ -22,6 +22,7 @@ namespace {
 
 constexpr uint32_t kBigLeafValues[] = {8u, 16u, 32u, 64u, BVHGPU_BIG_LEAF_NEVER};
 constexpr uint32_t kRefillValues[] = {1u, 8u, 16u};
+constexpr uint32_t kHiddenValues[] = {0u, 100u, 250u, 500u, 1000u};
 
 bool tunable(int k) {
     return k == BVHGPU_K_TRACE_BLAS || k == BVHGPU_K_TRACE_SCENE || k == BVHGPU_K_PERSISTENT_BOUNCE ||
@@ -35,7 +36,7 @@ bool persistent(int k) {
 bool valid_config(const bvhgpu_tune_config& c) {
     if (shape_index(c.block, c.min_blocks) < 0) return false;
     if (c.stack != 0 && c.stack != 8 && c.stack != 32 && c.stack != 256) return false;
-    return c.refill >= 1u && c.refill <= 32u;
+    return c.refill >= 1u && c.refill <= 32u && c.hidden <= 1000000u;
 }
 
 int run_job(bvhgpu_ctx* ctx, const bvhgpu_tune_job& j) {
@@ -126,7 +127,6 @@ int bvhgpu_tune_set(bvhgpu_ctx* ctx, int kernel, const bvhgpu_tune_config* cfg) 
     if (!tunable(kernel)) return record_error(ctx, BVHGPU_ERR_INVALID_ARG, "tune_set: kernel has no variants");
     if (!valid_config(*cfg)) return record_error(ctx, BVHGPU_ERR_INVALID_ARG, "tune_set: variant not compiled");
     ctx->tune[kernel] = *cfg;
-    ctx->tune[kernel].reserved = 0;
     return BVHGPU_OK;
 }
 
@@ -137,12 +137,13 @@ int bvhgpu_tune_space(int kernel, bvhgpu_tune_config* out, uint32_t cap, uint32_
     for (int sh = 0; sh < kNumShapes; ++sh)
         for (int st = 0; st < kNumStacks; ++st)
             for (uint32_t bl : kBigLeafValues)
-                for (uint32_t rf = 0; rf < nrefill; ++rf) {
-                    if (k < cap)
-                        out[k] = bvhgpu_tune_config{(uint32_t)kShapeBlock[sh], (uint32_t)kShapeMinBlocks[sh],
-                                                    (uint32_t)kStackSizes[st], bl, kRefillValues[rf], 0u};
-                    ++k;
-                }
+                for (uint32_t rf = 0; rf < nrefill; ++rf)
+                    for (uint32_t hd : kHiddenValues) {
+                        if (k < cap)
+                            out[k] = bvhgpu_tune_config{(uint32_t)kShapeBlock[sh], (uint32_t)kShapeMinBlocks[sh],
+                                                        (uint32_t)kStackSizes[st], bl, kRefillValues[rf], hd};
+                        ++k;
+                    }
     if (count) *count = k;
     return BVHGPU_OK;
 }
@@ -157,10 +158,10 @@ int bvhgpu_autotune(bvhgpu_ctx* ctx, const bvhgpu_tune_job* job, uint32_t reps, 
     const uint32_t depth = job_depth(ctx, j);
     Timer tm;
     // measured configs, keyed by the variant they resolve to plus the run-time knobs
-    std::map<std::tuple<int, int, uint32_t, uint32_t>, float> seen;
+    std::map<std::tuple<int, int, uint32_t, uint32_t, uint32_t>, float> seen;
     auto key = [&](const bvhgpu_tune_config& c) {
         const Variant v = resolve(c, depth);
-        return std::make_tuple(v.shape, v.stack, v.big_leaf, persistent(j.kernel) ? v.refill : 1u);
+        return std::make_tuple(v.shape, v.stack, v.pol.big_leaf, persistent(j.kernel) ? v.refill : 1u, c.hidden);
     };
     auto time_of = [&](const bvhgpu_tune_config& c) -> float {
         auto k = key(c);
@@ -172,7 +173,7 @@ int bvhgpu_autotune(bvhgpu_ctx* ctx, const bvhgpu_tune_job* job, uint32_t reps, 
         return ms;
     };
     bvhgpu_tune_config cur = ctx->tune[j.kernel];
-    if (!valid_config(cur)) cur = bvhgpu_tune_config{128u, 1u, 0u, 16u, 1u, 0u};
+    if (!valid_config(cur)) cur = bvhgpu_tune_config{128u, 5u, 256u, 16u, 8u, 500u};
     float cur_ms = time_of(cur);
     auto consider = [&](const bvhgpu_tune_config& c) {
         const float ms = time_of(c);
@@ -199,6 +200,12 @@ int bvhgpu_autotune(bvhgpu_ctx* ctx, const bvhgpu_tune_job* job, uint32_t reps, 
         for (uint32_t bl : kBigLeafValues) {
             bvhgpu_tune_config c = base_leaf;
             c.big_leaf = bl;
+            consider(c);
+        }
+        const bvhgpu_tune_config base_hidden = cur;
+        for (uint32_t hd : kHiddenValues) {
+            bvhgpu_tune_config c = base_hidden;
+            c.hidden = hd;
             consider(c);
         }
         if (persistent(j.kernel)) {

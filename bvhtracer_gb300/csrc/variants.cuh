@@ -5,7 +5,8 @@
 //    __launch_bounds__, which caps registers per thread (65,536 / (block * min_blocks));
 //  - the stack: 8 or 32 entries (4 in registers, the rest in shared memory), or 256 entries in
 //    local memory for deep trees.
-// The two run-time knobs (big-leaf threshold, refill) are kernel arguments.
+// The run-time knobs (leaf policy: big-leaf threshold and hidden-tree margin; refill) are kernel
+// arguments.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -68,7 +69,7 @@ decltype(auto) with_variant(int shape, int stack, F&& f) {
 struct Variant {
     int shape;
     int stack;
-    uint32_t big_leaf;
+    LeafPolicy pol;
     uint32_t refill;
 };
 
@@ -96,7 +97,8 @@ inline Variant resolve(const bvhgpu_tune_config& c, uint32_t depth) {
     v.stack = kStackSizes[kNumStacks - 1];
     for (int k = kNumStacks - 1; k >= 0; --k)
         if (kStackSizes[k] >= want) v.stack = kStackSizes[k];
-    v.big_leaf = c.big_leaf;
+    v.pol.big_leaf = c.big_leaf;
+    v.pol.max_duv = (float)c.hidden * 1e-3f;
     v.refill = c.refill < 1u ? 1u : (c.refill > 32u ? 32u : c.refill);
     return v;
 }

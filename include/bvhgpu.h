@@ -392,16 +392,20 @@ typedef struct bvhgpu_tune_config {
     /* ray batch of the persistent kernels: a warp fetches new rays once this many of its lanes
      * are idle (1..32; a warp whose lanes are all idle always fetches). */
     uint32_t refill;
-    uint32_t reserved; /* 0 */
+    /* hidden trees: a ray walks a large leaf's hidden tree (bvhgpu_blas_hidden) when its cull
+     * margin there, in thousandths of a triangle's barycentric range, is below this; otherwise the
+     * leaf is tested in order (big_leaf decides by whom).  0 = never. */
+    uint32_t hidden;
 } bvhgpu_tune_config;
-/* Defaults (the tuner's picks on GB300): block 128, min_blocks 6, stack 0, big_leaf 16, refill 1;
- * for the two-level kernels (TRACE_SCENE, SCENE_BOUNCE) stack 256 and refill 1 / 8. */
+/* Defaults (the tuner's picks on GB300): block 128, min_blocks 5, stack 256, big_leaf 16, refill 8,
+ * hidden 500; for the single-ray kernels (TRACE_BLAS, TRACE_SCENE) refill 1. */
 int bvhgpu_tune_get(bvhgpu_ctx* ctx, int kernel, bvhgpu_tune_config* out);
 /* BVHGPU_ERR_INVALID_ARG for a kernel that is not tunable or a shape / stack not compiled. */
 int bvhgpu_tune_set(bvhgpu_ctx* ctx, int kernel, const bvhgpu_tune_config* cfg);
 /* The candidate values the tuner searches, as a list of configs (cap entries at most; *count
- * gets the full number): every compiled shape x stack, big_leaf in {8, 16, 32, 64, NEVER} and
- * refill in {1, 8, 16} (refill only for the persistent kernels). */
+ * gets the full number): every compiled shape x stack, big_leaf in {8, 16, 32, 64, NEVER},
+ * refill in {1, 8, 16} (refill only for the persistent kernels) and hidden in
+ * {0, 100, 250, 500, 1000}. */
 int bvhgpu_tune_space(int kernel, bvhgpu_tune_config* out, uint32_t cap, uint32_t* count);
 
 /* One call for the tuner to time: the fields a kernel needs, others 0 / NULL.
@@ -423,7 +427,7 @@ typedef struct bvhgpu_tune_job {
     uint32_t nitems;
 } bvhgpu_tune_job;
 /* Times the job under candidate configs -- a coordinate search from the current config over
- * launch shape, stack, big_leaf and refill, two sweeps; each candidate runs once untimed, then
+ * launch shape, stack, big_leaf, refill and hidden, two sweeps; each candidate runs once untimed, then
  * `reps` times bracketed by events on the context's stream (median kept) -- stores the fastest
  * in the context and returns it with its ms per call (either pointer may be NULL).  The job's
  * outputs are overwritten.  Synchronous; not allowed during graph capture. */

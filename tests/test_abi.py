@@ -54,16 +54,17 @@ def test_host_entry_points_validate_arguments():
 
 
 def test_tune_space_lists_every_compiled_variant():
-    """bvhgpu_tune_space needs no device: 5 launch shapes x 3 stacks x 5 big-leaf values, times 3
-    refill sizes for the persistent kernels; the default shape (128, 1) is in it."""
+    """bvhgpu_tune_space needs no device: 5 launch shapes x 3 stacks x 5 big-leaf values x 5
+    hidden-tree margins, times 3 refill sizes for the persistent kernels."""
     from bvhtracer_gb300.api import Context
     import bvhtracer_gb300 as bt
-    for kernel, n in ((bt.K_TRACE_BLAS, 75), (bt.K_TRACE_SCENE, 75), (bt.K_PERSISTENT_BOUNCE, 225),
-                      (bt.K_TRACE_BATCH, 225), (bt.K_SCENE_BOUNCE, 225)):
+    for kernel, n in ((bt.K_TRACE_BLAS, 375), (bt.K_TRACE_SCENE, 375), (bt.K_PERSISTENT_BOUNCE, 1125),
+                      (bt.K_TRACE_BATCH, 1125), (bt.K_SCENE_BOUNCE, 1125)):
         space = Context.tune_space(kernel)
         assert len(space) == n
         assert {(c["block"], c["min_blocks"]) for c in space} == {(128, 1), (128, 5), (128, 6), (128, 8), (64, 1)}
         assert {c["stack"] for c in space} == {8, 32, 256}
         assert bt.BIG_LEAF_NEVER in {c["big_leaf"] for c in space}
+        assert {c["hidden"] for c in space} == {0, 100, 250, 500, 1000}
     lib = _lib.load()
     assert lib.bvhgpu_tune_space(3, None, 0, None) == 1  # bounce generation has no variants

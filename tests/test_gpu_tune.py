@@ -1,6 +1,7 @@
 """Launch configurations: every compiled variant of the five traversal kernels (launch shape x
-stack) with both leaf layouts and two refill sizes gives the oracle's hits bit for bit, and the
-autotuner returns a config from the search space under which the results are unchanged."""
+stack) with both leaf layouts, hidden trees on and off and two refill sizes gives the oracle's hits
+bit for bit, and the autotuner returns a config from the search space under which the results are
+unchanged."""
 import numpy as np
 import pytest
 
@@ -19,9 +20,10 @@ def ctx():
 
 
 def subset(kernel):
-    """All shapes x stacks; big_leaf 8 (warp-cooperative) and NEVER (per lane); refill 1 and 16."""
+    """All shapes x stacks; big_leaf 8 (warp-cooperative) and NEVER (per lane); refill 1 and 16;
+    hidden trees never (0) and at the widest margin (1000)."""
     return [c for c in bt.Context.tune_space(kernel)
-            if c["big_leaf"] in (8, bt.BIG_LEAF_NEVER) and c["refill"] in (1, 16)]
+            if c["big_leaf"] in (8, bt.BIG_LEAF_NEVER) and c["refill"] in (1, 16) and c["hidden"] in (0, 1000)]
 
 
 def build(tris):
