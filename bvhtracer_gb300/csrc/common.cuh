@@ -420,7 +420,18 @@ __device__ __forceinline__ bool test_hidden_leaf(const GBlas& b, uint32_t first,
     return better;
 }
 
+// box_live of a hidden node for a ray whose margins are on (the only rays that walk hidden trees),
+// with the common case -- no zero direction component -- as straight-line code.
 __device__ __forceinline__ bool hidden_box(float4 lo, float4 hi, float3 rd, const LeafCull& lc, float& t_enter) {
+    if (lc.zero == 0u) {
+        const float x1 = fmaf(lo.x, rd.x, lc.slo[0]), x2 = fmaf(hi.x, rd.x, lc.shi[0]);
+        const float y1 = fmaf(lo.y, rd.y, lc.slo[1]), y2 = fmaf(hi.y, rd.y, lc.shi[1]);
+        const float z1 = fmaf(lo.z, rd.z, lc.slo[2]), z2 = fmaf(hi.z, rd.z, lc.shi[2]);
+        const float tlo = fmaxf(fmaxf(lc.tlo, fminf(x1, x2)), fmaxf(fminf(y1, y2), fminf(z1, z2)));
+        const float thi = fminf(fminf(lc.thi, fmaxf(x1, x2)), fminf(fmaxf(y1, y2), fmaxf(z1, z2)));
+        t_enter = tlo;
+        return tlo <= thi;
+    }
     const float l[3] = {lo.x, lo.y, lo.z}, h[3] = {hi.x, hi.y, hi.z}, d[3] = {rd.x, rd.y, rd.z};
     return box_live(l, h, d, lc, t_enter);
 }
@@ -458,37 +469,37 @@ struct TravT {
         return true;
     }
 
-    // Processes one node.  A reference leaf with a hidden tree continues at the tree's root when
-    // the ray's margins (computed here) are narrow enough to cull; other leaves with more than
-    // `pol.big_leaf` triangles are not tested here: the step returns kStepBigLeaf with (first, cnt) describing the leaf, and the
-    // caller tests it (warp-cooperatively) and then calls pop().
-    __device__ __forceinline__ StepResult step(const GBlas& b, LaneRay& r, LeafPolicy pol, uint32_t* err) {
-        if (++steps > max_steps) {
-            atomicOr(err, kErrSteps);
-            return kStepFinished;
-        }
-        if (cnt > 0) {
-            if (cnt & kHiddenLeaf) {
-                if (test_hidden_leaf(b, first, cnt & ~kHiddenLeaf, r, held)) lc.thi = leaf_thi(lc, r.ct);
-                return pop() ? kStepFinished : kStepContinue;
-            }
-            if (b.hx != nullptr) {
-                const uint4 e = __ldg(b.hx + first);
-                if ((e.x | e.y) != 0u) {
-                    lc = leaf_cull(cull_ray_rd(r.o.x, r.o.y, r.o.z, r.d.x, r.d.y, r.d.z, r.rd.x, r.rd.y, r.rd.z),
-                                   __uint_as_float(e.z), __uint_as_float(e.w), r.ct, pol.max_duv);
-                    if (lc.on) {  // else: margins too wide for this ray, the leaf is tested in order
-                        held = false;
-                        first = e.x;
-                        cnt = e.y;
-                        return kStepContinue;
-                    }
-                }
-            }
-            if (cnt > pol.big_leaf) return kStepBigLeaf;
-            test_leaf_lane(b.tris, first, cnt, r);
+    // A leaf node (cnt > 0).  A hidden leaf is tested by the lane.  A reference leaf with a hidden
+    // tree continues at the tree's root when the ray's margins (computed here) are narrow enough to
+    // cull; other reference leaves with more than `pol.big_leaf` triangles are not tested here: the
+    // step returns kStepBigLeaf with (first, cnt) describing the leaf, and the caller tests it
+    // (warp-cooperatively) and then calls pop().
+    __device__ __forceinline__ StepResult leaf(const GBlas& b, LaneRay& r, LeafPolicy pol) {
+        if (cnt & kHiddenLeaf) {
+            if (test_hidden_leaf(b, first, cnt & ~kHiddenLeaf, r, held)) lc.thi = leaf_thi(lc, r.ct);
             return pop() ? kStepFinished : kStepContinue;
         }
+        if (b.hx != nullptr) {
+            const uint4 e = __ldg(b.hx + first);
+            if ((e.x | e.y) != 0u) {
+                lc = leaf_cull(cull_ray_rd(r.o.x, r.o.y, r.o.z, r.d.x, r.d.y, r.d.z, r.rd.x, r.rd.y, r.rd.z),
+                               __uint_as_float(e.z), __uint_as_float(e.w), r.ct, pol.max_duv);
+                if (lc.on) {  // else: margins too wide for this ray, the leaf is tested in order
+                    held = false;
+                    first = e.x;
+                    cnt = e.y;
+                    return kStepContinue;
+                }
+            }
+        }
+        if (cnt > pol.big_leaf) return kStepBigLeaf;
+        test_leaf_lane(b.tris, first, cnt, r);
+        return pop() ? kStepFinished : kStepContinue;
+    }
+
+    // An interior node (cnt == 0): its children's boxes -- the reference's slab test for reference
+    // nodes, the margins' exact cull for hidden ones -- then the near child, the far one pushed.
+    __device__ __forceinline__ StepResult interior(const GBlas& b, LaneRay& r, uint32_t* err) {
         const float4* N = b.nodes + 2ull * first;
         float4 l0 = __ldg(N);
         float4 l1 = __ldg(N + 1);
@@ -496,7 +507,7 @@ struct TravT {
         float4 r1 = __ldg(N + 3);
         float dl, dr;
         bool hl, hr, left_near;
-        if (first >= b.nodes_used) {  // hidden children: the margins' exact cull, any order
+        if (first >= b.nodes_used) {  // hidden children: any order is exact
             hl = hidden_box(l0, l1, r.rd, lc, dl);
             hr = hidden_box(r0, r1, r.rd, lc, dr);
             left_near = hl && (!hr || dl <= dr);
@@ -520,10 +531,31 @@ struct TravT {
         return pop() ? kStepFinished : kStepContinue;
     }
 
-    // Steps until the lane finishes or stops at a big leaf.
+    __device__ __forceinline__ bool over_cap(uint32_t* err) {
+        if (++steps > max_steps) {
+            atomicOr(err, kErrSteps);
+            return true;
+        }
+        return false;
+    }
+
+    // Processes one node.
+    __device__ __forceinline__ StepResult step(const GBlas& b, LaneRay& r, LeafPolicy pol, uint32_t* err) {
+        if (over_cap(err)) return kStepFinished;
+        return cnt > 0 ? leaf(b, r, pol) : interior(b, r, err);
+    }
+
+    // Steps until the lane finishes or stops at a big leaf: interior nodes in an inner loop, then
+    // leaves, so that the lanes of a warp run the same kind of node together.
     __device__ __forceinline__ StepResult advance(const GBlas& b, LaneRay& r, LeafPolicy pol, uint32_t* err) {
         for (;;) {
-            StepResult s = step(b, r, pol, err);
+            while (cnt == 0) {
+                if (over_cap(err)) return kStepFinished;
+                const StepResult s = interior(b, r, err);
+                if (s != kStepContinue) return s;
+            }
+            if (over_cap(err)) return kStepFinished;
+            const StepResult s = leaf(b, r, pol);
             if (s != kStepContinue) return s;
         }
     }
