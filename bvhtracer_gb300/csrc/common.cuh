@@ -545,17 +545,26 @@ struct TravT {
         return cnt > 0 ? leaf(b, r, pol) : interior(b, r, err);
     }
 
-    // Steps until the lane finishes or stops at a big leaf: interior nodes in an inner loop, then
-    // leaves, so that the lanes of a warp run the same kind of node together.
+    // Steps until the lane finishes or stops at a big leaf.  GROUPED: interior nodes in an inner
+    // loop, then leaves, so that the lanes of a warp run the same kind of node together (faster for
+    // warps of similar rays); otherwise one node of either kind per iteration (faster where a warp
+    // mixes rays of different kinds, as the persistent kernels' warps do).
+    template <bool GROUPED = false>
     __device__ __forceinline__ StepResult advance(const GBlas& b, LaneRay& r, LeafPolicy pol, uint32_t* err) {
-        for (;;) {
-            while (cnt == 0) {
+        if (GROUPED) {
+            for (;;) {
+                while (cnt == 0) {
+                    if (over_cap(err)) return kStepFinished;
+                    const StepResult s = interior(b, r, err);
+                    if (s != kStepContinue) return s;
+                }
                 if (over_cap(err)) return kStepFinished;
-                const StepResult s = interior(b, r, err);
+                const StepResult s = leaf(b, r, pol);
                 if (s != kStepContinue) return s;
             }
-            if (over_cap(err)) return kStepFinished;
-            const StepResult s = leaf(b, r, pol);
+        }
+        for (;;) {
+            const StepResult s = step(b, r, pol, err);
             if (s != kStepContinue) return s;
         }
     }
