@@ -235,7 +235,7 @@ uint32_t spread3(uint32_t x) {
 // depth first; the boxes and the leaf bounds Q, B are written by the refresh kernel from `work`.
 struct HiddenPlan {
     std::vector<float> nodes;  // 8 floats per hidden node (boxes 0 until refreshed)
-    std::vector<uint4> table;  // ntris entries (empty: no hidden tree)
+    std::vector<uint4> table;  // 2 per triangle index (empty: no hidden tree)
     std::vector<uint2> slots;  // per hidden pair
     std::vector<uint4> work;   // per hidden node, then per hidden root
     uint32_t nhid = 0, nhp = 0, depth = 0;
@@ -283,7 +283,7 @@ void plan_hidden(const bvhgpu_node* nodes, uint32_t nodes_used, const std::vecto
     for (uint32_t li : leaves) {
         const bvhgpu_node& n = nodes[li];
         if (n.primitive_count < kHiddenMinLeaf) continue;
-        if (hp.table.empty()) hp.table.assign(ntris, make_uint4(0u, 0u, 0u, 0u));
+        if (hp.table.empty()) hp.table.assign(2ull * ntris, make_uint4(0u, 0u, 0u, 0u));
         keys.clear();
         for (uint32_t k = 0; k < n.primitive_count; ++k) {
             const float* v = tris[n.left_first + k].vertices;
@@ -300,7 +300,7 @@ void plan_hidden(const bvhgpu_node* nodes, uint32_t nodes_used, const std::vecto
         std::sort(keys.begin(), keys.end());
         const uint32_t pa = P0 + hp.nhp;
         const uint2 root = make(make, 0, n.primitive_count, 0);
-        hp.table[n.left_first] = make_uint4(root.x, root.y, 0u, 0u);
+        hp.table[2ull * n.left_first] = make_uint4(root.x, 0u, 0u, 0u);  // root: interior (>= 16 triangles)
         roots.push_back(make_uint4(pa, P0 + hp.nhp, kWorkRoot | n.left_first, 0u));
     }
     hp.work.insert(hp.work.end(), roots.begin(), roots.end());
@@ -519,7 +519,7 @@ int bvhgpu_blas_upload(bvhgpu_ctx* ctx, const bvhgpu_node* nodes, uint32_t nodes
     b.depth = depth + hp.depth;
     const uint64_t nodes_all = (uint64_t)nodes_used + hp.nhid;
     const uint64_t pairs_all = (uint64_t)pairs_in_order(ntris) + hp.nhp;
-    const uint64_t hx_bytes = hp.table.empty() ? 0 : 16ull * ntris + 8ull * std::max<uint32_t>(1, hp.nhp);
+    const uint64_t hx_bytes = hp.table.empty() ? 0 : 32ull * ntris + 8ull * std::max<uint32_t>(1, hp.nhp);
     void* d_tris9 = nullptr;
     cudaError_t e = cudaSuccess;
     auto cleanup = [&]() {
@@ -551,9 +551,9 @@ int bvhgpu_blas_upload(bvhgpu_ctx* ctx, const bvhgpu_node* nodes, uint32_t nodes
         (e = cudaMemcpy(d_tris9, tris, 36ull * ntris, cudaMemcpyHostToDevice)) != cudaSuccess ||
         (hp.nhid && (e = cudaMemcpy(b.nodes + 2ull * nodes_used, hp.nodes.data(), 32ull * hp.nhid,
                                     cudaMemcpyHostToDevice)) != cudaSuccess) ||
-        (hx_bytes && (e = cudaMemcpy(b.hx, hp.table.data(), 16ull * ntris, cudaMemcpyHostToDevice)) != cudaSuccess) ||
+        (hx_bytes && (e = cudaMemcpy(b.hx, hp.table.data(), 32ull * ntris, cudaMemcpyHostToDevice)) != cudaSuccess) ||
         (hx_bytes && hp.nhp &&
-         (e = cudaMemcpy(b.hx + ntris, hp.slots.data(), 8ull * hp.nhp, cudaMemcpyHostToDevice)) != cudaSuccess) ||
+         (e = cudaMemcpy(b.hx + 2ull * ntris, hp.slots.data(), 8ull * hp.nhp, cudaMemcpyHostToDevice)) != cudaSuccess) ||
         (b.nwork && (e = cudaMemcpy(b.hwork, hp.work.data(), 16ull * b.nwork, cudaMemcpyHostToDevice)) != cudaSuccess) ||
         (e = launch_write_tris(ctx, b, static_cast<const float*>(d_tris9), ctx->stream)) != cudaSuccess ||
         (e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess) {

@@ -31,10 +31,10 @@ struct GBlas {
     // Triangle pairs (2p, 2p+1) interleaved for packed f32x2 math: 20 floats per pair, component
     // c of {v0x v0y v0z e1x e1y e1z e2x e2y e2z} of triangle 2p + h at float 2c + h.
     const ulonglong2* pairs;
-    // Hidden trees of the large leaves (null when none): ntris uint4 entries read at a leaf's first
-    // triangle, {first, count} of the hidden root node (both 0: no hidden tree) and the leaf's Q and
-    // B bits (cull.cuh), then one uint2 per hidden pair p >= (ntris + 1) / 2: the triangle indices
-    // of its two slots (0xFFFFFFFF: padding).  Hidden nodes follow the reference's nodes_used nodes
+    // Hidden trees of the large leaves (null when none): two uint4 per triangle index, read at a
+    // leaf's first triangle: {first child of the hidden root (0: no hidden tree), Q, B, nmin} and
+    // {cone axis xyz, cos_phi} (floats as bits, cull.cuh); then one uint2 per hidden pair
+    // p >= (ntris + 1) / 2: the triangle indices of its two slots (0xFFFFFFFF: padding).  Hidden nodes follow the reference's nodes_used nodes
     // in `nodes` (a node whose children start at or beyond nodes_used is hidden); a hidden leaf has
     // count = kHiddenLeaf | pairs and first = its first pair in `pairs`, after the (ntris + 1) / 2
     // pairs in triangle order.
@@ -50,6 +50,7 @@ constexpr uint32_t kHiddenLeaf = 0x80000000u;
 // kHiddenLeafTris triangles (two packed pairs).
 constexpr uint32_t kHiddenMinLeaf = 16;
 constexpr uint32_t kHiddenLeafTris = 4;
+static_assert(kHiddenMinLeaf > kHiddenLeafTris, "a hidden root is an interior node");
 
 __host__ __device__ __forceinline__ uint32_t pairs_in_order(uint32_t ntris) { return (ntris + 1u) / 2u; }
 
@@ -386,7 +387,7 @@ struct LocalStack {
 // while the held hit came from the same reference leaf (`held`): the reference's in-order leaf loop
 // keeps the lowest index among equal t, and a hit from an earlier leaf keeps equal t out.
 __device__ __forceinline__ bool test_hidden_leaf(const GBlas& b, uint32_t first, uint32_t np, LaneRay& r, bool& held) {
-    const uint2* hidx = reinterpret_cast<const uint2*>(b.hx + b.ntris) - pairs_in_order(b.ntris);
+    const uint2* hidx = reinterpret_cast<const uint2*>(b.hx + 2ull * b.ntris) - pairs_in_order(b.ntris);
     const f2 OX = f2_pack(r.o.x, r.o.x), OY = f2_pack(r.o.y, r.o.y), OZ = f2_pack(r.o.z, r.o.z);
     const f2 DX = f2_pack(r.d.x, r.d.x), DY = f2_pack(r.d.y, r.d.y), DZ = f2_pack(r.d.z, r.d.z);
     const f2 Z = f2_neg_zero();
@@ -480,14 +481,17 @@ struct TravT {
             return pop() ? kStepFinished : kStepContinue;
         }
         if (b.hx != nullptr) {
-            const uint4 e = __ldg(b.hx + first);
-            if ((e.x | e.y) != 0u) {
+            const uint4 e = __ldg(b.hx + 2ull * first);
+            if (e.x != 0u) {
+                const uint4 c = __ldg(b.hx + 2ull * first + 1);
+                const LeafCone cone = {__uint_as_float(c.x), __uint_as_float(c.y), __uint_as_float(c.z),
+                                       __uint_as_float(c.w), __uint_as_float(e.w)};
                 lc = leaf_cull(cull_ray_rd(r.o.x, r.o.y, r.o.z, r.d.x, r.d.y, r.d.z, r.rd.x, r.rd.y, r.rd.z),
-                               __uint_as_float(e.z), __uint_as_float(e.w), r.ct, pol.max_duv);
+                               __uint_as_float(e.y), __uint_as_float(e.z), r.ct, pol.max_duv, cone);
                 if (lc.on) {  // else: margins too wide for this ray, the leaf is tested in order
                     held = false;
-                    first = e.x;
-                    cnt = e.y;
+                    first = e.x;  // the hidden root is always an interior node
+                    cnt = 0u;
                     return kStepContinue;
                 }
             }

@@ -28,17 +28,22 @@
 // Both bounds are symmetric (|t - t*| <= Dt(t)), so an accepted hit (t > 1e-4) also has
 // t* > 1e-4 - Dt(1e-4): parts of the line behind that need no test either.
 //
+// The same bounds hold with 1e-4 (1 - rho) replaced by any lower bound Dlo of |det*|.  A leaf also
+// keeps a cone of its triangles' normal lines (an axis A with every |N_k . A| >= cos_phi |N_k| |A|,
+// N_k = e1 x e2) and a lower bound nmin of |N_k|; det* = -d . N_k, so for a ray whose line makes an
+// angle theta with A's, |det*| >= nmin |d| cos(theta + phi) when theta + phi < 90 degrees -- for
+// triangles facing the ray this is far above 1e-4, and the margins shrink by the same factor.
+//
 // The leaf keeps Q >= E1 + E2 (so E1 E2 <= Q^2 / 4) and B >= every |coordinate| of its boxes (so
 // S <= |o|_inf + B); the margins are computed once per ray and leaf (leaf_cull) and each box then
-// costs one slab test (box_live).  The evaluation never culls more than
-// the argument allows: every error term carries a factor 4, R another factor 2, 1 / 1e-4 is
-// rounded up to 10102 (>= 1 / 9.9e-5), 1 / (1 - x) is replaced by its upper bound 1 + 2x
-// (x < 1/2), the stored boxes are widened outward by a relative 4 u0 (they are computed from the
+// costs one slab test (box_live).  The evaluation never culls more than the argument allows:
+// every error term carries a factor 4, R another factor 2, every bound is rounded outward by a
+// few u0 (the cone's cosines and lengths included), the stored boxes are widened outward by a relative 4 u0 (they are computed from the
 // rounded vertices v0 + e1, v0 + e2), and the grown box gets an extra slack of
 // 8 u0 (2 B + |o_i| + R) per axis, which exceeds the rounding of the slab arithmetic
 // fma(lo, 1 / d, -(o + g) / d) with the IEEE reciprocal (<= 5.1 u0 R + 4.1 u0 |o| + 2.1 u0 |lo|).
 // Leaves with a non-finite or huge coordinate (Q = +inf), rays with a non-finite or huge component
-// or a tiny non-zero d_i (|1 / d_i| >= 1e20), and leaves where rho is not small are never culled.
+// or a tiny non-zero d_i (|1 / d_i| >= 1e20), and leaves without a positive Dlo are never culled.
 // Both properties were audited on the CPU against the float test on adversarial rays (aimed at
 // edges and vertices, grazing the plane, axis-aligned): no culled box held an accepted hit at or
 // below t_best, and the measured errors stayed below 5 % of the margins.
@@ -58,7 +63,6 @@ namespace bvhgpu {
 
 constexpr float kCullUnit = 5.9604645e-8f;  // u0 = 2^-24
 constexpr float kCullSafety = 4.0f;
-constexpr float kCullInvDet = 10102.0f;     // >= 1 / 9.9e-5 > 1 / 1e-4
 constexpr float kCullHuge = 1e15f;
 
 BVHGPU_HD float cull_fmax(float a, float b) { return a > b ? a : b; }
@@ -132,6 +136,58 @@ BVHGPU_HD CullRay cull_ray(float ox, float oy, float oz, float dx, float dy, flo
     return cull_ray_rd(ox, oy, oz, dx, dy, dz, 1.0f / dx, 1.0f / dy, 1.0f / dz);
 }
 
+// The normal cone of a leaf's triangles (see above); nmin = 0 or cos_phi <= 0: none.
+struct LeafCone {
+    float ax, ay, az;
+    float cos_phi, nmin;
+};
+
+// One triangle's contribution to a cone around axis (ax, ay, az): a lower bound of
+// |N . A| / (|N| |A|) and of |N| for the exact N = e1 x e2, from the float edges.
+BVHGPU_HD void cone_terms(const float e1[3], const float e2[3], float ax, float ay, float az, float& cos_lo,
+                          float& n_lo) {
+    const float u0 = kCullUnit;
+    // N = e1 x e2 in float, each component within eN of the exact one
+    const float n[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+    const float en[3] = {3.0f * u0 * (cull_abs(e1[1] * e2[2]) + cull_abs(e1[2] * e2[1])),
+                         3.0f * u0 * (cull_abs(e1[2] * e2[0]) + cull_abs(e1[0] * e2[2])),
+                         3.0f * u0 * (cull_abs(e1[0] * e2[1]) + cull_abs(e1[1] * e2[0]))};
+    const float a[3] = {ax, ay, az};
+    float dot = 0.0f, dot_err = 0.0f, nn = 0.0f, n_err = 0.0f, aa = 0.0f;
+    for (int i = 0; i < 3; ++i) {
+        dot += n[i] * a[i];
+        dot_err += (en[i] + 4.0f * u0 * cull_abs(n[i])) * cull_abs(a[i]);
+        nn += n[i] * n[i];
+        n_err += en[i];
+        aa += a[i] * a[i];
+    }
+    const float nlen = sqrtf(nn), alen = sqrtf(aa);
+    n_lo = (nlen * (1.0f - 8.0f * u0) - n_err) * (1.0f - 4.0f * u0);
+    const float num = cull_abs(dot) - dot_err;
+    const float den = (nlen * (1.0f + 8.0f * u0) + n_err) * alen * (1.0f + 8.0f * u0);
+    cos_lo = (num > 0.0f && den > 0.0f && n_lo > 0.0f) ? num / den * (1.0f - 8.0f * u0) : -1.0f;
+    if (!(n_lo > 0.0f)) n_lo = 0.0f;
+}
+
+// A lower bound of |d . N_k| for every triangle of a leaf with cone c (0 when it gives none).
+BVHGPU_HD float cone_det_lo(const float d[3], const LeafCone& c) {
+    const float u0 = kCullUnit;
+    if (!(c.nmin > 0.0f) || !(c.cos_phi > 0.0f) || !(c.cos_phi <= 1.0f)) return 0.0f;
+    const float a = d[0] * c.ax + d[1] * c.ay + d[2] * c.az;
+    const float a_err = 4.0f * u0 * (cull_abs(d[0] * c.ax) + cull_abs(d[1] * c.ay) + cull_abs(d[2] * c.az));
+    const float dd = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+    const float AA = c.ax * c.ax + c.ay * c.ay + c.az * c.az;
+    const float dlen = sqrtf(dd), alen = sqrtf(AA);
+    const float cos_t = (cull_abs(a) - a_err) / (dlen * alen * (1.0f + 8.0f * u0)) * (1.0f - 4.0f * u0);
+    if (!(cos_t > 0.0f)) return 0.0f;
+    const float sin_t = sqrtf(cull_fmax(0.0f, 1.0f - cos_t * cos_t * (1.0f - 4.0f * u0))) * (1.0f + 4.0f * u0);
+    const float sin_p = sqrtf(cull_fmax(0.0f, 1.0f - c.cos_phi * c.cos_phi * (1.0f - 4.0f * u0))) * (1.0f + 4.0f * u0);
+    const float cs = (cos_t * c.cos_phi * (1.0f - 4.0f * u0) - sin_t * sin_p * (1.0f + 4.0f * u0)) * (1.0f - 4.0f * u0);
+    if (!(cs > 0.0f)) return 0.0f;
+    const float lo = c.nmin * dlen * (1.0f - 4.0f * u0) * cs * (1.0f - 64.0f * u0);
+    return lo < FLT_MAX ? lo : 0.0f;
+}
+
 // The per-(ray, leaf) part: the grown slab planes folded with the origin, c_lo = o + g and
 // c_hi = o - g per axis, pre-scaled by -1 / d where d is not zero (slab t = fma(x, 1/d, s)), the
 // largest t that still matters (thi, from the ray's closest t) and the smallest (tlo: accepted hits
@@ -151,8 +207,8 @@ BVHGPU_HD float leaf_thi(const LeafCull& lc, float t_best) {
 }
 
 // max_duv: the largest barycentric margin (Du + Dv) worth culling with; on = false above it.
-BVHGPU_HD LeafCull leaf_cull(const CullRay& r, float Q, float B, float t_best, float max_duv = 0.5f) {
-    const float u0 = kCullUnit, K = kCullInvDet;
+BVHGPU_HD LeafCull leaf_cull(const CullRay& r, float Q, float B, float t_best, float max_duv, const LeafCone& cone) {
+    const float u0 = kCullUnit;
     LeafCull lc;
     lc.on = false;
     lc.zero = 0u;
@@ -168,19 +224,23 @@ BVHGPU_HD LeafCull leaf_cull(const CullRay& r, float Q, float B, float t_best, f
     const float S = (oinf + B) * (1.0f + 4.0f * u0);
     const float P = 0.25f * Q * Q * (1.0f + 4.0f * u0);  // >= E1 E2
     const float e_det = r.a_det * P;
-    const float rho = e_det * K;
-    if (!(rho < 0.25f)) return lc;
-    const float inv = 1.0f + 2.0f * (rho + 8.0f * u0);  // >= 1 / (1 - rho - 8 u0)
+    // |det*| >= Dlo: accepted |det| >= 1e-4 (the float 0.0001f, triangle.rs:47), or the cone's bound
+    const float d_acc = 0.0001f * (1.0f - 4.0f * u0) - e_det;
+    const float d_cone = cone_det_lo(r.d, cone);
+    const float Dlo = cull_fmax(d_acc, d_cone);
+    if (!(Dlo > 0.0f)) return lc;
+    const float KD = 1.0f / Dlo * (1.0f + 4.0f * u0);  // >= 1 / Dlo
+    if (!(KD < kCullHuge)) return lc;
     const float e_uv = r.b_uv * S * Q;                   // >= E_u + E_v
-    const float duv = ((e_uv + 2.0f * e_det) * K + 8.0f * u0) * inv;
+    const float duv = ((e_uv + 2.0f * e_det) * KD + 8.0f * u0) * (1.0f + 4.0f * u0);
     // margins of half a triangle or more cull little: the caller tests the leaf in order instead
     if (!(duv < max_duv)) return lc;
     const float R = 4.0f * (duv + 2.0f * u0) * Q * 1.0001f + 1e-30f;
     if (!(R < kCullHuge)) return lc;
     const float e_t = kCullSafety * 36.0f * u0 * S * P;
-    // Dt(t) = ((E_t + t E_det) / 1e-4 + 2 u0 t) / (1 - rho) <= dt0 + t dt1
-    lc.dt0 = e_t * K * inv * (1.0f + 4.0f * u0);
-    lc.dt1 = (e_det * K + 4.0f * u0) * inv * (1.0f + 4.0f * u0);
+    // Dt(t) = (E_t + t E_det) / Dlo + 2 u0 t <= dt0 + t dt1
+    lc.dt0 = e_t * KD * (1.0f + 4.0f * u0);
+    lc.dt1 = (e_det * KD + 4.0f * u0) * (1.0f + 4.0f * u0);
     lc.thi = leaf_thi(lc, t_best);
     const float th = 0.0001f;  // the test's threshold (triangle.rs:47)
     lc.tlo = cull_down(th - (lc.dt0 + th * lc.dt1) * (1.0f + 8.0f * u0)) - 1e-30f;

@@ -17,6 +17,7 @@
 
 #include "common.cuh"
 #include "internal.hpp"
+#include "variants.cuh"
 
 namespace bvhgpu {
 
@@ -42,13 +43,14 @@ inline GBlas to_gblas(const DeviceBlas& b) {
 }
 
 template <int STACK>
-__device__ __forceinline__ void warp_trace_local(const GBlas& b, bool active, LaneRay& r, uint32_t* err) {
+__device__ __forceinline__ void warp_trace_local(const GBlas& b, bool active, LaneRay& r, LeafPolicy pol,
+                                                 uint32_t* err) {
     Trav<STACK> tr;
     if (active) tr.init(b);
     StepResult st = active ? kStepContinue : kStepFinished;
     const unsigned lane = threadIdx.x & 31u;
     for (;;) {
-        if (st == kStepContinue) st = tr.advance(b, r, kDefaultPolicy, err);
+        if (st == kStepContinue) st = tr.template advance<true>(b, r, pol, err);
         unsigned pend = __ballot_sync(kFull, st == kStepBigLeaf);
         if (pend == 0u) break;
         while (pend) {
@@ -142,7 +144,7 @@ __global__ void __launch_bounds__(kBlock) k_lambert_forward(GBlas b, const float
                                                             const float* __restrict__ verts,
                                                             const float* __restrict__ vnormals, float3 light,
                                                             float* __restrict__ image, GHit* __restrict__ hits,
-                                                            uint32_t* err) {
+                                                            LeafPolicy pol, uint32_t* err) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (__all_sync(kFull, i >= n)) return;
     const bool active = i < n;
@@ -159,7 +161,7 @@ __global__ void __launch_bounds__(kBlock) k_lambert_forward(GBlas b, const float
         r.hp = 0;
         r.hit = false;
     }
-    warp_trace_local<STACK>(b, active, r, err);
+    warp_trace_local<STACK>(b, active, r, pol, err);
     if (!active) return;
     const bool hit = r.hit && r.ct < FLT_MAX;
     store_hit(hits, i, hit, r.ct, r.hu, r.hv, r.hp, 0u);
@@ -264,19 +266,21 @@ cudaError_t launch_lambert_forward(bvhgpu_ctx* ctx, DeviceMesh& m, const DeviceB
     if (n == 0) return cudaSuccess;
     GBlas g = to_gblas(b);
     float3 L = make_float3(light[0], light[1], light[2]);
+    // the leaf policy (big leaves, hidden-tree margin) of the plain trace kernel's launch config
+    const LeafPolicy pol = resolve(ctx->tune[BVHGPU_K_TRACE_BLAS], b.depth).pol;
     LaunchScope scope(ctx, BVHGPU_K_LAMBERT_FORWARD, s);
     switch (stack_variant(b.depth)) {
         case 32:
             k_lambert_forward<32><<<grid_for(n, kBlock), kBlock, 0, s>>>(g, rays, n, m.faces, m.verts, m.vnormals, L,
-                                                                         image, static_cast<GHit*>(hits), ctx->d_err);
+                                                                         image, static_cast<GHit*>(hits), pol, ctx->d_err);
             break;
         case 64:
             k_lambert_forward<64><<<grid_for(n, kBlock), kBlock, 0, s>>>(g, rays, n, m.faces, m.verts, m.vnormals, L,
-                                                                         image, static_cast<GHit*>(hits), ctx->d_err);
+                                                                         image, static_cast<GHit*>(hits), pol, ctx->d_err);
             break;
         default:
             k_lambert_forward<256><<<grid_for(n, kBlock), kBlock, 0, s>>>(g, rays, n, m.faces, m.verts, m.vnormals, L,
-                                                                          image, static_cast<GHit*>(hits), ctx->d_err);
+                                                                          image, static_cast<GHit*>(hits), pol, ctx->d_err);
             break;
     }
     g_launches++;

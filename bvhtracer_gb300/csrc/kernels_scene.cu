@@ -50,7 +50,7 @@ __global__ void k_write_tris(const float* __restrict__ tris9, uint32_t n, float4
 // ---- hidden trees of the large leaves, refreshed after every triangle write -----------------
 // Hidden pairs: the triangles of each pair's two slots (membership fixed at upload) copied into the
 // packed layout.  Then one warp per hidden node (and per hidden root): the widened box of the
-// node's pairs and, for a root, the leaf's bounds Q and B (cull.cuh).
+// node's pairs and, for a root, the leaf's bounds Q, B and normal cone (cull.cuh).
 __global__ void k_hidden_pairs(const float4* __restrict__ tris, const uint2* __restrict__ slots, uint32_t nhp,
                                float* __restrict__ pairs) {
     const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -106,17 +106,84 @@ __global__ void k_hidden_boxes(const uint4* __restrict__ work, uint32_t nwork, c
         e2m = fmaxf(e2m, __shfl_xor_sync(0xFFFFFFFFu, e2m, off));
     }
     finite = __all_sync(0xFFFFFFFFu, finite);
-    if (lane != 0) return;
     const GroupSeal g = group_seal(lo, hi, e1m, e2m, finite);
-    if (job.z & 0x80000000u) {
-        uint4& e = table[job.z & 0x7FFFFFFFu];
-        e.z = __float_as_uint(g.q);
-        e.w = __float_as_uint(g.b);
-    } else {
-        float4* N = nodes + 2ull * job.z;
-        N[0] = make_float4(g.lo[0], g.lo[1], g.lo[2], N[0].w);
-        N[1] = make_float4(g.hi[0], g.hi[1], g.hi[2], N[1].w);
+    if (!(job.z & 0x80000000u)) {
+        if (lane == 0) {
+            float4* N = nodes + 2ull * job.z;
+            N[0] = make_float4(g.lo[0], g.lo[1], g.lo[2], N[0].w);
+            N[1] = make_float4(g.hi[0], g.hi[1], g.hi[2], N[1].w);
+        }
+        return;
     }
+    // a hidden root: the leaf's Q, B and the cone of its normal lines (any axis is valid; the sum
+    // of unit normals, each turned towards the first triangle's, makes it narrow)
+    float rx = 0.0f, ry = 0.0f, rz = 0.0f;
+    if (lane == 0) {
+        for (uint32_t p = job.x; p < job.y; ++p) {
+            const uint2 idx = slots[p - p0];
+            const float* P = pairs + 20ull * p;
+            bool found = false;
+            for (int h = 0; h < 2 && !found; ++h) {
+                if ((h ? idx.y : idx.x) == kMiss) continue;
+                const float a[3] = {P[6 + h], P[8 + h], P[10 + h]}, b[3] = {P[12 + h], P[14 + h], P[16 + h]};
+                rx = a[1] * b[2] - a[2] * b[1];
+                ry = a[2] * b[0] - a[0] * b[2];
+                rz = a[0] * b[1] - a[1] * b[0];
+                found = isfinite(rx) && isfinite(ry) && isfinite(rz) && (rx != 0.0f || ry != 0.0f || rz != 0.0f);
+            }
+            if (found) break;
+        }
+    }
+    rx = __shfl_sync(0xFFFFFFFFu, rx, 0);
+    ry = __shfl_sync(0xFFFFFFFFu, ry, 0);
+    rz = __shfl_sync(0xFFFFFFFFu, rz, 0);
+    float sx = 0.0f, sy = 0.0f, sz = 0.0f;
+    for (uint32_t p = job.x + lane; p < job.y; p += 32u) {
+        const uint2 idx = slots[p - p0];
+        const float* P = pairs + 20ull * p;
+        for (int h = 0; h < 2; ++h) {
+            if ((h ? idx.y : idx.x) == kMiss) continue;
+            const float a[3] = {P[6 + h], P[8 + h], P[10 + h]}, b[3] = {P[12 + h], P[14 + h], P[16 + h]};
+            const float nx = a[1] * b[2] - a[2] * b[1], ny = a[2] * b[0] - a[0] * b[2], nz = a[0] * b[1] - a[1] * b[0];
+            const float len = sqrtf(nx * nx + ny * ny + nz * nz);
+            if (!(len > 0.0f) || !isfinite(len)) continue;
+            const float sg = (nx * rx + ny * ry + nz * rz) < 0.0f ? -1.0f : 1.0f;
+            sx += sg * nx / len;
+            sy += sg * ny / len;
+            sz += sg * nz / len;
+        }
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        sx += __shfl_xor_sync(0xFFFFFFFFu, sx, off);
+        sy += __shfl_xor_sync(0xFFFFFFFFu, sy, off);
+        sz += __shfl_xor_sync(0xFFFFFFFFu, sz, off);
+    }
+    float cmin = 2.0f, nmin = FLT_MAX;
+    for (uint32_t p = job.x + lane; p < job.y; p += 32u) {
+        const uint2 idx = slots[p - p0];
+        const float* P = pairs + 20ull * p;
+        for (int h = 0; h < 2; ++h) {
+            if ((h ? idx.y : idx.x) == kMiss) continue;
+            const float a[3] = {P[6 + h], P[8 + h], P[10 + h]}, b[3] = {P[12 + h], P[14 + h], P[16 + h]};
+            float cl, nl;
+            cone_terms(a, b, sx, sy, sz, cl, nl);
+            cmin = cl < cmin ? cl : (cl == cl ? cmin : -1.0f);  // NaN: no cone
+            nmin = nl < nmin ? nl : (nl == nl ? nmin : 0.0f);
+        }
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        cmin = fminf(cmin, __shfl_xor_sync(0xFFFFFFFFu, cmin, off));
+        nmin = fminf(nmin, __shfl_xor_sync(0xFFFFFFFFu, nmin, off));
+    }
+    if (lane != 0) return;
+    const bool cone_ok = isfinite(sx) && isfinite(sy) && isfinite(sz) && cmin > 0.0f && cmin <= 1.0f &&
+                         nmin > 0.0f && nmin < FLT_MAX;
+    uint4* e = table + 2ull * (job.z & 0x7FFFFFFFu);
+    e[0].y = __float_as_uint(g.q);
+    e[0].z = __float_as_uint(g.b);
+    e[0].w = __float_as_uint(cone_ok ? nmin : 0.0f);
+    e[1] = make_uint4(__float_as_uint(cone_ok ? sx : 0.0f), __float_as_uint(cone_ok ? sy : 0.0f),
+                      __float_as_uint(cone_ok ? sz : 0.0f), __float_as_uint(cone_ok ? cmin : -1.0f));
 }
 
 // ---- refit, parallel over triangles --------------------------------------------------------
@@ -859,7 +926,7 @@ cudaError_t launch_hidden_refresh(bvhgpu_ctx* ctx, DeviceBlas& b, cudaStream_t s
     if (b.nwork == 0) return cudaSuccess;
     LaunchScope scope(ctx, BVHGPU_K_OTHER, s);
     const uint32_t p0 = pairs_in_order(b.ntris);
-    const uint2* slots = reinterpret_cast<const uint2*>(b.hx + b.ntris);
+    const uint2* slots = reinterpret_cast<const uint2*>(b.hx + 2ull * b.ntris);
     float* pairs = reinterpret_cast<float*>(b.pairs);
     k_hidden_pairs<<<grid_for(b.nhp, 256), 256, 0, s>>>(b.tris, slots, b.nhp, pairs + 20ull * p0);
     k_hidden_boxes<<<grid_for(32u * b.nwork, 128), 128, 0, s>>>(b.hwork, b.nwork, pairs, slots, p0, b.nodes, b.hx);

@@ -806,7 +806,7 @@ cudaError_t launch_render(bvhgpu_ctx* ctx, const DeviceBlas& b, const bvhgpu_cam
     GBlas g = to_gblas(b);
     unsigned tiles = (unsigned)(((w + 7) / 8) * ((h + 7) / 8));
     LaunchScope scope(ctx, BVHGPU_K_RENDER, s);
-    BVHGPU_DISPATCH_STACK(b.depth, (k_render<S><<<tiles, 64, 0, s>>>(g, P, d_normals, d_rgba, kDefaultPolicy, ctx->d_err)));
+    BVHGPU_DISPATCH_STACK(b.depth, (k_render<S><<<tiles, 64, 0, s>>>(g, P, d_normals, d_rgba, resolve(ctx->tune[BVHGPU_K_TRACE_BLAS], b.depth).pol, ctx->d_err)));
     g_launches++;
     return cudaGetLastError();
 }

@@ -217,3 +217,23 @@ def test_instanced_scene_with_hidden_trees(ctx):
     sa = orc.SceneArrays([(bvh.nodes[:bvh.nodes_used], bvh.nodes_used, tris)], np.zeros(n, np.int64), inv)
     ref = orc.scene_intersect(tl, used, sa, rays, threads=8)
     same(sc.intersect(rays), ref, "scene")
+
+
+@pytest.mark.parametrize("hidden", [500, 100000])
+def test_large_triangles_far_camera_with_normal_cones(ctx, hidden):
+    """The sphere at 10x scale seen from distance 30 and 300 (margins set by the leaves' normal
+    cones), with rays at vertices and edges from every side -- including the grazing ones at the
+    silhouette, where the cone gives no bound -- at a moderate and an unlimited margin."""
+    verts, faces, _, _, cam, _ = scenes.config4(seed=0, level=5, width=96, height=96)
+    tris = np.ascontiguousarray(verts[faces].reshape(-1, 9), np.float32)
+    bvh = bt.BvhBuilder().build_for(tris)
+    blas = ctx.upload_blas(bvh, tris)
+    saved = ctx.tune_get(bt.K_TRACE_BLAS)
+    try:
+        ctx.tune_set(bt.K_TRACE_BLAS, hidden=hidden)
+        rays = np.concatenate([cam, edge_rays(tris, 20000, 31, eye_dist=30.0), edge_rays(tris, 20000, 32, eye_dist=300.0)])
+        ref = orc.bvh_intersect(bvh.nodes, bvh.nodes_used, tris, rays, threads=8)
+        assert (ref["prim"] != bt.MISS).sum() > 30000
+        same(blas.intersect(rays), ref, f"cones, hidden {hidden}")
+    finally:
+        ctx.tune_set(bt.K_TRACE_BLAS, **saved)
