@@ -131,7 +131,7 @@ struct bvhgpu_ctx {
     bvhgpu_ctx() {
         // defaults: the configs the autotuner picked on GB300 for the displaced-icosphere frame
         // (single BLAS) and the instanced frame (two-level)
-        for (auto& t : tune) t = bvhgpu_tune_config{128u, 5u, 256u, 16u, 8u, 500u};
+        for (auto& t : tune) t = bvhgpu_tune_config{128u, 5u, 256u, 16u, 8u, 2000u};
         tune[BVHGPU_K_TRACE_BLAS].refill = 1u;
         tune[BVHGPU_K_TRACE_SCENE].refill = 1u;
     }

@@ -399,7 +399,7 @@ typedef struct bvhgpu_tune_config {
     uint32_t hidden;
 } bvhgpu_tune_config;
 /* Defaults (the tuner's picks on GB300): block 128, min_blocks 5, stack 256, big_leaf 16, refill 8,
- * hidden 500; for the single-ray kernels (TRACE_BLAS, TRACE_SCENE) refill 1. */
+ * hidden 2000; for the single-ray kernels (TRACE_BLAS, TRACE_SCENE) refill 1. */
 int bvhgpu_tune_get(bvhgpu_ctx* ctx, int kernel, bvhgpu_tune_config* out);
 /* BVHGPU_ERR_INVALID_ARG for a kernel that is not tunable or a shape / stack not compiled. */
 int bvhgpu_tune_set(bvhgpu_ctx* ctx, int kernel, const bvhgpu_tune_config* cfg);
