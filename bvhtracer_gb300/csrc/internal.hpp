@@ -84,6 +84,8 @@ struct ProfileRec {
 struct bvhgpu_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t copy_in = nullptr, copy_out = nullptr;  // chunked host calls (created on first use)
+    std::vector<cudaEvent_t> chunk_events;
     uint32_t* d_err = nullptr;       // device error flags
     uint32_t* d_scratch = nullptr;   // small device scratch: queue counters etc. (64 words)
     void* l2_flush = nullptr;
@@ -155,10 +157,14 @@ struct LaunchScope {
 // ---- launchers (kernels_trace.cu) ------------------------------------------------------
 cudaError_t launch_trace_blas(bvhgpu_ctx* ctx, const DeviceBlas& b, const float4* rays, uint32_t n, void* hits,
                               cudaStream_t s);
+// `base`: index of the first ray in the caller's whole ray set (the bounce directions' random key is
+// the ray's index there, so a call split in chunks gives the same bounces).
 cudaError_t launch_bounce_plain(bvhgpu_ctx* ctx, const DeviceBlas& b, const float4* rays, uint32_t n, uint32_t seed,
-                                void* hits0, void* hits1, cudaStream_t s);
+                                void* hits0, void* hits1, cudaStream_t s, uint32_t base = 0);
 cudaError_t launch_bounce_persistent(bvhgpu_ctx* ctx, const DeviceBlas& b, const float4* rays, uint32_t n,
-                                     uint32_t seed, void* hits0, void* hits1, cudaStream_t s);
+                                     uint32_t seed, void* hits0, void* hits1, cudaStream_t s, uint32_t base = 0);
+// Adds the number of hit records with a primitive (prim != miss) among hits[0, n) to *count.
+cudaError_t launch_count_hits(bvhgpu_ctx* ctx, const void* hits, uint32_t n, uint32_t* count, cudaStream_t s);
 cudaError_t launch_bounce_rays(bvhgpu_ctx* ctx, const DeviceBlas& b, const float4* rays, const void* hits0,
                                uint32_t n, uint32_t seed, float4* out, uint8_t* valid, cudaStream_t s);
 cudaError_t launch_trace_batch(bvhgpu_ctx* ctx, const std::vector<const DeviceBlas*>& blases,

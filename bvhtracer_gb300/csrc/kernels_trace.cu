@@ -144,7 +144,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_trace_blas(GBlas b, const float
 __global__ void __launch_bounds__(kBlock) k_bounce_gen(GBlas b, const float4* __restrict__ rays,
                                                        const GHit* __restrict__ hits0, uint32_t n, uint32_t seed,
                                                        float4* __restrict__ queue_rays, uint32_t* __restrict__ queue_pix,
-                                                       uint32_t* queue_count, GHit* __restrict__ hits1) {
+                                                       uint32_t* queue_count, GHit* __restrict__ hits1, uint32_t key0) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     bool have = false;
     float3 po = make_float3(0, 0, 0), pd = make_float3(0, 0, 0);
@@ -156,7 +156,7 @@ __global__ void __launch_bounds__(kBlock) k_bounce_gen(GBlas b, const float4* __
             float t0;
             load_ray(rays, i, o, d, t0);
             const float4* T = b.tris + 3ull * h.prim;
-            have = bounce_dir(o, d, h.t, __ldg(T), __ldg(T + 1), __ldg(T + 2), seed, i, po, pd);
+            have = bounce_dir(o, d, h.t, __ldg(T), __ldg(T + 1), __ldg(T + 2), seed, key0 + i, po, pd);
         }
     }
     unsigned mask = __ballot_sync(kFull, have);
@@ -194,6 +194,13 @@ __global__ void k_bounce_rays(GBlas b, const float4* __restrict__ rays, const GH
     valid[i] = have ? 1 : 0;
 }
 
+// Hit records with a primitive among hits[0, n), one atomicAdd per warp.
+__global__ void k_count_hits(const GHit* __restrict__ hits, uint32_t n, uint32_t* count) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned m = __ballot_sync(kFull, i < n && hits[i].prim != kMiss);
+    if ((threadIdx.x & 31u) == 0u && m) atomicAdd(count, (uint32_t)__popc(m));
+}
+
 // ---- persistent: primary + bounce in one launch -------------------------------------------
 // Each warp keeps 32 ray slots.  A slot whose ray finished is refilled from the global queue
 // (ballot -> one atomicAdd per warp -> shfl); a primary that hit continues in the same slot
@@ -206,7 +213,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_persistent_bounce(GBlas b, cons
                                                                    uint32_t n, uint32_t seed,
                                                                    GHit* __restrict__ hits0, GHit* __restrict__ hits1,
                                                                    uint32_t* queue, LeafPolicy pol, uint32_t refill,
-                                                                   uint32_t* err) {
+                                                                   uint32_t key0, uint32_t* err) {
     extern __shared__ uint2 stack_smem[];
     const unsigned lane = threadIdx.x & 31u;
     if (refill >= 32u) {
@@ -232,7 +239,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_persistent_bounce(GBlas b, cons
             bool have = false;
             if (h) {
                 const float4* T = b.tris + 3ull * r.hp;
-                have = bounce_dir(r.o, r.d, r.ct, __ldg(T), __ldg(T + 1), __ldg(T + 2), seed, my, po, pd);
+                have = bounce_dir(r.o, r.d, r.ct, __ldg(T), __ldg(T + 1), __ldg(T + 2), seed, key0 + my, po, pd);
             }
             if (active && !have) store_hit(hits1, my, false, 0, 0, 0, 0, 0);
             LaneRay r2;
@@ -289,7 +296,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_persistent_bounce(GBlas b, cons
             bool have = false;
             if (h) {
                 const float4* T = b.tris + 3ull * r.hp;
-                have = bounce_dir(r.o, r.d, r.ct, __ldg(T), __ldg(T + 1), __ldg(T + 2), seed, idx, po, pd);
+                have = bounce_dir(r.o, r.d, r.ct, __ldg(T), __ldg(T + 1), __ldg(T + 2), seed, key0 + idx, po, pd);
             }
             if (!have) {
                 store_hit(hits1, idx, false, 0, 0, 0, 0, 0);
@@ -636,7 +643,7 @@ cudaError_t launch_trace_blas(bvhgpu_ctx* ctx, const DeviceBlas& b, const float4
 }
 
 cudaError_t launch_bounce_plain(bvhgpu_ctx* ctx, const DeviceBlas& b, const float4* rays, uint32_t n, uint32_t seed,
-                                void* hits0, void* hits1, cudaStream_t s) {
+                                void* hits0, void* hits1, cudaStream_t s, uint32_t base) {
     if (n == 0) return cudaSuccess;
     cudaError_t e = launch_trace_blas(ctx, b, rays, n, hits0, s);
     if (e != cudaSuccess) return e;
@@ -648,7 +655,7 @@ cudaError_t launch_bounce_plain(bvhgpu_ctx* ctx, const DeviceBlas& b, const floa
         LaunchScope scope(ctx, BVHGPU_K_BOUNCE_GEN, s);
         k_bounce_gen<<<grid_for(n, kBlock), kBlock, 0, s>>>(g, rays, static_cast<const GHit*>(hits0), n, seed,
                                                             static_cast<float4*>(ctx->bounce_rays), ctx->bounce_pix,
-                                                            qcount, static_cast<GHit*>(hits1));
+                                                            qcount, static_cast<GHit*>(hits1), base);
         g_launches++;
     }
     e = cudaGetLastError();
@@ -664,7 +671,7 @@ cudaError_t launch_bounce_plain(bvhgpu_ctx* ctx, const DeviceBlas& b, const floa
 }
 
 cudaError_t launch_bounce_persistent(bvhgpu_ctx* ctx, const DeviceBlas& b, const float4* rays, uint32_t n,
-                                     uint32_t seed, void* hits0, void* hits1, cudaStream_t s) {
+                                     uint32_t seed, void* hits0, void* hits1, cudaStream_t s, uint32_t base) {
     if (n == 0) return cudaSuccess;
     uint32_t* queue = ctx->d_scratch + 2;
     cudaError_t e = cudaMemsetAsync(queue, 0, sizeof(uint32_t), s);
@@ -678,12 +685,20 @@ cudaError_t launch_bounce_persistent(bvhgpu_ctx* ctx, const DeviceBlas& b, const
         auto* k = k_persistent_bounce<SH::block, SH::minb, STK>;
         const size_t smem = stack_smem_bytes<STK>(SH::block);
         k<<<persistent_grid(ctx, k, SH::block, smem), SH::block, smem, s>>>(
-            g, rays, n, seed, static_cast<GHit*>(hits0), static_cast<GHit*>(hits1), queue, v.pol, v.refill,
+            g, rays, n, seed, static_cast<GHit*>(hits0), static_cast<GHit*>(hits1), queue, v.pol, v.refill, base,
             ctx->d_err);
         return cudaGetLastError();
     });
     g_launches++;
     return e;
+}
+
+cudaError_t launch_count_hits(bvhgpu_ctx* ctx, const void* hits, uint32_t n, uint32_t* count, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    LaunchScope scope(ctx, BVHGPU_K_OTHER, s);
+    k_count_hits<<<grid_for(n, 256), 256, 0, s>>>(static_cast<const GHit*>(hits), n, count);
+    g_launches++;
+    return cudaGetLastError();
 }
 
 cudaError_t launch_bounce_rays(bvhgpu_ctx* ctx, const DeviceBlas& b, const float4* rays, const void* hits0,

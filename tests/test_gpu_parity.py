@@ -159,6 +159,28 @@ def test_bounce_rays_and_hits(ctx):
         assert nb == int((ref0["prim"] != bt.MISS).sum())
 
 
+@pytest.mark.parametrize("mode", [bt.MODE_PLAIN, bt.MODE_PERSISTENT])
+def test_chunked_host_call_equals_one_device_launch(ctx, mode):
+    """bvhgpu_blas_trace_bounce runs large calls in chunks (copies overlapping the tracing): the
+    hits and bounce hits equal one device launch over all rays, and the bounce count is exact."""
+    tris, rays, _ = scenes.config1(seed=5, width=960, height=544)  # 522,240 rays: 2 chunks
+    tris, bvh = build(tris)
+    blas = ctx.upload_blas(bvh, tris)
+    n = len(rays)
+    pr = ctx.pinned((n,), bt.RAY)
+    pr.array[:] = rays
+    h0, h1, nb = blas.trace_bounce(pr.array, 77, mode)
+    d_rays = ctx.to_device(rays)
+    d0 = ctx.device_buffer(n * bt.HIT.itemsize)
+    d1 = ctx.device_buffer(n * bt.HIT.itemsize)
+    blas.trace_bounce_async(d_rays, n, 77, mode, d0, d1)
+    ctx.sync()
+    g0 = d0.download(np.zeros(n, bt.HIT))
+    g1 = d1.download(np.zeros(n, bt.HIT))
+    assert h0.tobytes() == g0.tobytes() and h1.tobytes() == g1.tobytes()
+    assert nb == int((g0["prim"] != bt.MISS).sum())
+
+
 def test_near_tie_rays_counted_and_identical(ctx):
     """The parity rule counts rays whose two nearest hits lie within 1e-5 relative in t apart.  The
     traversal keeps the reference's visit order and strict `<`, so even exact ties (duplicated
