@@ -322,7 +322,8 @@ int bvhgpu_create(bvhgpu_ctx** out, int device) {
     cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaMalloc(&ctx->d_err, sizeof(uint32_t)) != cudaSuccess ||
-        cudaMalloc(&ctx->d_scratch, 64 * sizeof(uint32_t)) != cudaSuccess) {
+        cudaMalloc(&ctx->d_scratch, 64 * sizeof(uint32_t)) != cudaSuccess ||
+        cudaMallocHost(&ctx->host_word, 64) != cudaSuccess) {
         delete ctx;
         return BVHGPU_ERR_CUDA;
     }
@@ -360,9 +361,7 @@ int bvhgpu_destroy(bvhgpu_ctx* ctx) {
     cudaFree(ctx->bounce_rays);
     cudaFree(ctx->bounce_pix);
     cudaFree(ctx->batch_table);
-    for (auto e : ctx->chunk_events) cudaEventDestroy(e);
-    if (ctx->copy_in) cudaStreamDestroy(ctx->copy_in);
-    if (ctx->copy_out) cudaStreamDestroy(ctx->copy_out);
+    cudaFreeHost(ctx->host_word);
     cudaStreamDestroy(ctx->stream);
     delete ctx;
     return BVHGPU_OK;
@@ -762,79 +761,35 @@ int bvhgpu_blas_trace_bounce_async(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhg
     return BVHGPU_OK;
 }
 
-// The host-buffer call runs in chunks so that copies overlap the tracing: chunk k's rays go up on
-// one copy stream while chunk k-1 is traced on the context's stream and chunk k-2's hit records
-// come down on another.  Bounce directions are keyed by the ray's index in the whole call, so
-// the result is the same as one launch over all rays.
-static int ensure_chunk_streams(bvhgpu_ctx* ctx, size_t nevents) {
-    if (!ctx->copy_in && cudaStreamCreateWithFlags(&ctx->copy_in, cudaStreamNonBlocking) != cudaSuccess)
-        return cuda_fail(ctx, cudaGetLastError(), "copy stream");
-    if (!ctx->copy_out && cudaStreamCreateWithFlags(&ctx->copy_out, cudaStreamNonBlocking) != cudaSuccess)
-        return cuda_fail(ctx, cudaGetLastError(), "copy stream");
-    while (ctx->chunk_events.size() < nevents) {
-        cudaEvent_t e;
-        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
-            return cuda_fail(ctx, cudaGetLastError(), "chunk event");
-        ctx->chunk_events.push_back(e);
-    }
-    return BVHGPU_OK;
-}
-
+// One upload, one launch, one download: on GB300 the host copies run at ~200 GB/s (0.8 ms for a
+// 1080p frame), while splitting the launch to overlap them costs more (each extra launch adds a
+// ramp-up and a tail of ~0.3-0.5 ms).  The bounce count is reduced on the device.
 int bvhgpu_blas_trace_bounce(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhgpu_ray* rays, uint32_t n, uint32_t seed,
                              int mode, bvhgpu_hit* hits0, bvhgpu_hit* hits1, uint32_t* n_bounce) {
     if (!ctx || (n && (!rays || !hits0 || !hits1))) return BVHGPU_ERR_INVALID_ARG;
-    if (ctx->capturing) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "trace_bounce: host buffers during capture");
     if (n == 0) {
         if (n_bounce) *n_bounce = 0;
         return BVHGPU_OK;
     }
-    DeviceBlas* b = find_blas(ctx, blas_id);
-    if (!b) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown BLAS %u", blas_id);
-    if (mode != BVHGPU_MODE_PLAIN && mode != BVHGPU_MODE_PERSISTENT)
-        return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown mode %d", mode);
-    const uint32_t nchunks = std::min<uint32_t>(8u, (n + 262143u) / 262144u);  // >= 256 k rays a chunk
-    const uint32_t csize = (((n + nchunks - 1) / nchunks) + 31u) & ~31u;
     int rc = ensure(ctx, &ctx->stage_in, &ctx->stage_in_bytes, 32ull * n);
     if (!rc) rc = ensure(ctx, &ctx->stage_out, &ctx->stage_out_bytes, 20ull * n);
     if (!rc) rc = ensure(ctx, &ctx->stage_out2, &ctx->stage_out2_bytes, 20ull * n);
-    if (!rc && mode == BVHGPU_MODE_PLAIN) rc = ensure_bounce(ctx, csize);
-    if (!rc) rc = ensure_chunk_streams(ctx, 2ull * nchunks);
     if (rc) return rc;
     uint32_t* d_count = ctx->d_scratch + 16;
-    char* d_in = static_cast<char*>(ctx->stage_in);
-    char* d_h0 = static_cast<char*>(ctx->stage_out);
-    char* d_h1 = static_cast<char*>(ctx->stage_out2);
+    CK(cudaMemcpyAsync(ctx->stage_in, rays, 32ull * n, cudaMemcpyHostToDevice, ctx->stream), "upload rays");
+    rc = bvhgpu_blas_trace_bounce_async(ctx, blas_id, static_cast<const bvhgpu_ray*>(ctx->stage_in), n, seed, mode,
+                                        static_cast<bvhgpu_hit*>(ctx->stage_out),
+                                        static_cast<bvhgpu_hit*>(ctx->stage_out2), nullptr);
+    if (rc) return rc;
     CK(cudaMemsetAsync(d_count, 0, sizeof(uint32_t), ctx->stream), "count");
-    for (uint32_t k = 0; k < nchunks; ++k) {
-        const uint32_t off = k * csize;
-        if (off >= n) break;
-        const uint32_t m = std::min(csize, n - off);
-        cudaEvent_t up = ctx->chunk_events[2 * k], traced = ctx->chunk_events[2 * k + 1];
-        CK(cudaMemcpyAsync(d_in + 32ull * off, rays + off, 32ull * m, cudaMemcpyHostToDevice, ctx->copy_in),
-           "upload rays");
-        CK(cudaEventRecord(up, ctx->copy_in), "event");
-        CK(cudaStreamWaitEvent(ctx->stream, up, 0), "event");
-        const float4* r = reinterpret_cast<const float4*>(d_in + 32ull * off);
-        if (mode == BVHGPU_MODE_PLAIN)
-            CK(launch_bounce_plain(ctx, *b, r, m, seed, d_h0 + 20ull * off, d_h1 + 20ull * off, ctx->stream, off),
-               "bounce (plain)");
-        else
-            CK(launch_bounce_persistent(ctx, *b, r, m, seed, d_h0 + 20ull * off, d_h1 + 20ull * off, ctx->stream, off),
-               "bounce (persistent)");
-        CK(launch_count_hits(ctx, d_h0 + 20ull * off, m, d_count, ctx->stream), "count");
-        CK(cudaEventRecord(traced, ctx->stream), "event");
-        CK(cudaStreamWaitEvent(ctx->copy_out, traced, 0), "event");
-        CK(cudaMemcpyAsync(hits0 + off, d_h0 + 20ull * off, 20ull * m, cudaMemcpyDeviceToHost, ctx->copy_out),
-           "download hits");
-        CK(cudaMemcpyAsync(hits1 + off, d_h1 + 20ull * off, 20ull * m, cudaMemcpyDeviceToHost, ctx->copy_out),
-           "download hits");
-    }
-    uint32_t count = 0;
-    CK(cudaMemcpyAsync(&count, d_count, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->copy_out), "count");
-    CK(cudaStreamSynchronize(ctx->copy_out), "download");
+    CK(launch_count_hits(ctx, ctx->stage_out, n, d_count, ctx->stream), "count");
+    CK(cudaMemcpyAsync(hits0, ctx->stage_out, 20ull * n, cudaMemcpyDeviceToHost, ctx->stream), "download hits");
+    CK(cudaMemcpyAsync(hits1, ctx->stage_out2, 20ull * n, cudaMemcpyDeviceToHost, ctx->stream), "download hits");
+    uint32_t* h_count = static_cast<uint32_t*>(ctx->host_word);
+    CK(cudaMemcpyAsync(h_count, d_count, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream), "count");
     rc = finish(ctx);
     if (rc) return rc;
-    if (n_bounce) *n_bounce = count;
+    if (n_bounce) *n_bounce = *h_count;
     return BVHGPU_OK;
 }
 

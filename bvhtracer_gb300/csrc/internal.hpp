@@ -84,8 +84,7 @@ struct ProfileRec {
 struct bvhgpu_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
-    cudaStream_t copy_in = nullptr, copy_out = nullptr;  // chunked host calls (created on first use)
-    std::vector<cudaEvent_t> chunk_events;
+    void* host_word = nullptr;  // 64 bytes of pinned host memory for small results
     uint32_t* d_err = nullptr;       // device error flags
     uint32_t* d_scratch = nullptr;   // small device scratch: queue counters etc. (64 words)
     void* l2_flush = nullptr;
@@ -158,7 +157,7 @@ struct LaunchScope {
 cudaError_t launch_trace_blas(bvhgpu_ctx* ctx, const DeviceBlas& b, const float4* rays, uint32_t n, void* hits,
                               cudaStream_t s);
 // `base`: index of the first ray in the caller's whole ray set (the bounce directions' random key is
-// the ray's index there, so a call split in chunks gives the same bounces).
+// the ray's index there, so a ray set traced in parts gives the same bounces).
 cudaError_t launch_bounce_plain(bvhgpu_ctx* ctx, const DeviceBlas& b, const float4* rays, uint32_t n, uint32_t seed,
                                 void* hits0, void* hits1, cudaStream_t s, uint32_t base = 0);
 cudaError_t launch_bounce_persistent(bvhgpu_ctx* ctx, const DeviceBlas& b, const float4* rays, uint32_t n,
