@@ -599,6 +599,24 @@ int bvhgpu_blas_hidden(bvhgpu_ctx* ctx, uint32_t blas_id, uint32_t* nodes, uint3
     return BVHGPU_OK;
 }
 
+int bvhgpu_blas_trace_counts(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhgpu_ray* d_rays, uint32_t n,
+                             bvhgpu_hit* d_hits, uint64_t counts[6]) {
+    if (!ctx || !counts || (n && (!d_rays || !d_hits))) return BVHGPU_ERR_INVALID_ARG;
+    if (ctx->capturing) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "trace_counts: not allowed during capture");
+    DeviceBlas* b = find_blas(ctx, blas_id);
+    if (!b) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown BLAS %u", blas_id);
+    unsigned long long* d_out = reinterpret_cast<unsigned long long*>(ctx->d_scratch + 32);  // 6 x u64
+    CK(cudaMemsetAsync(d_out, 0, 6 * sizeof(unsigned long long), ctx->stream), "counters");
+    CK(launch_trace_count(ctx, *b, reinterpret_cast<const float4*>(d_rays), n, d_hits, d_out, ctx->stream),
+       "trace (counting)");
+    unsigned long long h[6];
+    CK(cudaMemcpyAsync(h, d_out, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream), "counters");
+    const int rc = finish(ctx);
+    if (rc) return rc;
+    for (int k = 0; k < 6; ++k) counts[k] = h[k];
+    return BVHGPU_OK;
+}
+
 int bvhgpu_blas_update_vertices_async(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhgpu_triangle* d_tris,
                                       bvhgpu_stream s) {
     if (!ctx || !d_tris) return BVHGPU_ERR_INVALID_ARG;

@@ -437,12 +437,24 @@ __device__ __forceinline__ bool hidden_box(float4 lo, float4 hi, float3 rd, cons
     return box_live(l, h, d, lc, t_enter);
 }
 
-template <class STK>
+// Per-ray work counters of the counting traversal (TravT<..., true>): what the ray fetched.
+struct TraceCounts {
+    uint32_t ref_nodes;    // reference interior nodes (each loads its two children, 64 B)
+    uint32_t hid_nodes;    // hidden interior nodes (64 B)
+    uint32_t entries;      // hidden trees entered (the leaf's table entry, 32 B)
+    uint32_t hid_pairs;    // hidden pairs tested (80 B + 8 B slot indices)
+    uint32_t lane_tris;    // triangles of small reference leaves tested by the lane (48 B)
+    uint32_t coop_tris;    // triangles of big reference leaves tested by the warp (40 B a triangle)
+};
+
+template <class STK, bool COUNT = false>
 struct TravT {
+    static constexpr bool kCount = COUNT;
     STK stk;
     uint32_t cnt, first, steps, max_steps;
     LeafCull lc;  // the ray's margins in the hidden tree being walked
     bool held;    // the closest hit came from the reference leaf of that hidden tree
+    TraceCounts cn;
 
     __device__ __forceinline__ void init(const GBlas& b) {
         stk.clear();
@@ -451,6 +463,7 @@ struct TravT {
         steps = 0;
         max_steps = 2u * (b.nodes_used + b.ntris) + 16u;  // hidden nodes: fewer than ntris
         held = false;
+        if constexpr (COUNT) cn = TraceCounts{0u, 0u, 0u, 0u, 0u, 0u};
     }
 
     __device__ __forceinline__ bool pop() {
@@ -477,6 +490,7 @@ struct TravT {
     // (warp-cooperatively) and then calls pop().
     __device__ __forceinline__ StepResult leaf(const GBlas& b, LaneRay& r, LeafPolicy pol) {
         if (cnt & kHiddenLeaf) {
+            if constexpr (COUNT) cn.hid_pairs += cnt & ~kHiddenLeaf;
             if (test_hidden_leaf(b, first, cnt & ~kHiddenLeaf, r, held)) lc.thi = leaf_thi(lc, r.ct);
             return pop() ? kStepFinished : kStepContinue;
         }
@@ -489,6 +503,7 @@ struct TravT {
                 lc = leaf_cull(cull_ray_rd(r.o.x, r.o.y, r.o.z, r.d.x, r.d.y, r.d.z, r.rd.x, r.rd.y, r.rd.z),
                                __uint_as_float(e.y), __uint_as_float(e.z), r.ct, pol.max_duv, cone);
                 if (lc.on) {  // else: margins too wide for this ray, the leaf is tested in order
+                    if constexpr (COUNT) ++cn.entries;
                     held = false;
                     first = e.x;  // the hidden root is always an interior node
                     cnt = 0u;
@@ -497,6 +512,7 @@ struct TravT {
             }
         }
         if (cnt > pol.big_leaf) return kStepBigLeaf;
+        if constexpr (COUNT) cn.lane_tris += cnt;
         test_leaf_lane(b.tris, first, cnt, r);
         return pop() ? kStepFinished : kStepContinue;
     }
@@ -511,6 +527,9 @@ struct TravT {
         float4 r1 = __ldg(N + 3);
         float dl, dr;
         bool hl, hr, left_near;
+        if constexpr (COUNT) {
+            if (first >= b.nodes_used) ++cn.hid_nodes; else ++cn.ref_nodes;
+        }
         if (first >= b.nodes_used) {  // hidden children: any order is exact
             hl = hidden_box(l0, l1, r.rd, lc, dl);
             hr = hidden_box(r0, r1, r.rd, lc, dr);

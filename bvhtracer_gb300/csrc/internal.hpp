@@ -162,6 +162,9 @@ cudaError_t launch_bounce_plain(bvhgpu_ctx* ctx, const DeviceBlas& b, const floa
                                 void* hits0, void* hits1, cudaStream_t s, uint32_t base = 0);
 cudaError_t launch_bounce_persistent(bvhgpu_ctx* ctx, const DeviceBlas& b, const float4* rays, uint32_t n,
                                      uint32_t seed, void* hits0, void* hits1, cudaStream_t s, uint32_t base = 0);
+// The plain traversal with per-ray work counters summed into out[0..5] (TraceCounts order).
+cudaError_t launch_trace_count(bvhgpu_ctx* ctx, const DeviceBlas& b, const float4* rays, uint32_t n, void* hits,
+                               unsigned long long* out, cudaStream_t s);
 // Adds the number of hit records with a primitive (prim != miss) among hits[0, n) to *count.
 cudaError_t launch_count_hits(bvhgpu_ctx* ctx, const void* hits, uint32_t n, uint32_t* count, cudaStream_t s);
 cudaError_t launch_bounce_rays(bvhgpu_ctx* ctx, const DeviceBlas& b, const float4* rays, const void* hits0,

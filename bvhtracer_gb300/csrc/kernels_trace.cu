@@ -77,10 +77,16 @@ __device__ __forceinline__ void coop_leaf_phase(unsigned pend, const GBlas& blas
                 const int b = __ffs(group) - 1;
                 group &= group - 1u;
                 coop_leaf2(P, f, c, a, b, r);
-                if ((int)lane == a || (int)lane == b) st = tr.pop() ? kStepFinished : kStepContinue;
+                if ((int)lane == a || (int)lane == b) {
+                    if constexpr (TR::kCount) tr.cn.coop_tris += c;
+                    st = tr.pop() ? kStepFinished : kStepContinue;
+                }
             } else {
                 coop_leaf(P, f, c, a, r);
-                if ((int)lane == a) st = tr.pop() ? kStepFinished : kStepContinue;
+                if ((int)lane == a) {
+                    if constexpr (TR::kCount) tr.cn.coop_tris += c;
+                    st = tr.pop() ? kStepFinished : kStepContinue;
+                }
             }
         }
     }
@@ -137,6 +143,42 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_trace_blas(GBlas b, const float
     warp_trace<STK>(b, active, r, pol, err, stack_smem);
     // bvh.rs:295: a hit needs closest_ray.t < f32::MAX as well.
     if (active) store_hit(hits, out_index ? out_index[i] : i, r.hit && r.ct < FLT_MAX, r.ct, r.hu, r.hv, r.hp, 0u);
+}
+
+// The plain traversal with per-ray work counters (one variant: block 128, local stack), summed
+// over the launch into out[0..5] in TraceCounts order -- the bytes each ray fetched, for the
+// roofline.  Results are the same as k_trace_blas's.
+__global__ void __launch_bounds__(kBlock) k_trace_count(GBlas b, const float4* __restrict__ rays, uint32_t n,
+                                                        GHit* __restrict__ hits, LeafPolicy pol,
+                                                        unsigned long long* out, uint32_t* err) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (__all_sync(kFull, i >= n)) return;
+    const bool active = i < n;
+    LaneRay r;
+    if (active) {
+        float3 o, d;
+        float t;
+        load_ray(rays, i, o, d, t);
+        init_lane_ray(r, o, d, t);
+    }
+    TravT<LocalStack<256>, true> tr;
+    tr.init(b);
+    StepResult st = active ? kStepContinue : kStepFinished;
+    for (;;) {
+        if (st == kStepContinue) st = tr.template advance<true>(b, r, pol, err);
+        const unsigned pend = __ballot_sync(kFull, st == kStepBigLeaf);
+        if (pend == 0u) break;
+        coop_leaf_phase(pend, b, tr, r, st);
+    }
+    if (active) store_hit(hits, i, r.hit && r.ct < FLT_MAX, r.ct, r.hu, r.hv, r.hp, 0u);
+    if (!active) tr.cn = TraceCounts{0u, 0u, 0u, 0u, 0u, 0u};
+    const uint32_t v[6] = {tr.cn.ref_nodes, tr.cn.hid_nodes, tr.cn.entries, tr.cn.hid_pairs, tr.cn.lane_tris,
+                           tr.cn.coop_tris};
+    for (int k = 0; k < 6; ++k) {
+        unsigned long long s = v[k];
+        for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(kFull, s, off);
+        if ((threadIdx.x & 31u) == 0u && s) atomicAdd(out + k, s);
+    }
 }
 
 // Bounce generation with warp-aggregated compaction: one atomicAdd per warp appends the
@@ -691,6 +733,17 @@ cudaError_t launch_bounce_persistent(bvhgpu_ctx* ctx, const DeviceBlas& b, const
     });
     g_launches++;
     return e;
+}
+
+cudaError_t launch_trace_count(bvhgpu_ctx* ctx, const DeviceBlas& b, const float4* rays, uint32_t n, void* hits,
+                               unsigned long long* out, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    const Variant v = resolve(ctx->tune[BVHGPU_K_TRACE_BLAS], b.depth);
+    LaunchScope scope(ctx, BVHGPU_K_OTHER, s);
+    k_trace_count<<<grid_for(n, kBlock), kBlock, 0, s>>>(to_gblas(b), rays, n, static_cast<GHit*>(hits), v.pol, out,
+                                                         ctx->d_err);
+    g_launches++;
+    return cudaGetLastError();
 }
 
 cudaError_t launch_count_hits(bvhgpu_ctx* ctx, const void* hits, uint32_t n, uint32_t* count, cudaStream_t s) {

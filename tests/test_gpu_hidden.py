@@ -237,3 +237,23 @@ def test_large_triangles_far_camera_with_normal_cones(ctx, hidden):
         same(blas.intersect(rays), ref, f"cones, hidden {hidden}")
     finally:
         ctx.tune_set(bt.K_TRACE_BLAS, **saved)
+
+
+def test_trace_counts_measure_the_culled_work(ctx):
+    """The counting traversal returns the plain call's hits, and its counters show what the hidden
+    trees save: triangles tested per ray far below the reference's (the oracle's counters)."""
+    tris = scenes.displaced_icosphere(6, 0).triangles().copy()
+    bvh = bt.BvhBuilder().build_for(tris)
+    blas = ctx.upload_blas(bvh, tris)
+    rays = scenes.look_at_rays(256, 192, (0, 0, -3.2), (0, 0, 0), 50.0)
+    n = len(rays)
+    d_rays = ctx.to_device(rays)
+    d_h = ctx.device_buffer(n * bt.HIT.itemsize)
+    c = blas.trace_counts(d_rays, n, d_h)
+    got = d_h.download(np.zeros(n, bt.HIT))
+    assert got.tobytes() == blas.intersect(rays).tobytes()
+    ref, cnt = orc.bvh_intersect(bvh.nodes, bvh.nodes_used, tris, rays, counters=True)
+    assert got.tobytes() == ref.tobytes()
+    assert c["ref_nodes"] == int(cnt["interior"].sum())  # the reference's own node visits
+    tested = 2 * c["hidden_pairs"] + c["lane_tris"] + c["warp_tris"]
+    assert c["hidden_entries"] > 0 and tested < 0.05 * int(cnt["tris"].sum())
