@@ -217,22 +217,13 @@ void pack_nodes(const bvhgpu_node* nodes, uint32_t n, std::vector<float>& out) {
     }
 }
 
-// Spreads the low 10 bits of x to every third bit (Morton interleave).
-uint32_t spread3(uint32_t x) {
-    x &= 0x3FFu;
-    x = (x | (x << 16)) & 0x030000FFu;
-    x = (x | (x << 8)) & 0x0300F00Fu;
-    x = (x | (x << 4)) & 0x030C30C3u;
-    x = (x | (x << 2)) & 0x09249249u;
-    return x;
-}
-
-// Hidden trees over the leaves with at least kHiddenMinLeaf triangles.  A leaf's triangles are put
-// in the Morton order of their centroids (10 bits per axis inside the leaf's box, ties by
-// triangle index) and split in halves (the left half rounded up to an even size) down to at most
-// kHiddenLeafTris triangles, which are stored as packed pairs (a padding slot is all zero with
-// index 0xFFFFFFFF).  Hidden nodes get indices from nodes_used on, children adjacent, allocated
-// depth first; the boxes and the leaf bounds Q, B are written by the refresh kernel from `work`.
+// Hidden trees over the leaves with at least kHiddenMinLeaf triangles, built by binned SAH: a node's
+// triangles are split at the cheapest of 15 planes (16 bins of the centroids along the widest
+// centroid axis, cost = area x count of each side), in halves by index order when the centroids
+// coincide or below depth 32, down to at most kHiddenLeafTris triangles stored as packed pairs (a padding slot is
+// all zero with index 0xFFFFFFFF).  Hidden nodes get indices from nodes_used on, children
+// adjacent, allocated depth first; the boxes and the leaf bounds Q, B and normal cone are written
+// by the refresh kernels from `work`.  Only speed depends on the tree's shape.
 struct HiddenPlan {
     std::vector<float> nodes;  // 8 floats per hidden node (boxes 0 until refreshed)
     std::vector<uint4> table;  // 2 per triangle index (empty: no hidden tree)
@@ -242,12 +233,90 @@ struct HiddenPlan {
 };
 constexpr uint32_t kWorkRoot = 0x80000000u;
 
+struct SahTri {
+    float c[3], lo[3], hi[3];
+};
+
+inline float half_area(const float lo[3], const float hi[3]) {
+    const float e0 = hi[0] - lo[0], e1 = hi[1] - lo[1], e2 = hi[2] - lo[2];
+    return e0 * e1 + e1 * e2 + e2 * e0;
+}
+
+// Reorders ids[a, b) into two non-empty parts by the binned SAH; returns the split position.
+uint32_t sah_split(std::vector<uint32_t>& ids, const std::vector<SahTri>& info, uint32_t a, uint32_t b) {
+    const uint32_t mid = a + (b - a) / 2;
+    float cl[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, ch[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    for (uint32_t j = a; j < b; ++j)
+        for (int k = 0; k < 3; ++k) {
+            cl[k] = std::min(cl[k], info[ids[j]].c[k]);
+            ch[k] = std::max(ch[k], info[ids[j]].c[k]);
+        }
+    int ax = 0;
+    for (int k = 1; k < 3; ++k)
+        if (ch[k] - cl[k] > ch[ax] - cl[ax]) ax = k;
+    const float ext = ch[ax] - cl[ax];
+    if (!(ext > 0.0f) || !(ext < FLT_MAX)) return mid;
+    constexpr int kBins = 16;
+    auto bin_of = [&](uint32_t id) {
+        const float x = (info[id].c[ax] - cl[ax]) / ext * (float)kBins;
+        return x >= 0.0f ? std::min(kBins - 1, (int)x) : 0;  // NaN -> 0
+    };
+    uint32_t cnt[kBins] = {};
+    float blo[kBins][3], bhi[kBins][3];
+    for (int i = 0; i < kBins; ++i)
+        for (int k = 0; k < 3; ++k) {
+            blo[i][k] = FLT_MAX;
+            bhi[i][k] = -FLT_MAX;
+        }
+    for (uint32_t j = a; j < b; ++j) {
+        const int i = bin_of(ids[j]);
+        ++cnt[i];
+        for (int k = 0; k < 3; ++k) {
+            blo[i][k] = std::min(blo[i][k], info[ids[j]].lo[k]);
+            bhi[i][k] = std::max(bhi[i][k], info[ids[j]].hi[k]);
+        }
+    }
+    float right_cost[kBins] = {};
+    float rlo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, rhi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    uint32_t rn = 0;
+    for (int i = kBins - 1; i > 0; --i) {  // right side = bins i..15
+        rn += cnt[i];
+        for (int k = 0; k < 3; ++k) {
+            rlo[k] = std::min(rlo[k], blo[i][k]);
+            rhi[k] = std::max(rhi[k], bhi[i][k]);
+        }
+        right_cost[i] = rn ? half_area(rlo, rhi) * (float)rn : 0.0f;
+    }
+    float llo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, lhi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    uint32_t ln = 0;
+    float best = FLT_MAX;
+    int best_bin = -1;  // left side = bins 0..best_bin
+    for (int i = 0; i < kBins - 1; ++i) {
+        ln += cnt[i];
+        for (int k = 0; k < 3; ++k) {
+            llo[k] = std::min(llo[k], blo[i][k]);
+            lhi[k] = std::max(lhi[k], bhi[i][k]);
+        }
+        if (ln == 0 || ln == b - a) continue;
+        const float cost = half_area(llo, lhi) * (float)ln + right_cost[i + 1];
+        if (cost < best) {
+            best = cost;
+            best_bin = i;
+        }
+    }
+    if (best_bin < 0) return mid;
+    auto it = std::stable_partition(ids.begin() + a, ids.begin() + b,
+                                    [&](uint32_t id) { return bin_of(id) <= best_bin; });
+    return (uint32_t)(it - ids.begin());
+}
+
 void plan_hidden(const bvhgpu_node* nodes, uint32_t nodes_used, const std::vector<uint32_t>& leaves,
                  const bvhgpu_triangle* tris, uint32_t ntris, HiddenPlan& hp) {
     const uint32_t P0 = pairs_in_order(ntris);
-    std::vector<std::pair<uint32_t, uint32_t>> keys;
+    std::vector<uint32_t> ids;
+    std::vector<SahTri> info;
     std::vector<uint4> roots;
-    // (first, count) of the subtree over keys[a, b); its pairs are allocated contiguously
+    // (first, count) of the subtree over ids[a, b); its pairs are allocated contiguously
     auto make = [&](auto&& self, uint32_t a, uint32_t b, uint32_t depth) -> uint2 {
         hp.depth = std::max(hp.depth, depth);
         if (b - a <= kHiddenLeafTris) {
@@ -255,12 +324,13 @@ void plan_hidden(const bvhgpu_node* nodes, uint32_t nodes_used, const std::vecto
             const uint32_t p0 = P0 + hp.nhp;
             for (uint32_t q = 0; q < np; ++q) {
                 const uint32_t s0 = a + 2 * q;
-                hp.slots.push_back(make_uint2(keys[s0].second, s0 + 1 < b ? keys[s0 + 1].second : kMiss));
+                hp.slots.push_back(make_uint2(ids[s0], s0 + 1 < b ? ids[s0 + 1] : kMiss));
             }
             hp.nhp += np;
             return make_uint2(p0, kHiddenLeaf | np);
         }
-        const uint32_t m = a + ((((b - a) / 2) + 1) & ~1u);
+        // SAH down to depth 32, then halves (a balanced rest keeps the stack need bounded)
+        const uint32_t m = depth < 32 ? sah_split(ids, info, a, b) : a + (b - a) / 2;
         const uint32_t li = hp.nhid;
         hp.nhid += 2;
         hp.nodes.resize(8ull * hp.nhid, 0.0f);
@@ -280,24 +350,23 @@ void plan_hidden(const bvhgpu_node* nodes, uint32_t nodes_used, const std::vecto
         hp.work[li + 1] = make_uint4(pm, pb, nodes_used + li + 1, 0u);
         return make_uint2(nodes_used + li, 0u);
     };
+    info.resize(ntris);
     for (uint32_t li : leaves) {
         const bvhgpu_node& n = nodes[li];
         if (n.primitive_count < kHiddenMinLeaf) continue;
         if (hp.table.empty()) hp.table.assign(2ull * ntris, make_uint4(0u, 0u, 0u, 0u));
-        keys.clear();
+        ids.resize(n.primitive_count);
         for (uint32_t k = 0; k < n.primitive_count; ++k) {
-            const float* v = tris[n.left_first + k].vertices;
-            uint32_t code = 0;
+            const uint32_t t = n.left_first + k;
+            const float* v = tris[t].vertices;
+            SahTri& s = info[t];
             for (int a = 0; a < 3; ++a) {
-                const float c = (v[a] + v[3 + a] + v[6 + a]) / 3.0f;
-                const float ext = n.bounds_max[a] - n.bounds_min[a];
-                const float x = ext > 0.0f ? (c - n.bounds_min[a]) / ext * 1024.0f : 0.0f;
-                const float q = std::min(1023.0f, std::max(0.0f, x));  // NaN -> 0
-                code |= spread3((uint32_t)q) << a;
+                s.c[a] = (v[a] + v[3 + a] + v[6 + a]) / 3.0f;
+                s.lo[a] = std::min(v[a], std::min(v[3 + a], v[6 + a]));
+                s.hi[a] = std::max(v[a], std::max(v[3 + a], v[6 + a]));
             }
-            keys.push_back({code, n.left_first + k});
+            ids[k] = t;
         }
-        std::sort(keys.begin(), keys.end());
         const uint32_t pa = P0 + hp.nhp;
         const uint2 root = make(make, 0, n.primitive_count, 0);
         hp.table[2ull * n.left_first] = make_uint4(root.x, 0u, 0u, 0u);  // root: interior (>= 16 triangles)
