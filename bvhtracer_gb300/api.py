@@ -397,11 +397,12 @@ class Blas:
                                                        ctypes.byref(d)))
         return {"nodes": n.value, "pairs": p.value, "depth": d.value}
 
-    TRACE_COUNT_NAMES = ("ref_nodes", "hidden_nodes", "hidden_entries", "hidden_pairs", "lane_tris", "warp_tris")
+    TRACE_COUNT_NAMES = ("ref_nodes", "hidden_nodes", "hidden_entries", "hidden_pairs", "lane_tris", "warp_tris",
+                         "cone_switches")
 
     def trace_counts(self, d_rays: "DeviceBuffer", n: int, d_hits: "DeviceBuffer") -> dict:
         """The plain traversal with work counters summed over the rays (bvhgpu_blas_trace_counts)."""
-        out = (ctypes.c_uint64 * 6)()
+        out = (ctypes.c_uint64 * 7)()
         self.ctx.check(self.ctx.lib.bvhgpu_blas_trace_counts(self.ctx.h, self.id, d_rays.ptr, n, d_hits.ptr, out))
         return {k: int(v) for k, v in zip(self.TRACE_COUNT_NAMES, out)}
 

@@ -127,6 +127,7 @@ void free_blas(DeviceBlas& b) {
     cudaFree(b.tri_leaf);
     cudaFree(b.leaf_keys);
     cudaFree(b.hx);
+    cudaFree(b.cones);
     cudaFree(b.hwork);
     b = DeviceBlas();
 }
@@ -226,12 +227,12 @@ void pack_nodes(const bvhgpu_node* nodes, uint32_t n, std::vector<float>& out) {
 // by the refresh kernels from `work`.  Only speed depends on the tree's shape.
 struct HiddenPlan {
     std::vector<float> nodes;  // 8 floats per hidden node (boxes 0 until refreshed)
-    std::vector<uint4> table;  // 2 per triangle index (empty: no hidden tree)
+    std::vector<uint2> table;  // per triangle index, rounded up to even (empty: no hidden tree)
     std::vector<uint2> slots;  // per hidden pair
-    std::vector<uint4> work;   // per hidden node, then per hidden root
-    uint32_t nhid = 0, nhp = 0, depth = 0;
+    std::vector<uint4> work;   // per hidden node (box), then per cone
+    uint32_t nhid = 0, nhp = 0, ncones = 0, depth = 0;
 };
-constexpr uint32_t kWorkRoot = 0x80000000u;
+constexpr uint32_t kNoWork = 0xFFFFFFFFu;
 
 struct SahTri {
     float c[3], lo[3], hi[3];
@@ -315,9 +316,10 @@ void plan_hidden(const bvhgpu_node* nodes, uint32_t nodes_used, const std::vecto
     const uint32_t P0 = pairs_in_order(ntris);
     std::vector<uint32_t> ids;
     std::vector<SahTri> info;
-    std::vector<uint4> roots;
-    // (first, count) of the subtree over ids[a, b); its pairs are allocated contiguously
-    auto make = [&](auto&& self, uint32_t a, uint32_t b, uint32_t depth) -> uint2 {
+    std::vector<uint4> cones;  // cone work: {first pair, end pair, ~0, cone}
+    // (first, count) of the subtree over ids[a, b) at `depth` below the hidden root; its pairs are
+    // allocated contiguously.  Nodes at even depth get their own cone, the others inherit `gov`.
+    auto make = [&](auto&& self, uint32_t a, uint32_t b, uint32_t depth, uint32_t gov) -> uint2 {
         hp.depth = std::max(hp.depth, depth);
         if (b - a <= kHiddenLeafTris) {
             const uint32_t np = (b - a + 1) / 2;
@@ -329,16 +331,18 @@ void plan_hidden(const bvhgpu_node* nodes, uint32_t nodes_used, const std::vecto
             hp.nhp += np;
             return make_uint2(p0, kHiddenLeaf | np);
         }
+        const uint32_t pa = P0 + hp.nhp;
+        const uint32_t own = (depth >= 2 && depth % 2 == 0) ? hp.ncones++ : kNoWork;
+        if (own != kNoWork) gov = own;
         // SAH down to depth 32, then halves (a balanced rest keeps the stack need bounded)
         const uint32_t m = depth < 32 ? sah_split(ids, info, a, b) : a + (b - a) / 2;
         const uint32_t li = hp.nhid;
         hp.nhid += 2;
         hp.nodes.resize(8ull * hp.nhid, 0.0f);
         hp.work.resize(hp.nhid);
-        const uint32_t pa = P0 + hp.nhp;
-        const uint2 L = self(self, a, m, depth + 1);
+        const uint2 L = self(self, a, m, depth + 1, gov);
         const uint32_t pm = P0 + hp.nhp;
-        const uint2 R = self(self, m, b, depth + 1);
+        const uint2 R = self(self, m, b, depth + 1, gov);
         const uint32_t pb = P0 + hp.nhp;
         const uint2 meta[2] = {L, R};
         for (int c = 0; c < 2; ++c) {
@@ -346,15 +350,16 @@ void plan_hidden(const bvhgpu_node* nodes, uint32_t nodes_used, const std::vecto
             std::memcpy(&o[3], &meta[c].x, 4);
             std::memcpy(&o[7], &meta[c].y, 4);
         }
-        hp.work[li] = make_uint4(pa, pm, nodes_used + li, 0u);
-        hp.work[li + 1] = make_uint4(pm, pb, nodes_used + li + 1, 0u);
-        return make_uint2(nodes_used + li, 0u);
+        hp.work[li] = make_uint4(pa, pm, nodes_used + li, kNoWork);
+        hp.work[li + 1] = make_uint4(pm, pb, nodes_used + li + 1, kNoWork);
+        if (own != kNoWork) cones.push_back(make_uint4(pa, pb, kNoWork, own));
+        return make_uint2(nodes_used + li, kHiddenInterior | gov);
     };
     info.resize(ntris);
     for (uint32_t li : leaves) {
         const bvhgpu_node& n = nodes[li];
         if (n.primitive_count < kHiddenMinLeaf) continue;
-        if (hp.table.empty()) hp.table.assign(2ull * ntris, make_uint4(0u, 0u, 0u, 0u));
+        if (hp.table.empty()) hp.table.assign(hidden_table_u2(ntris), make_uint2(0u, 0u));
         ids.resize(n.primitive_count);
         for (uint32_t k = 0; k < n.primitive_count; ++k) {
             const uint32_t t = n.left_first + k;
@@ -368,11 +373,12 @@ void plan_hidden(const bvhgpu_node* nodes, uint32_t nodes_used, const std::vecto
             ids[k] = t;
         }
         const uint32_t pa = P0 + hp.nhp;
-        const uint2 root = make(make, 0, n.primitive_count, 0);
-        hp.table[2ull * n.left_first] = make_uint4(root.x, 0u, 0u, 0u);  // root: interior (>= 16 triangles)
-        roots.push_back(make_uint4(pa, P0 + hp.nhp, kWorkRoot | n.left_first, 0u));
+        const uint32_t root_cone = hp.ncones++;
+        const uint2 root = make(make, 0, n.primitive_count, 0, root_cone);  // interior: >= 16 triangles
+        hp.table[n.left_first] = root;
+        cones.push_back(make_uint4(pa, P0 + hp.nhp, kNoWork, root_cone));
     }
-    hp.work.insert(hp.work.end(), roots.begin(), roots.end());
+    hp.work.insert(hp.work.end(), cones.begin(), cones.end());
 }
 
 }  // namespace
@@ -585,12 +591,13 @@ int bvhgpu_blas_upload(bvhgpu_ctx* ctx, const bvhgpu_node* nodes, uint32_t nodes
     plan_hidden(nodes, nodes_used, leaves, tris, ntris, hp);
     b.nhid = hp.nhid;
     b.nhp = hp.nhp;
+    b.ncones = hp.ncones;
     b.nwork = (uint32_t)hp.work.size();
     b.ref_depth = depth;
     b.depth = depth + hp.depth;
     const uint64_t nodes_all = (uint64_t)nodes_used + hp.nhid;
     const uint64_t pairs_all = (uint64_t)pairs_in_order(ntris) + hp.nhp;
-    const uint64_t hx_bytes = hp.table.empty() ? 0 : 32ull * ntris + 8ull * std::max<uint32_t>(1, hp.nhp);
+    const uint64_t hx_bytes = hp.table.empty() ? 0 : 8ull * hidden_table_u2(ntris) + 8ull * std::max<uint32_t>(1, hp.nhp);
     void* d_tris9 = nullptr;
     cudaError_t e = cudaSuccess;
     auto cleanup = [&]() {
@@ -608,6 +615,7 @@ int bvhgpu_blas_upload(bvhgpu_ctx* ctx, const bvhgpu_node* nodes, uint32_t nodes
         (e = cudaMalloc(&b.leaf_keys, 48ull * std::max<size_t>(1, leaves.size()))) != cudaSuccess ||
         (e = cudaMalloc(&d_tris9, 36ull * ntris)) != cudaSuccess ||
         (hx_bytes && (e = cudaMalloc(&b.hx, hx_bytes)) != cudaSuccess) ||
+        (b.ncones && (e = cudaMalloc(&b.cones, 32ull * b.ncones)) != cudaSuccess) ||
         (b.nwork && (e = cudaMalloc(&b.hwork, 16ull * b.nwork)) != cudaSuccess)) {
         cleanup();
         return fail(ctx, BVHGPU_ERR_OUT_OF_MEMORY, "blas_upload: %s", cudaGetErrorString(e));
@@ -622,9 +630,9 @@ int bvhgpu_blas_upload(bvhgpu_ctx* ctx, const bvhgpu_node* nodes, uint32_t nodes
         (e = cudaMemcpy(d_tris9, tris, 36ull * ntris, cudaMemcpyHostToDevice)) != cudaSuccess ||
         (hp.nhid && (e = cudaMemcpy(b.nodes + 2ull * nodes_used, hp.nodes.data(), 32ull * hp.nhid,
                                     cudaMemcpyHostToDevice)) != cudaSuccess) ||
-        (hx_bytes && (e = cudaMemcpy(b.hx, hp.table.data(), 32ull * ntris, cudaMemcpyHostToDevice)) != cudaSuccess) ||
+        (hx_bytes && (e = cudaMemcpy(b.hx, hp.table.data(), 8ull * hp.table.size(), cudaMemcpyHostToDevice)) != cudaSuccess) ||
         (hx_bytes && hp.nhp &&
-         (e = cudaMemcpy(b.hx + 2ull * ntris, hp.slots.data(), 8ull * hp.nhp, cudaMemcpyHostToDevice)) != cudaSuccess) ||
+         (e = cudaMemcpy(b.hx + hp.table.size(), hp.slots.data(), 8ull * hp.nhp, cudaMemcpyHostToDevice)) != cudaSuccess) ||
         (b.nwork && (e = cudaMemcpy(b.hwork, hp.work.data(), 16ull * b.nwork, cudaMemcpyHostToDevice)) != cudaSuccess) ||
         (e = launch_write_tris(ctx, b, static_cast<const float*>(d_tris9), ctx->stream)) != cudaSuccess ||
         (e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess) {
@@ -669,20 +677,20 @@ int bvhgpu_blas_hidden(bvhgpu_ctx* ctx, uint32_t blas_id, uint32_t* nodes, uint3
 }
 
 int bvhgpu_blas_trace_counts(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhgpu_ray* d_rays, uint32_t n,
-                             bvhgpu_hit* d_hits, uint64_t counts[6]) {
+                             bvhgpu_hit* d_hits, uint64_t counts[7]) {
     if (!ctx || !counts || (n && (!d_rays || !d_hits))) return BVHGPU_ERR_INVALID_ARG;
     if (ctx->capturing) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "trace_counts: not allowed during capture");
     DeviceBlas* b = find_blas(ctx, blas_id);
     if (!b) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown BLAS %u", blas_id);
-    unsigned long long* d_out = reinterpret_cast<unsigned long long*>(ctx->d_scratch + 32);  // 6 x u64
-    CK(cudaMemsetAsync(d_out, 0, 6 * sizeof(unsigned long long), ctx->stream), "counters");
+    unsigned long long* d_out = reinterpret_cast<unsigned long long*>(ctx->d_scratch + 32);  // 7 x u64
+    CK(cudaMemsetAsync(d_out, 0, 7 * sizeof(unsigned long long), ctx->stream), "counters");
     CK(launch_trace_count(ctx, *b, reinterpret_cast<const float4*>(d_rays), n, d_hits, d_out, ctx->stream),
        "trace (counting)");
-    unsigned long long h[6];
+    unsigned long long h[7];
     CK(cudaMemcpyAsync(h, d_out, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream), "counters");
     const int rc = finish(ctx);
     if (rc) return rc;
-    for (int k = 0; k < 6; ++k) counts[k] = h[k];
+    for (int k = 0; k < 7; ++k) counts[k] = h[k];
     return BVHGPU_OK;
 }
 
@@ -969,6 +977,7 @@ int bvhgpu_scene_create(bvhgpu_ctx* ctx, const uint32_t* blas_ids, uint32_t nobj
             g.tris = b->tris;
             g.pairs = b->pairs;
             g.hx = b->hx;
+            g.cones = b->cones;
             g.nodes_used = b->nodes_used;
             g.ntris = b->ntris;
             g.root_count = b->root_count;

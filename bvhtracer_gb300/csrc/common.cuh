@@ -31,14 +31,18 @@ struct GBlas {
     // Triangle pairs (2p, 2p+1) interleaved for packed f32x2 math: 20 floats per pair, component
     // c of {v0x v0y v0z e1x e1y e1z e2x e2y e2z} of triangle 2p + h at float 2c + h.
     const ulonglong2* pairs;
-    // Hidden trees of the large leaves (null when none): two uint4 per triangle index, read at a
-    // leaf's first triangle: {first child of the hidden root (0: no hidden tree), Q, B, nmin} and
-    // {cone axis xyz, cos_phi} (floats as bits, cull.cuh); then one uint2 per hidden pair
-    // p >= (ntris + 1) / 2: the triangle indices of its two slots (0xFFFFFFFF: padding).  Hidden nodes follow the reference's nodes_used nodes
-    // in `nodes` (a node whose children start at or beyond nodes_used is hidden); a hidden leaf has
-    // count = kHiddenLeaf | pairs and first = its first pair in `pairs`, after the (ntris + 1) / 2
-    // pairs in triangle order.
-    const uint4* hx;
+    // Hidden trees of the large leaves (null when none): one uint2 per triangle index (rounded up
+    // to even), read at a leaf's first triangle, {first, count} of the hidden root ({0, 0}: no
+    // hidden tree); then one uint2 per hidden pair p >= (ntris + 1) / 2: the triangle indices of
+    // its two slots (0xFFFFFFFF: padding).  Hidden nodes follow the reference's nodes_used nodes in
+    // `nodes` (a node whose children start at or beyond nodes_used is hidden): an interior one has
+    // count = kHiddenInterior | its cone, a leaf count = kHiddenLeaf | pairs and first = its first
+    // pair in `pairs`, after the (ntris + 1) / 2 pairs in triangle order.
+    const uint2* hx;
+    // Cone records of the hidden trees, 2 float4 each: {axis xyz, cos_phi}, {sin_phi, nmin, Q, B}
+    // (cull.cuh) -- one per hidden root and per hidden node at even depth; an interior hidden
+    // node's cone covers all its triangles.
+    const float4* cones;
     uint32_t nodes_used;
     uint32_t ntris;
     uint32_t root_count;  // root node meta (node 0)
@@ -46,6 +50,12 @@ struct GBlas {
 };
 
 constexpr uint32_t kHiddenLeaf = 0x80000000u;
+constexpr uint32_t kHiddenInterior = 0x40000000u;
+constexpr uint32_t kConeMask = 0x3FFFFFFFu;
+
+// Interior: a reference branch (count 0) or a hidden one (kHiddenInterior | cone).
+__host__ __device__ __forceinline__ bool node_interior(uint32_t cnt) { return cnt == 0u || (cnt >> 30) == 1u; }
+__host__ __device__ __forceinline__ uint32_t hidden_table_u2(uint32_t ntris) { return (ntris + 1u) & ~1u; }
 // Reference leaves with at least this many triangles get a hidden tree, whose leaves hold at most
 // kHiddenLeafTris triangles (two packed pairs).
 constexpr uint32_t kHiddenMinLeaf = 16;
@@ -387,7 +397,7 @@ struct LocalStack {
 // while the held hit came from the same reference leaf (`held`): the reference's in-order leaf loop
 // keeps the lowest index among equal t, and a hit from an earlier leaf keeps equal t out.
 __device__ __forceinline__ bool test_hidden_leaf(const GBlas& b, uint32_t first, uint32_t np, LaneRay& r, bool& held) {
-    const uint2* hidx = reinterpret_cast<const uint2*>(b.hx + 2ull * b.ntris) - pairs_in_order(b.ntris);
+    const uint2* hidx = b.hx + hidden_table_u2(b.ntris) - pairs_in_order(b.ntris);
     const f2 OX = f2_pack(r.o.x, r.o.x), OY = f2_pack(r.o.y, r.o.y), OZ = f2_pack(r.o.z, r.o.z);
     const f2 DX = f2_pack(r.d.x, r.d.x), DY = f2_pack(r.d.y, r.d.y), DZ = f2_pack(r.d.z, r.d.z);
     const f2 Z = f2_neg_zero();
@@ -445,6 +455,7 @@ struct TraceCounts {
     uint32_t hid_pairs;    // hidden pairs tested (80 B + 8 B slot indices)
     uint32_t lane_tris;    // triangles of small reference leaves tested by the lane (48 B)
     uint32_t coop_tris;    // triangles of big reference leaves tested by the warp (40 B a triangle)
+    uint32_t cone_switches;  // margins recomputed for another cone (2 x 16 B cone record)
 };
 
 template <class STK, bool COUNT = false>
@@ -452,8 +463,10 @@ struct TravT {
     static constexpr bool kCount = COUNT;
     STK stk;
     uint32_t cnt, first, steps, max_steps;
-    LeafCull lc;  // the ray's margins in the hidden tree being walked
-    bool held;    // the closest hit came from the reference leaf of that hidden tree
+    LeafCull lc;         // the ray's margins in the hidden tree being walked, valid below cone `lcone`
+    uint32_t lcone;      // the cone lc was computed for
+    uint32_t leaf_cone;  // the hidden tree's root cone (its margins hold everywhere in the tree)
+    bool held;           // the closest hit came from the reference leaf of that hidden tree
     TraceCounts cn;
 
     __device__ __forceinline__ void init(const GBlas& b) {
@@ -463,7 +476,7 @@ struct TravT {
         steps = 0;
         max_steps = 2u * (b.nodes_used + b.ntris) + 16u;  // hidden nodes: fewer than ntris
         held = false;
-        if constexpr (COUNT) cn = TraceCounts{0u, 0u, 0u, 0u, 0u, 0u};
+        if constexpr (COUNT) cn = TraceCounts{0u, 0u, 0u, 0u, 0u, 0u, 0u};
     }
 
     __device__ __forceinline__ bool pop() {
@@ -483,7 +496,7 @@ struct TravT {
         return true;
     }
 
-    // A leaf node (cnt > 0).  A hidden leaf is tested by the lane.  A reference leaf with a hidden
+    // A leaf node (!node_interior(cnt)).  A hidden leaf is tested by the lane.  A reference leaf with a hidden
     // tree continues at the tree's root when the ray's margins (computed here) are narrow enough to
     // cull; other reference leaves with more than `pol.big_leaf` triangles are not tested here: the
     // step returns kStepBigLeaf with (first, cnt) describing the leaf, and the caller tests it
@@ -495,18 +508,16 @@ struct TravT {
             return pop() ? kStepFinished : kStepContinue;
         }
         if (b.hx != nullptr) {
-            const uint4 e = __ldg(b.hx + 2ull * first);
+            const uint2 e = __ldg(b.hx + first);
             if (e.x != 0u) {
-                const uint4 c = __ldg(b.hx + 2ull * first + 1);
-                const LeafCone cone = {__uint_as_float(c.x), __uint_as_float(c.y), __uint_as_float(c.z),
-                                       __uint_as_float(c.w), __uint_as_float(e.w)};
-                lc = leaf_cull(cull_ray_rd(r.o.x, r.o.y, r.o.z, r.d.x, r.d.y, r.d.z, r.rd.x, r.rd.y, r.rd.z),
-                               __uint_as_float(e.y), __uint_as_float(e.z), r.ct, pol.max_duv, cone);
+                const uint32_t c = e.y & kConeMask;
+                lc = cone_cull(b, r, c, pol);
                 if (lc.on) {  // else: margins too wide for this ray, the leaf is tested in order
                     if constexpr (COUNT) ++cn.entries;
                     held = false;
+                    lcone = leaf_cone = c;
                     first = e.x;  // the hidden root is always an interior node
-                    cnt = 0u;
+                    cnt = e.y;
                     return kStepContinue;
                 }
             }
@@ -517,9 +528,16 @@ struct TravT {
         return pop() ? kStepFinished : kStepContinue;
     }
 
-    // An interior node (cnt == 0): its children's boxes -- the reference's slab test for reference
+    // An interior node (node_interior(cnt)): its children's boxes -- the reference's slab test for reference
     // nodes, the margins' exact cull for hidden ones -- then the near child, the far one pushed.
-    __device__ __forceinline__ StepResult interior(const GBlas& b, LaneRay& r, uint32_t* err) {
+    __device__ __forceinline__ StepResult interior(const GBlas& b, LaneRay& r, LeafPolicy pol, uint32_t* err) {
+        if (first >= b.nodes_used && (cnt & kConeMask) != lcone) {
+            // a subtree under another cone: its own (tighter) margins, else the tree's root cone's
+            lcone = cnt & kConeMask;
+            lc = cone_cull(b, r, lcone, pol);
+            if (!lc.on) lc = cone_cull(b, r, leaf_cone, pol);
+            if constexpr (COUNT) ++cn.cone_switches;
+        }
         const float4* N = b.nodes + 2ull * first;
         float4 l0 = __ldg(N);
         float4 l1 = __ldg(N + 1);
@@ -562,10 +580,18 @@ struct TravT {
         return false;
     }
 
+    // The ray's margins under cone record c (its Q, B, normal cone), thi from the closest t.
+    __device__ __forceinline__ LeafCull cone_cull(const GBlas& b, const LaneRay& r, uint32_t c, LeafPolicy pol) const {
+        const float4 a = __ldg(b.cones + 2ull * c), q = __ldg(b.cones + 2ull * c + 1);
+        const LeafCone cone = {a.x, a.y, a.z, a.w, q.x, q.y};
+        return leaf_cull(cull_ray_rd(r.o.x, r.o.y, r.o.z, r.d.x, r.d.y, r.d.z, r.rd.x, r.rd.y, r.rd.z), q.z, q.w, r.ct,
+                         pol.max_duv, cone);
+    }
+
     // Processes one node.
     __device__ __forceinline__ StepResult step(const GBlas& b, LaneRay& r, LeafPolicy pol, uint32_t* err) {
         if (over_cap(err)) return kStepFinished;
-        return cnt > 0 ? leaf(b, r, pol) : interior(b, r, err);
+        return node_interior(cnt) ? interior(b, r, pol, err) : leaf(b, r, pol);
     }
 
     // Steps until the lane finishes or stops at a big leaf.  GROUPED: interior nodes in an inner
@@ -576,9 +602,9 @@ struct TravT {
     __device__ __forceinline__ StepResult advance(const GBlas& b, LaneRay& r, LeafPolicy pol, uint32_t* err) {
         if (GROUPED) {
             for (;;) {
-                while (cnt == 0) {
+                while (node_interior(cnt)) {
                     if (over_cap(err)) return kStepFinished;
-                    const StepResult s = interior(b, r, err);
+                    const StepResult s = interior(b, r, pol, err);
                     if (s != kStepContinue) return s;
                 }
                 if (over_cap(err)) return kStepFinished;

@@ -136,11 +136,16 @@ BVHGPU_HD CullRay cull_ray(float ox, float oy, float oz, float dx, float dy, flo
     return cull_ray_rd(ox, oy, oz, dx, dy, dz, 1.0f / dx, 1.0f / dy, 1.0f / dz);
 }
 
-// The normal cone of a leaf's triangles (see above); nmin = 0 or cos_phi <= 0: none.
+// The normal cone of a group of triangles (see above); nmin = 0 or cos_phi <= 0: none.  sin_phi is
+// an upper bound of sqrt(1 - cos_phi^2) (cone_sin).
 struct LeafCone {
     float ax, ay, az;
-    float cos_phi, nmin;
+    float cos_phi, sin_phi, nmin;
 };
+
+BVHGPU_HD float cone_sin(float cos_phi) {
+    return sqrtf(cull_fmax(0.0f, 1.0f - cos_phi * cos_phi * (1.0f - 4.0f * kCullUnit))) * (1.0f + 4.0f * kCullUnit);
+}
 
 // One triangle's contribution to a cone around axis (ax, ay, az): a lower bound of
 // |N . A| / (|N| |A|) and of |N| for the exact N = e1 x e2, from the float edges.
@@ -172,7 +177,7 @@ BVHGPU_HD void cone_terms(const float e1[3], const float e2[3], float ax, float 
 // A lower bound of |d . N_k| for every triangle of a leaf with cone c (0 when it gives none).
 BVHGPU_HD float cone_det_lo(const float d[3], const LeafCone& c) {
     const float u0 = kCullUnit;
-    if (!(c.nmin > 0.0f) || !(c.cos_phi > 0.0f) || !(c.cos_phi <= 1.0f)) return 0.0f;
+    if (!(c.nmin > 0.0f) || !(c.cos_phi > 0.0f) || !(c.cos_phi <= 1.0f) || !(c.sin_phi >= 0.0f)) return 0.0f;
     const float a = d[0] * c.ax + d[1] * c.ay + d[2] * c.az;
     const float a_err = 4.0f * u0 * (cull_abs(d[0] * c.ax) + cull_abs(d[1] * c.ay) + cull_abs(d[2] * c.az));
     const float dd = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
@@ -181,7 +186,7 @@ BVHGPU_HD float cone_det_lo(const float d[3], const LeafCone& c) {
     const float cos_t = (cull_abs(a) - a_err) / (dlen * alen * (1.0f + 8.0f * u0)) * (1.0f - 4.0f * u0);
     if (!(cos_t > 0.0f)) return 0.0f;
     const float sin_t = sqrtf(cull_fmax(0.0f, 1.0f - cos_t * cos_t * (1.0f - 4.0f * u0))) * (1.0f + 4.0f * u0);
-    const float sin_p = sqrtf(cull_fmax(0.0f, 1.0f - c.cos_phi * c.cos_phi * (1.0f - 4.0f * u0))) * (1.0f + 4.0f * u0);
+    const float sin_p = c.sin_phi;
     const float cs = (cos_t * c.cos_phi * (1.0f - 4.0f * u0) - sin_t * sin_p * (1.0f + 4.0f * u0)) * (1.0f - 4.0f * u0);
     if (!(cs > 0.0f)) return 0.0f;
     const float lo = c.nmin * dlen * (1.0f - 4.0f * u0) * cs * (1.0f - 64.0f * u0);

@@ -26,11 +26,13 @@ struct DeviceBlas {
     uint32_t* counters = nullptr;// refit arrival counters, one per node (kept zeroed)
     uint32_t* tri_leaf = nullptr;        // leaf slot (index into `leaves`) of each triangle, or none
     unsigned long long* leaf_keys = nullptr;  // refit reduction keys, 6 per leaf (kept at identity)
-    uint4* hx = nullptr;         // hidden-tree table and pair slots (GBlas::hx), or null
-    uint4* hwork = nullptr;      // refresh work: {first pair, end pair, node index | table index + flag, 0}
+    uint2* hx = nullptr;         // hidden-tree table and pair slots (GBlas::hx), or null
+    float4* cones = nullptr;     // hidden-tree cone records (GBlas::cones)
+    uint32_t ncones = 0;
+    uint4* hwork = nullptr;      // refresh work: {first pair, end pair, node index or ~0, cone index or ~0}
     uint32_t nhid = 0;           // hidden nodes (after the nodes_used reference nodes)
     uint32_t nhp = 0;            // hidden pairs (after the (ntris + 1) / 2 pairs in triangle order)
-    uint32_t nwork = 0;          // hidden nodes + hidden roots
+    uint32_t nwork = 0;          // hidden nodes + cones
     uint32_t ref_depth = 0;      // depth of the reference tree (depth adds the hidden trees')
     uint32_t nodes_used = 0;
     uint32_t ntris = 0;
@@ -162,7 +164,7 @@ cudaError_t launch_bounce_plain(bvhgpu_ctx* ctx, const DeviceBlas& b, const floa
                                 void* hits0, void* hits1, cudaStream_t s, uint32_t base = 0);
 cudaError_t launch_bounce_persistent(bvhgpu_ctx* ctx, const DeviceBlas& b, const float4* rays, uint32_t n,
                                      uint32_t seed, void* hits0, void* hits1, cudaStream_t s, uint32_t base = 0);
-// The plain traversal with per-ray work counters summed into out[0..5] (TraceCounts order).
+// The plain traversal with per-ray work counters summed into out[0..6] (TraceCounts order).
 cudaError_t launch_trace_count(bvhgpu_ctx* ctx, const DeviceBlas& b, const float4* rays, uint32_t n, void* hits,
                                unsigned long long* out, cudaStream_t s);
 // Adds the number of hit records with a primitive (prim != miss) among hits[0, n) to *count.

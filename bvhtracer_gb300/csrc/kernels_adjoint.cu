@@ -35,6 +35,7 @@ inline GBlas to_gblas(const DeviceBlas& b) {
     g.tris = b.tris;
     g.pairs = b.pairs;
     g.hx = b.hx;
+    g.cones = b.cones;
     g.nodes_used = b.nodes_used;
     g.ntris = b.ntris;
     g.root_count = b.root_count;

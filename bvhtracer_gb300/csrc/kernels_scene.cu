@@ -49,8 +49,8 @@ __global__ void k_write_tris(const float* __restrict__ tris9, uint32_t n, float4
 
 // ---- hidden trees of the large leaves, refreshed after every triangle write -----------------
 // Hidden pairs: the triangles of each pair's two slots (membership fixed at upload) copied into the
-// packed layout.  Then one warp per hidden node (and per hidden root): the widened box of the
-// node's pairs and, for a root, the leaf's bounds Q, B and normal cone (cull.cuh).
+// packed layout.  Then one warp per hidden node and per cone record: the widened box of the
+// node's pairs, or for a cone record the bounds Q, B and the normal cone of its pairs (cull.cuh).
 __global__ void k_hidden_pairs(const float4* __restrict__ tris, const uint2* __restrict__ slots, uint32_t nhp,
                                float* __restrict__ pairs) {
     const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -73,7 +73,7 @@ __global__ void k_hidden_pairs(const float4* __restrict__ tris, const uint2* __r
 
 __global__ void k_hidden_boxes(const uint4* __restrict__ work, uint32_t nwork, const float* __restrict__ pairs,
                                const uint2* __restrict__ slots, uint32_t p0, float4* __restrict__ nodes,
-                               uint4* __restrict__ table) {
+                               float4* __restrict__ cones) {
     const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const unsigned lane = threadIdx.x & 31u;
     if (w >= nwork) return;  // whole warps leave together
@@ -107,7 +107,7 @@ __global__ void k_hidden_boxes(const uint4* __restrict__ work, uint32_t nwork, c
     }
     finite = __all_sync(0xFFFFFFFFu, finite);
     const GroupSeal g = group_seal(lo, hi, e1m, e2m, finite);
-    if (!(job.z & 0x80000000u)) {
+    if (job.z != 0xFFFFFFFFu) {  // a node's box
         if (lane == 0) {
             float4* N = nodes + 2ull * job.z;
             N[0] = make_float4(g.lo[0], g.lo[1], g.lo[2], N[0].w);
@@ -115,8 +115,8 @@ __global__ void k_hidden_boxes(const uint4* __restrict__ work, uint32_t nwork, c
         }
         return;
     }
-    // a hidden root: the leaf's Q, B and the cone of its normal lines (any axis is valid; the sum
-    // of unit normals, each turned towards the first triangle's, makes it narrow)
+    // a cone record: Q, B and the cone of the normal lines (any axis is valid; the sum of unit
+    // normals, each turned towards the first triangle's, makes it narrow)
     float rx = 0.0f, ry = 0.0f, rz = 0.0f;
     if (lane == 0) {
         for (uint32_t p = job.x; p < job.y; ++p) {
@@ -178,12 +178,9 @@ __global__ void k_hidden_boxes(const uint4* __restrict__ work, uint32_t nwork, c
     if (lane != 0) return;
     const bool cone_ok = isfinite(sx) && isfinite(sy) && isfinite(sz) && cmin > 0.0f && cmin <= 1.0f &&
                          nmin > 0.0f && nmin < FLT_MAX;
-    uint4* e = table + 2ull * (job.z & 0x7FFFFFFFu);
-    e[0].y = __float_as_uint(g.q);
-    e[0].z = __float_as_uint(g.b);
-    e[0].w = __float_as_uint(cone_ok ? nmin : 0.0f);
-    e[1] = make_uint4(__float_as_uint(cone_ok ? sx : 0.0f), __float_as_uint(cone_ok ? sy : 0.0f),
-                      __float_as_uint(cone_ok ? sz : 0.0f), __float_as_uint(cone_ok ? cmin : -1.0f));
+    float4* C = cones + 2ull * job.w;
+    C[0] = make_float4(cone_ok ? sx : 0.0f, cone_ok ? sy : 0.0f, cone_ok ? sz : 0.0f, cone_ok ? cmin : -1.0f);
+    C[1] = make_float4(cone_ok ? cone_sin(cmin) : 1.0f, cone_ok ? nmin : 0.0f, g.q, g.b);
 }
 
 // ---- refit, parallel over triangles --------------------------------------------------------
@@ -587,6 +584,7 @@ struct SceneTrav {
         blas.tris = nullptr;
         blas.pairs = nullptr;
         blas.hx = nullptr;
+        blas.cones = nullptr;
         blas.nodes_used = blas.ntris = blas.root_count = blas.root_first = 0;
     }
 
@@ -926,10 +924,10 @@ cudaError_t launch_hidden_refresh(bvhgpu_ctx* ctx, DeviceBlas& b, cudaStream_t s
     if (b.nwork == 0) return cudaSuccess;
     LaunchScope scope(ctx, BVHGPU_K_OTHER, s);
     const uint32_t p0 = pairs_in_order(b.ntris);
-    const uint2* slots = reinterpret_cast<const uint2*>(b.hx + 2ull * b.ntris);
+    const uint2* slots = b.hx + hidden_table_u2(b.ntris);
     float* pairs = reinterpret_cast<float*>(b.pairs);
     k_hidden_pairs<<<grid_for(b.nhp, 256), 256, 0, s>>>(b.tris, slots, b.nhp, pairs + 20ull * p0);
-    k_hidden_boxes<<<grid_for(32u * b.nwork, 128), 128, 0, s>>>(b.hwork, b.nwork, pairs, slots, p0, b.nodes, b.hx);
+    k_hidden_boxes<<<grid_for(32u * b.nwork, 128), 128, 0, s>>>(b.hwork, b.nwork, pairs, slots, p0, b.nodes, b.cones);
     g_launches += 2;
     return cudaGetLastError();
 }

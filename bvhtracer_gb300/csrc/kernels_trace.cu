@@ -31,6 +31,7 @@ inline GBlas to_gblas(const DeviceBlas& b) {
     g.tris = b.tris;
     g.pairs = b.pairs;
     g.hx = b.hx;
+    g.cones = b.cones;
     g.nodes_used = b.nodes_used;
     g.ntris = b.ntris;
     g.root_count = b.root_count;
@@ -146,7 +147,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_trace_blas(GBlas b, const float
 }
 
 // The plain traversal with per-ray work counters (one variant: block 128, local stack), summed
-// over the launch into out[0..5] in TraceCounts order -- the bytes each ray fetched, for the
+// over the launch into out[0..6] in TraceCounts order -- the bytes each ray fetched, for the
 // roofline.  Results are the same as k_trace_blas's.
 __global__ void __launch_bounds__(kBlock) k_trace_count(GBlas b, const float4* __restrict__ rays, uint32_t n,
                                                         GHit* __restrict__ hits, LeafPolicy pol,
@@ -171,10 +172,10 @@ __global__ void __launch_bounds__(kBlock) k_trace_count(GBlas b, const float4* _
         coop_leaf_phase(pend, b, tr, r, st);
     }
     if (active) store_hit(hits, i, r.hit && r.ct < FLT_MAX, r.ct, r.hu, r.hv, r.hp, 0u);
-    if (!active) tr.cn = TraceCounts{0u, 0u, 0u, 0u, 0u, 0u};
-    const uint32_t v[6] = {tr.cn.ref_nodes, tr.cn.hid_nodes, tr.cn.entries, tr.cn.hid_pairs, tr.cn.lane_tris,
-                           tr.cn.coop_tris};
-    for (int k = 0; k < 6; ++k) {
+    if (!active) tr.cn = TraceCounts{0u, 0u, 0u, 0u, 0u, 0u, 0u};
+    const uint32_t v[7] = {tr.cn.ref_nodes, tr.cn.hid_nodes, tr.cn.entries, tr.cn.hid_pairs, tr.cn.lane_tris,
+                           tr.cn.coop_tris, tr.cn.cone_switches};
+    for (int k = 0; k < 7; ++k) {
         unsigned long long s = v[k];
         for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(kFull, s, off);
         if ((threadIdx.x & 31u) == 0u && s) atomicAdd(out + k, s);
@@ -384,6 +385,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_trace_batch_persistent(const Ba
     b.tris = nullptr;
     b.pairs = nullptr;
     b.hx = nullptr;
+    b.cones = nullptr;
     b.nodes_used = b.ntris = b.root_count = b.root_first = 0;
     LaneRay r;
     TravT<STK> tr;

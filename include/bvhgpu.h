@@ -235,12 +235,13 @@ int bvhgpu_blas_info(bvhgpu_ctx* ctx, uint32_t blas_id, uint32_t* nodes_used, ui
  * NULL. */
 int bvhgpu_blas_hidden(bvhgpu_ctx* ctx, uint32_t blas_id, uint32_t* nodes, uint32_t* pairs, uint32_t* depth);
 /* bvhgpu_blas_intersect_async's traversal with work counters (device buffers; synchronous): the
- * hits (identical to the plain call's) and, summed over the rays, counts[0..5] = reference
+ * hits (identical to the plain call's) and, summed over the rays, counts[0..6] = reference
  * interior nodes visited, hidden interior nodes visited, hidden trees entered, hidden triangle
- * pairs tested, triangles tested lane by lane, triangles tested by the warp -- the node and
- * triangle bytes each ray fetched.  No reference counterpart: for measurement. */
+ * pairs tested, triangles tested lane by lane, triangles tested by the warp, cone records read
+ * on entering another cone's subtree -- the node and triangle bytes each ray fetched.  No
+ * reference counterpart: for measurement. */
 int bvhgpu_blas_trace_counts(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhgpu_ray* d_rays, uint32_t n,
-                             bvhgpu_hit* d_hits, uint64_t counts[6]);
+                             bvhgpu_hit* d_hits, uint64_t counts[7]);
 /* New vertex positions (same triangle order), e.g. an animated mesh before refit. */
 int bvhgpu_blas_update_vertices(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhgpu_triangle* tris);
 int bvhgpu_blas_update_vertices_async(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhgpu_triangle* d_tris,
