@@ -52,6 +52,10 @@ struct GBlas {
 constexpr uint32_t kHiddenLeaf = 0x80000000u;
 constexpr uint32_t kHiddenInterior = 0x40000000u;
 constexpr uint32_t kConeMask = 0x3FFFFFFFu;
+constexpr uint32_t kAnyCone = 0xFFFFFFFFu;  // TravT::lcone: the margins hold in the whole hidden tree
+// Below this root-cone margin a ray keeps the root cone's margins in the whole hidden tree (the
+// finer cones would cost more to evaluate than they save).
+constexpr float kConeSwitchDuv = 0.05f;
 
 // Interior: a reference branch (count 0) or a hidden one (kHiddenInterior | cone).
 __host__ __device__ __forceinline__ bool node_interior(uint32_t cnt) { return cnt == 0u || (cnt >> 30) == 1u; }
@@ -515,7 +519,8 @@ struct TravT {
                 if (lc.on) {  // else: margins too wide for this ray, the leaf is tested in order
                     if constexpr (COUNT) ++cn.entries;
                     held = false;
-                    lcone = leaf_cone = c;
+                    leaf_cone = c;
+                    lcone = lc.duv < kConeSwitchDuv ? kAnyCone : c;
                     first = e.x;  // the hidden root is always an interior node
                     cnt = e.y;
                     return kStepContinue;
@@ -531,7 +536,7 @@ struct TravT {
     // An interior node (node_interior(cnt)): its children's boxes -- the reference's slab test for reference
     // nodes, the margins' exact cull for hidden ones -- then the near child, the far one pushed.
     __device__ __forceinline__ StepResult interior(const GBlas& b, LaneRay& r, LeafPolicy pol, uint32_t* err) {
-        if (first >= b.nodes_used && (cnt & kConeMask) != lcone) {
+        if (first >= b.nodes_used && lcone != kAnyCone && (cnt & kConeMask) != lcone) {
             // a subtree under another cone: its own (tighter) margins, else the tree's root cone's
             lcone = cnt & kConeMask;
             lc = cone_cull(b, r, lcone, pol);

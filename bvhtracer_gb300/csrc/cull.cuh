@@ -202,6 +202,7 @@ struct LeafCull {
     float slo[3], shi[3];
     float thi, tlo;
     float dt0, dt1;  // Dt(t) <= dt0 + t dt1 (rounded up)
+    float duv;       // the barycentric margin Du + Dv the planes were grown for
     bool on;
     uint32_t zero;
 };
@@ -224,6 +225,7 @@ BVHGPU_HD LeafCull leaf_cull(const CullRay& r, float Q, float B, float t_best, f
     lc.thi = INFINITY;
     lc.tlo = -INFINITY;
     lc.dt0 = lc.dt1 = 0.0f;
+    lc.duv = INFINITY;
     if (!r.ok || !(Q < kCullHuge) || !(B < kCullHuge)) return lc;
     const float oinf = cull_fmax(cull_abs(r.o[0]), cull_fmax(cull_abs(r.o[1]), cull_abs(r.o[2])));
     const float S = (oinf + B) * (1.0f + 4.0f * u0);
@@ -239,6 +241,7 @@ BVHGPU_HD LeafCull leaf_cull(const CullRay& r, float Q, float B, float t_best, f
     const float e_uv = r.b_uv * S * Q;                   // >= E_u + E_v
     const float duv = ((e_uv + 2.0f * e_det) * KD + 8.0f * u0) * (1.0f + 4.0f * u0);
     // margins of half a triangle or more cull little: the caller tests the leaf in order instead
+    lc.duv = duv;
     if (!(duv < max_duv)) return lc;
     const float R = 4.0f * (duv + 2.0f * u0) * Q * 1.0001f + 1e-30f;
     if (!(R < kCullHuge)) return lc;
