@@ -511,7 +511,7 @@ struct TravT {
             if (test_hidden_leaf(b, first, cnt & ~kHiddenLeaf, r, held)) lc.thi = leaf_thi(lc, r.ct);
             return pop() ? kStepFinished : kStepContinue;
         }
-        if (b.hx != nullptr) {
+        if (b.hx != nullptr && pol.max_duv > 0.0f) {
             const uint2 e = __ldg(b.hx + first);
             if (e.x != 0u) {
                 const uint32_t c = e.y & kConeMask;
