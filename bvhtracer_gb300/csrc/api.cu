@@ -856,9 +856,22 @@ int bvhgpu_blas_trace_bounce_async(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhg
     return BVHGPU_OK;
 }
 
-// One upload, one launch, one download: on GB300 the host copies run at ~200 GB/s (0.8 ms for a
-// 1080p frame), while splitting the launch to overlap them costs more (each extra launch adds a
-// ramp-up and a tail of ~0.3-0.5 ms).  The bounce count is reduced on the device.
+// The device address of host memory the GPU can read and write in place (page-locked memory from
+// cudaHostAlloc / bvhgpu_host_alloc), or null.
+static void* mapped_device_ptr(const void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();  // clear: an unregistered pointer is not an error here
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
+// With page-locked host buffers the launch reads the rays and writes the hit records in place
+// (over NVLink-C2C on Grace machines), so no copy phase precedes or follows it.  Otherwise: one
+// upload, one launch, one download -- on GB300 the staged copies run at ~200 GB/s, while splitting
+// the launch to overlap them costs more (each extra launch adds a ramp-up and a tail of
+// ~0.3-0.5 ms).  The bounce count is reduced on the device either way.
 int bvhgpu_blas_trace_bounce(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhgpu_ray* rays, uint32_t n, uint32_t seed,
                              int mode, bvhgpu_hit* hits0, bvhgpu_hit* hits1, uint32_t* n_bounce) {
     if (!ctx || (n && (!rays || !hits0 || !hits1))) return BVHGPU_ERR_INVALID_ARG;
@@ -866,11 +879,28 @@ int bvhgpu_blas_trace_bounce(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhgpu_ray
         if (n_bounce) *n_bounce = 0;
         return BVHGPU_OK;
     }
+    uint32_t* d_count = ctx->d_scratch + 16;
+    uint32_t* h_count = static_cast<uint32_t*>(ctx->host_word);
+    void* m_rays = mapped_device_ptr(rays);
+    void* m_h0 = m_rays ? mapped_device_ptr(hits0) : nullptr;
+    void* m_h1 = m_h0 ? mapped_device_ptr(hits1) : nullptr;
+    if (m_rays && m_h0 && m_h1) {
+        int rc = bvhgpu_blas_trace_bounce_async(ctx, blas_id, static_cast<const bvhgpu_ray*>(m_rays), n, seed, mode,
+                                                static_cast<bvhgpu_hit*>(m_h0), static_cast<bvhgpu_hit*>(m_h1),
+                                                nullptr);
+        if (rc) return rc;
+        CK(cudaMemsetAsync(d_count, 0, sizeof(uint32_t), ctx->stream), "count");
+        CK(launch_count_hits(ctx, m_h0, n, d_count, ctx->stream), "count");
+        CK(cudaMemcpyAsync(h_count, d_count, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream), "count");
+        rc = finish(ctx);
+        if (rc) return rc;
+        if (n_bounce) *n_bounce = *h_count;
+        return BVHGPU_OK;
+    }
     int rc = ensure(ctx, &ctx->stage_in, &ctx->stage_in_bytes, 32ull * n);
     if (!rc) rc = ensure(ctx, &ctx->stage_out, &ctx->stage_out_bytes, 20ull * n);
     if (!rc) rc = ensure(ctx, &ctx->stage_out2, &ctx->stage_out2_bytes, 20ull * n);
     if (rc) return rc;
-    uint32_t* d_count = ctx->d_scratch + 16;
     CK(cudaMemcpyAsync(ctx->stage_in, rays, 32ull * n, cudaMemcpyHostToDevice, ctx->stream), "upload rays");
     rc = bvhgpu_blas_trace_bounce_async(ctx, blas_id, static_cast<const bvhgpu_ray*>(ctx->stage_in), n, seed, mode,
                                         static_cast<bvhgpu_hit*>(ctx->stage_out),
@@ -880,7 +910,6 @@ int bvhgpu_blas_trace_bounce(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhgpu_ray
     CK(launch_count_hits(ctx, ctx->stage_out, n, d_count, ctx->stream), "count");
     CK(cudaMemcpyAsync(hits0, ctx->stage_out, 20ull * n, cudaMemcpyDeviceToHost, ctx->stream), "download hits");
     CK(cudaMemcpyAsync(hits1, ctx->stage_out2, 20ull * n, cudaMemcpyDeviceToHost, ctx->stream), "download hits");
-    uint32_t* h_count = static_cast<uint32_t*>(ctx->host_word);
     CK(cudaMemcpyAsync(h_count, d_count, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream), "count");
     rc = finish(ctx);
     if (rc) return rc;

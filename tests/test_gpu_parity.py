@@ -160,16 +160,26 @@ def test_bounce_rays_and_hits(ctx):
 
 
 @pytest.mark.parametrize("mode", [bt.MODE_PLAIN, bt.MODE_PERSISTENT])
-def test_host_call_equals_device_launch(ctx, mode):
-    """bvhgpu_blas_trace_bounce with host buffers (and its device-side bounce count) gives what
-    the device-buffer launch gives."""
+@pytest.mark.parametrize("pinned", [False, True])
+def test_host_call_equals_device_launch(ctx, mode, pinned):
+    """bvhgpu_blas_trace_bounce with host buffers -- staged through device copies, or read and
+    written in place when every buffer is page-locked -- and its device-side bounce count give
+    what the device-buffer launch gives."""
     tris, rays, _ = scenes.config1(seed=5, width=960, height=544)
     tris, bvh = build(tris)
     blas = ctx.upload_blas(bvh, tris)
     n = len(rays)
-    pr = ctx.pinned((n,), bt.RAY)
-    pr.array[:] = rays
-    h0, h1, nb = blas.trace_bounce(pr.array, 77, mode)
+    if pinned:
+        pr, p0, p1 = ctx.pinned((n,), bt.RAY), ctx.pinned((n,), bt.HIT), ctx.pinned((n,), bt.HIT)
+        pr.array[:] = rays
+        import ctypes
+        from bvhtracer_gb300._lib import ptr
+        nb_c = ctypes.c_uint32()
+        ctx.check(ctx.lib.bvhgpu_blas_trace_bounce(ctx.h, blas.id, ptr(pr.array), n, 77, mode, ptr(p0.array),
+                                                   ptr(p1.array), ctypes.byref(nb_c)))
+        h0, h1, nb = p0.array.copy(), p1.array.copy(), nb_c.value
+    else:
+        h0, h1, nb = blas.trace_bounce(rays, 77, mode)
     d_rays = ctx.to_device(rays)
     d0 = ctx.device_buffer(n * bt.HIT.itemsize)
     d1 = ctx.device_buffer(n * bt.HIT.itemsize)
