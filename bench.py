@@ -323,7 +323,9 @@ def run_ours(args):
             else (other_value / (value / world)),
         },
         "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": n * bt.RAY.itemsize,
-                "d2h_bytes_per_step": 2 * n * bt.HIT.itemsize},
+                "d2h_bytes_per_step": 2 * n * bt.HIT.itemsize,
+                "transfer": "page-locked host buffers, read and written in place by the launch (NVLink-C2C); "
+                            "wall clock around bvhgpu_blas_trace_bounce"},
         "gpu_launches": None,
         "clocks": clk,
         "kernel_ms": {k: {"ms_total": v[0], "launches": v[1]} for k, v in prof.items()},
