@@ -361,7 +361,8 @@ def run_ours(args):
                           "traffic_kind": traffic_kind, "traffic_source": traffic_src,
                           "algorithmic_bytes_per_launch": own_bytes, "launch_ms": per_launch_s * 1e3,
                           "bytes_basis": "node + triangle bytes fetched by the kernel's traversal (device counters: "
-                                         "64 B per interior node, 40 B per hidden-tree entry, 32 B per cone switch, "
+                                         "64 B per reference interior node, 32 B per hidden child box, 40 B per "
+                                         "hidden-tree entry, 32 B per cone switch, "
                                          "88 B per hidden pair, "
                                          "48 / 40 B per lane / warp triangle) + 32 B ray + 20 B hit per ray",
                           "fetched": fetched,
@@ -386,7 +387,7 @@ def fetched_bytes(ctx, blas, rays, seed):
         d_r = ctx.to_device(rs)
         d_h = ctx.device_buffer(max(1, n) * bt.HIT.itemsize)
         c = blas.trace_counts(d_r, n, d_h)
-        node_b = 64 * (c["ref_nodes"] + c["hidden_nodes"]) + 40 * c["hidden_entries"] + 32 * c["cone_switches"]
+        node_b = 64 * c["ref_nodes"] + 32 * c["hidden_boxes"] + 40 * c["hidden_entries"] + 32 * c["cone_switches"]
         tri_b = 88 * c["hidden_pairs"] + 48 * c["lane_tris"] + 40 * c["warp_tris"]
         total = node_b + tri_b + (32 + 20) * n
         out[key] = {"rays": n, "bytes": total, "bytes_per_ray": total / max(1, n),

@@ -397,7 +397,7 @@ class Blas:
                                                        ctypes.byref(d)))
         return {"nodes": n.value, "pairs": p.value, "depth": d.value}
 
-    TRACE_COUNT_NAMES = ("ref_nodes", "hidden_nodes", "hidden_entries", "hidden_pairs", "lane_tris", "warp_tris",
+    TRACE_COUNT_NAMES = ("ref_nodes", "hidden_boxes", "hidden_entries", "hidden_pairs", "lane_tris", "warp_tris",
                          "cone_switches")
 
     def trace_counts(self, d_rays: "DeviceBuffer", n: int, d_hits: "DeviceBuffer") -> dict:

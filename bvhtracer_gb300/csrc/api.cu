@@ -218,12 +218,13 @@ void pack_nodes(const bvhgpu_node* nodes, uint32_t n, std::vector<float>& out) {
     }
 }
 
-// Hidden trees over the leaves with at least kHiddenMinLeaf triangles, built by binned SAH: a node's
-// triangles are split at the cheapest of 15 planes (16 bins of the centroids along the widest
+// Hidden trees over the leaves with at least kHiddenMinLeaf triangles, built by binned SAH: a range
+// of triangles is split at the cheapest of 15 planes (16 bins of the centroids along the widest
 // centroid axis, cost = area x count of each side), in halves by index order when the centroids
-// coincide or below depth 32, down to at most kHiddenLeafTris triangles stored as packed pairs (a padding slot is
-// all zero with index 0xFFFFFFFF).  Hidden nodes get indices from nodes_used on, children
-// adjacent, allocated depth first; the boxes and the leaf bounds Q, B and normal cone are written
+// coincide or below 32 binary levels, down to at most kHiddenLeafTris triangles stored as packed
+// pairs (a padding slot is all zero with index 0xFFFFFFFF).  Two levels of splits make one 4-wide
+// node.  Hidden nodes get indices from nodes_used on, a node's children consecutive, allocated
+// depth first; the boxes and the leaf bounds Q, B and normal cone are written
 // by the refresh kernels from `work`.  Only speed depends on the tree's shape.
 struct HiddenPlan {
     std::vector<float> nodes;  // 8 floats per hidden node (boxes 0 until refreshed)
@@ -317,8 +318,9 @@ void plan_hidden(const bvhgpu_node* nodes, uint32_t nodes_used, const std::vecto
     std::vector<uint32_t> ids;
     std::vector<SahTri> info;
     std::vector<uint4> cones;  // cone work: {first pair, end pair, ~0, cone}
-    // (first, count) of the subtree over ids[a, b) at `depth` below the hidden root; its pairs are
-    // allocated contiguously.  Nodes at even depth get their own cone, the others inherit `gov`.
+    // (first, count) of the subtree over ids[a, b) at `depth` (4-wide levels) below the hidden
+    // root; its pairs are allocated contiguously.  An interior node gets its children from two
+    // levels of binary SAH splits (2 to 4 ranges); nodes below the root get their own cone.
     auto make = [&](auto&& self, uint32_t a, uint32_t b, uint32_t depth, uint32_t gov) -> uint2 {
         hp.depth = std::max(hp.depth, depth);
         if (b - a <= kHiddenLeafTris) {
@@ -332,28 +334,35 @@ void plan_hidden(const bvhgpu_node* nodes, uint32_t nodes_used, const std::vecto
             return make_uint2(p0, kHiddenLeaf | np);
         }
         const uint32_t pa = P0 + hp.nhp;
-        const uint32_t own = (depth >= 2 && depth % 2 == 0) ? hp.ncones++ : kNoWork;
+        const uint32_t own = depth >= 1 ? hp.ncones++ : kNoWork;
         if (own != kNoWork) gov = own;
-        // SAH down to depth 32, then halves (a balanced rest keeps the stack need bounded)
-        const uint32_t m = depth < 32 ? sah_split(ids, info, a, b) : a + (b - a) / 2;
+        // SAH down to 32 binary levels, then halves (a balanced rest keeps the stack need bounded)
+        auto split = [&](uint32_t x, uint32_t y) {
+            return 2 * depth < 32 ? sah_split(ids, info, x, y) : x + (y - x) / 2;
+        };
+        uint32_t ranges[5];
+        uint32_t nr = 0;
+        const uint32_t m = split(a, b);
+        ranges[nr++] = a;
+        if (m - a > kHiddenLeafTris) ranges[nr++] = split(a, m);
+        ranges[nr++] = m;
+        if (b - m > kHiddenLeafTris) ranges[nr++] = split(m, b);
+        ranges[nr] = b;
+        const uint32_t k = nr;  // 2..4 children
         const uint32_t li = hp.nhid;
-        hp.nhid += 2;
+        hp.nhid += k;
         hp.nodes.resize(8ull * hp.nhid, 0.0f);
         hp.work.resize(hp.nhid);
-        const uint2 L = self(self, a, m, depth + 1, gov);
-        const uint32_t pm = P0 + hp.nhp;
-        const uint2 R = self(self, m, b, depth + 1, gov);
-        const uint32_t pb = P0 + hp.nhp;
-        const uint2 meta[2] = {L, R};
-        for (int c = 0; c < 2; ++c) {
+        for (uint32_t c = 0; c < k; ++c) {
+            const uint32_t pc = P0 + hp.nhp;
+            const uint2 meta = self(self, ranges[c], ranges[c + 1], depth + 1, gov);
             float* o = &hp.nodes[8ull * (li + c)];
-            std::memcpy(&o[3], &meta[c].x, 4);
-            std::memcpy(&o[7], &meta[c].y, 4);
+            std::memcpy(&o[3], &meta.x, 4);
+            std::memcpy(&o[7], &meta.y, 4);
+            hp.work[li + c] = make_uint4(pc, P0 + hp.nhp, nodes_used + li + c, kNoWork);
         }
-        hp.work[li] = make_uint4(pa, pm, nodes_used + li, kNoWork);
-        hp.work[li + 1] = make_uint4(pm, pb, nodes_used + li + 1, kNoWork);
-        if (own != kNoWork) cones.push_back(make_uint4(pa, pb, kNoWork, own));
-        return make_uint2(nodes_used + li, kHiddenInterior | gov);
+        if (own != kNoWork) cones.push_back(make_uint4(pa, P0 + hp.nhp, kNoWork, own));
+        return make_uint2(nodes_used + li, kHiddenInterior | ((k - 1) << kWideShift) | gov);
     };
     info.resize(ntris);
     for (uint32_t li : leaves) {

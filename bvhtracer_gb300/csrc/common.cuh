@@ -36,8 +36,9 @@ struct GBlas {
     // hidden tree); then one uint2 per hidden pair p >= (ntris + 1) / 2: the triangle indices of
     // its two slots (0xFFFFFFFF: padding).  Hidden nodes follow the reference's nodes_used nodes in
     // `nodes` (a node whose children start at or beyond nodes_used is hidden): an interior one has
-    // count = kHiddenInterior | its cone, a leaf count = kHiddenLeaf | pairs and first = its first
-    // pair in `pairs`, after the (ntris + 1) / 2 pairs in triangle order.
+    // 2 to 4 children, consecutive from `first`, and count = kHiddenInterior | (children - 1) << 28 |
+    // its cone; a leaf has count = kHiddenLeaf | pairs and first = its first pair in `pairs`, after
+    // the (ntris + 1) / 2 pairs in triangle order.
     const uint2* hx;
     // Cone records of the hidden trees, 2 float4 each: {axis xyz, cos_phi}, {sin_phi, nmin, Q, B}
     // (cull.cuh) -- one per hidden root and per hidden node at even depth; an interior hidden
@@ -51,7 +52,8 @@ struct GBlas {
 
 constexpr uint32_t kHiddenLeaf = 0x80000000u;
 constexpr uint32_t kHiddenInterior = 0x40000000u;
-constexpr uint32_t kConeMask = 0x3FFFFFFFu;
+constexpr uint32_t kConeMask = 0x0FFFFFFFu;
+constexpr uint32_t kWideShift = 28;  // hidden interior count: bits 28-29 = children - 1 (2..4 children)
 constexpr uint32_t kAnyCone = 0xFFFFFFFFu;  // TravT::lcone: the margins hold in the whole hidden tree
 // Below this root-cone margin a ray keeps the root cone's margins in the whole hidden tree (the
 // finer cones would cost more to evaluate than they save).
@@ -454,7 +456,7 @@ __device__ __forceinline__ bool hidden_box(float4 lo, float4 hi, float3 rd, cons
 // Per-ray work counters of the counting traversal (TravT<..., true>): what the ray fetched.
 struct TraceCounts {
     uint32_t ref_nodes;    // reference interior nodes (each loads its two children, 64 B)
-    uint32_t hid_nodes;    // hidden interior nodes (64 B)
+    uint32_t hid_boxes;    // hidden child boxes tested (32 B each; 2 to 4 per hidden interior node)
     uint32_t entries;      // hidden trees entered (the leaf's table entry, 32 B)
     uint32_t hid_pairs;    // hidden pairs tested (80 B + 8 B slot indices)
     uint32_t lane_tris;    // triangles of small reference leaves tested by the lane (48 B)
@@ -533,16 +535,51 @@ struct TravT {
         return pop() ? kStepFinished : kStepContinue;
     }
 
-    // An interior node (node_interior(cnt)): its children's boxes -- the reference's slab test for reference
-    // nodes, the margins' exact cull for hidden ones -- then the near child, the far one pushed.
-    __device__ __forceinline__ StepResult interior(const GBlas& b, LaneRay& r, LeafPolicy pol, uint32_t* err) {
-        if (first >= b.nodes_used && lcone != kAnyCone && (cnt & kConeMask) != lcone) {
+    // A hidden interior node: its 2 to 4 children's boxes under the margins' exact cull (any
+    // order is exact), the nearest entered, the other live ones pushed.
+    __device__ __forceinline__ StepResult hidden_interior(const GBlas& b, LaneRay& r, LeafPolicy pol, uint32_t* err) {
+        if (lcone != kAnyCone && (cnt & kConeMask) != lcone) {
             // a subtree under another cone: its own (tighter) margins, else the tree's root cone's
             lcone = cnt & kConeMask;
             lc = cone_cull(b, r, lcone, pol);
             if (!lc.on) lc = cone_cull(b, r, leaf_cone, pol);
             if constexpr (COUNT) ++cn.cone_switches;
         }
+        const uint32_t k = ((cnt >> kWideShift) & 3u) + 1u;
+        const float4* N = b.nodes + 2ull * first;
+        if constexpr (COUNT) cn.hid_boxes += k;
+        bool any = false;
+        uint2 near_e = make_uint2(0u, 0u);
+        float near_t = 0.0f;
+        for (uint32_t c = 0; c < k; ++c) {
+            const float4 lo = __ldg(N + 2 * c), hi = __ldg(N + 2 * c + 1);
+            float te;
+            if (!hidden_box(lo, hi, r.rd, lc, te)) continue;
+            const uint2 e = make_uint2(ubits(hi.w), ubits(lo.w));
+            if (!any) {
+                any = true;
+                near_e = e;
+                near_t = te;
+            } else if (te < near_t) {
+                if (!push(near_e, err)) return kStepFinished;
+                near_e = e;
+                near_t = te;
+            } else if (!push(e, err)) {
+                return kStepFinished;
+            }
+        }
+        if (any) {
+            cnt = near_e.x;
+            first = near_e.y;
+            return kStepContinue;
+        }
+        return pop() ? kStepFinished : kStepContinue;
+    }
+
+    // An interior node (node_interior(cnt)): for a reference node its children's boxes under the
+    // reference's slab test, the near child entered, the far one pushed (its visit order).
+    __device__ __forceinline__ StepResult interior(const GBlas& b, LaneRay& r, LeafPolicy pol, uint32_t* err) {
+        if (first >= b.nodes_used) return hidden_interior(b, r, pol, err);
         const float4* N = b.nodes + 2ull * first;
         float4 l0 = __ldg(N);
         float4 l1 = __ldg(N + 1);
@@ -550,20 +587,12 @@ struct TravT {
         float4 r1 = __ldg(N + 3);
         float dl, dr;
         bool hl, hr, left_near;
-        if constexpr (COUNT) {
-            if (first >= b.nodes_used) ++cn.hid_nodes; else ++cn.ref_nodes;
-        }
-        if (first >= b.nodes_used) {  // hidden children: any order is exact
-            hl = hidden_box(l0, l1, r.rd, lc, dl);
-            hr = hidden_box(r0, r1, r.rd, lc, dr);
-            left_near = hl && (!hr || dl <= dr);
-        } else {
-            hl = slab(l0, l1, r.o, r.rd, r.ct, dl);
-            hr = slab(r0, r1, r.o, r.rd, r.ct, dr);
-            const float kl = hl ? dl : FLT_MAX;
-            const float kr = hr ? dr : FLT_MAX;
-            left_near = kl < kr;
-        }
+        if constexpr (COUNT) ++cn.ref_nodes;
+        hl = slab(l0, l1, r.o, r.rd, r.ct, dl);
+        hr = slab(r0, r1, r.o, r.rd, r.ct, dr);
+        const float kl = hl ? dl : FLT_MAX;
+        const float kr = hr ? dr : FLT_MAX;
+        left_near = kl < kr;
         const bool near_hit = left_near ? hl : hr;
         const bool far_hit = left_near ? hr : hl;
         if (near_hit) {

@@ -173,7 +173,7 @@ __global__ void __launch_bounds__(kBlock) k_trace_count(GBlas b, const float4* _
     }
     if (active) store_hit(hits, i, r.hit && r.ct < FLT_MAX, r.ct, r.hu, r.hv, r.hp, 0u);
     if (!active) tr.cn = TraceCounts{0u, 0u, 0u, 0u, 0u, 0u, 0u};
-    const uint32_t v[7] = {tr.cn.ref_nodes, tr.cn.hid_nodes, tr.cn.entries, tr.cn.hid_pairs, tr.cn.lane_tris,
+    const uint32_t v[7] = {tr.cn.ref_nodes, tr.cn.hid_boxes, tr.cn.entries, tr.cn.hid_pairs, tr.cn.lane_tris,
                            tr.cn.coop_tris, tr.cn.cone_switches};
     for (int k = 0; k < 7; ++k) {
         unsigned long long s = v[k];

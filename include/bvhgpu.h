@@ -231,12 +231,12 @@ int bvhgpu_blas_info(bvhgpu_ctx* ctx, uint32_t blas_id, uint32_t* nodes_used, ui
  * triangles): nodes, triangle pairs and the deepest tree's depth below its leaf.  A hidden box is
  * skipped for a ray only when provably no triangle in it is accepted at or below the ray's closest
  * t, and ties keep the lowest triangle index, so results equal the reference's in-order leaf loop
- * (bvh.rs:250-258).  No reference counterpart: exposed for tests and tuning.  Any pointer may be
- * NULL. */
+ * (bvh.rs:250-258).  Hidden interior nodes have 2 to 4 children.  No reference counterpart:
+ * exposed for tests and tuning.  Any pointer may be NULL. */
 int bvhgpu_blas_hidden(bvhgpu_ctx* ctx, uint32_t blas_id, uint32_t* nodes, uint32_t* pairs, uint32_t* depth);
 /* bvhgpu_blas_intersect_async's traversal with work counters (device buffers; synchronous): the
  * hits (identical to the plain call's) and, summed over the rays, counts[0..6] = reference
- * interior nodes visited, hidden interior nodes visited, hidden trees entered, hidden triangle
+ * interior nodes visited, hidden child boxes tested, hidden trees entered, hidden triangle
  * pairs tested, triangles tested lane by lane, triangles tested by the warp, cone records read
  * on entering another cone's subtree -- the node and triangle bytes each ray fetched.  No
  * reference counterpart: for measurement. */
