@@ -603,7 +603,7 @@ int bvhgpu_blas_upload(bvhgpu_ctx* ctx, const bvhgpu_node* nodes, uint32_t nodes
     b.ncones = hp.ncones;
     b.nwork = (uint32_t)hp.work.size();
     b.ref_depth = depth;
-    b.depth = depth + hp.depth;
+    b.depth = depth + 3 * hp.depth;  // a 4-wide hidden level can leave 3 children pending
     const uint64_t nodes_all = (uint64_t)nodes_used + hp.nhid;
     const uint64_t pairs_all = (uint64_t)pairs_in_order(ntris) + hp.nhp;
     const uint64_t hx_bytes = hp.table.empty() ? 0 : 8ull * hidden_table_u2(ntris) + 8ull * std::max<uint32_t>(1, hp.nhp);
@@ -681,7 +681,7 @@ int bvhgpu_blas_hidden(bvhgpu_ctx* ctx, uint32_t blas_id, uint32_t* nodes, uint3
     if (!b) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown BLAS %u", blas_id);
     if (nodes) *nodes = b->nhid;
     if (pairs) *pairs = b->nhp;
-    if (depth) *depth = b->depth - b->ref_depth;
+    if (depth) *depth = (b->depth - b->ref_depth) / 3;
     return BVHGPU_OK;
 }
 

@@ -63,7 +63,7 @@ def test_flat_leaf_edges_vertices_and_random(ctx):
     bvh = one_leaf_bvh(tris)
     blas = ctx.upload_blas(bvh, tris)
     h = blas.hidden()
-    assert h["pairs"] >= len(tris) // 2 and h["depth"] >= 10
+    assert h["pairs"] >= len(tris) // 2 and h["depth"] >= 5  # 4-wide levels
     rays = np.concatenate([edge_rays(tris, 20000, 1), scenes.sphere_rays(20000, 2, box=4.0)])
     ref = orc.bvh_intersect(bvh.nodes, bvh.nodes_used, tris, rays, threads=8)
     same(blas.intersect(rays), ref, "flat leaf")
