@@ -604,7 +604,7 @@ int bvhgpu_blas_upload(bvhgpu_ctx* ctx, const bvhgpu_node* nodes, uint32_t nodes
     b.nwork = (uint32_t)hp.work.size();
     b.ref_depth = depth;
     b.depth = depth + 3 * hp.depth;  // a 4-wide hidden level can leave 3 children pending
-    const uint64_t nodes_all = (uint64_t)nodes_used + hp.nhid;
+    const uint64_t nodes_all = (uint64_t)nodes_used + hp.nhid + 1;  // + a spare record (4-wide reads)
     const uint64_t pairs_all = (uint64_t)pairs_in_order(ntris) + hp.nhp;
     const uint64_t hx_bytes = hp.table.empty() ? 0 : 8ull * hidden_table_u2(ntris) + 8ull * std::max<uint32_t>(1, hp.nhp);
     void* d_tris9 = nullptr;
@@ -633,6 +633,7 @@ int bvhgpu_blas_upload(bvhgpu_ctx* ctx, const bvhgpu_node* nodes, uint32_t nodes
         (e = cudaMemcpy(b.parent, parent.data(), 4ull * nodes_used, cudaMemcpyHostToDevice)) != cudaSuccess ||
         (e = cudaMemcpy(b.leaves, leaves.data(), 4ull * leaves.size(), cudaMemcpyHostToDevice)) != cudaSuccess ||
         (e = cudaMemset(b.counters, 0, 4ull * nodes_used)) != cudaSuccess ||
+        (e = cudaMemset(b.nodes + 2ull * (nodes_all - 1), 0, 32)) != cudaSuccess ||
         (e = cudaMemcpy(b.tri_leaf, tri_leaf.data(), 4ull * ntris, cudaMemcpyHostToDevice)) != cudaSuccess ||
         (e = cudaMemcpy(b.leaf_keys, key_init.data(), 8ull * key_init.size(), cudaMemcpyHostToDevice)) != cudaSuccess ||
         (e = cudaMemset(b.pairs, 0, 80ull * pairs_all)) != cudaSuccess ||

@@ -551,21 +551,29 @@ struct TravT {
         bool any = false;
         uint2 near_e = make_uint2(0u, 0u);
         float near_t = 0.0f;
-        for (uint32_t c = 0; c < k; ++c) {
-            const float4 lo = __ldg(N + 2 * c), hi = __ldg(N + 2 * c + 1);
-            float te;
-            if (!hidden_box(lo, hi, r.rd, lc, te)) continue;
-            const uint2 e = make_uint2(ubits(hi.w), ubits(lo.w));
-            if (!any) {
-                any = true;
-                near_e = e;
-                near_t = te;
-            } else if (te < near_t) {
-                if (!push(near_e, err)) return kStepFinished;
-                near_e = e;
-                near_t = te;
-            } else if (!push(e, err)) {
-                return kStepFinished;
+        // children two at a time, both loads issued together (a child record past the last one is
+        // always readable: the node array ends with a spare record)
+        for (uint32_t c = 0; c < k; c += 2) {
+            const float4 lo0 = __ldg(N + 2 * c), hi0 = __ldg(N + 2 * c + 1);
+            const float4 lo1 = __ldg(N + 2 * c + 2), hi1 = __ldg(N + 2 * c + 3);
+#pragma unroll
+            for (uint32_t h = 0; h < 2; ++h) {
+                if (c + h >= k) break;
+                const float4 lo = h ? lo1 : lo0, hi = h ? hi1 : hi0;
+                float te;
+                if (!hidden_box(lo, hi, r.rd, lc, te)) continue;
+                const uint2 e = make_uint2(ubits(hi.w), ubits(lo.w));
+                if (!any) {
+                    any = true;
+                    near_e = e;
+                    near_t = te;
+                } else if (te < near_t) {
+                    if (!push(near_e, err)) return kStepFinished;
+                    near_e = e;
+                    near_t = te;
+                } else if (!push(e, err)) {
+                    return kStepFinished;
+                }
             }
         }
         if (any) {
