@@ -548,37 +548,48 @@ struct TravT {
         const uint32_t k = ((cnt >> kWideShift) & 3u) + 1u;
         const float4* N = b.nodes + 2ull * first;
         if constexpr (COUNT) cn.hid_boxes += k;
-        bool any = false;
-        uint2 near_e = make_uint2(0u, 0u);
-        float near_t = 0.0f;
+        // the live children by entry distance (dead ones at +inf), sorted by a 5-exchange network;
+        // the nearest is entered, the others pushed farthest first so they pop in distance order
+        float t[4] = {INFINITY, INFINITY, INFINITY, INFINITY};
+        uint2 e[4] = {make_uint2(0u, 0u), make_uint2(0u, 0u), make_uint2(0u, 0u), make_uint2(0u, 0u)};
         // children two at a time, both loads issued together (a child record past the last one is
         // always readable: the node array ends with a spare record)
-        for (uint32_t c = 0; c < k; c += 2) {
+#pragma unroll
+        for (uint32_t c = 0; c < 4; c += 2) {
+            if (c >= k) break;
             const float4 lo0 = __ldg(N + 2 * c), hi0 = __ldg(N + 2 * c + 1);
             const float4 lo1 = __ldg(N + 2 * c + 2), hi1 = __ldg(N + 2 * c + 3);
-#pragma unroll
-            for (uint32_t h = 0; h < 2; ++h) {
-                if (c + h >= k) break;
-                const float4 lo = h ? lo1 : lo0, hi = h ? hi1 : hi0;
-                float te;
-                if (!hidden_box(lo, hi, r.rd, lc, te)) continue;
-                const uint2 e = make_uint2(ubits(hi.w), ubits(lo.w));
-                if (!any) {
-                    any = true;
-                    near_e = e;
-                    near_t = te;
-                } else if (te < near_t) {
-                    if (!push(near_e, err)) return kStepFinished;
-                    near_e = e;
-                    near_t = te;
-                } else if (!push(e, err)) {
-                    return kStepFinished;
-                }
+            float te;
+            if (hidden_box(lo0, hi0, r.rd, lc, te)) {
+                t[c] = te;
+                e[c] = make_uint2(ubits(hi0.w), ubits(lo0.w));
+            }
+            if (c + 1 < k && hidden_box(lo1, hi1, r.rd, lc, te)) {
+                t[c + 1] = te;
+                e[c + 1] = make_uint2(ubits(hi1.w), ubits(lo1.w));
             }
         }
-        if (any) {
-            cnt = near_e.x;
-            first = near_e.y;
+        auto cx = [&](int i, int j) {
+            if (t[j] < t[i]) {
+                const float tt = t[i];
+                t[i] = t[j];
+                t[j] = tt;
+                const uint2 ee = e[i];
+                e[i] = e[j];
+                e[j] = ee;
+            }
+        };
+        cx(0, 1);
+        cx(2, 3);
+        cx(0, 2);
+        cx(1, 3);
+        cx(1, 2);
+        if (t[0] < INFINITY) {
+#pragma unroll
+            for (int i = 3; i >= 1; --i)
+                if (t[i] < INFINITY && !push(e[i], err)) return kStepFinished;
+            cnt = e[0].x;
+            first = e[0].y;
             return kStepContinue;
         }
         return pop() ? kStepFinished : kStepContinue;
