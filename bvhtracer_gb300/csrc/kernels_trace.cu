@@ -247,9 +247,7 @@ __global__ void k_count_hits(const GHit* __restrict__ hits, uint32_t n, uint32_t
 // ---- persistent: primary + bounce in one launch -------------------------------------------
 // Each warp keeps 32 ray slots.  A slot whose ray finished is refilled from the global queue
 // (ballot -> one atomicAdd per warp -> shfl); a primary that hit continues in the same slot
-// with its bounce ray, so no compaction pass and no second launch are needed.  With refill 32
-// the warp instead takes 32 rays at a time and traces their primaries, then their bounces, as
-// whole-warp batches (similar rays together; better where rays are cheap).
+// with its bounce ray, so no compaction pass and no second launch are needed.
 
 template <int BLOCK, int MINB, class STK>
 __global__ void __launch_bounds__(BLOCK, MINB) k_persistent_bounce(GBlas b, const float4* __restrict__ rays,
@@ -259,38 +257,6 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_persistent_bounce(GBlas b, cons
                                                                    uint32_t key0, uint32_t* err) {
     extern __shared__ uint2 stack_smem[];
     const unsigned lane = threadIdx.x & 31u;
-    if (refill >= 32u) {
-        // whole-warp batches: 32 primaries traced together, then their bounces together
-        for (;;) {
-            uint32_t base = 0;
-            if (lane == 0) base = atomicAdd(queue, 32u);
-            base = __shfl_sync(kFull, base, 0);
-            if (base >= n) return;
-            const uint32_t my = base + lane;
-            const bool active = my < n;
-            LaneRay r;
-            if (active) {
-                float3 o, d;
-                float t0;
-                load_ray(rays, my, o, d, t0);
-                init_lane_ray(r, o, d, t0);
-            }
-            warp_trace<STK>(b, active, r, pol, err, stack_smem);
-            const bool h = active && r.hit && r.ct < FLT_MAX;
-            if (active) store_hit(hits0, my, h, r.ct, r.hu, r.hv, r.hp, 0u);
-            float3 po, pd;
-            bool have = false;
-            if (h) {
-                const float4* T = b.tris + 3ull * r.hp;
-                have = bounce_dir(r.o, r.d, r.ct, __ldg(T), __ldg(T + 1), __ldg(T + 2), seed, key0 + my, po, pd);
-            }
-            if (active && !have) store_hit(hits1, my, false, 0, 0, 0, 0, 0);
-            LaneRay r2;
-            if (have) init_lane_ray(r2, po, pd, FLT_MAX);
-            warp_trace<STK>(b, have, r2, pol, err, stack_smem);
-            if (have) store_hit(hits1, my, r2.hit && r2.ct < FLT_MAX, r2.ct, r2.hu, r2.hv, r2.hp, 0u);
-        }
-    }
     int phase = 0;  // 0 needs work, 1 primary ray, 2 bounce ray, 3 retired
     uint32_t idx = 0;
     LaneRay r;

@@ -21,7 +21,7 @@ using namespace bvhgpu;
 namespace {
 
 constexpr uint32_t kBigLeafValues[] = {8u, 16u, 32u, 64u, BVHGPU_BIG_LEAF_NEVER};
-constexpr uint32_t kRefillValues[] = {1u, 8u, 16u, 32u};
+constexpr uint32_t kRefillValues[] = {1u, 8u, 16u};
 constexpr uint32_t kHiddenValues[] = {0u, 100u, 250u, 500u, 1000u};
 
 bool tunable(int k) {
@@ -132,7 +132,7 @@ int bvhgpu_tune_set(bvhgpu_ctx* ctx, int kernel, const bvhgpu_tune_config* cfg) 
 
 int bvhgpu_tune_space(int kernel, bvhgpu_tune_config* out, uint32_t cap, uint32_t* count) {
     if (!tunable(kernel) || (cap && !out)) return BVHGPU_ERR_INVALID_ARG;
-    const uint32_t nrefill = persistent(kernel) ? 4u : 1u;
+    const uint32_t nrefill = persistent(kernel) ? 3u : 1u;
     uint32_t k = 0;
     for (int sh = 0; sh < kNumShapes; ++sh)
         for (int st = 0; st < kNumStacks; ++st)

@@ -398,8 +398,7 @@ typedef struct bvhgpu_tune_config {
      * BVHGPU_BIG_LEAF_NEVER = every leaf by its lane. */
     uint32_t big_leaf;
     /* ray batch of the persistent kernels: a warp fetches new rays once this many of its lanes
-     * are idle (1..32; a warp whose lanes are all idle always fetches).  For PERSISTENT_BOUNCE, 32
-     * means whole-warp batches: 32 primaries traced together, then their bounces together. */
+     * are idle (1..32; a warp whose lanes are all idle always fetches). */
     uint32_t refill;
     /* hidden trees: a ray walks a large leaf's hidden tree (bvhgpu_blas_hidden) when its cull
      * margin there, in thousandths of a triangle's barycentric range, is below this; otherwise the
@@ -413,7 +412,7 @@ int bvhgpu_tune_get(bvhgpu_ctx* ctx, int kernel, bvhgpu_tune_config* out);
 int bvhgpu_tune_set(bvhgpu_ctx* ctx, int kernel, const bvhgpu_tune_config* cfg);
 /* The candidate values the tuner searches, as a list of configs (cap entries at most; *count
  * gets the full number): every compiled shape x stack, big_leaf in {8, 16, 32, 64, NEVER},
- * refill in {1, 8, 16, 32} (refill only for the persistent kernels) and hidden in
+ * refill in {1, 8, 16} (refill only for the persistent kernels) and hidden in
  * {0, 100, 250, 500, 1000}. */
 int bvhgpu_tune_space(int kernel, bvhgpu_tune_config* out, uint32_t cap, uint32_t* count);
 

@@ -55,11 +55,11 @@ def test_host_entry_points_validate_arguments():
 
 def test_tune_space_lists_every_compiled_variant():
     """bvhgpu_tune_space needs no device: 5 launch shapes x 3 stacks x 5 big-leaf values x 5
-    hidden-tree margins, times 4 refill sizes for the persistent kernels."""
+    hidden-tree margins, times 3 refill sizes for the persistent kernels."""
     from bvhtracer_gb300.api import Context
     import bvhtracer_gb300 as bt
-    for kernel, n in ((bt.K_TRACE_BLAS, 375), (bt.K_TRACE_SCENE, 375), (bt.K_PERSISTENT_BOUNCE, 1500),
-                      (bt.K_TRACE_BATCH, 1500), (bt.K_SCENE_BOUNCE, 1500)):
+    for kernel, n in ((bt.K_TRACE_BLAS, 375), (bt.K_TRACE_SCENE, 375), (bt.K_PERSISTENT_BOUNCE, 1125),
+                      (bt.K_TRACE_BATCH, 1125), (bt.K_SCENE_BOUNCE, 1125)):
         space = Context.tune_space(kernel)
         assert len(space) == n
         assert {(c["block"], c["min_blocks"]) for c in space} == {(128, 1), (128, 5), (128, 6), (128, 8), (64, 1)}

@@ -20,10 +20,10 @@ def ctx():
 
 
 def subset(kernel):
-    """All shapes x stacks; big_leaf 8 (warp-cooperative) and NEVER (per lane); refill 1 and 32;
+    """All shapes x stacks; big_leaf 8 (warp-cooperative) and NEVER (per lane); refill 1 and 16;
     hidden trees never (0) and at the widest margin (1000)."""
     return [c for c in bt.Context.tune_space(kernel)
-            if c["big_leaf"] in (8, bt.BIG_LEAF_NEVER) and c["refill"] in (1, 32) and c["hidden"] in (0, 1000)]
+            if c["big_leaf"] in (8, bt.BIG_LEAF_NEVER) and c["refill"] in (1, 16) and c["hidden"] in (0, 1000)]
 
 
 def build(tris):
