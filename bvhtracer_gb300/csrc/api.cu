@@ -894,6 +894,20 @@ int bvhgpu_blas_trace_bounce(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhgpu_ray
     void* m_rays = mapped_device_ptr(rays);
     void* m_h0 = m_rays ? mapped_device_ptr(hits0) : nullptr;
     void* m_h1 = m_h0 ? mapped_device_ptr(hits1) : nullptr;
+    DeviceBlas* b = find_blas(ctx, blas_id);
+    if (!b) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown BLAS %u", blas_id);
+    if (m_rays && m_h0 && m_h1 && mode == BVHGPU_MODE_PERSISTENT) {
+        // the persistent launch counts its primary hits itself
+        CK(cudaMemsetAsync(d_count, 0, sizeof(uint32_t), ctx->stream), "count");
+        CK(launch_bounce_persistent(ctx, *b, static_cast<const float4*>(m_rays), n, seed, m_h0, m_h1, ctx->stream, 0,
+                                    d_count),
+           "bounce (persistent)");
+        CK(cudaMemcpyAsync(h_count, d_count, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream), "count");
+        const int rc = finish(ctx);
+        if (rc) return rc;
+        if (n_bounce) *n_bounce = *h_count;
+        return BVHGPU_OK;
+    }
     if (m_rays && m_h0 && m_h1) {
         int rc = bvhgpu_blas_trace_bounce_async(ctx, blas_id, static_cast<const bvhgpu_ray*>(m_rays), n, seed, mode,
                                                 static_cast<bvhgpu_hit*>(m_h0), static_cast<bvhgpu_hit*>(m_h1),

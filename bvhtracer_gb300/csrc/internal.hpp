@@ -162,8 +162,10 @@ cudaError_t launch_trace_blas(bvhgpu_ctx* ctx, const DeviceBlas& b, const float4
 // the ray's index there, so a ray set traced in parts gives the same bounces).
 cudaError_t launch_bounce_plain(bvhgpu_ctx* ctx, const DeviceBlas& b, const float4* rays, uint32_t n, uint32_t seed,
                                 void* hits0, void* hits1, cudaStream_t s, uint32_t base = 0);
+// hit_count (may be null): primary hits are added to *hit_count.
 cudaError_t launch_bounce_persistent(bvhgpu_ctx* ctx, const DeviceBlas& b, const float4* rays, uint32_t n,
-                                     uint32_t seed, void* hits0, void* hits1, cudaStream_t s, uint32_t base = 0);
+                                     uint32_t seed, void* hits0, void* hits1, cudaStream_t s, uint32_t base = 0,
+                                     uint32_t* hit_count = nullptr);
 // The plain traversal with per-ray work counters summed into out[0..6] (TraceCounts order).
 cudaError_t launch_trace_count(bvhgpu_ctx* ctx, const DeviceBlas& b, const float4* rays, uint32_t n, void* hits,
                                unsigned long long* out, cudaStream_t s);

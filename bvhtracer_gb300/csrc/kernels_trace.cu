@@ -254,11 +254,12 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_persistent_bounce(GBlas b, cons
                                                                    uint32_t n, uint32_t seed,
                                                                    GHit* __restrict__ hits0, GHit* __restrict__ hits1,
                                                                    uint32_t* queue, LeafPolicy pol, uint32_t refill,
-                                                                   uint32_t key0, uint32_t* err) {
+                                                                   uint32_t key0, uint32_t* hit_count, uint32_t* err) {
     extern __shared__ uint2 stack_smem[];
     const unsigned lane = threadIdx.x & 31u;
     int phase = 0;  // 0 needs work, 1 primary ray, 2 bounce ray, 3 retired
     uint32_t idx = 0;
+    uint32_t nhit = 0;  // primary hits of this lane (summed into *hit_count at the end, if given)
     LaneRay r;
     TravT<STK> tr;
     tr.stk.bind(stack_smem);
@@ -301,6 +302,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_persistent_bounce(GBlas b, cons
                 break;
             }
             store_hit(hits0, idx, h, r.ct, r.hu, r.hv, r.hp, 0u);
+            nhit += h ? 1u : 0u;
             float3 po, pd;
             bool have = false;
             if (h) {
@@ -319,7 +321,13 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_persistent_bounce(GBlas b, cons
         }
         unsigned pend = __ballot_sync(kFull, (phase == 1 || phase == 2) && st == kStepBigLeaf);
         if (pend == 0u) {
-            if (!queue_open && __ballot_sync(kFull, phase == 0 || phase == 1 || phase == 2) == 0u) break;
+            if (!queue_open && __ballot_sync(kFull, phase == 0 || phase == 1 || phase == 2) == 0u) {
+                if (hit_count) {
+                    for (int off = 16; off > 0; off >>= 1) nhit += __shfl_xor_sync(kFull, nhit, off);
+                    if (lane == 0 && nhit) atomicAdd(hit_count, nhit);
+                }
+                break;
+            }
             continue;
         }
         coop_leaf_phase(pend, b, tr, r, st);
@@ -681,7 +689,8 @@ cudaError_t launch_bounce_plain(bvhgpu_ctx* ctx, const DeviceBlas& b, const floa
 }
 
 cudaError_t launch_bounce_persistent(bvhgpu_ctx* ctx, const DeviceBlas& b, const float4* rays, uint32_t n,
-                                     uint32_t seed, void* hits0, void* hits1, cudaStream_t s, uint32_t base) {
+                                     uint32_t seed, void* hits0, void* hits1, cudaStream_t s, uint32_t base,
+                                     uint32_t* hit_count) {
     if (n == 0) return cudaSuccess;
     uint32_t* queue = ctx->d_scratch + 2;
     cudaError_t e = cudaMemsetAsync(queue, 0, sizeof(uint32_t), s);
@@ -696,7 +705,7 @@ cudaError_t launch_bounce_persistent(bvhgpu_ctx* ctx, const DeviceBlas& b, const
         const size_t smem = stack_smem_bytes<STK>(SH::block);
         k<<<persistent_grid(ctx, k, SH::block, smem), SH::block, smem, s>>>(
             g, rays, n, seed, static_cast<GHit*>(hits0), static_cast<GHit*>(hits1), queue, v.pol, v.refill, base,
-            ctx->d_err);
+            hit_count, ctx->d_err);
         return cudaGetLastError();
     });
     g_launches++;
