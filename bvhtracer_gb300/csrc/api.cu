@@ -1031,7 +1031,6 @@ int bvhgpu_scene_create(bvhgpu_ctx* ctx, const uint32_t* blas_ids, uint32_t nobj
             g.pairs = b->pairs;
             g.hx = b->hx;
             g.cones = b->cones;
-            g.hwork = b->hwork;
             g.nodes_used = b->nodes_used;
             g.ntris = b->ntris;
             g.root_count = b->root_count;

@@ -44,9 +44,6 @@ struct GBlas {
     // (cull.cuh) -- one per hidden root and per hidden node at even depth; an interior hidden
     // node's cone covers all its triangles.
     const float4* cones;
-    // Pair range {first, end, node, -} of every hidden node (index: node - nodes_used), then of the
-    // cone records: the warp-cooperative test of a hidden tree tests subtrees by range.
-    const uint4* hwork;
     uint32_t nodes_used;
     uint32_t ntris;
     uint32_t root_count;  // root node meta (node 0)
@@ -842,208 +839,6 @@ __device__ __forceinline__ void coop_leaf2(const ulonglong2* __restrict__ pairs,
     }
     reduce_and_take(ba, pairs, srcA, r);
     reduce_and_take(bb, pairs, srcB, r);
-}
-
-// ---- warp-cooperative test of a hidden tree --------------------------------------------------
-// For a ray whose margins at a large leaf are too wide to walk the hidden tree alone, the warp
-// culls the tree's (up to 16) subtrees two levels below the root with the same exact margins
-// (root cone, no margin limit) and tests the surviving subtrees' pair ranges together, one pair
-// per lane.  The running best is the smallest (t, triangle index), started at (closest t, 0): the
-// in-order loop's result for the whole leaf.
-
-struct BestLex {
-    float t;
-    uint32_t k;
-    __device__ __forceinline__ void take(const PairHit& h, uint2 idx) {
-        if (h.okA && (h.tA < t || (h.tA == t && idx.x < k))) {
-            t = h.tA;
-            k = idx.x;
-        }
-        if (h.okB && (h.tB < t || (h.tB == t && idx.y < k))) {
-            t = h.tB;
-            k = idx.y;
-        }
-    }
-};
-
-// Warp argmin of (t, triangle); lane `src` takes the hit when the minimum t is below t0 (the ray's
-// closest t when the leaf test began), u, v recomputed as reduce_and_take does.
-__device__ __forceinline__ void reduce_and_take_lex(BestLex b, float t0, const ulonglong2* __restrict__ pairs, int src,
-                                                    LaneRay& r) {
-    const unsigned kAll = 0xFFFFFFFFu;
-    const unsigned lane = threadIdx.x & 31u;
-    float bt = b.t;
-    uint32_t bk = b.k;
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-        const float ot = __shfl_xor_sync(kAll, bt, off);
-        const uint32_t ok = __shfl_xor_sync(kAll, bk, off);
-        if (ot < bt || (ot == bt && ok < bk)) {
-            bt = ot;
-            bk = ok;
-        }
-    }
-    if (bt < t0 && (int)lane == src) {
-        float4 v0, e1, e2;
-        load_pair_tri(pairs, bk, v0, e1, e2);
-        float t, u, v;
-        tri_test(v0, e1, e2, r.o, r.d, t, u, v);
-        r.ct = bt;
-        r.hu = u;
-        r.hv = v;
-        r.hp = bk;
-        r.hit = true;
-        r.inst = r.inst_cur;
-    }
-}
-
-// Subtree `lane` (< 16) of the hidden tree with root {first, count}: grandchild lane % 4 of root
-// child lane / 4 (a root child that is a leaf is its own subtree, at lane % 4 == 0).
-struct HiddenSub {
-    bool valid;
-    float4 lo, hi;
-    uint32_t pa, pb;  // pair range
-};
-
-__device__ __forceinline__ HiddenSub hidden_subtree(const GBlas& b, uint2 root, unsigned lane) {
-    HiddenSub s;
-    s.valid = false;
-    s.pa = s.pb = 0u;
-    const uint32_t c1 = lane >> 2, c2 = lane & 3u;
-    if (lane >= 16u || c1 > ((root.y >> kWideShift) & 3u)) return s;
-    const float4* R1 = b.nodes + 2ull * (root.x + c1);
-    const float4 lo1 = __ldg(R1), hi1 = __ldg(R1 + 1);
-    const uint32_t first1 = ubits(lo1.w), cnt1 = ubits(hi1.w);
-    if (cnt1 & kHiddenLeaf) {
-        if (c2 != 0u) return s;
-        s.valid = true;
-        s.lo = lo1;
-        s.hi = hi1;
-        s.pa = first1;
-        s.pb = first1 + (cnt1 & ~kHiddenLeaf);
-        return s;
-    }
-    if (c2 > ((cnt1 >> kWideShift) & 3u)) return s;
-    const uint32_t node = first1 + c2;
-    const float4* R2 = b.nodes + 2ull * node;
-    s.lo = __ldg(R2);
-    s.hi = __ldg(R2 + 1);
-    const uint32_t cnt2 = ubits(s.hi.w);
-    if (cnt2 & kHiddenLeaf) {
-        s.pa = ubits(s.lo.w);
-        s.pb = s.pa + (cnt2 & ~kHiddenLeaf);
-    } else {
-        const uint4 w = __ldg(b.hwork + (node - b.nodes_used));
-        s.pa = w.x;
-        s.pb = w.y;
-    }
-    s.valid = true;
-    return s;
-}
-
-// The ray's margins anywhere in the hidden tree of root cone `cone` (no margin limit).
-__device__ __forceinline__ LeafCull hidden_root_cull(const GBlas& b, const CoopRay& c, float3 rd, uint32_t cone) {
-    const float4 a = __ldg(b.cones + 2ull * cone), q = __ldg(b.cones + 2ull * cone + 1);
-    const LeafCone lcn = {a.x, a.y, a.z, a.w, q.x, q.y};
-    return leaf_cull(cull_ray_rd(c.ox, c.oy, c.oz, c.dx, c.dy, c.dz, rd.x, rd.y, rd.z), q.z, q.w, c.ct, INFINITY, lcn);
-}
-
-__device__ __forceinline__ float3 bcast_rd(const LaneRay& r, int src) {
-    const unsigned kAll = 0xFFFFFFFFu;
-    return make_float3(__shfl_sync(kAll, r.rd.x, src), __shfl_sync(kAll, r.rd.y, src), __shfl_sync(kAll, r.rd.z, src));
-}
-
-// One ray (lane srcA) or two (srcB >= 0) against the hidden tree of root {first, count}.
-__device__ __forceinline__ void coop_hidden(const GBlas& b, uint2 root, int srcA, int srcB, LaneRay& r) {
-    const unsigned kAll = 0xFFFFFFFFu;
-    const unsigned lane = threadIdx.x & 31u;
-    const bool two = srcB >= 0;
-    const uint32_t cone = root.y & kConeMask;
-    const CoopRay ca = bcast_ray(r, srcA);
-    const CoopRay cb = bcast_ray(r, two ? srcB : srcA);
-    const float3 rda = bcast_rd(r, srcA), rdb = bcast_rd(r, two ? srcB : srcA);
-    const HiddenSub sub = hidden_subtree(b, root, lane);
-    bool la = sub.valid, lb = sub.valid && two;
-    {
-        const LeafCull lca = hidden_root_cull(b, ca, rda, cone);
-        float te;
-        if (la && lca.on) la = hidden_box(sub.lo, sub.hi, rda, lca, te);
-    }
-    if (two) {
-        const LeafCull lcb = hidden_root_cull(b, cb, rdb, cone);
-        float te;
-        if (lb && lcb.on) lb = hidden_box(sub.lo, sub.hi, rdb, lcb, te);
-    }
-    const unsigned ma = __ballot_sync(kAll, la), mb = __ballot_sync(kAll, lb);
-    const bool same_o = __float_as_uint(ca.ox) == __float_as_uint(cb.ox) &&
-                        __float_as_uint(ca.oy) == __float_as_uint(cb.oy) &&
-                        __float_as_uint(ca.oz) == __float_as_uint(cb.oz);
-    const uint2* hidx = b.hx + hidden_table_u2(b.ntris) - pairs_in_order(b.ntris);
-    const f2 AOX = f2_pack(ca.ox, ca.ox), AOY = f2_pack(ca.oy, ca.oy), AOZ = f2_pack(ca.oz, ca.oz);
-    const f2 ADX = f2_pack(ca.dx, ca.dx), ADY = f2_pack(ca.dy, ca.dy), ADZ = f2_pack(ca.dz, ca.dz);
-    const f2 BOX = f2_pack(cb.ox, cb.ox), BOY = f2_pack(cb.oy, cb.oy), BOZ = f2_pack(cb.oz, cb.oz);
-    const f2 BDX = f2_pack(cb.dx, cb.dx), BDY = f2_pack(cb.dy, cb.dy), BDZ = f2_pack(cb.dz, cb.dz);
-    const f2 Z = f2_neg_zero();
-    BestLex ba{ca.ct, 0u}, bb{cb.ct, 0u};
-    unsigned m = ma | mb;
-    while (m) {
-        const int i = __ffs(m) - 1;
-        m &= m - 1u;
-        const bool ta = (ma >> i) & 1u, tb = (mb >> i) & 1u;
-        const uint32_t pa = __shfl_sync(kAll, sub.pa, i), pb = __shfl_sync(kAll, sub.pb, i);
-        for (uint32_t p = pa + lane; p < pb; p += 32u) {
-            const uint2 idx = __ldg(hidx + p);
-            const bool va = idx.x != kMiss, vb = idx.y != kMiss;
-            const PairData pd = load_pair(b.pairs + 5ull * p);
-            if (same_o) {
-                const OriginTerms ot = origin_terms(pd, AOX, AOY, AOZ, Z);
-                if (ta) ba.take(ray_terms(pd, ot, ADX, ADY, ADZ, Z, va, vb), idx);
-                if (tb) bb.take(ray_terms(pd, ot, BDX, BDY, BDZ, Z, va, vb), idx);
-            } else {
-                if (ta) ba.take(ray_terms(pd, origin_terms(pd, AOX, AOY, AOZ, Z), ADX, ADY, ADZ, Z, va, vb), idx);
-                if (tb) bb.take(ray_terms(pd, origin_terms(pd, BOX, BOY, BOZ, Z), BDX, BDY, BDZ, Z, va, vb), idx);
-            }
-        }
-    }
-    reduce_and_take_lex(ba, ca.ct, b.pairs, srcA, r);
-    if (two) reduce_and_take_lex(bb, cb.ct, b.pairs, srcB, r);
-}
-
-// Leaves of at least this many triangles with a hidden tree are tested by coop_hidden; smaller
-// ones (and leaves without one) in order by coop_leaf / coop_leaf2.
-constexpr uint32_t kCoopHiddenMin = 256;
-
-// The warp-cooperative test of the big leaf [f, f + cnt) of BLAS b for one ray (srcB < 0) or two.
-__device__ __forceinline__ void coop_leaf_any(const GBlas& b, uint32_t f, uint32_t cnt, int srcA, int srcB,
-                                              LaneRay& r) {
-    uint2 root = make_uint2(0u, 0u);
-    if (b.hx != nullptr && cnt >= kCoopHiddenMin) root = __ldg(b.hx + f);
-    if (root.x != 0u)
-        coop_hidden(b, root, srcA, srcB, r);
-    else if (srcB >= 0)
-        coop_leaf2(b.pairs, f, cnt, srcA, srcB, r);
-    else
-        coop_leaf(b.pairs, f, cnt, srcA, r);
-}
-
-// The group leader's BLAS descriptor on every lane (the lanes of a group share it).
-__device__ __forceinline__ GBlas bcast_blas(const GBlas& g, int src) {
-    const unsigned kAll = 0xFFFFFFFFu;
-    auto p64 = [&](const void* p) {
-        return reinterpret_cast<const void*>(__shfl_sync(kAll, reinterpret_cast<unsigned long long>(p), src));
-    };
-    GBlas o;
-    o.nodes = static_cast<const float4*>(p64(g.nodes));
-    o.tris = static_cast<const float4*>(p64(g.tris));
-    o.pairs = static_cast<const ulonglong2*>(p64(g.pairs));
-    o.hx = static_cast<const uint2*>(p64(g.hx));
-    o.cones = static_cast<const float4*>(p64(g.cones));
-    o.hwork = static_cast<const uint4*>(p64(g.hwork));
-    o.nodes_used = __shfl_sync(kAll, g.nodes_used, src);
-    o.ntris = __shfl_sync(kAll, g.ntris, src);
-    o.root_count = __shfl_sync(kAll, g.root_count, src);
-    o.root_first = __shfl_sync(kAll, g.root_first, src);
-    return o;
 }
 
 __device__ __forceinline__ void load_ray(const float4* rays, uint32_t i, float3& o, float3& d, float& t) {

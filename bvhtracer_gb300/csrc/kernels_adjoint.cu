@@ -36,7 +36,6 @@ inline GBlas to_gblas(const DeviceBlas& b) {
     g.pairs = b.pairs;
     g.hx = b.hx;
     g.cones = b.cones;
-    g.hwork = b.hwork;
     g.nodes_used = b.nodes_used;
     g.ntris = b.ntris;
     g.root_count = b.root_count;
@@ -67,10 +66,10 @@ __device__ __forceinline__ void warp_trace_local(const GBlas& b, bool active, La
                 if (group) {
                     const int bb = __ffs(group) - 1;
                     group &= group - 1u;
-                    coop_leaf_any(b, f, c, a, bb, r);
+                    coop_leaf2(b.pairs, f, c, a, bb, r);
                     if ((int)lane == a || (int)lane == bb) st = tr.pop() ? kStepFinished : kStepContinue;
                 } else {
-                    coop_leaf_any(b, f, c, a, -1, r);
+                    coop_leaf(b.pairs, f, c, a, r);
                     if ((int)lane == a) st = tr.pop() ? kStepFinished : kStepContinue;
                 }
             }

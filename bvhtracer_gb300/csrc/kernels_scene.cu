@@ -585,7 +585,6 @@ struct SceneTrav {
         blas.pairs = nullptr;
         blas.hx = nullptr;
         blas.cones = nullptr;
-        blas.hwork = nullptr;
         blas.nodes_used = blas.ntris = blas.root_count = blas.root_first = 0;
     }
 
@@ -679,7 +678,7 @@ __device__ __forceinline__ void scene_coop_phase(unsigned pend, SceneTrav<STK, T
         const uint32_t f = __shfl_sync(kFull, tr.bt.first, leader);
         const uint32_t c = __shfl_sync(kFull, tr.bt.cnt, leader);
         const unsigned long long lk = __shfl_sync(kFull, key, leader);
-        const GBlas B = bcast_blas(tr.blas, leader);
+        const ulonglong2* P = reinterpret_cast<const ulonglong2*>(lk);
         unsigned group = __ballot_sync(kFull, ((pend >> lane) & 1u) && tr.bt.first == f && key == lk);
         pend &= ~group;
         while (group) {
@@ -688,10 +687,10 @@ __device__ __forceinline__ void scene_coop_phase(unsigned pend, SceneTrav<STK, T
             if (group) {
                 const int b = __ffs(group) - 1;
                 group &= group - 1u;
-                coop_leaf_any(B, f, c, a, b, r);
+                coop_leaf2(P, f, c, a, b, r);
                 if ((int)lane == a || (int)lane == b) st = tr.after_leaf();
             } else {
-                coop_leaf_any(B, f, c, a, -1, r);
+                coop_leaf(P, f, c, a, r);
                 if ((int)lane == a) st = tr.after_leaf();
             }
         }

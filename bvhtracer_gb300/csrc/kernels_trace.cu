@@ -32,7 +32,6 @@ inline GBlas to_gblas(const DeviceBlas& b) {
     g.pairs = b.pairs;
     g.hx = b.hx;
     g.cones = b.cones;
-    g.hwork = b.hwork;
     g.nodes_used = b.nodes_used;
     g.ntris = b.ntris;
     g.root_count = b.root_count;
@@ -69,7 +68,7 @@ __device__ __forceinline__ void coop_leaf_phase(unsigned pend, const GBlas& blas
         const uint32_t f = __shfl_sync(kFull, tr.first, leader);
         const uint32_t c = __shfl_sync(kFull, tr.cnt, leader);
         const unsigned long long lk = __shfl_sync(kFull, key, leader);
-        const GBlas B = bcast_blas(blas, leader);
+        const ulonglong2* P = reinterpret_cast<const ulonglong2*>(lk);
         unsigned group = __ballot_sync(kFull, ((pend >> lane) & 1u) && tr.first == f && key == lk);
         pend &= ~group;
         while (group) {
@@ -78,13 +77,13 @@ __device__ __forceinline__ void coop_leaf_phase(unsigned pend, const GBlas& blas
             if (group) {
                 const int b = __ffs(group) - 1;
                 group &= group - 1u;
-                coop_leaf_any(B, f, c, a, b, r);
+                coop_leaf2(P, f, c, a, b, r);
                 if ((int)lane == a || (int)lane == b) {
                     if constexpr (TR::kCount) tr.cn.coop_tris += c;
                     st = tr.pop() ? kStepFinished : kStepContinue;
                 }
             } else {
-                coop_leaf_any(B, f, c, a, -1, r);
+                coop_leaf(P, f, c, a, r);
                 if ((int)lane == a) {
                     if constexpr (TR::kCount) tr.cn.coop_tris += c;
                     st = tr.pop() ? kStepFinished : kStepContinue;
@@ -361,7 +360,6 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_trace_batch_persistent(const Ba
     b.pairs = nullptr;
     b.hx = nullptr;
     b.cones = nullptr;
-    b.hwork = nullptr;
     b.nodes_used = b.ntris = b.root_count = b.root_first = 0;
     LaneRay r;
     TravT<STK> tr;
