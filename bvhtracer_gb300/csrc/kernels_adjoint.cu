@@ -17,6 +17,7 @@
 
 #include "common.cuh"
 #include "internal.hpp"
+#include "persistent.cuh"
 #include "variants.cuh"
 
 namespace bvhgpu {
@@ -41,40 +42,6 @@ inline GBlas to_gblas(const DeviceBlas& b) {
     g.root_count = b.root_count;
     g.root_first = b.root_first;
     return g;
-}
-
-template <int STACK>
-__device__ __forceinline__ void warp_trace_local(const GBlas& b, bool active, LaneRay& r, LeafPolicy pol,
-                                                 uint32_t* err) {
-    Trav<STACK> tr;
-    if (active) tr.init(b);
-    StepResult st = active ? kStepContinue : kStepFinished;
-    const unsigned lane = threadIdx.x & 31u;
-    for (;;) {
-        if (st == kStepContinue) st = tr.template advance<true>(b, r, pol, err);
-        unsigned pend = __ballot_sync(kFull, st == kStepBigLeaf);
-        if (pend == 0u) break;
-        while (pend) {
-            const int leader = __ffs(pend) - 1;
-            const uint32_t f = __shfl_sync(kFull, tr.first, leader);
-            const uint32_t c = __shfl_sync(kFull, tr.cnt, leader);
-            unsigned group = __ballot_sync(kFull, ((pend >> lane) & 1u) && tr.first == f);
-            pend &= ~group;
-            while (group) {
-                const int a = __ffs(group) - 1;
-                group &= group - 1u;
-                if (group) {
-                    const int bb = __ffs(group) - 1;
-                    group &= group - 1u;
-                    coop_leaf2(b.pairs, f, c, a, bb, r);
-                    if ((int)lane == a || (int)lane == bb) st = tr.pop() ? kStepFinished : kStepContinue;
-                } else {
-                    coop_leaf(b.pairs, f, c, a, r);
-                    if ((int)lane == a) st = tr.pop() ? kStepFinished : kStepContinue;
-                }
-            }
-        }
-    }
 }
 
 struct Shade {
@@ -139,39 +106,74 @@ __global__ void k_mesh_tris(const float* __restrict__ verts, const uint32_t* __r
     for (int k = 0; k < 9; ++k) P[2 * k] = comp[k];
 }
 
-template <int STACK>
-__global__ void __launch_bounds__(kBlock) k_lambert_forward(GBlas b, const float4* __restrict__ rays, uint32_t n,
-                                                            const uint32_t* __restrict__ faces,
-                                                            const float* __restrict__ verts,
-                                                            const float* __restrict__ vnormals, float3 light,
-                                                            float* __restrict__ image, GHit* __restrict__ hits,
-                                                            LeafPolicy pol, uint32_t* err) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (__all_sync(kFull, i >= n)) return;
-    const bool active = i < n;
+// Forward pass, persistent: each warp keeps 32 pixel slots and refills the finished ones from a
+// global queue (ballot -> one atomicAdd per warp -> shfl), so that lanes whose pixel missed the
+// mesh or finished early take new pixels instead of idling until the slowest ray of their block
+// is done.  A finished pixel stores its hit record (the adjoint's checkpoint) and its intensity.
+template <int BLOCK, int MINB, class STK>
+__global__ void __launch_bounds__(BLOCK, MINB) k_lambert_forward(GBlas b, const float4* __restrict__ rays, uint32_t n,
+                                                                 const uint32_t* __restrict__ faces,
+                                                                 const float* __restrict__ verts,
+                                                                 const float* __restrict__ vnormals, float3 light,
+                                                                 float* __restrict__ image, GHit* __restrict__ hits,
+                                                                 uint32_t* queue, LeafPolicy pol, uint32_t refill,
+                                                                 uint32_t* err) {
+    extern __shared__ uint2 stack_smem[];
+    const unsigned lane = threadIdx.x & 31u;
+    int phase = 0;  // 0 needs a pixel, 1 tracing, 3 retired
+    uint32_t idx = 0;
     LaneRay r;
-    float3 o = make_float3(0, 0, 0), d = o;
-    if (active) {
-        float t0;
-        load_ray(rays, i, o, d, t0);
-        r.o = o;
-        r.d = d;
-        r.rd = recip3(d);
-        r.ct = t0;
-        r.hu = r.hv = 0.0f;
-        r.hp = 0;
-        r.hit = false;
+    TravT<STK> tr;
+    tr.stk.bind(stack_smem);
+    StepResult st = kStepFinished;
+    bool queue_open = true;
+    for (;;) {
+        const unsigned need = __ballot_sync(kFull, phase == 0);
+        const unsigned busy = __ballot_sync(kFull, phase == 1);
+        // refill once `refill` lanes are idle (or none is busy)
+        if (need != 0u && ((uint32_t)__popc(need) >= refill || busy == 0u)) {
+            const int leader = __ffs(need) - 1;
+            uint32_t base = 0;
+            if ((int)lane == leader) base = atomicAdd(queue, (uint32_t)__popc(need));
+            base = __shfl_sync(kFull, base, leader);
+            if (base + (uint32_t)__popc(need) >= n) queue_open = false;
+            if (phase == 0) {
+                const uint32_t my = base + __popc(need & ((1u << lane) - 1u));
+                if (my < n) {
+                    idx = my;
+                    float3 o, d;
+                    float t0;
+                    load_ray(rays, idx, o, d, t0);
+                    init_lane_ray(r, o, d, t0);
+                    tr.init(b);
+                    st = kStepContinue;
+                    phase = 1;
+                } else {
+                    phase = 3;
+                }
+            }
+        }
+        if (phase == 1) {
+            if (st == kStepContinue) st = tr.advance(b, r, pol, err);
+            if (st == kStepFinished) {
+                const bool hit = r.hit && r.ct < FLT_MAX;
+                store_hit(hits, idx, hit, r.ct, r.hu, r.hv, r.hp, 0u);
+                float I = 0.0f;
+                if (hit) {
+                    Shade sh;
+                    I = shade(r.o, r.d, r.ct, r.hu, r.hv, faces, r.hp, verts, vnormals, light, sh);
+                }
+                image[idx] = I;
+                phase = 0;
+            }
+        }
+        const unsigned pend = __ballot_sync(kFull, phase == 1 && st == kStepBigLeaf);
+        if (pend == 0u) {
+            if (!queue_open && __ballot_sync(kFull, phase == 0 || phase == 1) == 0u) break;
+            continue;
+        }
+        coop_leaf_phase(pend, b, tr, r, st);
     }
-    warp_trace_local<STACK>(b, active, r, pol, err);
-    if (!active) return;
-    const bool hit = r.hit && r.ct < FLT_MAX;
-    store_hit(hits, i, hit, r.ct, r.hu, r.hv, r.hp, 0u);
-    float I = 0.0f;
-    if (hit) {
-        Shade s;
-        I = shade(o, d, r.ct, r.hu, r.hv, faces, r.hp, verts, vnormals, light, s);
-    }
-    image[i] = I;
 }
 
 // Per-block partial sums of (I - T)^2 in double.
@@ -240,13 +242,6 @@ __global__ void k_sgd(float* __restrict__ verts, float* __restrict__ grad, uint3
     grad[i] = 0.0f;
 }
 
-inline int stack_variant(uint32_t depth) {
-    if (depth <= 33) return 32;
-    if (depth <= 65) return 64;
-    if (depth <= 129) return 128;
-    return 256;
-}
-
 }  // namespace
 
 cudaError_t launch_mesh_update(bvhgpu_ctx* ctx, DeviceMesh& m, DeviceBlas& b, cudaStream_t s) {
@@ -267,25 +262,25 @@ cudaError_t launch_lambert_forward(bvhgpu_ctx* ctx, DeviceMesh& m, const DeviceB
     if (n == 0) return cudaSuccess;
     GBlas g = to_gblas(b);
     float3 L = make_float3(light[0], light[1], light[2]);
-    // the leaf policy (big leaves, hidden-tree margin) of the plain trace kernel's launch config
-    const LeafPolicy pol = resolve(ctx->tune[BVHGPU_K_TRACE_BLAS], b.depth).pol;
+    // the launch shape, stack and leaf policy (big leaves, hidden-tree margin) of the plain trace
+    // kernel's launch config, and its refill threshold
+    const Variant v = resolve(ctx->tune[BVHGPU_K_TRACE_BLAS], b.depth);
+    uint32_t* queue = ctx->d_scratch + 5;
+    cudaError_t e = cudaMemsetAsync(queue, 0, sizeof(uint32_t), s);
+    if (e != cudaSuccess) return e;
     LaunchScope scope(ctx, BVHGPU_K_LAMBERT_FORWARD, s);
-    switch (stack_variant(b.depth)) {
-        case 32:
-            k_lambert_forward<32><<<grid_for(n, kBlock), kBlock, 0, s>>>(g, rays, n, m.faces, m.verts, m.vnormals, L,
-                                                                         image, static_cast<GHit*>(hits), pol, ctx->d_err);
-            break;
-        case 64:
-            k_lambert_forward<64><<<grid_for(n, kBlock), kBlock, 0, s>>>(g, rays, n, m.faces, m.verts, m.vnormals, L,
-                                                                         image, static_cast<GHit*>(hits), pol, ctx->d_err);
-            break;
-        default:
-            k_lambert_forward<256><<<grid_for(n, kBlock), kBlock, 0, s>>>(g, rays, n, m.faces, m.verts, m.vnormals, L,
-                                                                          image, static_cast<GHit*>(hits), pol, ctx->d_err);
-            break;
-    }
+    e = with_variant(v.shape, v.stack, [&](auto sh, auto tg) {
+        using SH = decltype(sh);
+        using STK = typename decltype(tg)::type;
+        auto* k = k_lambert_forward<SH::block, SH::minb, STK>;
+        const size_t smem = stack_smem_bytes<STK>(SH::block);
+        k<<<persistent_grid(ctx, k, SH::block, smem), SH::block, smem, s>>>(
+            g, rays, n, m.faces, m.verts, m.vnormals, L, image, static_cast<GHit*>(hits), queue, v.pol, v.refill,
+            ctx->d_err);
+        return cudaGetLastError();
+    });
     g_launches++;
-    return cudaGetLastError();
+    return e;
 }
 
 cudaError_t launch_mse_partials(bvhgpu_ctx* ctx, const float* image, const float* target, uint32_t n, double* partials,

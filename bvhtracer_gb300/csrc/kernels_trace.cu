@@ -14,6 +14,7 @@
 
 #include "common.cuh"
 #include "internal.hpp"
+#include "persistent.cuh"
 #include "variants.cuh"
 
 namespace bvhgpu {
@@ -55,44 +56,6 @@ inline unsigned grid_for(uint32_t n, int block) { return (unsigned)((n + block -
 // (coop_leaf), one waiting ray at a time.  All 32 lanes stay in the loop until every ray of
 // the warp has finished, so the cooperative step always has the full warp.
 
-// Cooperative leaf phase: lanes waiting on the same leaf form a group; the group's rays are
-// tested two at a time (coop_leaf2 shares each loaded triangle pair between the two rays), an
-// odd one alone.  `key` identifies the BLAS (pairs pointer) so that different scenes of a batch
-// never share a leaf.
-template <class TR>
-__device__ __forceinline__ void coop_leaf_phase(unsigned pend, const GBlas& blas, TR& tr, LaneRay& r, StepResult& st) {
-    const unsigned lane = threadIdx.x & 31u;
-    const unsigned long long key = reinterpret_cast<unsigned long long>(blas.pairs);
-    while (pend) {
-        const int leader = __ffs(pend) - 1;
-        const uint32_t f = __shfl_sync(kFull, tr.first, leader);
-        const uint32_t c = __shfl_sync(kFull, tr.cnt, leader);
-        const unsigned long long lk = __shfl_sync(kFull, key, leader);
-        const ulonglong2* P = reinterpret_cast<const ulonglong2*>(lk);
-        unsigned group = __ballot_sync(kFull, ((pend >> lane) & 1u) && tr.first == f && key == lk);
-        pend &= ~group;
-        while (group) {
-            const int a = __ffs(group) - 1;
-            group &= group - 1u;
-            if (group) {
-                const int b = __ffs(group) - 1;
-                group &= group - 1u;
-                coop_leaf2(P, f, c, a, b, r);
-                if ((int)lane == a || (int)lane == b) {
-                    if constexpr (TR::kCount) tr.cn.coop_tris += c;
-                    st = tr.pop() ? kStepFinished : kStepContinue;
-                }
-            } else {
-                coop_leaf(P, f, c, a, r);
-                if ((int)lane == a) {
-                    if constexpr (TR::kCount) tr.cn.coop_tris += c;
-                    st = tr.pop() ? kStepFinished : kStepContinue;
-                }
-            }
-        }
-    }
-}
-
 // Traces the rays of one warp (inactive lanes take part in the cooperative steps only).
 template <class STK>
 __device__ __forceinline__ void warp_trace(const GBlas& b, bool active, LaneRay& r, LeafPolicy pol, uint32_t* err,
@@ -107,16 +70,6 @@ __device__ __forceinline__ void warp_trace(const GBlas& b, bool active, LaneRay&
         if (pend == 0u) break;
         coop_leaf_phase(pend, b, tr, r, st);
     }
-}
-
-__device__ __forceinline__ void init_lane_ray(LaneRay& r, float3 o, float3 d, float t) {
-    r.o = o;
-    r.d = d;
-    r.rd = recip3(d);
-    r.ct = t;
-    r.hu = r.hv = 0.0f;
-    r.hp = 0;
-    r.hit = false;
 }
 
 // ---- plain -------------------------------------------------------------------------------
@@ -615,14 +568,6 @@ __global__ void __launch_bounds__(64) k_render(GBlas b, RenderParams P, const fl
             break;
     }
     reinterpret_cast<uchar4*>(rgba)[(size_t)y * P.width + x] = c;
-}
-
-template <class K>
-int persistent_grid(bvhgpu_ctx* ctx, K kernel, int block, size_t smem) {
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, smem);
-    if (per_sm < 1) per_sm = 1;
-    return per_sm * ctx->num_sms;
 }
 
 }  // namespace
