@@ -101,6 +101,27 @@ def setup_workload():
     return tris, bvh, rays
 
 
+TUNE_FIELDS = ("block", "min_blocks", "stack", "big_leaf", "refill", "hidden")
+
+
+def apply_tune_args(ctx, args) -> dict:
+    """Launch configs given with --tune KERNEL=block,min_blocks,stack,big_leaf,refill,hidden
+    (e.g. the picks printed by an earlier tuned run), set on the context before any launch."""
+    import bvhtracer_gb300 as bt
+    given = {}
+    for spec in args.tune or []:
+        name, _, vals = spec.partition("=")
+        if name not in bt._KERNELS:
+            raise SystemExit(f"--tune: unknown kernel {name!r} (one of {', '.join(bt._KERNELS)})")
+        nums = [int(v) for v in vals.split(",")]
+        if len(nums) != len(TUNE_FIELDS):
+            raise SystemExit(f"--tune {spec}: expected {len(TUNE_FIELDS)} values ({','.join(TUNE_FIELDS)})")
+        cfg = dict(zip(TUNE_FIELDS, nums))
+        ctx.tune_set(bt._KERNELS.index(name), **cfg)
+        given[name] = dict(cfg, source="--tune")
+    return given
+
+
 def measured_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -214,6 +235,7 @@ def run_ours(args):
     tris, bvh, rays = setup_workload()
     n = len(rays)
     ctx = bt.Context(local_rank)
+    given = apply_tune_args(ctx, args)
     blas = ctx.upload_blas(bvh, tris)
     d_rays = ctx.to_device(rays)
     d_h0 = ctx.device_buffer(n * bt.HIT.itemsize)
@@ -230,7 +252,7 @@ def run_ours(args):
     rays_per_step = n + n_bounce
 
     # autotune both pipelines on this frame (configs never change results, only speed)
-    tuned, tune_s = {}, 0.0
+    tuned, tune_s = dict(given), 0.0
     if not args.no_tune:
         t0 = time.perf_counter()
         cfg, ms_ = ctx.autotune(bt.K_PERSISTENT_BOUNCE, d_rays, n, d_h0, d_h1, target=blas.id, seed=BOUNCE_SEED,
@@ -468,6 +490,7 @@ def run_batch(args):
     built = setup_batch(args.scenes)
     setup_s = time.perf_counter() - t0
     ctx = bt.Context(local_rank)
+    given = apply_tune_args(ctx, args)
     # the same 64 SAH builds on the GPU (BvhBuilder::build_for on the device), checked bit for bit
     # against the host builds above
     t0 = time.perf_counter()
@@ -494,7 +517,7 @@ def run_batch(args):
     ev = [(ctx.event(), ctx.event()) for _ in range(args.steps)]
 
     # autotune on a 1/16 sample of every scene (its first primaries and first random rays)
-    tuned, tune_s = {}, 0.0
+    tuned, tune_s = dict(given), 0.0
     if not args.no_tune:
         t0 = time.perf_counter()
         s_items = np.zeros(len(built), bt.BATCH_ITEM)
@@ -626,6 +649,7 @@ def run_adjoint(args):
     verts, faces, vn, tverts, rays, light = scenes.config4(seed=SEED)
     n = len(rays)
     ctx = bt.Context(local_rank)
+    given = apply_tune_args(ctx, args)
     m = bt.DiffMesh(ctx, verts, faces, vn)
     d_rays = ctx.to_device(rays)
     d_img = ctx.device_buffer(4 * n)
@@ -697,7 +721,8 @@ def run_adjoint(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": sum(tot) / len(tot), "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
         "config": {"workload": WORKLOAD4, "pixels": n, "triangles": int(len(faces)), "vertices": int(len(verts)),
-                   "bvh_nodes": m.bvh.nodes_used, "l2": "flushed between steps (256 MB memset)", "seed": SEED},
+                   "bvh_nodes": m.bvh.nodes_used, "l2": "flushed between steps (256 MB memset)", "seed": SEED,
+                   "tuned": given},
         "adjoint": {"forward_ms": fwd_ms, "adjoint_ms": adj_ms, "update_refit_ms": sum(upd) / len(upd),
                     "step_ms": sum(tot) / len(tot), "adjoint_over_forward": adj_ms / fwd_ms,
                     "forward_mrays_per_s": n / fwd_ms / 1e3,
@@ -723,6 +748,7 @@ def run_frames(args):
     cfg = scenes.config2(seed=SEED)
     nframes = 60
     ctx = bt.Context(local_rank)
+    given = apply_tune_args(ctx, args)
     sc = AnimatedScene(ctx, cfg)
     n = sc.n
     # one profiled frame outside the graph (per-kernel breakdown), then capture
@@ -735,7 +761,7 @@ def run_frames(args):
     ctx.sync()
     prof = ctx.profile_read()
     ctx.profile(False)
-    tuned, tune_s = {}, 0.0
+    tuned, tune_s = dict(given), 0.0
     if not args.no_tune:  # tune the frame's trace kernel before the graph captures its launch
         t0 = time.perf_counter()
         cfg_t, ms_ = ctx.autotune(bt.K_SCENE_BOUNCE, sc.d_rays, n, sc.d_hits0, sc.d_hits1, target=sc.scene.id,
@@ -809,11 +835,16 @@ def main():
     ap.add_argument("--scenes", type=int, default=64,
                     help="config 3: number of scenes (64 = the workload; fewer only for small profiling runs)")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (use the default launch configs)")
+    ap.add_argument("--tune", action="append", metavar="KERNEL=B,M,S,L,R,H",
+                    help="set a kernel's launch config (block, min_blocks, stack, big_leaf, refill, hidden) and "
+                         "skip the autotuner, e.g. to profile the configs an earlier tuned run picked; repeatable")
     ap.add_argument("--no-cpu-baseline", action="store_true",
                     help="skip the CPU-baseline leg (outside the timed region), e.g. under a profiler")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.tune:
+        args.no_tune = True
     if args.impl == "reference":
         return run_reference(args)
     if args.config == 2:

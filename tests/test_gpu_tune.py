@@ -1,5 +1,5 @@
-"""Launch configurations: every compiled variant of the five traversal kernels (launch shape x
-stack) with both leaf layouts, hidden trees on and off and two refill sizes gives the oracle's hits
+"""Launch configurations: every compiled variant of the five traversal kernels and the Lambertian
+forward pass (launch shape x stack) with both leaf layouts, hidden trees on and off and two refill sizes gives the oracle's hits
 bit for bit, and the autotuner returns a config from the search space under which the results are
 unchanged."""
 import numpy as np
@@ -95,6 +95,35 @@ def random_instances(n, seed):
     inv = np.linalg.inv(M)
     return (np.ascontiguousarray(M.transpose(0, 2, 1).reshape(n, 16), np.float32),
             np.ascontiguousarray(inv.transpose(0, 2, 1).reshape(n, 16), np.float32))
+
+
+def test_lambert_forward_every_variant(ctx):
+    """The persistent Lambertian forward pass runs under the single-ray trace kernel's config:
+    every variant gives the oracle's hits and one and the same image."""
+    verts, faces, vn, _, rays, light = scenes.config4(seed=4, level=5, width=64, height=64)
+    n = len(rays)
+    m = bt.DiffMesh(ctx, verts, faces, vn)
+    d_rays = ctx.to_device(rays)
+    d_img = ctx.device_buffer(4 * n)
+    d_hits = ctx.device_buffer(bt.HIT.itemsize * n)
+    ref = orc.bvh_intersect(m.bvh.nodes, m.bvh.nodes_used, m.tris, rays, threads=8)
+    default = ctx.tune_get(bt.K_TRACE_BLAS)
+    image = None
+    try:
+        for cfg in subset(bt.K_TRACE_BLAS):
+            ctx.tune_set(bt.K_TRACE_BLAS, **cfg)
+            d_img.zero()
+            m.forward_async(d_rays, n, light, d_img, d_hits)
+            ctx.sync()
+            h = d_hits.download(np.zeros(n, bt.HIT))
+            img = d_img.download(np.zeros(n, np.float32))
+            assert h.tobytes() == ref.tobytes(), f"lambert forward {cfg}"
+            if image is None:
+                image = img
+            assert img.tobytes() == image.tobytes(), f"lambert forward image {cfg}"
+        assert (ref["prim"] != bt.MISS).mean() > 0.2
+    finally:
+        ctx.tune_set(bt.K_TRACE_BLAS, **default)
 
 
 def test_scene_kernels_every_variant(ctx):
