@@ -363,7 +363,8 @@ int bvhgpu_mesh_set_vertices(bvhgpu_ctx* ctx, uint32_t mesh_id, const float* ver
 int bvhgpu_mesh_update_async(bvhgpu_ctx* ctx, uint32_t mesh_id, bvhgpu_stream s);
 /* Forward: closest hit per ray, hit records {t, u, v, prim} written to d_hits (the checkpoint the
  * adjoint reuses), image[i] = max(0, n_hat . l_hat) with n the barycentric vertex normal and l the
- * direction from the hit point to the point light `light` (0 for a miss). */
+ * direction from the hit point to the point light `light` (0 for a miss).  One persistent launch
+ * under the BVHGPU_K_TRACE_BLAS launch config (shape, stack, leaf policy, refill). */
 int bvhgpu_lambert_forward_async(bvhgpu_ctx* ctx, uint32_t mesh_id, const bvhgpu_ray* d_rays, uint32_t n,
                                  const float light[3], float* d_image, bvhgpu_hit* d_hits, bvhgpu_stream s);
 /* Mean squared error between image and target (n floats each, device), computed on the device in
