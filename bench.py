@@ -391,9 +391,9 @@ def run_ours(args):
                           "reference_algorithm_bytes_per_launch": alg_bytes,
                           "reference_algorithm_frac": alg_bytes / per_launch_s / 1e9 / peak,
                           "reference_counters": counters,
-                          "note": "the bytes are fetched mostly from L1 / L2 (ncu: L1 hit 96 %), so the HBM "
+                          "note": "the bytes are fetched mostly from L1 / L2 (ncu: L1 hit 93 %), so the HBM "
                                   "fraction is a data-movement rate, not HBM-bound; the kernel is bound by "
-                                  "divergence and latency (ncu: SIMT 10.6 of 32, issue 53 %)"}
+                                  "divergence and latency (ncu: SIMT 13.9 of 32, issue 55 %)"}
     print(json.dumps(result), flush=True)
     return 0
 
@@ -420,9 +420,9 @@ def fetched_bytes(ctx, blas, rays, seed):
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of each bench's dominant
 # kernel, from the ncu captures summarised under profiles/ (the command is in each summary).
 NCU_TRAFFIC = {
-    "persistent_bounce": (75.980288e6 + 48.580864e6, "ncu capture of the 1080p frame",
+    "persistent_bounce": (76.082432e6 + 50.145280e6, "ncu capture of the 1080p frame",
                           "profiles/k_persistent_bounce_config1_full.md"),
-    # 8-scene capture (10,057,687 rays, 523.2 MB: 52 B of ray in + hit out per ray, the BVHs once)
+    # 8-scene capture (10,057,687 rays, 573.0 MB: 52 B of ray in + hit out per ray, the BVHs once)
     # scaled to the 64-scene launch: 52 B x rays + 88 B x triangles (tris + pairs, read once)
     "trace_batch": (None, "8-scene ncu capture scaled by rays and triangles",
                     "profiles/k_trace_batch_persistent_config3.md"),
