@@ -113,7 +113,10 @@ def apply_tune_args(ctx, args) -> dict:
         name, _, vals = spec.partition("=")
         if name not in bt._KERNELS:
             raise SystemExit(f"--tune: unknown kernel {name!r} (one of {', '.join(bt._KERNELS)})")
-        nums = [int(v) for v in vals.split(",")]
+        try:
+            nums = [int(v) for v in vals.split(",")]
+        except ValueError:
+            nums = []
         if len(nums) != len(TUNE_FIELDS):
             raise SystemExit(f"--tune {spec}: expected {len(TUNE_FIELDS)} values ({','.join(TUNE_FIELDS)})")
         cfg = dict(zip(TUNE_FIELDS, nums))

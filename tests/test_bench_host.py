@@ -1,0 +1,80 @@
+"""bench.py host logic on the CPU: the --tune launch-config option and the byte basis of the
+roofline (node + triangle bytes fetched per ray, from the device counters)."""
+import importlib.util
+import os
+
+import numpy as np
+import pytest
+
+import bvhtracer_gb300 as bt
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def bench():
+    spec = importlib.util.spec_from_file_location("bench_under_test", os.path.join(ROOT, "bench.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+class FakeCtx:
+    """Records tune_set calls; hands out placeholder device buffers."""
+
+    def __init__(self):
+        self.calls = []
+
+    def tune_set(self, kernel, **cfg):
+        self.calls.append((kernel, cfg))
+
+    def to_device(self, arr):
+        return ("device", len(arr))
+
+    def device_buffer(self, nbytes):
+        return ("buffer", nbytes)
+
+
+class Args:
+    def __init__(self, tune):
+        self.tune = tune
+
+
+def test_tune_option_sets_each_kernel(bench):
+    ctx = FakeCtx()
+    given = bench.apply_tune_args(ctx, Args(["trace_batch=128,6,256,16,8,100", "trace_blas=64,1,32,8,1,0"]))
+    assert ctx.calls == [
+        (bt.K_TRACE_BATCH, dict(block=128, min_blocks=6, stack=256, big_leaf=16, refill=8, hidden=100)),
+        (bt.K_TRACE_BLAS, dict(block=64, min_blocks=1, stack=32, big_leaf=8, refill=1, hidden=0)),
+    ]
+    assert given["trace_batch"]["source"] == "--tune" and given["trace_blas"]["hidden"] == 0
+    assert bench.apply_tune_args(FakeCtx(), Args(None)) == {}
+
+
+@pytest.mark.parametrize("spec", ["no_such_kernel=128,5,256,16,8,2000", "trace_blas=128,5", "trace_blas"])
+def test_tune_option_rejects_bad_specs(bench, spec):
+    with pytest.raises(SystemExit):
+        bench.apply_tune_args(FakeCtx(), Args([spec]))
+
+
+def test_fetched_bytes_basis(bench):
+    """64 B per reference node, 32 B per hidden box, 40 B per hidden-tree entry, 32 B per cone
+    switch, 88 B per hidden pair, 48 / 40 B per lane / warp triangle, 52 B of ray + hit per ray."""
+    counts = {"ref_nodes": 10, "hidden_boxes": 20, "hidden_entries": 1, "hidden_pairs": 3, "lane_tris": 2,
+              "warp_tris": 5, "cone_switches": 4}
+
+    class FakeBlas:
+        def bounce_rays(self, rays, seed):
+            valid = np.zeros(len(rays), bool)
+            valid[:1] = True
+            return rays.copy(), valid
+
+        def trace_counts(self, d_rays, n, d_hits):
+            return dict(counts)
+
+    rays = np.zeros(2, bt.RAY)
+    out = bench.fetched_bytes(FakeCtx(), FakeBlas(), rays, 0)
+    per_call = 64 * 10 + 32 * 20 + 40 * 1 + 32 * 4 + 88 * 3 + 48 * 2 + 40 * 5
+    assert out["primary"]["rays"] == 2 and out["primary"]["bytes"] == per_call + 52 * 2
+    assert out["bounce"]["rays"] == 1 and out["bounce"]["bytes"] == per_call + 52
+    assert out["primary"]["per_ray"]["hidden_boxes"] == 10.0
