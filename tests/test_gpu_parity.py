@@ -1,7 +1,7 @@
 """GPU parity: the CUDA library through its C ABI against the CPU oracle.
 
 Bar: identical hit primitive / instance ids and bit-identical t, u, v (the kernels follow
-the reference's f32 operation order, so no tolerance is needed; the benchmark spec's tolerance
+the reference's f32 operation order, so no tolerance is needed; the path's stated tolerance
 of 1e-5 relative is asserted as well for the record), bit-identical refit nodes and TLAS
 nodes, identical images.
 """
@@ -13,7 +13,7 @@ from bvhtracer_gb300 import scenes
 from oracle import oracle as orc
 
 pytestmark = pytest.mark.gpu
-REL_TOL = 1e-5  # spec tolerance for t/u/v; the kernels are expected to be bit-exact
+REL_TOL = 1e-5  # the stated tolerance for t/u/v; the kernels are expected to be bit-exact
 
 
 @pytest.fixture(scope="module")
