@@ -96,7 +96,7 @@ class Clocks:
 def setup_workload():
     import bvhtracer_gb300 as bt
     from bvhtracer_gb300 import scenes
-    tris, rays, _ = scenes.config1(seed=SEED)
+    tris, rays, _ = scenes.icosphere_frame(seed=SEED)
     bvh = bt.BvhBuilder().build_for(tris)
     return tris, bvh, rays
 
@@ -424,11 +424,11 @@ def fetched_bytes(ctx, blas, rays, seed):
 # kernel, from the ncu captures summarised under profiles/ (the command is in each summary).
 NCU_TRAFFIC = {
     "persistent_bounce": (76.082432e6 + 50.145280e6, "ncu capture of the 1080p frame",
-                          "profiles/k_persistent_bounce_config1_full.md"),
+                          "profiles/k_persistent_bounce_icosphere_1080p_full.md"),
     # 8-scene capture (10,057,687 rays, 573.0 MB: 52 B of ray in + hit out per ray, the BVHs once)
     # scaled to the 64-scene launch: 52 B x rays + 88 B x triangles (tris + pairs, read once)
     "trace_batch": (None, "8-scene ncu capture scaled by rays and triangles",
-                    "profiles/k_trace_batch_persistent_config3.md"),
+                    "profiles/k_trace_batch_persistent_64_scene_batch.md"),
 }
 
 
@@ -441,10 +441,10 @@ def setup_batch(nscenes: int = 64, seed: int = SEED):
     import bvhtracer_gb300 as bt
     from concurrent.futures import ThreadPoolExecutor
     from bvhtracer_gb300 import scenes
-    ntris, nrays = scenes.config3_specs(seed, nscenes)
+    ntris, nrays = scenes.batch_specs(seed, nscenes)
 
     def make(i):
-        tris, rays = scenes.config3_scene(i, int(ntris[i]), int(nrays[i]), seed)
+        tris, rays = scenes.batch_scene(i, int(ntris[i]), int(nrays[i]), seed)
         original = tris.copy()
         bvh = bt.BvhBuilder().build_for(tris)
         return tris, bvh, rays, original
@@ -649,7 +649,7 @@ def run_adjoint(args):
     import bvhtracer_gb300 as bt
     from bvhtracer_gb300 import scenes
     rank, world, local_rank = dist_env()
-    verts, faces, vn, tverts, rays, light = scenes.config4(seed=SEED)
+    verts, faces, vn, tverts, rays, light = scenes.lambert_scene(seed=SEED)
     n = len(rays)
     ctx = bt.Context(local_rank)
     given = apply_tune_args(ctx, args)
@@ -748,7 +748,7 @@ def run_frames(args):
     from bvhtracer_gb300 import scenes
     from bvhtracer_gb300.frames import AnimatedScene
     rank, world, local_rank = dist_env()
-    cfg = scenes.config2(seed=SEED)
+    cfg = scenes.instanced_animation(seed=SEED)
     nframes = 60
     ctx = bt.Context(local_rank)
     given = apply_tune_args(ctx, args)
@@ -832,11 +832,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--mode", choices=["persistent", "plain"], default="persistent")
-    ap.add_argument("--config", type=int, choices=[1, 2, 3, 4], default=1,
-                    help="1: displaced icosphere frame + bounce (default); 2: instanced animated frames in a CUDA "
-                         "graph; 3: uneven 64-scene batch; 4: differentiable render (adjoint ms/step)")
+    ap.add_argument("--workload", choices=["icosphere", "instanced", "batch", "lambert"], default="icosphere",
+                    help="icosphere: 81,920-triangle displaced icosphere, 1920x1080 primaries + bounce (default); "
+                         "instanced: 256 instances of 3 BLASes, 60 animated 1280x720 frames in a CUDA graph; "
+                         "batch: uneven 64-scene batch; lambert: differentiable render of 327,680 triangles at "
+                         "512x512 (adjoint ms/step)")
     ap.add_argument("--scenes", type=int, default=64,
-                    help="config 3: number of scenes (64 = the workload; fewer only for small profiling runs)")
+                    help="batch: number of scenes (64 = the workload; fewer only for small profiling runs)")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (use the default launch configs)")
     ap.add_argument("--tune", action="append", metavar="KERNEL=B,M,S,L,R,H",
                     help="set a kernel's launch config (block, min_blocks, stack, big_leaf, refill, hidden) and "
@@ -850,11 +852,11 @@ def main():
         args.no_tune = True
     if args.impl == "reference":
         return run_reference(args)
-    if args.config == 2:
+    if args.workload == "instanced":
         return run_frames(args)
-    if args.config == 3:
+    if args.workload == "batch":
         return run_batch(args)
-    if args.config == 4:
+    if args.workload == "lambert":
         return run_adjoint(args)
     return run_ours(args)
 

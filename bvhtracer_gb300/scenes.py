@@ -193,9 +193,9 @@ def sphere_rays(n: int, seed: int, box: float = 10.0) -> np.ndarray:
     return make_rays(o, d)
 
 
-# ---- the benchmark configurations ---------------------------------------------------------------
+# ---- the benchmark workloads ---------------------------------------------------------------------
 
-def config0(seed: int = 0):
+def soup_frame(seed: int = 0):
     """4096-triangle soup, camera (0,0,-18) through the plane z = -15 spanning [-1,1]^2,
     640 x 640 pixel-centre rays."""
     tris = soup(4096, seed)
@@ -203,7 +203,7 @@ def config0(seed: int = 0):
     return tris, rays
 
 
-def config1(seed: int = 0, width: int = 1920, height: int = 1080):
+def icosphere_frame(seed: int = 0, width: int = 1920, height: int = 1080):
     """Displaced icosphere, 6 subdivisions (81,920 triangles), camera at distance 3,
     1920 x 1080 primaries (a cosine bounce per hit pixel is generated on the GPU)."""
     mesh = displaced_icosphere(6, seed)
@@ -212,7 +212,7 @@ def config1(seed: int = 0, width: int = 1920, height: int = 1080):
     return tris, rays, mesh
 
 
-def config3_specs(seed: int = 0, nscenes: int = 64, tri_range=(1_000, 2_000_000), ray_range=(65_536, 4_194_304)):
+def batch_specs(seed: int = 0, nscenes: int = 64, tri_range=(1_000, 2_000_000), ray_range=(65_536, 4_194_304)):
     """Sizes of the uneven batch: triangle and ray counts log-uniform in the given ranges."""
     u_t = uniform(seed, 30, nscenes)
     u_r = uniform(seed, 31, nscenes)
@@ -221,8 +221,8 @@ def config3_specs(seed: int = 0, nscenes: int = 64, tri_range=(1_000, 2_000_000)
     return np.round(np.exp(lt)).astype(np.int64), np.round(np.exp(lr)).astype(np.int64)
 
 
-def config3_scene(i: int, ntris: int, nrays: int, seed: int = 0):
-    """Scene i of the uneven batch: even i a config-0-style soup grown to `ntris` triangles
+def batch_scene(i: int, ntris: int, nrays: int, seed: int = 0):
+    """Scene i of the uneven batch: even i a soup (the soup_frame formula) grown to `ntris` triangles
     (box scaled by (ntris/4096)^(1/3)), odd i a displaced icosphere at the subdivision level
     nearest to `ntris`; rays: half pinhole primaries (tile order), half origins
     U[-10, 10]^3 (times the scene scale) with uniform-sphere directions."""
@@ -245,9 +245,9 @@ def config3_scene(i: int, ntris: int, nrays: int, seed: int = 0):
     return tris, np.concatenate([prim, rnd])
 
 
-def config4(seed: int = 0, level: int = 7, width: int = 512, height: int = 512, sigma: float = 0.01,
+def lambert_scene(seed: int = 0, level: int = 7, width: int = 512, height: int = 512, sigma: float = 0.01,
             scale: float = 10.0):
-    """Differentiable-render workload: displaced icosphere (config-1 displacement) with `level`
+    """Differentiable-render workload: displaced icosphere (icosphere_frame's displacement) with `level`
     subdivisions, its radial unit directions as fixed vertex normals, a target mesh whose vertices
     are moved radially by N(0, sigma^2), a point light at (2, 2, -3), and width x height
     pixel-centre primaries from distance 3 (tile order) -- all lengths multiplied by `scale`.
@@ -266,8 +266,8 @@ def config4(seed: int = 0, level: int = 7, width: int = 512, height: int = 512, 
     return verts, mesh.faces.astype(np.uint32), vnormals, target_verts, rays, light
 
 
-def config2(seed: int = 0, ninstances: int = 256, width: int = 1280, height: int = 720, levels=(4, 5, 6)):
-    """Instanced animated scene: three displaced icospheres (config-1 displacement) at the given
+def instanced_animation(seed: int = 0, ninstances: int = 256, width: int = 1280, height: int = 720, levels=(4, 5, 6)):
+    """Instanced animated scene: three displaced icospheres (icosphere_frame's displacement) at the given
     subdivision levels, `ninstances` instances (instance i uses mesh i % 3) with a seeded random
     rotation, uniform scale U[0.5, 2] and translation in a 40^3 box; per frame (dt = 1/30 s) each
     instance turns about a seeded axis at U[-1, 1] rad/s and every vertex wobbles radially by

@@ -31,7 +31,7 @@ def rel_err(a, b):
 
 @pytest.mark.parametrize("level,size", [(5, 128), (7, 512)])
 def test_lambert_forward_adjoint_against_fp64(level, size):
-    verts, faces, vn, tverts, rays, light = scenes.config4(seed=3, level=level, width=size, height=size)
+    verts, faces, vn, tverts, rays, light = scenes.lambert_scene(seed=3, level=level, width=size, height=size)
     n = len(rays)
     with bt.Context(0) as ctx:
         m = bt.DiffMesh(ctx, verts, faces, vn)
@@ -105,7 +105,7 @@ def test_lambert_forward_adjoint_against_fp64(level, size):
 
 
 def test_descent_lowers_the_loss():
-    verts, faces, vn, tverts, rays, light = scenes.config4(seed=4, level=4, width=96, height=96)
+    verts, faces, vn, tverts, rays, light = scenes.lambert_scene(seed=4, level=4, width=96, height=96)
     n = len(rays)
     with bt.Context(0) as ctx:
         m = bt.DiffMesh(ctx, verts, faces, vn)

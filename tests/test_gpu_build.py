@@ -71,9 +71,9 @@ def test_degenerate_meshes(ctx):
 
 
 def test_uneven_batch_scenes(ctx):
-    ntris, _ = scenes.config3_specs(0, 64)
+    ntris, _ = scenes.batch_specs(0, 64)
     for i in (0, 1, 2, 5, 10, 31):
-        tris, _ = scenes.config3_scene(i, int(min(ntris[i], 400_000)), 64, 0)
+        tris, _ = scenes.batch_scene(i, int(min(ntris[i], 400_000)), 64, 0)
         assert_same_build(ctx, tris)
 
 
@@ -95,7 +95,7 @@ def test_panicking_mesh_is_refused_like_the_host_build(ctx):
 
 
 def test_blas_built_on_the_gpu_traces_like_the_host_built_one(ctx):
-    tris, rays, _ = scenes.config1(seed=2, width=96, height=64)
+    tris, rays, _ = scenes.icosphere_frame(seed=2, width=96, height=64)
     host = np.ascontiguousarray(tris, np.float32).copy()
     bvh = bt.BvhBuilder().build_for(host)
     ref = ctx.upload_blas(bvh, host).intersect(rays)

@@ -1,4 +1,4 @@
-"""Animated instanced frames captured in a CUDA graph (config 2 pattern) against the oracle on
+"""Animated instanced frames captured in a CUDA graph (the instanced-animation workload's pattern) against the oracle on
 the frame's own state: refit nodes, TLAS, primary hits, bounce rays and bounce hits all
 bit-identical."""
 import numpy as np
@@ -13,7 +13,7 @@ pytestmark = pytest.mark.gpu
 
 
 def test_animated_frames_in_a_graph_match_the_oracle():
-    cfg = scenes.config2(seed=2, ninstances=48, width=256, height=144)
+    cfg = scenes.instanced_animation(seed=2, ninstances=48, width=256, height=144)
     with bt.Context(0) as ctx:
         sc = AnimatedScene(ctx, cfg)
         initial = [(m.bvh.nodes.copy(), m.bvh.nodes_used) for m in sc.meshes]

@@ -224,7 +224,7 @@ def test_large_triangles_far_camera_with_normal_cones(ctx, hidden):
     """The sphere at 10x scale seen from distance 30 and 300 (margins set by the leaves' normal
     cones), with rays at vertices and edges from every side -- including the grazing ones at the
     silhouette, where the cone gives no bound -- at a moderate and an unlimited margin."""
-    verts, faces, _, _, cam, _ = scenes.config4(seed=0, level=5, width=96, height=96)
+    verts, faces, _, _, cam, _ = scenes.lambert_scene(seed=0, level=5, width=96, height=96)
     tris = np.ascontiguousarray(verts[faces].reshape(-1, 9), np.float32)
     bvh = bt.BvhBuilder().build_for(tris)
     blas = ctx.upload_blas(bvh, tris)

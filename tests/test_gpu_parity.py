@@ -84,23 +84,23 @@ def test_cube_scene_known_answers(ctx):
 
 # ---- plain traversal --------------------------------------------------------------------------
 
-def test_config0_full_frame(ctx):
-    tris, rays = scenes.config0(seed=0)
+def test_soup_full_frame(ctx):
+    tris, rays = scenes.soup_frame(seed=0)
     tris, bvh = build(tris)
     blas = ctx.upload_blas(bvh, tris)
     gpu = blas.intersect(rays)
     ref = orc.bvh_intersect(bvh.nodes, bvh.nodes_used, tris, rays, threads=8)
-    assert_hits_equal(gpu, ref, "config0")
+    assert_hits_equal(gpu, ref, "soup_frame")
     assert (ref["prim"] != bt.MISS).mean() > 0.2
 
 
-def test_config1_sampled(ctx):
-    tris, rays, _ = scenes.config1(seed=1, width=480, height=272)
+def test_icosphere_frame_sampled(ctx):
+    tris, rays, _ = scenes.icosphere_frame(seed=1, width=480, height=272)
     tris, bvh = build(tris)
     blas = ctx.upload_blas(bvh, tris)
     gpu = blas.intersect(rays)
     ref = orc.bvh_intersect(bvh.nodes, bvh.nodes_used, tris, rays, threads=8)
-    assert_hits_equal(gpu, ref, "config1")
+    assert_hits_equal(gpu, ref, "icosphere_frame")
 
 
 def test_incoherent_rays_and_edge_cases(ctx):
@@ -125,7 +125,7 @@ def test_empty_and_single_ray(ctx):
 
 
 def test_async_device_path_matches_host_path(ctx):
-    tris, rays = scenes.config0(seed=2)
+    tris, rays = scenes.soup_frame(seed=2)
     tris, bvh = build(tris)
     blas = ctx.upload_blas(bvh, tris)
     d_rays = ctx.to_device(rays)
@@ -139,7 +139,7 @@ def test_async_device_path_matches_host_path(ctx):
 # ---- bounce -------------------------------------------------------------------------------------
 
 def test_bounce_rays_and_hits(ctx):
-    tris, rays, _ = scenes.config1(seed=3, width=320, height=184)
+    tris, rays, _ = scenes.icosphere_frame(seed=3, width=320, height=184)
     tris, bvh = build(tris)
     blas = ctx.upload_blas(bvh, tris)
     seed = 1234
@@ -165,7 +165,7 @@ def test_host_call_equals_device_launch(ctx, mode, pinned):
     """bvhgpu_blas_trace_bounce with host buffers -- staged through device copies, or read and
     written in place when every buffer is page-locked -- and its device-side bounce count give
     what the device-buffer launch gives."""
-    tris, rays, _ = scenes.config1(seed=5, width=960, height=544)
+    tris, rays, _ = scenes.icosphere_frame(seed=5, width=960, height=544)
     tris, bvh = build(tris)
     blas = ctx.upload_blas(bvh, tris)
     n = len(rays)

@@ -42,7 +42,7 @@ def bounce_refs(primaries, ref0, bounce_fn, trace_fn):
 
 @pytest.fixture(scope="module")
 def blas_case(ctx):
-    tris, cam, _ = scenes.config1(seed=8, width=96, height=64)
+    tris, cam, _ = scenes.icosphere_frame(seed=8, width=96, height=64)
     rays = np.concatenate([cam, scenes.sphere_rays(2048, 3, box=1.5)])
     tris, bvh = build(tris)
     blas = ctx.upload_blas(bvh, tris)
@@ -100,7 +100,7 @@ def random_instances(n, seed):
 def test_lambert_forward_every_variant(ctx):
     """The persistent Lambertian forward pass runs under the single-ray trace kernel's config:
     every variant gives the oracle's hits and one and the same image."""
-    verts, faces, vn, _, rays, light = scenes.config4(seed=4, level=5, width=64, height=64)
+    verts, faces, vn, _, rays, light = scenes.lambert_scene(seed=4, level=5, width=64, height=64)
     n = len(rays)
     m = bt.DiffMesh(ctx, verts, faces, vn)
     d_rays = ctx.to_device(rays)

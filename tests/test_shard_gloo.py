@@ -51,7 +51,7 @@ def _worker(rank, world, port, out_dir):
         from oracle import oracle as orc
         from bvhtracer_gb300 import scenes
         # a frame, sharded by ray range
-        tris, rays, _ = scenes.config1(seed=4, width=64, height=40)
+        tris, rays, _ = scenes.icosphere_frame(seed=4, width=64, height=40)
         t, nodes, used = orc.bvh_build(tris)
         b, e = shard.ray_range(len(rays), rank, world)
         local = orc.bvh_intersect(nodes, used, t, rays[b:e])
