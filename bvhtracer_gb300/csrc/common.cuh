@@ -672,33 +672,6 @@ struct TravT {
     }
 };
 
-// The local-memory traversal used where no tuned variant applies (render, adjoint).
-template <int STACK>
-using Trav = TravT<LocalStack<STACK>>;
-
-// Whole traversal by one lane, every leaf tested by the lane itself.
-template <int STACK>
-__device__ __forceinline__ bool trace_blas(const GBlas& b, float3 o, float3 d, float3 rd, float& closest_t,
-                                           float& hu, float& hv, uint32_t& hprim, uint32_t* err) {
-    Trav<STACK> tr;
-    tr.init(b);
-    LaneRay r;
-    r.o = o;
-    r.d = d;
-    r.rd = rd;
-    r.ct = closest_t;
-    r.hu = hu;
-    r.hv = hv;
-    r.hp = hprim;
-    r.hit = false;
-    tr.advance(b, r, LeafPolicy{0xFFFFFFFFu, kDefaultPolicy.max_duv}, err);
-    closest_t = r.ct;
-    hu = r.hu;
-    hv = r.hv;
-    hprim = r.hp;
-    return r.hit;
-}
-
 // Running best of one ray inside a cooperative leaf test (triangle index order kept: a pair's
 // triangle A before B, strict `<`).  Only t and the triangle are kept; the winner's u, v are
 // recomputed once after the warp reduction (reduce_and_take).
