@@ -53,6 +53,24 @@ def test_host_entry_points_validate_arguments():
     assert lib.bvhgpu_sync(None) == 1
 
 
+def test_every_entry_point_rejects_a_null_context():
+    """Every entry point that takes a context returns BVHGPU_ERR_INVALID_ARG (1) for a null
+    context and null / zero arguments, before touching the device: no crash, no CUDA call."""
+    lib = _lib.load()
+    no_ctx = {"bvhgpu_create", "bvhgpu_launch_count", "bvhgpu_tune_space", "bvhgpu_last_error",
+              "bvhgpu_get_stream"}
+    checked = 0
+    for name, (res, args) in _lib.SIGNATURES.items():
+        if name in no_ctx or not args:
+            continue
+        vals = [None if a in (ctypes.c_void_p, ctypes.c_char_p) else a(0) for a in args]
+        assert getattr(lib, name)(*vals) == 1, name
+        checked += 1
+    assert checked >= 80
+    assert lib.bvhgpu_get_stream(None) is None
+    assert b"context" in lib.bvhgpu_last_error(None)
+
+
 def test_tune_space_lists_every_compiled_variant():
     """bvhgpu_tune_space needs no device: 5 launch shapes x 3 stacks x 5 big-leaf values x 5
     hidden-tree margins, times 3 refill sizes for the persistent kernels."""
