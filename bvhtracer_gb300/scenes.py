@@ -17,7 +17,11 @@ import math
 
 import numpy as np
 
-from ._lib import FLT_MAX, RAY
+# The ray record of the C ABI (bvhgpu_ray, 32 bytes).  Defined here rather than imported so that
+# this module has no dependency on the rest of the package: it can be loaded on its own (by file
+# path) by code that must not touch the CUDA library, such as a CPU-only timing of the same inputs.
+RAY = np.dtype([("origin", "<f4", 3), ("t", "<f4"), ("direction", "<f4", 3), ("reserved", "<u4")])
+FLT_MAX = np.float32(np.finfo(np.float32).max)
 
 _M64 = np.uint64(0xFFFFFFFFFFFFFFFF)
 

@@ -78,3 +78,40 @@ def test_fetched_bytes_basis(bench):
     assert out["primary"]["rays"] == 2 and out["primary"]["bytes"] == per_call + 52 * 2
     assert out["bounce"]["rays"] == 1 and out["bounce"]["bytes"] == per_call + 52
     assert out["primary"]["per_ray"]["hidden_boxes"] == 10.0
+
+
+def test_reference_arm_loads_no_cuda_library():
+    """--impl reference times the oracle only: the CUDA library is never loaded (checked on the
+    process's own memory map) and the line carries the reference arm's keys."""
+    import json
+    import subprocess
+    import sys
+    code = ("import runpy, sys, json\n"
+            "sys.argv = ['bench.py', '--impl', 'reference', '--steps', '1', '--warmup', '3', '--ref-fraction', '512']\n"
+            "try:\n    runpy.run_path('bench.py', run_name='__main__')\n"
+            "except SystemExit as e:\n    assert not e.code, e.code\n"
+            "maps = open('/proc/self/maps').read()\n"
+            "print(json.dumps({'bvhgpu': 'libbvhgpu' in maps, 'orc': 'liborc' in maps, "
+            "'pkg': [m for m in sys.modules if m.startswith('bvhtracer_gb300')]}))\n")
+    out = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stderr
+    lines = [json.loads(x) for x in out.stdout.strip().splitlines()]
+    line, probe = lines[0], lines[-1]
+    assert line["impl"] == "reference" and line["value"] > 0 and line["e2e"]["h2d_bytes_per_step"] == 0
+    assert line["cpu_baseline"]["kind"] == "port" and "every 512th 8x8 tile" in line["config"]["sample_per_step"]
+    assert probe == {"bvhgpu": False, "orc": True, "pkg": []}
+
+
+def test_parity_fail_reads_every_parity_object(bench):
+    ok = {"checks": {"a": {"mismatch_outside_near_ties": 0}}, "identical_bvh": True}
+    bad = {"checks": {"a": {"mismatch_outside_near_ties": 0}, "b": {"mismatch_outside_near_ties": 2}}}
+    assert not bench.parity_fail({"parity": ok})
+    assert bench.parity_fail({"parity": bad})
+    assert bench.parity_fail({"parity": dict(ok, identical_bvh=False)})
+    assert bench.parity_fail({"parity": ok, "batch": {"parity": bad}})
+    assert not bench.parity_fail({"parity": ok, "batch": {"parity": ok}, "adjoint": {"parity": None}})
+
+
+def test_gpus_flag_must_match_world_size(bench, monkeypatch):
+    monkeypatch.setenv("WORLD_SIZE", "1")
+    assert bench.main(["--gpus", "2", "--impl", "reference"]) == 2
