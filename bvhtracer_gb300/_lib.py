@@ -70,6 +70,7 @@ ERRORS = {1: "invalid argument", 2: "out of memory", 3: "CUDA error", 4: "stack 
 ACC_INTERSECTION, ACC_DEPTH, ACC_UV, ACC_NORMAL, ACC_TEXTURE = 0, 1, 2, 3, 4
 SHADER_RADIANCE, SHADER_INTERSECTION, SHADER_DEPTH = 0, 1, 2
 MODE_PLAIN, MODE_PERSISTENT = 0, 1
+LOOKUP_REFERENCE, LOOKUP_HIT_OBJECT = 0, 1
 LIST_CLOSEST, LIST_MUT = 0, 1
 MESH_TRI, MESH_OBJ = 0, 1
 
@@ -142,6 +143,8 @@ SIGNATURES = {
     "bvhgpu_graph_free": (_I, [_P, _U32]),
     "bvhgpu_render": (_I, [_P, _U32, _P, _I, _I, _I, _P, _I, _P, _P, _P, _P]),
     "bvhgpu_render_textured": (_I, [_P, _U32, _P, _I, _I, _P, _P, _U32, _U32, _I, _P, _P, _P]),
+    "bvhgpu_blas_set_shading": (_I, [_P, _U32, _P, _P, _P, _U32, _U32]),
+    "bvhgpu_render_scene": (_I, [_P, _U32, _P, _I, _I, _I, _P, _I, _P, _I, _P, _P]),
     "bvhgpu_mesh_create": (_I, [_P, _U32, _P, _U32, _P, _P, _U32, _P]),
     "bvhgpu_mesh_free": (_I, [_P, _U32]),
     "bvhgpu_mesh_vertices": (_I, [_P, _U32, _P]),

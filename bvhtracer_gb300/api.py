@@ -11,6 +11,7 @@ Errors raise :class:`BvhGpuError`; there is no CPU fallback.
 from __future__ import annotations
 
 import ctypes
+import os
 
 import numpy as np
 
@@ -458,6 +459,15 @@ class Blas:
         self.ctx.check(self.ctx.lib.bvhgpu_blas_download_nodes(self.ctx.h, self.id, ptr(out)))
         return out
 
+    def set_shading(self, normals=None, tex_coords=None, texels=None):
+        """The model's shading data for scene renders: corner normals [ntris, 9], corner texture
+        coordinates [ntris, 6] (BLAS triangle order), RGB8 texture [h, w, 3]; None keeps an array."""
+        nrm = None if normals is None else np.ascontiguousarray(normals, np.float32).reshape(self.ntris, 9)
+        tc = None if tex_coords is None else np.ascontiguousarray(tex_coords, np.float32).reshape(self.ntris, 6)
+        tx = None if texels is None else np.ascontiguousarray(texels, np.uint8)
+        th, tw = (0, 0) if tx is None else tx.shape[:2]
+        self.ctx.check(self.ctx.lib.bvhgpu_blas_set_shading(self.ctx.h, self.id, ptr(nrm), ptr(tc), ptr(tx), tw, th))
+
     def render(self, camera: "Camera", width: int, height: int, accumulator: int, shader: int,
                acc_params=None, shader_params=None, normals=None):
         """PathTracer::evaluate on this BLAS: returns (rgba [h, w, 4] uint8, rays traced)."""
@@ -575,6 +585,21 @@ class Scene:
         self.ctx.check(self.ctx.lib.bvhgpu_scene_intersect_async(self.ctx.h, self.id, d_rays.ptr, n, d_hits.ptr,
                                                                  stream))
 
+    def render(self, camera: "Camera", width: int, height: int, accumulator: int, shader: int,
+               acc_params=None, shader_params=None, lookup: int = _lib.LOOKUP_REFERENCE):
+        """PathTracer::evaluate over the whole scene (Renderer::render with a Scene): returns (rgba
+        [h, w, 4] uint8, rays traced).  The normal / texture accumulators read the shading data set
+        with Blas.set_shading; `lookup` picks the reference's instance-0 lookup or the hit's object."""
+        cam = camera.to_struct()
+        rgba = np.zeros((height, width, 4), np.uint8)
+        ap = None if acc_params is None else np.ascontiguousarray(acc_params, np.float32)
+        sp = None if shader_params is None else np.ascontiguousarray(shader_params, np.float32)
+        rays = ctypes.c_uint64()
+        self.ctx.check(self.ctx.lib.bvhgpu_render_scene(self.ctx.h, self.id, ptr(cam), width, height, accumulator,
+                                                        ptr(ap), shader, ptr(sp), lookup, ptr(rgba),
+                                                        ctypes.byref(rays)))
+        return rgba, rays.value
+
     def free(self):
         if self.id:
             self.ctx.lib.bvhgpu_scene_free(self.ctx.h, self.id)
@@ -627,6 +652,16 @@ class DiffMesh:
     def update_async(self, stream=None):
         self.ctx.check(self.ctx.lib.bvhgpu_mesh_update_async(self.ctx.h, self.id, stream))
 
+    def checkpoint(self, path: str, step: int, losses=(), lr: float | None = None):
+        """Saves the descent state: the device vertices, the step count and the loss history."""
+        save_descent_state(path, self.vertices(), step, losses, lr)
+
+    def resume(self, path: str) -> dict:
+        """Restores the vertices of a checkpoint (and refits the BLAS); returns the checkpoint."""
+        state = load_descent_state(path)
+        self.set_vertices(state["verts"])
+        return state
+
     def forward_async(self, d_rays: DeviceBuffer, n: int, light, d_image: DeviceBuffer, d_hits: DeviceBuffer,
                       stream=None):
         L = np.ascontiguousarray(light, np.float32)
@@ -647,6 +682,24 @@ class DiffMesh:
 
     def sgd_step_async(self, d_grad: DeviceBuffer, lr: float, stream=None):
         self.ctx.check(self.ctx.lib.bvhgpu_mesh_sgd_step_async(self.ctx.h, self.id, d_grad.ptr, float(lr), stream))
+
+
+def save_descent_state(path: str, verts: np.ndarray, step: int, losses=(), lr: float | None = None):
+    """Checkpoint of a gradient descent on a mesh's vertices: the vertices (float32 [nverts, 3]), the
+    number of steps taken, the loss history and the learning rate, written to `path` (.npz) through a
+    temporary file and a rename, so an interrupted write never leaves a partial checkpoint."""
+    tmp = f"{path}.tmp{os.getpid()}.npz"
+    np.savez(tmp, verts=np.ascontiguousarray(verts, np.float32), step=np.int64(step),
+             losses=np.asarray(list(losses), np.float64), lr=np.float64(np.nan if lr is None else lr))
+    os.replace(tmp, path)
+
+
+def load_descent_state(path: str) -> dict:
+    """The checkpoint written by save_descent_state: {verts, step, losses, lr}."""
+    with np.load(path) as d:
+        lr = float(d["lr"])
+        return {"verts": d["verts"].astype(np.float32), "step": int(d["step"]),
+                "losses": [float(x) for x in d["losses"]], "lr": None if np.isnan(lr) else lr}
 
 
 def mse_loss(ctx: Context, d_image: DeviceBuffer, d_target: DeviceBuffer, n: int) -> float:

@@ -1,12 +1,14 @@
 // C ABI of the bvhgpu library (include/bvhgpu.h): context, memory helpers, timing, BLAS and
 // scene management, and the trace / refit / rebuild / render entry points.
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <cfloat>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "common.cuh"
@@ -16,7 +18,16 @@ namespace bvhgpu {
 
 std::atomic<uint64_t> g_launches{0};
 
+// NVTX range names per kernel id (BVHGPU_K_*): every launch is bracketed by a host range, so a timeline
+// tool shows refit / TLAS rebuild / trace / render / adjoint phases.  Without a tool attached an NVTX
+// call costs a branch.
+static const char* const kRangeNames[BVHGPU_KERNEL_COUNT] = {
+    "bvhgpu trace", "bvhgpu trace scene", "bvhgpu trace + bounce (persistent)", "bvhgpu bounce generation",
+    "bvhgpu trace queue", "bvhgpu trace batch", "bvhgpu refit", "bvhgpu TLAS rebuild", "bvhgpu render",
+    "bvhgpu other", "bvhgpu Lambert forward", "bvhgpu Lambert adjoint", "bvhgpu scene trace + bounce"};
+
 LaunchScope::LaunchScope(bvhgpu_ctx* c, int k, cudaStream_t st) : ctx(c), kernel(k), s(st) {
+    nvtxRangePushA(k >= 0 && k < BVHGPU_KERNEL_COUNT ? kRangeNames[k] : "bvhgpu");
     if (!ctx->profiling) return;
     if (ctx->event_pool.size() >= 2) {
         e1 = ctx->event_pool.back();
@@ -31,6 +42,7 @@ LaunchScope::LaunchScope(bvhgpu_ctx* c, int k, cudaStream_t st) : ctx(c), kernel
 }
 
 LaunchScope::~LaunchScope() {
+    nvtxRangePop();
     if (!e0) return;
     cudaEventRecord(e1, s);
     ctx->prof.push_back(ProfileRec{kernel, e0, e1});
@@ -97,6 +109,10 @@ int read_errors(bvhgpu_ctx* ctx) {
     if (flags) {
         CK(cudaMemset(ctx->d_err, 0, sizeof(uint32_t)), "reset error flags");
         if (flags & kErrStack) return fail(ctx, BVHGPU_ERR_STACK_DEPTH, "traversal stack overflow (tree too deep)");
+        if (flags & kErrLookup)
+            return fail(ctx, BVHGPU_ERR_INVALID_ARG,
+                        "a hit's primitive index lies outside the looked-up model's shading data (the reference "
+                        "indexes out of bounds and panics there)");
         return fail(ctx, BVHGPU_ERR_STEP_CAP, "traversal step cap exceeded (malformed tree)");
     }
     return BVHGPU_OK;
@@ -129,6 +145,9 @@ void free_blas(DeviceBlas& b) {
     cudaFree(b.hx);
     cudaFree(b.cones);
     cudaFree(b.hwork);
+    cudaFree(b.normals);
+    cudaFree(b.tex_coords);
+    cudaFree(b.texels);
     b = DeviceBlas();
 }
 
@@ -987,6 +1006,11 @@ int bvhgpu_trace_batch_async(bvhgpu_ctx* ctx, const bvhgpu_batch_item* items, ui
         if ((uint64_t)items[i].ray_offset + items[i].ray_count > nrays)
             return fail(ctx, BVHGPU_ERR_INVALID_ARG, "batch item %u: rays past %u", i, nrays);
     }
+    // a new item list is uploaded synchronously (stream synchronize, allocation, copy), which a stream
+    // capture cannot record: trace a new list once before capturing it
+    if (mode == BVHGPU_MODE_PERSISTENT && nitems && ctx->capturing && !batch_table_current(ctx, items, nitems))
+        return fail(ctx, BVHGPU_ERR_INVALID_ARG,
+                    "trace_batch: a new item list cannot be set up during graph capture (trace it once first)");
     CK(launch_trace_batch(ctx, blases, items, nitems, reinterpret_cast<const float4*>(d_rays), nrays, mode, d_hits,
                           pick(ctx, s)),
        "trace batch");
@@ -1476,6 +1500,80 @@ int bvhgpu_render_textured(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhgpu_camer
     CK(launch_render(ctx, *b, *camera, width, height, BVHGPU_ACC_TEXTURE, nullptr, shader, shader_params, nullptr,
                      d_tc, d_tex, tex_w, tex_h, static_cast<uint8_t*>(ctx->stage_out), ctx->stream),
        "render");
+    CK(cudaMemcpyAsync(rgba, ctx->stage_out, 4 * px, cudaMemcpyDeviceToHost, ctx->stream), "download frame");
+    rc = finish(ctx);
+    if (rc) return rc;
+    if (rays_traced) *rays_traced = px;
+    return BVHGPU_OK;
+}
+
+// ---- scene render -----------------------------------------------------------------------------
+
+int bvhgpu_blas_set_shading(bvhgpu_ctx* ctx, uint32_t blas_id, const float* normals, const float* tex_coords,
+                            const uint8_t* texels, uint32_t tex_w, uint32_t tex_h) {
+    if (!ctx) return BVHGPU_ERR_INVALID_ARG;
+    DeviceBlas* b = find_blas(ctx, blas_id);
+    if (!b) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown BLAS %u", blas_id);
+    if (texels && (tex_w == 0 || tex_h == 0))
+        return fail(ctx, BVHGPU_ERR_INVALID_ARG, "a texture needs tex_w > 0 and tex_h > 0");
+    // the caller's stream may still read the old arrays
+    CK(cudaStreamSynchronize(ctx->stream), "stream synchronize");
+    auto replace = [&](auto** dst, const void* src, size_t bytes) -> int {
+        void* p = nullptr;
+        cudaError_t e = cudaMalloc(&p, std::max<size_t>(bytes, 16));
+        if (e != cudaSuccess) return fail(ctx, BVHGPU_ERR_OUT_OF_MEMORY, "cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e));
+        e = cudaMemcpy(p, src, bytes, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            cudaFree(p);
+            return cuda_fail(ctx, e, "upload shading data");
+        }
+        cudaFree(*dst);
+        *dst = static_cast<std::remove_pointer_t<decltype(dst)>>(p);
+        return BVHGPU_OK;
+    };
+    int rc = BVHGPU_OK;
+    if (normals) rc = replace(&b->normals, normals, 36ull * b->ntris);
+    if (!rc && tex_coords) rc = replace(&b->tex_coords, tex_coords, 24ull * b->ntris);
+    if (!rc && texels) {
+        rc = replace(&b->texels, texels, 3ull * tex_w * tex_h);
+        if (!rc) {
+            b->tex_w = tex_w;
+            b->tex_h = tex_h;
+        }
+    }
+    return rc;
+}
+
+int bvhgpu_render_scene(bvhgpu_ctx* ctx, uint32_t scene_id, const bvhgpu_camera* camera, int width, int height,
+                        int accumulator, const float* acc_params, int shader, const float* shader_params, int lookup,
+                        uint8_t* rgba, uint64_t* rays_traced) {
+    if (!ctx || !camera || !rgba || width <= 0 || height <= 0) return BVHGPU_ERR_INVALID_ARG;
+    if (accumulator < 0 || accumulator > 4 || shader < 0 || shader > 2)
+        return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown accumulator %d or shader %d", accumulator, shader);
+    if (lookup != BVHGPU_LOOKUP_REFERENCE && lookup != BVHGPU_LOOKUP_HIT_OBJECT)
+        return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown lookup %d", lookup);
+    if (accumulator == BVHGPU_ACC_INTERSECTION && !acc_params)
+        return fail(ctx, BVHGPU_ERR_INVALID_ARG, "accumulator needs parameters");
+    if ((shader == BVHGPU_SHADER_INTERSECTION || shader == BVHGPU_SHADER_DEPTH) && !shader_params)
+        return fail(ctx, BVHGPU_ERR_INVALID_ARG, "shader needs parameters");
+    DeviceScene* sc = find_scene(ctx, scene_id);
+    if (!sc) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown scene %u", scene_id);
+    if (sc->nobjects == 0) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "scene %u has no objects", scene_id);
+    std::vector<ShadeEntry> tab(sc->table_blas.size());
+    for (size_t k = 0; k < tab.size(); ++k) {
+        const DeviceBlas* b = find_blas(ctx, sc->table_blas[k]);
+        if (!b) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "scene %u uses a freed BLAS", scene_id);
+        tab[k] = ShadeEntry{b->normals, b->tex_coords, b->texels, b->tex_w, b->tex_h, b->ntris, 0};
+    }
+    const size_t px = (size_t)width * height, tab_bytes = tab.size() * sizeof(ShadeEntry);
+    int rc = ensure(ctx, &ctx->stage_out, &ctx->stage_out_bytes, 4 * px);
+    if (!rc) rc = ensure(ctx, &ctx->stage_in, &ctx->stage_in_bytes, tab_bytes + 16);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(ctx->stage_in, tab.data(), tab_bytes, cudaMemcpyHostToDevice, ctx->stream), "shade table");
+    CK(launch_render_scene(ctx, *sc, *camera, width, height, accumulator, acc_params, shader, shader_params,
+                           static_cast<const ShadeEntry*>(ctx->stage_in), lookup,
+                           static_cast<uint8_t*>(ctx->stage_out), ctx->stream),
+       "render scene");
     CK(cudaMemcpyAsync(rgba, ctx->stage_out, 4 * px, cudaMemcpyDeviceToHost, ctx->stream), "download frame");
     rc = finish(ctx);
     if (rc) return rc;

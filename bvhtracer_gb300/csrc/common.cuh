@@ -19,6 +19,7 @@ namespace bvhgpu {
 // Device error flags (OR-ed into the context's error word).
 constexpr uint32_t kErrStack = 1u;
 constexpr uint32_t kErrSteps = 2u;
+constexpr uint32_t kErrLookup = 4u;  // a render's shading lookup fell outside the model's data
 
 constexpr uint32_t kMiss = 0xFFFFFFFFu;
 constexpr float kThreshold = 0.0001f;  // num_traits::cast(0.0001_f64) (triangle.rs:47)

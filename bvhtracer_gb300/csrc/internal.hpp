@@ -40,6 +40,19 @@ struct DeviceBlas {
     uint32_t depth = 0;          // traversal depth: reference tree plus the deepest hidden tree
     uint32_t root_count = 0;
     uint32_t root_first = 0;
+    // shading data of the BLAS's model (bvhgpu_blas_set_shading), for rendering a scene
+    float* normals = nullptr;     // 9 floats per triangle (corner normals), or null
+    float* tex_coords = nullptr;  // 6 floats per triangle (corner texture coordinates), or null
+    uint8_t* texels = nullptr;    // RGB8 texture, row-major tex_w x tex_h, or null
+    uint32_t tex_w = 0, tex_h = 0;
+};
+
+// Per entry of a scene's BLAS table: what the normal / texture accumulators read of a model.
+struct ShadeEntry {
+    const float* normals;
+    const float* tex_coords;
+    const uint8_t* texels;
+    uint32_t tex_w, tex_h, ntris, pad;
 };
 
 struct DeviceScene {
@@ -173,11 +186,16 @@ cudaError_t launch_trace_count(bvhgpu_ctx* ctx, const DeviceBlas& b, const float
 cudaError_t launch_count_hits(bvhgpu_ctx* ctx, const void* hits, uint32_t n, uint32_t* count, cudaStream_t s);
 cudaError_t launch_bounce_rays(bvhgpu_ctx* ctx, const DeviceBlas& b, const float4* rays, const void* hits0,
                                uint32_t n, uint32_t seed, float4* out, uint8_t* valid, cudaStream_t s);
+// True when the persistent batch's device table already describes `items` (no upload needed).
+bool batch_table_current(const bvhgpu_ctx* ctx, const bvhgpu_batch_item* items, uint32_t nitems);
 cudaError_t launch_trace_batch(bvhgpu_ctx* ctx, const std::vector<const DeviceBlas*>& blases,
                                const bvhgpu_batch_item* items, uint32_t nitems, const float4* rays, uint32_t nrays,
                                int mode, void* hits, cudaStream_t s);
 cudaError_t launch_triangle_list(bvhgpu_ctx* ctx, const float* tris, uint32_t ntris, const float4* rays, uint32_t n,
                                  int mode, void* hits, cudaStream_t s);
+cudaError_t launch_render_scene(bvhgpu_ctx* ctx, DeviceScene& sc, const bvhgpu_camera& cam, int w, int h, int acc,
+                                const float* acc_params, int shader, const float* shader_params,
+                                const ShadeEntry* d_shade, int lookup, uint8_t* d_rgba, cudaStream_t s);
 cudaError_t launch_render(bvhgpu_ctx* ctx, const DeviceBlas& b, const bvhgpu_camera& cam, int w, int h, int acc,
                           const float* acc_params, int shader, const float* shader_params, const float* d_normals,
                           const float* d_tex_coords, const uint8_t* d_texels, uint32_t tex_w, uint32_t tex_h,

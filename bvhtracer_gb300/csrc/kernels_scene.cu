@@ -14,6 +14,7 @@
 
 #include "common.cuh"
 #include "internal.hpp"
+#include "render.cuh"
 #include "variants.cuh"
 
 namespace bvhgpu {
@@ -735,6 +736,76 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_trace_scene(SceneData sd, const
     if (active) store_hit(hits, i, r.hit && r.ct < FLT_MAX, r.ct, r.hu, r.hv, r.hp, r.inst);
 }
 
+// PathTracer::evaluate over a whole scene (renderer.rs:345-384 -> Scene::intersect, scene.rs:32-34):
+// one 64-thread block per 8x8 tile, the camera ray through the pixel's top-left corner, the two-level
+// traversal of k_trace_scene, then the accumulator and shader.  The normal and texture accumulators
+// look up `scene.get_unchecked(instance_index)` (renderer.rs:258-263, 312-317): with lookup 0 the
+// reference's packed index -- instance 0, because Bvh::intersect packs instance 0
+// (InstancePrimitiveIndex::from_primitive, bvh.rs:296), and the primitive's low 20 bits
+// (intersection.rs:57-60) -- with lookup 1 the hit's own object.  A primitive outside the looked-up
+// model's data (where the reference's slice indexing panics) or missing shading data sets kErrLookup
+// and the pixel's radiance is zero.
+template <int STACK>
+__global__ void __launch_bounds__(64) k_render_scene(SceneData sd, RenderParams P,
+                                                     const ShadeEntry* __restrict__ shade_tab,
+                                                     const float* __restrict__ xf, int lookup,
+                                                     uint8_t* __restrict__ rgba, LeafPolicy pol, uint32_t* err) {
+    const int tiles_x = (P.width + 7) / 8;
+    const int tile = blockIdx.x;
+    const int x = (tile % tiles_x) * 8 + (threadIdx.x & 7);
+    const int y = (tile / tiles_x) * 8 + (threadIdx.x >> 3);
+    const bool active = x < P.width && y < P.height;  // all lanes stay for the cooperative leaf steps
+    LaneRay r;
+    SceneTrav<LocalStack<STACK>, kTlasStack> tr;
+    tr.bt.stk.bind(nullptr);
+    StepResult st = kStepFinished;
+    if (active) {
+        float3 o, d;
+        camera_ray(P, x, y, o, d);
+        r.o = o;
+        r.d = d;
+        r.rd = recip3(d);
+        r.ct = FLT_MAX;
+        r.hu = r.hv = 0.0f;
+        r.hp = 0;
+        r.hit = false;
+        r.inst = r.inst_cur = 0;
+        tr.init(sd, r);
+        st = kStepContinue;
+    }
+    for (;;) {
+        if (st == kStepContinue) st = tr.advance(sd, r, pol, err);
+        const unsigned pend = __ballot_sync(kFull, st == kStepBigLeaf);
+        if (pend == 0u) break;
+        scene_coop_phase(pend, tr, r, st);
+    }
+    if (!active) return;
+    const bool hit = r.hit && r.ct < FLT_MAX;
+    const float* nrm = nullptr;
+    const float* tc = nullptr;
+    const uint8_t* tex = nullptr;
+    uint32_t tw = 0, th = 0, prim = r.hp;
+    const float* oxf = xf;
+    bool ok = true;
+    if (hit && (P.acc_kind == BVHGPU_ACC_NORMAL || P.acc_kind == BVHGPU_ACC_TEXTURE)) {
+        const uint32_t obj = lookup ? r.inst : 0u;
+        prim = lookup ? r.hp : (r.hp & 0x000FFFFFu);
+        const ShadeEntry e = shade_tab[__ldg(sd.obj_blas + obj)];
+        oxf = xf + 16ull * obj;
+        nrm = e.normals;
+        tc = e.tex_coords;
+        tex = e.texels;
+        tw = e.tex_w;
+        th = e.tex_h;
+        ok = prim < e.ntris && (P.acc_kind == BVHGPU_ACC_NORMAL ? nrm != nullptr
+                                                                : (tc != nullptr && tex != nullptr && tw && th));
+        if (!ok) atomicOr(err, kErrLookup);
+    }
+    const float3 rad = ok ? accumulate(P, hit, r.ct, r.hu, r.hv, prim, nrm, oxf, tc, tex, tw, th)
+                          : make_float3(0.0f, 0.0f, 0.0f);
+    reinterpret_cast<uchar4*>(rgba)[(size_t)y * P.width + x] = shade(P, rad);
+}
+
 // Persistent primary + bounce over a scene (the instanced frame): idle lanes are refilled from
 // the queue; a primary that hits continues in its lane with the bounce ray of its hit.
 template <int BLOCK, int MINB, class STK>
@@ -989,6 +1060,28 @@ cudaError_t launch_trace_scene(bvhgpu_ctx* ctx, DeviceScene& sc, const float4* r
     });
     g_launches++;
     return e;
+}
+
+cudaError_t launch_render_scene(bvhgpu_ctx* ctx, DeviceScene& sc, const bvhgpu_camera& cam, int w, int h, int acc,
+                                const float* acc_params, int shader, const float* shader_params,
+                                const ShadeEntry* d_shade, int lookup, uint8_t* d_rgba, cudaStream_t s) {
+    uint32_t depth = 1;
+    SceneData sd = scene_data(ctx, sc, &depth);
+    const RenderParams P = make_render_params(cam, w, h, acc, acc_params, shader, shader_params);
+    const LeafPolicy pol = resolve(ctx->tune[BVHGPU_K_TRACE_SCENE], depth).pol;
+    const unsigned tiles = (unsigned)(((w + 7) / 8) * ((h + 7) / 8));
+    LaunchScope scope(ctx, BVHGPU_K_RENDER, s);
+    // the smallest local stack that holds the deepest BLAS's pending far children
+    if (depth <= 33)
+        k_render_scene<32><<<tiles, 64, 0, s>>>(sd, P, d_shade, sc.xf, lookup, d_rgba, pol, ctx->d_err);
+    else if (depth <= 65)
+        k_render_scene<64><<<tiles, 64, 0, s>>>(sd, P, d_shade, sc.xf, lookup, d_rgba, pol, ctx->d_err);
+    else if (depth <= 129)
+        k_render_scene<128><<<tiles, 64, 0, s>>>(sd, P, d_shade, sc.xf, lookup, d_rgba, pol, ctx->d_err);
+    else
+        k_render_scene<256><<<tiles, 64, 0, s>>>(sd, P, d_shade, sc.xf, lookup, d_rgba, pol, ctx->d_err);
+    g_launches++;
+    return cudaGetLastError();
 }
 
 cudaError_t launch_scene_bounce(bvhgpu_ctx* ctx, DeviceScene& sc, const float4* rays, uint32_t n, uint32_t seed,

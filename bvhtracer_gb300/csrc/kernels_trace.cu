@@ -15,6 +15,7 @@
 #include "common.cuh"
 #include "internal.hpp"
 #include "persistent.cuh"
+#include "render.cuh"
 #include "variants.cuh"
 
 namespace bvhgpu {
@@ -424,51 +425,9 @@ __global__ void __launch_bounds__(kListTile) k_triangle_list(const float* __rest
 
 // ---- tiled render --------------------------------------------------------------------------
 
-__device__ __forceinline__ float3 xf_point(const float* m, float3 p) {
-    return make_float3(fadd(fadd(fadd(fmul(m[0], p.x), fmul(m[4], p.y)), fmul(m[8], p.z)), fmul(m[12], 1.0f)),
-                       fadd(fadd(fadd(fmul(m[1], p.x), fmul(m[5], p.y)), fmul(m[9], p.z)), fmul(m[13], 1.0f)),
-                       fadd(fadd(fadd(fmul(m[2], p.x), fmul(m[6], p.y)), fmul(m[10], p.z)), fmul(m[14], 1.0f)));
-}
-__device__ __forceinline__ float3 xf_vector(const float* m, float3 p) {
-    return make_float3(fadd(fadd(fadd(fmul(m[0], p.x), fmul(m[4], p.y)), fmul(m[8], p.z)), fmul(m[12], 0.0f)),
-                       fadd(fadd(fadd(fmul(m[1], p.x), fmul(m[5], p.y)), fmul(m[9], p.z)), fmul(m[13], 0.0f)),
-                       fadd(fadd(fadd(fmul(m[2], p.x), fmul(m[6], p.y)), fmul(m[10], p.z)), fmul(m[14], 0.0f)));
-}
-__device__ __forceinline__ float3 normalize3(float3 v) {
-    float m = __fsqrt_rn(dot3(v.x, v.y, v.z, v.x, v.y, v.z));
-    return make_float3(__fdiv_rn(v.x, m), __fdiv_rn(v.y, m), __fdiv_rn(v.z, m));
-}
-
-struct RenderParams {
-    float cam[9 + 16];
-    float acc[16];
-    float sh[8];
-    int width, height, acc_kind, shader_kind;
-    const float* tex_coords;  // BVHGPU_ACC_TEXTURE: 6 floats per triangle (per-corner u, v)
-    const uint8_t* texels;    //   RGB8, row-major
-    uint32_t tex_w, tex_h;
-};
-
-__device__ __forceinline__ unsigned long long f32_as_usize(float x) {  // Rust `as usize`: saturating
-    if (!(x > 0.0f)) return 0ull;
-    if (x >= 18446744073709551616.0f) return 0xFFFFFFFFFFFFFFFFull;
-    return (unsigned long long)x;
-}
-
-__device__ __forceinline__ uint8_t f32_as_u8(float x) {  // Rust `as u8`: saturating, NaN -> 0
-    if (!(x > 0.0f)) return 0;
-    if (x >= 255.0f) return 255;
-    return (uint8_t)x;
-}
-__device__ __forceinline__ int32_t f32_as_i32(float x) {  // Rust `as i32`: saturating, NaN -> 0
-    if (x != x) return 0;
-    if (x >= 2147483648.0f) return INT32_MAX;
-    if (x <= -2147483648.0f) return INT32_MIN;
-    return (int32_t)x;
-}
-
 // PathTracer::evaluate (renderer.rs:345-384): one 64-thread block per 8x8 tile; the camera ray
-// goes through the pixel's top-left corner u = x / w, v = y / h (renderer.rs:358-361).
+// goes through the pixel's top-left corner u = x / w, v = y / h (renderer.rs:358-361).  The
+// normal accumulator's object transform is P.acc (16 floats).
 template <int STACK>
 __global__ void __launch_bounds__(64) k_render(GBlas b, RenderParams P, const float* __restrict__ normals,
                                                uint8_t* __restrict__ rgba, LeafPolicy pol, uint32_t* err) {
@@ -477,97 +436,16 @@ __global__ void __launch_bounds__(64) k_render(GBlas b, RenderParams P, const fl
     const int x = (tile % tiles_x) * 8 + (threadIdx.x & 7);
     const int y = (tile / tiles_x) * 8 + (threadIdx.x >> 3);
     const bool active = x < P.width && y < P.height;  // all lanes stay for the cooperative leaf steps
-    const float* C = P.cam;
-    float u = __fdiv_rn((float)x, (float)P.width);
-    float v = __fdiv_rn((float)y, (float)P.height);
-    // Camera::get_ray_eye (camera.rs:994-1002)
-    float3 tl = make_float3(C[0], C[1], C[2]), tr = make_float3(C[3], C[4], C[5]), bl = make_float3(C[6], C[7], C[8]);
-    float3 org = make_float3(0.0f, 0.0f, 0.0f);
-    float3 p = make_float3(fadd(org.x, tl.x), fadd(org.y, tl.y), fadd(org.z, tl.z));
-    p = make_float3(fadd(p.x, fmul(fsub(tr.x, tl.x), u)), fadd(p.y, fmul(fsub(tr.y, tl.y), u)),
-                    fadd(p.z, fmul(fsub(tr.z, tl.z), u)));
-    p = make_float3(fadd(p.x, fmul(fsub(bl.x, tl.x), v)), fadd(p.y, fmul(fsub(bl.y, tl.y), v)),
-                    fadd(p.z, fmul(fsub(bl.z, tl.z), v)));
-    float3 dir = normalize3(make_float3(fsub(p.x, org.x), fsub(p.y, org.y), fsub(p.z, org.z)));
-    // Camera::get_ray_world (camera.rs:1004-1010)
-    float3 o = xf_point(C + 9, org);
-    float3 d = xf_vector(C + 9, dir);
+    float3 o, d;
+    camera_ray(P, x, y, o, d);
     LaneRay lr;
     init_lane_ray(lr, o, d, FLT_MAX);
     warp_trace<LocalStack<STACK>>(b, active, lr, pol, err, nullptr);
     if (!active) return;
-    const float t = lr.ct, hu = lr.hu, hv = lr.hv;
-    const uint32_t hp = lr.hp;
-    const bool hit = lr.hit && t < FLT_MAX;
-    float3 rad = make_float3(0.0f, 0.0f, 0.0f);
-    switch (P.acc_kind) {
-        case BVHGPU_ACC_INTERSECTION:  // renderer.rs:145-153
-            rad = hit ? make_float3(P.acc[0], P.acc[1], P.acc[2]) : make_float3(P.acc[3], P.acc[4], P.acc[5]);
-            break;
-        case BVHGPU_ACC_DEPTH: {  // renderer.rs:184-193
-            float tt = hit ? t : FLT_MAX;
-            rad = make_float3(tt, tt, tt);
-            break;
-        }
-        case BVHGPU_ACC_UV:  // renderer.rs:233-244
-            if (hit) rad = make_float3(hu, hv, fsub(1.0f, fadd(hu, hv)));
-            break;
-        case BVHGPU_ACC_NORMAL:  // renderer.rs:256-285
-            if (hit) {
-                const float* nn = normals + 9ull * hp;
-                float w0 = fsub(fsub(1.0f, hu), hv);
-                float3 nm;
-                nm.x = fadd(fadd(fmul(nn[0], w0), fmul(nn[3], hu)), fmul(nn[6], hv));
-                nm.y = fadd(fadd(fmul(nn[1], w0), fmul(nn[4], hu)), fmul(nn[7], hv));
-                nm.z = fadd(fadd(fmul(nn[2], w0), fmul(nn[5], hu)), fmul(nn[8], hv));
-                float3 nz = normalize3(xf_vector(P.acc, nm));
-                rad = make_float3(fmul(fadd(nz.x, 1.0f), 0.5f), fmul(fadd(nz.y, 1.0f), 0.5f),
-                                  fmul(fadd(nz.z, 1.0f), 0.5f));
-            }
-            break;
-        case BVHGPU_ACC_TEXTURE:  // TextureMaterialAccumulator, renderer.rs:289-334
-            if (hit) {
-                const float* tc = P.tex_coords + 6ull * hp;
-                const float w0 = fsub(fsub(1.0f, hu), hv);
-                const float uvx = fadd(fadd(fmul(tc[0], w0), fmul(tc[2], hu)), fmul(tc[4], hv));
-                const float uvy = fadd(fadd(fmul(tc[1], w0), fmul(tc[3], hu)), fmul(tc[5], hv));
-                // TextureMaterial::evaluate (materials/material.rs:44-52)
-                const unsigned long long iu = f32_as_usize(fmul(uvx, __uint2float_rn(P.tex_w))) % P.tex_w;
-                const unsigned long long iv = f32_as_usize(fmul(uvy, __uint2float_rn(P.tex_h))) % P.tex_h;
-                const uint8_t* px = P.texels + 3ull * (iv * P.tex_w + iu);
-                const float sc = 0.00390625f;  // 1 / 256, exact
-                rad = make_float3(fmul(__uint2float_rn(px[0]), sc), fmul(__uint2float_rn(px[1]), sc),
-                                  fmul(__uint2float_rn(px[2]), sc));
-            }
-            break;
-        default:
-            break;
-    }
-    uchar4 c;
-    switch (P.shader_kind) {
-        case BVHGPU_SHADER_INTERSECTION: {  // renderer.rs:166-173
-            bool nz = !(rad.x == 0.0f && rad.y == 0.0f && rad.z == 0.0f);
-            const float* s = nz ? P.sh : P.sh + 4;
-            c = make_uchar4((uint8_t)s[0], (uint8_t)s[1], (uint8_t)s[2], (uint8_t)s[3]);
-            break;
-        }
-        case BVHGPU_SHADER_DEPTH: {  // renderer.rs:207-221 (u32 arithmetic wraps)
-            if (rad.x < FLT_MAX) {
-                uint32_t col = 255u - (uint32_t)f32_as_i32(fmul(fsub(rad.x, P.sh[1]), P.sh[0]));
-                uint32_t cc = col * 0x010101u;
-                c = make_uchar4((uint8_t)((cc & 0x00FF0000u) >> 16), (uint8_t)((cc & 0x0000FF00u) >> 8),
-                                (uint8_t)(cc & 0xFFu), 255);
-            } else {
-                c = make_uchar4(0, 0, 0, 255);
-            }
-            break;
-        }
-        default:  // RadianceToRgbShader (renderer.rs:124-131)
-            c = make_uchar4(f32_as_u8(fmul(255.0f, rad.x)), f32_as_u8(fmul(255.0f, rad.y)),
-                            f32_as_u8(fmul(255.0f, rad.z)), 255);
-            break;
-    }
-    reinterpret_cast<uchar4*>(rgba)[(size_t)y * P.width + x] = c;
+    const bool hit = lr.hit && lr.ct < FLT_MAX;
+    const float3 rad = accumulate(P, hit, lr.ct, lr.hu, lr.hv, lr.hp, normals, P.acc, P.tex_coords, P.texels,
+                                  P.tex_w, P.tex_h);
+    reinterpret_cast<uchar4*>(rgba)[(size_t)y * P.width + x] = shade(P, rad);
 }
 
 }  // namespace
@@ -687,6 +565,14 @@ cudaError_t launch_bounce_rays(bvhgpu_ctx* ctx, const DeviceBlas& b, const float
     return cudaGetLastError();
 }
 
+bool batch_table_current(const bvhgpu_ctx* ctx, const bvhgpu_batch_item* items, uint32_t nitems) {
+    return ctx->batch_items.size() == nitems && ctx->batch_table != nullptr &&
+           std::equal(items, items + nitems, ctx->batch_items.begin(),
+                      [](const bvhgpu_batch_item& a, const bvhgpu_batch_item& b) {
+                          return a.blas == b.blas && a.ray_offset == b.ray_offset && a.ray_count == b.ray_count;
+                      });
+}
+
 cudaError_t launch_trace_batch(bvhgpu_ctx* ctx, const std::vector<const DeviceBlas*>& blases,
                                const bvhgpu_batch_item* items, uint32_t nitems, const float4* rays, uint32_t nrays,
                                int mode, void* hits, cudaStream_t s) {
@@ -701,12 +587,7 @@ cudaError_t launch_trace_batch(bvhgpu_ctx* ctx, const std::vector<const DeviceBl
         return cudaSuccess;
     }
     // persistent: a device table of (BLAS, ray offset, work prefix), cached across calls
-    bool same = ctx->batch_items.size() == nitems && ctx->batch_table != nullptr &&
-                std::equal(items, items + nitems, ctx->batch_items.begin(),
-                           [](const bvhgpu_batch_item& a, const bvhgpu_batch_item& b) {
-                               return a.blas == b.blas && a.ray_offset == b.ray_offset && a.ray_count == b.ray_count;
-                           });
-    if (!same) {
+    if (!batch_table_current(ctx, items, nitems)) {
         std::vector<BatchEntry> table(nitems);
         uint32_t total = 0;
         uint32_t depth = 1;
@@ -774,21 +655,7 @@ cudaError_t launch_render(bvhgpu_ctx* ctx, const DeviceBlas& b, const bvhgpu_cam
                           const float* acc_params, int shader, const float* shader_params, const float* d_normals,
                           const float* d_tex_coords, const uint8_t* d_texels, uint32_t tex_w, uint32_t tex_h,
                           uint8_t* d_rgba, cudaStream_t s) {
-    RenderParams P;
-    std::copy(cam.top_left, cam.top_left + 3, P.cam);
-    std::copy(cam.top_right, cam.top_right + 3, P.cam + 3);
-    std::copy(cam.bottom_left, cam.bottom_left + 3, P.cam + 6);
-    std::copy(cam.view_inv, cam.view_inv + 16, P.cam + 9);
-    std::fill(P.acc, P.acc + 16, 0.0f);
-    std::fill(P.sh, P.sh + 8, 0.0f);
-    if (acc == BVHGPU_ACC_INTERSECTION && acc_params) std::copy(acc_params, acc_params + 6, P.acc);
-    if (acc == BVHGPU_ACC_NORMAL && acc_params) std::copy(acc_params, acc_params + 16, P.acc);
-    if (shader == BVHGPU_SHADER_INTERSECTION && shader_params) std::copy(shader_params, shader_params + 8, P.sh);
-    if (shader == BVHGPU_SHADER_DEPTH && shader_params) std::copy(shader_params, shader_params + 2, P.sh);
-    P.width = w;
-    P.height = h;
-    P.acc_kind = acc;
-    P.shader_kind = shader;
+    RenderParams P = make_render_params(cam, w, h, acc, acc_params, shader, shader_params);
     P.tex_coords = d_tex_coords;
     P.texels = d_texels;
     P.tex_w = tex_w;

@@ -26,7 +26,9 @@ constexpr uint32_t kNone = 0xFFFFFFFFu;
 // Scratch: parent link and arrival counter per node (2 x 4 bytes x BVHGPU_NOALLOC_MAX_NODES = 8 MiB).
 static __device__ __align__(256) uint32_t g_refit_scratch[2u * BVHGPU_NOALLOC_MAX_NODES];
 
-// Device address of g_refit_scratch per device, looked up once with that device current.
+// Device address of g_refit_scratch per device, looked up once with that device current (the
+// first call on the device).  cudaDeviceReset destroys the context that address belongs to, so a
+// process that resets a device must not call bvhgpu_refit_noalloc on that device afterwards.
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
 uint32_t* g_scratch_addr[kMaxDevices] = {};
@@ -57,8 +59,14 @@ __device__ __forceinline__ float max_ni(float a, float b) {
     return (b > a) ? b : a;
 }
 
-// Parent links of every branch's two children.  Indices are checked; a malformed node is
-// skipped and reported in *status.
+// Status values OR-ed into the caller's *status word for malformed node arrays.
+constexpr uint32_t kBadChild = 1u;     // a branch's child index is out of range or not above it
+constexpr uint32_t kBadLeaf = 2u;      // a leaf addresses triangles past ntris
+constexpr uint32_t kSharedChild = 4u;  // a node claimed as a child by two branches
+
+// Parent links of every branch's two children.  Indices are checked before any access; a
+// malformed branch is skipped and reported in *status.  A child index is always above its
+// parent's, so the bottom-up walk below only moves to lower indices and ends.
 __global__ void k_links(const bvhgpu_node* __restrict__ nodes, uint32_t nodes_used, uint32_t* parent,
                         uint32_t* status) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -67,11 +75,14 @@ __global__ void k_links(const bvhgpu_node* __restrict__ nodes, uint32_t nodes_us
     if (n.primitive_count != 0u) return;
     uint32_t l = n.left_first;
     if (l <= i || l < 2u || (uint64_t)l + 1u >= nodes_used) {
-        if (status) atomicOr(status, 1u);
+        if (status) atomicOr(status, kBadChild);
         return;
     }
-    parent[l] = i;
-    parent[l + 1u] = i;
+    // first claim wins; a second branch claiming the same child is reported (and, missing an
+    // arrival, never computed)
+    const uint32_t a = atomicCAS(&parent[l], kNone, i);
+    const uint32_t b = atomicCAS(&parent[l + 1u], kNone, i);
+    if ((a != kNone || b != kNone) && status) atomicOr(status, kSharedChild);
 }
 
 // Bottom-up refit: one thread per leaf; the second child to arrive at a parent computes it.
@@ -84,7 +95,7 @@ __global__ void k_refit_nodes(bvhgpu_node* nodes, uint32_t nodes_used, const flo
     if (cnt == 0u) return;
     const uint32_t first = nodes[i].left_first;
     if ((uint64_t)first + cnt > ntris) {
-        if (status) atomicOr(status, 2u);
+        if (status) atomicOr(status, kBadLeaf);
         return;
     }
     float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX};
@@ -134,9 +145,12 @@ extern "C" int bvhgpu_refit_noalloc(bvhgpu_node* d_nodes, uint32_t nodes_used, c
     if (cudaMemsetAsync(parent, 0xFF, 4ull * nodes_used, s) != cudaSuccess ||
         cudaMemsetAsync(counters, 0, 4ull * nodes_used, s) != cudaSuccess)
         return BVHGPU_ERR_CUDA;
+    // launch errors are read with cudaPeekAtLastError, which leaves the runtime's error state as
+    // it is for the caller's own error handling
     const unsigned grid = (nodes_used + 127u) / 128u;
     k_links<<<grid, 128, 0, s>>>(d_nodes, nodes_used, parent, d_status);
+    if (cudaPeekAtLastError() != cudaSuccess) return BVHGPU_ERR_CUDA;
     k_refit_nodes<<<grid, 128, 0, s>>>(d_nodes, nodes_used, reinterpret_cast<const float*>(d_tris), ntris, parent,
                                        counters, d_status);
-    return cudaGetLastError() == cudaSuccess ? BVHGPU_OK : BVHGPU_ERR_CUDA;
+    return cudaPeekAtLastError() == cudaSuccess ? BVHGPU_OK : BVHGPU_ERR_CUDA;
 }

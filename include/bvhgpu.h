@@ -273,7 +273,10 @@ int bvhgpu_blas_bounce_rays(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhgpu_ray*
 
 /* Uneven batch of scenes in one call: Scene::intersect repeated over many scenes.
  * mode BVHGPU_MODE_PLAIN launches once per item; BVHGPU_MODE_PERSISTENT runs one
- * work-stealing launch over all items. */
+ * work-stealing launch over all items, from a device table of the items that the context keeps
+ * and rebuilds (synchronously) when the item list changes -- so under graph capture
+ * (bvhgpu_graph_begin) a persistent batch must use the item list of an earlier call, else
+ * BVHGPU_ERR_INVALID_ARG. */
 int bvhgpu_trace_batch(bvhgpu_ctx* ctx, const bvhgpu_batch_item* items, uint32_t nitems,
                        const bvhgpu_ray* rays, uint32_t nrays, int mode, bvhgpu_hit* hits);
 int bvhgpu_trace_batch_async(bvhgpu_ctx* ctx, const bvhgpu_batch_item* items, uint32_t nitems,
@@ -346,6 +349,34 @@ int bvhgpu_render(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhgpu_camera* camera
 int bvhgpu_render_textured(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhgpu_camera* camera, int width, int height,
                            const float* tex_coords, const uint8_t* texels, uint32_t tex_w, uint32_t tex_h,
                            int shader, const float* shader_params, uint8_t* rgba, uint64_t* rays_traced);
+
+/* Shading data of a BLAS's model -- what Model holds beside the BVH (BT/src/model/model.rs:16-24,
+ * mesh normals and texture coordinates of BT/src/mesh/mesh.rs, the texture of
+ * BT/src/materials/material.rs) and what bvhgpu_render_scene's normal and texture accumulators read:
+ * corner normals (9 floats per triangle), corner texture coordinates (6 floats per triangle), both
+ * in the BLAS's triangle order, and an RGB8 texture (texels, tex_w x tex_h, row-major).  Each
+ * pointer may be NULL (that array is kept as it is).  Synchronous (copies the data to the device). */
+int bvhgpu_blas_set_shading(bvhgpu_ctx* ctx, uint32_t blas_id, const float* normals, const float* tex_coords,
+                            const uint8_t* texels, uint32_t tex_w, uint32_t tex_h);
+/* Integrator::evaluate for PathTracer on a whole Scene (BT/src/renderer.rs:104-106, 345-384 ->
+ * Scene::intersect, BT/src/scene/scene.rs:32-34): every pixel's camera ray through the TLAS and the
+ * instances' BLASes, then the accumulator (any BVHGPU_ACC_*) and the shader -> RGBA8 (row-major,
+ * w*h*4 bytes).  acc_params only for BVHGPU_ACC_INTERSECTION (hit rgb, miss rgb); the normal
+ * accumulator's transform is the looked-up object's own (SceneObject::get_transform).  The normal
+ * and texture accumulators look up the model named by the hit's InstancePrimitiveIndex
+ * (renderer.rs:258-263, 312-317):
+ *  BVHGPU_LOOKUP_REFERENCE: what the reference computes -- its Bvh::intersect always packs
+ *    instance 0 (bvh.rs:296, intersection.rs:63-66), so object 0's model and transform, with the
+ *    primitive id's low 20 bits;
+ *  BVHGPU_LOOKUP_HIT_OBJECT: the hit's own object and primitive.
+ * A primitive outside the looked-up model's shading data (the reference panics: slice index out of
+ * bounds), or a model without the needed data, returns BVHGPU_ERR_INVALID_ARG after the frame
+ * (those pixels get zero radiance).  Returns rays traced in *rays_traced. */
+#define BVHGPU_LOOKUP_REFERENCE 0
+#define BVHGPU_LOOKUP_HIT_OBJECT 1
+int bvhgpu_render_scene(bvhgpu_ctx* ctx, uint32_t scene_id, const bvhgpu_camera* camera, int width, int height,
+                        int accumulator, const float* acc_params, int shader, const float* shader_params, int lookup,
+                        uint8_t* rgba, uint64_t* rays_traced);
 
 /* ---- differentiable Lambertian render (not in the reference) ----------------------------------- */
 /* Indexed mesh over a BLAS: triangle i of the BLAS is (verts[faces[3i]], verts[faces[3i+1]],
@@ -501,9 +532,12 @@ int bvhgpu_scene_run_async(bvhgpu_ctx* ctx, uint32_t scene_id, float dt, bvhgpu_
  * device address (cudaGetSymbolAddress) with that device current; make that first call before any
  * stream capture.  Every call shares the one scratch array and resets the part it uses, so calls
  * whose work overlaps on the GPU (different streams, or different threads with the same device)
- * race and must be serialised by the caller.  If d_status (device, caller-owned, may be NULL) is
- * given, bit 1 is OR-ed in for a branch with a bad child index and bit 2 for a leaf addressing
- * triangles past ntris (such nodes are skipped); the caller clears it. */
+ * race and must be serialised by the caller.  A process that calls cudaDeviceReset on a device must
+ * not call this entry point on that device afterwards (the looked-up address belonged to the
+ * destroyed context).  If d_status (device, caller-owned, may be NULL) is given, the value 1 is
+ * OR-ed in for a branch whose child index is out of range or not above its own, 2 for a leaf
+ * addressing triangles past ntris, 4 for a node that two branches claim as a child; such nodes
+ * are skipped, and their ancestors keep their old bounds.  The caller clears it. */
 #define BVHGPU_NOALLOC_MAX_NODES (1u << 20)
 int bvhgpu_refit_noalloc(bvhgpu_node* d_nodes, uint32_t nodes_used, const bvhgpu_triangle* d_tris, uint32_t ntris,
                          bvhgpu_stream stream, uint32_t* d_status);

@@ -1222,12 +1222,102 @@ static inline int32_t rust_f32_as_i32(float x) {
     return (int32_t)x;
 }
 
+// The accumulators of renderer.rs:134-334 for one camera ray's closest hit (`hit`, record h), then
+// the pixel shaders of renderer.rs:116-222 into o[4].  normals / tex_coords / texels are the
+// looked-up model's (per-triangle corner normals, 9 floats; corner texture coordinates, 6 floats;
+// RGB8 texture, row-major tex_w x tex_h); normal_xf is the object transform applied to the
+// interpolated normal (Transform3::transform_vector).  Returns ORC_ERR_ARG for an unknown kind.
+static int shade_pixel(int accumulator, const float* P, int shader, const float* S, bool hit, const Hit& h,
+                       const float* normals, const float* normal_xf, const float* tex_coords, const uint8_t* texels,
+                       uint32_t tex_w, uint32_t tex_h, uint8_t* o, float* radiance) {
+    V3 rad = mk(0, 0, 0);
+    switch (accumulator) {
+        case ACC_INTERSECTION:
+            rad = hit ? mk(P[0], P[1], P[2]) : mk(P[3], P[4], P[5]);
+            break;
+        case ACC_DEPTH: {
+            float t = hit ? h.t : FLT_MAX;
+            rad = mk(t, t, t);
+            break;
+        }
+        case ACC_UV:
+            rad = hit ? mk(h.u, h.v, 1.0f - (h.u + h.v)) : mk(0, 0, 0);
+            break;
+        case ACC_NORMAL: {
+            if (hit) {
+                const float* nn = normals + 9 * (size_t)h.prim;
+                V3 n0 = mk(nn[0], nn[1], nn[2]), n1 = mk(nn[3], nn[4], nn[5]), n2 = mk(nn[6], nn[7], nn[8]);
+                float w0 = 1.0f - h.u - h.v;
+                V3 nm = add(add(muls(n0, w0), muls(n1, h.u)), muls(n2, h.v));
+                V3 nw = xf_vector(normal_xf, nm);
+                V3 nz = normalize(nw);
+                rad = muls(add(nz, mk(1.0f, 1.0f, 1.0f)), 0.5f);
+            }
+            break;
+        }
+        case ACC_TEXTURE: {
+            if (hit) {
+                const float* tc = tex_coords + 6 * (size_t)h.prim;
+                const float w0 = 1.0f - h.u - h.v;
+                // tex_coords[0] * (1 - u - v) + tex_coords[1] * u + tex_coords[2] * v
+                const float uvx = (tc[0] * w0 + tc[2] * h.u) + tc[4] * h.v;
+                const float uvy = (tc[1] * w0 + tc[3] * h.u) + tc[5] * h.v;
+                const uint64_t iu = rust_f32_as_usize(uvx * (float)tex_w) % tex_w;
+                const uint64_t iv = rust_f32_as_usize(uvy * (float)tex_h) % tex_h;
+                const uint8_t* px = texels + 3 * (iv * tex_w + iu);
+                const float sc = 1.0f / 256.0f;  // rgb8_to_rgb32f
+                rad = mk((float)px[0] * sc, (float)px[1] * sc, (float)px[2] * sc);
+            }
+            break;
+        }
+        default:
+            return ORC_ERR_ARG;
+    }
+    if (radiance) {
+        radiance[0] = rad.x; radiance[1] = rad.y; radiance[2] = rad.z;
+    }
+    switch (shader) {
+        case SH_RADIANCE:
+            o[0] = rust_f32_as_u8(255.0f * rad.x);
+            o[1] = rust_f32_as_u8(255.0f * rad.y);
+            o[2] = rust_f32_as_u8(255.0f * rad.z);
+            o[3] = 255;
+            break;
+        case SH_INTERSECTION: {
+            // shader params: hit rgba, miss rgba (0..255)
+            bool nz = !(rad.x == 0.0f && rad.y == 0.0f && rad.z == 0.0f);
+            const float* c = nz ? S : S + 4;
+            o[0] = (uint8_t)c[0]; o[1] = (uint8_t)c[1]; o[2] = (uint8_t)c[2]; o[3] = (uint8_t)c[3];
+            break;
+        }
+        case SH_DEPTH: {
+            float scale = S[0], offset = S[1];
+            float t = rad.x;
+            if (t < FLT_MAX) {
+                uint32_t col = 255u - (uint32_t)rust_f32_as_i32((t - offset) * scale);
+                uint32_t c = col * 0x010101u;
+                o[0] = (uint8_t)((c & 0x00FF0000u) >> 16);
+                o[1] = (uint8_t)((c & 0x0000FF00u) >> 8);
+                o[2] = (uint8_t)(c & 0x000000FFu);
+            } else {
+                o[0] = 0; o[1] = 0; o[2] = 0;
+            }
+            o[3] = 255;
+            break;
+        }
+        default:
+            return ORC_ERR_ARG;
+    }
+    return ORC_OK;
+}
+
 // renderer.rs:345-384 (PathTracer::evaluate) with the accumulators of renderer.rs:134-286
 // and the shaders of renderer.rs:116-222.  The frame is w x h with 8x8 tiles; the
 // reference's fixed 80x80 tile grid is the w = h = 640 case.
 // TextureMaterialAccumulator (renderer.rs:289-334) reads per-corner texture coordinates (6 floats
 // per triangle) and an RGB8 texture (row-major, tex_w x tex_h) through TextureMaterial::evaluate
-// (materials/material.rs:44-52).
+// (materials/material.rs:44-52).  For the normal accumulator the object transform comes in
+// acc_params (16 floats).
 int orc_render_textured(const float corners[9], const float view_inv[16], int width, int height, int accumulator,
                         const float* acc_params, int shader, const float* shader_params, const orc_node* nodes,
                         uint32_t nodes_used, const orc_tri* tris, uint32_t ntris, const float* normals,
@@ -1251,87 +1341,76 @@ int orc_render_textured(const float corners[9], const float view_inv[16], int wi
             Ray r = load_ray(rr);
             Hit h{0, 0, 0, 0};
             bool hit = bvh_intersect_impl(node_at, tri_at, 0, r, &h, nullptr);
-            V3 rad = mk(0, 0, 0);
-            switch (accumulator) {
-                case ACC_INTERSECTION:
-                    rad = hit ? mk(P[0], P[1], P[2]) : mk(P[3], P[4], P[5]);
-                    break;
-                case ACC_DEPTH: {
-                    float t = hit ? h.t : FLT_MAX;
-                    rad = mk(t, t, t);
-                    break;
+            size_t pix = (size_t)y * width + x;
+            int rc = shade_pixel(accumulator, P, shader, S, hit, h, normals, P, tex_coords, texels, tex_w, tex_h,
+                                 rgba + 4 * pix, radiance ? radiance + 3 * pix : nullptr);
+            if (rc != ORC_OK) return rc;
+        }
+    }
+    return ORC_OK;
+}
+
+// PathTracer::evaluate over a whole Scene (renderer.rs:345-384 -> Scene::intersect, scene.rs:32-34,
+// tlas.rs:123-177, scene_object.rs:78-89), accumulators of renderer.rs:134-334.  The normal and
+// texture accumulators look up `scene.get_unchecked(instance_index)` with the instance and primitive
+// indices of the hit's InstancePrimitiveIndex (renderer.rs:258-263, 312-317):
+//  lookup 0 (the reference): Bvh::intersect packs instance 0 (InstancePrimitiveIndex::from_primitive,
+//    bvh.rs:296, intersection.rs:63-66), so every hit reads object 0's model and transform, with the
+//    primitive index masked to its 20 bits (intersection.rs:57-60); an index outside object 0's mesh
+//    panics in the reference (slice index out of bounds) -> ORC_ERR_PANIC;
+//  lookup 1: the hit's own object and primitive.
+// Per BLAS bl: nodes at node_off[bl], triangles (and their normals / texture coordinates, 9 / 6 floats
+// each) at tri_off[bl] with tri_count[bl] of them, texture at texel_off[bl] (bytes) of tex_w[bl] x
+// tex_h[bl].  xf: object transforms (16 floats, column-major); inv: their cached inverses.
+int orc_render_scene(const float corners[9], const float view_inv[16], int width, int height, int accumulator,
+                     const float* acc_params, int shader, const float* shader_params, const orc_tlas_node* tlas,
+                     const uint32_t* blas_of, const float* xf, const float* inv, uint32_t nobj,
+                     const orc_node* nodes, const uint32_t* node_off, const orc_tri* tris, const uint32_t* tri_off,
+                     const uint32_t* tri_count, const float* normals, const float* tex_coords, const uint8_t* texels,
+                     const uint64_t* texel_off, const uint32_t* tex_w, const uint32_t* tex_h, int lookup,
+                     uint8_t* rgba, float* radiance) {
+    if (width <= 0 || height <= 0 || !tlas || !blas_of || !xf || !inv || !nodes || !node_off || !tris ||
+        !tri_off || !tri_count || !rgba || nobj == 0)
+        return ORC_ERR_ARG;
+    if (accumulator == ACC_NORMAL && !normals) return ORC_ERR_ARG;
+    if (accumulator == ACC_TEXTURE && (!tex_coords || !texels || !texel_off || !tex_w || !tex_h)) return ORC_ERR_ARG;
+    const float* P = acc_params;
+    const float* S = shader_params;
+    if (accumulator == ACC_INTERSECTION && !P) return ORC_ERR_ARG;
+    if ((shader == SH_INTERSECTION || shader == SH_DEPTH) && !S) return ORC_ERR_ARG;
+    SceneView sv{tlas, blas_of, inv, nobj, nodes, node_off, tris, tri_off};
+    for (int y = 0; y < height; ++y) {
+        for (int x = 0; x < width; ++x) {
+            orc_ray rr;
+            orc_camera_ray(corners, view_inv, (float)x / (float)width, (float)y / (float)height, &rr);
+            orc_hit oh;
+            const bool hit = scene_intersect_one(sv, load_ray(rr), &oh, nullptr, 0);
+            Hit h{oh.t, oh.u, oh.v, oh.prim};
+            const float* nrm = nullptr;
+            const float* tc = nullptr;
+            const uint8_t* tex = nullptr;
+            uint32_t tw = 0, th = 0;
+            const float* oxf = xf;
+            if (hit && (accumulator == ACC_NORMAL || accumulator == ACC_TEXTURE)) {
+                const uint32_t obj = lookup ? oh.inst : 0u;
+                const uint32_t prim = lookup ? oh.prim : (oh.prim & 0x000FFFFFu);
+                const uint32_t bl = blas_of[obj];
+                if (prim >= tri_count[bl]) return ORC_ERR_PANIC;
+                h.prim = prim;
+                oxf = xf + 16 * (size_t)obj;
+                if (normals) nrm = normals + 9 * (size_t)tri_off[bl];
+                if (tex_coords) tc = tex_coords + 6 * (size_t)tri_off[bl];
+                if (accumulator == ACC_TEXTURE) {
+                    tex = texels + texel_off[bl];
+                    tw = tex_w[bl];
+                    th = tex_h[bl];
+                    if (tw == 0 || th == 0) return ORC_ERR_ARG;
                 }
-                case ACC_UV:
-                    rad = hit ? mk(h.u, h.v, 1.0f - (h.u + h.v)) : mk(0, 0, 0);
-                    break;
-                case ACC_NORMAL: {
-                    if (hit) {
-                        const float* nn = normals + 9 * (size_t)h.prim;
-                        V3 n0 = mk(nn[0], nn[1], nn[2]), n1 = mk(nn[3], nn[4], nn[5]), n2 = mk(nn[6], nn[7], nn[8]);
-                        float w0 = 1.0f - h.u - h.v;
-                        V3 nm = add(add(muls(n0, w0), muls(n1, h.u)), muls(n2, h.v));
-                        // object transform (accumulator params, 16 floats) applied as a vector
-                        V3 nw = xf_vector(P, nm);
-                        V3 nz = normalize(nw);
-                        rad = muls(add(nz, mk(1.0f, 1.0f, 1.0f)), 0.5f);
-                    }
-                    break;
-                }
-                case ACC_TEXTURE: {
-                    if (hit) {
-                        const float* tc = tex_coords + 6 * (size_t)h.prim;
-                        const float w0 = 1.0f - h.u - h.v;
-                        // tex_coords[0] * (1 - u - v) + tex_coords[1] * u + tex_coords[2] * v
-                        const float uvx = (tc[0] * w0 + tc[2] * h.u) + tc[4] * h.v;
-                        const float uvy = (tc[1] * w0 + tc[3] * h.u) + tc[5] * h.v;
-                        const uint64_t iu = rust_f32_as_usize(uvx * (float)tex_w) % tex_w;
-                        const uint64_t iv = rust_f32_as_usize(uvy * (float)tex_h) % tex_h;
-                        const uint8_t* px = texels + 3 * (iv * tex_w + iu);
-                        const float sc = 1.0f / 256.0f;  // rgb8_to_rgb32f
-                        rad = mk((float)px[0] * sc, (float)px[1] * sc, (float)px[2] * sc);
-                    }
-                    break;
-                }
-                default:
-                    return ORC_ERR_ARG;
             }
             size_t pix = (size_t)y * width + x;
-            if (radiance) {
-                radiance[3 * pix] = rad.x; radiance[3 * pix + 1] = rad.y; radiance[3 * pix + 2] = rad.z;
-            }
-            uint8_t* o = rgba + 4 * pix;
-            switch (shader) {
-                case SH_RADIANCE:
-                    o[0] = rust_f32_as_u8(255.0f * rad.x);
-                    o[1] = rust_f32_as_u8(255.0f * rad.y);
-                    o[2] = rust_f32_as_u8(255.0f * rad.z);
-                    o[3] = 255;
-                    break;
-                case SH_INTERSECTION: {
-                    // shader params: hit rgba, miss rgba (0..255)
-                    bool nz = !(rad.x == 0.0f && rad.y == 0.0f && rad.z == 0.0f);
-                    const float* c = nz ? S : S + 4;
-                    o[0] = (uint8_t)c[0]; o[1] = (uint8_t)c[1]; o[2] = (uint8_t)c[2]; o[3] = (uint8_t)c[3];
-                    break;
-                }
-                case SH_DEPTH: {
-                    float scale = S[0], offset = S[1];
-                    float t = rad.x;
-                    if (t < FLT_MAX) {
-                        uint32_t col = 255u - (uint32_t)rust_f32_as_i32((t - offset) * scale);
-                        uint32_t c = col * 0x010101u;
-                        o[0] = (uint8_t)((c & 0x00FF0000u) >> 16);
-                        o[1] = (uint8_t)((c & 0x0000FF00u) >> 8);
-                        o[2] = (uint8_t)(c & 0x000000FFu);
-                    } else {
-                        o[0] = 0; o[1] = 0; o[2] = 0;
-                    }
-                    o[3] = 255;
-                    break;
-                }
-                default:
-                    return ORC_ERR_ARG;
-            }
+            int rc = shade_pixel(accumulator, P, shader, S, hit, h, nrm, oxf, tc, tex, tw, th, rgba + 4 * pix,
+                                 radiance ? radiance + 3 * pix : nullptr);
+            if (rc != ORC_OK) return rc;
         }
     }
     return ORC_OK;

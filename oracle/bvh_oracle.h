@@ -121,7 +121,7 @@ int orc_scene_intersect_mt(const orc_tlas_node* tlas, uint32_t tlas_nodes_used,
  * view_inv = 16 floats column-major. */
 void orc_camera_ray(const float corners[9], const float view_inv[16], float u, float v, orc_ray* out);
 /* PathTracer::evaluate over a w x h frame (8x8 tiles, pixel top-left corner samples) on a
- * single BLAS (nobj == 0) or a scene; accumulator / shader kinds as in include/bvhgpu.h. */
+ * single BLAS; accumulator / shader kinds as in include/bvhgpu.h. */
 int orc_render_textured(const float corners[9], const float view_inv[16], int width, int height, int accumulator,
                         const float* acc_params, int shader, const float* shader_params, const orc_node* nodes,
                         uint32_t nodes_used, const orc_tri* tris, uint32_t ntris, const float* normals,
@@ -132,6 +132,20 @@ int orc_render(const float corners[9], const float view_inv[16], int width, int 
                const orc_node* nodes, uint32_t nodes_used, const orc_tri* tris, uint32_t ntris,
                const float* normals /* 9 floats per triangle, may be NULL */,
                uint8_t* rgba, float* radiance);
+
+/* PathTracer::evaluate over a Scene (the TLAS with instance transforms).  lookup 0: the normal /
+ * texture accumulators read object 0's model and transform with the 20-bit primitive index, as the
+ * reference does (ORC_ERR_PANIC where its slice index would be out of bounds); lookup 1: the hit's
+ * own object.  Per-BLAS arrays are concatenated: nodes at node_off[bl], triangles, normals (9 floats)
+ * and texture coordinates (6 floats) at tri_off[bl] (tri_count[bl] of them), texels at byte
+ * texel_off[bl] (tex_w[bl] x tex_h[bl] RGB8). */
+int orc_render_scene(const float corners[9], const float view_inv[16], int width, int height, int accumulator,
+                     const float* acc_params, int shader, const float* shader_params, const orc_tlas_node* tlas,
+                     const uint32_t* blas_of, const float* xf, const float* inv, uint32_t nobj,
+                     const orc_node* nodes, const uint32_t* node_off, const orc_tri* tris, const uint32_t* tri_off,
+                     const uint32_t* tri_count, const float* normals, const float* tex_coords, const uint8_t* texels,
+                     const uint64_t* texel_off, const uint32_t* tex_w, const uint32_t* tex_h, int lookup,
+                     uint8_t* rgba, float* radiance);
 
 /* --- bounce rays (not in the reference: cosine-weighted diffuse bounce) ---------------- */
 int orc_bounce_ray(const orc_ray* primary, const orc_hit* hit, const orc_tri* tri, uint32_t seed,

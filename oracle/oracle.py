@@ -93,6 +93,8 @@ def lib():
         L.orc_camera_ray.restype = None
         L.orc_render.argtypes = [P, P, i32, i32, i32, P, i32, P, P, u32, P, u32, P, P, P]
         L.orc_render_textured.argtypes = [P, P, i32, i32, i32, P, i32, P, P, u32, P, u32, P, P, P, u32, u32, P, P]
+        L.orc_render_scene.argtypes = [P, P, i32, i32, i32, P, i32, P, P, P, P, P, u32, P, P, P, P, P, P, P, P, P,
+                                       P, P, i32, P, P]
         L.orc_bounce_ray.argtypes = [P, P, P, u32, u32, P]
         L.orc_bounce_rays.argtypes = [P, P, u32, P, u32, P, P]
         L.orc_scene_bounce_rays.argtypes = [P, P, P, P, P, P, u32, u32, P, P]
@@ -340,6 +342,50 @@ def render(corners, view_inv, width, height, nodes, nodes_used, tris, accumulato
     if rc != 0:
         raise RuntimeError(f"oracle render failed ({rc})")
     return rgba, rad
+
+
+def render_scene(corners, view_inv, width, height, tlas, sa: SceneArrays, xf, accumulator, shader,
+                 acc_params=None, shader_params=None, normals=None, tex_coords=None, textures=None, lookup=0):
+    """PathTracer::evaluate over a scene (TLAS + instances).  normals / tex_coords: one array per BLAS
+    of `sa` ([ntris, 9] / [ntris, 6]) or None; textures: one [h, w, 3] uint8 array per BLAS or None.
+    lookup 0 = the reference's instance-0 lookup for the normal / texture accumulators, 1 = the hit's
+    object.  Raises PanicError where the reference would panic (a primitive index outside object 0's
+    mesh)."""
+    corners = _c(corners, np.float32).reshape(9)
+    view_inv = _c(view_inv, np.float32).reshape(16)
+    tlas = _c(tlas, TLAS_NODE)
+    xf = _c(xf, np.float32).reshape(-1, 16)
+    nb = len(sa.node_off)
+    counts = np.array([(sa.tri_off[i + 1] if i + 1 < nb else len(sa.tris)) - sa.tri_off[i] for i in range(nb)],
+                      np.uint32)
+    nrm = None if normals is None else _c(np.concatenate([np.asarray(a, np.float32).reshape(-1, 9)
+                                                          for a in normals]), np.float32)
+    tc = None if tex_coords is None else _c(np.concatenate([np.asarray(a, np.float32).reshape(-1, 6)
+                                                           for a in tex_coords]), np.float32)
+    tx = toff = tw = th = None
+    if textures is not None:
+        tx = _c(np.concatenate([np.asarray(t, np.uint8).reshape(-1) for t in textures]), np.uint8)
+        sizes = [np.asarray(t).size for t in textures]
+        toff = np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(np.uint64)
+        tw = np.array([np.asarray(t).shape[1] for t in textures], np.uint32)
+        th = np.array([np.asarray(t).shape[0] for t in textures], np.uint32)
+    ap = None if acc_params is None else _c(acc_params, np.float32)
+    sp = None if shader_params is None else _c(shader_params, np.float32)
+    rgba = np.zeros((height, width, 4), np.uint8)
+    rad = np.zeros((height, width, 3), np.float32)
+    rc = lib().orc_render_scene(_p(corners), _p(view_inv), width, height, accumulator, _p(ap), shader, _p(sp),
+                                _p(tlas), _p(sa.blas_of), _p(xf), _p(sa.inv), len(sa.blas_of), _p(sa.nodes),
+                                _p(sa.node_off), _p(sa.tris), _p(sa.tri_off), _p(counts), _p(nrm), _p(tc), _p(tx),
+                                _p(toff), _p(tw), _p(th), int(lookup), _p(rgba), _p(rad))
+    if rc == 2:
+        raise PanicError("the reference would panic: a hit's primitive index is outside object 0's mesh")
+    if rc != 0:
+        raise RuntimeError(f"oracle render_scene failed ({rc})")
+    return rgba, rad
+
+
+class PanicError(RuntimeError):
+    """The reference would panic on this input."""
 
 
 def bounce_rays(primaries, hits, tris, seed):

@@ -427,6 +427,33 @@ def test_uneven_batch_persistent_equals_plain_equals_oracle(ctx):
     assert_hits_equal(pers, ref, "batch persistent")
 
 
+def test_persistent_batch_in_a_graph_needs_a_known_item_list(ctx):
+    """A persistent batch sets up its item table synchronously, which a stream capture cannot
+    record: under capture a new item list is refused (status 1, nothing recorded, the capture still
+    ends cleanly); a list traced once before capture replays from the graph with the same hits."""
+    t1, b1 = build(scenes.soup(800, 31))
+    t2, b2 = build(scenes.displaced_icosphere(2, 32).triangles())
+    blas1, blas2 = ctx.upload_blas(b1, t1), ctx.upload_blas(b2, t2)
+    rays = np.concatenate([scenes.sphere_rays(3000, 33), scenes.sphere_rays(2000, 34, box=3.0)])
+    items = np.array([(blas1.id, 0, 3000, 0), (blas2.id, 3000, 2000, 0)], dtype=bt.BATCH_ITEM)
+    new_items = np.array([(blas2.id, 0, 2500, 0), (blas1.id, 2500, 2500, 0)], dtype=bt.BATCH_ITEM)
+    d_rays = ctx.to_device(rays)
+    d_hits = ctx.device_buffer(len(rays) * bt.HIT.itemsize)
+    expect = ctx.trace_batch(items, rays, bt.MODE_PERSISTENT)        # sets up `items`
+    ctx.graph_begin()
+    with pytest.raises(bt.BvhGpuError) as e:
+        ctx.trace_batch_async(new_items, d_rays, len(rays), bt.MODE_PERSISTENT, d_hits)
+    assert e.value.code == 1
+    ctx.trace_batch_async(items, d_rays, len(rays), bt.MODE_PERSISTENT, d_hits)
+    gid = ctx.graph_end()
+    d_hits.zero()
+    ctx.graph_launch(gid)
+    ctx.sync()
+    got = d_hits.download(np.zeros(len(rays), bt.HIT))
+    ctx.graph_free(gid)
+    assert got.tobytes() == expect.tobytes()
+
+
 # ---- errors -----------------------------------------------------------------------------------------
 
 def test_invalid_inputs_are_rejected(ctx):
