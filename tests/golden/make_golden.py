@@ -1,8 +1,8 @@
 """Generate the committed golden fixtures from the reference repository's assets.
 
-Run in a container that has the reference checkout (read-only) mounted:
+Run where a checkout of the reference repository is available, giving its root:
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <path to the lambdaxymox/bvhtracer checkout>
 
 It parses the reference's ``bvhtracer/assets/cube.obj`` the way the reference's
 ObjMeshDecoder does (BT/src/mesh/decoders.rs:157-215: one triangle per face,
@@ -104,4 +104,6 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py <path to the reference checkout>")
+    main(sys.argv[1])

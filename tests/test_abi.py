@@ -86,3 +86,18 @@ def test_tune_space_lists_every_compiled_variant():
         assert {c["hidden"] for c in space} == {0, 100, 250, 500, 1000}
     lib = _lib.load()
     assert lib.bvhgpu_tune_space(3, None, 0, None) == 1  # bounce generation has no variants
+
+
+def test_rust_sys_binding_is_generated_from_the_header():
+    """bvhgpu-sys/src/lib.rs is the generator's output for the current header (no cargo here to
+    compile it; this keeps the Rust declarations in step with include/bvhgpu.h), and it declares
+    every entry point of the header."""
+    import subprocess
+    import sys
+    crate = os.path.join(ROOT, "bvhtracer_gb300", "rust", "bvhgpu-sys")
+    rc = subprocess.run([sys.executable, os.path.join(crate, "gen_bindings.py"), "--check"]).returncode
+    assert rc == 0, "bvhgpu-sys/src/lib.rs is stale: rerun gen_bindings.py"
+    with open(os.path.join(crate, "src", "lib.rs")) as f:
+        rs = f.read()
+    rust_fns = set(re.findall(r"pub fn (bvhgpu_[a-z0-9_]+)\(", rs))
+    assert rust_fns == set(declared()), set(declared()) ^ rust_fns
