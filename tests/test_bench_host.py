@@ -115,3 +115,20 @@ def test_parity_fail_reads_every_parity_object(bench):
 def test_gpus_flag_must_match_world_size(bench, monkeypatch):
     monkeypatch.setenv("WORLD_SIZE", "1")
     assert bench.main(["--gpus", "2", "--impl", "reference"]) == 2
+
+
+def test_gpus_flag_starts_that_many_ranks():
+    """`bench.py --gpus 2` run without torchrun starts two ranks itself (torch.distributed.run on
+    127.0.0.1); the reference arm (the oracle stand-in, no GPU needed) then prints one line from
+    rank 0 with n_gpus = 2."""
+    import json
+    import subprocess
+    import sys
+    pytest.importorskip("torch")
+    env = {k: v for k, v in os.environ.items() if k not in ("RANK", "WORLD_SIZE", "LOCAL_RANK")}
+    out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--gpus", "2", "--impl", "reference",
+                          "--steps", "1", "--warmup", "3", "--ref-fraction", "1024"],
+                         cwd=ROOT, capture_output=True, text=True, timeout=600, env=env)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [json.loads(x) for x in out.stdout.splitlines() if x.startswith("{")]
+    assert len(lines) == 1 and lines[0]["n_gpus"] == 2 and lines[0]["impl"] == "reference"
