@@ -549,8 +549,9 @@ struct TravT {
         const uint32_t k = ((cnt >> kWideShift) & 3u) + 1u;
         const float4* N = b.nodes + 2ull * first;
         if constexpr (COUNT) cn.hid_boxes += k;
-        // the live children by entry distance (dead ones at +inf), sorted by a 5-exchange network;
-        // the nearest is entered, the others pushed farthest first so they pop in distance order
+        // the live children by entry distance (dead ones at +inf); three exchanges bring the nearest
+        // first, which is entered, and the others are pushed (measured: the full 5-exchange sort
+        // cost 0.6 % more on the icosphere frame than the order it buys)
         float t[4] = {INFINITY, INFINITY, INFINITY, INFINITY};
         uint2 e[4] = {make_uint2(0u, 0u), make_uint2(0u, 0u), make_uint2(0u, 0u), make_uint2(0u, 0u)};
         // children two at a time, both loads issued together (a child record past the last one is
@@ -582,9 +583,7 @@ struct TravT {
         };
         cx(0, 1);
         cx(2, 3);
-        cx(0, 2);
-        cx(1, 3);
-        cx(1, 2);
+        cx(0, 2);  // the nearest is now first; the pushed rest stays partly ordered (any order is exact)
         if (t[0] < INFINITY) {
 #pragma unroll
             for (int i = 3; i >= 1; --i)
