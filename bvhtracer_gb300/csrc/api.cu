@@ -155,6 +155,7 @@ void free_mesh(DeviceMesh& m) {
     cudaFree(m.faces);
     cudaFree(m.verts);
     cudaFree(m.vnormals);
+    cudaFree(m.sched);
     m = DeviceMesh();
 }
 

@@ -80,6 +80,17 @@ struct DeviceWorld {
     uint32_t ngens = 0;
 };
 
+// Layout of a mesh's forward-pass schedule (u32 words, for up to `cap` rays): per parity p (the
+// pass epoch's low bit) a flag per ray (the epoch of the pass that serves the ray from its long
+// list, else 0) and a long list of ray ids; then the counters.
+struct ForwardSchedule {
+    static constexpr uint32_t kQueue = 0, kHead = 1, kCount = 2 /* + parity */, kEpoch = 4, kCounters = 8;
+    static __host__ __device__ size_t flags(uint32_t cap, uint32_t p) { return (size_t)p * cap; }
+    static __host__ __device__ size_t list(uint32_t cap, uint32_t p) { return (size_t)(2u + p) * cap; }
+    static __host__ __device__ size_t counters(uint32_t cap) { return 4ull * cap; }
+    static size_t words(uint32_t cap) { return 4ull * cap + kCounters; }
+};
+
 struct DeviceMesh {
     uint32_t blas = 0;           // BLAS whose triangle i is face i
     uint32_t* faces = nullptr;   // 3 vertex ids per face, in the BLAS's triangle order
@@ -87,6 +98,8 @@ struct DeviceMesh {
     float* vnormals = nullptr;   // 3 floats per vertex (fixed shading normals)
     uint32_t nfaces = 0;
     uint32_t nverts = 0;
+    uint32_t* sched = nullptr;   // forward-pass schedule (ForwardSchedule), for up to sched_cap rays
+    uint32_t sched_cap = 0;
 };
 
 struct ProfileRec {

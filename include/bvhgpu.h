@@ -395,7 +395,11 @@ int bvhgpu_mesh_update_async(bvhgpu_ctx* ctx, uint32_t mesh_id, bvhgpu_stream s)
 /* Forward: closest hit per ray, hit records {t, u, v, prim} written to d_hits (the checkpoint the
  * adjoint reuses), image[i] = max(0, n_hat . l_hat) with n the barycentric vertex normal and l the
  * direction from the hit point to the point light `light` (0 for a miss).  One persistent launch
- * under the BVHGPU_K_TRACE_BLAS launch config (shape, stack, leaf policy, refill). */
+ * under the BVHGPU_K_TRACE_BLAS launch config (shape, stack, leaf policy, refill).  Each pass
+ * records which rays took long to trace, and the mesh's next pass starts those first, spread over
+ * the launch (results never depend on it); the record takes 16 bytes per ray, allocated by the first
+ * pass at a larger ray count (outside stream capture; a captured pass that finds it too small runs
+ * without it).  Passes of one mesh must not run concurrently. */
 int bvhgpu_lambert_forward_async(bvhgpu_ctx* ctx, uint32_t mesh_id, const bvhgpu_ray* d_rays, uint32_t n,
                                  const float light[3], float* d_image, bvhgpu_hit* d_hits, bvhgpu_stream s);
 /* Mean squared error between image and target (n floats each, device), computed on the device in

@@ -196,3 +196,53 @@ def test_repeated_forward_passes_are_identical():
             out.append((d_img.download(np.zeros(n, np.float32)).tobytes(),
                         d_hits.download(np.zeros(n, bt.HIT)).tobytes()))
     assert out[0] == out[1] == out[2]
+
+
+def test_forward_schedule_across_ray_counts_and_orders():
+    """The forward pass serves the rays its previous pass found long first (a per-mesh schedule that
+    the previous pass writes).  Passes over a prefix of the rays, over the rays reversed, over a
+    larger batch (the schedule grows) and replays of a captured pass must each trace every ray exactly
+    once: hit records and images equal, ray by ray, those of the first (unscheduled) pass."""
+    verts, faces, vn, _, rays, light = scenes.lambert_scene(seed=6, level=7, width=256, height=256)
+    n = len(rays)
+    with bt.Context(0) as ctx:
+        m = bt.DiffMesh(ctx, verts, faces, vn)
+
+        def forward(rs):
+            k = len(rs)
+            d_rays = ctx.to_device(np.ascontiguousarray(rs))
+            d_img = ctx.device_buffer(4 * k)
+            d_hits = ctx.device_buffer(bt.HIT.itemsize * k)
+            d_img.zero()
+            d_hits.zero()
+            m.forward_async(d_rays, k, light, d_img, d_hits)
+            ctx.sync()
+            return d_img.download(np.zeros(k, np.float32)), d_hits.download(np.zeros(k, bt.HIT))
+
+        img0, hits0 = forward(rays)
+        assert (hits0["prim"] != bt.MISS).mean() > 0.2
+        cases = [(rays, slice(None)), (rays, slice(None)), (rays[: n // 3], slice(0, n // 3)),
+                 (rays[::-1], slice(None, None, -1)), (rays, slice(None)), (rays, slice(None))]
+        for rs, sel in cases:
+            img, hits = forward(rs)
+            assert img.tobytes() == img0[sel].tobytes() and hits.tobytes() == hits0[sel].tobytes()
+        both = np.concatenate([rays, rays[::-1]])
+        img, hits = forward(both)
+        assert img.tobytes() == np.concatenate([img0, img0[::-1]]).tobytes()
+        assert hits.tobytes() == np.concatenate([hits0, hits0[::-1]]).tobytes()
+
+        # a captured pass replays with the schedule on the device (its epoch advances per replay)
+        d_rays = ctx.to_device(rays)
+        d_img = ctx.device_buffer(4 * n)
+        d_hits = ctx.device_buffer(bt.HIT.itemsize * n)
+        ctx.graph_begin()
+        m.forward_async(d_rays, n, light, d_img, d_hits)
+        gid = ctx.graph_end()
+        for _ in range(3):
+            d_img.zero()
+            d_hits.zero()
+            ctx.graph_launch(gid)
+            ctx.sync()
+            assert d_img.download(np.zeros(n, np.float32)).tobytes() == img0.tobytes()
+            assert d_hits.download(np.zeros(n, bt.HIT)).tobytes() == hits0.tobytes()
+        ctx.graph_free(gid)
