@@ -145,6 +145,10 @@ void free_blas(DeviceBlas& b) {
     cudaFree(b.hx);
     cudaFree(b.cones);
     cudaFree(b.hwork);
+    cudaFree(b.hchunks);
+    cudaFree(b.hchunk0);
+    cudaFree(b.hpart);
+    cudaFree(b.harrivals);
     cudaFree(b.normals);
     cudaFree(b.tex_coords);
     cudaFree(b.texels);
@@ -251,9 +255,12 @@ struct HiddenPlan {
     std::vector<uint2> table;  // per triangle index, rounded up to even (empty: no hidden tree)
     std::vector<uint2> slots;  // per hidden pair
     std::vector<uint4> work;   // per hidden node (box), then per cone
+    std::vector<uint2> chunks;    // {group, first pair}: each group in kRefreshChunk-pair chunks
+    std::vector<uint32_t> chunk0;  // first chunk of each group, then the total
+    uint32_t nbox_chunks = 0;      // chunks of the node groups (they come first)
     uint32_t nhid = 0, nhp = 0, ncones = 0, depth = 0;
 };
-constexpr uint32_t kNoWork = 0xFFFFFFFFu;
+constexpr uint32_t kNoWork = kNoRefresh;
 
 struct SahTri {
     float c[3], lo[3], hi[3];
@@ -408,6 +415,12 @@ void plan_hidden(const bvhgpu_node* nodes, uint32_t nodes_used, const std::vecto
         cones.push_back(make_uint4(pa, P0 + hp.nhp, kNoWork, root_cone));
     }
     hp.work.insert(hp.work.end(), cones.begin(), cones.end());
+    for (uint32_t j = 0; j < hp.work.size(); ++j) {
+        hp.chunk0.push_back((uint32_t)hp.chunks.size());
+        for (uint32_t p = hp.work[j].x; p < hp.work[j].y; p += kRefreshChunk) hp.chunks.push_back(make_uint2(j, p));
+        if (hp.work[j].z != kNoWork) hp.nbox_chunks = (uint32_t)hp.chunks.size();  // node groups come first
+    }
+    hp.chunk0.push_back((uint32_t)hp.chunks.size());
 }
 
 }  // namespace
@@ -622,6 +635,9 @@ int bvhgpu_blas_upload(bvhgpu_ctx* ctx, const bvhgpu_node* nodes, uint32_t nodes
     b.nhp = hp.nhp;
     b.ncones = hp.ncones;
     b.nwork = (uint32_t)hp.work.size();
+    b.nchunks = (uint32_t)hp.chunks.size();
+    b.nbox_chunks = hp.nbox_chunks;
+    const size_t part_bytes = std::max(sizeof(float2), sizeof(RefreshAgg)) * std::max<size_t>(1, hp.chunks.size());
     b.ref_depth = depth;
     b.depth = depth + 3 * hp.depth;  // a 4-wide hidden level can leave 3 children pending
     const uint64_t nodes_all = (uint64_t)nodes_used + hp.nhid + 1;  // + a spare record (4-wide reads)
@@ -645,7 +661,11 @@ int bvhgpu_blas_upload(bvhgpu_ctx* ctx, const bvhgpu_node* nodes, uint32_t nodes
         (e = cudaMalloc(&d_tris9, 36ull * ntris)) != cudaSuccess ||
         (hx_bytes && (e = cudaMalloc(&b.hx, hx_bytes)) != cudaSuccess) ||
         (b.ncones && (e = cudaMalloc(&b.cones, 32ull * b.ncones)) != cudaSuccess) ||
-        (b.nwork && (e = cudaMalloc(&b.hwork, 16ull * b.nwork)) != cudaSuccess)) {
+        (b.nwork && (e = cudaMalloc(&b.hwork, 16ull * b.nwork)) != cudaSuccess) ||
+        (b.nwork && (e = cudaMalloc(&b.hchunks, 8ull * b.nchunks)) != cudaSuccess) ||
+        (b.nwork && (e = cudaMalloc(&b.hchunk0, 4ull * (b.nwork + 1))) != cudaSuccess) ||
+        (b.nwork && (e = cudaMalloc(&b.hpart, part_bytes)) != cudaSuccess) ||
+        (b.nwork && (e = cudaMalloc(&b.harrivals, 4ull * b.nwork)) != cudaSuccess)) {
         cleanup();
         return fail(ctx, BVHGPU_ERR_OUT_OF_MEMORY, "blas_upload: %s", cudaGetErrorString(e));
     }
@@ -664,6 +684,9 @@ int bvhgpu_blas_upload(bvhgpu_ctx* ctx, const bvhgpu_node* nodes, uint32_t nodes
         (hx_bytes && hp.nhp &&
          (e = cudaMemcpy(b.hx + hp.table.size(), hp.slots.data(), 8ull * hp.nhp, cudaMemcpyHostToDevice)) != cudaSuccess) ||
         (b.nwork && (e = cudaMemcpy(b.hwork, hp.work.data(), 16ull * b.nwork, cudaMemcpyHostToDevice)) != cudaSuccess) ||
+        (b.nwork && (e = cudaMemcpy(b.hchunks, hp.chunks.data(), 8ull * b.nchunks, cudaMemcpyHostToDevice)) != cudaSuccess) ||
+        (b.nwork && (e = cudaMemcpy(b.hchunk0, hp.chunk0.data(), 4ull * (b.nwork + 1), cudaMemcpyHostToDevice)) != cudaSuccess) ||
+        (b.nwork && (e = cudaMemset(b.harrivals, 0, 4ull * b.nwork)) != cudaSuccess) ||
         (e = launch_write_tris(ctx, b, static_cast<const float*>(d_tris9), ctx->stream)) != cudaSuccess ||
         (e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess) {
         cleanup();

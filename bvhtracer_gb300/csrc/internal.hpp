@@ -16,6 +16,16 @@ namespace bvhgpu {
 
 extern std::atomic<uint64_t> g_launches;
 
+// Hidden-tree refresh: pairs per chunk (one warp), and the "none" marker of a group's node / cone.
+constexpr uint32_t kRefreshChunk = 256;
+constexpr uint32_t kNoRefresh = 0xFFFFFFFFu;
+// A chunk's partial result of the refresh's first pass: raw bounds of v0, v0 + e1, v0 + e2, the
+// largest |e1_i|, |e2_i|, the sum of the folded unit normals (cone groups), all inputs finite.
+struct RefreshAgg {
+    float lo[3], hi[3], e1m, e2m, sx, sy, sz;
+    bool finite;
+};
+
 struct DeviceBlas {
     float4* nodes = nullptr;     // 2 float4 per node (nodes_used nodes)
     float4* tris = nullptr;      // 3 float4 per triangle (v0, e1, e2): traversal layout
@@ -29,10 +39,15 @@ struct DeviceBlas {
     uint2* hx = nullptr;         // hidden-tree table and pair slots (GBlas::hx), or null
     float4* cones = nullptr;     // hidden-tree cone records (GBlas::cones)
     uint32_t ncones = 0;
-    uint4* hwork = nullptr;      // refresh work: {first pair, end pair, node index or ~0, cone index or ~0}
+    uint4* hwork = nullptr;      // refresh groups: {first pair, end pair, node index or ~0, cone index or ~0}
+    uint2* hchunks = nullptr;    // refresh chunks: {group, first pair}, node groups' chunks first
+    uint32_t* hchunk0 = nullptr; // first chunk of each group (nwork + 1 entries)
+    void* hpart = nullptr;       // per-chunk partial results of the refresh
+    uint32_t* harrivals = nullptr;  // per-group arrival counters of the refresh (kept zeroed)
     uint32_t nhid = 0;           // hidden nodes (after the nodes_used reference nodes)
     uint32_t nhp = 0;            // hidden pairs (after the (ntris + 1) / 2 pairs in triangle order)
     uint32_t nwork = 0;          // hidden nodes + cones
+    uint32_t nchunks = 0, nbox_chunks = 0;
     uint32_t ref_depth = 0;      // depth of the reference tree (depth adds the hidden trees')
     uint32_t nodes_used = 0;
     uint32_t ntris = 0;

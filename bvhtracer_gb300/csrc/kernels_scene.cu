@@ -72,55 +72,66 @@ __global__ void k_hidden_pairs(const float4* __restrict__ tris, const uint2* __r
     P[18] = P[19] = 0.0f;
 }
 
-__global__ void k_hidden_boxes(const uint4* __restrict__ work, uint32_t nwork, const float* __restrict__ pairs,
-                               const uint2* __restrict__ slots, uint32_t p0, float4* __restrict__ nodes,
-                               float4* __restrict__ cones) {
-    const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const unsigned lane = threadIdx.x & 31u;
-    if (w >= nwork) return;  // whole warps leave together
-    const uint4 job = work[w];
-    float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
-    float e1m = 0.0f, e2m = 0.0f;
-    bool finite = true;
-    for (uint32_t p = job.x + lane; p < job.y; p += 32u) {
-        const uint2 idx = slots[p - p0];
-        const float* P = pairs + 20ull * p;
-        for (int h = 0; h < 2; ++h) {
-            if ((h ? idx.y : idx.x) == kMiss) continue;
-            for (int i = 0; i < 3; ++i) {
-                const float v = P[2 * i + h], a = P[2 * (3 + i) + h], b = P[2 * (6 + i) + h];
-                const float p1 = fadd(v, a), p2 = fadd(v, b);
-                finite = finite && isfinite(v) && isfinite(a) && isfinite(b) && isfinite(p1) && isfinite(p2);
-                lo[i] = fminf(lo[i], fminf(v, fminf(p1, p2)));
-                hi[i] = fmaxf(hi[i], fmaxf(v, fmaxf(p1, p2)));
-                e1m = fmaxf(e1m, fabsf(a));
-                e2m = fmaxf(e2m, fabsf(b));
-            }
-        }
+// The refresh runs over chunks of at most kRefreshChunk pairs, one warp each, so that the large
+// groups near the hidden roots (up to ~10,000 pairs) are spread over many warps instead of
+// holding one warp each for the whole launch.  A group's chunks are consecutive; the last chunk of
+// a group to finish (arrival counter, reset by it) combines the group's partial results in chunk
+// order, so every result is deterministic.  Pass 1 (k_hidden_refresh_boxes): the raw box
+// aggregates of every group and, for cone groups, the sum of the sign-folded unit normals; a
+// node group writes its widened box, a cone group its axis and the bounds Q, B.  Pass 2
+// (k_hidden_refresh_cones, cone groups only): the cone's angle and the smallest normal, from the
+// axis.  Min / max are exact in any order: boxes and cone angles do not depend on the chunking;
+// the axis (a float sum) does, and any axis gives a valid cone.
+__device__ __forceinline__ void agg_init(RefreshAgg& g) {
+    for (int i = 0; i < 3; ++i) {
+        g.lo[i] = FLT_MAX;
+        g.hi[i] = -FLT_MAX;
     }
-    for (int off = 16; off > 0; off >>= 1) {
-        for (int i = 0; i < 3; ++i) {
-            lo[i] = fminf(lo[i], __shfl_xor_sync(0xFFFFFFFFu, lo[i], off));
-            hi[i] = fmaxf(hi[i], __shfl_xor_sync(0xFFFFFFFFu, hi[i], off));
-        }
-        e1m = fmaxf(e1m, __shfl_xor_sync(0xFFFFFFFFu, e1m, off));
-        e2m = fmaxf(e2m, __shfl_xor_sync(0xFFFFFFFFu, e2m, off));
+    g.e1m = g.e2m = 0.0f;
+    g.sx = g.sy = g.sz = 0.0f;
+    g.finite = true;
+}
+
+// Folds b into a: min / max of the bounds, sum of the normals.
+__device__ __forceinline__ void agg_fold(RefreshAgg& a, const RefreshAgg& b) {
+    for (int i = 0; i < 3; ++i) {
+        a.lo[i] = fminf(a.lo[i], b.lo[i]);
+        a.hi[i] = fmaxf(a.hi[i], b.hi[i]);
     }
-    finite = __all_sync(0xFFFFFFFFu, finite);
-    const GroupSeal g = group_seal(lo, hi, e1m, e2m, finite);
-    if (job.z != 0xFFFFFFFFu) {  // a node's box
-        if (lane == 0) {
-            float4* N = nodes + 2ull * job.z;
-            N[0] = make_float4(g.lo[0], g.lo[1], g.lo[2], N[0].w);
-            N[1] = make_float4(g.hi[0], g.hi[1], g.hi[2], N[1].w);
-        }
-        return;
+    a.e1m = fmaxf(a.e1m, b.e1m);
+    a.e2m = fmaxf(a.e2m, b.e2m);
+    a.sx += b.sx;
+    a.sy += b.sy;
+    a.sz += b.sz;
+    a.finite = a.finite && b.finite;
+}
+
+__device__ __forceinline__ RefreshAgg agg_shfl_xor(const RefreshAgg& g, int off) {
+    RefreshAgg o;
+    for (int i = 0; i < 3; ++i) {
+        o.lo[i] = __shfl_xor_sync(0xFFFFFFFFu, g.lo[i], off);
+        o.hi[i] = __shfl_xor_sync(0xFFFFFFFFu, g.hi[i], off);
     }
-    // a cone record: Q, B and the cone of the normal lines (any axis is valid; the sum of unit
-    // normals, each turned towards the first triangle's, makes it narrow)
+    o.e1m = __shfl_xor_sync(0xFFFFFFFFu, g.e1m, off);
+    o.e2m = __shfl_xor_sync(0xFFFFFFFFu, g.e2m, off);
+    o.sx = __shfl_xor_sync(0xFFFFFFFFu, g.sx, off);
+    o.sy = __shfl_xor_sync(0xFFFFFFFFu, g.sy, off);
+    o.sz = __shfl_xor_sync(0xFFFFFFFFu, g.sz, off);
+    o.finite = __shfl_xor_sync(0xFFFFFFFFu, g.finite ? 1 : 0, off) != 0;
+    return o;
+}
+
+// The warp's fold of every lane's aggregate (the same fixed tree on every lane).
+__device__ __forceinline__ void agg_warp(RefreshAgg& g) {
+    for (int off = 16; off > 0; off >>= 1) agg_fold(g, agg_shfl_xor(g, off));
+}
+
+// The first valid normal of a cone group in pair order (the sign reference of its folded normals).
+__device__ __forceinline__ float3 group_reference_normal(const float* __restrict__ pairs, const uint2* __restrict__ slots,
+                                                         uint32_t p0, uint32_t first, uint32_t end) {
     float rx = 0.0f, ry = 0.0f, rz = 0.0f;
-    if (lane == 0) {
-        for (uint32_t p = job.x; p < job.y; ++p) {
+    if ((threadIdx.x & 31u) == 0u) {
+        for (uint32_t p = first; p < end; ++p) {
             const uint2 idx = slots[p - p0];
             const float* P = pairs + 20ull * p;
             bool found = false;
@@ -135,39 +146,128 @@ __global__ void k_hidden_boxes(const uint4* __restrict__ work, uint32_t nwork, c
             if (found) break;
         }
     }
-    rx = __shfl_sync(0xFFFFFFFFu, rx, 0);
-    ry = __shfl_sync(0xFFFFFFFFu, ry, 0);
-    rz = __shfl_sync(0xFFFFFFFFu, rz, 0);
-    float sx = 0.0f, sy = 0.0f, sz = 0.0f;
-    for (uint32_t p = job.x + lane; p < job.y; p += 32u) {
+    return make_float3(__shfl_sync(0xFFFFFFFFu, rx, 0), __shfl_sync(0xFFFFFFFFu, ry, 0), __shfl_sync(0xFFFFFFFFu, rz, 0));
+}
+
+// Pass 1, one warp per chunk {group, first pair}.
+__global__ void k_hidden_refresh_boxes(const uint4* __restrict__ work, const uint2* __restrict__ chunks, uint32_t nchunks,
+                                       const uint32_t* __restrict__ chunk0, RefreshAgg* __restrict__ part,
+                                       uint32_t* __restrict__ arrivals, const float* __restrict__ pairs,
+                                       const uint2* __restrict__ slots, uint32_t p0, float4* __restrict__ nodes,
+                                       float4* __restrict__ cones) {
+    const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const unsigned lane = threadIdx.x & 31u;
+    if (w >= nchunks) return;  // whole warps leave together
+    const uint2 ch = chunks[w];
+    const uint4 job = work[ch.x];
+    const uint32_t end = min(ch.y + kRefreshChunk, job.y);
+    const bool cone = job.w != kNoRefresh;
+    RefreshAgg g;
+    agg_init(g);
+    for (uint32_t p = ch.y + lane; p < end; p += 32u) {
         const uint2 idx = slots[p - p0];
         const float* P = pairs + 20ull * p;
         for (int h = 0; h < 2; ++h) {
             if ((h ? idx.y : idx.x) == kMiss) continue;
-            const float a[3] = {P[6 + h], P[8 + h], P[10 + h]}, b[3] = {P[12 + h], P[14 + h], P[16 + h]};
-            const float nx = a[1] * b[2] - a[2] * b[1], ny = a[2] * b[0] - a[0] * b[2], nz = a[0] * b[1] - a[1] * b[0];
-            const float len = sqrtf(nx * nx + ny * ny + nz * nz);
-            if (!(len > 0.0f) || !isfinite(len)) continue;
-            const float sg = (nx * rx + ny * ry + nz * rz) < 0.0f ? -1.0f : 1.0f;
-            sx += sg * nx / len;
-            sy += sg * ny / len;
-            sz += sg * nz / len;
+            for (int i = 0; i < 3; ++i) {
+                const float v = P[2 * i + h], a = P[2 * (3 + i) + h], b = P[2 * (6 + i) + h];
+                const float p1 = fadd(v, a), p2 = fadd(v, b);
+                g.finite = g.finite && isfinite(v) && isfinite(a) && isfinite(b) && isfinite(p1) && isfinite(p2);
+                g.lo[i] = fminf(g.lo[i], fminf(v, fminf(p1, p2)));
+                g.hi[i] = fmaxf(g.hi[i], fmaxf(v, fmaxf(p1, p2)));
+                g.e1m = fmaxf(g.e1m, fabsf(a));
+                g.e2m = fmaxf(g.e2m, fabsf(b));
+            }
         }
     }
-    for (int off = 16; off > 0; off >>= 1) {
-        sx += __shfl_xor_sync(0xFFFFFFFFu, sx, off);
-        sy += __shfl_xor_sync(0xFFFFFFFFu, sy, off);
-        sz += __shfl_xor_sync(0xFFFFFFFFu, sz, off);
+    if (cone) {
+        // the sum of the unit normals, each turned towards the group's first one (any axis is
+        // valid; this one makes the cone narrow)
+        const float3 r = group_reference_normal(pairs, slots, p0, job.x, job.y);
+        for (uint32_t p = ch.y + lane; p < end; p += 32u) {
+            const uint2 idx = slots[p - p0];
+            const float* P = pairs + 20ull * p;
+            for (int h = 0; h < 2; ++h) {
+                if ((h ? idx.y : idx.x) == kMiss) continue;
+                const float a[3] = {P[6 + h], P[8 + h], P[10 + h]}, b[3] = {P[12 + h], P[14 + h], P[16 + h]};
+                const float nx = a[1] * b[2] - a[2] * b[1], ny = a[2] * b[0] - a[0] * b[2], nz = a[0] * b[1] - a[1] * b[0];
+                const float len = sqrtf(nx * nx + ny * ny + nz * nz);
+                if (!(len > 0.0f) || !isfinite(len)) continue;
+                const float sg = (nx * r.x + ny * r.y + nz * r.z) < 0.0f ? -1.0f : 1.0f;
+                g.sx += sg * nx / len;
+                g.sy += sg * ny / len;
+                g.sz += sg * nz / len;
+            }
+        }
     }
+    agg_warp(g);
+    const uint32_t c0 = chunk0[ch.x], nc = chunk0[ch.x + 1] - c0;
+    if (nc > 1) {
+        // the group's last chunk to arrive combines the partials in chunk order
+        bool last = false;
+        if (lane == 0u) {
+            part[w] = g;
+            __threadfence();
+            last = atomicAdd(arrivals + ch.x, 1u) == nc - 1u;
+        }
+        if (!__shfl_sync(0xFFFFFFFFu, last ? 1 : 0, 0)) return;
+        __threadfence();
+        agg_init(g);
+        for (uint32_t k = lane; k < nc; k += 32u) {
+            const RefreshAgg* q = part + c0 + k;
+            RefreshAgg o;
+            for (int i = 0; i < 3; ++i) {
+                o.lo[i] = __ldcg(&q->lo[i]);
+                o.hi[i] = __ldcg(&q->hi[i]);
+            }
+            o.e1m = __ldcg(&q->e1m);
+            o.e2m = __ldcg(&q->e2m);
+            o.sx = __ldcg(&q->sx);
+            o.sy = __ldcg(&q->sy);
+            o.sz = __ldcg(&q->sz);
+            o.finite = *reinterpret_cast<volatile const bool*>(&q->finite);
+            agg_fold(g, o);
+        }
+        agg_warp(g);
+        if (lane == 0u) arrivals[ch.x] = 0u;  // ready for the next refresh
+    }
+    if (lane != 0u) return;
+    const GroupSeal s = group_seal(g.lo, g.hi, g.e1m, g.e2m, g.finite);
+    if (!cone) {  // a node's box
+        float4* N = nodes + 2ull * job.z;
+        N[0] = make_float4(s.lo[0], s.lo[1], s.lo[2], N[0].w);
+        N[1] = make_float4(s.hi[0], s.hi[1], s.hi[2], N[1].w);
+        return;
+    }
+    // the axis and the bounds Q, B, for pass 2
+    float4* C = cones + 2ull * job.w;
+    C[0] = make_float4(g.sx, g.sy, g.sz, 0.0f);
+    C[1] = make_float4(0.0f, 0.0f, s.q, s.b);
+}
+
+// Pass 2, one warp per chunk of a cone group: the cone of the normal lines around the axis.
+__global__ void k_hidden_refresh_cones(const uint4* __restrict__ work, const uint2* __restrict__ chunks,
+                                       uint32_t first_chunk, uint32_t nchunks, const uint32_t* __restrict__ chunk0,
+                                       float2* __restrict__ part, uint32_t* __restrict__ arrivals,
+                                       const float* __restrict__ pairs, const uint2* __restrict__ slots, uint32_t p0,
+                                       float4* __restrict__ cones) {
+    const uint32_t w = first_chunk + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const unsigned lane = threadIdx.x & 31u;
+    if (w >= nchunks) return;  // whole warps leave together
+    const uint2 ch = chunks[w];
+    const uint4 job = work[ch.x];
+    const uint32_t end = min(ch.y + kRefreshChunk, job.y);
+    float4* C = cones + 2ull * job.w;
+    const float4 ax = __ldcg(C);
     float cmin = 2.0f, nmin = FLT_MAX;
-    for (uint32_t p = job.x + lane; p < job.y; p += 32u) {
+    for (uint32_t p = ch.y + lane; p < end; p += 32u) {
         const uint2 idx = slots[p - p0];
         const float* P = pairs + 20ull * p;
         for (int h = 0; h < 2; ++h) {
             if ((h ? idx.y : idx.x) == kMiss) continue;
             const float a[3] = {P[6 + h], P[8 + h], P[10 + h]}, b[3] = {P[12 + h], P[14 + h], P[16 + h]};
             float cl, nl;
-            cone_terms(a, b, sx, sy, sz, cl, nl);
+            cone_terms(a, b, ax.x, ax.y, ax.z, cl, nl);
             cmin = cl < cmin ? cl : (cl == cl ? cmin : -1.0f);  // NaN: no cone
             nmin = nl < nmin ? nl : (nl == nl ? nmin : 0.0f);
         }
@@ -176,12 +276,35 @@ __global__ void k_hidden_boxes(const uint4* __restrict__ work, uint32_t nwork, c
         cmin = fminf(cmin, __shfl_xor_sync(0xFFFFFFFFu, cmin, off));
         nmin = fminf(nmin, __shfl_xor_sync(0xFFFFFFFFu, nmin, off));
     }
-    if (lane != 0) return;
-    const bool cone_ok = isfinite(sx) && isfinite(sy) && isfinite(sz) && cmin > 0.0f && cmin <= 1.0f &&
+    const uint32_t c0 = chunk0[ch.x], nc = chunk0[ch.x + 1] - c0;
+    if (nc > 1) {
+        bool last = false;
+        if (lane == 0u) {
+            part[w] = make_float2(cmin, nmin);
+            __threadfence();
+            last = atomicAdd(arrivals + ch.x, 1u) == nc - 1u;
+        }
+        if (!__shfl_sync(0xFFFFFFFFu, last ? 1 : 0, 0)) return;
+        __threadfence();
+        cmin = 2.0f;
+        nmin = FLT_MAX;
+        for (uint32_t k = lane; k < nc; k += 32u) {
+            const float2 q = __ldcg(part + c0 + k);
+            cmin = fminf(cmin, q.x);
+            nmin = fminf(nmin, q.y);
+        }
+        for (int off = 16; off > 0; off >>= 1) {
+            cmin = fminf(cmin, __shfl_xor_sync(0xFFFFFFFFu, cmin, off));
+            nmin = fminf(nmin, __shfl_xor_sync(0xFFFFFFFFu, nmin, off));
+        }
+        if (lane == 0u) arrivals[ch.x] = 0u;
+    }
+    if (lane != 0u) return;
+    const float4 qb = __ldcg(C + 1);
+    const bool cone_ok = isfinite(ax.x) && isfinite(ax.y) && isfinite(ax.z) && cmin > 0.0f && cmin <= 1.0f &&
                          nmin > 0.0f && nmin < FLT_MAX;
-    float4* C = cones + 2ull * job.w;
-    C[0] = make_float4(cone_ok ? sx : 0.0f, cone_ok ? sy : 0.0f, cone_ok ? sz : 0.0f, cone_ok ? cmin : -1.0f);
-    C[1] = make_float4(cone_ok ? cone_sin(cmin) : 1.0f, cone_ok ? nmin : 0.0f, g.q, g.b);
+    C[0] = make_float4(cone_ok ? ax.x : 0.0f, cone_ok ? ax.y : 0.0f, cone_ok ? ax.z : 0.0f, cone_ok ? cmin : -1.0f);
+    C[1] = make_float4(cone_ok ? cone_sin(cmin) : 1.0f, cone_ok ? nmin : 0.0f, qb.z, qb.w);
 }
 
 // ---- refit, parallel over triangles --------------------------------------------------------
@@ -998,8 +1121,16 @@ cudaError_t launch_hidden_refresh(bvhgpu_ctx* ctx, DeviceBlas& b, cudaStream_t s
     const uint2* slots = b.hx + hidden_table_u2(b.ntris);
     float* pairs = reinterpret_cast<float*>(b.pairs);
     k_hidden_pairs<<<grid_for(b.nhp, 256), 256, 0, s>>>(b.tris, slots, b.nhp, pairs + 20ull * p0);
-    k_hidden_boxes<<<grid_for(32u * b.nwork, 128), 128, 0, s>>>(b.hwork, b.nwork, pairs, slots, p0, b.nodes, b.cones);
+    k_hidden_refresh_boxes<<<grid_for(32u * b.nchunks, 128), 128, 0, s>>>(
+        b.hwork, b.hchunks, b.nchunks, b.hchunk0, static_cast<RefreshAgg*>(b.hpart), b.harrivals, pairs, slots, p0,
+        b.nodes, b.cones);
     g_launches += 2;
+    if (b.nchunks > b.nbox_chunks) {
+        k_hidden_refresh_cones<<<grid_for(32u * (b.nchunks - b.nbox_chunks), 128), 128, 0, s>>>(
+            b.hwork, b.hchunks, b.nbox_chunks, b.nchunks, b.hchunk0, static_cast<float2*>(b.hpart), b.harrivals,
+            pairs, slots, p0, b.cones);
+        g_launches++;
+    }
     return cudaGetLastError();
 }
 
