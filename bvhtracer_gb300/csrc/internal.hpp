@@ -96,10 +96,12 @@ struct DeviceWorld {
 };
 
 // Layout of a mesh's forward-pass schedule (u32 words, for up to `cap` rays): per parity p (the
-// pass epoch's low bit) a flag per ray (the epoch of the pass that serves the ray from its long
-// list, else 0) and a long list of ray ids; then the counters.
+// pass number's low bit) a flag per ray (1: the next pass serves the ray from its long list) and a
+// long list of ray ids; then the counters: the pixel queue, the long list's head, the list sizes
+// per parity, the pass number, and the ray counts of the last two passes.
 struct ForwardSchedule {
-    static constexpr uint32_t kQueue = 0, kHead = 1, kCount = 2 /* + parity */, kEpoch = 4, kCounters = 8;
+    static constexpr uint32_t kQueue = 0, kHead = 1, kCount = 2 /* + parity */, kPass = 4, kRays = 5, kPrevRays = 6,
+                              kCounters = 8;
     static __host__ __device__ size_t flags(uint32_t cap, uint32_t p) { return (size_t)p * cap; }
     static __host__ __device__ size_t list(uint32_t cap, uint32_t p) { return (size_t)(2u + p) * cap; }
     static __host__ __device__ size_t counters(uint32_t cap) { return 4ull * cap; }

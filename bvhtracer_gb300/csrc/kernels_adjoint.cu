@@ -123,8 +123,8 @@ __global__ void k_mesh_tris(const float* __restrict__ verts, const uint32_t* __r
 // layout) each pass records its long rays, and the next pass serves them first from that list,
 // an even share of them per warp at a time (any number once the pixel queue is empty), while
 // the pixel queue skips them.  Every ray is traced exactly once either way:
-// flag_cur[i] == epoch exactly when i is in the list (both written by the previous pass), and each
-// hit depends on its ray only.
+// for i below the previous pass's ray count, flag_cur[i] is set exactly when i is in the list
+// (the previous pass wrote both, for each of its rays), and each hit depends on its ray only.
 template <int BLOCK, int MINB, class STK>
 __global__ void __launch_bounds__(BLOCK, MINB) k_lambert_forward(GBlas b, const float4* __restrict__ rays, uint32_t n,
                                                                  const uint32_t* __restrict__ faces,
@@ -142,9 +142,9 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_lambert_forward(GBlas b, const 
     tr.stk.bind(stack_smem);
     StepResult st = kStepFinished;
     bool queue_open = true;
-    // the schedule of this pass (epoch e): flags and list of the previous pass (parity e & 1), and
-    // those this pass writes for the next one
-    uint32_t epoch = 0, lcount = 0;
+    // the schedule of this pass (pass number k): the previous pass's flags and list (parity k & 1),
+    // its ray count, and the flags and list this pass writes for the next one
+    uint32_t parity = 0, lcount = 0, n_prev = 0;
     const uint32_t* flag_cur = nullptr;
     const uint32_t* list_cur = nullptr;
     uint32_t* flag_nxt = nullptr;
@@ -153,13 +153,13 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_lambert_forward(GBlas b, const 
     if (sched != nullptr) {
         ctr = sched + ForwardSchedule::counters(cap);
         queue = ctr + ForwardSchedule::kQueue;
-        epoch = *reinterpret_cast<volatile uint32_t*>(ctr + ForwardSchedule::kEpoch);
-        const uint32_t cur = epoch & 1u;
-        flag_cur = sched + ForwardSchedule::flags(cap, cur);
-        list_cur = sched + ForwardSchedule::list(cap, cur);
-        flag_nxt = sched + ForwardSchedule::flags(cap, cur ^ 1u);
-        list_nxt = sched + ForwardSchedule::list(cap, cur ^ 1u);
-        lcount = *reinterpret_cast<volatile uint32_t*>(ctr + ForwardSchedule::kCount + cur);
+        parity = *reinterpret_cast<volatile uint32_t*>(ctr + ForwardSchedule::kPass) & 1u;
+        n_prev = *reinterpret_cast<volatile uint32_t*>(ctr + ForwardSchedule::kPrevRays);
+        flag_cur = sched + ForwardSchedule::flags(cap, parity);
+        list_cur = sched + ForwardSchedule::list(cap, parity);
+        flag_nxt = sched + ForwardSchedule::flags(cap, parity ^ 1u);
+        list_nxt = sched + ForwardSchedule::list(cap, parity ^ 1u);
+        lcount = *reinterpret_cast<volatile uint32_t*>(ctr + ForwardSchedule::kCount + parity);
     }
     bool long_open = lcount > 0u;
     bool is_long = false;
@@ -200,7 +200,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_lambert_forward(GBlas b, const 
                     is_long = true;
                 } else if (nreg) {
                     my = base + rank - got;
-                    if (my < n && flag_cur != nullptr && __ldcg(flag_cur + my) == epoch) my = n;  // in the list
+                    if (my < n_prev && __ldcg(flag_cur + my) != 0u) my = n;  // in the list
                     is_long = false;
                 }
                 if (my < n) {
@@ -230,8 +230,8 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_lambert_forward(GBlas b, const 
                 image[idx] = I;
                 if (sched != nullptr) {
                     const bool lng = tr.steps > kLongSteps;
-                    __stcg(flag_nxt + idx, lng ? epoch + 1u : 0u);
-                    if (lng) __stcg(list_nxt + atomicAdd(ctr + ForwardSchedule::kCount + ((epoch & 1u) ^ 1u), 1u), idx);
+                    __stcg(flag_nxt + idx, lng ? 1u : 0u);
+                    if (lng) __stcg(list_nxt + atomicAdd(ctr + ForwardSchedule::kCount + (parity ^ 1u), 1u), idx);
                 }
                 phase = 0;
             }
@@ -245,15 +245,17 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_lambert_forward(GBlas b, const 
     }
 }
 
-// Starts a scheduled forward pass: the next epoch, empty queues, and an empty list for the pass
-// after it.
-__global__ void k_forward_prep(uint32_t* ctr) {
-    uint32_t e = ctr[ForwardSchedule::kEpoch] + 1u;
-    if (e == 0u) e = 1u;  // 0 marks "not long" in the flags
-    ctr[ForwardSchedule::kEpoch] = e;
+// Starts a scheduled forward pass over n rays: the next pass number (its parity alternates, also
+// across the counter's wrap), the previous pass's ray count, empty queues, and an empty list for
+// the pass after it.
+__global__ void k_forward_prep(uint32_t* ctr, uint32_t n) {
+    const uint32_t k = ctr[ForwardSchedule::kPass] + 1u;
+    ctr[ForwardSchedule::kPass] = k;
+    ctr[ForwardSchedule::kPrevRays] = ctr[ForwardSchedule::kRays];
+    ctr[ForwardSchedule::kRays] = n;
     ctr[ForwardSchedule::kQueue] = 0u;
     ctr[ForwardSchedule::kHead] = 0u;
-    ctr[ForwardSchedule::kCount + ((e & 1u) ^ 1u)] = 0u;
+    ctr[ForwardSchedule::kCount + ((k & 1u) ^ 1u)] = 0u;
 }
 
 // Per-block partial sums of (I - T)^2 in double.
@@ -363,7 +365,7 @@ cudaError_t launch_lambert_forward(bvhgpu_ctx* ctx, DeviceMesh& m, const DeviceB
     }
     uint32_t* sched = m.sched_cap >= n ? m.sched : nullptr;
     if (sched != nullptr) {
-        k_forward_prep<<<1, 1, 0, s>>>(sched + ForwardSchedule::counters(m.sched_cap));
+        k_forward_prep<<<1, 1, 0, s>>>(sched + ForwardSchedule::counters(m.sched_cap), n);
         g_launches++;
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     } else if ((e = cudaMemsetAsync(queue, 0, sizeof(uint32_t), s)) != cudaSuccess) {
