@@ -109,6 +109,7 @@ SIGNATURES = {
     "bvhgpu_blas_free": (_I, [_P, _U32]),
     "bvhgpu_blas_info": (_I, [_P, _U32, _P, _P, _P]),
     "bvhgpu_blas_hidden": (_I, [_P, _U32, _P, _P, _P]),
+    "bvhgpu_blas_hidden_download": (_I, [_P, _U32, _P, _P, _P, _P, _P]),
     "bvhgpu_blas_trace_counts": (_I, [_P, _U32, _P, _U32, _P, _P]),
     "bvhgpu_blas_update_vertices": (_I, [_P, _U32, _P]),
     "bvhgpu_blas_update_vertices_async": (_I, [_P, _U32, _P, _P]),

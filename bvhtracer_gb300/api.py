@@ -398,6 +398,23 @@ class Blas:
                                                        ctypes.byref(d)))
         return {"nodes": n.value, "pairs": p.value, "depth": d.value}
 
+    def hidden_download(self) -> dict:
+        """The hidden trees' device data (bvhgpu_blas_hidden_download): node records (n x 8 float32,
+        `first` / `count` as their bits), cone records (m x 8), pair slots (pairs x 2 uint32) and the
+        per-triangle table ((ntris + 1) & ~1 x 2 uint32)."""
+        h = self.hidden()
+        nc = ctypes.c_uint32()
+        self.ctx.check(self.ctx.lib.bvhgpu_blas_hidden_download(self.ctx.h, self.id, None, None, None, None,
+                                                                 ctypes.byref(nc)))
+        ntris = self.ntris
+        nodes = np.zeros((h["nodes"], 8), np.float32)
+        cones = np.zeros((nc.value, 8), np.float32)
+        slots = np.zeros((h["pairs"], 2), np.uint32)
+        table = np.zeros(((ntris + 1) & ~1, 2), np.uint32)
+        self.ctx.check(self.ctx.lib.bvhgpu_blas_hidden_download(self.ctx.h, self.id, ptr(nodes), ptr(cones), ptr(slots),
+                                                                 ptr(table), ctypes.byref(nc)))
+        return {"nodes": nodes, "cones": cones, "slots": slots, "table": table}
+
     TRACE_COUNT_NAMES = ("ref_nodes", "hidden_boxes", "hidden_entries", "hidden_pairs", "lane_tris", "warp_tris",
                          "cone_switches")
 

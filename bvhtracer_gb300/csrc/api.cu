@@ -729,6 +729,27 @@ int bvhgpu_blas_hidden(bvhgpu_ctx* ctx, uint32_t blas_id, uint32_t* nodes, uint3
     return BVHGPU_OK;
 }
 
+int bvhgpu_blas_hidden_download(bvhgpu_ctx* ctx, uint32_t blas_id, float* nodes, float* cones, uint32_t* slots,
+                                uint32_t* table, uint32_t* ncones) {
+    if (!ctx) return BVHGPU_ERR_INVALID_ARG;
+    if (ctx->capturing) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "hidden_download: not allowed during capture");
+    DeviceBlas* b = find_blas(ctx, blas_id);
+    if (!b) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown BLAS %u", blas_id);
+    if (ncones) *ncones = b->ncones;
+    CK(cudaStreamSynchronize(ctx->stream), "stream synchronize");
+    if (nodes && b->nhid)
+        CK(cudaMemcpy(nodes, b->nodes + 2ull * b->nodes_used, 32ull * b->nhid, cudaMemcpyDeviceToHost), "hidden nodes");
+    if (cones && b->ncones) CK(cudaMemcpy(cones, b->cones, 32ull * b->ncones, cudaMemcpyDeviceToHost), "cones");
+    if (b->hx != nullptr) {
+        const size_t t = hidden_table_u2(b->ntris);
+        if (slots && b->nhp) CK(cudaMemcpy(slots, b->hx + t, 8ull * b->nhp, cudaMemcpyDeviceToHost), "pair slots");
+        if (table) CK(cudaMemcpy(table, b->hx, 8ull * t, cudaMemcpyDeviceToHost), "hidden table");
+    } else if (table) {
+        std::memset(table, 0, 8ull * hidden_table_u2(b->ntris));
+    }
+    return BVHGPU_OK;
+}
+
 int bvhgpu_blas_trace_counts(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhgpu_ray* d_rays, uint32_t n,
                              bvhgpu_hit* d_hits, uint64_t counts[7]) {
     if (!ctx || !counts || (n && (!d_rays || !d_hits))) return BVHGPU_ERR_INVALID_ARG;

@@ -222,6 +222,7 @@ extern "C" {
     pub fn bvhgpu_blas_free(ctx: *mut bvhgpu_ctx, blas_id: u32) -> c_int;
     pub fn bvhgpu_blas_info(ctx: *mut bvhgpu_ctx, blas_id: u32, nodes_used: *mut u32, ntris: *mut u32, depth: *mut u32) -> c_int;
     pub fn bvhgpu_blas_hidden(ctx: *mut bvhgpu_ctx, blas_id: u32, nodes: *mut u32, pairs: *mut u32, depth: *mut u32) -> c_int;
+    pub fn bvhgpu_blas_hidden_download(ctx: *mut bvhgpu_ctx, blas_id: u32, nodes: *mut f32, cones: *mut f32, slots: *mut u32, table: *mut u32, ncones: *mut u32) -> c_int;
     pub fn bvhgpu_blas_trace_counts(ctx: *mut bvhgpu_ctx, blas_id: u32, d_rays: *const bvhgpu_ray, n: u32, d_hits: *mut bvhgpu_hit, counts: *mut u64) -> c_int;
     pub fn bvhgpu_blas_update_vertices(ctx: *mut bvhgpu_ctx, blas_id: u32, tris: *const bvhgpu_triangle) -> c_int;
     pub fn bvhgpu_blas_update_vertices_async(ctx: *mut bvhgpu_ctx, blas_id: u32, d_tris: *const bvhgpu_triangle, s: bvhgpu_stream) -> c_int;

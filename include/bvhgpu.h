@@ -234,6 +234,15 @@ int bvhgpu_blas_info(bvhgpu_ctx* ctx, uint32_t blas_id, uint32_t* nodes_used, ui
  * (bvh.rs:250-258).  Hidden interior nodes have 2 to 4 children.  No reference counterpart:
  * exposed for tests and tuning.  Any pointer may be NULL. */
 int bvhgpu_blas_hidden(bvhgpu_ctx* ctx, uint32_t blas_id, uint32_t* nodes, uint32_t* pairs, uint32_t* depth);
+/* The hidden trees' device data, for tests (no reference counterpart): `nodes` gets the hidden node
+ * records (bvhgpu_blas_hidden's node count x 8 floats: lo.xyz, first, hi.xyz, count, the integers
+ * as their bits), `cones` the cone records (*ncones x 8 floats: axis.xyz, cos_phi, sin_phi, nmin,
+ * Q, B), `slots` the two triangle indices of each hidden pair (pairs x 2, 0xFFFFFFFF for a padding
+ * slot) and `table` the per-triangle entries ((ntris + 1) & ~1 entries x 2: {first, count} of the
+ * hidden root at a large leaf's first triangle, else {0, 0}).  Any array may be NULL; *ncones
+ * (if not NULL) gets the number of cone records.  Synchronous. */
+int bvhgpu_blas_hidden_download(bvhgpu_ctx* ctx, uint32_t blas_id, float* nodes, float* cones, uint32_t* slots,
+                                uint32_t* table, uint32_t* ncones);
 /* bvhgpu_blas_intersect_async's traversal with work counters (device buffers; synchronous): the
  * hits (identical to the plain call's) and, summed over the rays, counts[0..6] = reference
  * interior nodes visited, hidden child boxes tested, hidden trees entered, hidden triangle

@@ -257,3 +257,105 @@ def test_trace_counts_measure_the_culled_work(ctx):
     assert c["ref_nodes"] == int(cnt["interior"].sum())  # the reference's own node visits
     tested = 2 * c["hidden_pairs"] + c["lane_tris"] + c["warp_tris"]
     assert c["hidden_entries"] > 0 and tested < 0.05 * int(cnt["tris"].sum())
+
+
+F32 = np.float32
+U0 = F32(5.9604645e-8)
+HUGE = F32(1e15)
+HIDDEN_LEAF, HIDDEN_INTERIOR, CONE_MASK = 0x80000000, 0x40000000, 0x0FFFFFFF
+
+
+def group_seal(lo, hi, e1m, e2m, finite):
+    """The leaf seal of cull.cuh (group_seal) in float32: the raw bounds of v0, v0 + e1, v0 + e2
+    rounded outward by 4 u0, Q = (max |e1_i| + max |e2_i|) (1 + 4 u0), B = the largest |bound|."""
+    one_up, one_dn = F32(1) + F32(4) * U0, F32(1) - F32(4) * U0
+    ok = finite and e1m < HUGE and e2m < HUGE and np.all(np.abs(lo) < HUGE) and np.all(np.abs(hi) < HUGE)
+    clo = np.where(lo < 0, lo * one_up, lo * one_dn).astype(F32)
+    chi = np.where(hi < 0, hi * one_dn, hi * one_up).astype(F32)
+    b = F32(max(0.0, float(np.abs(clo).max()), float(np.abs(chi).max())))
+    if not ok:
+        return np.zeros(3, F32), np.zeros(3, F32), F32(np.inf), F32(0)
+    return clo, chi, F32((F32(e1m) + F32(e2m)) * one_up), b
+
+
+def check_hidden_records(blas, tris, min_valid_share=0.0):
+    """Every hidden node's box and every cone record's Q, B against group_seal over the node's own
+    triangles (restated here in float32: exact, since they are minima and maxima), and every cone
+    (axis, cos_phi, nmin) against the triangles it covers in float64."""
+    hd = blas.hidden_download()
+    nodes, cones, slots, table = hd["nodes"], hd["cones"], hd["slots"], hd["table"]
+    ui = nodes.view(np.uint32)
+    nused = blas.nodes_used
+    p0 = (len(tris) + 1) // 2
+    v = tris.reshape(-1, 3, 3).astype(F32)
+    v0, e1, e2 = v[:, 0], (v[:, 1] - v[:, 0]).astype(F32), (v[:, 2] - v[:, 0]).astype(F32)
+    p1, p2 = (v0 + e1).astype(F32), (v0 + e2).astype(F32)
+    memo = {}
+
+    def tri_set(first, count):
+        """Triangles under a hidden entry (first, count)."""
+        key = (first, count)
+        if key in memo:
+            return memo[key]
+        if count & HIDDEN_LEAF:
+            ids = slots[first - p0: first - p0 + (count & ~HIDDEN_LEAF)].ravel()
+            out = ids[ids != 0xFFFFFFFF]
+        else:
+            k = ((count >> 28) & 3) + 1
+            out = np.concatenate([tri_set(int(ui[first - nused + c, 3]), int(ui[first - nused + c, 7]))
+                                  for c in range(k)])
+        memo[key] = out
+        return out
+
+    def seal_of(ids):
+        lo = np.minimum(np.minimum(v0[ids], p1[ids]), p2[ids]).min(0)
+        hi = np.maximum(np.maximum(v0[ids], p1[ids]), p2[ids]).max(0)
+        finite = bool(np.isfinite(v0[ids]).all() and np.isfinite(e1[ids]).all() and np.isfinite(e2[ids]).all()
+                      and np.isfinite(p1[ids]).all() and np.isfinite(p2[ids]).all())
+        return group_seal(lo, hi, np.abs(e1[ids]).max(), np.abs(e2[ids]).max(), finite)
+
+    checked_nodes = checked_cones = 0
+    for i in range(len(nodes)):
+        first, count = int(ui[i, 3]), int(ui[i, 7])
+        lo, hi, _, _ = seal_of(tri_set(first, count))
+        assert nodes[i, :3].tobytes() == lo.tobytes() and nodes[i, 4:7].tobytes() == hi.tobytes(), f"node {i}"
+        checked_nodes += 1
+    # cone records: at each hidden root (from the table) and at interior nodes; the count field of
+    # an interior entry names the cone governing its subtree
+    entries = [(int(f), int(c)) for f, c in table if c != 0]
+    entries += [(int(ui[i, 3]), int(ui[i, 7])) for i in range(len(nodes)) if ui[i, 7] & HIDDEN_INTERIOR]
+    valid = 0
+    for first, count in entries:  # each interior entry names its own cone (the root's: the tree's)
+        c = count & CONE_MASK
+        ids = tri_set(first, count)
+        _, _, q, b = seal_of(ids)
+        assert cones[c, 6].tobytes() == q.tobytes() and cones[c, 7].tobytes() == b.tobytes(), f"cone {c} Q, B"
+        n = np.cross(e1[ids].astype(np.float64), e2[ids].astype(np.float64))
+        nl = np.linalg.norm(n, axis=1)
+        a = cones[c, :3].astype(np.float64)
+        if cones[c, 3] > 0:  # a valid cone: every normal line within the cone, no normal shorter than nmin
+            cos = np.abs(n @ a) / (nl * np.linalg.norm(a))
+            assert (cos >= cones[c, 3] * (1 - 1e-9)).all(), f"cone {c}"
+            assert (nl >= cones[c, 5] * (1 - 1e-9)).all(), f"cone {c} nmin"
+            valid += 1
+        checked_cones += 1
+    assert checked_nodes == len(nodes) and checked_cones == len(cones) and valid >= min_valid_share * len(cones)
+    return checked_nodes, checked_cones
+
+
+def test_hidden_records_equal_the_restated_seal_after_upload_and_updates(ctx):
+    """The refresh (chunks of pairs per warp, combined in order) writes the boxes and Q, B that the
+    seal gives over each node's triangles, bit for bit, and cones that hold every covered normal:
+    after the upload and after two vertex updates (radial wobble, then a larger move)."""
+    mesh = scenes.displaced_icosphere(6, 4)
+    tris = mesh.triangles().copy()
+    bvh = bt.BvhBuilder().build_for(tris)
+    blas = ctx.upload_blas(bvh, tris)
+    check_hidden_records(blas, tris, min_valid_share=0.5)
+    rng = np.random.default_rng(9)
+    for amp in (0.002, 0.01):  # 4 % and 20 % of an edge, per corner
+        moved = (tris.reshape(-1, 3, 3) * (1 + amp * rng.standard_normal((len(tris), 3, 1)))).astype(F32)
+        moved = np.ascontiguousarray(moved.reshape(-1, 9))
+        blas.update_vertices(moved)
+        tris = moved
+        check_hidden_records(blas, tris)
