@@ -9,7 +9,7 @@ from .api import (BATCH_ITEM, FLT_MAX, HIT, MISS, NODE, RAY, TLAS_NODE, Blas, Bv
                   DeviceBuffer, DiffMesh, Event, PinnedArray, Scene, World, decode_mesh, load_descent_state,
                   load_mesh, mse_loss, save_descent_state)
 from ._lib import (ACC_DEPTH, ACC_INTERSECTION, ACC_NORMAL, ACC_TEXTURE, ACC_UV, BIG_LEAF_NEVER, LIST_CLOSEST, LIST_MUT,
-                   LOOKUP_HIT_OBJECT, LOOKUP_REFERENCE, MESH_OBJ, MESH_TRI, MODE_PERSISTENT, MODE_PLAIN, RIGID_BODY, FORCE_GENERATOR, FORCE_GRAVITY,
+                   LOOKUP_HIT_OBJECT, LOOKUP_REFERENCE, ERR_DEADLINE, MESH_OBJ, MESH_TRI, MODE_PERSISTENT, MODE_PLAIN, RIGID_BODY, FORCE_GENERATOR, FORCE_GRAVITY,
                    FORCE_SPRING, rigid_body_default,
                    SHADER_DEPTH, SHADER_INTERSECTION, SHADER_RADIANCE, BvhGpuError)
 from ._lib import KERNELS as _KERNELS
@@ -25,6 +25,6 @@ __all__ = ["Context", "DeviceBuffer", "PinnedArray", "Event", "Bvh", "BvhBuilder
            "DiffMesh", "mse_loss", "save_descent_state", "load_descent_state",
            "RAY", "HIT", "NODE", "TLAS_NODE", "BATCH_ITEM", "MISS", "FLT_MAX", "BvhGpuError",
            "ACC_INTERSECTION", "ACC_DEPTH", "ACC_UV", "ACC_NORMAL", "ACC_TEXTURE", "SHADER_RADIANCE", "SHADER_INTERSECTION",
-           "SHADER_DEPTH", "MODE_PLAIN", "MODE_PERSISTENT", "LOOKUP_REFERENCE", "LOOKUP_HIT_OBJECT", "BIG_LEAF_NEVER", "LIST_CLOSEST", "LIST_MUT", "MESH_TRI", "MESH_OBJ", "decode_mesh", "load_mesh", "World", "RIGID_BODY", "FORCE_GENERATOR", "FORCE_GRAVITY", "FORCE_SPRING",
+           "SHADER_DEPTH", "MODE_PLAIN", "MODE_PERSISTENT", "LOOKUP_REFERENCE", "LOOKUP_HIT_OBJECT", "ERR_DEADLINE", "BIG_LEAF_NEVER", "LIST_CLOSEST", "LIST_MUT", "MESH_TRI", "MESH_OBJ", "decode_mesh", "load_mesh", "World", "RIGID_BODY", "FORCE_GENERATOR", "FORCE_GRAVITY", "FORCE_SPRING",
            "rigid_body_default", "K_TRACE_BLAS", "K_TRACE_SCENE",
            "K_PERSISTENT_BOUNCE", "K_TRACE_BATCH", "K_SCENE_BOUNCE"]

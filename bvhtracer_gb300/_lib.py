@@ -65,7 +65,8 @@ FLT_MAX = np.float32(np.finfo(np.float32).max)
 OK = 0
 ERRORS = {1: "invalid argument", 2: "out of memory", 3: "CUDA error", 4: "stack depth exceeded",
           5: "step cap exceeded", 6: "build would panic", 7: "no CUDA device",
-          8: "input larger than the entry point's fixed maximum"}
+          8: "input larger than the entry point's fixed maximum", 9: "launch stopped at the deadline"}
+ERR_DEADLINE = 9
 
 ACC_INTERSECTION, ACC_DEPTH, ACC_UV, ACC_NORMAL, ACC_TEXTURE = 0, 1, 2, 3, 4
 SHADER_RADIANCE, SHADER_INTERSECTION, SHADER_DEPTH = 0, 1, 2
@@ -110,6 +111,7 @@ SIGNATURES = {
     "bvhgpu_blas_info": (_I, [_P, _U32, _P, _P, _P]),
     "bvhgpu_blas_hidden": (_I, [_P, _U32, _P, _P, _P]),
     "bvhgpu_blas_hidden_download": (_I, [_P, _U32, _P, _P, _P, _P, _P]),
+    "bvhgpu_set_deadline": (_I, [_P, ctypes.c_uint64]),
     "bvhgpu_blas_trace_counts": (_I, [_P, _U32, _P, _U32, _P, _P]),
     "bvhgpu_blas_update_vertices": (_I, [_P, _U32, _P]),
     "bvhgpu_blas_update_vertices_async": (_I, [_P, _U32, _P, _P]),

@@ -55,6 +55,11 @@ class Context:
     def sync(self):
         self.check(self.lib.bvhgpu_sync(self.h))
 
+    def set_deadline(self, ns: int):
+        """Time budget of each persistent launch in nanoseconds (0: none); a launch past it stops
+        and the next synchronising call raises BvhGpuError with code ERR_DEADLINE."""
+        self.check(self.lib.bvhgpu_set_deadline(self.h, int(ns)))
+
     @property
     def stream(self):
         return self.lib.bvhgpu_get_stream(self.h)

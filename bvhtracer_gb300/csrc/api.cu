@@ -109,6 +109,8 @@ int read_errors(bvhgpu_ctx* ctx) {
     if (flags) {
         CK(cudaMemset(ctx->d_err, 0, sizeof(uint32_t)), "reset error flags");
         if (flags & kErrStack) return fail(ctx, BVHGPU_ERR_STACK_DEPTH, "traversal stack overflow (tree too deep)");
+        if (flags & kErrDeadline)
+            return fail(ctx, BVHGPU_ERR_DEADLINE, "a launch stopped at the context's deadline; its outputs are incomplete");
         if (flags & kErrLookup)
             return fail(ctx, BVHGPU_ERR_INVALID_ARG,
                         "a hit's primitive index lies outside the looked-up model's shading data (the reference "
@@ -438,13 +440,13 @@ int bvhgpu_create(bvhgpu_ctx** out, int device) {
     ctx->device = device;
     cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaMalloc(&ctx->d_err, sizeof(uint32_t)) != cudaSuccess ||
+        cudaMalloc(&ctx->d_err, 4 * sizeof(uint32_t)) != cudaSuccess ||  // flags, pad, deadline (u64 ns)
         cudaMalloc(&ctx->d_scratch, 64 * sizeof(uint32_t)) != cudaSuccess ||
         cudaMallocHost(&ctx->host_word, 64) != cudaSuccess) {
         delete ctx;
         return BVHGPU_ERR_CUDA;
     }
-    cudaMemset(ctx->d_err, 0, sizeof(uint32_t));
+    cudaMemset(ctx->d_err, 0, 4 * sizeof(uint32_t));
     cudaMemset(ctx->d_scratch, 0, 64 * sizeof(uint32_t));
     cudaDeviceSynchronize();
     *out = ctx;
@@ -726,6 +728,14 @@ int bvhgpu_blas_hidden(bvhgpu_ctx* ctx, uint32_t blas_id, uint32_t* nodes, uint3
     if (nodes) *nodes = b->nhid;
     if (pairs) *pairs = b->nhp;
     if (depth) *depth = (b->depth - b->ref_depth) / 3;
+    return BVHGPU_OK;
+}
+
+int bvhgpu_set_deadline(bvhgpu_ctx* ctx, uint64_t ns) {
+    if (!ctx) return BVHGPU_ERR_INVALID_ARG;
+    if (ctx->capturing) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "set_deadline: not allowed during capture");
+    CK(cudaMemcpyAsync(ctx->d_err + 2, &ns, sizeof(ns), cudaMemcpyHostToDevice, ctx->stream), "deadline");
+    CK(cudaStreamSynchronize(ctx->stream), "stream synchronize");
     return BVHGPU_OK;
 }
 

@@ -20,6 +20,32 @@ namespace bvhgpu {
 constexpr uint32_t kErrStack = 1u;
 constexpr uint32_t kErrSteps = 2u;
 constexpr uint32_t kErrLookup = 4u;  // a render's shading lookup fell outside the model's data
+constexpr uint32_t kErrDeadline = 8u;  // a persistent launch stopped at the context's deadline
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// A persistent launch's time budget (bvhgpu_set_deadline), kept in the two words after the
+// context's error word (0: none).  A warp stops taking and tracing rays once its launch has run
+// longer, raises kErrDeadline and leaves: no wait, so an expired launch ends promptly, and the host
+// reports the launch's outputs as incomplete.
+struct Deadline {
+    unsigned long long end;  // globaltimer value at which the warp stops; 0: no deadline
+    __device__ __forceinline__ void start(const uint32_t* err) {
+        const unsigned long long budget = *reinterpret_cast<const volatile unsigned long long*>(err + 2);
+        end = budget != 0ull ? global_ns() + budget : 0ull;
+    }
+    // Warp-uniform: lane 0's clock decides.
+    __device__ __forceinline__ bool expired(uint32_t* err) const {
+        if (end == 0ull) return false;
+        const bool late = __shfl_sync(0xFFFFFFFFu, global_ns() > end ? 1 : 0, 0) != 0;
+        if (late && (threadIdx.x & 31u) == 0u) atomicOr(err, kErrDeadline);
+        return late;
+    }
+};
 
 constexpr uint32_t kMiss = 0xFFFFFFFFu;
 constexpr float kThreshold = 0.0001f;  // num_traits::cast(0.0001_f64) (triangle.rs:47)

@@ -98,10 +98,11 @@ struct DeviceWorld {
 // Layout of a mesh's forward-pass schedule (u32 words, for up to `cap` rays): per parity p (the
 // pass number's low bit) a flag per ray (1: the next pass serves the ray from its long list) and a
 // long list of ray ids; then the counters: the pixel queue, the long list's head, the list sizes
-// per parity, the pass number, and the ray counts of the last two passes.
+// per parity, the pass number, the ray counts of the last two passes, and whether the last pass
+// stopped at a deadline (its flags and list are then incomplete and the next pass ignores them).
 struct ForwardSchedule {
     static constexpr uint32_t kQueue = 0, kHead = 1, kCount = 2 /* + parity */, kPass = 4, kRays = 5, kPrevRays = 6,
-                              kCounters = 8;
+                              kStopped = 7, kCounters = 8;
     static __host__ __device__ size_t flags(uint32_t cap, uint32_t p) { return (size_t)p * cap; }
     static __host__ __device__ size_t list(uint32_t cap, uint32_t p) { return (size_t)(2u + p) * cap; }
     static __host__ __device__ size_t counters(uint32_t cap) { return 4ull * cap; }

@@ -159,11 +159,17 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_lambert_forward(GBlas b, const 
         list_cur = sched + ForwardSchedule::list(cap, parity);
         flag_nxt = sched + ForwardSchedule::flags(cap, parity ^ 1u);
         list_nxt = sched + ForwardSchedule::list(cap, parity ^ 1u);
-        lcount = *reinterpret_cast<volatile uint32_t*>(ctr + ForwardSchedule::kCount + parity);
+        lcount = min(*reinterpret_cast<volatile uint32_t*>(ctr + ForwardSchedule::kCount + parity), cap);
     }
     bool long_open = lcount > 0u;
     bool is_long = false;
+    Deadline dl;
+    dl.start(err);
     for (;;) {
+        if (dl.expired(err)) {
+            if (ctr != nullptr && lane == 0u) atomicExch(ctr + ForwardSchedule::kStopped, 1u);
+            return;
+        }
         const unsigned need = __ballot_sync(kFull, phase == 0);
         const unsigned busy = __ballot_sync(kFull, phase == 1);
         const unsigned longs = __ballot_sync(kFull, phase == 1 && is_long);
@@ -231,7 +237,10 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_lambert_forward(GBlas b, const 
                 if (sched != nullptr) {
                     const bool lng = tr.steps > kLongSteps;
                     __stcg(flag_nxt + idx, lng ? 1u : 0u);
-                    if (lng) __stcg(list_nxt + atomicAdd(ctr + ForwardSchedule::kCount + (parity ^ 1u), 1u), idx);
+                    if (lng) {
+                        const uint32_t slot = atomicAdd(ctr + ForwardSchedule::kCount + (parity ^ 1u), 1u);
+                        if (slot < cap) __stcg(list_nxt + slot, idx);  // a ray finishes once a pass: always true
+                    }
                 }
                 phase = 0;
             }
@@ -246,13 +255,16 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_lambert_forward(GBlas b, const 
 }
 
 // Starts a scheduled forward pass over n rays: the next pass number (its parity alternates, also
-// across the counter's wrap), the previous pass's ray count, empty queues, and an empty list for
-// the pass after it.
+// across the counter's wrap), the previous pass's ray count (0, and an empty list, when that pass
+// stopped at a deadline), empty queues, and an empty list for the pass after it.
 __global__ void k_forward_prep(uint32_t* ctr, uint32_t n) {
     const uint32_t k = ctr[ForwardSchedule::kPass] + 1u;
+    const bool stopped = ctr[ForwardSchedule::kStopped] != 0u;
     ctr[ForwardSchedule::kPass] = k;
-    ctr[ForwardSchedule::kPrevRays] = ctr[ForwardSchedule::kRays];
+    ctr[ForwardSchedule::kPrevRays] = stopped ? 0u : ctr[ForwardSchedule::kRays];
     ctr[ForwardSchedule::kRays] = n;
+    ctr[ForwardSchedule::kStopped] = 0u;
+    if (stopped) ctr[ForwardSchedule::kCount + (k & 1u)] = 0u;
     ctr[ForwardSchedule::kQueue] = 0u;
     ctr[ForwardSchedule::kHead] = 0u;
     ctr[ForwardSchedule::kCount + ((k & 1u) ^ 1u)] = 0u;

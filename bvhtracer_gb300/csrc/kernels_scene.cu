@@ -947,7 +947,10 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_scene_persistent_bounce(SceneDa
     tr.bt.stk.bind(stack_smem);
     StepResult st = kStepFinished;
     bool queue_open = true;
+    Deadline dl;
+    dl.start(err);
     for (;;) {
+        if (dl.expired(err)) return;
         const unsigned need = __ballot_sync(kFull, phase == 0);
         const unsigned busy = __ballot_sync(kFull, phase == 1 || phase == 2);
         if (need != 0u && ((uint32_t)__popc(need) >= refill || busy == 0u)) {

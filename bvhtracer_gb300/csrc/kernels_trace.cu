@@ -219,7 +219,10 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_persistent_bounce(GBlas b, cons
     tr.stk.bind(stack_smem);
     StepResult st = kStepFinished;
     bool queue_open = true;
+    Deadline dl;
+    dl.start(err);
     for (;;) {
+        if (dl.expired(err)) return;
         const unsigned need = __ballot_sync(kFull, phase == 0);
         const unsigned busy = __ballot_sync(kFull, phase == 1 || phase == 2);
         // refill once `refill` lanes are idle (or none is busy)
@@ -320,7 +323,10 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_trace_batch_persistent(const Ba
     tr.stk.bind(stack_smem);
     StepResult st = kStepFinished;
     bool queue_open = true;
+    Deadline dl;
+    dl.start(err);
     for (;;) {
+        if (dl.expired(err)) return;
         const unsigned need = __ballot_sync(kFull, phase == 0);
         const unsigned busy = __ballot_sync(kFull, phase == 1);
         if (need != 0u && ((uint32_t)__popc(need) >= refill || busy == 0u)) {

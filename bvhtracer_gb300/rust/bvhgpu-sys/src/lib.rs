@@ -23,6 +23,7 @@ pub const BVHGPU_ERR_STEP_CAP: c_int = 5;
 pub const BVHGPU_ERR_BUILD: c_int = 6;
 pub const BVHGPU_ERR_NO_DEVICE: c_int = 7;
 pub const BVHGPU_ERR_TOO_LARGE: c_int = 8;
+pub const BVHGPU_ERR_DEADLINE: c_int = 9;
 pub const BVHGPU_MISS: u32 = 0xFFFF_FFFF;
 pub const BVHGPU_ACC_INTERSECTION: c_int = 0;
 pub const BVHGPU_ACC_DEPTH: c_int = 1;
@@ -196,6 +197,7 @@ extern "C" {
     pub fn bvhgpu_launch_count() -> u64;
     pub fn bvhgpu_sync(ctx: *mut bvhgpu_ctx) -> c_int;
     pub fn bvhgpu_get_stream(ctx: *mut bvhgpu_ctx) -> bvhgpu_stream;
+    pub fn bvhgpu_set_deadline(ctx: *mut bvhgpu_ctx, ns: u64) -> c_int;
     pub fn bvhgpu_device_alloc(ctx: *mut bvhgpu_ctx, bytes: usize, out: *mut *mut c_void) -> c_int;
     pub fn bvhgpu_device_free(ctx: *mut bvhgpu_ctx, p: *mut c_void) -> c_int;
     pub fn bvhgpu_host_alloc(ctx: *mut bvhgpu_ctx, bytes: usize, out: *mut *mut c_void) -> c_int;

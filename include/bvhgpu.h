@@ -39,6 +39,7 @@ extern "C" {
 #define BVHGPU_ERR_BUILD 6         /* the reference's BvhBuilder would panic on this mesh */
 #define BVHGPU_ERR_NO_DEVICE 7
 #define BVHGPU_ERR_TOO_LARGE 8     /* input larger than a fixed-size entry point accepts */
+#define BVHGPU_ERR_DEADLINE 9      /* a persistent launch ran past bvhgpu_set_deadline's budget */
 
 /* ---- data layouts ------------------------------------------------------------------- */
 
@@ -131,6 +132,14 @@ uint64_t bvhgpu_launch_count(void);
 /* Waits for the context's stream and reports any device-side error flag. */
 int bvhgpu_sync(bvhgpu_ctx* ctx);
 bvhgpu_stream bvhgpu_get_stream(bvhgpu_ctx* ctx);
+/* A time budget for each persistent launch of this context (the single-BLAS bounce, batch, scene
+ * bounce and Lambertian forward launches), in nanoseconds of the device clock from the start of
+ * each of its warps; 0 (the default) means none.  A launch past it stops taking and tracing rays
+ * and the next synchronising call (or bvhgpu_sync) returns BVHGPU_ERR_DEADLINE; that launch's
+ * outputs are then incomplete, and the context stays usable.  For a serving caller that must
+ * bound a frame's time; no reference counterpart (the reference has no time limit).  Applies to
+ * launches issued after the call; not allowed during graph capture. */
+int bvhgpu_set_deadline(bvhgpu_ctx* ctx, uint64_t ns);
 
 /* ---- memory helpers (for callers without their own CUDA allocator) ------------------- */
 int bvhgpu_device_alloc(bvhgpu_ctx* ctx, size_t bytes, void** out);
