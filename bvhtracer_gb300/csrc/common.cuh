@@ -840,6 +840,33 @@ __device__ __forceinline__ void coop_leaf2(const ulonglong2* __restrict__ pairs,
     reduce_and_take(bb, pairs, srcB, r);
 }
 
+// Four rays with the same origin (bit for bit) waiting on the same leaf: each loaded pair's origin
+// terms once, tested against the four directions.
+__device__ __forceinline__ void coop_leaf4(const ulonglong2* __restrict__ pairs, uint32_t first, uint32_t cnt,
+                                           int s0, int s1, int s2, int s3, LaneRay& r) {
+    const unsigned lane = threadIdx.x & 31u;
+    const CoopRay c0 = bcast_ray(r, s0), c1 = bcast_ray(r, s1), c2 = bcast_ray(r, s2), c3 = bcast_ray(r, s3);
+    const f2 OX = f2_pack(c0.ox, c0.ox), OY = f2_pack(c0.oy, c0.oy), OZ = f2_pack(c0.oz, c0.oz);
+    const f2 Z = f2_neg_zero();
+    const uint32_t end = first + cnt;
+    const uint32_t pbeg = first >> 1, pend = (end + 1) >> 1;
+    Best b0{c0.ct, 0xFFFFFFFFu}, b1{c1.ct, 0xFFFFFFFFu}, b2{c2.ct, 0xFFFFFFFFu}, b3{c3.ct, 0xFFFFFFFFu};
+    for (uint32_t p = pbeg + lane; p < pend; p += 32u) {
+        const uint32_t kA = 2u * p;
+        const bool va = kA >= first, vb = kA + 1u < end;
+        PairData pd = load_pair(pairs + 5ull * p);
+        OriginTerms ot = origin_terms(pd, OX, OY, OZ, Z);
+        b0.take(ray_terms(pd, ot, f2_pack(c0.dx, c0.dx), f2_pack(c0.dy, c0.dy), f2_pack(c0.dz, c0.dz), Z, va, vb), kA);
+        b1.take(ray_terms(pd, ot, f2_pack(c1.dx, c1.dx), f2_pack(c1.dy, c1.dy), f2_pack(c1.dz, c1.dz), Z, va, vb), kA);
+        b2.take(ray_terms(pd, ot, f2_pack(c2.dx, c2.dx), f2_pack(c2.dy, c2.dy), f2_pack(c2.dz, c2.dz), Z, va, vb), kA);
+        b3.take(ray_terms(pd, ot, f2_pack(c3.dx, c3.dx), f2_pack(c3.dy, c3.dy), f2_pack(c3.dz, c3.dz), Z, va, vb), kA);
+    }
+    reduce_and_take(b0, pairs, s0, r);
+    reduce_and_take(b1, pairs, s1, r);
+    reduce_and_take(b2, pairs, s2, r);
+    reduce_and_take(b3, pairs, s3, r);
+}
+
 __device__ __forceinline__ void load_ray(const float4* rays, uint32_t i, float3& o, float3& d, float& t) {
     float4 a = __ldg(rays + 2ull * i);
     float4 b = __ldg(rays + 2ull * i + 1);

@@ -69,7 +69,7 @@ __device__ __forceinline__ void warp_trace(const GBlas& b, bool active, LaneRay&
         if (st == kStepContinue) st = tr.template advance<true>(b, r, pol, err);
         unsigned pend = __ballot_sync(kFull, st == kStepBigLeaf);
         if (pend == 0u) break;
-        coop_leaf_phase(pend, b, tr, r, st);
+        coop_leaf_phase<true>(pend, b, tr, r, st);
     }
 }
 
@@ -369,7 +369,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_trace_batch_persistent(const Ba
             if (!queue_open && __ballot_sync(kFull, phase == 0 || phase == 1) == 0u) break;
             continue;
         }
-        coop_leaf_phase(pend, b, tr, r, st);
+        coop_leaf_phase<true>(pend, b, tr, r, st);
     }
 }
 
