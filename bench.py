@@ -286,10 +286,10 @@ class leaf_policy:
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of each workload's dominant
 # kernel, from the ncu captures summarised under profiles/ (the command is in each summary).
 NCU_TRAFFIC = {
-    "persistent_bounce": (76.082432e6 + 50.145280e6, "ncu capture of the 1080p frame",
+    "persistent_bounce": (76.118528e6 + 49.763328e6, "ncu capture of the 1080p frame",
                           "profiles/k_persistent_bounce_icosphere_1080p_full.md"),
-    # 8-scene capture: 573.0 MB for 10,057,687 rays; scaled to a launch by its ray count
-    "trace_batch": (573.0e6 / 10057687, "8-scene ncu capture, bytes per ray x rays",
+    # 8-scene capture: 584.9 MB for 10,057,687 rays; scaled to a launch by its ray count
+    "trace_batch": (584.920064e6 / 10057687, "8-scene ncu capture, bytes per ray x rays",
                     "profiles/k_trace_batch_persistent_64_scene_batch.md"),
 }
 
