@@ -288,6 +288,8 @@ class leaf_policy:
 NCU_TRAFFIC = {
     "persistent_bounce": (76.118528e6 + 49.763328e6, "ncu capture of the 1080p frame",
                           "profiles/k_persistent_bounce_icosphere_1080p_full.md"),
+    "scene_bounce": (43.6e6 + 15.2e6, "ncu capture of one instanced 720p frame's trace launch",
+                     "profiles/k_scene_persistent_bounce_instanced_720p_full.md"),
     # 8-scene capture: 584.9 MB for 10,057,687 rays; scaled to a launch by its ray count
     "trace_batch": (584.920064e6 / 10057687, "8-scene ncu capture, bytes per ray x rays",
                     "profiles/k_trace_batch_persistent_64_scene_batch.md"),
@@ -944,10 +946,16 @@ def bench_instanced(args, local_rank: int, reps: int):
         result["roofline"] = {
             "bound": "hbm", "kernel": "scene_bounce", "achieved": bytes_frame / per_launch_s / 1e9, "peak": peak,
             "peak_kind": peak_kind, "unit": "GB/s", "frac": bytes_frame / per_launch_s / 1e9 / peak,
-            "traffic": None, "launch_ms": per_launch_s * 1e3, "algorithmic_bytes_per_launch": bytes_frame,
-            "basis": "SURVEY-style reference bytes per ray (oracle counters: 32 B x (1 + 2 x interior nodes) "
+            "traffic": NCU_TRAFFIC["scene_bounce"][0], "traffic_kind": NCU_TRAFFIC["scene_bounce"][1],
+            "traffic_source": NCU_TRAFFIC["scene_bounce"][2],
+            "launch_ms": per_launch_s * 1e3, "algorithmic_bytes_per_launch": bytes_frame,
+            "basis": "the reference algorithm's bytes per ray (oracle counters: 32 B x (1 + 2 x interior nodes) "
                      "+ 36 B x triangles + TLAS nodes + 48 B per BLAS entry + 44 B ray/hit), every 16th ray of "
-                     "the last frame, over the frame kernel's launch time (one profiled frame)"}
+                     "the last frame, over the frame kernel's launch time (one profiled frame)",
+            "dram": {"bytes_per_launch": NCU_TRAFFIC["scene_bounce"][0],
+                     "gbs": NCU_TRAFFIC["scene_bounce"][0] / per_launch_s / 1e9,
+                     "frac": NCU_TRAFFIC["scene_bounce"][0] / per_launch_s / 1e9 / peak,
+                     "note": "DRAM bytes of the ncu capture / this run's launch time: the HBM fraction proper"}}
     else:
         result["roofline"] = None
     return result, ctx
