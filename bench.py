@@ -444,9 +444,11 @@ def bench_icosphere(args, pg=None):
                 "transfer": "page-locked host buffers, read and written in place by the launch (NVLink-C2C); "
                             "wall clock around bvhgpu_blas_trace_bounce"},
         "e2e_pageable": {"value": e2e_pg_value, "unit": "Mrays/s",
-                         "transfer": "ordinary host memory (e.g. a Rust Vec): the library stages the rays and "
-                                     "hits through its own page-locked copies; wall clock around "
-                                     "bvhgpu_blas_trace_bounce"},
+                         "transfer": "ordinary host memory (e.g. a Rust Vec), reused across calls: read and "
+                                     "written in place by the launch on a GPU that accesses pageable memory "
+                                     "coherently (Grace-attached GB300: yes), the hit pages touched by the CPU "
+                                     "first, else staged through the library's page-locked copies; wall clock "
+                                     "around bvhgpu_blas_trace_bounce"},
         "e2e_hits_identical_to_timed": bool(e2e_identical),
         "gpu_launches": kernel_launches,
         "clocks": clk,

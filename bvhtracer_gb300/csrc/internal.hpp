@@ -136,6 +136,7 @@ struct bvhgpu_ctx {
     void* l2_flush = nullptr;
     size_t l2_flush_bytes = 0;
     int num_sms = 0;
+    int pageable_access = 0;  // kernels may read / write ordinary host memory coherently
     std::string last_error;
     std::map<uint32_t, bvhgpu::DeviceBlas> blas;
     std::map<uint32_t, bvhgpu::DeviceScene> scenes;

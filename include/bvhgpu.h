@@ -279,7 +279,10 @@ int bvhgpu_blas_intersect_async(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhgpu_
  * pattern of its demos).  hits0[i] is ray i's closest hit, hits1[i] the hit of its bounce
  * (miss when ray i missed).  mode: BVHGPU_MODE_PLAIN (trace, compact, trace) or
  * BVHGPU_MODE_PERSISTENT (one work-stealing launch).  n_bounce (may be NULL) receives the
- * number of bounce rays traced. */
+ * number of bounce rays traced.  The launch reads the rays and writes the hits in place when the
+ * buffers are page-locked (bvhgpu_host_alloc), or ordinary host memory on a device that accesses
+ * it coherently (Grace-attached GPUs; the hit arrays' pages are written once by the CPU first);
+ * otherwise they are staged through the context's device buffers. */
 int bvhgpu_blas_trace_bounce(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhgpu_ray* rays, uint32_t n,
                              uint32_t seed, int mode, bvhgpu_hit* hits0, bvhgpu_hit* hits1, uint32_t* n_bounce);
 int bvhgpu_blas_trace_bounce_async(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhgpu_ray* d_rays, uint32_t n,
