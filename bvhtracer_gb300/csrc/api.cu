@@ -180,6 +180,7 @@ void free_scene(DeviceScene& s) {
     cudaFree(s.obj_blas);
     cudaFree(s.blas_table);
     cudaFree(s.tlas);
+    cudaFree(s.tlas_work);
     s = DeviceScene();
 }
 
@@ -1115,7 +1116,9 @@ int bvhgpu_trace_batch(bvhgpu_ctx* ctx, const bvhgpu_batch_item* items, uint32_t
 int bvhgpu_scene_create(bvhgpu_ctx* ctx, const uint32_t* blas_ids, uint32_t nobjects, uint32_t* scene_id) {
     if (!ctx || !blas_ids || !scene_id || nobjects == 0)
         return fail(ctx, BVHGPU_ERR_INVALID_ARG, "scene_create: empty scene");
-    if (nobjects > kMaxSceneObjects) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "scene_create: at most 4096 objects");
+    if (nobjects > kMaxSceneObjects)
+        return fail(ctx, BVHGPU_ERR_INVALID_ARG, "scene_create: at most %u objects (16-bit TLAS node indices)",
+                    kMaxSceneObjects);
     DeviceScene sc;
     sc.nobjects = nobjects;
     sc.blas_ids.assign(blas_ids, blas_ids + nobjects);
@@ -1152,7 +1155,8 @@ int bvhgpu_scene_create(bvhgpu_ctx* ctx, const uint32_t* blas_ids, uint32_t nobj
         (e = cudaMalloc(&sc.inv, 64ull * nobjects)) != cudaSuccess ||
         (e = cudaMalloc(&sc.obj_blas, 4ull * nobjects)) != cudaSuccess ||
         (e = cudaMalloc(&sc.blas_table, sizeof(GBlas) * table.size())) != cudaSuccess ||
-        (e = cudaMalloc(&sc.tlas, 64ull * nobjects)) != cudaSuccess) {
+        (e = cudaMalloc(&sc.tlas, 64ull * nobjects)) != cudaSuccess ||
+        (nobjects > kTlasSharedObjects && (e = cudaMalloc(&sc.tlas_work, tlas_smem_bytes(nobjects))) != cudaSuccess)) {
         free_scene(sc);
         return fail(ctx, BVHGPU_ERR_OUT_OF_MEMORY, "scene_create: %s", cudaGetErrorString(e));
     }

@@ -80,6 +80,7 @@ struct DeviceScene {
     uint32_t nblas = 0;
     std::vector<uint32_t> table_blas;   // context BLAS id of each table entry
     float4* tlas = nullptr;    // 2 float4 per TLAS node (2*nobjects nodes)
+    void* tlas_work = nullptr; // TLAS rebuild state (40 B per object) above kTlasSharedObjects objects
     uint32_t tlas_nodes_used = 0;
     uint32_t tlas_depth_cap = 0;
     uint32_t world = 0;              // bound physics world (0: none)
@@ -248,7 +249,12 @@ int build_bvh_device(bvhgpu_ctx* ctx, float* mesh, uint32_t n, bvhgpu_node* node
                      uint32_t* perm_out, const char** what);
 // Sets ctx->last_error to msg and returns code (the ABI's error path).
 int record_error(bvhgpu_ctx* ctx, int code, const char* msg);
-constexpr uint32_t kMaxSceneObjects = 4096;  // TLAS rebuild shared memory: 40 B per object
+// A TLAS of n objects has 2n nodes and LeftRightIndex packs two 16-bit node indices (tlas.rs:18-22),
+// so a scene holds at most 32,768 objects; the rebuild keeps its 40 B per object in shared memory
+// up to kTlasSharedObjects objects and in the scene's global scratch above.
+constexpr uint32_t kMaxSceneObjects = 32768;
+constexpr uint32_t kTlasSharedObjects = 4096;
+size_t tlas_smem_bytes(uint32_t nobj);  // the TLAS rebuild's per-object state
 cudaError_t launch_tlas_rebuild(bvhgpu_ctx* ctx, DeviceScene& sc, cudaStream_t s);
 cudaError_t launch_trace_scene(bvhgpu_ctx* ctx, DeviceScene& sc, const float4* rays, uint32_t n, void* hits,
                                cudaStream_t s);

@@ -449,6 +449,10 @@ __global__ void __launch_bounds__(kBlock) k_refit_leaves(float4* nodes, const fl
 // where position a itself leaves the list (its stale entry is then scanned like a rescan).
 
 constexpr int kTlasThreads = 512;
+// Above this many objects the rebuild scans instead of caching each position's best match: the
+// cache's rescans grow with the clusters (measured: 4,096 objects 2.5 s cached, 10 ms scanning;
+// 256 objects, the instanced frame's, 0.46 ms cached, 0.61 ms scanning).
+constexpr uint32_t kTlasCachedObjects = 256;
 constexpr unsigned long long kNoKey = 0xFFFFFFFFFFFFFFFFull;
 
 struct TlasSmem {  // one entry per list position
@@ -518,21 +522,47 @@ __device__ __forceinline__ void store_tlas_node(float4* out, uint32_t i, const B
     out[2ull * i + 1] = make_float4(b.hx, b.hy, b.hz, __uint_as_float(blas));
 }
 
+// One merge of the walk by warp 0's lanes 0-6 (each touches only its own array): lane c < 6 the
+// c-th coordinate array, lane 6 the node list.  Node `used` gets Aabb::new of positions a and b and
+// LeftRightIndex::new(node a, node b) = a + (b << 16) (tlas.rs:18-22, 234-236); position a then
+// holds it and position b the list's last node (tlas.rs:238-240).
+__device__ __forceinline__ void tlas_merge(const TlasSmem& S, int n, float4* tlas_out, int a, int b, int last, int used,
+                                           int lane) {
+    if (lane >= 7) return;
+    // node `used` as 8 floats: lo.xyz, left_right, hi.xyz, blas (0 for an inner node)
+    float* out = reinterpret_cast<float*>(tlas_out) + 8ull * (uint32_t)used;
+    if (lane < 6) {
+        float* arr = S.lx + lane * n;  // lx, ly, lz, hx, hy, hz are consecutive arrays
+        const float va = arr[a], vb = arr[b];
+        const float m = lane < 3 ? min_ni(va, vb) : max_ni(va, vb);
+        arr[a] = m;
+        arr[b] = arr[last];
+        out[lane < 3 ? lane : lane + 1] = m;
+    } else {
+        out[3] = __uint_as_float((uint32_t)S.node[a] + ((uint32_t)S.node[b] << 16));
+        out[7] = __uint_as_float(0u);
+        S.node[a] = used;
+        S.node[b] = S.node[last];
+    }
+}
+
 // One block.  Object world bounds (SceneObject::set_transform, scene_object.rs:60-75) in
 // parallel, the cache filled one warp per position, then the walk: every thread follows it
 // (it only reads the keys), warp 0 writes the merged nodes, all threads update the cache.
-// status[0] gets nodes_used, status[1] an error (the reference would panic).
+// status[0] gets nodes_used, status[1] an error (the reference would panic).  The per-position
+// state lives in shared memory, or in `gwork` (global, same layout) for scenes too large for it.
 __global__ void __launch_bounds__(kTlasThreads) k_tlas_rebuild(const GBlas* __restrict__ blas_table,
                                                                const uint32_t* __restrict__ obj_blas,
                                                                const float* __restrict__ xf, uint32_t nobj,
-                                                               float4* __restrict__ tlas_out, uint32_t* status) {
+                                                               float4* __restrict__ tlas_out, uint32_t* status,
+                                                               unsigned long long* gwork) {
     extern __shared__ unsigned long long tsm_keys[];
     __shared__ int s_ninval;
     __shared__ unsigned long long s_key_a;
     const int n = (int)nobj;
     TlasSmem S;
-    S.key = tsm_keys;
-    float* f = reinterpret_cast<float*>(tsm_keys + n);
+    S.key = gwork != nullptr ? gwork : tsm_keys;
+    float* f = reinterpret_cast<float*>(S.key + n);
     S.lx = f;
     S.ly = f + n;
     S.lz = f + 2 * n;
@@ -568,17 +598,66 @@ __global__ void __launch_bounds__(kTlasThreads) k_tlas_rebuild(const GBlas* __re
         store_tlas_node(tlas_out, 1u + (uint32_t)i, Box6{lo[0], lo[1], lo[2], hi[0], hi[1], hi[2]}, 0u, (uint32_t)i);
     }
     __syncthreads();
+    int count = n, used = 1 + n, a = 0;
+    uint32_t err = 0;
+    uint64_t steps = 0;
+    const uint64_t max_steps = 4ull * nobj * nobj + 64;
+    if (n > (int)kTlasCachedObjects) {
+        // the reference's walk as written: every find_best_match a full scan by the block (no cache:
+        // with many objects the merged clusters become the cached best of many positions, whose
+        // rescans after each merge grow as n^2 per merge)
+        auto best = [&](int p) {
+            if (tid == 0) s_key_a = kNoKey;
+            __syncthreads();
+            const int chunk = (count + nwarps - 1) / nwarps;
+            const int r0 = warp * chunk, r1 = min(count, r0 + chunk);
+            if (r0 < r1) {
+                const unsigned long long k = warp_best_key(S, p, r0, r1);
+                if (lane == 0 && k != kNoKey) atomicMin(&s_key_a, k);
+            }
+            __syncthreads();
+            const int r = key_pos(s_key_a);
+            __syncthreads();
+            return r;
+        };
+        int b = best(0);
+        while (count > 1) {
+            if (b < 0 || ++steps > max_steps) {
+                err = 1;
+                break;
+            }
+            const int c = best(b);
+            if (a != c) {
+                a = b;
+                b = c;
+                continue;
+            }
+            if (warp == 0) tlas_merge(S, n, tlas_out, a, b, count - 1, used, lane);
+            count -= 1;
+            used += 1;
+            __syncthreads();
+            b = best(a);
+        }
+        __syncthreads();
+        if (tid == 0) {
+            if (err == 0) {
+                const uint32_t r = (uint32_t)S.node[a];
+                const float4 r0 = tlas_out[2ull * r], r1 = tlas_out[2ull * r + 1];
+                tlas_out[0] = r0;
+                tlas_out[1] = r1;
+            }
+            status[0] = (uint32_t)used;
+            status[1] = err;
+        }
+        return;
+    }
     for (int p = warp; p < n; p += nwarps) {
         const unsigned long long k = warp_best_key(S, p, 0, n);
         if (lane == 0) S.key[p] = k;
     }
     __syncthreads();
 
-    int count = n, used = 1 + n, a = 0;
     int b = key_pos(S.key[0]);
-    uint32_t err = 0;
-    uint64_t steps = 0;
-    const uint64_t max_steps = 4ull * nobj * nobj + 64;
     while (count > 1) {
         if (b < 0 || ++steps > max_steps) {
             err = 1;
@@ -592,26 +671,10 @@ __global__ void __launch_bounds__(kTlasThreads) k_tlas_rebuild(const GBlas* __re
         }
         const int last = count - 1;
         // Between the previous merge's last barrier and here the threads only read keys, so
-        // warp 0 may rewrite the boxes and the node list right away: lane c < 6 the c-th
-        // coordinate array, lane 6 the node list (each lane touches only its own array).
-        if (warp == 0 && lane < 7) {
-            // node `used` as 8 floats: lo.xyz, left_right, hi.xyz, blas (0 for an inner node)
-            float* out = reinterpret_cast<float*>(tlas_out) + 8ull * (uint32_t)used;
-            if (lane < 6) {
-                float* arr = S.lx + lane * n;  // lx, ly, lz, hx, hy, hz are consecutive arrays
-                const float va = arr[a], vb = arr[b];
-                const float m = lane < 3 ? min_ni(va, vb) : max_ni(va, vb);  // Aabb::new of a and b
-                arr[a] = m;
-                arr[b] = arr[last];  // list[b] = list[count - 1], after list[a] (tlas.rs:238-240)
-                out[lane < 3 ? lane : lane + 1] = m;
-            } else {
-                // LeftRightIndex::new(a, b) = a + (b << 16) (tlas.rs:18-22)
-                out[3] = __uint_as_float((uint32_t)S.node[a] + ((uint32_t)S.node[b] << 16));
-                out[7] = __uint_as_float(0u);
-                S.node[a] = used;
-                S.node[b] = S.node[last];
-                s_ninval = 0;  // last read before the previous merge's final barrier
-            }
+        // warp 0 may rewrite the boxes and the node list right away.
+        if (warp == 0) {
+            tlas_merge(S, n, tlas_out, a, b, last, used, lane);
+            if (lane == 6) s_ninval = 0;  // last read before the previous merge's final barrier
         }
         count = last;
         used += 1;
@@ -1150,16 +1213,17 @@ cudaError_t launch_refit(bvhgpu_ctx* ctx, DeviceBlas& b, cudaStream_t s) {
 size_t tlas_smem_bytes(uint32_t nobj) { return (8ull + 8ull * sizeof(float)) * nobj; }
 
 cudaError_t launch_tlas_rebuild(bvhgpu_ctx* ctx, DeviceScene& sc, cudaStream_t s) {
-    size_t smem = tlas_smem_bytes(sc.nobjects);
+    auto* gwork = static_cast<unsigned long long*>(sc.tlas_work);
+    const size_t smem = gwork != nullptr ? 0 : tlas_smem_bytes(sc.nobjects);
     static bool attr_set = false;  // set outside graph capture: the first rebuild is scene_create's
     if (!attr_set) {
         cudaFuncSetAttribute(k_tlas_rebuild, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)tlas_smem_bytes(kMaxSceneObjects));
+                             (int)tlas_smem_bytes(kTlasSharedObjects));
         attr_set = true;
     }
     LaunchScope scope(ctx, BVHGPU_K_TLAS_BUILD, s);
     k_tlas_rebuild<<<1, kTlasThreads, smem, s>>>(static_cast<const GBlas*>(sc.blas_table), sc.obj_blas, sc.xf,
-                                                  sc.nobjects, sc.tlas, ctx->d_scratch + 8);
+                                                  sc.nobjects, sc.tlas, ctx->d_scratch + 8, gwork);
     g_launches++;
     return cudaGetLastError();
 }

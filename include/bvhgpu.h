@@ -306,7 +306,8 @@ int bvhgpu_trace_batch_async(bvhgpu_ctx* ctx, const bvhgpu_batch_item* items, ui
 
 /* ---- scene / TLAS ----------------------------------------------------------------------- */
 /* SceneBuilder::build (BT/src/scene/scene.rs:224-234): objects i = 0..n-1 instance BLAS
- * blas_ids[i].  Transforms start as identity. */
+ * blas_ids[i].  Transforms start as identity.  At most 32,768 objects: the TLAS's 2n nodes are
+ * addressed by LeftRightIndex's 16-bit halves (tlas.rs:18-22). */
 int bvhgpu_scene_create(bvhgpu_ctx* ctx, const uint32_t* blas_ids, uint32_t nobjects, uint32_t* scene_id);
 int bvhgpu_scene_free(bvhgpu_ctx* ctx, uint32_t scene_id);
 /* SceneObject::set_transform (BT/src/scene/scene_object.rs:60-75) for all objects: the

@@ -313,11 +313,13 @@ def test_tlas_rebuild_and_scene_trace(ctx):
     assert (ref["prim"] != bt.MISS).sum() > 1000
 
 
-@pytest.mark.parametrize("n,dup", [(1, 0), (2, 0), (3, 0), (37, 0), (300, 3), (1000, 0), (1000, 2), (4096, 0)])
+@pytest.mark.parametrize("n,dup", [(1, 0), (2, 0), (3, 0), (37, 0), (300, 3), (1000, 0), (1000, 2), (4096, 0),
+                                   (4097, 0), (12000, 5)])
 def test_tlas_rebuild_sizes_and_ties(ctx, n, dup):
-    """TLAS nodes bit-identical to Tlas::rebuild from 1 to the 4,096-object maximum; with dup > 0
-    every dup-th object copies object 0's transform, so find_best_match meets exact area ties
-    (decided by list position) and zero-area merges."""
+    """TLAS nodes bit-identical to Tlas::rebuild from 1 object to 12,000 (above 4,096 the rebuild
+    keeps its state in global instead of shared memory); with dup > 0 every dup-th object copies
+    object 0's transform, so find_best_match meets exact area ties (decided by list position) and
+    zero-area merges."""
     tris, bvh = build(scenes.displaced_icosphere(2, 5).triangles())
     blas = ctx.upload_blas(bvh, tris)
     xf, inv = random_instances(n, 100 + n)
@@ -335,6 +337,15 @@ def test_tlas_rebuild_sizes_and_ties(ctx, n, dup):
     assert gpu_used == ref_used
     assert gpu_nodes.tobytes() == ref_nodes.tobytes(), "TLAS not bit-identical to Tlas::rebuild"
     sc.free()
+
+
+def test_scene_above_the_object_limit_is_rejected(ctx):
+    """A TLAS of n objects has 2n nodes in 16-bit indices (LeftRightIndex): 32,768 objects at most."""
+    tris, bvh = build(scenes.displaced_icosphere(1, 5).triangles())
+    blas = ctx.upload_blas(bvh, tris)
+    xf, inv = random_instances(32769, 7)
+    with pytest.raises(bt.BvhGpuError):
+        ctx.scene([blas] * 32769, xf, inv)
 
 
 # ---- render ----------------------------------------------------------------------------------------
