@@ -16,7 +16,10 @@
  *    stream) and return before the work finishes; the others take HOST pointers and
  *    return after the results are in host memory.
  *  - A context is not thread-safe (one per host thread), like the reference's
- *    single-threaded Rc<RefCell<Model>> ownership (BT/src/model/model.rs:16-24).
+ *    single-threaded Rc<RefCell<Model>> ownership (BT/src/model/model.rs:16-24).  Its
+ *    launches share the context's work-queue counters and scratch, so work issued on
+ *    different streams must not overlap on the GPU: use one stream per context (or order
+ *    the streams with events); separate contexts run concurrently.
  *  - There is no CPU fallback: without a usable CUDA device bvhgpu_create fails.
  */
 #ifndef BVHGPU_H
