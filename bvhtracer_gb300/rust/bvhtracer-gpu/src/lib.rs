@@ -130,6 +130,28 @@ impl Context {
         self.check(rc)
     }
 
+    /// Primaries + one diffuse bounce per hit in one persistent launch (`bvhgpu_blas_trace_bounce`).
+    /// `rays` and the hit slices are read and written in place when the GPU can (page-locked memory,
+    /// or ordinary memory on a Grace-attached GPU); returns the number of bounce rays traced.
+    pub fn trace_bounce(&mut self, blas: u32, rays: &[sys::bvhgpu_ray], seed: u32, hits0: &mut [sys::bvhgpu_hit],
+                        hits1: &mut [sys::bvhgpu_hit]) -> Result<u32, GpuError> {
+        assert!(hits0.len() == rays.len() && hits1.len() == rays.len());
+        let mut n_bounce = 0u32;
+        let rc = unsafe {
+            sys::bvhgpu_blas_trace_bounce(self.raw, blas, rays.as_ptr(), rays.len() as u32, seed,
+                                          sys::BVHGPU_MODE_PERSISTENT, hits0.as_mut_ptr(), hits1.as_mut_ptr(),
+                                          &mut n_bounce)
+        };
+        self.check(rc).map(|_| n_bounce)
+    }
+
+    /// A time budget for each persistent launch of this context (0: none).  A launch past it returns
+    /// `GpuError { code: BVHGPU_ERR_DEADLINE, .. }` with its outputs incomplete; the context stays usable.
+    pub fn set_deadline(&mut self, budget: std::time::Duration) -> Result<(), GpuError> {
+        let ns = u64::try_from(budget.as_nanos()).unwrap_or(u64::MAX);
+        self.check(unsafe { sys::bvhgpu_set_deadline(self.raw, ns) })
+    }
+
     /// `PathTracer::evaluate` over a scene into `rgba` (width * height * 4 bytes); returns the rays traced.
     #[allow(clippy::too_many_arguments)]
     pub fn render_scene(&mut self, scene: u32, camera: &sys::bvhgpu_camera, width: usize, height: usize,
