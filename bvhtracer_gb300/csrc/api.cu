@@ -764,9 +764,19 @@ int bvhgpu_blas_hidden_download(bvhgpu_ctx* ctx, uint32_t blas_id, float* nodes,
     return BVHGPU_OK;
 }
 
+// The kernels read a ray as two float4 and write a hit record field by field, so a ray array the
+// GPU reads in place must be 16-byte aligned and a hit array 4-byte aligned (cudaMalloc,
+// bvhgpu_device_alloc and bvhgpu_host_alloc memory is; a view at an odd offset need not be).
+static bool rays_aligned(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+static bool hits_aligned(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 3u) == 0; }
+static int misaligned(bvhgpu_ctx* ctx, const char* fn) {
+    return fail(ctx, BVHGPU_ERR_INVALID_ARG, "%s: ray arrays must be 16-byte and hit arrays 4-byte aligned", fn);
+}
+
 int bvhgpu_blas_trace_counts(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhgpu_ray* d_rays, uint32_t n,
                              bvhgpu_hit* d_hits, uint64_t counts[7]) {
     if (!ctx || !counts || (n && (!d_rays || !d_hits))) return BVHGPU_ERR_INVALID_ARG;
+    if (n && (!rays_aligned(d_rays) || !hits_aligned(d_hits))) return misaligned(ctx, "trace_counts");
     if (ctx->capturing) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "trace_counts: not allowed during capture");
     DeviceBlas* b = find_blas(ctx, blas_id);
     if (!b) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown BLAS %u", blas_id);
@@ -840,6 +850,7 @@ int bvhgpu_blas_download_nodes(bvhgpu_ctx* ctx, uint32_t blas_id, bvhgpu_node* n
 int bvhgpu_blas_intersect_async(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhgpu_ray* d_rays, uint32_t n,
                                 bvhgpu_hit* d_hits, bvhgpu_stream s) {
     if (!ctx || (n && (!d_rays || !d_hits))) return BVHGPU_ERR_INVALID_ARG;
+    if (n && (!rays_aligned(d_rays) || !hits_aligned(d_hits))) return misaligned(ctx, "blas_intersect_async");
     DeviceBlas* b = find_blas(ctx, blas_id);
     if (!b) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown BLAS %u", blas_id);
     CK(launch_trace_blas(ctx, *b, reinterpret_cast<const float4*>(d_rays), n, d_hits, pick(ctx, s)), "trace");
@@ -883,6 +894,7 @@ int bvhgpu_triangles_intersect_async(bvhgpu_ctx* ctx, const bvhgpu_triangle* d_t
                                      const bvhgpu_ray* d_rays, uint32_t n, int mode, bvhgpu_hit* d_hits,
                                      bvhgpu_stream s) {
     if (!ctx || (n && (!d_rays || !d_hits)) || (ntris && !d_tris)) return BVHGPU_ERR_INVALID_ARG;
+    if (n && (!rays_aligned(d_rays) || !hits_aligned(d_hits))) return misaligned(ctx, "triangles_intersect_async");
     if (mode != BVHGPU_LIST_CLOSEST && mode != BVHGPU_LIST_MUT)
         return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown triangle-list mode %d", mode);
     CK(launch_triangle_list(ctx, reinterpret_cast<const float*>(d_tris), ntris,
@@ -929,6 +941,8 @@ int bvhgpu_blas_trace_bounce_async(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhg
                                    uint32_t seed, int mode, bvhgpu_hit* d_hits0, bvhgpu_hit* d_hits1,
                                    bvhgpu_stream s) {
     if (!ctx || (n && (!d_rays || !d_hits0 || !d_hits1))) return BVHGPU_ERR_INVALID_ARG;
+    if (n && (!rays_aligned(d_rays) || !hits_aligned(d_hits0) || !hits_aligned(d_hits1)))
+        return misaligned(ctx, "blas_trace_bounce_async");
     DeviceBlas* b = find_blas(ctx, blas_id);
     if (!b) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown BLAS %u", blas_id);
     const float4* r = reinterpret_cast<const float4*>(d_rays);
@@ -985,7 +999,9 @@ int bvhgpu_blas_trace_bounce(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhgpu_ray
     void* m_rays = mapped_device_ptr(rays);
     void* m_h0 = m_rays ? mapped_device_ptr(hits0) : nullptr;
     void* m_h1 = m_h0 ? mapped_device_ptr(hits1) : nullptr;
-    if (!(m_rays && m_h0 && m_h1) && ctx->pageable_access) {
+    if (!(rays_aligned(m_rays) && hits_aligned(m_h0) && hits_aligned(m_h1))) m_rays = m_h0 = m_h1 = nullptr;
+    if (!(m_rays && m_h0 && m_h1) && ctx->pageable_access && rays_aligned(rays) && hits_aligned(hits0) &&
+        hits_aligned(hits1)) {
         touch_pages(hits0, 20ull * n);
         touch_pages(hits1, 20ull * n);
         m_rays = const_cast<bvhgpu_ray*>(rays);
@@ -1076,6 +1092,7 @@ int bvhgpu_blas_bounce_rays(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhgpu_ray*
 int bvhgpu_trace_batch_async(bvhgpu_ctx* ctx, const bvhgpu_batch_item* items, uint32_t nitems,
                              const bvhgpu_ray* d_rays, uint32_t nrays, int mode, bvhgpu_hit* d_hits, bvhgpu_stream s) {
     if (!ctx || (nitems && (!items || !d_rays || !d_hits))) return BVHGPU_ERR_INVALID_ARG;
+    if (nitems && (!rays_aligned(d_rays) || !hits_aligned(d_hits))) return misaligned(ctx, "trace_batch_async");
     if (mode != BVHGPU_MODE_PLAIN && mode != BVHGPU_MODE_PERSISTENT)
         return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown mode %d", mode);
     std::vector<const DeviceBlas*> blases(nitems);
@@ -1248,6 +1265,7 @@ int bvhgpu_scene_download_tlas(bvhgpu_ctx* ctx, uint32_t scene_id, bvhgpu_tlas_n
 int bvhgpu_scene_intersect_async(bvhgpu_ctx* ctx, uint32_t scene_id, const bvhgpu_ray* d_rays, uint32_t n,
                                  bvhgpu_hit* d_hits, bvhgpu_stream s) {
     if (!ctx || (n && (!d_rays || !d_hits))) return BVHGPU_ERR_INVALID_ARG;
+    if (n && (!rays_aligned(d_rays) || !hits_aligned(d_hits))) return misaligned(ctx, "scene_intersect_async");
     DeviceScene* sc = find_scene(ctx, scene_id);
     if (!sc) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown scene %u", scene_id);
     CK(launch_trace_scene(ctx, *sc, reinterpret_cast<const float4*>(d_rays), n, d_hits, pick(ctx, s)), "trace scene");
@@ -1342,6 +1360,8 @@ int bvhgpu_mesh_set_vertices(bvhgpu_ctx* ctx, uint32_t mesh_id, const float* ver
 int bvhgpu_lambert_forward_async(bvhgpu_ctx* ctx, uint32_t mesh_id, const bvhgpu_ray* d_rays, uint32_t n,
                                  const float light[3], float* d_image, bvhgpu_hit* d_hits, bvhgpu_stream s) {
     if (!ctx || !light || (n && (!d_rays || !d_image || !d_hits))) return BVHGPU_ERR_INVALID_ARG;
+    if (n && (!rays_aligned(d_rays) || !hits_aligned(d_hits) || !hits_aligned(d_image)))
+        return misaligned(ctx, "lambert_forward_async");
     DeviceMesh* m = find_mesh(ctx, mesh_id);
     if (!m) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown mesh %u", mesh_id);
     DeviceBlas* b = find_blas(ctx, m->blas);
@@ -1381,6 +1401,7 @@ int bvhgpu_lambert_adjoint_async(bvhgpu_ctx* ctx, uint32_t mesh_id, const bvhgpu
                                  const float light[3], const bvhgpu_hit* d_hits, const float* d_image,
                                  const float* d_target, float* d_grad, bvhgpu_stream s) {
     if (!ctx || !light || (n && (!d_rays || !d_hits || !d_image || !d_target || !d_grad))) return BVHGPU_ERR_INVALID_ARG;
+    if (n && (!rays_aligned(d_rays) || !hits_aligned(d_hits))) return misaligned(ctx, "lambert_adjoint_async");
     DeviceMesh* m = find_mesh(ctx, mesh_id);
     if (!m) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown mesh %u", mesh_id);
     CK(launch_lambert_adjoint(ctx, *m, reinterpret_cast<const float4*>(d_rays), n, light, d_hits, d_image, d_target,
@@ -1402,6 +1423,8 @@ int bvhgpu_mesh_sgd_step_async(bvhgpu_ctx* ctx, uint32_t mesh_id, float* d_grad,
 int bvhgpu_scene_trace_bounce_async(bvhgpu_ctx* ctx, uint32_t scene_id, const bvhgpu_ray* d_rays, uint32_t n,
                                     uint32_t seed, bvhgpu_hit* d_hits0, bvhgpu_hit* d_hits1, bvhgpu_stream s) {
     if (!ctx || (n && (!d_rays || !d_hits0 || !d_hits1))) return BVHGPU_ERR_INVALID_ARG;
+    if (n && (!rays_aligned(d_rays) || !hits_aligned(d_hits0) || !hits_aligned(d_hits1)))
+        return misaligned(ctx, "scene_trace_bounce_async");
     DeviceScene* sc = find_scene(ctx, scene_id);
     if (!sc) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown scene %u", scene_id);
     CK(launch_scene_bounce(ctx, *sc, reinterpret_cast<const float4*>(d_rays), n, seed, d_hits0, d_hits1, pick(ctx, s)),

@@ -14,7 +14,9 @@
  *    buffers behind BLAS / scene handles are owned by the context.
  *  - "_async" entry points take DEVICE pointers and a stream (NULL = the context's
  *    stream) and return before the work finishes; the others take HOST pointers and
- *    return after the results are in host memory.
+ *    return after the results are in host memory.  Device ray arrays must be 16-byte
+ *    aligned (a ray is read as two float4) and hit arrays 4-byte aligned, as memory from
+ *    cudaMalloc / bvhgpu_device_alloc is; otherwise the call returns BVHGPU_ERR_INVALID_ARG.
  *  - A context is not thread-safe (one per host thread), like the reference's
  *    single-threaded Rc<RefCell<Model>> ownership (BT/src/model/model.rs:16-24).  Its
  *    launches share the context's work-queue counters and scratch, so work issued on
