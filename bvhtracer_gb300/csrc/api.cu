@@ -996,6 +996,8 @@ int bvhgpu_blas_trace_bounce(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhgpu_ray
     }
     uint32_t* d_count = ctx->d_scratch + 16;
     uint32_t* h_count = static_cast<uint32_t*>(ctx->host_word);
+    DeviceBlas* b = find_blas(ctx, blas_id);
+    if (!b) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown BLAS %u", blas_id);
     void* m_rays = mapped_device_ptr(rays);
     void* m_h0 = m_rays ? mapped_device_ptr(hits0) : nullptr;
     void* m_h1 = m_h0 ? mapped_device_ptr(hits1) : nullptr;
@@ -1008,8 +1010,6 @@ int bvhgpu_blas_trace_bounce(bvhgpu_ctx* ctx, uint32_t blas_id, const bvhgpu_ray
         m_h0 = hits0;
         m_h1 = hits1;
     }
-    DeviceBlas* b = find_blas(ctx, blas_id);
-    if (!b) return fail(ctx, BVHGPU_ERR_INVALID_ARG, "unknown BLAS %u", blas_id);
     if (m_rays && m_h0 && m_h1 && mode == BVHGPU_MODE_PERSISTENT) {
         // the persistent launch counts its primary hits itself
         CK(cudaMemsetAsync(d_count, 0, sizeof(uint32_t), ctx->stream), "count");
