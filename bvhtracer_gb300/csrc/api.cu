@@ -265,7 +265,6 @@ struct HiddenPlan {
     uint32_t nbox_chunks = 0;      // chunks of the node groups (they come first)
     uint32_t nhid = 0, nhp = 0, ncones = 0, depth = 0;
 };
-constexpr uint32_t kNoWork = kNoRefresh;
 
 struct SahTri {
     float c[3], lo[3], hi[3];
@@ -366,8 +365,8 @@ void plan_hidden(const bvhgpu_node* nodes, uint32_t nodes_used, const std::vecto
             return make_uint2(p0, kHiddenLeaf | np);
         }
         const uint32_t pa = P0 + hp.nhp;
-        const uint32_t own = depth >= 1 ? hp.ncones++ : kNoWork;
-        if (own != kNoWork) gov = own;
+        const uint32_t own = depth >= 1 ? hp.ncones++ : kNoRefresh;
+        if (own != kNoRefresh) gov = own;
         // SAH down to 32 binary levels, then halves (a balanced rest keeps the stack need bounded)
         auto split = [&](uint32_t x, uint32_t y) {
             return 2 * depth < 32 ? sah_split(ids, info, x, y) : x + (y - x) / 2;
@@ -391,9 +390,9 @@ void plan_hidden(const bvhgpu_node* nodes, uint32_t nodes_used, const std::vecto
             float* o = &hp.nodes[8ull * (li + c)];
             std::memcpy(&o[3], &meta.x, 4);
             std::memcpy(&o[7], &meta.y, 4);
-            hp.work[li + c] = make_uint4(pc, P0 + hp.nhp, nodes_used + li + c, kNoWork);
+            hp.work[li + c] = make_uint4(pc, P0 + hp.nhp, nodes_used + li + c, kNoRefresh);
         }
-        if (own != kNoWork) cones.push_back(make_uint4(pa, P0 + hp.nhp, kNoWork, own));
+        if (own != kNoRefresh) cones.push_back(make_uint4(pa, P0 + hp.nhp, kNoRefresh, own));
         return make_uint2(nodes_used + li, kHiddenInterior | ((k - 1) << kWideShift) | gov);
     };
     info.resize(ntris);
@@ -417,13 +416,13 @@ void plan_hidden(const bvhgpu_node* nodes, uint32_t nodes_used, const std::vecto
         const uint32_t root_cone = hp.ncones++;
         const uint2 root = make(make, 0, n.primitive_count, 0, root_cone);  // interior: >= 16 triangles
         hp.table[n.left_first] = root;
-        cones.push_back(make_uint4(pa, P0 + hp.nhp, kNoWork, root_cone));
+        cones.push_back(make_uint4(pa, P0 + hp.nhp, kNoRefresh, root_cone));
     }
     hp.work.insert(hp.work.end(), cones.begin(), cones.end());
     for (uint32_t j = 0; j < hp.work.size(); ++j) {
         hp.chunk0.push_back((uint32_t)hp.chunks.size());
         for (uint32_t p = hp.work[j].x; p < hp.work[j].y; p += kRefreshChunk) hp.chunks.push_back(make_uint2(j, p));
-        if (hp.work[j].z != kNoWork) hp.nbox_chunks = (uint32_t)hp.chunks.size();  // node groups come first
+        if (hp.work[j].z != kNoRefresh) hp.nbox_chunks = (uint32_t)hp.chunks.size();  // node groups come first
     }
     hp.chunk0.push_back((uint32_t)hp.chunks.size());
 }
