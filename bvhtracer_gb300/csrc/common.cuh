@@ -36,7 +36,8 @@ struct Deadline {
     unsigned long long end;  // globaltimer value at which the warp stops; 0: no deadline
     __device__ __forceinline__ void start(const uint32_t* err) {
         const unsigned long long budget = *reinterpret_cast<const volatile unsigned long long*>(err + 2);
-        end = budget != 0ull ? global_ns() + budget : 0ull;
+        const unsigned long long now = global_ns();
+        end = budget == 0ull ? 0ull : budget > ~0ull - now ? ~0ull : now + budget;  // saturating
     }
     // Warp-uniform: lane 0's clock decides.
     __device__ __forceinline__ bool expired(uint32_t* err) const {

@@ -37,6 +37,9 @@ def test_persistent_bounce_stops_at_the_deadline_and_recovers():
         ctx.set_deadline(0)
         h0, h1, _ = blas.trace_bounce(rays, SEED, bt.MODE_PERSISTENT)
         assert h0.tobytes() == ref0.tobytes() and h1.tobytes() == ref1.tobytes()
+        ctx.set_deadline(2 ** 64 - 1)  # "no limit" from a caller: the end time saturates, no wrap
+        h0, h1, _ = blas.trace_bounce(rays, SEED, bt.MODE_PERSISTENT)
+        assert h0.tobytes() == ref0.tobytes() and h1.tobytes() == ref1.tobytes()
 
 
 def test_batch_stops_at_the_deadline_and_recovers():
