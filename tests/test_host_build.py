@@ -56,3 +56,47 @@ def test_rejects_bad_mesh():
         bt.BvhBuilder().build_for(np.zeros((4, 9), np.float64))
     with pytest.raises(bt.BvhGpuError):
         bt.BvhBuilder().build_for(np.zeros((0, 9), np.float32))
+
+
+def random_mesh(rng, kind):
+    n = int(rng.integers(1, 400))
+    if kind == 0:    # uniform soup
+        return rng.uniform(-10, 10, (n, 9)).astype(np.float32)
+    if kind == 1:    # tight clusters with shared vertices
+        c = rng.uniform(-5, 5, (int(rng.integers(1, 6)), 3))
+        pts = c[rng.integers(0, len(c), n * 3)] + rng.normal(0, 1e-3, (n * 3, 3))
+        return pts.reshape(n, 9).astype(np.float32)
+    if kind == 2:    # coplanar (z = const) and axis-aligned edges
+        t = rng.integers(-20, 20, (n, 9)).astype(np.float32) * np.float32(0.25)
+        t[:, 2::3] = np.float32(rng.integers(-3, 3))
+        return t
+    if kind == 3:    # duplicates of a few triangles
+        base = rng.uniform(-1, 1, (int(rng.integers(1, 5)), 9)).astype(np.float32)
+        return base[rng.integers(0, len(base), n)]
+    # mixed scales: tiny and huge triangles, negative-only coordinates
+    s = np.float32(10.0) ** rng.integers(-3, 4, (n, 1)).astype(np.float32)
+    return (rng.uniform(-1, 0, (n, 9)).astype(np.float32) * s).astype(np.float32)
+
+
+def test_random_meshes_match_or_both_refuse():
+    """300 random meshes of five kinds (soups, near-coincident clusters, coplanar grids, duplicates,
+    mixed scales): the host build equals the oracle's bit for bit, or both refuse where the
+    reference's build would panic."""
+    rng = np.random.default_rng(2024)
+    refused = 0
+    for case in range(300):
+        tris = random_mesh(rng, case % 5)
+        try:
+            ref_tris, ref_nodes, ref_used = orc.bvh_build(np.ascontiguousarray(tris))
+        except orc.PanicError:
+            with pytest.raises(bt.BvhGpuError) as e:
+                bt.BvhBuilder().build_for(tris.copy())
+            assert e.value.code == 6, f"case {case}"
+            refused += 1
+            continue
+        mine = tris.copy()
+        bvh = bt.BvhBuilder().build_for(mine)
+        assert bvh.nodes_used == ref_used, f"case {case}"
+        assert mine.tobytes() == ref_tris.tobytes(), f"case {case}"
+        assert bvh.nodes.tobytes() == ref_nodes.tobytes(), f"case {case}"
+    assert refused < 300
