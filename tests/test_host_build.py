@@ -100,3 +100,28 @@ def test_random_meshes_match_or_both_refuse():
         assert mine.tobytes() == ref_tris.tobytes(), f"case {case}"
         assert bvh.nodes.tobytes() == ref_nodes.tobytes(), f"case {case}"
     assert refused < 300
+
+
+@pytest.mark.parametrize("kind", range(5))
+def test_indexed_build_permutation(kind):
+    """bvhgpu_build_bvh_host_indexed: the same nodes and order as the plain host build, and
+    perm[i] the input index of the triangle at position i (so an indexed mesh's faces follow)."""
+    import ctypes
+    from bvhtracer_gb300 import _lib
+    from bvhtracer_gb300._lib import ptr
+    rng = np.random.default_rng(70 + kind)
+    tris = np.ascontiguousarray(random_mesh(rng, kind))
+    n = len(tris)
+    try:
+        ref_tris, ref_nodes, ref_used = orc.bvh_build(tris)
+    except orc.PanicError:
+        pytest.skip("the reference's build panics on this mesh")
+    mesh = tris.copy()
+    nodes = np.zeros(2 * n, bt.NODE)
+    used = ctypes.c_uint32()
+    perm = np.zeros(n, np.uint32)
+    rc = _lib.load().bvhgpu_build_bvh_host_indexed(ptr(mesh), n, ptr(nodes), ctypes.byref(used), ptr(perm))
+    assert rc == 0
+    assert used.value == ref_used and nodes.tobytes() == ref_nodes.tobytes() and mesh.tobytes() == ref_tris.tobytes()
+    assert sorted(perm.tolist()) == list(range(n))
+    assert tris[perm].tobytes() == mesh.tobytes()
